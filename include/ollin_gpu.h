@@ -1,0 +1,204 @@
+/*
+ * ollin_gpu.h -- C ABI of the GB300 evolution library for OllinAxis-BiB.
+ *
+ * The reference (malcubi/OllinAxis-BiB, Fortran 90) has no plugin or FFI
+ * layer: the evolution is the argument-less recursive subroutine
+ * ``onestep(level)`` operating on module arrays.  The seam this ABI replaces is
+ * the single call ``call onestep(0)`` in the main loop of
+ * ``src/base/evolve.f90:381`` plus the t=0 preparation of
+ * ``src/base/evolve.f90:128-195`` (symmetries, ``auxiliary`` on every level,
+ * Gamma-driver initialisation).  A Fortran host binds these entry points with
+ * ISO_C_BINDING; all arguments are plain pointers,
+ * integers and doubles.
+ *
+ * Conventions
+ *  - Every entry point returns 0 on success and a non-zero OLLIN_E* code on
+ *    failure; ``ollin_gpu_last_error`` returns a message for the calling
+ *    thread.  The Fortran wrapper maps a non-zero code to ``call die``
+ *    (src/base/die.f90:3-29).
+ *  - Host arrays are the reference's grid functions: ``real(8)`` arrays
+ *    dimensioned ``(1-ghost:Nr, 1-ghost:Nz)``, column-major (r fastest).
+ *    A pointer argument points at element ``(1-ghost, 1-ghost)``; ``ld_r`` is
+ *    the leading dimension in elements (``Nr+ghost`` for an unpadded array).
+ *  - One handle = one evolution = one CUDA stream.  Device memory is owned by
+ *    the handle.  Handles are independent; several may live at once.
+ *  - Only box 0 (Nb = 0, concentric box-in-box levels) is supported.
+ */
+#ifndef OLLIN_GPU_H
+#define OLLIN_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---------------------------------------------------- */
+#define OLLIN_OK            0
+#define OLLIN_EINVAL        1   /* bad argument or unsupported parameter combination */
+#define OLLIN_ECUDA         2   /* a CUDA runtime call failed */
+#define OLLIN_ENAN          3   /* a non-finite value was detected in the state */
+#define OLLIN_ENOMEM        4   /* device allocation failed */
+#define OLLIN_ESTATE        5   /* call out of order (e.g. step before initialize) */
+
+/* ---- enumerated parameter values (param.f90 character parameters) ---- */
+#define OLLIN_INTEGRATOR_RK4    0   /* integrator = "rk4" */
+#define OLLIN_INTEGRATOR_ICN    1   /* integrator = "icn" */
+
+#define OLLIN_SLICING_1PLUSLOG  0   /* slicing = "1+log"      */
+#define OLLIN_SLICING_HARMONIC  1   /* slicing = "harmonic"   */
+#define OLLIN_SLICING_SHOCKAVOID 2  /* slicing = "shockavoid" */
+#define OLLIN_SLICING_STATIC    3   /* slicing = "static"     */
+
+#define OLLIN_SHIFT_NONE        0   /* shift = "none"         */
+#define OLLIN_SHIFT_ZERO        1   /* shift = "zero"         */
+#define OLLIN_SHIFT_STATIC      2   /* shift = "static"       */
+#define OLLIN_SHIFT_GAMMADRIVER2 3  /* shift = "Gammadriver2" */
+
+#define OLLIN_BOUND_RADIATIVE   0   /* boundtype = "radiative" */
+#define OLLIN_BOUND_NONE        1   /* boundtype = "none"      */
+
+#define OLLIN_MATTER_VACUUM     0   /* mattertype = "vacuum" */
+#define OLLIN_MATTER_SCALAR     1   /* mattertype = "scalar" */
+
+#define OLLIN_POTENTIAL_NONE    0   /* scalarpotential = "none" */
+#define OLLIN_POTENTIAL_PHI2    1   /* scalarpotential = "phi2" */
+#define OLLIN_POTENTIAL_PHI4    2   /* scalarpotential = "phi4" */
+
+#define OLLIN_IDATA_MINKOWSKI       0   /* idata = "minkowski"      */
+#define OLLIN_IDATA_SCHWARZSCHILD   1   /* idata = "schwarzschild"  */
+#define OLLIN_IDATA_BRILLLINDQUIST  2   /* idata = "BrillLindquist" (one hole) */
+
+#define OLLIN_ILAPSE_ONE        0   /* ilapse = "one"       */
+#define OLLIN_ILAPSE_ISOTROPIC  1   /* ilapse = "isotropic" */
+#define OLLIN_ILAPSE_PSIMINUS2  2   /* ilapse = "psiminus2" */
+#define OLLIN_ILAPSE_PSIMINUS4  3   /* ilapse = "psiminus4" */
+
+/*
+ * Parsed parameters, field for field the values of the reference's
+ * ``param`` module (src/base/param.f90) that the evolution path reads.
+ * ``ollin_params_default`` fills the reference's defaults.
+ */
+typedef struct ollin_params {
+    /* grid: param.f90:95-141 */
+    int    nrtotal, nztotal;   /* Nrtotal, Nztotal: points per level (without ghosts) */
+    int    nl0;                /* Nl0: refinement levels above the base grid */
+    int    ghost;              /* 0 = from order (3 for order four) */
+    int    eqsym;              /* equatorial symmetry */
+    double dr0, dz0;           /* base-grid spacing */
+    double dtfac;              /* dt0 = dtfac*min(dr0,dz0) (setupboxes.f90:119) */
+    /* time integration: param.f90:410-427 */
+    int    integrator;         /* OLLIN_INTEGRATOR_* */
+    int    icniter;
+    int    order;              /* 4 ("four"); 2 is rejected */
+    /* formulation: param.f90:407-438 */
+    int    slicing;            /* OLLIN_SLICING_* */
+    double gauge_f;
+    int    shift;              /* OLLIN_SHIFT_* */
+    double drivercsi, drivereta;
+    int    driveradv, shiftadvect;
+    int    chimethod, chipower;
+    int    evolveH, evolveKTH, nolambda;
+    int    lagrangian;         /* bssnflavor = "lagrangian" (1) / "eulerian" (0) */
+    int    factorhdet;
+    double eta;                /* BSSN Delta damping multiple of the momentum constraint */
+    double geodiss, scalardiss;
+    double ft[8];              /* ft1..ft8 */
+    int    boundtype;          /* OLLIN_BOUND_* */
+    int    interp_bicubic;     /* interporder = "bicubic" (1) / "bilinear" (0) */
+    /* matter: param.f90:612-643 */
+    int    mattertype;         /* OLLIN_MATTER_* */
+    int    scalarpotential;    /* OLLIN_POTENTIAL_* */
+    double scalar_mass, scalar_lambda;
+    /* initial data (host side, initial.f90) */
+    int    idata;              /* OLLIN_IDATA_* */
+    int    ilapse;             /* OLLIN_ILAPSE_* */
+    double bh1mass;
+} ollin_params;
+
+/* Evolved and auxiliary fields addressable by upload/download.  The names are
+ * the reference's array names (src/base/arrays.config). */
+enum ollin_field {
+    OLLIN_F_ALPHA = 0, OLLIN_F_PHI, OLLIN_F_CHI,
+    OLLIN_F_A, OLLIN_F_B, OLLIN_F_H, OLLIN_F_C,
+    OLLIN_F_TRK, OLLIN_F_KTA, OLLIN_F_KTB, OLLIN_F_KTH, OLLIN_F_KTC,
+    OLLIN_F_DELTA_R, OLLIN_F_DELTA_Z,
+    OLLIN_F_LAMBDA, OLLIN_F_ALAMBDA,
+    OLLIN_F_BETA_R, OLLIN_F_BETA_Z, OLLIN_F_DTBETA_R, OLLIN_F_DTBETA_Z,
+    OLLIN_F_SCALAR_PHI, OLLIN_F_SCALAR_XI_R, OLLIN_F_SCALAR_XI_Z, OLLIN_F_SCALAR_PI,
+    OLLIN_F_NEVOLVED,                     /* number of evolved-field slots */
+    /* derived (read-only) fields, computed on request */
+    OLLIN_F_HAM = 64, OLLIN_F_MOM_R, OLLIN_F_MOM_Z,
+    OLLIN_F_RSCAL, OLLIN_F_KT2, OLLIN_F_LAPLA_ALPHA
+};
+
+/* One level's geometry (box 0): arrays are (1-ghost:nr, 1-ghost:nz). */
+typedef struct ollin_level_desc {
+    int    level;
+    int    nr, nz, ghost;
+    double dr, dz, dt;
+    double rmin, rmax, zmin, zmax;  /* rminl/rmaxl/zminl/zmaxl incl. ghosts (evolve.f90:75-92) */
+    double time;                    /* t(0,level) */
+    int    steps;                   /* s(0,level) */
+} ollin_level_desc;
+
+typedef struct ollin_handle ollin_handle;
+
+/* Fill ``p`` with the reference defaults of param.f90. */
+void ollin_params_default(ollin_params* p);
+
+/* Allocate the level hierarchy on the current CUDA device.
+ * Replaces: allocatearrays('on') + setupboxes (src/base/main.f90:333-365). */
+int ollin_gpu_create(const ollin_params* p, ollin_handle** out);
+void ollin_gpu_destroy(ollin_handle* h);
+
+/* Level geometry and clocks. */
+int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out);
+int ollin_gpu_num_levels(const ollin_handle* h);
+
+/* Host <-> device copies of one grid function of one level.
+ * Replaces direct access to grid(0,level)%<field> (generated mytypes.f90). */
+int ollin_gpu_upload(ollin_handle* h, int level, int field, const double* a, int ld_r);
+int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r);
+
+/* Host-side initial data for the supported ``idata`` values, uploaded to
+ * every level.  Replaces: call initial (src/base/evolve.f90:124,
+ * src/base/initial.f90:59-218, 528-645). */
+int ollin_gpu_initial_data(ollin_handle* h);
+
+/* Symmetries, auxiliary quantities on every level at t=0 and the
+ * Gamma-driver initialisation.  Replaces src/base/evolve.f90:128-195. */
+int ollin_gpu_initialize(ollin_handle* h);
+
+/* Recompute auxiliary quantities of one level after the host changed its
+ * state (e.g. an elliptic lapse).  Replaces: call auxiliary
+ * (src/base/auxiliary.f90:26-56) for the current grid. */
+int ollin_gpu_aux(ollin_handle* h, int level);
+
+/* One coarse time step of every level: the exact equivalent of
+ * ``call onestep(0)`` (src/base/onestep.f90:2-522, called from
+ * src/base/evolve.f90:381).  ``t_out`` (may be NULL) receives t(0,0). */
+int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
+
+/* Constraint norms and 0-D statistics of one field of one level, the five
+ * numbers of save0Dvariable (src/base/save0Ddata.f90:221-288):
+ * out[0]=max, out[1]=min, out[2]=nm1 (max |f|), out[3]=nm2 (RMS), out[4]=origin value.
+ * Derived fields (OLLIN_F_HAM ...) are computed first (constraints.f90:55-149). */
+int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
+
+/* Total point-updates performed by this handle so far (interior points of
+ * each level times the steps taken on it). */
+double ollin_gpu_point_updates(const ollin_handle* h);
+
+/* The CUDA stream (cudaStream_t) all work of this handle is ordered on,
+ * so a caller can record events or synchronise on it. */
+void* ollin_gpu_stream(const ollin_handle* h);
+
+/* Number of kernel launches this handle has issued so far. */
+long long ollin_gpu_launch_count(const ollin_handle* h);
+
+/* Message for the last failure on the calling thread ("" if none). */
+const char* ollin_gpu_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OLLIN_GPU_H */

@@ -1,0 +1,28 @@
+/* ORACLE -- test infrastructure only.  C API of the CPU restatement of the
+ * OllinAxis-BiB evolution path; it takes the same ollin_params as the GPU
+ * library (include/ollin_gpu.h) so that one harness drives both. */
+#ifndef OLLIN_ORACLE_H
+#define OLLIN_ORACLE_H
+#include "../include/ollin_gpu.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+typedef struct ollin_oracle ollin_oracle;
+const char* ollin_oracle_last_error(void);
+int ollin_oracle_create(const ollin_params* p, ollin_oracle** out);
+void ollin_oracle_destroy(ollin_oracle* o);
+int ollin_oracle_initialize(ollin_oracle* o);
+int ollin_oracle_step(ollin_oracle* o, double* t_out);
+int ollin_oracle_num_levels(const ollin_oracle* o);
+int ollin_oracle_dims(const ollin_oracle* o, int level, int* nr, int* nz, int* ghost);
+double ollin_oracle_time(const ollin_oracle* o, int level);
+int ollin_oracle_get(ollin_oracle* o, int level, const char* name, double* a, int ld_r);
+int ollin_oracle_set(ollin_oracle* o, int level, const char* name, const double* a, int ld_r);
+int ollin_oracle_aux(ollin_oracle* o, int level);
+int ollin_oracle_constraints(ollin_oracle* o, int level);
+int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]);
+double ollin_oracle_point_updates(const ollin_oracle* o);
+#ifdef __cplusplus
+}
+#endif
+#endif

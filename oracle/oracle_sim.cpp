@@ -1,0 +1,590 @@
+// ORACLE -- test infrastructure only.  CPU restatement of the OllinAxis-BiB
+// evolution path used to check the GB300 library; never linked into it.
+//
+// This file restates the time stepper and the mesh-refinement transfer:
+//   src/base/onestep.f90 (recursive Berger-Oliger step, RK4/ICN stages),
+//   the Perl-generated saveold/accumulate/update/symmetries_r/symmetries_z
+//   (prl/arrays.pl:134-218), src/base/finebound.f90 with bound_interp.inc,
+//   src/base/restrict.f90 with restrict_interp.inc, src/base/interp.f90,
+//   the box-0 bookkeeping of main.f90/setupboxes.f90/evolve.f90:42-219,
+//   initial data of src/base/initial.f90:59-218,528-645, and the 0-D norms
+//   of src/base/save0Ddata.f90:221-288,370-374.
+// It exposes a C API (ollin_oracle.h) with the same parameter struct as the
+// GPU library so that one harness drives both.
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+
+#include "oracle_sim.h"
+#include "ollin_oracle.h"
+
+namespace oracle {
+
+// ---------------------------------------------------------------------------
+// bookkeeping
+// ---------------------------------------------------------------------------
+static void setup(Sim& S) {
+    const ollin_params& P = S.P;
+    if (P.order != 4) throw std::runtime_error("oracle: only order four is restated");
+    if (P.chipower != 2 || !P.chimethod) throw std::runtime_error("oracle: chimethod with chipower 2 only");
+    if (!P.lagrangian || !P.factorhdet || !P.evolveH) throw std::runtime_error("oracle: lagrangian+factorhdet+evolveH only");
+    if (P.evolveKTH) throw std::runtime_error("oracle: evolveKTH unsupported");
+    S.g = P.ghost ? P.ghost : 3;
+    S.Nlmax = P.nl0;
+    const int L = S.Nlmax;
+    const double dt0 = P.dtfac * std::min(P.dr0, P.dz0);
+    S.dtl.resize(L + 1); S.drl.resize(L + 1); S.dzl.resize(L + 1);
+    for (int l = 0; l <= L; ++l) {  // setupboxes.f90:121-125
+        S.dtl[l] = dt0 / (double)(1 << l);
+        S.drl[l] = P.dr0 / (double)(1 << l);
+        S.dzl[l] = P.dz0 / (double)(1 << l);
+    }
+    int nz = P.nztotal;
+    if (!P.eqsym && (nz + S.g) % 2 == 0) nz += 1;  // setupboxes.f90:131-135
+    S.t.assign(L + 1, 0.0); S.t1.assign(L + 1, 0.0); S.t2.assign(L + 1, 0.0); S.s.assign(L + 1, 0);
+    S.rminl.resize(L + 1); S.rmaxl.resize(L + 1); S.zminl.resize(L + 1); S.zmaxl.resize(L + 1);
+    S.L.resize(L + 1);
+    const int g = S.g;
+    for (int l = 0; l <= L; ++l) {
+        Level& lv = S.L[l];
+        lv.level = l; lv.g = g; lv.Nr = P.nrtotal; lv.Nz = nz;
+        lv.dr = S.drl[l]; lv.dz = S.dzl[l]; lv.dt = S.dtl[l];
+        lv.eqsym = P.eqsym != 0;
+        lv.ownaxis = true;
+        lv.ownequator = P.eqsym != 0;  // main.f90:393-424 (box 0, one process)
+        Arr& r = lv.a("r"); Arr& z = lv.a("z"); Arr& rr = lv.a("rr");
+        for (int j = 1 - g; j <= lv.Nz; ++j)
+            for (int i = 1 - g; i <= lv.Nr; ++i) {  // evolve.f90:42-70
+                r(i, j) = ((double)(0 + i) - 0.5) * lv.dr;
+                if (P.eqsym) z(i, j) = ((double)(0 + j) - 0.5) * lv.dz;
+                else z(i, j) = 0.0 + ((double)(0 + j) - 0.5 * (double)(lv.Nz - g + 1)) * lv.dz;
+            }
+        for (int j = 1 - g; j <= lv.Nz; ++j)
+            for (int i = 1 - g; i <= lv.Nr; ++i) rr(i, j) = std::sqrt(p2(r(i, j)) + p2(z(i, j)));
+        S.rminl[l] = r(1 - g, 0);
+        S.rmaxl[l] = r(lv.Nr, 0);
+        S.zminl[l] = z(0, 1 - g);
+        S.zmaxl[l] = z(0, lv.Nz);
+    }
+    // EVOLVE arrays in generated update.f90 order, with their parity tags
+    // (src/base/arrays.config:154-1045)
+    auto add = [&](const char* n, int sr, int sz) { S.evolved.push_back({n, sr, sz}); };
+    const bool shift = P.shift != OLLIN_SHIFT_NONE;
+    add("alpha", +1, +1); add("dtalpha", +1, +1);
+    if (shift) { add("beta_r", -1, +1); add("beta_z", +1, -1); add("dtbeta_r", -1, +1); add("dtbeta_z", +1, -1); add("fdriver", +1, +1); }
+    add("phi", +1, +1); add("dtphi", +1, +1); add("chi", +1, +1);
+    add("A", +1, +1); add("B", +1, +1); add("H", +1, +1); add("C", +1, -1);
+    add("trK", +1, +1); add("KTA", +1, +1); add("KTB", +1, +1); add("KTH", +1, +1); add("KTC", +1, -1);
+    add("Delta_r", -1, +1); add("Delta_z", +1, -1);
+    add("lambda", +1, +1); add("Alambda", +1, +1);
+    add("V_r", -1, +1); add("V_z", +1, -1); add("z4theta", +1, +1);
+    if (P.mattertype == OLLIN_MATTER_SCALAR) {
+        add("scalar_phi", +1, +1); add("scalar_xi_r", -1, +1); add("scalar_xi_z", +1, -1); add("scalar_pi", +1, +1);
+    }
+    for (Level& lv : S.L)
+        for (const EvolvedVar& e : S.evolved) {
+            lv.a(e.name); lv.a(e.name + "_p"); lv.a(e.name + "_a"); lv.a("s" + e.name);
+            const size_t nr_hist = (size_t)g * (lv.Nz + g) * 3, nz_hist = (size_t)(lv.Nr + g) * g * 3;
+            lv.hist[e.name + "_rL"].assign(nr_hist, 0.0);
+            lv.hist[e.name + "_rR"].assign(nr_hist, 0.0);
+            lv.hist[e.name + "_zL"].assign(nz_hist, 0.0);
+            lv.hist[e.name + "_zR"].assign(nz_hist, 0.0);
+        }
+}
+
+// flat offsets of the history arrays: rX(m, j, k) with m in 0:g-1,
+// j in 1-g:Nz, k in 0:2; zX(i, n, k) with i in 1-g:Nr, n in 0:g-1
+static inline size_t hr(const Level& L, int m, int j, int k) { return (size_t)m + (size_t)L.g * ((size_t)(j - 1 + L.g) + (size_t)(L.Nz + L.g) * k); }
+static inline size_t hz(const Level& L, int i, int n, int k) { return (size_t)(i - 1 + L.g) + (size_t)(L.Nr + L.g) * ((size_t)n + (size_t)L.g * k); }
+
+static void currentgrid(Sim& S, Level& L) { L.time = S.t[L.level]; }
+
+// ---------------------------------------------------------------------------
+// generated per-array routines
+// ---------------------------------------------------------------------------
+static void saveold(Sim& S, Level& L) {
+    const int g = L.g, Nr = L.Nr, Nz = L.Nz;
+    for (const EvolvedVar& e : S.evolved) {
+        Arr& v = L.a(e.name);
+        L.a(e.name + "_p") = v;
+        auto& rL = L.hist[e.name + "_rL"]; auto& rR = L.hist[e.name + "_rR"];
+        auto& zL = L.hist[e.name + "_zL"]; auto& zR = L.hist[e.name + "_zR"];
+        for (int i = 0; i <= g - 1; ++i) {
+            for (int j = 1 - g; j <= Nz; ++j) {
+                rL[hr(L, i, j, 2)] = rL[hr(L, i, j, 1)]; rL[hr(L, i, j, 1)] = rL[hr(L, i, j, 0)]; rL[hr(L, i, j, 0)] = v(1 - g + i, j);
+                rR[hr(L, i, j, 2)] = rR[hr(L, i, j, 1)]; rR[hr(L, i, j, 1)] = rR[hr(L, i, j, 0)]; rR[hr(L, i, j, 0)] = v(Nr - i, j);
+            }
+            for (int ii = 1 - g; ii <= Nr; ++ii) {
+                zL[hz(L, ii, i, 2)] = zL[hz(L, ii, i, 1)]; zL[hz(L, ii, i, 1)] = zL[hz(L, ii, i, 0)]; zL[hz(L, ii, i, 0)] = v(ii, 1 - g + i);
+                zR[hz(L, ii, i, 2)] = zR[hz(L, ii, i, 1)]; zR[hz(L, ii, i, 1)] = zR[hz(L, ii, i, 0)]; zR[hz(L, ii, i, 0)] = v(ii, Nz - i);
+            }
+        }
+    }
+}
+
+static void accumulate(Sim& S, Level& L, int k, int niter, double w) {
+    const bool first = (k == 1), last = (k == niter);
+    for (const EvolvedVar& e : S.evolved) {
+        Arr& a = L.a(e.name + "_a"); Arr& s = L.a("s" + e.name);
+        const size_t n = a.v.size();
+        if (!last) {
+            if (first) for (size_t q = 0; q < n; ++q) a.v[q] = w * s.v[q];
+            else for (size_t q = 0; q < n; ++q) a.v[q] = a.v[q] + w * s.v[q];
+        } else {
+            for (size_t q = 0; q < n; ++q) s.v[q] = a.v[q] + w * s.v[q];
+        }
+    }
+}
+
+static void update(Sim& S, Level& L, double dtw) {
+    for (const EvolvedVar& e : S.evolved) {
+        Arr& v = L.a(e.name); Arr& vp = L.a(e.name + "_p"); Arr& s = L.a("s" + e.name);
+        const size_t n = v.v.size();
+        for (size_t q = 0; q < n; ++q) v.v[q] = vp.v[q] + dtw * s.v[q];
+    }
+}
+
+static void symmetries_r(Sim& S, Level& L) {
+    for (const EvolvedVar& e : S.evolved) {
+        Arr& v = L.a(e.name);
+        for (int i = 1; i <= L.g; ++i)
+            for (int j = 1 - L.g; j <= L.Nz; ++j) v(1 - i, j) = e.symr * v(i, j);
+    }
+}
+
+static void symmetries_z(Sim& S, Level& L) {
+    for (const EvolvedVar& e : S.evolved) {
+        Arr& v = L.a(e.name);
+        for (int j = 1; j <= L.g; ++j)
+            for (int i = 1 - L.g; i <= L.Nr; ++i) v(i, 1 - j) = e.symz * v(i, j);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// interp.f90:2-270 -- value of one grid function of (box 0, level) at (r0,z0)
+// ---------------------------------------------------------------------------
+static double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
+    Level& L = S.L[level];
+    const int g = L.g;
+    const double small = 1.0e-10;
+    const double rmin = S.rminl[level] - small, rmax = S.rmaxl[level];
+    const double zmin = S.zminl[level] - small, zmax = S.zmaxl[level];
+    if (r0 < rmin || r0 > rmax || z0 < zmin || z0 > zmax)
+        throw std::runtime_error("interp: interpolating point is outside the local grid");
+    Arr& r = L.a("r"); Arr& z = L.a("z");
+    const int i0 = (int)((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
+    const double deltar = r0 - r(i0, 0);
+    const int j0 = (int)((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
+    const double deltaz = z0 - z(0, j0);
+    if (deltar == 0.0 && deltaz == 0.0) return var(i0, j0);
+    const bool forcelinear = ((S.rmaxl[level] - r0) < S.drl[level]) || ((S.zmaxl[level] - z0) < S.dzl[level])
+        || ((r0 - S.rminl[level]) < S.drl[level]) || ((z0 - S.zminl[level]) < S.dzl[level]);
+    double fa[4][4];
+    if (forcelinear) {
+        for (int i = 0; i <= 1; ++i)
+            for (int j = 0; j <= 1; ++j) fa[i + 1][j + 1] = var(i0 + i, j0 + j);
+    } else {
+        for (int i = -1; i <= 2; ++i)
+            for (int j = -1; j <= 2; ++j) fa[i + 1][j + 1] = var(i0 + i, j0 + j);
+    }
+    const double auxr = deltar / S.drl[level];
+    const double auxz = deltaz / S.dzl[level];
+    if (!S.P.interp_bicubic || forcelinear) {
+        return fa[1][1] * (1.0 - auxr) * (1.0 - auxz) + fa[2][1] * auxr * (1.0 - auxz)
+            + fa[1][2] * (1.0 - auxr) * auxz + fa[2][2] * auxr * auxz;
+    }
+    double res = 0.0;
+    for (int i = -1; i <= 2; ++i)
+        for (int j = -1; j <= 2; ++j) {
+            double aux = 1.0;
+            for (int m = -1; m <= 2; ++m) {
+                if (m == i) continue;
+                aux = aux * (auxr - (double)m) / (double)(i - m);
+            }
+            for (int n = -1; n <= 2; ++n) {
+                if (n == j) continue;
+                aux = aux * (auxz - (double)n) / (double)(j - n);
+            }
+            res = res + aux * fa[i + 1][j + 1];
+        }
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// finebound.f90:2-407 (all=.true.) with the generated bound_interp.inc
+// ---------------------------------------------------------------------------
+static void finebound(Sim& S, int level, double dtw) {
+    Level& F = S.L[level];
+    const int g = F.g;
+    const int bbox_level = level - 1;
+    const double tp = S.t[level - 1], t0 = S.t[level], tm1 = S.t1[level];
+    const double tl = t0 + dtw;
+    const int imax = (tp == tl) ? g + 2 : g - 1;
+    const int jmax = imax;
+    const int border = (tm1 == 0.0) ? 1 : 2;
+    Arr& r = F.a("r"); Arr& z = F.a("z");
+    Level& Cl = S.L[bbox_level];
+
+    // one strip point: all evolving variables (bound_interp.inc)
+    auto point = [&](double r0, double z0, int m, int n, char bd) {
+        const int ii = (int)nint_((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
+        const int jj = (int)nint_((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
+        const bool flag1 = (ii >= 1 - g) && (ii <= F.Nr) && (jj >= 1 - g) && (jj <= F.Nz);
+        for (const EvolvedVar& e : S.evolved) {
+            const double aux2 = interp(S, bbox_level, Cl.a(e.name), r0, z0);
+            if (!flag1) continue;
+            Arr& v = F.a(e.name);
+            if (border == 1) {
+                v(ii, jj) = (tl - t0) / (tp - t0) * aux2 + (tl - tp) / (t0 - tp) * F.a(e.name + "_p")(ii, jj);
+            } else {
+                // history terms; an index beyond the declared history depth
+                // (m or n > ghost-1, reachable only when tp == tl) carries a
+                // zero weight in the reference and contributes nothing here
+                double h0 = 0.0, h1 = 0.0;
+                if (bd == 'r') {
+                    if (m <= g - 1) {
+                        const auto& H = F.hist[e.name + "_rR"];
+                        h0 = H[hr(F, m, jj, 0)]; h1 = H[hr(F, m, jj, 1)];
+                    }
+                } else {
+                    if (n <= g - 1) {
+                        const auto& H = F.hist[e.name + "_zR"];
+                        h0 = H[hz(F, ii, n, 0)]; h1 = H[hz(F, ii, n, 1)];
+                    }
+                }
+                v(ii, jj) = (tl - t0) * (tl - tm1) / ((tp - t0) * (tp - tm1)) * aux2
+                    + (tl - tp) * (tl - tm1) / ((t0 - tp) * (t0 - tm1)) * h0
+                    + (tl - tp) * (tl - t0) / ((tm1 - tp) * (tm1 - t0)) * h1;
+            }
+        }
+    };
+    // upper r boundary (finebound.f90:153-187)
+    for (int m = 0; m <= imax; ++m)
+        for (int n = 0; n <= F.Nz + g - 1; ++n) {
+            const double r0 = S.rmaxl[level] - (double)m * S.drl[level];
+            const double z0 = S.zminl[level] + (double)n * S.dzl[level];
+            point(r0, z0, m, n, 'r');
+        }
+    // upper z boundary (finebound.f90:296-316)
+    for (int n = 0; n <= jmax; ++n)
+        for (int m = 0; m <= F.Nr + g - 1; ++m) {
+            const double r0 = S.rminl[level] + (double)m * S.drl[level];
+            const double z0 = S.zmaxl[level] - (double)n * S.dzl[level];
+            point(r0, z0, m, n, 'z');
+        }
+    if (!S.P.eqsym) throw std::runtime_error("oracle: finebound lower-z strip (eqsym=.false.) not restated");
+}
+
+// restrict.f90:2-169 with restrict_interp.inc
+static void restrict_(Sim& S, int level) {
+    Level& F = S.L[level];
+    Level& Cl = S.L[level - 1];
+    const int g = F.g;
+    const double deltar = (double)(2 * g) * S.drl[level] + 1.0e-10;
+    const double deltaz = (double)(2 * g) * S.dzl[level] + 1.0e-10;
+    Arr& rc = Cl.a("r"); Arr& zc = Cl.a("z");
+    for (int n = 0; n <= Cl.Nz + g - 1; ++n)
+        for (int m = 0; m <= Cl.Nr + g - 1; ++m) {
+            const double r0 = S.rminl[level - 1] + (double)m * S.drl[level - 1];
+            const double z0 = S.zminl[level - 1] + (double)n * S.dzl[level - 1];
+            const double rmin = (S.rminl[level] < 0.0) ? 0.0 : S.rminl[level] + deltar;
+            const double zmin = (S.P.eqsym && S.zminl[level] < 0.0) ? 0.0 : S.zminl[level] + deltaz;
+            const double rmax = S.rmaxl[level] - deltar;
+            const double zmax = S.zmaxl[level] - deltaz;
+            if (r0 > rmin && r0 < rmax && z0 > zmin && z0 < zmax) {
+                const int i = (int)nint_((r0 - rc(1 - g, 0)) / S.drl[level - 1]) + 1 - g;
+                const int j = (int)nint_((z0 - zc(0, 1 - g)) / S.dzl[level - 1]) + 1 - g;
+                const bool flag1 = (i >= 1 - g) && (i <= Cl.Nr) && (j >= 1 - g) && (j <= Cl.Nz);
+                for (const EvolvedVar& e : S.evolved) {
+                    const double aux2 = interp(S, level, F.a(e.name), r0, z0);
+                    if (flag1) Cl.a(e.name)(i, j) = aux2;
+                }
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// onestep.f90:2-522 (box 0 only; Nb = 0 so syncboxes never runs)
+// ---------------------------------------------------------------------------
+static void onestep(Sim& S, int level) {
+    const ollin_params& P = S.P;
+    const bool rk4 = P.integrator == OLLIN_INTEGRATOR_RK4;
+    const bool matter = P.mattertype != OLLIN_MATTER_VACUUM;
+    Level& L = S.L[level];
+    currentgrid(S, L);
+    saveold(S, L);
+    const int niter = rk4 ? 4 : P.icniter;
+    const double dt = L.dt;
+    for (int iter = 1; iter <= niter; ++iter) {
+        double dtw = 0, weight = 0;
+        if (rk4) {
+            switch (iter) {
+                case 1: dtw = 0.5 * dt; weight = 1.0 / 6.0; break;
+                case 2: dtw = 0.5 * dt; weight = 1.0 / 3.0; break;
+                case 3: dtw = dt; weight = 1.0 / 3.0; break;
+                case 4: dtw = dt; weight = 1.0 / 6.0; break;
+            }
+        } else {
+            dtw = (iter < niter) ? 0.5 * dt : dt;
+        }
+        sources_geometry(S, L);
+        sources_lapse(S, L);
+        if (P.shift != OLLIN_SHIFT_NONE) sources_shift(S, L);
+        if (matter) sources_scalar(S, L);
+        if (level == 0 && P.boundtype == OLLIN_BOUND_RADIATIVE) radiative_geometry(S, L);
+        if (rk4) accumulate(S, L, iter, niter, weight);
+        update(S, L, dtw);
+        if (level > 0) finebound(S, level, dtw);
+        if (L.ownaxis) symmetries_r(S, L);
+        if (L.eqsym && L.ownequator) symmetries_z(S, L);
+        auxiliary(S, L);
+    }
+    S.t2[level] = S.t1[level];
+    S.t1[level] = S.t[level];
+    S.s[level] = S.s[level] + 1;
+    S.t[level] = S.t[level] + dt;
+    S.point_updates += (double)L.Nr * (double)(L.eqsym ? L.Nz : L.Nz + L.g);
+    if (level < S.Nlmax) {
+        onestep(S, level + 1);
+        onestep(S, level + 1);
+    }
+    if (level > 0 && S.s[level] % 2 == 0) {
+        restrict_(S, level);
+        Level& Cl = S.L[level - 1];
+        currentgrid(S, Cl);
+        if (Cl.ownaxis) symmetries_r(S, Cl);
+        if (Cl.eqsym && Cl.ownequator) symmetries_z(S, Cl);
+        auxiliary(S, Cl);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// initial.f90:59-218, 528-645 for minkowski / schwarzschild / Brill-Lindquist
+// ---------------------------------------------------------------------------
+static void initial(Sim& S) {
+    const ollin_params& P = S.P;
+    const double zero = 0.0, half = 0.5, third = 1.0 / 3.0, one = 1.0, two = 2.0;
+    for (Level& L : S.L) {
+        currentgrid(S, L);
+        const int g = L.g, Nr = L.Nr, Nz = L.Nz;
+        auto setc = [&](const char* n, double v) { Arr& a = L.a(n); for (double& x : a.v) x = v; };
+        setc("alpha", one); setc("dtalpha", zero);
+        if (P.shift != OLLIN_SHIFT_NONE) { setc("beta_r", zero); setc("beta_z", zero); setc("dtbeta_r", zero); setc("dtbeta_z", zero); setc("fdriver", one); }
+        setc("psi", one); setc("phi", zero); setc("chi", one); setc("psi2", one); setc("psi4", one);
+        setc("A", one); setc("B", one); setc("H", one); setc("C", zero);
+        setc("g_A", one); setc("g_B", one); setc("g_H", one); setc("g_C", zero);
+        setc("trK", zero); setc("KTA", zero); setc("KTB", zero); setc("KTC", zero); setc("KTH", zero);
+        setc("Delta_r", zero); setc("Delta_z", zero); setc("lambda", zero); setc("Alambda", zero); setc("z4theta", zero);
+        Arr& psi = L.a("psi"); Arr& phi = L.a("phi"); Arr& chi = L.a("chi"); Arr& psi2 = L.a("psi2"); Arr& psi4 = L.a("psi4");
+        Arr& rr = L.a("rr"); Arr& alpha = L.a("alpha"); Arr& r = L.a("r"); Arr& z = L.a("z");
+        const double M = P.bh1mass;
+        if (P.idata == OLLIN_IDATA_SCHWARZSCHILD || P.idata == OLLIN_IDATA_BRILLLINDQUIST) {
+            for (int j = 1 - g; j <= Nz; ++j)
+                for (int i = 1 - g; i <= Nr; ++i) {
+                    if (P.idata == OLLIN_IDATA_SCHWARZSCHILD) psi(i, j) = one + half * M / std::fabs(rr(i, j));
+                    else psi(i, j) = one + half * M / std::sqrt(p2(r(i, j)) + p2(z(i, j) - 0.0));
+                    phi(i, j) = std::log(psi(i, j));
+                    chi(i, j) = one / std::pow(psi(i, j), (double)P.chipower);
+                    psi2(i, j) = p2(psi(i, j));
+                    psi4(i, j) = p4(psi(i, j));
+                    if (P.idata == OLLIN_IDATA_SCHWARZSCHILD && P.ilapse == OLLIN_ILAPSE_ISOTROPIC)
+                        alpha(i, j) = (one - half * M / std::fabs(rr(i, j))) / (one + half * M / std::fabs(rr(i, j)));
+                }
+        }
+        (void)psi2;
+    }
+    if (P.factorhdet) {  // initial.f90:528-577
+        for (Level& L : S.L) {
+            const int g = L.g, Nr = L.Nr, Nz = L.Nz;
+            Arr& A = L.a("A"); Arr& B = L.a("B"); Arr& C = L.a("C"); Arr& H = L.a("H"); Arr& r = L.a("r");
+            Arr& hdet = L.a("hdet"); Arr& ihdet = L.a("ihdet"); Arr& phi = L.a("phi"); Arr& aux = L.a("auxarray");
+            Arr& psi = L.a("psi"); Arr& psi2 = L.a("psi2"); Arr& psi4 = L.a("psi4");
+            for (int j = 1 - g; j <= Nz; ++j)
+                for (int i = 1 - g; i <= Nr; ++i) {
+                    hdet(i, j) = (A(i, j) * B(i, j) - p2(r(i, j) * C(i, j))) * H(i, j);
+                    phi(i, j) = phi(i, j) + std::log(hdet(i, j)) / 12.0;
+                    aux(i, j) = std::pow(hdet(i, j), third);
+                    A(i, j) = A(i, j) / aux(i, j);
+                    B(i, j) = B(i, j) / aux(i, j);
+                    C(i, j) = C(i, j) / aux(i, j);
+                    H(i, j) = H(i, j) / aux(i, j);
+                    hdet(i, j) = 1.0;
+                    ihdet(i, j) = 1.0;
+                    psi(i, j) = std::exp(phi(i, j));
+                    psi2(i, j) = p2(psi(i, j));
+                    psi4(i, j) = p4(psi(i, j));
+                }
+        }
+    }
+    for (Level& L : S.L) {  // initial.f90:583-607 traceless projection
+        const int g = L.g, Nr = L.Nr, Nz = L.Nz;
+        Arr& g_A = L.a("g_A"); Arr& g_B = L.a("g_B"); Arr& g_H = L.a("g_H"); Arr& g_C = L.a("g_C");
+        Arr& KTA = L.a("KTA"); Arr& KTB = L.a("KTB"); Arr& KTH = L.a("KTH"); Arr& KTC = L.a("KTC");
+        Arr& A = L.a("A"); Arr& B = L.a("B"); Arr& C = L.a("C"); Arr& H = L.a("H"); Arr& r = L.a("r"); Arr& aux = L.a("auxarray");
+        for (int j = 1 - g; j <= Nz; ++j)
+            for (int i = 1 - g; i <= Nr; ++i) aux(i, j) = g_A(i, j) * KTA(i, j) + g_B(i, j) * KTB(i, j) + g_H(i, j) * KTH(i, j) + two * p2(r(i, j)) * g_C(i, j) * KTC(i, j);
+        for (int j = 1 - g; j <= Nz; ++j)
+            for (int i = 1 - g; i <= Nr; ++i) {
+                KTA(i, j) = KTA(i, j) - third * A(i, j) * aux(i, j);
+                KTB(i, j) = KTB(i, j) - third * B(i, j) * aux(i, j);
+                KTH(i, j) = KTH(i, j) - third * H(i, j) * aux(i, j);
+                KTC(i, j) = KTC(i, j) - third * C(i, j) * aux(i, j);
+            }
+    }
+    if (P.ilapse == OLLIN_ILAPSE_PSIMINUS2 || P.ilapse == OLLIN_ILAPSE_PSIMINUS4) {
+        for (Level& L : S.L) {
+            Arr& alpha = L.a("alpha"); Arr& psi = L.a("psi");
+            for (size_t q = 0; q < alpha.v.size(); ++q)
+                alpha.v[q] = (P.ilapse == OLLIN_ILAPSE_PSIMINUS2) ? one / p2(psi.v[q]) : one / p4(psi.v[q]);
+        }
+    }
+}
+
+// evolve.f90:124-195 (box 0, no maximal slicing)
+static void initialize(Sim& S) {
+    initial(S);
+    for (Level& L : S.L) {
+        currentgrid(S, L);
+        if (L.ownaxis) symmetries_r(S, L);
+        if (L.eqsym && L.ownequator) symmetries_z(S, L);
+    }
+    for (Level& L : S.L) {
+        currentgrid(S, L);
+        auxiliary(S, L);
+    }
+    if (S.P.shift == OLLIN_SHIFT_GAMMADRIVER2) {
+        for (Level& L : S.L) {
+            Arr& b = L.a("dtbeta_r"); Arr& bz = L.a("dtbeta_z"); Arr& dr_ = L.a("Delta_r"); Arr& dz_ = L.a("Delta_z");
+            for (size_t q = 0; q < b.v.size(); ++q) { b.v[q] = S.P.drivercsi * dr_.v[q]; bz.v[q] = S.P.drivercsi * dz_.v[q]; }
+        }
+    }
+}
+
+// save0Ddata.f90:221-288 and the origin value at :370-374
+static void norms(Sim& S, int level, const Arr& v, double out[5]) {
+    Level& L = S.L[level];
+    double vmax = -1.0e10, vmin = +1.0e10, nm1 = 0.0, nm2 = 0.0, NN = 0.0;
+    for (int j = 1; j <= L.Nz - L.g; ++j)
+        for (int i = 1; i <= L.Nr - L.g; ++i) {
+            const double aux = v(i, j);
+            if (std::isnan(aux)) throw std::runtime_error("norms: NaN found");
+            NN = NN + 1.0;
+            vmin = std::min(vmin, aux);
+            vmax = std::max(vmax, aux);
+            nm1 = std::max(nm1, std::fabs(aux));
+            nm2 = nm2 + p2(aux);
+        }
+    out[0] = vmax; out[1] = vmin; out[2] = nm1; out[3] = std::sqrt(nm2 / NN);
+    out[4] = interp(S, level, v, 0.0, 0.0);
+}
+
+}  // namespace oracle
+
+// ---------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------
+using namespace oracle;
+
+struct ollin_oracle { Sim S; };
+
+static thread_local std::string g_oracle_err;
+
+extern "C" {
+
+const char* ollin_oracle_last_error(void) { return g_oracle_err.c_str(); }
+
+int ollin_oracle_create(const ollin_params* p, ollin_oracle** out) {
+    try {
+        auto* o = new ollin_oracle();
+        o->S.P = *p;
+        setup(o->S);
+        *out = o;
+        return 0;
+    } catch (const std::exception& e) {
+        g_oracle_err = e.what();
+        return 1;
+    }
+}
+
+void ollin_oracle_destroy(ollin_oracle* o) { delete o; }
+
+int ollin_oracle_initialize(ollin_oracle* o) {
+    try { initialize(o->S); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }
+}
+
+int ollin_oracle_step(ollin_oracle* o, double* t_out) {
+    try {
+        onestep(o->S, 0);
+        if (t_out) *t_out = o->S.t[0];
+        return 0;
+    } catch (const std::exception& e) {
+        g_oracle_err = e.what();
+        return 1;
+    }
+}
+
+int ollin_oracle_num_levels(const ollin_oracle* o) { return (int)o->S.L.size(); }
+
+int ollin_oracle_dims(const ollin_oracle* o, int level, int* nr, int* nz, int* ghost) {
+    if (level < 0 || level >= (int)o->S.L.size()) return 1;
+    const Level& L = o->S.L[level];
+    *nr = L.Nr; *nz = L.Nz; *ghost = L.g;
+    return 0;
+}
+
+double ollin_oracle_time(const ollin_oracle* o, int level) { return o->S.t[level]; }
+
+// Copy grid function ``name`` of ``level`` into ``a`` (column-major,
+// leading dimension ld_r, element (1-ghost,1-ghost) first).
+int ollin_oracle_get(ollin_oracle* o, int level, const char* name, double* a, int ld_r) {
+    if (level < 0 || level >= (int)o->S.L.size()) { g_oracle_err = "bad level"; return 1; }
+    Level& L = o->S.L[level];
+    auto it = L.arrs.find(name);
+    if (it == L.arrs.end()) { g_oracle_err = std::string("unknown array ") + name; return 1; }
+    const Arr& v = it->second;
+    for (int j = 0; j < L.Nz + L.g; ++j)
+        for (int i = 0; i < L.Nr + L.g; ++i) a[(size_t)i + (size_t)j * ld_r] = v.v[(size_t)i + (size_t)j * v.ld];
+    return 0;
+}
+
+int ollin_oracle_set(ollin_oracle* o, int level, const char* name, const double* a, int ld_r) {
+    if (level < 0 || level >= (int)o->S.L.size()) { g_oracle_err = "bad level"; return 1; }
+    Level& L = o->S.L[level];
+    Arr& v = L.a(name);
+    for (int j = 0; j < L.Nz + L.g; ++j)
+        for (int i = 0; i < L.Nr + L.g; ++i) v.v[(size_t)i + (size_t)j * v.ld] = a[(size_t)i + (size_t)j * ld_r];
+    return 0;
+}
+
+int ollin_oracle_aux(ollin_oracle* o, int level) {
+    try {
+        Level& L = o->S.L[level];
+        L.time = o->S.t[level];
+        auxiliary(o->S, L);
+        return 0;
+    } catch (const std::exception& e) {
+        g_oracle_err = e.what();
+        return 1;
+    }
+}
+
+int ollin_oracle_constraints(ollin_oracle* o, int level) {
+    try { constraints(o->S, o->S.L[level]); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }
+}
+
+int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]) {
+    try {
+        Level& L = o->S.L[level];
+        auto it = L.arrs.find(name);
+        if (it == L.arrs.end()) { g_oracle_err = std::string("unknown array ") + name; return 1; }
+        norms(o->S, level, it->second, out);
+        return 0;
+    } catch (const std::exception& e) {
+        g_oracle_err = e.what();
+        return 1;
+    }
+}
+
+double ollin_oracle_point_updates(const ollin_oracle* o) { return o->S.point_updates; }
+
+}  // extern "C"
