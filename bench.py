@@ -1,0 +1,336 @@
+"""Benchmark: FP64 BSSN point-updates/s of the OllinAxis-BiB evolution path.
+
+Workload (one "step" = one coarse step, ``call onestep(0)``): the large plain
+configuration -- a Schwarzschild puncture (M=1, psi = 1 + M/2r, lapse psi^-2)
+with 1+log slicing and the Gamma-driver-2 shift (drivereta = 2/M), 6
+box-in-box levels of 512x512 points (finest dr = dz = 0.00625), RK4, 4th-order
+differences, Kreiss-Oliger eps = 0.02, Courant factor 0.25, FP64.  One coarse
+step advances level l by 2^l steps: 63 x 512^2 = 16.5 M point-updates.  Data
+are synthetic (analytic initial data); the state (~1.5 GB) is far larger than
+the 129 MB L2, so no L2 flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+``value`` is device-resident throughput timed with CUDA events on the
+library's stream.  ``e2e`` is measured through the C ABI as a host-resident
+caller would use it: every step copies the evolved state of all levels from
+pinned host memory to the device, runs the coarse step and copies it back.
+``--impl reference`` times the CPU restatement of the reference (oracle/,
+the reference Fortran itself cannot be compiled on these hosts) on the host
+cores.  With N > 1 (torchrun) every rank evolves an independent replica.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "ollinaxis-bib_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+WORKLOAD = dict(nrtotal=512, nztotal=512, nl0=5, dr0=0.2, dz0=0.2, eqsym=1, idata="schwarzschild",
+                bh1mass=1.0, ilapse="psiminus2", slicing="1+log", gauge_f=2.0, shift="Gammadriver2",
+                drivercsi=0.75, drivereta=2.0, integrator="rk4", order="four", geodiss=0.02,
+                dtfac=0.25, boundtype="radiative")
+METRIC = "FP64 BSSN point-updates/s"
+UNIT = "point-updates/s"
+F_EVOLVED = 16          # fields with non-zero sources (12 BSSN + 4 shift)
+ALG_BYTES_PER_PU = 136 * F_EVOLVED  # compulsory FP64 traffic per point-update (3-register RK4)
+
+
+def config_dict(args):
+    nlev, n = args.levels, args.size
+    return {"workload": "schwarzschild puncture, %d box-in-box levels of %dx%d, Gammadriver2, 1+log, RK4, FP64" % (nlev, n, n),
+            "levels": nlev, "points_per_level": "%dx%d" % (n, n), "finest_dr": 0.2 / 2 ** (nlev - 1),
+            "coarse_steps_per_step": 1, "point_updates_per_step": (2 ** nlev - 1) * n * n,
+            "integrator": "rk4", "order": 4,
+            "l2": "inputs larger than L2 (1.5 GB state), no flush", "parallelism": "replicas" if args.gpus > 1 else "single"}
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(threads=None, seconds=10.0):
+    """The oracle (CPU restatement of the reference, C++ -O2) on one 512x512
+    level of the same physics, timed for roughly ``seconds`` of work."""
+    if threads is not None:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle_bind import Oracle
+    from ollin.params import params_from_dict
+    cfg = dict(WORKLOAD, nl0=0)
+    o = Oracle(params_from_dict(cfg))
+    o.initial_data()
+    o.initialize()
+    o.step()  # warm-up
+    pu0 = o.point_updates()
+    t0 = time.time()
+    n = 0
+    while True:
+        o.step()
+        n += 1
+        if time.time() - t0 >= seconds or n >= 50:
+            break
+    dt = time.time() - t0
+    v = (o.point_updates() - pu0) / dt
+    return {"value": v, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", "1")), "kind": "port",
+            "sample": "%d RK4 steps of one 512x512 level (Gammadriver2, 1+log, FP64), %.1f s" % (n, dt)}
+
+
+def run_reference(args):
+    world, rank, _, pg = dist_setup(args)
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle_bind import Oracle
+    from ollin.params import params_from_dict
+    cfg = dict(WORKLOAD, nl0=0)
+    o = Oracle(params_from_dict(cfg))
+    o.initial_data()
+    o.initialize()
+    for _ in range(args.warmup):
+        o.step()
+    pu0 = o.point_updates()
+    t0 = time.time()
+    for _ in range(args.steps):
+        o.step()
+    dt = time.time() - t0
+    v = (o.point_updates() - pu0) / dt
+    sample = "%d RK4 steps of one 512x512 level of the workload's physics per timed region" % args.steps
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (analytic Schwarzschild initial data)", "config": config_dict(args),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    world, rank, local, pg = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    from ollin.gpu import Evolution, load, field_id
+    from ollin.params import params_from_dict
+    L = load()
+    p = params_from_dict(WORKLOAD)
+    e = Evolution(p)
+    e.initial_data()
+    e.initialize()
+    stream = torch.cuda.ExternalStream(e.stream())
+    for _ in range(args.warmup):
+        e.step()
+    torch.cuda.synchronize()
+    # ---- device-resident throughput -------------------------------------
+    e.kernel_timing(True)
+    launches0 = e.launch_count()
+    pu0 = e.point_updates()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        e.step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(pg)
+    clocks = sampler.stop()
+    ms_local = ev0.elapsed_time(ev1)
+    launches = e.launch_count() - launches0
+    pu = e.point_updates() - pu0
+    rhs_ms, rhs_n, rhs_pts = e.kernel_stats()
+    e.kernel_timing(False)
+    ms = max_over_ranks(pg, ms_local)
+    pu_all = sum_over_ranks(pg, pu)
+    value = pu_all / (ms * 1e-3)
+    # ---- end to end through the C ABI with host-resident state -----------
+    names = ["alpha", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTC", "Delta_r", "Delta_z",
+             "beta_r", "beta_z", "dtbeta_r", "dtbeta_z"]
+    host = {}
+    for lev in e.levels():
+        d = e.desc(lev)
+        for nm in names:
+            host[(lev, nm)] = torch.empty((d.nz + d.ghost, d.nr + d.ghost), dtype=torch.float64).pin_memory()
+            e.L.ollin_gpu_download(e.h, lev, field_id(nm), ctypes.c_void_p(host[(lev, nm)].data_ptr()),
+                                   d.nr + d.ghost)
+    bytes_per_dir = sum(t.numel() * 8 for t in host.values())
+    e2e_steps = max(2, args.steps // 2)
+    barrier(pg)
+    t0 = time.perf_counter()
+    pu1 = e.point_updates()
+    for _ in range(e2e_steps):
+        for (lev, nm), t in host.items():
+            rc = e.L.ollin_gpu_upload(e.h, lev, field_id(nm), ctypes.c_void_p(t.data_ptr()), t.shape[1])
+            assert rc == 0
+        e.step()
+        for (lev, nm), t in host.items():
+            rc = e.L.ollin_gpu_download(e.h, lev, field_id(nm), ctypes.c_void_p(t.data_ptr()), t.shape[1])
+            assert rc == 0
+    torch.cuda.synchronize()
+    dt_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+    e2e_value = sum_over_ranks(pg, e.point_updates() - pu1) / dt_e2e
+    # ---- roofline of the right-hand-side kernel --------------------------
+    # algorithmic bytes per launch = 136 F / 4 bytes per point-stage x points
+    avg_launch_s = rhs_ms * 1e-3 / max(rhs_n, 1)
+    alg_bytes_per_launch = (ALG_BYTES_PER_PU / 4.0) * rhs_pts / max(rhs_n, 1)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak, peak_note = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        with open(peaks_path) as f:
+            hbm_peak = float(json.load(f).get("hbm_gbs", hbm_peak))
+            peak_note = "measured"
+    achieved = alg_bytes_per_launch / avg_launch_s / 1e9
+    dfma_rate = L.ollin_gpu_fp64_rate()
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "rhs_kernel_traffic.json")
+    if os.path.exists(prof):
+        with open(prof) as f:
+            pj = json.load(f)
+        traffic = pj.get("dram_bytes_per_point_stage", None)
+        if traffic is not None:
+            traffic = traffic * rhs_pts / max(rhs_n, 1)
+        dp_per_pt = pj.get("dp_instructions_per_point_stage", None)
+    else:
+        dp_per_pt = None
+    fp64 = {"peak_dfma_per_s": dfma_rate, "peak_note": "measured live (DFMA chains on all SMs)"}
+    if dp_per_pt:
+        achieved_dp = dp_per_pt * rhs_pts / (rhs_ms * 1e-3)
+        fp64.update({"dp_instructions_per_point_stage": dp_per_pt, "achieved_dp_per_s": achieved_dp,
+                     "frac": achieved_dp / dfma_rate})
+    e.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (analytic Schwarzschild initial data)", "config": config_dict(args),
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_per_dir,
+                        "d2h_bytes_per_step": bytes_per_dir, "steps": e2e_steps},
+                "gpu_launches": launches,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": achieved / hbm_peak, "traffic": traffic,
+                             "kernel": "rhs_kernel (fused RHS + RK stage)", "peak_source": peak_note,
+                             "binding_ceiling": "fp64", "fp64": fp64,
+                             "rhs_launches": rhs_n, "rhs_avg_launch_ms": avg_launch_s * 1e3,
+                             "rhs_share_of_step": (rhs_ms / max(ms_local, 1e-9))},
+                "clocks": clocks}
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(threads=os.cpu_count(), seconds=args.cpu_seconds)
+        print(json.dumps(line))
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
+    ap.add_argument("--size", type=int, default=512, help="points per level per direction")
+    args = ap.parse_args()
+    WORKLOAD.update(nl0=args.levels - 1, nrtotal=args.size, nztotal=args.size)
+    if args.impl == "reference":
+        if args.steps > 3:
+            args.steps = 3  # bounded CPU sample per timed region
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -195,6 +195,17 @@ void* ollin_gpu_stream(const ollin_handle* h);
 /* Number of kernel launches this handle has issued so far. */
 long long ollin_gpu_launch_count(const ollin_handle* h);
 
+/* Per-launch timing of the right-hand-side kernel with CUDA events on the
+ * handle's stream (for roofline reporting).  Enabling resets the counters.
+ * No counterpart in the reference, which has no timers. */
+int ollin_gpu_kernel_timing(ollin_handle* h, int enable);
+int ollin_gpu_kernel_stats(ollin_handle* h, double* rhs_ms, long long* launches, double* point_stages);
+
+/* Measured FP64 fused-multiply-add instruction rate of the current device
+ * (DFMA per second), the ceiling the right-hand-side kernel is held to.
+ * No counterpart in the reference. */
+double ollin_gpu_fp64_rate(void);
+
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);
 

@@ -1,0 +1,793 @@
+// Host side of the GB300 evolution library: level hierarchy, buffer
+// rotation, the Berger-Oliger schedule of src/base/onestep.f90 and the C ABI
+// declared in include/ollin_gpu.h.
+//
+// Schedule per level step (onestep.f90:90-357):
+//   saveold          -> rotate state slots: pp <- p, p <- cur (no copy)
+//   per RK4 stage    -> rhs (sources + dissipation + radiative boundary +
+//                       accumulate + update), prolongation of the fine-level
+//                       boundary strips, parity ghost fill, aux_point,
+//                       aux_deriv (the ``auxiliary`` of the next stage)
+//   then two steps of the next finer level, and restriction to the coarser
+//   level when both coincide in time (onestep.f90:375-469).
+// The boundary history var_bound_* of the reference is the strip of the
+// state at the start of the current (p) and previous (pp) step, so it is read
+// straight from those slots.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ollin_gpu.h"
+#include "ollin_kernels.h"
+
+using namespace ollin;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_OR_FAIL(x)                                                               \
+    do {                                                                              \
+        cudaError_t e_ = (x);                                                         \
+        if (e_ != cudaSuccess) return fail(OLLIN_ECUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int kSlots = 4;
+
+struct DLevel {
+    int level = 0, nr = 0, nz = 0, g = 3, ld = 0, rows = 0;
+    size_t n = 0;  // elements per grid function
+    double dr = 0, dz = 0, dt = 0;
+    double* pool = nullptr;
+    double* slot[kSlots][NFIELDS] = {};
+    double* acc[NFIELDS] = {};
+    double* aux[NAUX] = {};
+    double* coords = nullptr;  // rcol | ircol | zrow
+    int cur = 0, p = 1, pp = 2;
+    LevelGeom G{};
+    bool last_aux_t0 = true;
+    std::vector<double> rh, zh;  // host copies of the coordinates
+};
+
+}  // namespace
+
+struct ollin_handle {
+    ollin_params P{};
+    int g = 3, nlev = 0;
+    std::vector<DLevel> L;
+    std::vector<double> t, t1, t2, rminl, rmaxl, zminl, zmaxl;
+    std::vector<long> s;
+    std::vector<int> fields;  // active field slots
+    int symr[NFIELDS] = {}, symz[NFIELDS] = {};
+    cudaStream_t stream = nullptr;
+    unsigned int* d_flag = nullptr;
+    double* d_norm = nullptr;
+    double point_updates = 0;
+    long long launches = 0;
+    bool initialized = false;
+    bool shift = false, scalar = false;
+    PhysParams phys{};
+    // optional per-launch timing of the right-hand-side kernel
+    bool ktime = false;
+    std::vector<cudaEvent_t> ev;  // start/stop pairs
+    size_t ev_used = 0;
+    double rhs_point_stages = 0;
+    long long rhs_launches = 0;
+};
+
+namespace {
+
+// parity tags of the evolved fields (src/base/arrays.config)
+void parity_table(ollin_handle* h) {
+    auto set = [&](int f, int sr, int sz) { h->symr[f] = sr; h->symz[f] = sz; };
+    for (int f = 0; f < NFIELDS; ++f) set(f, +1, +1);
+    set(F_C, +1, -1); set(F_KTC, +1, -1);
+    set(F_DLR, -1, +1); set(F_DLZ, +1, -1);
+    set(F_BETAR, -1, +1); set(F_BETAZ, +1, -1);
+    set(F_DTBETAR, -1, +1); set(F_DTBETAZ, +1, -1);
+    set(F_SXIR, -1, +1); set(F_SXIZ, +1, -1);
+}
+
+double* base_ptr(const DLevel& L, double* p) { return p ? p + (L.g - 1) + (size_t)(L.g - 1) * L.ld : nullptr; }
+
+int check_params(const ollin_params& P) {
+    if (P.order != 4) return fail(OLLIN_EINVAL, "order must be \"four\" (4)");
+    if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
+    if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
+    if (!P.eqsym) return fail(OLLIN_EINVAL, "only equatorial symmetry (eqsym) is supported");
+    if (P.ghost != 0 && P.ghost != 3) return fail(OLLIN_EINVAL, "ghost must be 3 for order four");
+    if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
+    if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
+    if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
+    if (P.shift != OLLIN_SHIFT_NONE && P.shift != OLLIN_SHIFT_GAMMADRIVER2)
+        return fail(OLLIN_EINVAL, "shift must be none or Gammadriver2");
+    if (P.slicing < 0 || P.slicing > 3) return fail(OLLIN_EINVAL, "unknown slicing");
+    if (P.integrator != OLLIN_INTEGRATOR_RK4 && P.integrator != OLLIN_INTEGRATOR_ICN) return fail(OLLIN_EINVAL, "unknown integrator");
+    if (P.integrator == OLLIN_INTEGRATOR_ICN && P.icniter < 1) return fail(OLLIN_EINVAL, "icniter must be positive");
+    if (P.mattertype != OLLIN_MATTER_VACUUM && P.mattertype != OLLIN_MATTER_SCALAR) return fail(OLLIN_EINVAL, "unknown mattertype");
+    if (P.boundtype != OLLIN_BOUND_RADIATIVE && P.boundtype != OLLIN_BOUND_NONE) return fail(OLLIN_EINVAL, "unknown boundtype");
+    if (!(P.dr0 > 0 && P.dz0 > 0 && P.dtfac > 0)) return fail(OLLIN_EINVAL, "dr0, dz0 and dtfac must be positive");
+    return OLLIN_OK;
+}
+
+int alloc_level(ollin_handle* h, DLevel& L, int level) {
+    const ollin_params& P = h->P;
+    const int g = h->g;
+    L.level = level;
+    L.g = g;
+    L.nr = P.nrtotal;
+    L.nz = P.nztotal;
+    L.ld = ((L.nr + g + 31) / 32) * 32;
+    L.rows = L.nz + g;
+    L.n = (size_t)L.ld * L.rows;
+    const double dt0 = P.dtfac * std::min(P.dr0, P.dz0);
+    L.dt = dt0 / (double)(1 << level);  // setupboxes.f90:121-125
+    L.dr = P.dr0 / (double)(1 << level);
+    L.dz = P.dz0 / (double)(1 << level);
+    const size_t ncoord = (size_t)(L.nr + g) * 2 + (size_t)(L.nz + g);
+    const size_t narrays = (size_t)kSlots * NFIELDS + NFIELDS + NAUX;
+    const size_t bytes = (narrays * L.n + ncoord + 64) * sizeof(double);
+    if (cudaMalloc(&L.pool, bytes) != cudaSuccess) return fail(OLLIN_ENOMEM, "device allocation failed for level " + std::to_string(level));
+    CUDA_OR_FAIL(cudaMemsetAsync(L.pool, 0, bytes, h->stream));
+    double* q = L.pool;
+    for (int k = 0; k < kSlots; ++k)
+        for (int f = 0; f < NFIELDS; ++f) { L.slot[k][f] = q; q += L.n; }
+    for (int f = 0; f < NFIELDS; ++f) { L.acc[f] = q; q += L.n; }
+    for (int x = 0; x < NAUX; ++x) { L.aux[x] = q; q += L.n; }
+    L.coords = q;
+    // coordinates (evolve.f90:42-70, box 0, one process)
+    L.rh.resize(L.nr + g);
+    L.zh.resize(L.nz + g);
+    std::vector<double> host(ncoord);
+    for (int i = 1 - g; i <= L.nr; ++i) {
+        const double r = ((double)(0 + i) - 0.5) * L.dr;
+        L.rh[i - 1 + g] = r;
+        host[i - 1 + g] = r;
+        host[(size_t)(L.nr + g) + (i - 1 + g)] = 1.0 / r;
+    }
+    for (int j = 1 - g; j <= L.nz; ++j) {
+        const double z = ((double)(0 + j) - 0.5) * L.dz;
+        L.zh[j - 1 + g] = z;
+        host[(size_t)(L.nr + g) * 2 + (j - 1 + g)] = z;
+    }
+    CUDA_OR_FAIL(cudaMemcpyAsync(L.coords, host.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    LevelGeom& G = L.G;
+    G.nr = L.nr; G.nz = L.nz; G.g = g; G.ld = L.ld;
+    G.eqsym = P.eqsym ? 1 : 0;
+    G.jlo = P.eqsym ? 1 : 1 - g;
+    G.dr = L.dr; G.dz = L.dz; G.dt = L.dt;
+    G.idr = 1.0 / L.dr; G.idz = 1.0 / L.dz;
+    G.rcol = L.coords + (g - 1);                 // rcol[i] for i >= 1-g
+    G.ircol = L.coords + (L.nr + g) + (g - 1);
+    G.zrow = L.coords + 2 * (L.nr + g) + (g - 1);
+    h->rminl[level] = L.rh[0];
+    h->rmaxl[level] = L.rh[L.nr - 1 + g];
+    h->zminl[level] = L.zh[0];
+    h->zmaxl[level] = L.zh[L.nz - 1 + g];
+    L.cur = 0; L.p = 1; L.pp = 2;
+    return OLLIN_OK;
+}
+
+PhysParams make_phys(const ollin_params& P) {
+    PhysParams q{};
+    q.slicing = P.slicing;
+    q.gauge_f = P.gauge_f;
+    q.shift = P.shift == OLLIN_SHIFT_GAMMADRIVER2 ? 1 : 0;
+    q.shiftadvect = P.shiftadvect;
+    q.driveradv = P.driveradv;
+    q.drivercsi = P.drivercsi;
+    q.drivereta = P.drivereta;
+    q.eta = P.eta;
+    q.geodiss = P.geodiss;
+    q.scalardiss = P.scalardiss;
+    for (int k = 0; k < 8; ++k) q.ft[k] = P.ft[k];
+    q.scalar = P.mattertype == OLLIN_MATTER_SCALAR;
+    q.potential = P.scalarpotential;
+    q.scalar_mass = P.scalar_mass;
+    q.scalar_lambda = P.scalar_lambda;
+    q.boundtype = P.boundtype;
+    return q;
+}
+
+// ---- kernel launch helpers ---------------------------------------------------
+int after_launch(ollin_handle* h) {
+    h->launches++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(OLLIN_ECUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return OLLIN_OK;
+}
+
+int do_symmetry(ollin_handle* h, DLevel& L, int slot, const std::vector<int>& fl) {
+    SymArgs a{};
+    a.G = L.G;
+    a.nf = 0;
+    for (int f : fl) {
+        a.st[a.nf] = base_ptr(L, L.slot[slot][f]);
+        a.symr[a.nf] = h->symr[f];
+        a.symz[a.nf] = h->symz[f];
+        a.fid[a.nf] = f;
+        a.nf++;
+    }
+    launch_symmetry(a, h->stream);
+    return after_launch(h);
+}
+
+std::vector<int> active_fields(const ollin_handle* h, bool with_phi) {
+    std::vector<int> v;
+    for (int f : h->fields)
+        if (f != F_PHI || with_phi) v.push_back(f);
+    return v;
+}
+
+// ``auxiliary`` on one level's current slot (auxiliary_geometry.f90 parts
+// that feed the right-hand side).
+int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0) {
+    AuxArgs a{};
+    a.G = L.G;
+    for (int f = 0; f < NFIELDS; ++f) a.st[f] = base_ptr(L, L.slot[slot][f]);
+    for (int x = 0; x < NAUX; ++x) a.aux[x] = base_ptr(L, L.aux[x]);
+    a.t0 = t0 ? 1 : 0;
+    a.scalar = h->scalar ? 1 : 0;
+    launch_aux_point(a, h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    launch_aux_deriv(a, h->stream);
+    rc = after_launch(h);
+    if (rc) return rc;
+    if (t0) {
+        rc = do_symmetry(h, L, slot, {F_DLR, F_DLZ});
+        if (rc) return rc;
+    }
+    L.last_aux_t0 = t0;
+    return OLLIN_OK;
+}
+
+StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool t0) {
+    StageArgs a{};
+    a.G = L.G;
+    a.P = h->phys;
+    for (int f = 0; f < NFIELDS; ++f) {
+        a.in[f] = base_ptr(L, L.slot[in_slot][f]);
+        a.pst[f] = base_ptr(L, L.slot[L.p][f]);
+        a.out[f] = base_ptr(L, L.slot[out_slot][f]);
+        a.acc[f] = base_ptr(L, L.acc[f]);
+    }
+    for (int x = 0; x < NAUX; ++x) {
+        a.aux[x] = base_ptr(L, L.aux[x]);
+        a.auxw[x] = base_ptr(L, L.aux[x]);
+    }
+    a.t0 = t0 ? 1 : 0;
+    a.level0 = L.level == 0;
+    a.rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
+    a.nanflag = h->d_flag;
+    return a;
+}
+
+int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
+    DLevel& F = h->L[level];
+    DLevel& C = h->L[level - 1];
+    ProlongArgs a{};
+    a.F = F.G;
+    a.Cg = C.G;
+    const bool t0 = h->t[level] == 0.0;
+    a.nf = 0;
+    for (int f : active_fields(h, t0)) {
+        a.fid[a.nf++] = f;
+    }
+    for (int f = 0; f < NFIELDS; ++f) {
+        a.fout[f] = base_ptr(F, F.slot[out_slot][f]);
+        a.fp[f] = base_ptr(F, F.slot[F.p][f]);
+        a.fpp[f] = base_ptr(F, F.slot[F.pp][f]);
+        a.cin[f] = base_ptr(C, C.slot[C.cur][f]);
+    }
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
+    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
+    a.tp = h->t[level - 1];
+    a.t0 = h->t[level];
+    a.tm1 = h->t1[level];
+    a.tl = a.t0 + dtw;
+    a.imax = (a.tp == a.tl) ? h->g + 2 : h->g - 1;  // finebound.f90:106-112
+    a.border = (a.tm1 == 0.0) ? 1 : 2;              // finebound.f90:118-122
+    a.bicubic = h->P.interp_bicubic;
+    launch_prolong(a, h->stream);
+    return after_launch(h);
+}
+
+int restrict_level(ollin_handle* h, int level) {
+    DLevel& F = h->L[level];
+    DLevel& C = h->L[level - 1];
+    RestrictArgs a{};
+    a.F = F.G;
+    a.Cg = C.G;
+    a.nf = 0;
+    for (int f : active_fields(h, false)) a.fid[a.nf++] = f;
+    for (int f = 0; f < NFIELDS; ++f) {
+        a.fin[f] = base_ptr(F, F.slot[F.cur][f]);
+        a.cout[f] = base_ptr(C, C.slot[C.cur][f]);
+    }
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.eqsym = h->P.eqsym;
+    a.bicubic = h->P.interp_bicubic;
+    launch_restrict(a, h->stream);
+    return after_launch(h);
+}
+
+// onestep.f90:2-522 for box 0
+int onestep(ollin_handle* h, int level) {
+    DLevel& L = h->L[level];
+    const bool rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
+    const bool t0 = h->t[level] == 0.0;  // currentgrid: time = t(box,level)
+    // saveold: pp <- p, p <- cur
+    L.pp = L.p;
+    L.p = L.cur;
+    int freeslots[2], nfree = 0;
+    for (int k = 0; k < kSlots && nfree < 2; ++k)
+        if (k != L.p && k != L.pp) freeslots[nfree++] = k;
+    const int niter = rk4 ? 4 : h->P.icniter;
+    const double dt = L.dt;
+    int in_slot = L.p;
+    for (int iter = 1; iter <= niter; ++iter) {
+        double dtw, weight = 0;
+        if (rk4) {
+            switch (iter) {
+                case 1: dtw = 0.5 * dt; weight = 1.0 / 6.0; break;
+                case 2: dtw = 0.5 * dt; weight = 1.0 / 3.0; break;
+                case 3: dtw = dt; weight = 1.0 / 3.0; break;
+                default: dtw = dt; weight = 1.0 / 6.0; break;
+            }
+        } else {
+            dtw = (iter < niter) ? 0.5 * dt : dt;
+        }
+        const int out_slot = freeslots[(iter - 1) & 1];
+        StageArgs a = stage_args(h, L, in_slot, out_slot, t0);
+        a.iter = iter;
+        a.niter = niter;
+        a.dtw = dtw;
+        a.weight = weight;
+        if (h->ktime) {
+            if (h->ev_used + 2 > h->ev.size()) {
+                for (int k = 0; k < 256; ++k) {
+                    cudaEvent_t e;
+                    CUDA_OR_FAIL(cudaEventCreate(&e));
+                    h->ev.push_back(e);
+                }
+            }
+            CUDA_OR_FAIL(cudaEventRecord(h->ev[h->ev_used], h->stream));
+        }
+        launch_rhs(a, h->stream);
+        int rc = after_launch(h);
+        if (rc) return rc;
+        if (h->ktime) {
+            CUDA_OR_FAIL(cudaEventRecord(h->ev[h->ev_used + 1], h->stream));
+            h->ev_used += 2;
+            h->rhs_point_stages += (double)L.nr * (double)L.nz;
+            h->rhs_launches++;
+        }
+        if (level > 0) {
+            rc = prolong(h, level, out_slot, dtw);
+            if (rc) return rc;
+        }
+        rc = do_symmetry(h, L, out_slot, active_fields(h, t0));
+        if (rc) return rc;
+        rc = do_aux(h, L, out_slot, t0);
+        if (rc) return rc;
+        in_slot = out_slot;
+    }
+    L.cur = in_slot;
+    h->t2[level] = h->t1[level];
+    h->t1[level] = h->t[level];
+    h->s[level] = h->s[level] + 1;
+    h->t[level] = h->t[level] + dt;
+    h->point_updates += (double)L.nr * (double)L.nz;
+    if (level < h->nlev - 1) {
+        int rc = onestep(h, level + 1);
+        if (rc) return rc;
+        rc = onestep(h, level + 1);
+        if (rc) return rc;
+    }
+    if (level > 0 && h->s[level] % 2 == 0) {
+        int rc = restrict_level(h, level);
+        if (rc) return rc;
+        DLevel& C = h->L[level - 1];
+        rc = do_symmetry(h, C, C.cur, active_fields(h, false));
+        if (rc) return rc;
+        rc = do_aux(h, C, C.cur, h->t[level - 1] == 0.0);
+        if (rc) return rc;
+    }
+    return OLLIN_OK;
+}
+
+int internal_field(int field, bool* is_aux) {
+    *is_aux = false;
+    switch (field) {
+        case OLLIN_F_ALPHA: return F_ALPHA;
+        case OLLIN_F_PHI: return F_PHI;
+        case OLLIN_F_CHI: return F_CHI;
+        case OLLIN_F_A: return F_A;
+        case OLLIN_F_B: return F_B;
+        case OLLIN_F_H: return F_H;
+        case OLLIN_F_C: return F_C;
+        case OLLIN_F_TRK: return F_TRK;
+        case OLLIN_F_KTA: return F_KTA;
+        case OLLIN_F_KTB: return F_KTB;
+        case OLLIN_F_KTC: return F_KTC;
+        case OLLIN_F_DELTA_R: return F_DLR;
+        case OLLIN_F_DELTA_Z: return F_DLZ;
+        case OLLIN_F_BETA_R: return F_BETAR;
+        case OLLIN_F_BETA_Z: return F_BETAZ;
+        case OLLIN_F_DTBETA_R: return F_DTBETAR;
+        case OLLIN_F_DTBETA_Z: return F_DTBETAZ;
+        case OLLIN_F_SCALAR_PHI: return F_SPHI;
+        case OLLIN_F_SCALAR_XI_R: return F_SXIR;
+        case OLLIN_F_SCALAR_XI_Z: return F_SXIZ;
+        case OLLIN_F_SCALAR_PI: return F_SPI;
+        case OLLIN_F_KTH: *is_aux = true; return X_KTH;
+        case OLLIN_F_LAMBDA: *is_aux = true; return X_LAM;
+        case OLLIN_F_ALAMBDA: *is_aux = true; return X_ALAM;
+        case OLLIN_F_HAM: *is_aux = true; return X_HAM;
+        case OLLIN_F_MOM_R: *is_aux = true; return X_MOMR;
+        case OLLIN_F_MOM_Z: *is_aux = true; return X_MOMZ;
+        case OLLIN_F_RSCAL: *is_aux = true; return X_RSCAL;
+        case OLLIN_F_KT2: *is_aux = true; return X_KT2;
+        case OLLIN_F_LAPLA_ALPHA: *is_aux = true; return X_LAPLA;
+        default: return -1;
+    }
+}
+
+bool field_active(const ollin_handle* h, int f) {
+    for (int x : h->fields)
+        if (x == f) return true;
+    return false;
+}
+
+// constraints.f90 on the current state: ham, mom_r, mom_z (+ RSCAL, KT2,
+// Lapla_alpha) of one level.
+int analysis(ollin_handle* h, int level) {
+    DLevel& L = h->L[level];
+    StageArgs a = stage_args(h, L, L.cur, L.cur, L.last_aux_t0);
+    a.analysis = 1;
+    launch_rhs(a, h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    launch_ham_edges(L.G, base_ptr(L, L.aux[X_HAM]), h->stream);
+    rc = after_launch(h);
+    if (rc) return rc;
+    SymArgs s{};
+    s.G = L.G;
+    s.nf = 2;
+    s.st[0] = base_ptr(L, L.aux[X_MOMR]); s.symr[0] = -1; s.symz[0] = +1;
+    s.st[1] = base_ptr(L, L.aux[X_MOMZ]); s.symr[1] = +1; s.symz[1] = -1;
+    launch_symmetry(s, h->stream);
+    return after_launch(h);
+}
+
+// Host restatement of initial.f90:59-218,528-645 for the supported data,
+// written straight into host arrays of every level (field slots of the
+// device layout), then uploaded.
+int initial_data(ollin_handle* h) {
+    const ollin_params& P = h->P;
+    const int g = h->g;
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        const size_t n = L.n;
+        std::vector<std::vector<double>> F(NFIELDS, std::vector<double>(n, 0.0));
+        auto at = [&](int i, int j) { return (size_t)(i - 1 + g) + (size_t)(j - 1 + g) * L.ld; };
+        for (int j = 1 - g; j <= L.nz; ++j)
+            for (int i = 1 - g; i <= L.nr; ++i) {
+                const size_t o = at(i, j);
+                const double r = L.rh[i - 1 + g], z = L.zh[j - 1 + g];
+                const double rr = std::sqrt(r * r + z * z);
+                double alpha = 1.0, psi = 1.0, phi = 0.0, chi = 1.0;
+                if (P.idata == OLLIN_IDATA_SCHWARZSCHILD || P.idata == OLLIN_IDATA_BRILLLINDQUIST) {
+                    const double M = P.bh1mass;
+                    psi = (P.idata == OLLIN_IDATA_SCHWARZSCHILD) ? 1.0 + 0.5 * M / std::fabs(rr)
+                                                                 : 1.0 + 0.5 * M / std::sqrt(r * r + (z - 0.0) * (z - 0.0));
+                    phi = std::log(psi);
+                    chi = 1.0 / std::pow(psi, (double)P.chipower);
+                    if (P.idata == OLLIN_IDATA_SCHWARZSCHILD && P.ilapse == OLLIN_ILAPSE_ISOTROPIC)
+                        alpha = (1.0 - 0.5 * M / std::fabs(rr)) / (1.0 + 0.5 * M / std::fabs(rr));
+                }
+                // factorhdet (initial.f90:528-577): the flat conformal metric has
+                // unit determinant, so phi gains log(1)/12 = 0 and psi = exp(phi)
+                if (P.factorhdet) {
+                    const double hdet = (1.0 * 1.0 - (r * 0.0) * (r * 0.0)) * 1.0;
+                    phi = phi + std::log(hdet) / 12.0;
+                    psi = std::exp(phi);
+                }
+                if (P.ilapse == OLLIN_ILAPSE_PSIMINUS2) alpha = 1.0 / (psi * psi);
+                else if (P.ilapse == OLLIN_ILAPSE_PSIMINUS4) alpha = 1.0 / ((psi * psi) * (psi * psi));
+                F[F_ALPHA][o] = alpha;
+                F[F_PHI][o] = phi;
+                F[F_CHI][o] = chi;
+                F[F_A][o] = 1.0; F[F_B][o] = 1.0; F[F_H][o] = 1.0; F[F_C][o] = 0.0;
+            }
+        for (int f : h->fields) {
+            CUDA_OR_FAIL(cudaMemcpyAsync(L.slot[L.cur][f], F[f].data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        }
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    }
+    return OLLIN_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+void ollin_params_default(ollin_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->nrtotal = 10; p->nztotal = 10; p->nl0 = 0; p->ghost = 0; p->eqsym = 0;
+    p->dr0 = 1.0; p->dz0 = 1.0; p->dtfac = 0.5;
+    p->integrator = OLLIN_INTEGRATOR_ICN; p->icniter = 3; p->order = 2;
+    p->slicing = OLLIN_SLICING_HARMONIC; p->gauge_f = 1.0;
+    p->shift = OLLIN_SHIFT_NONE; p->drivercsi = 0.75; p->drivereta = 0.0;
+    p->driveradv = 0; p->shiftadvect = 1;
+    p->chimethod = 1; p->chipower = 2;
+    p->evolveH = 1; p->evolveKTH = 0; p->nolambda = 1;
+    p->lagrangian = 1; p->factorhdet = 1;
+    p->eta = 2.0;
+    p->geodiss = (double)0.01f;     // real(8) :: geodiss = 0.01 (a default-real literal)
+    p->scalardiss = (double)0.01f;
+    p->boundtype = OLLIN_BOUND_RADIATIVE; p->interp_bicubic = 1;
+    p->mattertype = OLLIN_MATTER_VACUUM; p->scalarpotential = OLLIN_POTENTIAL_NONE;
+    p->idata = OLLIN_IDATA_MINKOWSKI; p->ilapse = OLLIN_ILAPSE_ONE; p->bh1mass = 1.0;
+}
+
+const char* ollin_gpu_last_error(void) { return g_err.c_str(); }
+
+int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
+    if (!p || !out) return fail(OLLIN_EINVAL, "null argument");
+    *out = nullptr;
+    int rc = check_params(*p);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(OLLIN_ECUDA, "no CUDA device is available");
+    auto* h = new ollin_handle();
+    h->P = *p;
+    h->g = 3;
+    h->nlev = p->nl0 + 1;
+    h->shift = p->shift == OLLIN_SHIFT_GAMMADRIVER2;
+    h->scalar = p->mattertype == OLLIN_MATTER_SCALAR;
+    h->phys = make_phys(*p);
+    parity_table(h);
+    for (int f : {F_ALPHA, F_CHI, F_PHI, F_A, F_B, F_H, F_C, F_TRK, F_KTA, F_KTB, F_KTC, F_DLR, F_DLZ}) h->fields.push_back(f);
+    if (h->shift)
+        for (int f : {F_BETAR, F_BETAZ, F_DTBETAR, F_DTBETAZ}) h->fields.push_back(f);
+    if (h->scalar)
+        for (int f : {F_SPHI, F_SXIR, F_SXIZ, F_SPI}) h->fields.push_back(f);
+    const int L = h->nlev;
+    h->t.assign(L, 0.0); h->t1.assign(L, 0.0); h->t2.assign(L, 0.0); h->s.assign(L, 0);
+    h->rminl.resize(L); h->rmaxl.resize(L); h->zminl.resize(L); h->zmaxl.resize(L);
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete h;
+        return fail(OLLIN_ECUDA, "cudaStreamCreate failed");
+    }
+    if (cudaMalloc(&h->d_flag, 64) != cudaSuccess || cudaMalloc(&h->d_norm, 8 * sizeof(double)) != cudaSuccess) {
+        ollin_gpu_destroy(h);
+        return fail(OLLIN_ENOMEM, "device allocation failed");
+    }
+    cudaMemsetAsync(h->d_flag, 0, 64, h->stream);
+    h->L.resize(L);
+    for (int l = 0; l < L; ++l) {
+        rc = alloc_level(h, h->L[l], l);
+        if (rc) {
+            ollin_gpu_destroy(h);
+            return rc;
+        }
+    }
+    *out = h;
+    return OLLIN_OK;
+}
+
+void ollin_gpu_destroy(ollin_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (DLevel& L : h->L)
+        if (L.pool) cudaFree(L.pool);
+    if (h->d_flag) cudaFree(h->d_flag);
+    if (h->d_norm) cudaFree(h->d_norm);
+    for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int ollin_gpu_num_levels(const ollin_handle* h) { return h ? h->nlev : 0; }
+
+int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out) {
+    if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad level");
+    const DLevel& L = h->L[level];
+    out->level = level; out->nr = L.nr; out->nz = L.nz; out->ghost = L.g;
+    out->dr = L.dr; out->dz = L.dz; out->dt = L.dt;
+    out->rmin = h->rminl[level]; out->rmax = h->rmaxl[level];
+    out->zmin = h->zminl[level]; out->zmax = h->zmaxl[level];
+    out->time = h->t[level];
+    out->steps = (int)h->s[level];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_upload(ollin_handle* h, int level, int field, const double* a, int ld_r) {
+    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    bool is_aux;
+    const int f = internal_field(field, &is_aux);
+    if (f < 0 || is_aux) return fail(OLLIN_EINVAL, "field cannot be uploaded (unknown or recomputed by auxiliary)");
+    if (!field_active(h, f)) return fail(OLLIN_EINVAL, "field is not evolved with these parameters");
+    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
+    CUDA_OR_FAIL(cudaMemcpy2DAsync(L.slot[L.cur][f], (size_t)L.ld * sizeof(double), a, (size_t)ld_r * sizeof(double),
+                                   (size_t)(L.nr + L.g) * sizeof(double), (size_t)(L.nz + L.g), cudaMemcpyHostToDevice, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r) {
+    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    bool is_aux;
+    const int f = internal_field(field, &is_aux);
+    if (f < 0) return fail(OLLIN_EINVAL, "unknown field");
+    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
+    const double* src = nullptr;
+    if (is_aux) {
+        if (f == X_HAM || f == X_MOMR || f == X_MOMZ || f == X_RSCAL || f == X_KT2 || f == X_LAPLA) {
+            int rc = analysis(h, level);
+            if (rc) return rc;
+        }
+        src = L.aux[f];
+    } else {
+        if (!field_active(h, f)) return fail(OLLIN_EINVAL, "field is not evolved with these parameters");
+        src = L.slot[L.cur][f];
+        if (f == F_PHI && !L.last_aux_t0) {
+            // after a t>0 ``auxiliary`` the reference holds phi = -log(chi)/2
+            // (auxiliary_geometry.f90:204)
+            launch_phi_from_chi(L.G, base_ptr(L, L.slot[L.cur][F_CHI]), base_ptr(L, L.aux[X_RSCAL]), h->stream);
+            int rc = after_launch(h);
+            if (rc) return rc;
+            src = L.aux[X_RSCAL];
+        }
+    }
+    CUDA_OR_FAIL(cudaMemcpy2DAsync(a, (size_t)ld_r * sizeof(double), src, (size_t)L.ld * sizeof(double),
+                                   (size_t)(L.nr + L.g) * sizeof(double), (size_t)(L.nz + L.g), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_initial_data(ollin_handle* h) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    const ollin_params& P = h->P;
+    if (P.idata != OLLIN_IDATA_MINKOWSKI && P.idata != OLLIN_IDATA_SCHWARZSCHILD && P.idata != OLLIN_IDATA_BRILLLINDQUIST)
+        return fail(OLLIN_EINVAL, "idata not supported by the host initial-data routine");
+    // scalar-field slots start at zero; a scalar pulse needs the elliptic
+    // solve of idata_scalarpulse.f90 and is uploaded by the caller
+    return initial_data(h);
+}
+
+int ollin_gpu_initialize(ollin_handle* h) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    for (int l = 0; l < h->nlev; ++l) {  // evolve.f90:128-142
+        int rc = do_symmetry(h, h->L[l], h->L[l].cur, active_fields(h, true));
+        if (rc) return rc;
+    }
+    for (int l = 0; l < h->nlev; ++l) {  // evolve.f90:162-167
+        int rc = do_aux(h, h->L[l], h->L[l].cur, h->t[l] == 0.0);
+        if (rc) return rc;
+    }
+    if (h->shift) {  // evolve.f90:174-195
+        for (int l = 0; l < h->nlev; ++l) {
+            DLevel& L = h->L[l];
+            launch_gammadriver_init(L.G, base_ptr(L, L.slot[L.cur][F_DTBETAR]), base_ptr(L, L.slot[L.cur][F_DTBETAZ]),
+                                    base_ptr(L, L.slot[L.cur][F_DLR]), base_ptr(L, L.slot[L.cur][F_DLZ]), h->P.drivercsi, h->stream);
+            int rc = after_launch(h);
+            if (rc) return rc;
+        }
+    }
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    h->initialized = true;
+    return OLLIN_OK;
+}
+
+int ollin_gpu_aux(ollin_handle* h, int level) {
+    if (!h || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle or level");
+    DLevel& L = h->L[level];
+    int rc = do_aux(h, L, L.cur, h->t[level] == 0.0);
+    if (rc) return rc;
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
+    int rc = onestep(h, 0);
+    if (rc) return rc;
+    unsigned int flag = 0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    if (flag) return fail(OLLIN_ENAN, "non-finite value produced by the evolution");
+    if (t_out) *t_out = h->t[0];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
+    if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    bool is_aux;
+    const int f = internal_field(field, &is_aux);
+    if (f < 0) return fail(OLLIN_EINVAL, "unknown field");
+    const double* src;
+    if (is_aux) {
+        if (f == X_HAM || f == X_MOMR || f == X_MOMZ || f == X_RSCAL || f == X_KT2 || f == X_LAPLA) {
+            int rc = analysis(h, level);
+            if (rc) return rc;
+        }
+        src = base_ptr(L, L.aux[f]);
+    } else {
+        if (!field_active(h, f)) return fail(OLLIN_EINVAL, "field is not evolved with these parameters");
+        src = base_ptr(L, L.slot[L.cur][f]);
+        if (f == F_PHI && !L.last_aux_t0) {
+            launch_phi_from_chi(L.G, base_ptr(L, L.slot[L.cur][F_CHI]), base_ptr(L, L.aux[X_RSCAL]), h->stream);
+            int rc = after_launch(h);
+            if (rc) return rc;
+            src = base_ptr(L, L.aux[X_RSCAL]);
+        }
+    }
+    launch_norms(L.G, src, h->P.interp_bicubic, h->rminl[level], h->zminl[level], h->rmaxl[level], h->zmaxl[level],
+                 h->d_norm, h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    double res[6];
+    CUDA_OR_FAIL(cudaMemcpyAsync(res, h->d_norm, sizeof(res), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    if (res[5] != 0.0) return fail(OLLIN_ENAN, "NaN found in the field (save0Ddata.f90:229-264)");
+    for (int k = 0; k < 5; ++k) out[k] = res[k];
+    return OLLIN_OK;
+}
+
+double ollin_gpu_point_updates(const ollin_handle* h) { return h ? h->point_updates : 0.0; }
+
+double ollin_gpu_fp64_rate(void) { return measure_fp64_dfma_rate(0); }
+
+int ollin_gpu_kernel_timing(ollin_handle* h, int enable) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    h->ktime = enable != 0;
+    h->ev_used = 0;
+    h->rhs_point_stages = 0;
+    h->rhs_launches = 0;
+    return OLLIN_OK;
+}
+
+int ollin_gpu_kernel_stats(ollin_handle* h, double* rhs_ms, long long* launches, double* point_stages) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    double tot = 0;
+    for (size_t k = 0; k + 1 < h->ev_used; k += 2) {
+        float ms = 0;
+        CUDA_OR_FAIL(cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]));
+        tot += ms;
+    }
+    if (rhs_ms) *rhs_ms = tot;
+    if (launches) *launches = h->rhs_launches;
+    if (point_stages) *point_stages = h->rhs_point_stages;
+    return OLLIN_OK;
+}
+
+void* ollin_gpu_stream(const ollin_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+long long ollin_gpu_launch_count(const ollin_handle* h) { return h ? h->launches : 0; }
+
+}  // extern "C"

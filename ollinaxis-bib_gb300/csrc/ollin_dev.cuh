@@ -1,0 +1,171 @@
+// Device-side data layout and stencil primitives of the GB300 evolution
+// library for the OllinAxis-BiB time-evolution path.
+//
+// Layout in HBM: every grid function of a level is one FP64 array of
+// (Nr+ghost) x (Nz+ghost) points, column-major with r fastest (the
+// reference's (1-ghost:Nr, 1-ghost:Nz) arrays, generated allocatearrays.f90),
+// with the leading dimension padded to a multiple of 32 doubles so that each
+// z-row starts on a 256-byte boundary.  Kernels address element (i,j) through
+// a base pointer pre-offset so that f(i,j) = base[i + j*ld].
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ollin {
+
+constexpr int kMaxLevels = 12;
+
+// Evolved fields kept on the device (a subset of the reference's EVOLVE
+// arrays: the ones with non-zero sources in the supported formulation; the
+// others are constant or recomputed by ``auxiliary`` and are reconstructed on
+// download).
+enum Field : int {
+    F_ALPHA = 0, F_CHI, F_PHI, F_A, F_B, F_H, F_C,
+    F_TRK, F_KTA, F_KTB, F_KTC, F_DLR, F_DLZ,
+    F_BETAR, F_BETAZ, F_DTBETAR, F_DTBETAZ,
+    F_SPHI, F_SXIR, F_SXIZ, F_SPI,
+    NFIELDS
+};
+
+// Auxiliary point quantities written by the aux kernels and read by the
+// right-hand side (names of the reference's auxiliary arrays).
+enum AuxField : int {
+    X_GA = 0, X_GB, X_GH, X_GC,    // g_A, g_B, g_H, g_C (inverse conformal metric)
+    X_KTH, X_LAM, X_ALAM, X_GLAM,  // KTH, lambda, Alambda, g_lambda
+    X_DELDEFR, X_DELDEFZ,          // DelDef_r, DelDef_z
+    X_GDR, X_GDZ,                  // Dr_g_A + r Dz_g_C, Dz_g_B + r Dr_g_C (scalar-field source)
+    // derived output arrays (analysis)
+    X_HAM, X_MOMR, X_MOMZ, X_RSCAL, X_KT2, X_LAPLA,
+    NAUX
+};
+
+// Geometry of one level as seen by a kernel.
+struct LevelGeom {
+    int nr, nz, g, ld;   // Nr, Nz, ghost, leading dimension
+    int jlo;             // first z-row with a source: 1 (eqsym) or 1-g
+    int eqsym;
+    double dr, dz, dt;
+    double idr, idz;     // 1/dr, 1/dz
+    const double* rcol;  // r(i) for i = 1-g..nr   (indexed rcol[i])
+    const double* ircol; // 1/r(i)
+    const double* zrow;  // z(j) for j = 1-g..nz   (indexed zrow[j])
+};
+
+__host__ __device__ inline size_t off(const LevelGeom& G, int i, int j) { return (size_t)i + (size_t)j * G.ld; }
+
+// ---------------------------------------------------------------------------
+// one-dimensional stencils of the reference (src/base/derivatives.f90,
+// order four).  ``f`` is the base pointer (f(i,j) = f[i + j*ld]); ``s`` the
+// stride between consecutive points along the direction; ``k`` the position
+// class: 0 interior, 1 second-to-last, 2 last point (upper edge), -1 second
+// point, -2 first point (lower edge, used only without equatorial symmetry).
+// ``c`` is 1/(12 h) for first and 1/(12 h^2) for second derivatives.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double ld_(const double* p) { return __ldg(p); }
+
+__device__ __forceinline__ double d1(const double* f, long s, int k, double c) {
+    if (k == 0) {
+        return c * (8.0 * (ld_(f + s) - ld_(f - s)) - (ld_(f + 2 * s) - ld_(f - 2 * s)));
+    } else if (k == 1) {
+        return c * (3.0 * ld_(f + s) + 10.0 * ld_(f) - 18.0 * ld_(f - s) + 6.0 * ld_(f - 2 * s) - ld_(f - 3 * s));
+    } else if (k == 2) {
+        return c * (25.0 * ld_(f) - 48.0 * ld_(f - s) + 36.0 * ld_(f - 2 * s) - 16.0 * ld_(f - 3 * s) + 3.0 * ld_(f - 4 * s));
+    } else if (k == -1) {
+        return -c * (3.0 * ld_(f - s) + 10.0 * ld_(f) - 18.0 * ld_(f + s) + 6.0 * ld_(f + 2 * s) - ld_(f + 3 * s));
+    } else {
+        return -c * (25.0 * ld_(f) - 48.0 * ld_(f + s) + 36.0 * ld_(f + 2 * s) - 16.0 * ld_(f + 3 * s) + 3.0 * ld_(f + 4 * s));
+    }
+}
+
+__device__ __forceinline__ double d2(const double* f, long s, int k, double c) {
+    if (k == 0) {
+        return -c * (30.0 * ld_(f) - 16.0 * (ld_(f + s) + ld_(f - s)) + ld_(f + 2 * s) + ld_(f - 2 * s));
+    } else if (k == 1) {
+        return c * (10.0 * ld_(f + s) - 15.0 * ld_(f) - 4.0 * ld_(f - s) + 14.0 * ld_(f - 2 * s) - 6.0 * ld_(f - 3 * s) + ld_(f - 4 * s));
+    } else if (k == 2) {
+        return c * (45.0 * ld_(f) - 154.0 * ld_(f - s) + 214.0 * ld_(f - 2 * s) - 156.0 * ld_(f - 3 * s) + 61.0 * ld_(f - 4 * s) - 10.0 * ld_(f - 5 * s));
+    } else if (k == -1) {
+        return c * (10.0 * ld_(f - s) - 15.0 * ld_(f) - 4.0 * ld_(f + s) + 14.0 * ld_(f + 2 * s) - 6.0 * ld_(f + 3 * s) + ld_(f + 4 * s));
+    } else {
+        return c * (45.0 * ld_(f) - 154.0 * ld_(f + s) + 214.0 * ld_(f + 2 * s) - 156.0 * ld_(f + 3 * s) + 61.0 * ld_(f + 4 * s) - 10.0 * ld_(f + 5 * s));
+    }
+}
+
+// Position class along one direction for first/second derivatives.
+__device__ __forceinline__ int pclass(int i, int n, int g) {
+    if (i <= n - 2) return (i >= 3 - g) ? 0 : (i == 2 - g ? -1 : -2);
+    return (i == n - 1) ? 1 : 2;
+}
+
+// Mixed derivative d^2/(dr dz) with the reference's edge and corner rules
+// (derivatives.f90:615-700): 4th order inside, 2nd order on the two outermost
+// rows/columns, one-sided on the last one, and the z-edge rule overriding the
+// r-edge rule where both apply.
+__device__ __forceinline__ double d2rz(const double* f, long ld, int i, int j, int nr, int nz, int g, double idrz) {
+    const bool ri = (i >= 3 - g && i <= nr - 2), zi = (j >= 3 - g && j <= nz - 2);
+#define F_(a, b) ld_(f + (a) + (long)(b) * ld)
+    if (ri && zi) {
+        return idrz * ((F_(1, 1) + F_(-1, -1) - F_(1, -1) - F_(-1, 1)) * (1.0 / 3.0)
+                       - (F_(2, 2) + F_(-2, -2) - F_(2, -2) - F_(-2, 2)) * (1.0 / 48.0));
+    }
+    const bool zedge_loop = (i >= 2 - g && i <= nr - 1);  // z-boundary loop range
+    const bool redge_loop = (j >= 2 - g && j <= nz - 1);  // r-boundary loop range
+    if (zedge_loop && !zi) {
+        if (j == 2 - g || j == nz - 1)
+            return 0.25 * idrz * (F_(1, 1) + F_(-1, -1) - F_(-1, 1) - F_(1, -1));
+        if (j == nz)
+            return 0.25 * idrz * ((3.0 * F_(1, 0) - 4.0 * F_(1, -1) + F_(1, -2)) - (3.0 * F_(-1, 0) - 4.0 * F_(-1, -1) + F_(-1, -2)));
+        // j == 1-g
+        return -0.25 * idrz * ((3.0 * F_(1, 0) - 4.0 * F_(1, 1) + F_(1, 2)) - (3.0 * F_(-1, 0) - 4.0 * F_(-1, 1) + F_(-1, 2)));
+    }
+    if (redge_loop && !ri) {
+        if (i == 2 - g || i == nr - 1)
+            return 0.25 * idrz * (F_(1, 1) + F_(-1, -1) - F_(1, -1) - F_(-1, 1));
+        if (i == nr)
+            return 0.25 * idrz * ((3.0 * F_(0, 1) - 4.0 * F_(-1, 1) + F_(-2, 1)) - (3.0 * F_(0, -1) - 4.0 * F_(-1, -1) + F_(-2, -1)));
+        return -0.25 * idrz * ((3.0 * F_(0, 1) - 4.0 * F_(1, 1) + F_(2, 1)) - (3.0 * F_(0, -1) - 4.0 * F_(1, -1) + F_(2, -1)));
+    }
+    // corners
+    if (i == nr && j == nz)
+        return 0.25 * idrz * (9.0 * F_(0, 0) + 16.0 * F_(-1, -1) + F_(-2, -2) - 12.0 * (F_(0, -1) + F_(-1, 0))
+                              + 3.0 * (F_(0, -2) + F_(-2, 0)) - 4.0 * (F_(-1, -2) + F_(-2, -1)));
+    if (i == nr)  // j == 1-g
+        return -0.25 * idrz * (9.0 * F_(0, 0) + 16.0 * F_(-1, 1) + F_(-2, 2) - 12.0 * (F_(0, 1) + F_(-1, 0))
+                               + 3.0 * (F_(0, 2) + F_(-2, 0)) - 4.0 * (F_(-1, 2) + F_(-2, 1)));
+    if (j == nz)  // i == 1-g
+        return -0.25 * idrz * (9.0 * F_(0, 0) + 16.0 * F_(1, -1) + F_(2, -2) - 12.0 * (F_(1, 0) + F_(0, -1))
+                               + 3.0 * (F_(2, 0) + F_(0, -2)) - 4.0 * (F_(2, -1) + F_(1, -2)));
+    return 0.25 * idrz * (9.0 * F_(0, 0) + 16.0 * F_(1, 1) + F_(2, 2) - 12.0 * (F_(0, 1) + F_(1, 0))
+                          + 3.0 * (F_(0, 2) + F_(2, 0)) - 4.0 * (F_(1, 2) + F_(2, 1)));
+#undef F_
+}
+
+// Lopsided advective derivative (src/base/derivadvect.f90, order four).
+// ``neg`` is (beta <= 0) at the point; ``k`` the upper-edge class counted as
+// in diffadvr/diffadvz: 0 interior (i <= n-3), 3 second point of the
+// interior range (i = 3-ghost), 10 = n-2, 11 = n-1, 12 = n.
+__device__ __forceinline__ double dadv(const double* f, long s, int i, int n, int g, bool neg, double ih, bool zdir) {
+    const double q = 0.25 * ih;
+    auto left = [&]() { return +q * (3.0 * ld_(f + s) + 10.0 * ld_(f) - 18.0 * ld_(f - s) + 6.0 * ld_(f - 2 * s) - ld_(f - 3 * s)) * (1.0 / 3.0); };
+    auto right = [&]() { return -q * (3.0 * ld_(f - s) + 10.0 * ld_(f) - 18.0 * ld_(f + s) + 6.0 * ld_(f + 2 * s) - ld_(f + 3 * s)) * (1.0 / 3.0); };
+    auto cent = [&]() { return q * (8.0 * (ld_(f + s) - ld_(f - s)) - (ld_(f + 2 * s) - ld_(f - 2 * s))) * (1.0 / 3.0); };
+    if (i >= 4 - g && i <= n - 3) return neg ? left() : right();
+    if (i == n - 2) return neg ? left() : cent();
+    if (i == n - 1) return left();
+    if (i == n) return q * (25.0 * ld_(f) - 48.0 * ld_(f - s) + 36.0 * ld_(f - 2 * s) - 16.0 * ld_(f - 3 * s) + 3.0 * ld_(f - 4 * s)) * (1.0 / 3.0);
+    if (i == 3 - g) {
+        // the r and z lopsided routines treat this point with opposite branches
+        if (!zdir) return neg ? cent() : right();
+        return neg ? right() : cent();
+    }
+    if (i == 2 - g) return right();
+    return -q * (25.0 * ld_(f) - 48.0 * ld_(f + s) + 36.0 * ld_(f + 2 * s) - 16.0 * ld_(f + 3 * s) + 3.0 * ld_(f + 4 * s)) * (1.0 / 3.0);
+}
+
+// Kreiss-Oliger sixth difference along one direction, the bracket of
+// src/base/dissipation.f90:196-211 (without the -eps/dt/20 factor).
+__device__ __forceinline__ double ko6(const double* f, long s) {
+    return 20.0 * ld_(f) - 15.0 * (ld_(f + s) + ld_(f - s)) + 6.0 * (ld_(f + 2 * s) + ld_(f - 2 * s)) - (ld_(f + 3 * s) + ld_(f - 3 * s));
+}
+
+}  // namespace ollin

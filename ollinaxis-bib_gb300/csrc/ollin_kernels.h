@@ -1,0 +1,104 @@
+// Launch interfaces between the host scheduler (host.cpp) and the CUDA
+// kernels (rhs.cu, aux.cu, transfer.cu).  All arguments are passed by value;
+// pointers are device pointers pre-offset so that f(i,j) = f[i + j*ld].
+#pragma once
+#include "ollin_dev.cuh"
+
+namespace ollin {
+
+// Scalar parameters the right-hand side reads (src/base/param.f90 values).
+struct PhysParams {
+    int slicing;          // OLLIN_SLICING_*
+    double gauge_f;
+    int shift;            // 1 = Gammadriver2 active
+    int shiftadvect, driveradv;
+    double drivercsi, drivereta;
+    double eta;           // Delta damping (momentum-constraint multiple)
+    double geodiss, scalardiss;
+    double ft[8];
+    int scalar;           // real scalar field present
+    int potential;        // OLLIN_POTENTIAL_*
+    double scalar_mass, scalar_lambda;
+    int boundtype;        // OLLIN_BOUND_*
+};
+
+// One RK/ICN stage of one level.
+struct StageArgs {
+    LevelGeom G;
+    PhysParams P;
+    const double* in[NFIELDS];   // stage input state
+    const double* pst[NFIELDS];  // state at the start of the step (var_p)
+    double* out[NFIELDS];        // stage output state
+    double* acc[NFIELDS];        // RK4 accumulator (var_a)
+    const double* aux[NAUX];     // auxiliary quantities of the stage input
+    double* auxw[NAUX];          // writable aux (analysis outputs)
+    int t0;                      // level time == 0 (first step of the level)
+    int level0;                  // level 0 (outer radiative boundary applies)
+    int rk4, iter, niter;
+    double dtw, weight;
+    int analysis;                // 1: write ham/mom/RSCAL/KT2/Lapla_alpha instead of updating
+    unsigned int* nanflag;       // set to 1 if a non-finite source is produced
+};
+
+// Pointwise auxiliary quantities (auxiliary_geometry.f90 pointwise parts).
+struct AuxArgs {
+    LevelGeom G;
+    double* st[NFIELDS];         // state (modified in place: factordet, chi at t=0)
+    double* aux[NAUX];
+    int t0;
+    int scalar;
+};
+
+// Parity ghost fill of the evolved fields (generated symmetries_r/_z).
+struct SymArgs {
+    LevelGeom G;
+    double* st[NFIELDS];
+    int symr[NFIELDS], symz[NFIELDS];
+    int nf;                      // number of fields to fill (first nf slots used)
+    int fid[NFIELDS];            // which field slot each entry refers to
+};
+
+// Coarse -> fine boundary prolongation (finebound.f90 + bound_interp.inc).
+struct ProlongArgs {
+    LevelGeom F;                 // fine level
+    LevelGeom Cg;                // coarse level
+    double* fout[NFIELDS];       // fine stage output (written on the strips)
+    const double* fp[NFIELDS];   // fine var_p (border 1) and history level 0
+    const double* fpp[NFIELDS];  // fine history level 1 (previous step start)
+    const double* cin[NFIELDS];  // coarse current state
+    int fid[NFIELDS];
+    int nf;
+    double rminl_f, rmaxl_f, zminl_f, zmaxl_f;
+    double rminl_c, rmaxl_c, zminl_c, zmaxl_c;
+    double tp, t0, tm1, tl;
+    int imax, border, bicubic;
+};
+
+// Fine -> coarse restriction (restrict.f90 + restrict_interp.inc).
+struct RestrictArgs {
+    LevelGeom F, Cg;
+    const double* fin[NFIELDS];
+    double* cout[NFIELDS];
+    int fid[NFIELDS];
+    int nf;
+    double rminl_f, rmaxl_f, zminl_f, zmaxl_f;
+    double rminl_c, zminl_c;
+    int eqsym, bicubic;
+};
+
+void launch_rhs(const StageArgs& a, cudaStream_t s);
+void launch_aux_point(const AuxArgs& a, cudaStream_t s);
+void launch_aux_deriv(const AuxArgs& a, cudaStream_t s);
+void launch_symmetry(const SymArgs& a, cudaStream_t s);
+void launch_prolong(const ProlongArgs& a, cudaStream_t s);
+void launch_restrict(const RestrictArgs& a, cudaStream_t s);
+void launch_norms(const LevelGeom& G, const double* f, int origin_bicubic, double rminl, double zminl,
+                  double rmaxl, double zmaxl, double* dev_out, cudaStream_t s);
+void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s);
+void launch_gammadriver_init(const LevelGeom& G, double* dtbr, double* dtbz, const double* dlr,
+                             const double* dlz, double csi, cudaStream_t s);
+// DFMA instructions per second of this GPU (all SMs, independent chains).
+double measure_fp64_dfma_rate(cudaStream_t s);
+void launch_phi_from_chi(const LevelGeom& G, const double* chi, double* out, cudaStream_t s);
+
+}  // namespace ollin

@@ -1,0 +1,348 @@
+// Ghost fills, mesh-refinement transfer and reductions.
+//
+//  * parity ghost fill on the axis and the equator (generated
+//    symmetries_r.f90 / symmetries_z.f90, tags from src/base/arrays.config);
+//  * coarse -> fine boundary prolongation: bicubic Lagrange interpolation in
+//    space (src/base/interp.f90:146-263) times linear/quadratic Lagrange
+//    interpolation in time against the fine level's own history
+//    (src/base/finebound.f90:91-316 with bound_interp.inc);
+//  * fine -> coarse restriction at coarse points well inside the fine box
+//    (src/base/restrict.f90:70-123 with restrict_interp.inc);
+//  * the 0-D statistics of save0Ddata.f90:221-288 as a deterministic
+//    fixed-order block reduction.
+// The transfer arithmetic uses explicitly rounded operations (no FMA
+// contraction) so that it reproduces the reference's sequence of roundings.
+#include "ollin_kernels.h"
+
+namespace ollin {
+
+namespace {
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+
+// ---- parity ghost fill -------------------------------------------------
+__global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
+    const LevelGeom& G = a.G;
+    const int g = G.g;
+    // thread space: all points (i,j) with i <= 0 or (eqsym and j <= 0)
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const bool gi = i <= 0, gj = G.eqsym && j <= 0;
+    if (!gi && !gj) return;
+    const int si = gi ? 1 - i : i, sj = gj ? 1 - j : j;
+    const size_t o = (size_t)i + (size_t)j * G.ld, os = (size_t)si + (size_t)sj * G.ld;
+    for (int k = 0; k < a.nf; ++k) {
+        double* f = a.st[k];
+        double v = f[os];
+        if (gi && a.symr[k] < 0) v = -v;
+        if (gj && a.symz[k] < 0) v = -v;
+        f[o] = v;
+    }
+}
+
+// ---- interp.f90 on the device ---------------------------------------------
+struct InterpPt {
+    int i0, j0, mode;   // mode 0: copy node, 1: bilinear, 2: bicubic
+    double w[4][4];
+};
+
+__device__ void interp_weights(const LevelGeom& G, double rminl, double rmaxl, double zminl, double zmaxl,
+                               double r0, double z0, int bicubic, InterpPt& p) {
+    const int g = G.g;
+    const double dr = G.dr, dz = G.dz;
+    const double r1 = G.rcol[1 - g], z1 = G.zrow[1 - g];
+    p.i0 = (int)((r0 - r1) / dr) + 1 - g;
+    const double deltar = r0 - G.rcol[p.i0];
+    p.j0 = (int)((z0 - z1) / dz) + 1 - g;
+    const double deltaz = z0 - G.zrow[p.j0];
+    if (deltar == 0.0 && deltaz == 0.0) { p.mode = 0; return; }
+    const bool forcelinear = ((rmaxl - r0) < dr) || ((zmaxl - z0) < dz) || ((r0 - rminl) < dr) || ((z0 - zminl) < dz);
+    const double auxr = deltar / dr, auxz = deltaz / dz;
+    if (!bicubic || forcelinear) {
+        // factors kept separate: the reference multiplies left to right,
+        // fa(0,0)*(1-auxr)*(1-auxz) + fa(1,0)*auxr*(1-auxz) + ...
+        p.mode = 1;
+        p.w[0][0] = auxr;
+        p.w[0][1] = auxz;
+        return;
+    }
+    p.mode = 2;
+    for (int ii = -1; ii <= 2; ++ii)
+        for (int jj = -1; jj <= 2; ++jj) {
+            double aux = 1.0;
+            for (int m = -1; m <= 2; ++m) {
+                if (m == ii) continue;
+                aux = mul(aux, sub(auxr, (double)m)) / (double)(ii - m);
+            }
+            for (int n = -1; n <= 2; ++n) {
+                if (n == jj) continue;
+                aux = mul(aux, sub(auxz, (double)n)) / (double)(jj - n);
+            }
+            p.w[ii + 1][jj + 1] = aux;
+        }
+}
+
+__device__ double interp_apply(const LevelGeom& G, const double* f, const InterpPt& p) {
+    const long ld = G.ld;
+    if (p.mode == 0) return f[p.i0 + (long)p.j0 * ld];
+    if (p.mode == 1) {
+        // fa(0,0)*(1-auxr)*(1-auxz) + fa(1,0)*auxr*(1-auxz) + fa(0,1)*(1-auxr)*auxz + fa(1,1)*auxr*auxz
+        const double* b = f + p.i0 + (long)p.j0 * ld;
+        const double ar = p.w[0][0], az = p.w[0][1];
+        double v = mul(mul(b[0], sub(1.0, ar)), sub(1.0, az));
+        v = add(v, mul(mul(b[1], ar), sub(1.0, az)));
+        v = add(v, mul(mul(b[ld], sub(1.0, ar)), az));
+        v = add(v, mul(mul(b[1 + ld], ar), az));
+        return v;
+    }
+    double v = 0.0;
+    for (int ii = -1; ii <= 2; ++ii)
+        for (int jj = -1; jj <= 2; ++jj)
+            v = add(v, mul(p.w[ii + 1][jj + 1], f[(p.i0 + ii) + (long)(p.j0 + jj) * ld]));
+    return v;
+}
+
+// ---- prolongation ----------------------------------------------------------
+// Thread space: the upper-r strip (imax+1) x (Nz+g) followed by the upper-z
+// strip (jmax+1) x (Nr+g); corner points are written by both strips with the
+// same value, as in the reference.
+__global__ void __launch_bounds__(128) prolong_kernel(const __grid_constant__ ProlongArgs a) {
+    const LevelGeom& F = a.F;
+    const int g = F.g;
+    const int nstrip_r = (a.imax + 1) * (F.nz + g);
+    const int nstrip_z = (a.imax + 1) * (F.nr + g);
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= nstrip_r + nstrip_z) return;
+    double r0, z0;
+    if (t < nstrip_r) {
+        const int m = t / (F.nz + g), n = t % (F.nz + g);
+        r0 = sub(a.rmaxl_f, mul((double)m, F.dr));
+        z0 = add(a.zminl_f, mul((double)n, F.dz));
+    } else {
+        const int q = t - nstrip_r;
+        const int n = q / (F.nr + g), m = q % (F.nr + g);
+        r0 = add(a.rminl_f, mul((double)m, F.dr));
+        z0 = sub(a.zmaxl_f, mul((double)n, F.dz));
+    }
+    const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
+    const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
+    if (!(i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz)) return;
+    InterpPt p;
+    interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
+    const size_t o = (size_t)i + (size_t)j * F.ld;
+    const double tp = a.tp, t0 = a.t0, tm1 = a.tm1, tl = a.tl;
+    for (int k = 0; k < a.nf; ++k) {
+        const int f = a.fid[k];
+        const double aux2 = interp_apply(a.Cg, a.cin[f], p);
+        double v;
+        if (tp == tl) {
+            v = aux2;  // the history weights vanish exactly
+        } else if (a.border == 1) {
+            v = add(mul((tl - t0) / (tp - t0), aux2), mul((tl - tp) / (t0 - tp), a.fp[f][o]));
+        } else {
+            const double w0 = ((tl - t0) * (tl - tm1)) / ((tp - t0) * (tp - tm1));
+            const double w1 = ((tl - tp) * (tl - tm1)) / ((t0 - tp) * (t0 - tm1));
+            const double w2 = ((tl - tp) * (tl - t0)) / ((tm1 - tp) * (tm1 - t0));
+            v = add(add(mul(w0, aux2), mul(w1, a.fp[f][o])), mul(w2, a.fpp[f][o]));
+        }
+        a.fout[f][o] = v;
+    }
+}
+
+// ---- restriction -----------------------------------------------------------
+__global__ void __launch_bounds__(128) restrict_kernel(const __grid_constant__ RestrictArgs a) {
+    const LevelGeom& C = a.Cg;
+    const LevelGeom& F = a.F;
+    const int g = C.g;
+    const int m = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int n = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (m > C.nr + g - 1 || n > C.nz + g - 1) return;
+    const double r0 = add(a.rminl_c, mul((double)m, C.dr));
+    const double z0 = add(a.zminl_c, mul((double)n, C.dz));
+    const double deltar = add(mul((double)(2 * g), F.dr), 1.0e-10);
+    const double deltaz = add(mul((double)(2 * g), F.dz), 1.0e-10);
+    const double rmin = (a.rminl_f < 0.0) ? 0.0 : a.rminl_f + deltar;
+    const double zmin = (a.eqsym && a.zminl_f < 0.0) ? 0.0 : a.zminl_f + deltaz;
+    const double rmax = a.rmaxl_f - deltar, zmax = a.zmaxl_f - deltaz;
+    if (!(r0 > rmin && r0 < rmax && z0 > zmin && z0 < zmax)) return;
+    const int i = (int)round((r0 - C.rcol[1 - g]) / C.dr) + 1 - g;
+    const int j = (int)round((z0 - C.zrow[1 - g]) / C.dz) + 1 - g;
+    if (!(i >= 1 - g && i <= C.nr && j >= 1 - g && j <= C.nz)) return;
+    InterpPt p;
+    interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p);
+    const size_t o = (size_t)i + (size_t)j * C.ld;
+    for (int k = 0; k < a.nf; ++k) {
+        const int f = a.fid[k];
+        a.cout[f][o] = interp_apply(F, a.fin[f], p);
+    }
+}
+
+// ---- 0-D statistics (save0Ddata.f90:221-288, origin value :370-374) --------
+// One block; each thread walks the points in a fixed order and the partial
+// results are combined in a fixed tree, so the result does not depend on
+// scheduling.
+__global__ void __launch_bounds__(512) norms_kernel(LevelGeom G, const double* f, int bicubic,
+                                                    double rminl, double zminl, double rmaxl, double zmaxl,
+                                                    double* out) {
+    __shared__ double smax[512], smin[512], snm1[512], snm2[512];
+    __shared__ int snan[512];
+    const int ni = G.nr - G.g, nj = G.nz - G.g;
+    const long npts = (long)ni * nj;
+    double vmax = -1.0e10, vmin = 1.0e10, nm1 = 0.0, nm2 = 0.0;
+    int nan = 0;
+    for (long q = threadIdx.x; q < npts; q += blockDim.x) {
+        const int i = 1 + (int)(q % ni), j = 1 + (int)(q / ni);
+        const double v = f[(size_t)i + (size_t)j * G.ld];
+        if (v != v) nan = 1;
+        vmax = fmax(vmax, v);
+        vmin = fmin(vmin, v);
+        nm1 = fmax(nm1, fabs(v));
+        nm2 = nm2 + v * v;
+    }
+    smax[threadIdx.x] = vmax; smin[threadIdx.x] = vmin; snm1[threadIdx.x] = nm1; snm2[threadIdx.x] = nm2;
+    snan[threadIdx.x] = nan;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
+            snm1[threadIdx.x] = fmax(snm1[threadIdx.x], snm1[threadIdx.x + w]);
+            snm2[threadIdx.x] = snm2[threadIdx.x] + snm2[threadIdx.x + w];
+            snan[threadIdx.x] |= snan[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = smax[0];
+        out[1] = smin[0];
+        out[2] = snm1[0];
+        out[3] = sqrt(snm2[0] / (double)npts);
+        InterpPt p;
+        interp_weights(G, rminl, rmaxl, zminl, zmaxl, 0.0, 0.0, bicubic, p);
+        out[4] = interp_apply(G, f, p);
+        out[5] = snan[0] ? 1.0 : 0.0;
+    }
+}
+
+// constraints.f90:63-93: copy the next-to-edge value onto every outer edge,
+// then the axis/equator parity fill (even).  One thread per edge row/column.
+__global__ void ham_edges_kernel(LevelGeom G, double* h) {
+    const int g = G.g;
+    const long ld = G.ld;
+    auto H = [&](int i, int j) -> double& { return h[(size_t)i + (size_t)j * ld]; };
+    // four sequential edge copies in the reference order
+    for (int j = 1 - g + (int)threadIdx.x; j <= G.nz; j += blockDim.x) H(1 - g, j) = H(2 - g, j);
+    __syncthreads();
+    for (int j = 1 - g + (int)threadIdx.x; j <= G.nz; j += blockDim.x) H(G.nr, j) = H(G.nr - 1, j);
+    __syncthreads();
+    for (int i = 1 - g + (int)threadIdx.x; i <= G.nr; i += blockDim.x) H(i, 1 - g) = H(i, 2 - g);
+    __syncthreads();
+    for (int i = 1 - g + (int)threadIdx.x; i <= G.nr; i += blockDim.x) H(i, G.nz) = H(i, G.nz - 1);
+    __syncthreads();
+    for (int j = 1 - g + (int)threadIdx.x; j <= G.nz; j += blockDim.x)
+        for (int ii = 1; ii <= g; ++ii) H(1 - ii, j) = H(ii, j);
+    __syncthreads();
+    if (G.eqsym)
+        for (int i = 1 - g + (int)threadIdx.x; i <= G.nr; i += blockDim.x)
+            for (int jj = 1; jj <= g; ++jj) H(i, 1 - jj) = H(i, jj);
+}
+
+__global__ void gammadriver_init_kernel(LevelGeom G, double* dtbr, double* dtbz, const double* dlr, const double* dlz, double csi) {
+    const int i = 1 - G.g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - G.g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    dtbr[o] = csi * dlr[o];
+    dtbz[o] = csi * dlz[o];
+}
+
+__global__ void phi_from_chi_kernel(LevelGeom G, const double* chi, double* out) {
+    const int i = 1 - G.g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - G.g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    out[o] = -log(chi[o]) / 2.0;
+}
+
+// FP64 issue-rate probe: eight independent DFMA chains per thread.
+__global__ void fp64_probe_kernel(double* out, int iters, double seed) {
+    const int gid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    double a0 = seed + gid * 1e-9, a1 = a0 + 0.1, a2 = a0 + 0.2, a3 = a0 + 0.3;
+    double a4 = a0 + 0.4, a5 = a0 + 0.5, a6 = a0 + 0.6, a7 = a0 + 0.7;
+    const double m = 0.999999, c = 1e-7;
+    for (int k = 0; k < iters; ++k) {
+        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+    out[gid] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+dim3 full_grid(const LevelGeom& G, dim3 blk) {
+    return dim3((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+}
+
+}  // namespace
+
+void launch_symmetry(const SymArgs& a, cudaStream_t s) {
+    dim3 blk(64, 4);
+    symmetry_kernel<<<full_grid(a.G, blk), blk, 0, s>>>(a);
+}
+
+void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
+    const int n = (a.imax + 1) * (a.F.nz + a.F.g) + (a.imax + 1) * (a.F.nr + a.F.g);
+    prolong_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_restrict(const RestrictArgs& a, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((a.Cg.nr + a.Cg.g + blk.x - 1) / blk.x, (a.Cg.nz + a.Cg.g + blk.y - 1) / blk.y);
+    restrict_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_norms(const LevelGeom& G, const double* f, int bicubic, double rminl, double zminl,
+                  double rmaxl, double zmaxl, double* dev_out, cudaStream_t s) {
+    norms_kernel<<<1, 512, 0, s>>>(G, f, bicubic, rminl, zminl, rmaxl, zmaxl, dev_out);
+}
+
+void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s) {
+    ham_edges_kernel<<<1, 256, 0, s>>>(G, ham);
+}
+
+void launch_gammadriver_init(const LevelGeom& G, double* dtbr, double* dtbz, const double* dlr,
+                             const double* dlz, double csi, cudaStream_t s) {
+    dim3 blk(64, 4);
+    gammadriver_init_kernel<<<full_grid(G, blk), blk, 0, s>>>(G, dtbr, dtbz, dlr, dlz, csi);
+}
+
+void launch_phi_from_chi(const LevelGeom& G, const double* chi, double* out, cudaStream_t s) {
+    dim3 blk(64, 4);
+    phi_from_chi_kernel<<<full_grid(G, blk), blk, 0, s>>>(G, chi, out);
+}
+
+double measure_fp64_dfma_rate(cudaStream_t s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    double* out = nullptr;
+    if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, 16, 0.5);
+    cudaEventRecord(e0, s);
+    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.5);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    return (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
+}
+
+}  // namespace ollin

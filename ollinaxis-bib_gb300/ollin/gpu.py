@@ -1,0 +1,171 @@
+"""ctypes mirror of the C ABI (include/ollin_gpu.h).
+
+``Evolution`` follows the reference's driver (src/base/evolve.f90): create the
+level hierarchy, ``initial_data`` (initial.f90), ``initialize`` (symmetries,
+auxiliary quantities and Gamma-driver set-up at t=0), then ``step`` =
+``call onestep(0)``.  There is no CPU fallback: every call goes to the CUDA
+library, and loading fails loudly when it is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+from .params import FIELD_ID, DERIVED_ID, Params
+
+_lib = None
+
+ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENAN", 4: "ENOMEM", 5: "ESTATE"}
+
+
+class OllinError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, code), msg))
+        self.code = code
+
+
+class LevelDesc(ctypes.Structure):
+    _fields_ = [("level", ctypes.c_int), ("nr", ctypes.c_int), ("nz", ctypes.c_int), ("ghost", ctypes.c_int),
+                ("dr", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
+                ("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("zmin", ctypes.c_double),
+                ("zmax", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_int)]
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libollin_gpu.so (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError("libollin_gpu.so has not been built: run __graft_entry__.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.ollin_params_default.argtypes = [ctypes.c_void_p]
+    L.ollin_gpu_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(vp)]
+    L.ollin_gpu_destroy.argtypes = [vp]
+    L.ollin_gpu_num_levels.argtypes = [vp]
+    L.ollin_gpu_level_desc.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_upload.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.ollin_gpu_download.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.ollin_gpu_initial_data.argtypes = [vp]
+    L.ollin_gpu_initialize.argtypes = [vp]
+    L.ollin_gpu_aux.argtypes = [vp, ctypes.c_int]
+    L.ollin_gpu_coarse_step.argtypes = [vp, dp]
+    L.ollin_gpu_norms.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_point_updates.argtypes = [vp]
+    L.ollin_gpu_point_updates.restype = ctypes.c_double
+    L.ollin_gpu_stream.argtypes = [vp]
+    L.ollin_gpu_stream.restype = ctypes.c_void_p
+    L.ollin_gpu_launch_count.argtypes = [vp]
+    L.ollin_gpu_launch_count.restype = ctypes.c_longlong
+    L.ollin_gpu_last_error.restype = ctypes.c_char_p
+    L.ollin_gpu_kernel_timing.argtypes = [vp, ctypes.c_int]
+    L.ollin_gpu_fp64_rate.restype = ctypes.c_double
+    L.ollin_gpu_kernel_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
+    _lib = L
+    return L
+
+
+def field_id(name):
+    if name in FIELD_ID:
+        return FIELD_ID[name]
+    if name in ("KTH",):
+        return 10
+    if name in DERIVED_ID:
+        return DERIVED_ID[name]
+    raise KeyError(name)
+
+
+class Evolution:
+    """One evolution on the current CUDA device."""
+
+    def __init__(self, params):
+        self.L = load()
+        self.p = params
+        h = ctypes.c_void_p()
+        self._check(self.L.ollin_gpu_create(ctypes.byref(params), ctypes.byref(h)))
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise OllinError(rc, self.L.ollin_gpu_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ollin_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference driver steps ------------------------------------------------
+    def initial_data(self):
+        self._check(self.L.ollin_gpu_initial_data(self.h))
+
+    def initialize(self):
+        self._check(self.L.ollin_gpu_initialize(self.h))
+
+    def aux(self, level):
+        self._check(self.L.ollin_gpu_aux(self.h, level))
+
+    def step(self):
+        t = ctypes.c_double()
+        self._check(self.L.ollin_gpu_coarse_step(self.h, ctypes.byref(t)))
+        return t.value
+
+    # data --------------------------------------------------------------------
+    def levels(self):
+        return range(self.L.ollin_gpu_num_levels(self.h))
+
+    def desc(self, level):
+        d = LevelDesc()
+        self._check(self.L.ollin_gpu_level_desc(self.h, level, ctypes.byref(d)))
+        return d
+
+    def download(self, level, name):
+        """(Nr+g, Nz+g) array indexed [i+g-1, j+g-1] for Fortran (i, j)."""
+        d = self.desc(level)
+        nr, nz, g = d.nr, d.nz, d.ghost
+        a = np.zeros((nz + g, nr + g), dtype=np.float64)
+        self._check(self.L.ollin_gpu_download(self.h, level, field_id(name), a.ctypes.data, nr + g))
+        return np.ascontiguousarray(a.T)
+
+    def upload(self, level, name, arr):
+        d = self.desc(level)
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).T)
+        self._check(self.L.ollin_gpu_upload(self.h, level, field_id(name), a.ctypes.data, d.nr + d.ghost))
+
+    def norms(self, level, name):
+        out = np.zeros(5)
+        self._check(self.L.ollin_gpu_norms(self.h, level, field_id(name), out.ctypes.data))
+        return out
+
+    def point_updates(self):
+        return self.L.ollin_gpu_point_updates(self.h)
+
+    def stream(self):
+        return self.L.ollin_gpu_stream(self.h)
+
+    def launch_count(self):
+        return self.L.ollin_gpu_launch_count(self.h)
+
+    def kernel_timing(self, enable=True):
+        self._check(self.L.ollin_gpu_kernel_timing(self.h, 1 if enable else 0))
+
+    def kernel_stats(self):
+        """(total rhs-kernel ms, rhs launches, grid points x stages) since timing was enabled."""
+        ms, n, pts = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+        self._check(self.L.ollin_gpu_kernel_stats(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(pts)))
+        return ms.value, n.value, pts.value

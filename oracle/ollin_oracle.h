@@ -11,6 +11,7 @@ typedef struct ollin_oracle ollin_oracle;
 const char* ollin_oracle_last_error(void);
 int ollin_oracle_create(const ollin_params* p, ollin_oracle** out);
 void ollin_oracle_destroy(ollin_oracle* o);
+int ollin_oracle_initial_data(ollin_oracle* o);
 int ollin_oracle_initialize(ollin_oracle* o);
 int ollin_oracle_step(ollin_oracle* o, double* t_out);
 int ollin_oracle_num_levels(const ollin_oracle* o);

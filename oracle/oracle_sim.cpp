@@ -440,9 +440,8 @@ static void initial(Sim& S) {
     }
 }
 
-// evolve.f90:124-195 (box 0, no maximal slicing)
+// evolve.f90:128-195 (box 0, no maximal slicing); ``initial`` runs first
 static void initialize(Sim& S) {
-    initial(S);
     for (Level& L : S.L) {
         currentgrid(S, L);
         if (L.ownaxis) symmetries_r(S, L);
@@ -507,6 +506,10 @@ int ollin_oracle_create(const ollin_params* p, ollin_oracle** out) {
 }
 
 void ollin_oracle_destroy(ollin_oracle* o) { delete o; }
+
+int ollin_oracle_initial_data(ollin_oracle* o) {
+    try { initial(o->S); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }
+}
 
 int ollin_oracle_initialize(ollin_oracle* o) {
     try { initialize(o->S); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }

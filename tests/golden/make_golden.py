@@ -1,0 +1,114 @@
+"""Generates the golden vectors of tests/golden/*.npz by executing the
+reference's own Fortran evolution path (src/base/onestep.f90 and everything
+it calls, plus initial.f90 and constraints.f90) through ``ftn_subset``.
+
+Run from the repository root in a container that has the reference mounted:
+
+    python tests/golden/make_golden.py /root/reference
+
+Each fixture stores, for a small box-in-box configuration, the reference's
+grid functions (all points including ghosts, Fortran (i,j) at [i+g-1, j+g-1])
+after 0, 1, 2, ... coarse steps, together with the parameters.  The
+scalar-field case starts from an analytic Gaussian pulse written into the
+arrays after ``initial`` (its elliptic initial-data solve is outside the
+evolution path).
+"""
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+from refsim import RefSim  # noqa: E402
+
+BASE = dict(order="four", integrator="rk4", dtfac=0.25, boundtype="radiative", eqsym=True,
+            idata="schwarzschild", bh1mass=1.0, ilapse="psiminus2", slicing="1+log",
+            gauge_f=2.0, shift="none", geodiss=0.02)
+
+CASES = {
+    # Schwarzschild puncture, 1+log, no shift, 2 levels
+    "c1_small": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, _steps=[0, 1, 2, 4]),
+    # same with the Gamma-driver shift, 3 levels
+    "c2_small": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver2",
+                     drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # ICN with harmonic slicing and the isotropic lapse, one level
+    "icn_harmonic": dict(BASE, nrtotal=16, nztotal=20, nl0=0, dr0=0.25, dz0=0.25, integrator="icn",
+                         icniter=3, slicing="harmonic", gauge_f=1.0, ilapse="isotropic", _steps=[0, 1, 3]),
+    # massive real scalar field on Minkowski data with the Gamma-driver shift
+    "scalar_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.25, dz0=0.25, idata="minkowski",
+                         ilapse="one", mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5,
+                         shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, scalardiss=0.02,
+                         _steps=[0, 1, 3]),
+}
+
+FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
+          "Delta_r", "Delta_z", "lambda", "Alambda"]
+SHIFT_FIELDS = ["beta_r", "beta_z", "dtbeta_r", "dtbeta_z"]
+SCALAR_FIELDS = ["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"]
+DERIVED = ["ham", "mom_r", "mom_z", "RSCAL", "KT2", "Lapla_alpha"]
+
+
+def scalar_pulse(r, z, a0=0.05):
+    """phi = a0 exp(-(r^2+z^2)), xi = grad phi, pi = 0 (analytic, so every
+    ghost point already has the right parity)."""
+    ph = a0 * np.exp(-(r ** 2 + z ** 2))
+    return ph, -2.0 * r * ph, -2.0 * z * ph, np.zeros_like(ph)
+
+
+def run_case(refdir, name, cfg):
+    cfg = dict(cfg)
+    steps = cfg.pop("_steps")
+    sim = RefSim(refdir, cfg)
+    sim.initial()
+    if cfg.get("mattertype") == "scalar":
+        for lev in sim.levels():
+            r, z = sim.field(lev, "r"), sim.field(lev, "z")
+            ph, xr, xz, pi = scalar_pulse(r, z)
+            for nm, v in zip(["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"], [ph, xr, xz, pi]):
+                sim.set_field(lev, nm, v)
+    sim.initialize()
+    names = list(FIELDS)
+    if cfg.get("shift", "none") != "none":
+        names += SHIFT_FIELDS
+    if cfg.get("mattertype") == "scalar":
+        names += SCALAR_FIELDS
+    out = {}
+    done = 0
+    for target in steps:
+        while done < target:
+            t0 = time.time()
+            sim.step()
+            done += 1
+            print("  %s: step %d in %.1fs" % (name, done, time.time() - t0), flush=True)
+        for lev in sim.levels():
+            for nm in names:
+                out["s%d_L%d_%s" % (done, lev, nm)] = sim.field(lev, nm)
+            if done == steps[-1] or done == 0:
+                sim.analysis(lev)
+                for nm in DERIVED:
+                    out["s%d_L%d_%s" % (done, lev, nm)] = sim.field(lev, nm)
+            out["s%d_L%d_time" % (done, lev)] = np.array(float(sim.M.t[0, lev]))
+    meta = dict(cfg, steps=steps, fields=names)
+    out["meta"] = np.array(json.dumps(meta))
+    return out
+
+
+def main():
+    refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    only = sys.argv[2:]
+    for name, cfg in CASES.items():
+        if only and name not in only:
+            continue
+        t0 = time.time()
+        out = run_case(refdir, name, cfg)
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **out)
+        print("%s -> %s (%.0fs, %d KB)" % (name, path, time.time() - t0, os.path.getsize(path) // 1024))
+
+
+if __name__ == "__main__":
+    main()

@@ -294,10 +294,19 @@ class RefSim:
     def use(self, level):
         self._currentgrid(0, level, self.M.grid[0, level])
 
-    def initialize(self):
+    def initial(self):
+        """call initial (evolve.f90:124)."""
         M, F = self.M, self.prog.F
         object.__setattr__(M, "s", _int_array((0, 0), (0, M.nlmax)))
         F.initial()
+
+    def set_field(self, level, name, values):
+        a = getattr(self.M.grid[0, level], fs.pyname(name.lower()))
+        a.view(np.ndarray)[...] = values
+
+    def initialize(self):
+        """evolve.f90:128-195: symmetries, auxiliary at t=0, Gamma driver."""
+        M, F = self.M, self.prog.F
         for lev in self.levels():
             self.use(lev)
             if M.ownaxis:

@@ -31,6 +31,7 @@ def lib():
         L.ollin_oracle_create.argtypes = [ctypes.c_void_p, ctypes.POINTER(vp)]
         L.ollin_oracle_destroy.argtypes = [vp]
         L.ollin_oracle_initialize.argtypes = [vp]
+        L.ollin_oracle_initial_data.argtypes = [vp]
         L.ollin_oracle_step.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
         L.ollin_oracle_num_levels.argtypes = [vp]
         L.ollin_oracle_dims.argtypes = [vp, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3
@@ -67,6 +68,9 @@ class Oracle:
         if getattr(self, "h", None):
             self.L.ollin_oracle_destroy(self.h)
             self.h = None
+
+    def initial_data(self):
+        self._check(self.L.ollin_oracle_initial_data(self.h))
 
     def initialize(self):
         self._check(self.L.ollin_oracle_initialize(self.h))

@@ -1,0 +1,136 @@
+"""GPU evolution (C ABI, sm_103a kernels) against the oracle.
+
+Bound: FP64 fields agree to max relative difference <= 1e-10 (normwise per
+field and level, see parity_util.REL_TOL) and constraint norms to 1e-8."""
+import numpy as np
+import pytest
+
+from oracle_bind import Oracle
+from parity_util import (C1, REL_TOL, coords, field_list, params, rel_diff, scalar_pulse)
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(cfg):
+    from ollin.gpu import Evolution
+    p = params(cfg)
+    o = Oracle(p)
+    e = Evolution(p)
+    o.initial_data()
+    e.initial_data()
+    if cfg.get("mattertype") == "scalar":
+        for lev in o.levels():
+            nr, nz, g = o.dims(lev)
+            r, z = o.get(lev, "r"), o.get(lev, "z")
+            for nm, v in zip(["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"], scalar_pulse(r, z)):
+                o.set(lev, nm, v)
+                e.upload(lev, nm, v)
+    o.initialize()
+    e.initialize()
+    return o, e
+
+
+def compare(o, e, cfg, tol=REL_TOL, tag=""):
+    worst = 0.0
+    for lev in o.levels():
+        for nm in field_list(cfg):
+            a = e.download(lev, nm)
+            b = o.get(lev, nm)
+            d = rel_diff(a, b)
+            worst = max(worst, d)
+            assert d <= tol, "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
+    return worst
+
+
+def run(cfg, steps, check_every=None):
+    o, e = make_pair(cfg)
+    compare(o, e, cfg, tag="t=0")
+    worst = 0.0
+    for k in range(1, steps + 1):
+        to, te = o.step(), e.step()
+        assert to == te
+        if check_every and k % check_every == 0 or k == steps:
+            worst = max(worst, compare(o, e, cfg, tag="step %d" % k))
+    return o, e, worst
+
+
+def test_c1_single_level_20_steps():
+    cfg = dict(C1, nl0=0)
+    _, _, w = run(cfg, 20, check_every=5)
+    print("single level worst %.2e" % w)
+
+
+def test_c1_three_levels_100_steps():
+    """The plain small configuration (3 box-in-box levels of 64x64) to 100
+    coarse steps (t = 5M): fields and constraint norms."""
+    o, e, w = run(dict(C1), 100, check_every=25)
+    print("C1 100 steps worst field rel diff %.2e" % w)
+    for lev in o.levels():
+        o.constraints(lev)
+        for nm in ["ham", "mom_r", "mom_z"]:
+            ng = e.norms(lev, nm)
+            no = o.norms(lev, nm)
+            # L2 (nm2) and max-abs (nm1) of the constraints
+            for k in (2, 3):
+                assert abs(ng[k] - no[k]) <= 1e-8 * abs(no[k]), (lev, nm, k, ng[k], no[k])
+
+
+def test_gammadriver_shift_three_levels():
+    cfg = dict(C1, nrtotal=32, nztotal=32, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+    run(cfg, 12, check_every=4)
+
+
+def test_icn_harmonic_isotropic():
+    cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
+               gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)
+    run(cfg, 8, check_every=4)
+
+
+def test_scalar_field_with_shift():
+    cfg = dict(C1, nrtotal=32, nztotal=32, nl0=1, dr0=0.25, dz0=0.25, idata="minkowski", ilapse="one",
+               mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5, shift="Gammadriver2",
+               drivercsi=0.75, drivereta=2.0, scalardiss=0.02)
+    run(cfg, 8, check_every=4)
+
+
+def test_norms_match_oracle():
+    o, e = make_pair(dict(C1, nl0=1))
+    for _ in range(3):
+        o.step(), e.step()
+    for lev in o.levels():
+        for nm in ["alpha", "trK", "phi"]:
+            ng, no = e.norms(lev, nm), o.norms(lev, nm)
+            np.testing.assert_allclose(ng, no, rtol=1e-10, atol=1e-14)
+
+
+def test_minkowski_stays_flat():
+    """Known answer: flat space with unit lapse has identically zero sources."""
+    cfg = dict(C1, nrtotal=32, nztotal=32, nl0=1, idata="minkowski", ilapse="one",
+               shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+    from ollin.gpu import Evolution
+    e = Evolution(params(cfg))
+    e.initial_data()
+    e.initialize()
+    for _ in range(4):
+        e.step()
+    for lev in e.levels():
+        assert np.all(e.download(lev, "alpha") == 1.0)
+        assert np.all(e.download(lev, "A") == 1.0)
+        assert np.all(e.download(lev, "trK") == 0.0)
+        assert np.all(e.download(lev, "beta_r") == 0.0)
+
+
+def test_nan_is_reported():
+    """A non-finite value in the state is turned into OLLIN_ENAN by the
+    kernels' own check, not into a fault."""
+    from ollin.gpu import Evolution, OllinError
+    cfg = dict(C1, nrtotal=16, nztotal=16, nl0=0)
+    e = Evolution(params(cfg))
+    e.initial_data()
+    a = e.download(0, "alpha")
+    a[8, 8] = np.nan
+    e.upload(0, "alpha", a)
+    e.initialize()
+    with pytest.raises(OllinError) as ex:
+        e.step()
+    assert ex.value.code == 3
