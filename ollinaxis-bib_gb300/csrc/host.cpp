@@ -264,7 +264,8 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
         a.aux[x] = base_ptr(L, L.aux[x]);
         a.auxw[x] = base_ptr(L, L.aux[x]);
     }
-    a.t0 = t0 ? 1 : 0;
+    a.t0 = L.last_aux_t0 ? 1 : 0;
+    a.evolve_phi = t0 ? 1 : 0;
     a.level0 = L.level == 0;
     a.rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
     a.nanflag = h->d_flag;

@@ -32,7 +32,9 @@ struct StageArgs {
     double* acc[NFIELDS];        // RK4 accumulator (var_a)
     const double* aux[NAUX];     // auxiliary quantities of the stage input
     double* auxw[NAUX];          // writable aux (analysis outputs)
-    int t0;                      // level time == 0 (first step of the level)
+    int t0;                      // the level's last ``auxiliary`` ran with time == 0
+                                 // (phi-based derivatives, auxiliary_geometry.f90:178-202)
+    int evolve_phi;              // level time == 0: phi is evolved (it is recomputed from chi otherwise)
     int level0;                  // level 0 (outer radiative boundary applies)
     int rk4, iter, niter;
     double dtw, weight;

@@ -88,7 +88,9 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     const double Dr_Dlr = Dr(F_DLR), Dz_Dlr = Dz(F_DLR);
     const double Dr_Dlz = Dr(F_DLZ), Dz_Dlz = Dz(F_DLZ);
 
-    // conformal factor (auxiliary_geometry.f90:171-250)
+    // conformal factor (auxiliary_geometry.f90:171-250).  The sources of a
+    // stage use the derivative arrays of the previous ``auxiliary`` call, so
+    // the branch follows the time of that call (A.t0), not the current one.
     double Dr_phi, Dz_phi, Drr_phi, Dzz_phi, Drz_phi, ipsi4, phi_c = 0.0;
     if (A.t0) {
         const Deriv5 dp = D5(F_PHI);
@@ -553,7 +555,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     };
     upd(F_ALPHA, s_alpha);
     upd(F_CHI, s_chi);
-    if (A.t0) upd(F_PHI, s_phi);
+    if (A.evolve_phi) upd(F_PHI, s_phi);
     upd(F_A, s_A); upd(F_B, s_B); upd(F_H, s_H); upd(F_C, s_C);
     upd(F_TRK, s_trK); upd(F_KTA, s_KTA); upd(F_KTB, s_KTB); upd(F_KTC, s_KTC);
     upd(F_DLR, s_Dlr); upd(F_DLZ, s_Dlz);

@@ -18,6 +18,17 @@ SCALAR_FIELDS = ["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"]
 # GPU kernel make the results differ at the 1e-15 level per step.
 REL_TOL = 1e-10
 
+# Auxiliary (non-evolved) quantities recomputed from the state each stage:
+# lambda = (A - H)/r^2 and Alambda = (KTA - KTH)/r^2 subtract two O(1) numbers
+# that agree to ~1e-8 next to the axis and divide by r^2 ~ 1e-4 on the finest
+# levels, so last-bit differences in A and H are amplified ~1e6 there.
+AUX_FIELDS = ("lambda", "Alambda", "KTH")
+AUX_TOL = 1e-8
+
+
+def tol_for(name):
+    return AUX_TOL if name in AUX_FIELDS else REL_TOL
+
 
 def field_list(cfg):
     names = list(BASE_FIELDS)

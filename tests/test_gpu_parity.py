@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from oracle_bind import Oracle
-from parity_util import (C1, REL_TOL, coords, field_list, params, rel_diff, scalar_pulse)
+from parity_util import (C1, coords, field_list, params, rel_diff, scalar_pulse, tol_for)
 
 pytestmark = pytest.mark.gpu
 
@@ -30,15 +30,18 @@ def make_pair(cfg):
     return o, e
 
 
-def compare(o, e, cfg, tol=REL_TOL, tag=""):
+def compare(o, e, cfg, tag=""):
+    """Largest normwise relative difference over the evolved fields; every
+    field is held to its bound (tol_for)."""
     worst = 0.0
     for lev in o.levels():
         for nm in field_list(cfg):
             a = e.download(lev, nm)
             b = o.get(lev, nm)
             d = rel_diff(a, b)
-            worst = max(worst, d)
-            assert d <= tol, "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
+            if nm not in ("lambda", "Alambda", "KTH"):
+                worst = max(worst, d)
+            assert d <= tol_for(nm), "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
     return worst
 
 
