@@ -106,9 +106,13 @@ def test_norms_match_oracle():
             np.testing.assert_allclose(ng, no, rtol=1e-10, atol=1e-14)
 
 
-def test_minkowski_stays_flat():
-    """Known answer: flat space with unit lapse has identically zero sources."""
-    cfg = dict(C1, nrtotal=32, nztotal=32, nl0=1, idata="minkowski", ilapse="one",
+@pytest.mark.parametrize("nl0", [0, 1])
+def test_minkowski_stays_flat(nl0):
+    """Known answer: flat space with unit lapse has identically zero sources.
+    On one level the state stays exactly flat; with refinement levels the
+    bicubic prolongation weights sum to one only to rounding, so flatness
+    holds to ~1e-16 (as in the reference)."""
+    cfg = dict(C1, nrtotal=32, nztotal=32, nl0=nl0, idata="minkowski", ilapse="one",
                shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
     from ollin.gpu import Evolution
     e = Evolution(params(cfg))
@@ -116,11 +120,12 @@ def test_minkowski_stays_flat():
     e.initialize()
     for _ in range(4):
         e.step()
+    tol = 0.0 if nl0 == 0 else 1e-13
     for lev in e.levels():
-        assert np.all(e.download(lev, "alpha") == 1.0)
-        assert np.all(e.download(lev, "A") == 1.0)
-        assert np.all(e.download(lev, "trK") == 0.0)
-        assert np.all(e.download(lev, "beta_r") == 0.0)
+        assert np.max(np.abs(e.download(lev, "alpha") - 1.0)) <= tol
+        assert np.max(np.abs(e.download(lev, "A") - 1.0)) <= tol
+        assert np.max(np.abs(e.download(lev, "trK"))) <= tol
+        assert np.max(np.abs(e.download(lev, "beta_r"))) <= tol
 
 
 def test_nan_is_reported():
