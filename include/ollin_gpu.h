@@ -209,6 +209,37 @@ double ollin_gpu_fp64_rate(void);
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);
 
+/*
+ * The five 0-D statistics of ollin_gpu_norms (max, min, max|f|, RMS over
+ * i = 1..nr-ghost, j = 1..nz-ghost, and the bicubic value at the origin) of a
+ * grid function that the caller already holds in device memory, computed
+ * without allocating anything.  No counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc -- hosts whose device memory comes
+ * from their own allocator or pool, code inside a stream capture, tools that
+ * may only read.
+ *
+ * d_field points at element (1-ghost, 1-ghost) of a column-major
+ * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost must be 3
+ * and the grid equatorially symmetric (box-0 coordinates r = (i-1/2) dr,
+ * z = (j-1/2) dz).  ``stream`` is a cudaStream_t or NULL; the call returns
+ * after the result has reached ``out`` (host memory).
+ *
+ * Limit: nz - ghost <= 8192 interior rows (larger grids get OLLIN_EINVAL).
+ * The intermediate results live in one fixed 320 KiB device array that is
+ * part of the library image, so every GPU that loads the library holds it
+ * until the process exits.  The first call on a device looks up that array's
+ * device address (with the device current); make that first call before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * contents; every slot a call reads is written earlier in the same call, so
+ * no clearing is needed, but calls whose work overlaps on the GPU (other
+ * threads or streams, at the same time) race on it and must be serialised by
+ * the caller.
+ */
+int ollin_gpu_norms_noalloc(const double* d_field, int nr, int nz, int ghost, int ld_r, double dr, double dz,
+                            int eqsym, void* stream, double out[5]);
+/* Message for the last failure of ollin_gpu_norms_noalloc on the calling thread. */
+const char* ollin_gpu_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
