@@ -19,6 +19,7 @@
 // the redundant-halo recomputation a fully fused single pass would need costs
 // more FP64 work than re-reading those arrays costs bandwidth.
 #include "ollin_kernels.h"
+#include "rhs_algebra_gen.cuh"
 
 namespace ollin {
 
@@ -111,173 +112,28 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
         ipsi4 = chi * chi;  // 1/psi^4 with psi = chi^(-1/2)
     }
 
-    const double r2 = r * r, r3 = r2 * r, r4 = r2 * r2, r5 = r4 * r, ir2 = ir * ir;
-    const double gA2 = gA * gA, gB2 = gB * gB, gH2 = gH * gH, gC2 = gC * gC;
-    const double gA3 = gA2 * gA, gB3 = gB2 * gB, gC3 = gC2 * gC;
-    const double lamDef = (Ac - Hc) * ir2;
+    const double r2 = r * r;
 
-    // ---- lapse: covariant second derivatives and Laplacian (:1266-1324)
-    double D2A = da.rr - da.r * gC * r2 * dC.r
-        - (da.z * gB * dC.r + half * da.z * gC * dA.r + da.r * gC * Cc - half * da.r * gC * dA.z) * r
-        - half * da.r * gA * dA.r - da.z * gB * Cc + half * da.z * gB * dA.z;
-    double D2B = da.zz - da.z * gC * r2 * dC.z
-        - (da.r * gA * dC.z + half * da.r * gC * dB.z - half * da.z * gC * dB.r) * r
-        + half * da.r * gA * dB.r - half * da.z * gB * dB.z;
-    double D2H = -(-half * da.r * gC * dH.z - half * da.z * gC * dH.r) * r
-        + half * da.r * gA * dH.r + da.z * gC * Hc + half * da.z * gB * dH.z + da.r * gA * Hc * ir;
-    double D2C = da.rz * ir - half * da.r * gC * dB.r - half * da.z * gC * dA.z
-        - (half * da.r * gA * dA.z + half * da.z * gB * dB.r) * ir;
-    {
-        const double aux1 = gA * da.r * Dr_phi + gB * da.z * Dz_phi + r * gC * (da.r * Dz_phi + da.z * Dr_phi);
-        D2A = D2A - two * (two * da.r * Dr_phi - Ac * aux1);
-        D2B = D2B - two * (two * da.z * Dz_phi - Bc * aux1);
-        D2H = D2H + two * Hc * aux1;
-        D2C = D2C - two * ((da.r * ir) * Dz_phi + da.z * (Dr_phi * ir) - Cc * aux1);
-    }
-    const double Lapla_alpha = (gA * D2A + gB * D2B + gH * D2H + two * r2 * gC * D2C) * ipsi4;
-
-    // ---- Ricci tensor: conformal-factor part (:1331-1469)
-    double RA = -two * (Drr_phi - Dr_phi * gC * r2 * dC.r
-        - (Dz_phi * gB * dC.r + half * Dz_phi * gC * dA.r + Dr_phi * gC * Cc - half * Dr_phi * gC * dA.z) * r
-        - half * Dr_phi * gA * dA.r - Dz_phi * gB * Cc + half * Dz_phi * gB * dA.z);
-    double RB = -two * (Dzz_phi - Dz_phi * gC * r2 * dC.z
-        - (Dr_phi * gA * dC.z + half * Dr_phi * gC * dB.z - half * Dz_phi * gC * dB.r) * r
-        + half * Dr_phi * gA * dB.r - half * Dz_phi * gB * dB.z);
-    double RH = -two * (-(-half * Dr_phi * gC * dH.z - half * Dz_phi * gC * dH.r) * r
-        + half * Dr_phi * gA * dH.r + Dz_phi * gC * Hc + half * Dz_phi * gB * dH.z + Dr_phi * gA * Hc * ir);
-    double RC = -two * (Drz_phi * ir - half * Dr_phi * gC * dB.r - half * Dz_phi * gC * dA.z
-        - (half * Dr_phi * gA * dA.z + half * Dz_phi * gB * dB.r) * ir);
-    {
-        const double tr = gA * RA + gB * RB + gH * RH + two * r2 * gC * RC;
-        RA = RA + Ac * tr;
-        RB = RB + Bc * tr;
-        RH = RH + Hc * tr;
-        RC = RC + Cc * tr;
-        RA = RA + four * (Dr_phi * Dr_phi);
-        RB = RB + four * (Dz_phi * Dz_phi);
-        RC = RC + four * (Dr_phi * Dz_phi) * ir;
-        const double q = -two * (gA * Dr_phi * Dr_phi + gB * Dz_phi * Dz_phi + two * r * gC * Dr_phi * Dz_phi);
-        RA = RA + two * Ac * q;
-        RB = RB + two * Bc * q;
-        RH = RH + two * Hc * q;
-        RC = RC + two * Cc * q;
-    }
-    // calc_conformalRicci1.f90:76-86
-    RA = RA - gC * dA.rz * r - half * gB * dA.zz - half * gA * dA.rr - half * gH * dA.r * ir + gH * lamDef;
-    RB = RB - gC * dB.rz * r - half * gA * dB.rr - half * gB * dB.zz - half * gH * dB.r * ir;
-    RH = RH - gC * dH.rz * r - half * gB * dH.zz - half * gA * dH.rr - half * gH * dH.r * ir - gH * lamDef;
-    RC = RC - gC * dC.rz * r - half * gA * dC.rr - gC * dC.z - half * gB * dC.zz + (-gA * dC.r - half * gH * dC.r) * ir;
-    // calc_conformalRicci2.f90:73-83
-    RA = RA + Cc * Dr_Dlz * r + Ac * Dr_Dlr + half * (DDr * dA.r + DDz * dA.z);
-    RB = RB + Cc * Dz_Dlr * r + Bc * Dz_Dlz + half * (DDr * dB.r + DDz * dB.z);
-    RH = RH + half * (DDr * dH.r + DDz * dH.z) + Dlr * Hc * ir;
-    RC = RC + half * Cc * (Dr_Dlr + Dz_Dlz) + half * (DDr * dC.r + DDz * dC.z) + half * (Cc * Dlr + Ac * Dz_Dlr + Bc * Dr_Dlz) * ir;
-    {
-        const double dAr = dA.r, dAz = dA.z, dBr = dB.r, dBz = dB.z, dHr = dH.r, dHz = dH.z, dCr = dC.r, dCz = dC.z;
-        // calc_conformalRicci3.f90:316-340
-        RA = RA + (2.0 * gB * gC * dCr * dCz + gC2 * dAr * dCz + dAz * gC2 * dCr) * r3
-            + (2.0 * gB * gC * Cc * dCz - gB * gC * dCr * dBr + dAr * gC * gA * dCr + dAz * gC2 * Cc) * r2
-            + (dAz * gB * gC * dBr + dAz * gB * gA * dCr + dAr * gC * gA * Cc - gB * gC * Cc * dBr + dAz * gC * gA * dAr
-               + gB2 * dBr * dCz) * r
-            - half * gH2 * sq(dHr) - half * gB2 * sq(dBr) + gB * gA * Cc * dAz + half * sq(dAr) * gA2
-            + (gH * dHr + gH2 * Ac * dHr - 2.0 * gH2 * dHr * Hc) * ir;
-        RB = RB + (dBr * gC2 * dCz + gC2 * dBz * dCr + 2.0 * gA * gC * dCz * dCr) * r3
-            + (2.0 * gA * gC * dCz * Cc - gA * gC * dCz * dAz + gC2 * dBz * Cc + dBz * gC * gB * dCz) * r2
-            + (dBr * gA * gC * dAz + gA2 * dAz * dCr + dBr * gA * gB * dCz + dBr * gB * gC * dBz) * r
-            + half * gB2 * sq(dBz) + gA2 * dAz * Cc - half * gA2 * sq(dAz) + gH2 * dHz * Cc - half * gH2 * sq(dHz);
-        RH = RH - gC * dHz - r * glam * dHr;
-        RC = RC + (gC2 * dBr * dCr + gC * gB * sq(dCz) + dAz * gC2 * dCz + gC * gA * sq(dCr)) * r2
-            + (-half * gC * gA * dCr * dAz + 2.0 * gC * gA * dCr * Cc - half * gC2 * dBr * dAz - half * gC * gB * dCz * dBr
-               + half * dBz * gB * gC * dCr + gC2 * dBr * Cc + half * dBz * gC2 * dAr + half * dAr * gA * gC * dCz) * r
-            + half * dBr * gC * gA * dAr + half * dBr * gB * gA * dCr + half * gB2 * dBz * dCz + half * dAz * gA * gB * dCz
-            + half * gA2 * dAr * dCr + half * sq(dBr) * gB * gC + gC * gA * sq(Cc) - half * gC * gA * Cc * dAz
-            + half * dAz * gB * gC * dBz + half * sq(dAz) * gA * gC + half * dBz * gB * gC * Cc
-            + (half * gH2 * Cc * dHr + half * gB * gA * dBr * Cc - half * gH2 * dHz * dHr + half * gA2 * dAr * Cc) * ir
-            + half * dHz * gH2 * lam;
-        // calc_conformalRicci4.f90:272-298
-        RA = RA + dAz * gC2 * dCr * r3
-            + (-half * sq(dAz) * gC2 + dAz * gC2 * Cc + gB * gA * sq(dCr) + half * dAr * gC2 * dBr + dAr * gC * gA * dCr
-               + gB * gC * dCr * dBr) * r2
-            + (-dAz * gB * gA * dCr + 2.0 * gB * gA * dCr * Cc + gB * gC * Cc * dBr + dAr * gC * gA * Cc) * r
-            + fourth * gH2 * sq(dHr) - gB * gA * Cc * dAz + fourth * gB2 * sq(dBr) + gB * gA * sq(Cc)
-            + fourth * sq(dAr) * gA2 + half * gB * gA * sq(dAz);
-        RB = RB + dBr * gC2 * r3 * dCz
-            + (gA * gB * sq(dCz) + half * dAz * gC2 * dBz - half * gC2 * sq(dBr) + dBz * gC * gB * dCz + gA * gC * dCz * dAz) * r2
-            - dBr * gA * gB * dCz * r + fourth * gA2 * sq(dAz) + half * gB * gA * sq(dBr) + fourth * gH2 * sq(dHz)
-            + fourth * gB2 * sq(dBz);
-        RH = RH + (-half * Cc * gC * gH * dHr + gH * gC * dHz * dHr) * r + half * gH * sq(dHz) * gB
-            + 3.0 * half * gC * dHz + half * gH * gA * sq(dHr) - half * Cc * gB * gH * dHz - half * gH * Ac * gC * dHz - Cc * gC
-            - half * gC * dHz + half * (2.0 * gA - gH - gH * Ac * gA) * dHr * ir + gH * lam * (1.0 - gA * Hc);
-        RC = RC + gC2 * dCr * dCz * r3
-            + (-half * dAz * gC2 * dCz + gC2 * Cc * dCz - half * gC2 * dBr * dCr) * r2
-            + (-half * gC2 * dBr * Cc + fourth * dBz * gC2 * dAr + half * dAr * gA * gC * dCz + half * gC * gB * dCz * dBr
-               + 3.0 * fourth * gC2 * dBr * dAz + half * dBz * gB * gC * dCr + half * gC * gA * dCr * dAz) * r
-            + half * dAz * gA * gB * dCz + half * dBz * gB * gC * Cc + half * gC * gA * Cc * dAz + half * dBr * gB * gA * dCr
-            + (fourth * gH2 * dHz * dHr + half * gB * gA * dBr * Cc + fourth * gA2 * dAr * dAz + fourth * dBz * gB2 * dBr
-               - half * gB * gA * dAz * dBr) * ir;
-    }
-    const double RSCAL = (gA * RA + gB * RB + gH * RH + two * r2 * gC * RC) * ipsi4;
-
-    // ---- contravariant and squared traceless curvature (:944-1031)
-    const double KT_up_rr = (2.0 * gA * gC * kC + gC2 * kB) * r2 + gA2 * kA;
-    const double KT_up_zz = (gC2 * kA + 2.0 * gC * gB * kC) * r2 + gB2 * kB;
-    const double KT_up_rz = gC2 * r3 * kC + (gC * gA * kA + gB * gA * kC + gB * gC * kB) * r;
-    const double KT2_A = (2.0 * kA * gC * kC + sq(kC) * gB) * r2 + gA * sq(kA);
-    const double KT2_B = (sq(kC) * gA + 2.0 * kC * gC * kB) * r2 + gB * sq(kB);
-    const double KT2_H = sq(kH) * gH;
-    const double KT2_C = sq(kC) * gC * r2 + kA * gA * kC + kA * gC * kB + kC * gB * kB;
-    const double KT2 = gA * KT2_A + gB * KT2_B + gH * KT2_H + two * gC * KT2_C * r2;
-    const double K2 = KT2 + third * sq(trK);
-
-    // ---- divergence of the traceless curvature (calc_DIVKTA.f90:573-636)
-    double DIV_KT_r, DIV_KT_z, DIVA_KT_r, DIVA_KT_z;
-    {
-        const double dAr = dA.r, dAz = dA.z, dBr = dB.r, dBz = dB.z, dHr = dH.r, dHz = dH.z, dCr = dC.r, dCz = dC.z;
-        const double dkAr = Dr_KTA, dkAz = Dz_KTA, dkBr = Dr_KTB, dkBz = Dz_KTB, dkCr = Dr_KTC, dkCz = Dz_KTC;
-        DIV_KT_r = -gC3 * dCz * kC * r5 - gA * gC2 * kC * dCr * r4
-            + (gC2 * dkCz - half * gC3 * dBz * kA - gA * gC2 * kC * Cc - half * gC3 * dAz * kB - gA * dCz * gC2 * kA
-               - gA * dCz * gC * gB * kC - gC2 * dCz * gB * kB - gC2 * dBz * gB * kC - gA * dAz * gC2 * kC) * r3
-            + (2.0 * gA * gC * dkCr - Dlr * gC * kC - gC * dBr * gB * gA * kC - gB * gA2 * kC * dCr - dAr * gA2 * gC * kC
-               - gC * gA2 * kA * dCr + gC2 * dkBr - gA * gB * gC * kB * dCr - half * gA * dAr * gC2 * kB
-               - half * gC2 * dBr * gA * kA) * r2
-            + (2.0 * gA * gC * kC + gA * gC * dkAz - gC * gA2 * kA * Cc + gC * gH * kC - half * gH2 * kH * gC * dHz
-               - Dlz * gC * kB - gB * gA2 * kC * Cc - half * gA2 * dAz * gC * kA + gC * gB * dkBz + gA * gB * dkCz
-               - Dlz * gA * kC - gA * gB * gC * kB * Cc - gC * gH2 * kH * Cc - half * gC * dBz * gB2 * kB) * r
-            - half * gA * dBr * gB2 * kB - half * gH2 * kH * gA * dHr - Dlr * gA * kA + gA2 * dkAr
-            - half * gA3 * dAr * kA + r * gH * (gA * Alam + gH * kH * Cc * gC);
-        DIV_KT_z = -r5 * gC3 * kC * dCr + (-gC3 * kC * Cc - dCz * gC2 * gB * kC) * r4
-            + (gC2 * dkCr - gB * gC2 * kB * dCr - gC * gB * gA * kC * dCr - half * gC3 * dBr * kA - gC2 * gA * kA * dCr
-               - half * dAr * gC3 * kB - dAr * gA * gC2 * kC - gB * dBr * gC2 * kC) * r3
-            + (-gB * dCz * gC * gA * kA + gC2 * kC - dBz * gC * gB2 * kC - Dlz * gC * kC - gC * dCz * gB2 * kB
-               + gC2 * dkAz + 2.0 * gC * gB * dkCz - gC2 * gA * kA * Cc - dCz * gB2 * gA * kC - half * dAz * gB * gC2 * kB
-               - gC * dAz * gB * gA * kC - gB * gC2 * kB * Cc - half * gB * dBz * gC2 * kA - gC * gB * gA * kC * Cc) * r2
-            + (gB * gC * dkBr + gB * gA * dkCr + gC * gA * dkAr - half * gH2 * kH * gC * dHr - Dlr * gB * kC - Dlr * gC * kA
-               - half * gB2 * dBr * gC * kB - half * gC * dAr * gA2 * kA) * r
-            + gC * gH * kA + gB * gA * kC - half * dBz * gB3 * kB + gB2 * dkBz - Dlz * gB * kB - gC * gH2 * kH * Ac
-            - half * gB * dAz * gA2 * kA - half * gH2 * kH * gB * dHz - gC * gH * kH + gB * gH * kC - gB * gH2 * kH * Cc;
-        DIVA_KT_r = -r5 * gC3 * dCz * kC + (-gC3 * dCr * kB - gC3 * dBr * kC - 3.0 * gC2 * dCr * gA * kC) * r4
-            + (-gC3 * Cc * kB - 2.0 * gA * dCz * gC2 * kA - 3.0 * gC2 * Cc * gA * kC + gC2 * dkCz - gC2 * dAz * gA * kC
-               - 3.0 * gA * dCz * gC * gB * kC - 2.0 * gC2 * dBz * gB * kC - gC3 * dBz * kA - gC2 * dCz * gB * kB) * r3
-            + (-gA * dBr * gC2 * kA - gA * gB * gC * kB * dCr + 2.0 * gA * gC * dkCr - 2.0 * gC * dCr * gA2 * kA - Dlr * gC * kC
-               + gC2 * dkBr - gC2 * dBr * gB * kB - 2.0 * gA2 * dAr * gC * kC - gA * dAr * gC2 * kB
-               - gB * gA2 * kC * dCr - gA * dBr * gC * gB * kC) * r2
-            + (-gA * dCz * gB2 * kB - gB * gA2 * kC * Cc - gC * dBz * gB2 * kB + 2.0 * gA * gC * kC + gC * gB * dkBz
-               + gC * gH * kC + gA * gC * dkAz + gA * gB * dkCz - gA * dAz * gB * gC * kB - gC * gH2 * kH * Cc - Dlz * gC * kB
-               - gA2 * dAz * gB * kC - 2.0 * gC * Cc * gA2 * kA - Dlz * gA * kC - gA2 * dAz * gC * kA - gA * gB * gC * kB * Cc) * r
-            - dAr * gA3 * kA - Dlr * gA * kA + gA2 * dkAr + r * gA * gH * (Alam - lam * gH * kH);
-        DIVA_KT_z = -r5 * gC3 * kC * dCr
-            + (-3.0 * dCz * gC2 * gB * kC - dAz * gC3 * kC - dCz * gC3 * kA - gC3 * kC * Cc) * r4
-            + (-3.0 * gC * gB * gA * kC * dCr - 2.0 * dAr * gA * gC2 * kC + gC2 * dkCr - gB * dBr * gC2 * kC
-               - dAr * gC3 * kB - 2.0 * gB * gC2 * kB * dCr - gC2 * gA * kA * dCr) * r3
-            + (-gC * dAz * gB * gA * kC - gC2 * gA * kA * Cc - 2.0 * dBz * gC * gB2 * kC - dAz * gC2 * gA * kA
-               - dAz * gB * gC2 * kB - 3.0 * gC * gB * gA * kC * Cc - 2.0 * gC * dCz * gB2 * kB - Dlz * gC * kC
-               - dCz * gB2 * gA * kC + gC2 * kC + gC2 * dkAz + 2.0 * gC * gB * dkCz - gB * dCz * gC * gA * kA
-               - gB * dBz * gC2 * kA - 2.0 * gB * gC2 * kB * Cc) * r2
-            + (-Dlr * gB * kC + gB * gA * dkCr + gC * gA * dkAr + gB * gC * dkBr - gB2 * dBr * gC * kB - Dlr * gC * kA
-               - gB2 * dBr * gA * kC - gC * dAr * gA2 * kA - gB * dBr * gC * gA * kA - gB * gA2 * kA * dCr) * r
-            - Dlz * gB * kB - gB * gH2 * kH * Cc + gB2 * dkBz - gC * gH2 * kH * Ac - gB * gA2 * kA * Cc + gB * gH * kC
-            + gC * gH * kA + gB * gA * kC - dBz * gB3 * kB;
-    }
+    // ---- the pointwise algebra (Laplacian of the lapse, Ricci tensor and
+    //      scalar, curvature contractions, divergence of KT, geometric
+    //      sources and constraints), generated in FP64-instruction-minimised
+    //      form from csrc/gen/bssn_spec.py
+    AlgIn in;
+    in.r = r; in.ir = ir; in.alpha = alpha; in.chi = chi;
+    in.Ac = Ac; in.Bc = Bc; in.Hc = Hc; in.Cc = Cc;
+    in.trK = trK; in.kA = kA; in.kB = kB; in.kC = kC; in.kH = kH;
+    in.Dlr = Dlr; in.Dlz = Dlz; in.gA = gA; in.gB = gB; in.gH = gH; in.gC = gC;
+    in.lam = lam; in.Alam = Alam; in.glam = glam; in.DDr = DDr; in.DDz = DDz;
+    in.ipsi4 = ipsi4; in.eta = P.eta;
+    in.da_r = da.r; in.da_z = da.z; in.da_rr = da.rr; in.da_zz = da.zz; in.da_rz = da.rz;
+    in.dA_r = dA.r; in.dA_z = dA.z; in.dA_rr = dA.rr; in.dA_zz = dA.zz; in.dA_rz = dA.rz;
+    in.dB_r = dB.r; in.dB_z = dB.z; in.dB_rr = dB.rr; in.dB_zz = dB.zz; in.dB_rz = dB.rz;
+    in.dH_r = dH.r; in.dH_z = dH.z; in.dH_rr = dH.rr; in.dH_zz = dH.zz; in.dH_rz = dH.rz;
+    in.dC_r = dC.r; in.dC_z = dC.z; in.dC_rr = dC.rr; in.dC_zz = dC.zz; in.dC_rz = dC.rz;
+    in.Dr_phi = Dr_phi; in.Dz_phi = Dz_phi; in.Drr_phi = Drr_phi; in.Dzz_phi = Dzz_phi; in.Drz_phi = Drz_phi;
+    in.Dr_trK = Dr_trK; in.Dz_trK = Dz_trK; in.Dr_KTA = Dr_KTA; in.Dz_KTA = Dz_KTA;
+    in.Dr_KTB = Dr_KTB; in.Dz_KTB = Dz_KTB; in.Dr_KTC = Dr_KTC; in.Dz_KTC = Dz_KTC;
+    in.Dr_Dlr = Dr_Dlr; in.Dz_Dlr = Dz_Dlr; in.Dr_Dlz = Dr_Dlz; in.Dz_Dlz = Dz_Dlz;
 
     // ---- matter: scalar field stress-energy (stressenergy.f90:65-205) and
     //      its source (scalar.f90)
@@ -327,20 +183,12 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     double s_phi = -sixth * alpha * trK;
     double s_chi = 2.0 * sixth * alpha * chi * trK;
     double s_A = -two * alpha * kA, s_B = -two * alpha * kB, s_H = -two * alpha * kH, s_C = -two * alpha * kC;
-    double s_trK = -Lapla_alpha + alpha * K2;
-    double s_KTA = alpha * (trK * kA - two * KT2_A);
-    double s_KTB = alpha * (trK * kB - two * KT2_B);
-    double s_KTC = alpha * (trK * kC - two * KT2_C);
-    {
-        const double tr = -Lapla_alpha + alpha * RSCAL;
-        s_KTA = s_KTA + (-D2A + alpha * RA) * ipsi4 - third * Ac * tr;
-        s_KTB = s_KTB + (-D2B + alpha * RB) * ipsi4 - third * Bc * tr;
-        s_KTC = s_KTC + (-D2C + alpha * RC) * ipsi4 - third * Cc * tr;
+    double s_trK = 0, s_KTA = 0, s_KTB = 0, s_KTC = 0, s_Dlr = 0, s_Dlz = 0;
+    if (!A.analysis) {
+        SrcOut so;
+        bssn_sources(in, so);
+        s_trK = so.s_trK; s_KTA = so.s_KTA; s_KTB = so.s_KTB; s_KTC = so.s_KTC; s_Dlr = so.s_Dlr; s_Dlz = so.s_Dlz;
     }
-    double s_Dlr = -two * (KT_up_rr * da.r + KT_up_rz * da.z) - two * alpha * DIVA_KT_r;
-    s_Dlr = s_Dlr + P.eta * alpha * (DIV_KT_r + six * (KT_up_rr * Dr_phi + KT_up_rz * Dz_phi) - two * third * (gA * Dr_trK + r * gC * Dz_trK));
-    double s_Dlz = -two * (KT_up_rz * da.r + KT_up_zz * da.z) - two * alpha * DIVA_KT_z;
-    s_Dlz = s_Dlz + P.eta * alpha * (DIV_KT_z + six * (KT_up_rz * Dr_phi + KT_up_zz * Dz_phi) - two * third * (r * gC * Dr_trK + gB * Dz_trK));
     double s_alpha = 0.0;
     if (P.slicing == 0) s_alpha = -(alpha * P.gauge_f) * trK;                 // 1+log
     else if (P.slicing == 1) s_alpha = -(sq(alpha) * P.gauge_f) * trK;       // harmonic
@@ -439,20 +287,20 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     if (A.analysis) {
         // constraints.f90:55-149
         const double spf = 3.1415927410125732;  // acos(-1.0) in single precision
-        double ham = RSCAL - KT2 + two * third * sq(trK);
-        if constexpr (SCALAR) ham = ham - 16.0 * spf * rho;
-        double momr = DIV_KT_r + 6.0 * (KT_up_rr * Dr_phi + KT_up_rz * Dz_phi) - two * third * (gA * Dr_trK + r * gC * Dz_trK);
-        double momz = DIV_KT_z + 6.0 * (KT_up_rz * Dr_phi + KT_up_zz * Dz_phi) - two * third * (r * gC * Dr_trK + gB * Dz_trK);
+        AnaOut ao;
+        bssn_analysis(in, ao);
+        double ham = ao.ham, momr = ao.mom_r, momz = ao.mom_z;
         if constexpr (SCALAR) {
+            ham = ham - 16.0 * spf * rho;
             momr = momr - 8.0 * spf * J_r / ipsi4;
             momz = momz - 8.0 * spf * J_z / ipsi4;
         }
         A.auxw[X_HAM][o] = ham;
         A.auxw[X_MOMR][o] = momr;
         A.auxw[X_MOMZ][o] = momz;
-        A.auxw[X_RSCAL][o] = RSCAL;
-        A.auxw[X_KT2][o] = KT2;
-        A.auxw[X_LAPLA][o] = Lapla_alpha;
+        A.auxw[X_RSCAL][o] = ao.RSCAL;
+        A.auxw[X_KT2][o] = ao.KT2;
+        A.auxw[X_LAPLA][o] = ao.Lapla_alpha;
         return;
     }
 
