@@ -51,7 +51,19 @@ def cost(e):
     return sum(cost(a) for a in e.args)
 
 
+METRIC = ("gA", "gB", "gC", "gH", "r", "ir", "glam", "lam", "ipsi4")
+
+
+def _horner(poly_expr, gens):
+    try:
+        return sp.polys.polyfuncs.horner(poly_expr, *gens)
+    except Exception:
+        return poly_expr
+
+
 def horner_by_frequency(poly_expr, exclude=()):
+    """Cheapest multivariate Horner form over a few variable orderings:
+    by frequency, data (derivatives, curvature) first, metric first."""
     if not poly_expr.free_symbols:
         return poly_expr
     terms = sp.Add.make_args(poly_expr)
@@ -62,10 +74,11 @@ def horner_by_frequency(poly_expr, exclude=()):
     gens = sorted((s for s in freq if s not in exclude), key=lambda s: (-freq[s], s.name))
     if not gens:
         return poly_expr
-    try:
-        return sp.polys.polyfuncs.horner(poly_expr, *gens)
-    except Exception:
-        return poly_expr
+    data = [g for g in gens if g.name not in METRIC]
+    metric = [g for g in gens if g.name in METRIC]
+    cands = [_horner(poly_expr, gens), _horner(poly_expr, data + metric), _horner(poly_expr, metric + data),
+             _horner(poly_expr, list(reversed(gens)))]
+    return min(cands, key=cost)
 
 
 def optimise(expr, r, ir):

@@ -79,7 +79,7 @@ __device__ __forceinline__ double d1(const double* f, long s, int k, double c) {
 
 __device__ __forceinline__ double d2(const double* f, long s, int k, double c) {
     if (k == 0) {
-        return -c * (30.0 * ld_(f) - 16.0 * (ld_(f + s) + ld_(f - s)) + ld_(f + 2 * s) + ld_(f - 2 * s));
+        return -c * fma(30.0, ld_(f), fma(-16.0, ld_(f + s) + ld_(f - s), ld_(f + 2 * s) + ld_(f - 2 * s)));
     } else if (k == 1) {
         return c * (10.0 * ld_(f + s) - 15.0 * ld_(f) - 4.0 * ld_(f - s) + 14.0 * ld_(f - 2 * s) - 6.0 * ld_(f - 3 * s) + ld_(f - 4 * s));
     } else if (k == 2) {
@@ -105,8 +105,8 @@ __device__ __forceinline__ double d2rz(const double* f, long ld, int i, int j, i
     const bool ri = (i >= 3 - g && i <= nr - 2), zi = (j >= 3 - g && j <= nz - 2);
 #define F_(a, b) ld_(f + (a) + (long)(b) * ld)
     if (ri && zi) {
-        return idrz * ((F_(1, 1) + F_(-1, -1) - F_(1, -1) - F_(-1, 1)) * (1.0 / 3.0)
-                       - (F_(2, 2) + F_(-2, -2) - F_(2, -2) - F_(-2, 2)) * (1.0 / 48.0));
+        return fma(idrz * (1.0 / 3.0), (F_(1, 1) + F_(-1, -1)) - (F_(1, -1) + F_(-1, 1)),
+                   (idrz * (-1.0 / 48.0)) * ((F_(2, 2) + F_(-2, -2)) - (F_(2, -2) + F_(-2, 2))));
     }
     const bool zedge_loop = (i >= 2 - g && i <= nr - 1);  // z-boundary loop range
     const bool redge_loop = (j >= 2 - g && j <= nz - 1);  // r-boundary loop range
@@ -166,6 +166,19 @@ __device__ __forceinline__ double dadv(const double* f, long s, int i, int n, in
 // src/base/dissipation.f90:196-211 (without the -eps/dt/20 factor).
 __device__ __forceinline__ double ko6(const double* f, long s) {
     return 20.0 * ld_(f) - 15.0 * (ld_(f + s) + ld_(f - s)) + 6.0 * (ld_(f + 2 * s) + ld_(f - 2 * s)) - (ld_(f + 3 * s) + ld_(f - 3 * s));
+}
+
+// s - k * (ko6 along stride 1 + ko6 along stride ld), for points inside both
+// dissipation ranges: the two brackets share the centre and are summed
+// before scaling (13 FP64 operations instead of 16).
+__device__ __forceinline__ double ko6rz_apply(const double* f, long ld, double k, double s) {
+    const double a1 = (ld_(f + 1) + ld_(f - 1)) + (ld_(f + ld) + ld_(f - ld));
+    const double a2 = (ld_(f + 2) + ld_(f - 2)) + (ld_(f + 2 * ld) + ld_(f - 2 * ld));
+    const double a3 = (ld_(f + 3) + ld_(f - 3)) + (ld_(f + 3 * ld) + ld_(f - 3 * ld));
+    double t = fma(-40.0 * k, ld_(f), s);
+    t = fma(15.0 * k, a1, t);
+    t = fma(-6.0 * k, a2, t);
+    return fma(k, a3, t);
 }
 
 }  // namespace ollin

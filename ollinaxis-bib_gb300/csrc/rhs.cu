@@ -34,7 +34,13 @@ __device__ __forceinline__ bool nonfinite(double x) {
 struct Deriv5 { double r, z, rr, zz, rz; };
 
 template <bool SHIFT, bool SCALAR>
-__global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageArgs A) {
+#ifndef OLLIN_RHS_THREADS
+#define OLLIN_RHS_THREADS 128
+#endif
+#ifndef OLLIN_RHS_MINBLOCKS
+#define OLLIN_RHS_MINBLOCKS 3
+#endif
+__global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_kernel(const __grid_constant__ StageArgs A) {
     const LevelGeom& G = A.G;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
@@ -47,21 +53,21 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
     const double cr2 = G.idr * G.idr * (1.0 / 12.0), cz2 = G.idz * G.idz * (1.0 / 12.0);
     const double idrz = G.idr * G.idz;
-    const int kr = pclass(i, nr, g), kz = pclass(j, nz, g);
+    const int pcr = pclass(i, nr, g), pcz = pclass(j, nz, g);
 
     auto val = [&](int f) { return ld_(A.in[f] + o); };
     auto D5 = [&](int f) {
         const double* p = A.in[f] + o;
         Deriv5 d;
-        d.r = d1(p, 1, kr, cr1);
-        d.z = d1(p, ld, kz, cz1);
-        d.rr = d2(p, 1, kr, cr2);
-        d.zz = d2(p, ld, kz, cz2);
+        d.r = d1(p, 1, pcr, cr1);
+        d.z = d1(p, ld, pcz, cz1);
+        d.rr = d2(p, 1, pcr, cr2);
+        d.zz = d2(p, ld, pcz, cz2);
         d.rz = d2rz(p, ld, i, j, nr, nz, g, idrz);
         return d;
     };
-    auto Dr = [&](int f) { return d1(A.in[f] + o, 1, kr, cr1); };
-    auto Dz = [&](int f) { return d1(A.in[f] + o, ld, kz, cz1); };
+    auto Dr = [&](int f) { return d1(A.in[f] + o, 1, pcr, cr1); };
+    auto Dz = [&](int f) { return d1(A.in[f] + o, ld, pcz, cz1); };
     auto aux = [&](int x) { return ld_(A.aux[x] + o); };
 
     const double r = G.rcol[i], ir = G.ircol[i];
@@ -93,6 +99,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     // stage use the derivative arrays of the previous ``auxiliary`` call, so
     // the branch follows the time of that call (A.t0), not the current one.
     double Dr_phi, Dz_phi, Drr_phi, Dzz_phi, Drz_phi, ipsi4, phi_c = 0.0;
+    double Dr_chi = 0.0, Dz_chi = 0.0;
     if (A.t0) {
         const Deriv5 dp = D5(F_PHI);
         Dr_phi = dp.r; Dz_phi = dp.z; Drr_phi = dp.rr; Dzz_phi = dp.zz; Drz_phi = dp.rz;
@@ -102,13 +109,17 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
         ipsi4 = one / (psi2 * psi2);
     } else {
         const Deriv5 dc = D5(F_CHI);
+        Dr_chi = dc.r; Dz_chi = dc.z;
+        // phi = -log(chi)/2: D phi = -D chi/(2 chi),
+        // DD phi = -DD chi/(2 chi) + (D chi/chi)(D chi/chi)/2
         const double ichi = one / chi;
+        const double nhi = -half * ichi;
+        Dr_phi = dc.r * nhi;
+        Dz_phi = dc.z * nhi;
         const double xr = dc.r * ichi, xz = dc.z * ichi;
-        Dr_phi = -half * xr;
-        Dz_phi = -half * xz;
-        Drr_phi = -half * (dc.rr * ichi - xr * xr);
-        Dzz_phi = -half * (dc.zz * ichi - xz * xz);
-        Drz_phi = -half * (dc.rz * ichi - xr * xz);
+        Drr_phi = dc.rr * nhi - Dr_phi * xr;
+        Dzz_phi = dc.zz * nhi - Dz_phi * xz;
+        Drz_phi = dc.rz * nhi - Dr_phi * xz;
         ipsi4 = chi * chi;  // 1/psi^4 with psi = chi^(-1/2)
     }
 
@@ -179,7 +190,6 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
     }
 
     // ---- geometric sources (sources_geometry.f90, BSSN)
-    const double sigma = 1.0;  // lagrangian flavour
     double s_phi = -sixth * alpha * trK;
     double s_chi = 2.0 * sixth * alpha * chi * trK;
     double s_A = -two * alpha * kA, s_B = -two * alpha * kB, s_H = -two * alpha * kH, s_C = -two * alpha * kC;
@@ -200,79 +210,82 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
         const Deriv5 dbR = D5(F_BETAR), dbZ = D5(F_BETAZ);
         const bool adv = P.shiftadvect != 0;
         const bool negr = br <= 0.0, negz = bz <= 0.0;
-        auto DAr = [&](int f, const double dr_) { return adv ? dadv(A.in[f] + o, 1, i, nr, g, negr, G.idr, false) : dr_; };
-        auto DAz = [&](int f, const double dz_) { return adv ? dadv(A.in[f] + o, ld, j, nz, g, negz, G.idz, true) : dz_; };
+        // Advection term beta^r D_r f + beta^z D_z f with lopsided derivatives
+        // (derivadvect.f90).  Inside i = 4-ghost..Nr-3 the two upwind
+        // stencils are one 5-point sum taken with the stride pointing against
+        // the shift, and beta times its scale is -|beta|/(12 h) for either
+        // sign, so each field costs one stencil and one FMA per direction.
+        const bool lint_r = (i >= 4 - g && i <= nr - 3), lint_z = (j >= 4 - g && j <= nz - 3);
+        const long lsr = negr ? -1 : 1, lsz = negz ? -ld : ld;
+        const double kr = -fabs(br) * (G.idr * (1.0 / 12.0)), kz = -fabs(bz) * (G.idz * (1.0 / 12.0));
+        auto lop = [&](const double* p, long st) {
+            return 3.0 * ld_(p - st) + 10.0 * ld_(p) - 18.0 * ld_(p + st) + 6.0 * ld_(p + 2 * st) - ld_(p + 3 * st);
+        };
+        auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * dadv(p, 1, i, nr, g, negr, G.idr, false); };
+        auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ld, j, nz, g, negz, G.idz, true); };
+        auto ADV = [&](int f, double dr_, double dz_) {
+            if (!adv) return br * dr_ + bz * dz_;
+            const double* p = A.in[f] + o;
+            return ladv_r(p) + ladv_z(p);
+        };
         // DD_beta_rr = d/dr (beta_r / r): first derivative of beta_r/r
         double DD_beta_rr;
         {
             const double* pb = A.in[F_BETAR] + o;
             const double* ic = G.ircol + i;
             auto q = [&](int m) { return ld_(pb + m) * ic[m]; };
-            if (kr == 0) DD_beta_rr = cr1 * (8.0 * (q(1) - q(-1)) - (q(2) - q(-2)));
-            else if (kr == 1) DD_beta_rr = cr1 * (3.0 * q(1) + 10.0 * q(0) - 18.0 * q(-1) + 6.0 * q(-2) - q(-3));
+            if (pcr == 0) DD_beta_rr = cr1 * (8.0 * (q(1) - q(-1)) - (q(2) - q(-2)));
+            else if (pcr == 1) DD_beta_rr = cr1 * (3.0 * q(1) + 10.0 * q(0) - 18.0 * q(-1) + 6.0 * q(-2) - q(-3));
             else DD_beta_rr = cr1 * (25.0 * q(0) - 48.0 * q(-1) + 36.0 * q(-2) - 16.0 * q(-3) + 3.0 * q(-4));
         }
         const double DIV_beta = dbR.r + dbZ.z + br * ir;
         const double Dr_DIV_beta = dbR.rr + dbZ.rz + DD_beta_rr;
         const double Dz_DIV_beta = dbR.rz + dbZ.zz + dbR.z * ir;
-        const double DAr_al = DAr(F_ALPHA, da.r), DAz_al = DAz(F_ALPHA, da.z);
-        const double DAr_A = DAr(F_A, dA.r), DAz_A = DAz(F_A, dA.z);
-        const double DAr_B = DAr(F_B, dB.r), DAz_B = DAz(F_B, dB.z);
-        const double DAr_H = DAr(F_H, dH.r), DAz_H = DAz(F_H, dH.z);
-        const double DAr_C = DAr(F_C, dC.r), DAz_C = DAz(F_C, dC.z);
-        const double DAr_tK = DAr(F_TRK, Dr_trK), DAz_tK = DAz(F_TRK, Dz_trK);
-        const double DAr_kA = DAr(F_KTA, Dr_KTA), DAz_kA = DAz(F_KTA, Dz_KTA);
-        const double DAr_kB = DAr(F_KTB, Dr_KTB), DAz_kB = DAz(F_KTB, Dz_KTB);
-        const double DAr_kC = DAr(F_KTC, Dr_KTC), DAz_kC = DAz(F_KTC, Dz_KTC);
-        const double DAr_Dr = DAr(F_DLR, Dr_Dlr), DAz_Dr = DAz(F_DLR, Dz_Dlr);
-        const double DAr_Dz = DAr(F_DLZ, Dr_Dlz), DAz_Dz = DAz(F_DLZ, Dz_Dlz);
+        // sigma = 1 (lagrangian): the -2/3 sigma f DIV_beta terms
+        const double tdb = (2.0 / 3.0) * DIV_beta;
         if (A.t0) {
-            const double DAr_ph = DAr(F_PHI, Dr_phi), DAz_ph = DAz(F_PHI, Dz_phi);
-            s_phi = s_phi + br * DAr_ph + bz * DAz_ph + sixth * sigma * DIV_beta;
+            s_phi = s_phi + ADV(F_PHI, Dr_phi, Dz_phi) + sixth * DIV_beta;
             // chi's lopsided derivatives are not formed while the level time is
             // zero (the t=0 branch of auxiliary_geometry.f90:178-202 only
             // differentiates phi), so the advection term of chi reads zeros
-            s_chi = s_chi - sigma * 2.0 * sixth * chi * DIV_beta;
+            s_chi = s_chi - chi * (0.5 * tdb);
         } else {
-            const double dchr = d1(A.in[F_CHI] + o, 1, kr, cr1), dchz = d1(A.in[F_CHI] + o, ld, kz, cz1);
-            const double DAr_ch = DAr(F_CHI, dchr), DAz_ch = DAz(F_CHI, dchz);
-            s_chi = s_chi + br * DAr_ch + bz * DAz_ch - sigma * 2.0 * sixth * chi * DIV_beta;
+            s_chi = s_chi + ADV(F_CHI, Dr_chi, Dz_chi) - chi * (0.5 * tdb);
         }
         const double Drb = dbR.r, Dzb = dbR.z, Drbz = dbZ.r, Dzbz = dbZ.z;
-        s_A = s_A + br * DAr_A + bz * DAz_A + two * (Ac * Drb + r * Cc * Drbz) - two * third * sigma * Ac * DIV_beta;
-        s_B = s_B + br * DAr_B + bz * DAz_B + two * (Bc * Dzbz + r * Cc * Dzb) - two * third * sigma * Bc * DIV_beta;
-        s_H = s_H + br * DAr_H + bz * DAz_H + two * Hc * br * ir - two * third * sigma * Hc * DIV_beta;
-        s_C = s_C + br * DAr_C + bz * DAz_C + Cc * br * ir + Cc * (Drb + Dzbz) + (Bc * Drbz + Ac * Dzb) * ir
-            - two * third * sigma * Cc * DIV_beta;
-        s_trK = s_trK + br * DAr_tK + bz * DAz_tK;
-        s_KTA = s_KTA + br * DAr_kA + bz * DAz_kA + two * (kA * Drb + r * kC * Drbz) - two * third * sigma * kA * DIV_beta;
-        s_KTB = s_KTB + br * DAr_kB + bz * DAz_kB + two * (kB * Dzbz + r * kC * Dzb) - two * third * sigma * kB * DIV_beta;
-        s_KTC = s_KTC + br * DAr_kC + bz * DAz_kC + kC * br * ir + kC * (Drb + Dzbz) + (kB * Drbz + kA * Dzb) * ir
-            - two * third * sigma * kC * DIV_beta;
-        s_Dlr = s_Dlr + br * DAr_Dr + bz * DAz_Dr - Dlr * Drb - Dlz * Dzb;
-        s_Dlr = s_Dlr + two * r * gC * dbR.rz + gA * dbR.rr + gB * dbR.zz + gH * DD_beta_rr;
-        s_Dlr = s_Dlr + third * sigma * (gA * Dr_DIV_beta + r * gC * Dz_DIV_beta + two * Dlr * DIV_beta);
-        s_Dlz = s_Dlz + br * DAr_Dz + bz * DAz_Dz - Dlr * Drbz - Dlz * Dzbz;
-        s_Dlz = s_Dlz + two * r * gC * dbZ.rz + gA * dbZ.rr + gB * dbZ.zz + gH * Drbz * ir;
-        s_Dlz = s_Dlz + third * sigma * (r * gC * Dr_DIV_beta + gB * Dz_DIV_beta + two * Dlz * DIV_beta);
-        s_alpha = s_alpha + br * DAr_al + bz * DAz_al;
+        const double rDrbz = r * Drbz, rDzb = r * Dzb, Dsum = Drb + Dzbz, bir = br * ir;
+        s_A = s_A + ADV(F_A, dA.r, dA.z) + two * (Ac * Drb + Cc * rDrbz) - Ac * tdb;
+        s_B = s_B + ADV(F_B, dB.r, dB.z) + two * (Bc * Dzbz + Cc * rDzb) - Bc * tdb;
+        s_H = s_H + ADV(F_H, dH.r, dH.z) + Hc * (two * bir - tdb);
+        s_C = s_C + ADV(F_C, dC.r, dC.z) + Cc * (bir + Dsum - tdb) + (Bc * Drbz + Ac * Dzb) * ir;
+        s_trK = s_trK + ADV(F_TRK, Dr_trK, Dz_trK);
+        s_KTA = s_KTA + ADV(F_KTA, Dr_KTA, Dz_KTA) + two * (kA * Drb + kC * rDrbz) - kA * tdb;
+        s_KTB = s_KTB + ADV(F_KTB, Dr_KTB, Dz_KTB) + two * (kB * Dzbz + kC * rDzb) - kB * tdb;
+        s_KTC = s_KTC + ADV(F_KTC, Dr_KTC, Dz_KTC) + kC * (bir + Dsum - tdb) + (kB * Drbz + kA * Dzb) * ir;
+        const double rgC = r * gC;
+        s_Dlr = s_Dlr + ADV(F_DLR, Dr_Dlr, Dz_Dlr) - Dlr * Drb - Dlz * Dzb;
+        s_Dlr = s_Dlr + two * rgC * dbR.rz + gA * dbR.rr + gB * dbR.zz + gH * DD_beta_rr;
+        s_Dlr = s_Dlr + third * (gA * Dr_DIV_beta + rgC * Dz_DIV_beta) + Dlr * tdb;
+        s_Dlz = s_Dlz + ADV(F_DLZ, Dr_Dlz, Dz_Dlz) - Dlr * Drbz - Dlz * Dzbz;
+        s_Dlz = s_Dlz + two * rgC * dbZ.rz + gA * dbZ.rr + gB * dbZ.zz + gH * Drbz * ir;
+        s_Dlz = s_Dlz + third * (rgC * Dr_DIV_beta + gB * Dz_DIV_beta) + Dlz * tdb;
+        s_alpha = s_alpha + ADV(F_ALPHA, da.r, da.z);
         s_br = dbr;
         s_bz = dbz;
         if (P.driveradv) {
-            s_br = s_br + br * DAr(F_BETAR, dbR.r) + bz * DAz(F_BETAR, dbR.z);
-            s_bz = s_bz + br * DAr(F_BETAZ, dbZ.r) + bz * DAz(F_BETAZ, dbZ.z);
+            s_br = s_br + ADV(F_BETAR, dbR.r, dbR.z);
+            s_bz = s_bz + ADV(F_BETAZ, dbZ.r, dbZ.z);
         }
         (void)s_dbr; (void)s_dbz;
         if constexpr (SCALAR) {
             // auxiliary_matter.f90 always forms lopsided derivatives for the
             // scalar field when a shift is present (independent of shiftadvect)
-            auto LAr = [&](int f) { return dadv(A.in[f] + o, 1, i, nr, g, negr, G.idr, false); };
-            auto LAz = [&](int f) { return dadv(A.in[f] + o, ld, j, nz, g, negz, G.idz, true); };
+            auto LADV = [&](int f) { const double* p = A.in[f] + o; return ladv_r(p) + ladv_z(p); };
             const double sxr = val(F_SXIR), sxz = val(F_SXIZ);
             s_sphi = s_sphi + br * sxr + bz * sxz;
-            s_sxr = s_sxr + br * LAr(F_SXIR) + sxr * Drb + bz * LAz(F_SXIR) + sxz * Drbz;
-            s_sxz = s_sxz + br * LAr(F_SXIZ) + sxr * Dzb + bz * LAz(F_SXIZ) + sxz * Dzbz;
-            s_spi = s_spi + br * LAr(F_SPI) + bz * LAz(F_SPI);
+            s_sxr = s_sxr + LADV(F_SXIR) + sxr * Drb + sxz * Drbz;
+            s_sxz = s_sxz + LADV(F_SXIZ) + sxr * Dzb + sxz * Dzbz;
+            s_spi = s_spi + LADV(F_SPI);
         }
     }
     if constexpr (SCALAR) {
@@ -311,6 +324,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
         const double kd = P.geodiss / G.dt * (1.0 / 20.0);
         auto diss = [&](int f, double& s) {
             const double* p = A.in[f] + o;
+            if (diss_r && diss_z) { s = ko6rz_apply(p, ld, kd, s); return; }
             if (diss_r) s = s - kd * ko6(p, 1);
             if (diss_z) s = s - kd * ko6(p, ld);
         };
@@ -326,6 +340,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
             const double kd = P.scalardiss / G.dt * (1.0 / 20.0);
             auto diss = [&](int f, double& s) {
                 const double* p = A.in[f] + o;
+                if (diss_r && diss_z) { s = ko6rz_apply(p, ld, kd, s); return; }
                 if (diss_r) s = s - kd * ko6(p, 1);
                 if (diss_z) s = s - kd * ko6(p, ld);
             };
@@ -416,7 +431,7 @@ __global__ void __launch_bounds__(128) rhs_kernel(const __grid_constant__ StageA
 }  // namespace
 
 void launch_rhs(const StageArgs& a, cudaStream_t s) {
-    dim3 blk(32, 4);
+    dim3 blk(32, OLLIN_RHS_THREADS / 32);
     const int nj = a.G.nz - a.G.jlo + 1;
     dim3 grd((a.G.nr + blk.x - 1) / blk.x, (nj + blk.y - 1) / blk.y);
     const bool sh = a.P.shift != 0, sc = a.P.scalar != 0;

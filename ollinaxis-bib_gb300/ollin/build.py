@@ -12,7 +12,7 @@ import subprocess
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(CSRC, "_build")
-LIB = os.path.join(BUILD, "libollin_gpu.so")
+LIB = os.environ.get("OLLIN_GPU_LIB") or os.path.join(BUILD, "libollin_gpu.so")
 SOURCES = ["rhs.cu", "aux.cu", "transfer.cu", "noalloc.cu", "host.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
