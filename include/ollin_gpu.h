@@ -66,6 +66,16 @@ extern "C" {
 #define OLLIN_IDATA_MINKOWSKI       0   /* idata = "minkowski"      */
 #define OLLIN_IDATA_SCHWARZSCHILD   1   /* idata = "schwarzschild"  */
 #define OLLIN_IDATA_BRILLLINDQUIST  2   /* idata = "BrillLindquist" (one hole) */
+#define OLLIN_IDATA_BRILLWAVE       3   /* idata = "BrillWave" (brilltype = "Holz"), elliptic */
+#define OLLIN_IDATA_SCALARPULSE     4   /* idata = "scalarpulse" (mattertype = "scalar"), elliptic */
+
+#define OLLIN_ELL_NONE          0   /* ELL_solver = "none" */
+#define OLLIN_ELL_WAVE          1   /* ELL_solver = "wave" (WaveElliptic, the default) */
+#define OLLIN_ELL_SOR           2   /* ELL_solver = "sor"  */
+
+#define OLLIN_PULSE_SHELL       0   /* scalarpulse_type = "shell"     */
+#define OLLIN_PULSE_TORUS       1   /* scalarpulse_type = "torus"     */
+#define OLLIN_PULSE_BAUMGARTE   2   /* scalarpulse_type = "Baumgarte" */
 
 #define OLLIN_ILAPSE_ONE        0   /* ilapse = "one"       */
 #define OLLIN_ILAPSE_ISOTROPIC  1   /* ilapse = "isotropic" */
@@ -112,6 +122,19 @@ typedef struct ollin_params {
     int    idata;              /* OLLIN_IDATA_* */
     int    ilapse;             /* OLLIN_ILAPSE_* */
     double bh1mass;
+    /* elliptic initial data (appended; earlier offsets are unchanged):
+     * solver controls param.f90:454-491, Brill waves :573-582, scalar pulse
+     * :623-643 */
+    int    ell_solver;         /* OLLIN_ELL_* */
+    int    ell_maxiter;        /* ELL_maxiter */
+    double ell_epsilon;        /* ELL_epsilon */
+    int    we_method;          /* WE_method: OLLIN_INTEGRATOR_* */
+    int    we_maxiter;         /* WE_maxiter */
+    double we_eta, we_diss, we_dtfac, we_epsilon;
+    int    scalarpulse_type;   /* OLLIN_PULSE_* */
+    int    brilltype;          /* 0 = "Holz" */
+    double scalar_a0, scalar_r0, scalar_z0, scalar_sr0, scalar_sz0;
+    double brill_a0, brill_sr0, brill_sz0;
 } ollin_params;
 
 /* Evolved and auxiliary fields addressable by upload/download.  The names are

@@ -114,6 +114,8 @@ int check_params(const ollin_params& P) {
     if (P.mattertype != OLLIN_MATTER_VACUUM && P.mattertype != OLLIN_MATTER_SCALAR) return fail(OLLIN_EINVAL, "unknown mattertype");
     if (P.boundtype != OLLIN_BOUND_RADIATIVE && P.boundtype != OLLIN_BOUND_NONE) return fail(OLLIN_EINVAL, "unknown boundtype");
     if (!(P.dr0 > 0 && P.dz0 > 0 && P.dtfac > 0)) return fail(OLLIN_EINVAL, "dr0, dz0 and dtfac must be positive");
+    if (P.idata != OLLIN_IDATA_MINKOWSKI && P.idata != OLLIN_IDATA_SCHWARZSCHILD && P.idata != OLLIN_IDATA_BRILLLINDQUIST)
+        return fail(OLLIN_EINVAL, "idata must be minkowski, schwarzschild or BrillLindquist");
     return OLLIN_OK;
 }
 
@@ -546,6 +548,12 @@ void ollin_params_default(ollin_params* p) {
     p->boundtype = OLLIN_BOUND_RADIATIVE; p->interp_bicubic = 1;
     p->mattertype = OLLIN_MATTER_VACUUM; p->scalarpotential = OLLIN_POTENTIAL_NONE;
     p->idata = OLLIN_IDATA_MINKOWSKI; p->ilapse = OLLIN_ILAPSE_ONE; p->bh1mass = 1.0;
+    p->ell_solver = OLLIN_ELL_WAVE; p->ell_maxiter = 100000; p->ell_epsilon = 1.0e-8;
+    p->we_method = OLLIN_INTEGRATOR_ICN; p->we_maxiter = 100000;
+    p->we_eta = 0.0; p->we_diss = 0.1; p->we_dtfac = 0.6; p->we_epsilon = 1.0e-8;
+    p->scalarpulse_type = OLLIN_PULSE_SHELL; p->brilltype = 0;
+    p->scalar_a0 = 0.0; p->scalar_r0 = 0.0; p->scalar_z0 = 0.0; p->scalar_sr0 = 1.0; p->scalar_sz0 = 1.0;
+    p->brill_a0 = 0.0; p->brill_sr0 = 1.0; p->brill_sz0 = 1.0;
 }
 
 const char* ollin_gpu_last_error(void) { return g_err.c_str(); }

@@ -31,6 +31,14 @@ class Params(ctypes.Structure):
         ("mattertype", ctypes.c_int), ("scalarpotential", ctypes.c_int),
         ("scalar_mass", ctypes.c_double), ("scalar_lambda", ctypes.c_double),
         ("idata", ctypes.c_int), ("ilapse", ctypes.c_int), ("bh1mass", ctypes.c_double),
+        ("ell_solver", ctypes.c_int), ("ell_maxiter", ctypes.c_int), ("ell_epsilon", ctypes.c_double),
+        ("we_method", ctypes.c_int), ("we_maxiter", ctypes.c_int),
+        ("we_eta", ctypes.c_double), ("we_diss", ctypes.c_double), ("we_dtfac", ctypes.c_double),
+        ("we_epsilon", ctypes.c_double),
+        ("scalarpulse_type", ctypes.c_int), ("brilltype", ctypes.c_int),
+        ("scalar_a0", ctypes.c_double), ("scalar_r0", ctypes.c_double), ("scalar_z0", ctypes.c_double),
+        ("scalar_sr0", ctypes.c_double), ("scalar_sz0", ctypes.c_double),
+        ("brill_a0", ctypes.c_double), ("brill_sr0", ctypes.c_double), ("brill_sz0", ctypes.c_double),
     ]
 
 
@@ -40,7 +48,10 @@ SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3}
 BOUND = {"radiative": 0, "none": 1}
 MATTER = {"vacuum": 0, "scalar": 1}
 POTENTIAL = {"none": 0, "phi2": 1, "phi4": 2}
-IDATA = {"minkowski": 0, "schwarzschild": 1, "BrillLindquist": 2}
+IDATA = {"minkowski": 0, "schwarzschild": 1, "BrillLindquist": 2, "BrillWave": 3, "scalarpulse": 4}
+ELL_SOLVER = {"none": 0, "wave": 1, "sor": 2}
+PULSE = {"shell": 0, "torus": 1, "Baumgarte": 2}
+BRILLTYPE = {"Holz": 0}
 ILAPSE = {"one": 0, "isotropic": 1, "psiminus2": 2, "psiminus4": 3}
 
 # field ids of enum ollin_field
@@ -77,13 +88,25 @@ def default_params():
     p.mattertype, p.scalarpotential = MATTER["vacuum"], POTENTIAL["none"]
     p.scalar_mass, p.scalar_lambda = 0.0, 0.0
     p.idata, p.ilapse, p.bh1mass = IDATA["minkowski"], ILAPSE["one"], 1.0
+    p.ell_solver, p.ell_maxiter, p.ell_epsilon = ELL_SOLVER["wave"], 100000, 1.0e-8
+    p.we_method, p.we_maxiter = INTEGRATOR["icn"], 100000
+    p.we_eta, p.we_diss, p.we_dtfac, p.we_epsilon = 0.0, 0.1, 0.6, 1.0e-8
+    p.scalarpulse_type, p.brilltype = PULSE["shell"], BRILLTYPE["Holz"]
+    p.scalar_a0, p.scalar_r0, p.scalar_z0 = _single(0.0), _single(0.0), _single(0.0)
+    p.scalar_sr0, p.scalar_sz0 = _single(1.0), _single(1.0)
+    p.brill_a0, p.brill_sr0, p.brill_sz0 = _single(0.0), _single(1.0), _single(1.0)
     return p
 
 
 _ENUMS = {"integrator": INTEGRATOR, "slicing": SLICING, "shift": SHIFT, "boundtype": BOUND,
-          "mattertype": MATTER, "scalarpotential": POTENTIAL, "idata": IDATA, "ilapse": ILAPSE}
-_RENAME = {"Nrtotal": "nrtotal", "Nztotal": "nztotal", "Nl0": "nl0", "BH1mass": "bh1mass"}
-_IGNORED = {"Nt", "Ninfo", "Noutput0D", "Noutput1D", "Noutput2D", "outvars0D", "outvars1D",
+          "mattertype": MATTER, "scalarpotential": POTENTIAL, "idata": IDATA, "ilapse": ILAPSE,
+          "ell_solver": ELL_SOLVER, "we_method": INTEGRATOR, "scalarpulse_type": PULSE,
+          "brilltype": BRILLTYPE}
+_RENAME = {"Nrtotal": "nrtotal", "Nztotal": "nztotal", "Nl0": "nl0", "BH1mass": "bh1mass",
+           "ELL_solver": "ell_solver", "ELL_maxiter": "ell_maxiter", "ELL_epsilon": "ell_epsilon",
+           "WE_method": "we_method", "WE_maxiter": "we_maxiter", "WE_eta": "we_eta",
+           "WE_diss": "we_diss", "WE_dtfac": "we_dtfac", "WE_epsilon": "we_epsilon"}
+_IGNORED = {"Nt", "Ninfo", "ELL_verbose", "ELL_Noutput", "WE_verbose", "WE_Noutput", "Noutput0D", "Noutput1D", "Noutput2D", "outvars0D", "outvars1D",
             "outvars2D", "directory", "Nb", "checkpoint", "outparallel", "commenttype"}
 
 

@@ -23,6 +23,9 @@ int ollin_oracle_aux(ollin_oracle* o, int level);
 int ollin_oracle_constraints(ollin_oracle* o, int level);
 int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]);
 double ollin_oracle_point_updates(const ollin_oracle* o);
+/* iteration counts of the last elliptic solve on this thread: steps[0] of
+ * the coarse phase, steps[1] of the all-level phase (0 if there was none) */
+int ollin_oracle_ell_stats(int steps[2], double* gres);
 #ifdef __cplusplus
 }
 #endif

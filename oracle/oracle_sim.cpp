@@ -97,18 +97,22 @@ static void setup(Sim& S) {
 static inline size_t hr(const Level& L, int m, int j, int k) { return (size_t)m + (size_t)L.g * ((size_t)(j - 1 + L.g) + (size_t)(L.Nz + L.g) * k); }
 static inline size_t hz(const Level& L, int i, int n, int k) { return (size_t)(i - 1 + L.g) + (size_t)(L.Nr + L.g) * ((size_t)n + (size_t)L.g * k); }
 
-static void currentgrid(Sim& S, Level& L) { L.time = S.t[L.level]; }
+void currentgrid(Sim& S, Level& L) { L.time = S.t[L.level]; }
 
 // ---------------------------------------------------------------------------
 // generated per-array routines
 // ---------------------------------------------------------------------------
-static void saveold(Sim& S, Level& L) {
+void saveold(Sim& S, Level& L) {
     const int g = L.g, Nr = L.Nr, Nz = L.Nz;
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name);
         L.a(e.name + "_p") = v;
         auto& rL = L.hist[e.name + "_rL"]; auto& rR = L.hist[e.name + "_rR"];
         auto& zL = L.hist[e.name + "_zL"]; auto& zR = L.hist[e.name + "_zR"];
+        if (rL.empty()) {  // a variable evolved only here (the elliptic solver's ell_u, ell_v)
+            const size_t nr_hist = (size_t)g * (Nz + g) * 3, nz_hist = (size_t)(Nr + g) * g * 3;
+            rL.assign(nr_hist, 0.0); rR.assign(nr_hist, 0.0); zL.assign(nz_hist, 0.0); zR.assign(nz_hist, 0.0);
+        }
         for (int i = 0; i <= g - 1; ++i) {
             for (int j = 1 - g; j <= Nz; ++j) {
                 rL[hr(L, i, j, 2)] = rL[hr(L, i, j, 1)]; rL[hr(L, i, j, 1)] = rL[hr(L, i, j, 0)]; rL[hr(L, i, j, 0)] = v(1 - g + i, j);
@@ -122,7 +126,7 @@ static void saveold(Sim& S, Level& L) {
     }
 }
 
-static void accumulate(Sim& S, Level& L, int k, int niter, double w) {
+void accumulate(Sim& S, Level& L, int k, int niter, double w) {
     const bool first = (k == 1), last = (k == niter);
     for (const EvolvedVar& e : S.evolved) {
         Arr& a = L.a(e.name + "_a"); Arr& s = L.a("s" + e.name);
@@ -136,7 +140,7 @@ static void accumulate(Sim& S, Level& L, int k, int niter, double w) {
     }
 }
 
-static void update(Sim& S, Level& L, double dtw) {
+void update(Sim& S, Level& L, double dtw) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name); Arr& vp = L.a(e.name + "_p"); Arr& s = L.a("s" + e.name);
         const size_t n = v.v.size();
@@ -144,7 +148,7 @@ static void update(Sim& S, Level& L, double dtw) {
     }
 }
 
-static void symmetries_r(Sim& S, Level& L) {
+void symmetries_r(Sim& S, Level& L) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name);
         for (int i = 1; i <= L.g; ++i)
@@ -152,7 +156,7 @@ static void symmetries_r(Sim& S, Level& L) {
     }
 }
 
-static void symmetries_z(Sim& S, Level& L) {
+void symmetries_z(Sim& S, Level& L) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name);
         for (int j = 1; j <= L.g; ++j)
@@ -163,7 +167,7 @@ static void symmetries_z(Sim& S, Level& L) {
 // ---------------------------------------------------------------------------
 // interp.f90:2-270 -- value of one grid function of (box 0, level) at (r0,z0)
 // ---------------------------------------------------------------------------
-static double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
+double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
     Level& L = S.L[level];
     const int g = L.g;
     const double small = 1.0e-10;
@@ -213,7 +217,7 @@ static double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
 // ---------------------------------------------------------------------------
 // finebound.f90:2-407 (all=.true.) with the generated bound_interp.inc
 // ---------------------------------------------------------------------------
-static void finebound(Sim& S, int level, double dtw) {
+void finebound(Sim& S, int level, double dtw) {
     Level& F = S.L[level];
     const int g = F.g;
     const int bbox_level = level - 1;
@@ -276,7 +280,7 @@ static void finebound(Sim& S, int level, double dtw) {
 }
 
 // restrict.f90:2-169 with restrict_interp.inc
-static void restrict_(Sim& S, int level) {
+void restrict_(Sim& S, int level) {
     Level& F = S.L[level];
     Level& Cl = S.L[level - 1];
     const int g = F.g;
@@ -392,6 +396,13 @@ static void initial(Sim& S) {
                 }
         }
         (void)psi2;
+    }
+    // elliptic initial data (initial.f90:336-341, 380-394)
+    if (P.idata == OLLIN_IDATA_BRILLWAVE) idata_brillwave(S);
+    if (P.idata == OLLIN_IDATA_SCALARPULSE) {
+        if (P.mattertype != OLLIN_MATTER_SCALAR)
+            throw std::runtime_error("Scalar pulse initial data needs scalar field type matter.");
+        idata_scalarpulse(S);
     }
     if (P.factorhdet) {  // initial.f90:528-577
         for (Level& L : S.L) {
@@ -589,5 +600,12 @@ int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[
 }
 
 double ollin_oracle_point_updates(const ollin_oracle* o) { return o->S.point_updates; }
+
+int ollin_oracle_ell_stats(int steps[2], double* gres) {
+    steps[0] = g_ell_stats.steps[0];
+    steps[1] = g_ell_stats.steps[1];
+    if (gres) *gres = g_ell_stats.gres;
+    return g_ell_stats.phases;
+}
 
 }  // extern "C"

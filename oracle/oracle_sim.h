@@ -49,5 +49,30 @@ void radiative_geometry(Sim& S, Level& L);
 void constraints(Sim& S, Level& L);
 void diff1r(Level& L, const Arr& f, Arr& d, int symr);
 void diff1z(Level& L, const Arr& f, Arr& d, int symz);
+void diff2r(Level& L, const Arr& f, Arr& d, int symr);
+void diff2z(Level& L, const Arr& f, Arr& d, int symz);
+void dissipation(Level& L, const Arr& ev, Arr& src, int symr, int symz, double diss);
+void radbound(Level& L, const Arr& ev, Arr& src, const Arr& Dr_var, const Arr& Dz_var, double v, double var0);
+void potential(Sim& S, Level& L);
+
+// Berger-Oliger machinery over the variables listed in Sim::evolved
+// (oracle_sim.cpp)
+void currentgrid(Sim& S, Level& L);
+void saveold(Sim& S, Level& L);
+void accumulate(Sim& S, Level& L, int k, int niter, double w);
+void update(Sim& S, Level& L, double dtw);
+void symmetries_r(Sim& S, Level& L);
+void symmetries_z(Sim& S, Level& L);
+double interp(Sim& S, int level, const Arr& var, double r0, double z0);
+void finebound(Sim& S, int level, double dtw);
+void restrict_(Sim& S, int level);
+
+// elliptic initial data (oracle_elliptic.cpp)
+void idata_scalarpulse(Sim& S);
+void idata_brillwave(Sim& S);
+
+// solver statistics of the last elliptic solve: iterations of each phase
+struct EllStats { int steps[2] = {0, 0}; int phases = 0; double gres = 0.0; };
+extern thread_local EllStats g_ell_stats;
 
 }  // namespace oracle

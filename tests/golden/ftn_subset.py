@@ -689,6 +689,10 @@ class Unit:
         label_stack = []
         for st in exec_stmts:
             self._stmt(st, emit, ind, stack)
+        while stack and isinstance(stack[-1], tuple) and stack[-1][0] == "label":
+            emit("break")
+            ind[0] = ind[0][:-4]
+            stack.pop()
         if self.kind == "function":
             for nm in sorted(self.save_vars):
                 emit("_S[%r] = L_%s" % (nm, nm))
@@ -777,6 +781,28 @@ class Unit:
         if re.match(r"^end\s*if$", st):
             pop()
             stack.pop()
+            return
+        m = re.match(r"^do\s+while\s*(\(.*\))$", st)
+        if m:
+            cond, _ = _paren_split(m.group(1))
+            emit("while %s:" % self.parse_expr(cond))
+            push()
+            stack.append("while")
+            return
+        # "NNN continue" that a later "goto NNN" jumps back to: the rest of
+        # the routine becomes the body of a loop that the goto restarts
+        m = re.match(r"^(\d+)\s+continue$", st)
+        if m:
+            emit("while True:")
+            push()
+            stack.append(("label", m.group(1)))
+            return
+        m = re.match(r"^go\s*to\s+(\d+)$", st)
+        if m:
+            open_loops = [e for e in stack if e == "while" or (isinstance(e, tuple) and e[0] in ("do", "label"))]
+            if not open_loops or open_loops[-1] != ("label", m.group(1)):
+                raise SyntaxError("only a backward goto to an enclosing 'NNN continue' is supported")
+            emit("continue")
             return
         m = re.match(r"^do\s+([a-z_]\w*)\s*=\s*(.*)$", st)
         if m:

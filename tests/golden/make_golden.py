@@ -10,8 +10,9 @@ Each fixture stores, for a small box-in-box configuration, the reference's
 grid functions (all points including ghosts, Fortran (i,j) at [i+g-1, j+g-1])
 after 0, 1, 2, ... coarse steps, together with the parameters.  The
 scalar-field case starts from an analytic Gaussian pulse written into the
-arrays after ``initial`` (its elliptic initial-data solve is outside the
-evolution path).
+arrays after ``initial``.  The ``ell_*`` cases run the reference's elliptic
+initial data (idata_scalarpulse.f90 / idata_brillwave.f90 with
+wave_elliptic.f90 or sor_elliptic.f90) inside ``initial``.
 """
 import json
 import os
@@ -43,6 +44,25 @@ CASES = {
                          ilapse="one", mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5,
                          shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, scalardiss=0.02,
                          _steps=[0, 1, 3]),
+    # elliptic initial data (WaveElliptic, the default ELL_solver): a centred
+    # scalar pulse solved to convergence on one level
+    "ell_pulse_1lev": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                           ilapse="one", mattertype="scalar", scalar_a0=0.05, scalardiss=0.02,
+                           _steps=[0], _elliptic=True),
+    # an off-centre shell pulse on two levels (both solver phases: coarse
+    # solve, injection, all-level solve), the wave iterations capped at 150
+    # per phase so that the run is short; then one evolution step
+    "ell_pulse_2lev": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                           ilapse="one", mattertype="scalar", scalar_a0=0.05, scalar_r0=2.0,
+                           scalar_z0=2.0, scalardiss=0.02, we_maxiter=150, _steps=[0, 1],
+                           _elliptic=True),
+    # Holz Brill wave on two levels (factorhdet rescales the metric afterwards)
+    "ell_brill_2lev": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.25, dz0=0.25, idata="BrillWave",
+                           ilapse="one", brill_a0=1.0, we_maxiter=150, _steps=[0], _elliptic=True),
+    # the SOR solver (ELL_solver = "sor"): Robin coarse solve, Dirichlet fine
+    "ell_sor_2lev": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                         ilapse="one", mattertype="scalar", scalar_a0=0.05, ell_solver="sor",
+                         scalardiss=0.02, _steps=[0], _elliptic=True),
 }
 
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
@@ -62,9 +82,24 @@ def scalar_pulse(r, z, a0=0.05):
 def run_case(refdir, name, cfg):
     cfg = dict(cfg)
     steps = cfg.pop("_steps")
+    elliptic = cfg.pop("_elliptic", False)
     sim = RefSim(refdir, cfg)
+    # count the level-0 wave steps of the elliptic solve (one per iteration)
+    wave_iters = [0]
+    if elliptic and hasattr(sim.prog.F, "wavestep"):
+        inner = sim.prog.F.wavestep
+
+        def counted(level, typ, method):
+            if level == 0:
+                wave_iters[0] += 1
+            return inner(level, typ, method)
+        sim.prog.F.wavestep = counted
+    t_ini = time.time()
     sim.initial()
-    if cfg.get("mattertype") == "scalar":
+    if elliptic:
+        print("  %s: initial data in %.1fs, %d wave iterations" % (name, time.time() - t_ini, wave_iters[0]),
+              flush=True)
+    if cfg.get("mattertype") == "scalar" and not elliptic:
         for lev in sim.levels():
             r, z = sim.field(lev, "r"), sim.field(lev, "z")
             ph, xr, xz, pi = scalar_pulse(r, z)
@@ -77,6 +112,11 @@ def run_case(refdir, name, cfg):
     if cfg.get("mattertype") == "scalar":
         names += SCALAR_FIELDS
     out = {}
+    if elliptic:
+        out["wave_iterations"] = np.array(wave_iters[0])
+        for lev in sim.levels():
+            for nm in ("psi", "ell_u", "ell_S1"):
+                out["ell_L%d_%s" % (lev, nm)] = sim.field(lev, nm)
     done = 0
     for target in steps:
         while done < target:

@@ -39,6 +39,8 @@ SOURCES = [
     "src/matter/auxiliary_matter.f90", "src/matter/potential.f90",
     "src/matter/stressenergy.f90", "src/matter/sources_matter.f90",
     "src/matter/scalar.f90",
+    "src/elliptic/wave_elliptic.f90", "src/elliptic/sor_elliptic.f90",
+    "src/matter/idata_scalarpulse.f90", "src/geometry/idata_brillwave.f90",
 ]
 GENERATED = ["saveold.f90", "accumulate.f90", "update.f90", "symmetries_r.f90",
              "symmetries_z.f90"]
@@ -161,7 +163,10 @@ class RefSim:
         prog.define("currentgrid", self._currentgrid)
         prog.define("syncall", lambda: None)
         prog.define("syncboxes", self._unsupported("syncboxes"))
-        for nm in ("idata_kerr", "idata_brillwave", "idata_complexpulse",
+        prog.define("save1dvariable", lambda *a: None)
+        prog.define("save2dvariable", lambda *a: None)
+        prog.define("sync", lambda *a: None)
+        for nm in ("idata_kerr", "idata_complexpulse",
                    "idata_bosonstarcf", "idata_rotboson", "checkpointrestart",
                    "sources_complex", "constraintbound", "simpleboundary"):
             prog.define(nm, self._unsupported(nm))

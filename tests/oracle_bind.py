@@ -45,6 +45,7 @@ def lib():
         L.ollin_oracle_point_updates.argtypes = [vp]
         L.ollin_oracle_point_updates.restype = ctypes.c_double
         L.ollin_oracle_last_error.restype = ctypes.c_char_p
+        L.ollin_oracle_ell_stats.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -115,3 +116,12 @@ class Oracle:
 
     def point_updates(self):
         return self.L.ollin_oracle_point_updates(self.h)
+
+
+def ell_stats():
+    """(coarse-phase iterations, all-level iterations, phases, final residual)
+    of the last elliptic solve of the oracle on this thread."""
+    steps = (ctypes.c_int * 2)()
+    gres = ctypes.c_double()
+    phases = lib().ollin_oracle_ell_stats(steps, ctypes.byref(gres))
+    return steps[0], steps[1], phases, gres.value

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from oracle_bind import Oracle
+from oracle_bind import Oracle, ell_stats
 from parity_util import params, scalar_pulse
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -74,6 +74,65 @@ def test_oracle_matches_reference_fortran(name):
                     err = np.abs(got_i - ref_i).max() / scale
                     assert err <= TOL, "%s step %d level %d %s: rel %.3e" % (name, done, lev, nm, err)
     print("%s: worst relative difference %.2e" % (name, worst))
+
+
+ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev"]
+
+
+def ell_cfg(meta):
+    cfg = cfg_of(meta)
+    for k in list(cfg):
+        if k.startswith("_"):
+            cfg.pop(k)
+    return cfg
+
+
+@pytest.mark.parametrize("name", ELL_CASES)
+def test_oracle_elliptic_data_matches_reference_fortran(name):
+    """Elliptic initial data (idata_scalarpulse.f90 / idata_brillwave.f90 with
+    wave_elliptic.f90 or sor_elliptic.f90) executed by the reference's own
+    Fortran: the solution ell_u on every level including ghosts, the source
+    coefficient, the number of wave iterations, and the evolved state after
+    ``initialize`` and after the stored evolution steps."""
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture %s not generated" % name)
+    d, meta = load(name)
+    cfg = ell_cfg(meta)
+    o = Oracle(params(cfg))
+    o.initial_data()
+    s0, s1, phases, _ = ell_stats()
+    if cfg.get("ell_solver", "wave") == "wave":
+        assert s0 + s1 == int(d["wave_iterations"]), (s0, s1, int(d["wave_iterations"]))
+    for lev in o.levels():
+        for nm in ("ell_u", "psi", "ell_S1"):
+            ref = d["ell_L%d_%s" % (lev, nm)]
+            got = o.get(lev, nm)
+            if nm == "psi":
+                # the fixture holds psi after ``initialize``, whose t=0
+                # auxiliary call rebuilds its ghosts from the symmetric phi
+                ref, got = ref[3:, 3:], got[3:, 3:]
+            scale = max(np.abs(ref).max(), 1e-300)
+            err = np.abs(got - ref).max() / scale
+            assert err <= ELL_TOL, "%s level %d %s: rel %.3e" % (name, lev, nm, err)
+    o.initialize()
+    done = 0
+    for target in meta["steps"]:
+        while done < target:
+            o.step()
+            done += 1
+        for lev in o.levels():
+            for nm in meta["fields"]:
+                ref = d["s%d_L%d_%s" % (done, lev, nm)]
+                got = o.get(lev, nm)
+                scale = max(np.abs(ref).max(), 1e-300)
+                err = np.abs(got - ref).max() / scale
+                assert err <= ELL_TOL, "%s step %d level %d %s: rel %.3e" % (name, done, lev, nm, err)
+
+
+# The elliptic solves run hundreds of wave steps; the libm last-bit
+# differences of the initial data stay at the 1e-13 level through them.
+ELL_TOL = 1e-9
 
 
 def test_golden_fixture_inventory():
