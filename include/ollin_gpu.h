@@ -207,6 +207,13 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
  * Derived fields (OLLIN_F_HAM ...) are computed first (constraints.f90:55-149). */
 int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
 
+/* Iterations of the elliptic solve run by ollin_gpu_initial_data for
+ * idata = BrillWave / scalarpulse (wave_elliptic.f90:190-262): steps[0] in
+ * the coarse-grid phase, steps[1] in the all-level phase (0 with one level);
+ * ``gres`` (may be NULL) receives the final residual.  No counterpart call in
+ * the reference, which prints these numbers. */
+int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres);
+
 /* Total point-updates performed by this handle so far (interior points of
  * each level times the steps taken on it). */
 double ollin_gpu_point_updates(const ollin_handle* h);

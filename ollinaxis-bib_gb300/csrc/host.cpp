@@ -80,6 +80,9 @@ struct ollin_handle {
     size_t ev_used = 0;
     double rhs_point_stages = 0;
     long long rhs_launches = 0;
+    // iterations of the last elliptic solve (coarse phase, all-level phase)
+    int ell_steps[2] = {0, 0};
+    double ell_gres = 0.0;
 };
 
 namespace {
@@ -114,8 +117,12 @@ int check_params(const ollin_params& P) {
     if (P.mattertype != OLLIN_MATTER_VACUUM && P.mattertype != OLLIN_MATTER_SCALAR) return fail(OLLIN_EINVAL, "unknown mattertype");
     if (P.boundtype != OLLIN_BOUND_RADIATIVE && P.boundtype != OLLIN_BOUND_NONE) return fail(OLLIN_EINVAL, "unknown boundtype");
     if (!(P.dr0 > 0 && P.dz0 > 0 && P.dtfac > 0)) return fail(OLLIN_EINVAL, "dr0, dz0 and dtfac must be positive");
-    if (P.idata != OLLIN_IDATA_MINKOWSKI && P.idata != OLLIN_IDATA_SCHWARZSCHILD && P.idata != OLLIN_IDATA_BRILLLINDQUIST)
-        return fail(OLLIN_EINVAL, "idata must be minkowski, schwarzschild or BrillLindquist");
+    if (P.idata < OLLIN_IDATA_MINKOWSKI || P.idata > OLLIN_IDATA_SCALARPULSE) return fail(OLLIN_EINVAL, "unknown idata");
+    if (P.idata == OLLIN_IDATA_SCALARPULSE && P.mattertype != OLLIN_MATTER_SCALAR)
+        return fail(OLLIN_EINVAL, "Scalar pulse initial data needs scalar field type matter.");
+    if ((P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) && P.ell_solver != OLLIN_ELL_WAVE)
+        return fail(OLLIN_EINVAL, "elliptic initial data needs ELL_solver = wave on the device");
+    if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     return OLLIN_OK;
 }
 
@@ -476,12 +483,440 @@ int analysis(ollin_handle* h, int level) {
     return after_launch(h);
 }
 
+// ---------------------------------------------------------------------------
+// Elliptic initial data: WaveElliptic (wave_elliptic.f90) on the device.
+// The solver keeps its own (u, v) arrays per level, rotated like the
+// evolution's state slots, and its own time counters (the reference borrows
+// and restores the global ones, wave_elliptic.f90:95-103, 330-340).
+// ---------------------------------------------------------------------------
+struct WLevel {
+    double* pool = nullptr;
+    double* u[kSlots] = {};
+    double* v[kSlots] = {};
+    double* ua = nullptr; double* va = nullptr;
+    double* S0 = nullptr; double* S1 = nullptr; double* S5 = nullptr;
+    int cur = 0, p = 1, pp = 2;
+    double dt = 0;
+};
+
+struct WaveSolve {
+    ollin_handle* h = nullptr;
+    std::vector<WLevel> W;
+    std::vector<double> t, t1, t2;
+    std::vector<long> s;
+    EllCtl* ctl = nullptr;
+    double* partial = nullptr;
+    int nparts = 0;
+    int Nlmax = 0;
+    int steps[2] = {0, 0};
+    double gres = 0.0;
+    struct Snap {
+        std::vector<int> cur, p, pp;
+        std::vector<double> t, t1, t2;
+        std::vector<long> s;
+    };
+    ~WaveSolve() {
+        for (WLevel& w : W) cudaFree(w.pool);
+        cudaFree(ctl);
+        cudaFree(partial);
+    }
+    Snap snap() const {
+        Snap q;
+        for (const WLevel& w : W) { q.cur.push_back(w.cur); q.p.push_back(w.p); q.pp.push_back(w.pp); }
+        q.t = t; q.t1 = t1; q.t2 = t2; q.s = s;
+        return q;
+    }
+    void restore(const Snap& q) {
+        for (size_t l = 0; l < W.size(); ++l) { W[l].cur = q.cur[l]; W[l].p = q.p[l]; W[l].pp = q.pp[l]; }
+        t = q.t; t1 = q.t1; t2 = q.t2; s = q.s;
+    }
+};
+
+int wave_alloc(ollin_handle* h, WaveSolve& S) {
+    const ollin_params& P = h->P;
+    S.h = h;
+    S.W.resize(h->nlev);
+    S.t.assign(h->nlev, 0.0); S.t1.assign(h->nlev, 0.0); S.t2.assign(h->nlev, 0.0); S.s.assign(h->nlev, 0);
+    const double dt0 = P.we_dtfac * std::min(P.dr0, P.dz0);  // wave_elliptic.f90:148-151
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        const size_t narr = 2 * kSlots + 5;
+        if (cudaMalloc(&w.pool, narr * L.n * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the elliptic solver");
+        CUDA_OR_FAIL(cudaMemsetAsync(w.pool, 0, narr * L.n * sizeof(double), h->stream));
+        double* q = w.pool;
+        for (int k = 0; k < kSlots; ++k) { w.u[k] = q; q += L.n; }
+        for (int k = 0; k < kSlots; ++k) { w.v[k] = q; q += L.n; }
+        w.ua = q; q += L.n; w.va = q; q += L.n;
+        w.S0 = q; q += L.n; w.S1 = q; q += L.n; w.S5 = q; q += L.n;
+        w.dt = dt0 / (double)(1L << l);
+    }
+    S.nparts = wave_stage_blocks(h->L[0].G);
+    if (cudaMalloc(&S.ctl, sizeof(EllCtl)) != cudaSuccess || cudaMalloc(&S.partial, S.nparts * sizeof(double)) != cudaSuccess)
+        return fail(OLLIN_ENOMEM, "device allocation failed for the elliptic solver");
+    return OLLIN_OK;
+}
+
+int wave_symmetry(ollin_handle* h, WaveSolve& S, int level) {
+    DLevel& L = h->L[level];
+    WLevel& w = S.W[level];
+    SymArgs a{};
+    a.G = L.G;
+    a.nf = 2;
+    a.st[0] = base_ptr(L, w.u[w.cur]); a.symr[0] = +1; a.symz[0] = +1;
+    a.st[1] = base_ptr(L, w.v[w.cur]); a.symr[1] = +1; a.symz[1] = +1;
+    a.skip = &S.ctl->done;
+    launch_symmetry(a, h->stream);
+    return after_launch(h);
+}
+
+int wave_prolong(ollin_handle* h, WaveSolve& S, int level, int out, double dtw) {
+    DLevel& F = h->L[level];
+    DLevel& C = h->L[level - 1];
+    WLevel& wf = S.W[level];
+    WLevel& wc = S.W[level - 1];
+    ProlongArgs a{};
+    a.F = F.G;
+    a.Cg = C.G;
+    a.nf = 2;
+    a.fid[0] = 0; a.fid[1] = 1;
+    a.fout[0] = base_ptr(F, wf.u[out]); a.fout[1] = base_ptr(F, wf.v[out]);
+    a.fp[0] = base_ptr(F, wf.u[wf.p]); a.fp[1] = base_ptr(F, wf.v[wf.p]);
+    a.fpp[0] = base_ptr(F, wf.u[wf.pp]); a.fpp[1] = base_ptr(F, wf.v[wf.pp]);
+    a.cin[0] = base_ptr(C, wc.u[wc.cur]); a.cin[1] = base_ptr(C, wc.v[wc.cur]);
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
+    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
+    a.tp = S.t[level - 1];
+    a.t0 = S.t[level];
+    a.tm1 = S.t1[level];
+    a.tl = a.t0 + dtw;
+    a.imax = (a.tp == a.tl) ? h->g + 2 : h->g - 1;  // finebound.f90:106-112
+    a.border = (a.tm1 == 0.0) ? 1 : 2;
+    a.bicubic = h->P.interp_bicubic;
+    a.skip = &S.ctl->done;
+    launch_prolong(a, h->stream);
+    return after_launch(h);
+}
+
+int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
+    DLevel& F = h->L[level];
+    DLevel& C = h->L[level - 1];
+    WLevel& wf = S.W[level];
+    WLevel& wc = S.W[level - 1];
+    RestrictArgs a{};
+    a.F = F.G;
+    a.Cg = C.G;
+    a.nf = 2;
+    a.fid[0] = 0; a.fid[1] = 1;
+    a.fin[0] = base_ptr(F, wf.u[wf.cur]); a.fin[1] = base_ptr(F, wf.v[wf.cur]);
+    a.cout[0] = base_ptr(C, wc.u[wc.cur]); a.cout[1] = base_ptr(C, wc.v[wc.cur]);
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.eqsym = h->P.eqsym;
+    a.bicubic = h->P.interp_bicubic;
+    a.skip = &S.ctl->done;
+    launch_restrict(a, h->stream);
+    return after_launch(h);
+}
+
+// wave_elliptic.f90:347-770 (recursive subroutine wavestep), type = 'flat'
+int wavestep(ollin_handle* h, WaveSolve& S, int level) {
+    const ollin_params& P = h->P;
+    DLevel& L = h->L[level];
+    WLevel& w = S.W[level];
+    w.pp = w.p;
+    w.p = w.cur;
+    int freeslots[2], nfree = 0;
+    for (int k = 0; k < kSlots && nfree < 2; ++k)
+        if (k != w.p && k != w.pp) freeslots[nfree++] = k;
+    const bool rk4 = P.we_method == OLLIN_INTEGRATOR_RK4;
+    const int niter = rk4 ? 4 : P.icniter;
+    const double dt = w.dt;
+    int in = w.p;
+    for (int iter = 1; iter <= niter; ++iter) {
+        double dtw, weight = 0;
+        if (rk4) {
+            switch (iter) {
+                case 1: dtw = 0.5 * dt; weight = 1.0 / 6.0; break;
+                case 2: dtw = 0.5 * dt; weight = 1.0 / 3.0; break;
+                case 3: dtw = dt; weight = 1.0 / 3.0; break;
+                default: dtw = dt; weight = 1.0 / 6.0; break;
+            }
+        } else {
+            dtw = (iter < niter) ? 0.5 * dt : dt;
+        }
+        const int out = freeslots[(iter - 1) & 1];
+        WaveArgs a{};
+        a.G = L.G;
+        a.u_in = base_ptr(L, w.u[in]); a.v_in = base_ptr(L, w.v[in]);
+        a.u_p = base_ptr(L, w.u[w.p]); a.v_p = base_ptr(L, w.v[w.p]);
+        a.u_out = base_ptr(L, w.u[out]); a.v_out = base_ptr(L, w.v[out]);
+        a.u_acc = base_ptr(L, w.ua); a.v_acc = base_ptr(L, w.va);
+        a.S0 = base_ptr(L, w.S0); a.S1 = base_ptr(L, w.S1); a.S5 = base_ptr(L, w.S5);
+        a.eta = P.we_eta;
+        a.kdiss = P.we_diss / dt;
+        a.dtw = dtw;
+        a.weight = weight;
+        a.rk4 = rk4 ? 1 : 0;
+        a.iter = iter;
+        a.niter = niter;
+        a.res_partial = (level == 0 && iter == niter) ? S.partial : nullptr;
+        a.skip = &S.ctl->done;
+        launch_wave_stage(a, h->stream);
+        int rc = after_launch(h);
+        if (rc) return rc;
+        if (level > 0) {
+            rc = wave_prolong(h, S, level, out, dtw);
+            if (rc) return rc;
+        }
+        in = out;
+    }
+    w.cur = in;
+    S.t2[level] = S.t1[level];
+    S.t1[level] = S.t[level];
+    S.s[level] = S.s[level] + 1;
+    S.t[level] = S.t[level] + dt;
+    if (level < S.Nlmax) {
+        int rc = wavestep(h, S, level + 1);
+        if (rc) return rc;
+        rc = wavestep(h, S, level + 1);
+        if (rc) return rc;
+    }
+    if (S.Nlmax > 0) {
+        int rc = wave_symmetry(h, S, level);
+        if (rc) return rc;
+    }
+    if (level > 0 && S.s[level] % 2 == 0) {
+        int rc = wave_restrict(h, S, level);
+        if (rc) return rc;
+        rc = wave_symmetry(h, S, level - 1);
+        if (rc) return rc;
+    }
+    return OLLIN_OK;
+}
+
+// One solver phase: iterate until the stop condition of wave_elliptic.f90:206
+// holds.  Iterations are queued in batches; the device turns the ones after
+// convergence into no-ops, and the host takes back the slot rotation and the
+// time counters of the last iteration that ran.
+int wave_phase(ollin_handle* h, WaveSolve& S, int* steps) {
+    const ollin_params& P = h->P;
+    std::fill(S.t.begin(), S.t.end(), 0.0);
+    std::fill(S.t1.begin(), S.t1.end(), 0.0);
+    std::fill(S.t2.begin(), S.t2.end(), 0.0);
+    std::fill(S.s.begin(), S.s.end(), 0L);
+    EllCtl c{};
+    c.step = 0; c.done = 0; c.miniter = 100; c.maxiter = P.we_maxiter; c.eps = P.we_epsilon; c.gres = 1.0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(S.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+    int queued = 0;
+    int batch = 100;
+    for (;;) {
+        std::vector<WaveSolve::Snap> snaps;
+        snaps.reserve(batch);
+        for (int k = 0; k < batch; ++k) {
+            int rc = wavestep(h, S, 0);
+            if (rc) return rc;
+            launch_wave_residual(S.partial, S.nparts, h->L[0].nr, h->L[0].nz, S.ctl, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+            snaps.push_back(S.snap());
+        }
+        EllCtl hc{};
+        CUDA_OR_FAIL(cudaMemcpyAsync(&hc, S.ctl, sizeof(hc), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        if (hc.done) {
+            const int idx = hc.step - queued - 1;
+            if (idx < 0 || idx >= batch) return fail(OLLIN_ESTATE, "elliptic solver: inconsistent iteration count");
+            S.restore(snaps[idx]);
+            *steps = hc.step;
+            S.gres = hc.gres;
+            return OLLIN_OK;
+        }
+        queued += batch;
+        batch = std::min(256, std::max(16, queued / 4));
+    }
+}
+
+// wave_elliptic.f90:2-345 with type = 'flat' and init = 'one'; the
+// coefficient arrays S0, S1, S5 are set by the caller.
+int wave_elliptic(ollin_handle* h, WaveSolve& S) {
+    const ollin_params& P = h->P;
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        std::vector<double> ones(L.n, 1.0);
+        CUDA_OR_FAIL(cudaMemcpyAsync(w.u[w.cur], ones.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CUDA_OR_FAIL(cudaMemsetAsync(w.v[w.cur], 0, L.n * sizeof(double), h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    }
+    const int Nlmax_old = h->nlev - 1;
+    S.Nlmax = Nlmax_old > 0 ? 0 : Nlmax_old;
+    for (int phase = 0;; ++phase) {
+        int steps = 0;
+        int rc = wave_phase(h, S, &steps);
+        if (rc) return rc;
+        S.steps[phase] = steps;
+        if (steps != P.ell_maxiter && S.Nlmax != Nlmax_old) {
+            S.Nlmax = Nlmax_old;
+            WLevel& w0 = S.W[0];
+            DLevel& L0 = h->L[0];
+            CUDA_OR_FAIL(cudaMemsetAsync(w0.v[w0.cur], 0, L0.n * sizeof(double), h->stream));
+            for (int l = 1; l < h->nlev; ++l) {
+                DLevel& F = h->L[l];
+                WLevel& w = S.W[l];
+                InjectArgs a{};
+                a.F = F.G;
+                a.Cg = L0.G;
+                a.cin = base_ptr(L0, w0.u[w0.cur]);
+                a.fout = base_ptr(F, w.u[w.cur]);
+                a.rminl_f = h->rminl[l]; a.zminl_f = h->zminl[l];
+                a.rminl_c = h->rminl[0]; a.rmaxl_c = h->rmaxl[0];
+                a.zminl_c = h->zminl[0]; a.zmaxl_c = h->zmaxl[0];
+                a.bicubic = P.interp_bicubic;
+                launch_inject(a, h->stream);
+                rc = after_launch(h);
+                if (rc) return rc;
+            }
+            continue;
+        }
+        break;
+    }
+    return OLLIN_OK;
+}
+
+// The pre-solve part of the elliptic initial data, the solve, and the
+// solution of every level copied to the host (``ell_u``, all points).
+// Scalar pulse (idata_scalarpulse.f90:46-170): the pulse is evaluated here,
+// its gradient and the coefficients on the device, and the four scalar
+// fields are returned in ``scal``.  Brill wave (idata_brillwave.f90:60-118):
+// brillq and S1 are evaluated here, brillq is returned.
+int elliptic_data(ollin_handle* h, std::vector<std::vector<double>>& ell_u, std::vector<std::vector<double>>& brillq,
+                  std::vector<std::vector<std::vector<double>>>& scal) {
+    const ollin_params& P = h->P;
+    const int g = h->g;
+    if (P.ell_solver != OLLIN_ELL_WAVE)
+        return fail(OLLIN_EINVAL, "elliptic initial data on the device needs ELL_solver = wave");
+    WaveSolve S;
+    int rc = wave_alloc(h, S);
+    if (rc) return rc;
+    const bool pulse = P.idata == OLLIN_IDATA_SCALARPULSE;
+    const double pi = 3.141592653589793;
+    ell_u.assign(h->nlev, {});
+    brillq.assign(h->nlev, {});
+    scal.assign(h->nlev, {});
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        auto at = [&](int i, int j) { return (size_t)(i - 1 + g) + (size_t)(j - 1 + g) * L.ld; };
+        if (pulse) {
+            const double a0 = P.scalar_a0, r0 = P.scalar_r0, z0 = P.scalar_z0, sr0 = P.scalar_sr0, sz0 = P.scalar_sz0;
+            std::vector<double> ph(L.n, 0.0);
+            for (int j = 1 - g; j <= L.nz; ++j)
+                for (int i = 1 - g; i <= L.nr; ++i) {
+                    const double R = L.rh[i - 1 + g], Z = L.zh[j - 1 + g];
+                    const double RR = std::sqrt(R * R + Z * Z);
+                    double v;
+                    if (P.scalarpulse_type == OLLIN_PULSE_SHELL) {
+                        if (r0 == 0.0 && z0 == 0.0) {
+                            v = a0 * std::exp(-((R * R) / (sr0 * sr0) + (Z * Z) / (sz0 * sz0)));
+                        } else {
+                            const double cen = ((R * R) * r0 + (Z * Z) * z0) / (RR * RR);
+                            const double den = (R * R) * (sr0 * sr0) + (Z * Z) * (sz0 * sz0);
+                            v = a0 * (std::exp(-(((RR - cen) * (RR - cen)) * (RR * RR) / den))
+                                      + std::exp(-(((RR + cen) * (RR + cen)) * (RR * RR) / den)));
+                        }
+                    } else if (P.scalarpulse_type == OLLIN_PULSE_TORUS) {
+                        auto sq = [](double x) { return x * x; };
+                        if (r0 == 0.0 && z0 == 0.0) v = a0 * std::exp(-sq(R / sr0)) * std::exp(-sq(Z / sz0));
+                        else v = a0 * (std::exp(-sq((R - r0) / sr0)) + std::exp(-sq((R + r0) / sr0)))
+                                 * (std::exp(-sq((Z - z0) / sz0)) + std::exp(-sq((Z + z0) / sz0)));
+                    } else {
+                        v = a0 * std::exp(-((R * R) + (1.0 - sz0) * (Z * Z)));
+                    }
+                    ph[at(i, j)] = v;
+                }
+            CUDA_OR_FAIL(cudaMemcpyAsync(L.slot[L.cur][F_SPHI], ph.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            PulseCoeffArgs a{};
+            a.G = L.G;
+            a.sphi = base_ptr(L, L.slot[L.cur][F_SPHI]);
+            a.xir = base_ptr(L, L.slot[L.cur][F_SXIR]);
+            a.xiz = base_ptr(L, L.slot[L.cur][F_SXIZ]);
+            a.spi = base_ptr(L, L.slot[L.cur][F_SPI]);
+            a.S0 = base_ptr(L, w.S0); a.S1 = base_ptr(L, w.S1); a.S5 = base_ptr(L, w.S5);
+            a.potential = P.scalarpotential;
+            a.mass = P.scalar_mass;
+            a.lambda = P.scalar_lambda;
+            launch_pulse_xi(a, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+            SymArgs sy{};
+            sy.G = L.G;
+            sy.nf = 2;
+            sy.st[0] = a.xir; sy.symr[0] = -1; sy.symz[0] = +1;
+            sy.st[1] = a.xiz; sy.symr[1] = +1; sy.symz[1] = -1;
+            launch_symmetry(sy, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+            launch_pulse_coeffs(a, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+        } else {
+            const double a0 = P.brill_a0, sr0 = P.brill_sr0, sz0 = P.brill_sz0;
+            std::vector<double>& q = brillq[l];
+            q.assign(L.n, 0.0);
+            std::vector<double> s1(L.n, 0.0);
+            auto sq = [](double x) { return x * x; };
+            for (int j = 1 - g; j <= L.nz; ++j)
+                for (int i = 1 - g; i <= L.nr; ++i) {
+                    const double R = L.rh[i - 1 + g], Z = L.zh[j - 1 + g];
+                    const size_t o = at(i, j);
+                    q[o] = a0 * (R * R) * std::exp(-sq(R / sr0) - sq(Z / sz0));
+                    s1[o] = 0.5 * q[o] * (1.0 / (R * R) + 2.0 * (sq(R / (sr0 * sr0)) + sq(Z / (sz0 * sz0)))
+                                          - 5.0 / (sr0 * sr0) - 1.0 / (sz0 * sz0));
+                }
+            CUDA_OR_FAIL(cudaMemcpyAsync(w.S1, s1.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        }
+    }
+    rc = wave_elliptic(h, S);
+    if (rc) return rc;
+    h->ell_steps[0] = S.steps[0];
+    h->ell_steps[1] = S.steps[1];
+    h->ell_gres = S.gres;
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        ell_u[l].resize(L.n);
+        CUDA_OR_FAIL(cudaMemcpyAsync(ell_u[l].data(), w.u[w.cur], L.n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        if (pulse) {
+            scal[l].assign(4, std::vector<double>(L.n));
+            const int ids[4] = {F_SPHI, F_SXIR, F_SXIZ, F_SPI};
+            for (int k = 0; k < 4; ++k)
+                CUDA_OR_FAIL(cudaMemcpyAsync(scal[l][k].data(), L.slot[L.cur][ids[k]], L.n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    (void)pi;
+    return OLLIN_OK;
+}
+
 // Host restatement of initial.f90:59-218,528-645 for the supported data,
 // written straight into host arrays of every level (field slots of the
 // device layout), then uploaded.
 int initial_data(ollin_handle* h) {
     const ollin_params& P = h->P;
     const int g = h->g;
+    const bool ell = P.idata == OLLIN_IDATA_BRILLWAVE || P.idata == OLLIN_IDATA_SCALARPULSE;
+    std::vector<std::vector<double>> ell_u, brillq;
+    std::vector<std::vector<std::vector<double>>> scal;
+    if (ell) {
+        int rc = elliptic_data(h, ell_u, brillq, scal);
+        if (rc) return rc;
+    }
     for (int l = 0; l < h->nlev; ++l) {
         DLevel& L = h->L[l];
         const size_t n = L.n;
@@ -493,6 +928,7 @@ int initial_data(ollin_handle* h) {
                 const double r = L.rh[i - 1 + g], z = L.zh[j - 1 + g];
                 const double rr = std::sqrt(r * r + z * z);
                 double alpha = 1.0, psi = 1.0, phi = 0.0, chi = 1.0;
+                double A = 1.0, B = 1.0, H = 1.0, C = 0.0;
                 if (P.idata == OLLIN_IDATA_SCHWARZSCHILD || P.idata == OLLIN_IDATA_BRILLLINDQUIST) {
                     const double M = P.bh1mass;
                     psi = (P.idata == OLLIN_IDATA_SCHWARZSCHILD) ? 1.0 + 0.5 * M / std::fabs(rr)
@@ -502,11 +938,28 @@ int initial_data(ollin_handle* h) {
                     if (P.idata == OLLIN_IDATA_SCHWARZSCHILD && P.ilapse == OLLIN_ILAPSE_ISOTROPIC)
                         alpha = (1.0 - 0.5 * M / std::fabs(rr)) / (1.0 + 0.5 * M / std::fabs(rr));
                 }
-                // factorhdet (initial.f90:528-577): the flat conformal metric has
-                // unit determinant, so phi gains log(1)/12 = 0 and psi = exp(phi)
+                if (ell) {
+                    // psi = ell_u (idata_scalarpulse.f90:225-240, idata_brillwave.f90:200-215)
+                    psi = ell_u[l][o];
+                    phi = std::log(psi);
+                    chi = 1.0 / std::pow(psi, (double)P.chipower);
+                    if (P.idata == OLLIN_IDATA_BRILLWAVE) {
+                        A = std::exp(2.0 * brillq[l][o]);
+                        B = A;
+                        C = 0.0;
+                        H = 1.0;
+                    }
+                }
+                // factorhdet (initial.f90:528-577): unit-determinant conformal
+                // metric, the determinant moved into phi
                 if (P.factorhdet) {
-                    const double hdet = (1.0 * 1.0 - (r * 0.0) * (r * 0.0)) * 1.0;
+                    const double hdet = (A * B - (r * C) * (r * C)) * H;
                     phi = phi + std::log(hdet) / 12.0;
+                    const double aux = std::pow(hdet, 1.0 / 3.0);
+                    A = A / aux;
+                    B = B / aux;
+                    C = C / aux;
+                    H = H / aux;
                     psi = std::exp(phi);
                 }
                 if (P.ilapse == OLLIN_ILAPSE_PSIMINUS2) alpha = 1.0 / (psi * psi);
@@ -514,8 +967,11 @@ int initial_data(ollin_handle* h) {
                 F[F_ALPHA][o] = alpha;
                 F[F_PHI][o] = phi;
                 F[F_CHI][o] = chi;
-                F[F_A][o] = 1.0; F[F_B][o] = 1.0; F[F_H][o] = 1.0; F[F_C][o] = 0.0;
+                F[F_A][o] = A; F[F_B][o] = B; F[F_H][o] = H; F[F_C][o] = C;
             }
+        if (P.idata == OLLIN_IDATA_SCALARPULSE) {
+            F[F_SPHI] = scal[l][0]; F[F_SXIR] = scal[l][1]; F[F_SXIZ] = scal[l][2]; F[F_SPI] = scal[l][3];
+        }
         for (int f : h->fields) {
             CUDA_OR_FAIL(cudaMemcpyAsync(L.slot[L.cur][f], F[f].data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         }
@@ -678,8 +1134,7 @@ int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_
 int ollin_gpu_initial_data(ollin_handle* h) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     const ollin_params& P = h->P;
-    if (P.idata != OLLIN_IDATA_MINKOWSKI && P.idata != OLLIN_IDATA_SCHWARZSCHILD && P.idata != OLLIN_IDATA_BRILLLINDQUIST)
-        return fail(OLLIN_EINVAL, "idata not supported by the host initial-data routine");
+    (void)P;
     // scalar-field slots start at zero; a scalar pulse needs the elliptic
     // solve of idata_scalarpulse.f90 and is uploaded by the caller
     return initial_data(h);
@@ -796,6 +1251,14 @@ int ollin_gpu_kernel_stats(ollin_handle* h, double* rhs_ms, long long* launches,
 }
 
 void* ollin_gpu_stream(const ollin_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres) {
+    if (!h || !steps) return fail(OLLIN_EINVAL, "null argument");
+    steps[0] = h->ell_steps[0];
+    steps[1] = h->ell_steps[1];
+    if (gres) *gres = h->ell_gres;
+    return OLLIN_OK;
+}
 
 long long ollin_gpu_launch_count(const ollin_handle* h) { return h ? h->launches : 0; }
 

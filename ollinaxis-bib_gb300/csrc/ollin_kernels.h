@@ -58,6 +58,7 @@ struct SymArgs {
     int symr[NFIELDS], symz[NFIELDS];
     int nf;                      // number of fields to fill (first nf slots used)
     int fid[NFIELDS];            // which field slot each entry refers to
+    const int* skip;             // optional: the launch does nothing while *skip != 0
 };
 
 // Coarse -> fine boundary prolongation (finebound.f90 + bound_interp.inc).
@@ -74,6 +75,7 @@ struct ProlongArgs {
     double rminl_c, rmaxl_c, zminl_c, zmaxl_c;
     double tp, t0, tm1, tl;
     int imax, border, bicubic;
+    const int* skip;             // optional: the launch does nothing while *skip != 0
 };
 
 // Fine -> coarse restriction (restrict.f90 + restrict_interp.inc).
@@ -86,7 +88,66 @@ struct RestrictArgs {
     double rminl_f, rmaxl_f, zminl_f, zmaxl_f;
     double rminl_c, zminl_c;
     int eqsym, bicubic;
+    const int* skip;             // optional: the launch does nothing while *skip != 0
 };
+
+// Interpolation of one grid function of a coarser level to every point of a
+// finer one (the initial guess of the elliptic solvers on refined levels).
+struct InjectArgs {
+    LevelGeom F, Cg;
+    const double* cin;
+    double* fout;
+    double rminl_f, zminl_f;
+    double rminl_c, rmaxl_c, zminl_c, zmaxl_c;
+    int bicubic;
+};
+
+// Iteration control of a device-resident elliptic solve: the residual kernel
+// of each iteration updates it, and every launch of later iterations returns
+// at once when ``done`` is set, so the host can queue iterations in batches.
+struct EllCtl {
+    int step;      // iterations done in the current phase
+    int done;      // stop condition met
+    int miniter, maxiter;
+    double eps;    // tolerance on the residual
+    double gres;   // residual of the last iteration
+};
+
+// One WaveElliptic stage on one level (wave_elliptic.f90:505-700):
+// sources, dissipation, parity, radiative boundary, accumulate and update of
+// (u, v) at every point including ghosts.
+struct WaveArgs {
+    LevelGeom G;
+    const double* u_in; const double* v_in;   // stage input
+    const double* u_p; const double* v_p;     // start of the step
+    double* u_out; double* v_out;
+    double* u_acc; double* v_acc;
+    const double* S0; const double* S1; const double* S5;
+    double eta;        // WE_eta
+    double kdiss;      // WE_diss / dt
+    double dtw, weight;
+    int rk4, iter, niter;
+    double* res_partial;   // level 0, last stage: per-block sums of sell_v^2
+    const int* skip;
+};
+
+// Scalar-pulse coefficients (idata_scalarpulse.f90:108-170): xi = grad phi,
+// pi = 0, S1 = pi (xi_r^2 + xi_z^2), S5 = 2 pi V, S0 = 0.
+struct PulseCoeffArgs {
+    LevelGeom G;
+    const double* sphi;
+    double* xir; double* xiz; double* spi;
+    double* S0; double* S1; double* S5;
+    int potential;
+    double mass, lambda;
+};
+
+void launch_inject(const InjectArgs& a, cudaStream_t s);
+void launch_wave_stage(const WaveArgs& a, cudaStream_t s);
+int wave_stage_blocks(const LevelGeom& G);
+void launch_wave_residual(const double* partial, int nparts, int nr, int nz, EllCtl* ctl, cudaStream_t s);
+void launch_pulse_xi(const PulseCoeffArgs& a, cudaStream_t s);
+void launch_pulse_coeffs(const PulseCoeffArgs& a, cudaStream_t s);
 
 void launch_rhs(const StageArgs& a, cudaStream_t s);
 void launch_aux_point(const AuxArgs& a, cudaStream_t s);

@@ -24,6 +24,7 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 
 // ---- parity ghost fill -------------------------------------------------
 __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
+    if (a.skip && *a.skip) return;
     const LevelGeom& G = a.G;
     const int g = G.g;
     // thread space: all points (i,j) with i <= 0 or (eqsym and j <= 0)
@@ -110,6 +111,7 @@ __device__ double interp_apply(const LevelGeom& G, const double* f, const Interp
 // strip (jmax+1) x (Nr+g); corner points are written by both strips with the
 // same value, as in the reference.
 __global__ void __launch_bounds__(128) prolong_kernel(const __grid_constant__ ProlongArgs a) {
+    if (a.skip && *a.skip) return;
     const LevelGeom& F = a.F;
     const int g = F.g;
     const int nstrip_r = (a.imax + 1) * (F.nz + g);
@@ -154,6 +156,7 @@ __global__ void __launch_bounds__(128) prolong_kernel(const __grid_constant__ Pr
 
 // ---- restriction -----------------------------------------------------------
 __global__ void __launch_bounds__(128) restrict_kernel(const __grid_constant__ RestrictArgs a) {
+    if (a.skip && *a.skip) return;
     const LevelGeom& C = a.Cg;
     const LevelGeom& F = a.F;
     const int g = C.g;
@@ -178,6 +181,24 @@ __global__ void __launch_bounds__(128) restrict_kernel(const __grid_constant__ R
         const int f = a.fid[k];
         a.cout[f][o] = interp_apply(F, a.fin[f], p);
     }
+}
+
+// ---- injection: interpolate a coarser level to every point of a finer one --
+// (wave_elliptic.f90:270-328; sor_elliptic.f90:268-320)
+__global__ void __launch_bounds__(128) inject_kernel(const __grid_constant__ InjectArgs a) {
+    const LevelGeom& F = a.F;
+    const int g = F.g;
+    const int m = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int n = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (m > F.nr + g - 1 || n > F.nz + g - 1) return;
+    const double r0 = add(a.rminl_f, mul((double)m, F.dr));
+    const double z0 = add(a.zminl_f, mul((double)n, F.dz));
+    const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
+    const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
+    if (!(i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz)) return;
+    InterpPt p;
+    interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
+    a.fout[(size_t)i + (size_t)j * F.ld] = interp_apply(a.Cg, a.cin, p);
 }
 
 // ---- 0-D statistics (save0Ddata.f90:221-288, origin value :370-374) --------
@@ -294,6 +315,12 @@ void launch_symmetry(const SymArgs& a, cudaStream_t s) {
 void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
     const int n = (a.imax + 1) * (a.F.nz + a.F.g) + (a.imax + 1) * (a.F.nr + a.F.g);
     prolong_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+}
+
+void launch_inject(const InjectArgs& a, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((a.F.nr + a.F.g + blk.x - 1) / blk.x, (a.F.nz + a.F.g + blk.y - 1) / blk.y);
+    inject_kernel<<<grd, blk, 0, s>>>(a);
 }
 
 void launch_restrict(const RestrictArgs& a, cudaStream_t s) {

@@ -71,6 +71,7 @@ def load(build_if_missing=True):
     L.ollin_gpu_kernel_timing.argtypes = [vp, ctypes.c_int]
     L.ollin_gpu_fp64_rate.restype = ctypes.c_double
     L.ollin_gpu_kernel_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
+    L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     _lib = L
     return L
 
@@ -163,6 +164,14 @@ class Evolution:
 
     def kernel_timing(self, enable=True):
         self._check(self.L.ollin_gpu_kernel_timing(self.h, 1 if enable else 0))
+
+    def ell_stats(self):
+        """(coarse-phase iterations, all-level iterations, final residual) of
+        the elliptic solve of ``initial_data``."""
+        steps = (ctypes.c_int * 2)()
+        gres = ctypes.c_double()
+        self._check(self.L.ollin_gpu_ell_stats(self.h, steps, ctypes.byref(gres)))
+        return steps[0], steps[1], gres.value
 
     def kernel_stats(self):
         """(total rhs-kernel ms, rhs launches, grid points x stages) since timing was enabled."""
