@@ -1,5 +1,6 @@
 // Elliptic initial data on the device: the WaveElliptic solver of
-// src/elliptic/wave_elliptic.f90 and the scalar-pulse coefficients of
+// src/elliptic/wave_elliptic.f90, the SOR solver of
+// src/elliptic/sor_elliptic.f90 and the scalar-pulse coefficients of
 // src/matter/idata_scalarpulse.f90.
 //
 // WaveElliptic finds the stationary state of
@@ -154,7 +155,181 @@ __global__ void __launch_bounds__(128) pulse_coeff_kernel(const __grid_constant_
     a.S5[o] = (a.potential == 0) ? 0.0 : 2.0 * pi * V;
 }
 
+// ---- SOR (sor_elliptic.f90:562-802) --------------------------------------
+// Explicitly rounded operations throughout: the sweep and the boundary give
+// the same bits as the sequential Fortran loops (the flat operator couples a
+// point only to the other colour, so the order within a pass is immaterial).
+__device__ __forceinline__ double mrn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double arn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double srn(double a, double b) { return __dsub_rn(a, b); }
+
+constexpr int kSorBX = 32, kSorBY = 4, kSorThreads = kSorBX * kSorBY;
+
+// e(i,j) = aux(i,j) + S5 u^4 (sor_elliptic.f90:632-636)
+__global__ void __launch_bounds__(128) sor_e_kernel(LevelGeom G, double* e, const double* eaux, const double* S5,
+                                                    const double* u, const int* skip) {
+    if (skip && *skip) return;
+    const int g = G.g;
+    const int i = 2 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 2 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr - 1 || j > G.nz - 1) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    double u4 = mrn(u[o], u[o]);
+    u4 = mrn(u4, u4);
+    e[o] = arn(eaux[o], mrn(S5[o], u4));
+}
+
+// thread space: i over 2-g..Nr-1, jh over the points of the pass's parity in
+// each column
+__global__ void __launch_bounds__(kSorThreads) sor_pass_kernel(const __grid_constant__ SorPassArgs A) {
+    __shared__ double red[kSorThreads];
+    if (A.skip && *A.skip) return;
+    const LevelGeom& G = A.G;
+    const int g = G.g;
+    const int i = 2 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int jh = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    // first j >= 2-g with (i + j) of the pass's parity
+    int j = 2 - g;
+    if (((i + j) & 1) != A.parity) ++j;
+    j += 2 * jh;
+    double res = 0.0;
+    if (i <= G.nr - 1 && j <= G.nz - 1) {
+        const long ld = G.ld;
+        const size_t o = (size_t)i + (size_t)j * ld;
+        double* u = A.u + o;
+        const double ev = A.e[o];
+        double r = mrn(A.ca[i], u[1]);
+        r = arn(r, mrn(A.cb[i], u[-1]));
+        r = arn(r, mrn(A.cc, u[ld]));
+        r = arn(r, mrn(A.cc, u[-ld]));
+        r = arn(r, mrn(ev, u[0]));
+        r = srn(r, A.f[o]);
+        res = mrn(r, r);
+        u[0] = srn(u[0], __ddiv_rn(mrn(A.omega, r), ev));
+    }
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    red[t] = res;
+    __syncthreads();
+    for (int w = kSorThreads / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    if (t == 0) A.partial[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+// fixed-order sum of n partials by the whole block
+__device__ double block_sum(const double* partial, int n, double* red) {
+    const int t = threadIdx.x;
+    double acc = 0.0;
+    for (int k = t; k < n; k += blockDim.x) acc = acc + partial[k];
+    red[t] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    const double v = red[0];
+    __syncthreads();
+    return v;
+}
+
+__global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant__ SorFinishArgs A) {
+    __shared__ double red[1024];
+    EllCtl* ctl = A.ctl;
+    if (ctl->done) return;
+    const LevelGeom& G = A.G;
+    const int g = G.g, nr = G.nr, nz = G.nz;
+    const long ld = G.ld;
+    double* u = A.u;
+    auto U = [&](int i, int j) -> double& { return u[(size_t)i + (size_t)j * ld]; };
+    const double npts = (double)((nr + g) * (nz + g));  // imax*jmax
+    // anorm after pass 1 is sqrt(sum1/N); pass 2 keeps adding to that value
+    const double s1 = block_sum(A.partial1, A.nparts, red);
+    const double s2 = block_sum(A.partial2, A.nparts, red);
+    const double anorm1 = sqrt(s1 / npts);
+    const double ganorm = sqrt((anorm1 + s2) / npts);
+    if (A.robin && threadIdx.x == 0) {
+        // r boundary, j upwards (sor_elliptic.f90:698-712)
+        double cr = G.rcol[nr] / G.dr;
+        for (int j = 2 - g; j <= nz - 1; ++j) {
+            const double cz = G.zrow[j] / G.dz;
+            const double a = srn(mrn(4.0, U(nr - 1, j)), U(nr - 2, j));
+            double v = arn(A.uinf, mrn(mrn(0.5, cr), a));
+            v = srn(v, mrn(mrn(0.5, cz), srn(U(nr, j + 1), U(nr, j - 1))));
+            U(nr, j) = __ddiv_rn(v, arn(1.0, mrn(1.5, cr)));
+        }
+        // upper z boundary, i outwards (:716-728)
+        double cz = G.zrow[nz] / G.dz;
+        for (int i = 2 - g; i <= nr - 1; ++i) {
+            cr = G.rcol[i] / G.dr;
+            const double a = srn(mrn(4.0, U(i, nz - 1)), U(i, nz - 2));
+            double v = arn(A.uinf, mrn(mrn(0.5, cz), a));
+            v = srn(v, mrn(mrn(0.5, cr), srn(U(i + 1, nz), U(i - 1, nz))));
+            U(i, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, cz)));
+        }
+        // upper corner (:748-756)
+        cr = G.rcol[nr] / G.dr;
+        cz = G.zrow[nz] / G.dz;
+        double v = arn(A.uinf, mrn(mrn(0.5, cr), srn(mrn(4.0, U(nr - 1, nz)), U(nr - 2, nz))));
+        v = arn(v, mrn(mrn(0.5, cz), srn(mrn(4.0, U(nr, nz - 1)), U(nr, nz - 2))));
+        U(nr, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, arn(cr, cz))));
+    }
+    __syncthreads();
+    // parity fill: axis first over all rows, then the equator (:772-784)
+    for (int j = 1 - g + (int)threadIdx.x; j <= nz; j += blockDim.x)
+        for (int i = 1; i <= g; ++i) U(1 - i, j) = U(i, j);
+    __syncthreads();
+    if (G.eqsym)
+        for (int i = 1 - g + (int)threadIdx.x; i <= nr; i += blockDim.x)
+            for (int j = 1; j <= g; ++j) U(i, 1 - j) = U(i, j);
+    if (threadIdx.x == 0) {
+        const int step = ctl->step + 1;
+        ctl->step = step;
+        ctl->gres = ganorm;
+        ctl->done = (ganorm < ctl->eps || step >= ctl->maxiter) ? 1 : 0;
+    }
+}
+
+// out = c + x at every point
+__global__ void add_kernel(LevelGeom G, double* out, double c, const double* x) {
+    const int g = G.g;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    out[o] = arn(c, x[o]);
+}
+
 }  // namespace
+
+void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const double* S5, const double* u,
+                  const int* skip, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g - 2 + blk.x - 1) / blk.x, (G.nz + G.g - 2 + blk.y - 1) / blk.y);
+    sor_e_kernel<<<grd, blk, 0, s>>>(G, e, eaux, S5, u, skip);
+}
+
+int sor_pass_blocks(const LevelGeom& G) {
+    const int ni = G.nr + G.g - 2, nj = (G.nz + G.g - 2 + 1) / 2;
+    return ((ni + kSorBX - 1) / kSorBX) * ((nj + kSorBY - 1) / kSorBY);
+}
+
+void launch_sor_pass(const SorPassArgs& a, cudaStream_t s) {
+    const int ni = a.G.nr + a.G.g - 2, nj = (a.G.nz + a.G.g - 2 + 1) / 2;
+    dim3 blk(kSorBX, kSorBY);
+    dim3 grd((ni + kSorBX - 1) / kSorBX, (nj + kSorBY - 1) / kSorBY);
+    sor_pass_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_sor_finish(const SorFinishArgs& a, cudaStream_t s) {
+    sor_finish_kernel<<<1, 1024, 0, s>>>(a);
+}
+
+void launch_add(const LevelGeom& G, double* out, double c, const double* x, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+    add_kernel<<<grd, blk, 0, s>>>(G, out, c, x);
+}
 
 int wave_stage_blocks(const LevelGeom& G) {
     const int nx = (G.nr + G.g + kWaveBX - 1) / kWaveBX, ny = (G.nz + G.g + kWaveBY - 1) / kWaveBY;

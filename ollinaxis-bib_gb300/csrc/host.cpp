@@ -120,8 +120,9 @@ int check_params(const ollin_params& P) {
     if (P.idata < OLLIN_IDATA_MINKOWSKI || P.idata > OLLIN_IDATA_SCALARPULSE) return fail(OLLIN_EINVAL, "unknown idata");
     if (P.idata == OLLIN_IDATA_SCALARPULSE && P.mattertype != OLLIN_MATTER_SCALAR)
         return fail(OLLIN_EINVAL, "Scalar pulse initial data needs scalar field type matter.");
-    if ((P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) && P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "elliptic initial data needs ELL_solver = wave on the device");
+    if ((P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) && P.ell_solver != OLLIN_ELL_WAVE &&
+        P.ell_solver != OLLIN_ELL_SOR)
+        return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave or sor)");
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     return OLLIN_OK;
 }
@@ -506,6 +507,7 @@ struct WaveSolve {
     std::vector<long> s;
     EllCtl* ctl = nullptr;
     double* partial = nullptr;
+    double* partial2 = nullptr;
     int nparts = 0;
     int Nlmax = 0;
     int steps[2] = {0, 0};
@@ -519,6 +521,7 @@ struct WaveSolve {
         for (WLevel& w : W) cudaFree(w.pool);
         cudaFree(ctl);
         cudaFree(partial);
+        cudaFree(partial2);
     }
     Snap snap() const {
         Snap q;
@@ -788,6 +791,166 @@ int wave_elliptic(ollin_handle* h, WaveSolve& S) {
     return OLLIN_OK;
 }
 
+// ---------------------------------------------------------------------------
+// SOR (sor_elliptic.f90) on the device: coarse solve with Robin boundaries,
+// then every finer level with Dirichlet data interpolated from the level
+// below, then restriction back down.  The iteration is in place; batches of
+// iterations are queued and turned into no-ops by the device stop flag.
+// ---------------------------------------------------------------------------
+int sor_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* iters) {
+    const ollin_params& P = h->P;
+    DLevel& L = h->L[level];
+    WLevel& w = S.W[level];
+    const int g = h->g;
+    // coefficient columns a(i), b(i) and the constant part of e
+    // (sor_elliptic.f90:141-151), evaluated as written
+    std::vector<double> cab(2 * (size_t)(L.nr + g));
+    for (int i = 1 - g; i <= L.nr; ++i) {
+        const double r = L.rh[i - 1 + g];
+        cab[i - 1 + g] = (1.0 / L.dr + 0.5 / r) / L.dr;
+        cab[(L.nr + g) + (i - 1 + g)] = (1.0 / L.dr - 0.5 / r) / L.dr;
+    }
+    double* dcab = nullptr;
+    if (cudaMalloc(&dcab, cab.size() * sizeof(double)) != cudaSuccess) return fail(OLLIN_ENOMEM, "device allocation failed");
+    struct FreeOnExit { double* p; ~FreeOnExit() { cudaFree(p); } } free_cab{dcab};
+    CUDA_OR_FAIL(cudaMemcpyAsync(dcab, cab.data(), cab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    const double ec = -2.0 * (1.0 / (L.dr * L.dr) + 1.0 / (L.dz * L.dz));
+    double* eaux = w.ua;  // the WaveElliptic accumulators are free during SOR
+    double* e = w.va;
+    launch_add(L.G, base_ptr(L, eaux), ec, base_ptr(L, w.S1), h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    // with S5 = 0, e = aux + 0*u^4 = aux exactly, so the update is skipped
+    const bool s5 = P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
+    EllCtl c{};
+    c.maxiter = P.ell_maxiter; c.eps = P.ell_epsilon; c.gres = 1.0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(S.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+    double omega = 1.0;
+    int n = 0, batch = 64;
+    for (;;) {
+        for (int k = 0; k < batch; ++k) {
+            ++n;
+            if (s5) {
+                launch_sor_e(L.G, base_ptr(L, e), base_ptr(L, eaux), base_ptr(L, w.S5), base_ptr(L, w.u[w.cur]),
+                             &S.ctl->done, h->stream);
+                rc = after_launch(h);
+                if (rc) return rc;
+            }
+            for (int ipass = 1; ipass <= 2; ++ipass) {
+                SorPassArgs a{};
+                a.G = L.G;
+                a.u = base_ptr(L, w.u[w.cur]);
+                a.ca = dcab + (g - 1);
+                a.cb = dcab + (L.nr + g) + (g - 1);
+                a.cc = 1.0 / (L.dz * L.dz);
+                a.e = base_ptr(L, s5 ? e : eaux);
+                a.f = base_ptr(L, w.S0);
+                a.omega = omega;
+                a.parity = ipass == 1 ? 0 : 1;
+                a.partial = ipass == 1 ? S.partial : S.partial2;
+                a.skip = &S.ctl->done;
+                launch_sor_pass(a, h->stream);
+                rc = after_launch(h);
+                if (rc) return rc;
+                // Chebyshev acceleration (sor_elliptic.f90:690-694)
+                if (n == 1 && ipass == 1) omega = 1.0 / (1.0 - 0.5 * (rjac * rjac));
+                else omega = 1.0 / (1.0 - 0.25 * (rjac * rjac) * omega);
+            }
+            SorFinishArgs f{};
+            f.G = L.G;
+            f.u = base_ptr(L, w.u[w.cur]);
+            f.partial1 = S.partial;
+            f.partial2 = S.partial2;
+            f.nparts = sor_pass_blocks(L.G);
+            f.robin = robin ? 1 : 0;
+            f.uinf = 1.0;
+            f.ctl = S.ctl;
+            launch_sor_finish(f, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+        }
+        EllCtl hc{};
+        CUDA_OR_FAIL(cudaMemcpyAsync(&hc, S.ctl, sizeof(hc), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        if (hc.done) {
+            *iters = hc.step;
+            S.gres = hc.gres;
+            return OLLIN_OK;
+        }
+        batch = std::min(1024, std::max(64, n / 4));
+    }
+}
+
+int sor_elliptic(ollin_handle* h, WaveSolve& S) {
+    const ollin_params& P = h->P;
+    // partial sums of the two passes (every level has the same dimensions)
+    const int nparts = sor_pass_blocks(h->L[0].G);
+    if (S.nparts < nparts) {
+        cudaFree(S.partial);
+        S.partial = nullptr;
+        if (cudaMalloc(&S.partial, nparts * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the elliptic solver");
+        S.nparts = nparts;
+    }
+    if (cudaMalloc(&S.partial2, nparts * sizeof(double)) != cudaSuccess)
+        return fail(OLLIN_ENOMEM, "device allocation failed for the elliptic solver");
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        std::vector<double> ones(L.n, 1.0);
+        CUDA_OR_FAIL(cudaMemcpyAsync(w.u[w.cur], ones.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    }
+    // Jacobi spectral radius (sor_elliptic.f90:126-128): the grid-spacing
+    // ratio is the same on every level
+    const DLevel& L0 = h->L[0];
+    const double pi = 3.141592653589793;
+    const double rjac = (L0.dz / L0.dr * std::cos(pi / (double)(L0.nr + L0.g))
+                         + L0.dr / L0.dz * std::cos(pi / (double)(L0.nz + L0.g))) / (L0.dz / L0.dr + L0.dr / L0.dz);
+    int rc = sor_level(h, S, 0, true, rjac, &S.steps[0]);
+    if (rc) return rc;
+    for (int l = 1; l < h->nlev; ++l) {  // sor_elliptic.f90:268-530
+        DLevel& F = h->L[l];
+        DLevel& C = h->L[l - 1];
+        InjectArgs a{};
+        a.F = F.G;
+        a.Cg = C.G;
+        a.cin = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.fout = base_ptr(F, S.W[l].u[S.W[l].cur]);
+        a.rminl_f = h->rminl[l]; a.zminl_f = h->zminl[l];
+        a.rminl_c = h->rminl[l - 1]; a.rmaxl_c = h->rmaxl[l - 1];
+        a.zminl_c = h->zminl[l - 1]; a.zmaxl_c = h->zmaxl[l - 1];
+        a.bicubic = P.interp_bicubic;
+        launch_inject(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        int it = 0;
+        rc = sor_level(h, S, l, false, rjac, &it);
+        if (rc) return rc;
+        if (l == 1) S.steps[1] = it;
+    }
+    for (int l = 1; l < h->nlev; ++l) {  // sor_elliptic.f90:534-555
+        DLevel& F = h->L[l];
+        DLevel& C = h->L[l - 1];
+        RestrictArgs a{};
+        a.F = F.G;
+        a.Cg = C.G;
+        a.nf = 1;
+        a.fid[0] = 0;
+        a.fin[0] = base_ptr(F, S.W[l].u[S.W[l].cur]);
+        a.cout[0] = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.rminl_f = h->rminl[l]; a.rmaxl_f = h->rmaxl[l];
+        a.zminl_f = h->zminl[l]; a.zmaxl_f = h->zmaxl[l];
+        a.rminl_c = h->rminl[l - 1]; a.zminl_c = h->zminl[l - 1];
+        a.eqsym = P.eqsym;
+        a.bicubic = P.interp_bicubic;
+        launch_restrict(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+    }
+    return OLLIN_OK;
+}
+
 // The pre-solve part of the elliptic initial data, the solve, and the
 // solution of every level copied to the host (``ell_u``, all points).
 // Scalar pulse (idata_scalarpulse.f90:46-170): the pulse is evaluated here,
@@ -798,8 +961,6 @@ int elliptic_data(ollin_handle* h, std::vector<std::vector<double>>& ell_u, std:
                   std::vector<std::vector<std::vector<double>>>& scal) {
     const ollin_params& P = h->P;
     const int g = h->g;
-    if (P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "elliptic initial data on the device needs ELL_solver = wave");
     WaveSolve S;
     int rc = wave_alloc(h, S);
     if (rc) return rc;
@@ -882,7 +1043,7 @@ int elliptic_data(ollin_handle* h, std::vector<std::vector<double>>& ell_u, std:
             CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
         }
     }
-    rc = wave_elliptic(h, S);
+    rc = (P.ell_solver == OLLIN_ELL_SOR) ? sor_elliptic(h, S) : wave_elliptic(h, S);
     if (rc) return rc;
     h->ell_steps[0] = S.steps[0];
     h->ell_steps[1] = S.steps[1];

@@ -142,6 +142,41 @@ struct PulseCoeffArgs {
     double mass, lambda;
 };
 
+// One red-black pass of the SOR solver (sor_elliptic.f90:640-676) over the
+// points (i,j), 2-g <= i <= Nr-1, 2-g <= j <= Nz-1, with (i+j) of one
+// parity; flat Laplacian, so only the four axial neighbours couple.
+struct SorPassArgs {
+    LevelGeom G;
+    double* u;
+    const double* ca; const double* cb;  // a(i), b(i) per column, indexed [i]
+    double cc;                           // c = d = 1/dz^2
+    const double* e; const double* f;    // diagonal and source per point
+    double omega;
+    int parity;
+    double* partial;                     // per-block sums of resid^2
+    const int* skip;
+};
+
+// End of one SOR iteration (sor_elliptic.f90:678-790): residual norm of the
+// two passes, Robin boundary (sequential along each edge, as written), parity
+// fill, stop condition.
+struct SorFinishArgs {
+    LevelGeom G;
+    double* u;
+    const double* partial1; const double* partial2;
+    int nparts;
+    int robin;
+    double uinf;
+    EllCtl* ctl;
+};
+
+void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const double* S5, const double* u,
+                  const int* skip, cudaStream_t s);
+void launch_sor_pass(const SorPassArgs& a, cudaStream_t s);
+int sor_pass_blocks(const LevelGeom& G);
+void launch_sor_finish(const SorFinishArgs& a, cudaStream_t s);
+void launch_add(const LevelGeom& G, double* out, double c, const double* x, cudaStream_t s);
+
 void launch_inject(const InjectArgs& a, cudaStream_t s);
 void launch_wave_stage(const WaveArgs& a, cudaStream_t s);
 int wave_stage_blocks(const LevelGeom& G);
