@@ -233,8 +233,16 @@ __device__ double block_sum(const double* partial, int n, double* red) {
     return v;
 }
 
+// The Robin boundary of sor_elliptic.f90:698-756 is a recurrence along each
+// outer edge: the point j of the r edge uses the new value at j-1.  Every
+// other operand is known before the edge is swept, so the block first
+// evaluates those in parallel into shared memory (the same operations in the
+// same order), then one thread per edge runs the recurrence from shared
+// memory (the r and z edges do not read each other's new values), and the
+// block writes the edges back.  The corner follows from both edges.
 __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant__ SorFinishArgs A) {
     __shared__ double red[1024];
+    extern __shared__ double edge[];
     EllCtl* ctl = A.ctl;
     if (ctl->done) return;
     const LevelGeom& G = A.G;
@@ -248,31 +256,52 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
     const double s2 = block_sum(A.partial2, A.nparts, red);
     const double anorm1 = sqrt(s1 / npts);
     const double ganorm = sqrt((anorm1 + s2) / npts);
-    if (A.robin && threadIdx.x == 0) {
-        // r boundary, j upwards (sor_elliptic.f90:698-712)
-        double cr = G.rcol[nr] / G.dr;
-        for (int j = 2 - g; j <= nz - 1; ++j) {
-            const double cz = G.zrow[j] / G.dz;
-            const double a = srn(mrn(4.0, U(nr - 1, j)), U(nr - 2, j));
-            double v = arn(A.uinf, mrn(mrn(0.5, cr), a));
-            v = srn(v, mrn(mrn(0.5, cz), srn(U(nr, j + 1), U(nr, j - 1))));
-            U(nr, j) = __ddiv_rn(v, arn(1.0, mrn(1.5, cr)));
+    if (A.robin) {
+        const int nj = nz + g, ni = nr + g;  // edge arrays indexed by j+g-1 / i+g-1
+        double* Pr = edge;                 // uinf + 0.5 cr (4 u(Nr-1,j) - u(Nr-2,j))
+        double* Qr = Pr + nj;              // old u(Nr, j+1)
+        double* Hr = Qr + nj;              // 0.5 z(j)/dz
+        double* Pz = Hr + nj;              // uinf + 0.5 cz (4 u(i,Nz-1) - u(i,Nz-2))
+        double* Qz = Pz + ni;              // old u(i+1, Nz)
+        double* Hz = Qz + ni;              // 0.5 r(i)/dr
+        const double crn = G.rcol[nr] / G.dr, czn = G.zrow[nz] / G.dz;
+        for (int j = 2 - g + (int)threadIdx.x; j <= nz - 1; j += blockDim.x) {
+            const int k = j + g - 1;
+            Pr[k] = arn(A.uinf, mrn(mrn(0.5, crn), srn(mrn(4.0, U(nr - 1, j)), U(nr - 2, j))));
+            Qr[k] = U(nr, j + 1);
+            Hr[k] = mrn(0.5, G.zrow[j] / G.dz);
         }
-        // upper z boundary, i outwards (:716-728)
-        double cz = G.zrow[nz] / G.dz;
-        for (int i = 2 - g; i <= nr - 1; ++i) {
-            cr = G.rcol[i] / G.dr;
-            const double a = srn(mrn(4.0, U(i, nz - 1)), U(i, nz - 2));
-            double v = arn(A.uinf, mrn(mrn(0.5, cz), a));
-            v = srn(v, mrn(mrn(0.5, cr), srn(U(i + 1, nz), U(i - 1, nz))));
-            U(i, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, cz)));
+        for (int i = 2 - g + (int)threadIdx.x; i <= nr - 1; i += blockDim.x) {
+            const int k = i + g - 1;
+            Pz[k] = arn(A.uinf, mrn(mrn(0.5, czn), srn(mrn(4.0, U(i, nz - 1)), U(i, nz - 2))));
+            Qz[k] = U(i + 1, nz);
+            Hz[k] = mrn(0.5, G.rcol[i] / G.dr);
         }
-        // upper corner (:748-756)
-        cr = G.rcol[nr] / G.dr;
-        cz = G.zrow[nz] / G.dz;
-        double v = arn(A.uinf, mrn(mrn(0.5, cr), srn(mrn(4.0, U(nr - 1, nz)), U(nr - 2, nz))));
-        v = arn(v, mrn(mrn(0.5, cz), srn(mrn(4.0, U(nr, nz - 1)), U(nr, nz - 2))));
-        U(nr, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, arn(cr, cz))));
+        __syncthreads();
+        if (threadIdx.x == 0) {  // r edge, j upwards
+            const double den = arn(1.0, mrn(1.5, crn));
+            double prev = U(nr, 1 - g);
+            for (int k = 1; k <= nz - 2 + g; ++k) {  // j = 2-g .. nz-1
+                prev = __ddiv_rn(srn(Pr[k], mrn(Hr[k], srn(Qr[k], prev))), den);
+                Pr[k] = prev;
+            }
+        } else if (threadIdx.x == 32) {  // upper z edge, i outwards
+            const double den = arn(1.0, mrn(1.5, czn));
+            double prev = U(1 - g, nz);
+            for (int k = 1; k <= nr - 2 + g; ++k) {  // i = 2-g .. nr-1
+                prev = __ddiv_rn(srn(Pz[k], mrn(Hz[k], srn(Qz[k], prev))), den);
+                Pz[k] = prev;
+            }
+        }
+        __syncthreads();
+        for (int j = 2 - g + (int)threadIdx.x; j <= nz - 1; j += blockDim.x) U(nr, j) = Pr[j + g - 1];
+        for (int i = 2 - g + (int)threadIdx.x; i <= nr - 1; i += blockDim.x) U(i, nz) = Pz[i + g - 1];
+        __syncthreads();
+        if (threadIdx.x == 0) {  // upper corner (:748-756)
+            double v = arn(A.uinf, mrn(mrn(0.5, crn), srn(mrn(4.0, U(nr - 1, nz)), U(nr - 2, nz))));
+            v = arn(v, mrn(mrn(0.5, czn), srn(mrn(4.0, U(nr, nz - 1)), U(nr, nz - 2))));
+            U(nr, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, arn(crn, czn))));
+        }
     }
     __syncthreads();
     // parity fill: axis first over all rows, then the equator (:772-784)
@@ -321,8 +350,15 @@ void launch_sor_pass(const SorPassArgs& a, cudaStream_t s) {
     sor_pass_kernel<<<grd, blk, 0, s>>>(a);
 }
 
-void launch_sor_finish(const SorFinishArgs& a, cudaStream_t s) {
-    sor_finish_kernel<<<1, 1024, 0, s>>>(a);
+size_t sor_finish_smem(const LevelGeom& G) { return (size_t)3 * ((G.nz + G.g) + (G.nr + G.g)) * sizeof(double); }
+
+int launch_sor_finish(const SorFinishArgs& a, cudaStream_t s) {
+    const size_t smem = a.robin ? sor_finish_smem(a.G) : 0;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(sor_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 1;
+    sor_finish_kernel<<<1, 1024, smem, s>>>(a);
+    return 0;
 }
 
 void launch_add(const LevelGeom& G, double* out, double c, const double* x, cudaStream_t s) {

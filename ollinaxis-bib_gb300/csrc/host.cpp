@@ -865,7 +865,8 @@ int sor_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
             f.robin = robin ? 1 : 0;
             f.uinf = 1.0;
             f.ctl = S.ctl;
-            launch_sor_finish(f, h->stream);
+            if (launch_sor_finish(f, h->stream))
+                return fail(OLLIN_ECUDA, "SOR boundary kernel: shared memory for the Robin edges not available");
             rc = after_launch(h);
             if (rc) return rc;
         }
@@ -883,6 +884,9 @@ int sor_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
 
 int sor_elliptic(ollin_handle* h, WaveSolve& S) {
     const ollin_params& P = h->P;
+    // the Robin edges are staged in shared memory (six doubles per edge point)
+    if (sor_finish_smem(h->L[0].G) > (size_t)200 * 1024)
+        return fail(OLLIN_EINVAL, "ELL_solver = sor on the device supports Nrtotal + Nztotal up to 4260");
     // partial sums of the two passes (every level has the same dimensions)
     const int nparts = sor_pass_blocks(h->L[0].G);
     if (S.nparts < nparts) {

@@ -174,7 +174,10 @@ void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const doubl
                   const int* skip, cudaStream_t s);
 void launch_sor_pass(const SorPassArgs& a, cudaStream_t s);
 int sor_pass_blocks(const LevelGeom& G);
-void launch_sor_finish(const SorFinishArgs& a, cudaStream_t s);
+// Dynamic shared memory of the finish kernel with Robin edges; the launch
+// returns non-zero if the device cannot provide it.
+size_t sor_finish_smem(const LevelGeom& G);
+int launch_sor_finish(const SorFinishArgs& a, cudaStream_t s);
 void launch_add(const LevelGeom& G, double* out, double c, const double* x, cudaStream_t s);
 
 void launch_inject(const InjectArgs& a, cudaStream_t s);
