@@ -329,7 +329,206 @@ __global__ void add_kernel(LevelGeom G, double* out, double c, const double* x) 
     out[o] = arn(c, x[o]);
 }
 
+// ---- mixed-precision solve of the SOR discretisation --------------------
+// Unknowns u(i,j), 1 <= i <= Nr, 1 <= j <= Nz; ghosts mirror the first
+// interior points (u(1-k,j) = u(k,j), u(i,1-k) = u(i,k)).  Equations:
+//   interior  a_i u(i+1,j) + b_i u(i-1,j) + c (u(i,j+1) + u(i,j-1)) + e u - f = 0
+//   r edge    (1+1.5cr) u(Nr,j) - uinf - 0.5cr(4u(Nr-1,j) - u(Nr-2,j))
+//             + 0.5cz_j (u(Nr,j+1) - u(Nr,j-1)) = 0           (and the z edge)
+//   corner    (1+1.5(cr+cz)) u - uinf - 0.5cr(..) - 0.5cz(..) = 0
+// which is the fixed point of sor_elliptic.f90 (sweep, Robin rows, parity).
+constexpr int kMixBX = 32, kMixBY = 4, kMixThreads = kMixBX * kMixBY;
+
+__device__ __forceinline__ int mir(int k) { return k < 1 ? 1 - k : k; }
+
+__device__ __forceinline__ void block_partial(double v, double* out) {
+    __shared__ double red[kMixThreads];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    red[t] = v;
+    __syncthreads();
+    for (int w = kMixThreads / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    if (t == 0) out[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+// FP64 residual r = -R(u) at every unknown (zero on Dirichlet rows), its FP32
+// copy, d = 0, and per-block sums of r^2 over the interior equations.
+__global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_constant__ MixArgs A) {
+    const LevelGeom& G = A.G;
+    const int nr = G.nr, nz = G.nz;
+    const long ld = G.ld;
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    double sq = 0.0;
+    if (i <= nr && j <= nz) {
+        auto U = [&](int p, int q) { return A.u[(size_t)mir(p) + (size_t)mir(q) * ld]; };
+        const size_t o = (size_t)i + (size_t)j * ld;
+        double r = 0.0;
+        if (i <= nr - 1 && j <= nz - 1) {
+            const double R = A.ca[i] * U(i + 1, j) + A.cb[i] * U(i - 1, j) + A.cc * (U(i, j + 1) + U(i, j - 1))
+                             + A.e64[o] * U(i, j) - A.f64[o];
+            r = -R;
+            sq = r * r;
+        } else if (A.robin) {
+            const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
+            double R;
+            if (i == nr && j == nz) {
+                R = (1.0 + 1.5 * (cr + cz)) * U(i, j) - A.uinf - 0.5 * cr * (4.0 * U(i - 1, j) - U(i - 2, j))
+                    - 0.5 * cz * (4.0 * U(i, j - 1) - U(i, j - 2));
+            } else if (i == nr) {
+                R = (1.0 + 1.5 * cr) * U(i, j) - A.uinf - 0.5 * cr * (4.0 * U(i - 1, j) - U(i - 2, j))
+                    + 0.5 * cz * (U(i, j + 1) - U(i, j - 1));
+            } else {
+                R = (1.0 + 1.5 * cz) * U(i, j) - A.uinf - 0.5 * cz * (4.0 * U(i, j - 1) - U(i, j - 2))
+                    + 0.5 * cr * (U(i + 1, j) - U(i - 1, j));
+            }
+            r = -R;
+        }
+        A.r32[o] = (float)r;
+        A.d[o] = 0.0f;
+    }
+    block_partial(sq, A.partial);
+}
+
+// FP32 red-black relaxation of J d = r on the interior equations; the mirror
+// ghost of the first row/column is folded into the diagonal.
+__global__ void __launch_bounds__(kMixThreads) mix_pass_kernel(const __grid_constant__ MixArgs A) {
+    if (A.skip && *A.skip) return;
+    const LevelGeom& G = A.G;
+    const int nr = G.nr, nz = G.nz;
+    const long ld = G.ld;
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int jh = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    int j = 1;
+    if (((i + j) & 1) != A.parity) ++j;
+    j += 2 * jh;
+    double sq = 0.0;
+    if (i <= nr - 1 && j <= nz - 1) {
+        const size_t o = (size_t)i + (size_t)j * ld;
+        float* d = A.d + o;
+        const float a = A.ca32[i], b = A.cb32[i], c = A.cc32;
+        float diag = A.e32[o];
+        float off = a * d[1] + c * d[ld];
+        if (i > 1) off += b * d[-1]; else diag += b;
+        if (j > 1) off += c * d[-ld]; else diag += c;
+        const float res = A.r32[o] - (off + diag * d[0]);
+        sq = (double)res * (double)res;
+        d[0] = d[0] + (float)A.omega * res / diag;
+    }
+    block_partial(sq, A.partial);
+}
+
+// Robin rows of the correction (two-colour Gauss-Seidel along each edge, then
+// the corner), inner residual norm, stop test: done once the inner residual
+// is below ctl->eps or after ctl->maxiter sweeps.
+__global__ void __launch_bounds__(1024) mix_edges_kernel(const __grid_constant__ MixArgs A, const double* p1,
+                                                         const double* p2, int nparts, EllCtl* ctl) {
+    __shared__ double red[1024];
+    if (ctl->done) return;
+    const LevelGeom& G = A.G;
+    const int nr = G.nr, nz = G.nz;
+    const long ld = G.ld;
+    auto D = [&](int p, int q) -> float& { return A.d[(size_t)mir(p) + (size_t)mir(q) * ld]; };
+    if (A.robin) {
+        const float crn = (float)(G.rcol[nr] / G.dr), czn = (float)(G.zrow[nz] / G.dz);
+        for (int colour = 0; colour < 2; ++colour) {
+            for (int j = 1 + colour + 2 * (int)threadIdx.x; j <= nz - 1; j += 2 * blockDim.x) {
+                const float cz = (float)(G.zrow[j] / G.dz);
+                const float rhs = A.r32[(size_t)nr + (size_t)j * ld] + 0.5f * crn * (4.0f * D(nr - 1, j) - D(nr - 2, j))
+                                  - 0.5f * cz * (D(nr, j + 1) - D(nr, j - 1));
+                D(nr, j) = rhs / (1.0f + 1.5f * crn);
+            }
+            for (int i = 1 + colour + 2 * (int)threadIdx.x; i <= nr - 1; i += 2 * blockDim.x) {
+                const float cr = (float)(G.rcol[i] / G.dr);
+                const float rhs = A.r32[(size_t)i + (size_t)nz * ld] + 0.5f * czn * (4.0f * D(i, nz - 1) - D(i, nz - 2))
+                                  - 0.5f * cr * (D(i + 1, nz) - D(i - 1, nz));
+                D(i, nz) = rhs / (1.0f + 1.5f * czn);
+            }
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            const float rhs = A.r32[(size_t)nr + (size_t)nz * ld] + 0.5f * crn * (4.0f * D(nr - 1, nz) - D(nr - 2, nz))
+                              + 0.5f * czn * (4.0f * D(nr, nz - 1) - D(nr, nz - 2));
+            D(nr, nz) = rhs / (1.0f + 1.5f * (crn + czn));
+        }
+    }
+    const int t = threadIdx.x;
+    double acc = 0.0;
+    for (int k = t; k < nparts; k += blockDim.x) acc = acc + p1[k] + p2[k];
+    red[t] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        const double rms = sqrt(red[0] / (double)((nr - 1) * (nz - 1)));
+        const int step = ctl->step + 1;
+        ctl->step = step;
+        ctl->gres = rms;
+        ctl->done = (rms < ctl->eps || step >= ctl->maxiter) ? 1 : 0;
+    }
+}
+
+// u += d at the unknowns (FP64); the ghosts are filled once the solve ends
+__global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_constant__ MixArgs A) {
+    const LevelGeom& G = A.G;
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int lim_r = A.robin ? G.nr : G.nr - 1, lim_z = A.robin ? G.nz : G.nz - 1;
+    if (i > lim_r || j > lim_z) return;  // Dirichlet rows keep their data
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    A.u[o] = A.u[o] + (double)A.d[o];
+}
+
+__global__ void to_float_kernel(LevelGeom G, float* out, const double* in) {
+    const int g = G.g;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    out[o] = (float)in[o];
+}
+
 }  // namespace
+
+int mix_blocks(const LevelGeom& G) {
+    const int nx = (G.nr + kMixBX - 1) / kMixBX, ny = (G.nz + kMixBY - 1) / kMixBY;
+    return nx * ny;
+}
+
+void launch_mix_resid(const MixArgs& a, cudaStream_t s) {
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
+    mix_resid_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_mix_pass(const MixArgs& a, cudaStream_t s) {
+    // (i, jh) grid over the same number of blocks as mix_resid so that the
+    // partial-sum arrays have one size
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
+    mix_pass_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_mix_edges(const MixArgs& a, const double* partial1, const double* partial2, int nparts, EllCtl* ctl,
+                      cudaStream_t s) {
+    mix_edges_kernel<<<1, 1024, 0, s>>>(a, partial1, partial2, nparts, ctl);
+}
+
+void launch_mix_update(const MixArgs& a, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz + blk.y - 1) / blk.y);
+    mix_update_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+    to_float_kernel<<<grd, blk, 0, s>>>(G, out, in);
+}
 
 void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const double* S5, const double* u,
                   const int* skip, cudaStream_t s) {

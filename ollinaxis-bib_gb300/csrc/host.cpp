@@ -121,8 +121,8 @@ int check_params(const ollin_params& P) {
     if (P.idata == OLLIN_IDATA_SCALARPULSE && P.mattertype != OLLIN_MATTER_SCALAR)
         return fail(OLLIN_EINVAL, "Scalar pulse initial data needs scalar field type matter.");
     if ((P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) && P.ell_solver != OLLIN_ELL_WAVE &&
-        P.ell_solver != OLLIN_ELL_SOR)
-        return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave or sor)");
+        P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
+        return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave, sor or mixed)");
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     return OLLIN_OK;
 }
@@ -955,6 +955,222 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
     return OLLIN_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Mixed precision (ELL_solver = "mixed", no counterpart in the reference):
+// the discrete system of sor_elliptic.f90 solved by iterative refinement --
+// FP64 residual and update, FP32 red-black relaxation of each correction to
+// 1e-4 of its residual -- until the FP64 RMS residual of the interior
+// equations is below ELL_epsilon.  Same level sequence as SOR.
+// ---------------------------------------------------------------------------
+int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* outer_out, int* inner_out,
+              double* rms_out) {
+    const ollin_params& P = h->P;
+    DLevel& L = h->L[level];
+    WLevel& w = S.W[level];
+    const int g = h->g;
+    const size_t ncol = (size_t)(L.nr + g);
+    std::vector<double> cab(2 * ncol);
+    std::vector<float> cab32(2 * ncol);
+    for (int i = 1 - g; i <= L.nr; ++i) {
+        const double r = L.rh[i - 1 + g];
+        cab[i - 1 + g] = (1.0 / L.dr + 0.5 / r) / L.dr;
+        cab[ncol + (i - 1 + g)] = (1.0 / L.dr - 0.5 / r) / L.dr;
+        cab32[i - 1 + g] = (float)cab[i - 1 + g];
+        cab32[ncol + (i - 1 + g)] = (float)cab[ncol + (i - 1 + g)];
+    }
+    double* dcol = nullptr;
+    float* f32 = nullptr;
+    const size_t nf = 3 * L.n + 2 * ncol;
+    if (cudaMalloc(&dcol, 2 * ncol * sizeof(double)) != cudaSuccess || cudaMalloc(&f32, nf * sizeof(float)) != cudaSuccess) {
+        cudaFree(dcol);
+        return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
+    }
+    struct FreeOnExit { double* a; float* b; ~FreeOnExit() { cudaFree(a); cudaFree(b); } } free_all{dcol, f32};
+    float* d = f32;
+    float* r32 = f32 + L.n;
+    float* e32 = f32 + 2 * L.n;
+    float* col32 = f32 + 3 * L.n;
+    CUDA_OR_FAIL(cudaMemcpyAsync(dcol, cab.data(), 2 * ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_OR_FAIL(cudaMemcpyAsync(col32, cab32.data(), 2 * ncol * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_OR_FAIL(cudaMemsetAsync(f32, 0, 3 * L.n * sizeof(float), h->stream));
+    const double ec = -2.0 * (1.0 / (L.dr * L.dr) + 1.0 / (L.dz * L.dz));
+    double* eaux = w.ua;
+    double* e = w.va;
+    launch_add(L.G, base_ptr(L, eaux), ec, base_ptr(L, w.S1), h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    const bool s5 = P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
+    const int nparts = mix_blocks(L.G);
+    if (S.nparts < nparts) {
+        cudaFree(S.partial);
+        cudaFree(S.partial2);
+        S.partial = S.partial2 = nullptr;
+        if (cudaMalloc(&S.partial, nparts * sizeof(double)) != cudaSuccess ||
+            cudaMalloc(&S.partial2, nparts * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
+        S.nparts = nparts;
+    }
+    if (!S.partial2 && cudaMalloc(&S.partial2, S.nparts * sizeof(double)) != cudaSuccess)
+        return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
+    MixArgs a{};
+    a.G = L.G;
+    a.u = base_ptr(L, w.u[w.cur]);
+    a.e64 = base_ptr(L, s5 ? e : eaux);
+    a.f64 = base_ptr(L, w.S0);
+    a.ca = dcol + (g - 1);
+    a.cb = dcol + ncol + (g - 1);
+    a.cc = 1.0 / (L.dz * L.dz);
+    // FP32 arrays use the same (i + j*ld) addressing as the FP64 ones
+    const size_t off = (size_t)(g - 1) + (size_t)(g - 1) * L.ld;
+    a.d = d + off;
+    a.r32 = r32 + off;
+    a.e32 = e32 + off;
+    a.ca32 = col32 + (g - 1);
+    a.cb32 = col32 + ncol + (g - 1);
+    a.cc32 = (float)a.cc;
+    a.robin = robin ? 1 : 0;
+    a.uinf = 1.0;
+    a.skip = &S.ctl->done;
+    std::vector<double> hp(nparts);
+    int outer = 0, inner_total = 0;
+    double rms = 0.0;
+    for (;;) {
+        if (s5) {
+            launch_sor_e(L.G, base_ptr(L, e), base_ptr(L, eaux), base_ptr(L, w.S5), base_ptr(L, w.u[w.cur]), nullptr,
+                         h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+        }
+        launch_to_float(L.G, e32 + off, a.e64, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        a.partial = S.partial;
+        launch_mix_resid(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        CUDA_OR_FAIL(cudaMemcpyAsync(hp.data(), S.partial, nparts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        double sum = 0.0;
+        for (double x : hp) sum += x;
+        rms = std::sqrt(sum / (double)((L.nr - 1) * (L.nz - 1)));
+        if (!(rms >= P.ell_epsilon) || outer >= 60) break;  // converged, NaN, or too many refinements
+        ++outer;
+        EllCtl c{};
+        c.maxiter = P.ell_maxiter;
+        c.eps = 1.0e-4 * rms;
+        c.gres = rms;
+        CUDA_OR_FAIL(cudaMemcpyAsync(S.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
+        double omega = 1.0;
+        int n = 0, batch = 32;
+        for (;;) {
+            for (int k = 0; k < batch; ++k) {
+                ++n;
+                for (int ipass = 1; ipass <= 2; ++ipass) {
+                    a.omega = omega;
+                    a.parity = ipass == 1 ? 0 : 1;
+                    a.partial = ipass == 1 ? S.partial : S.partial2;
+                    launch_mix_pass(a, h->stream);
+                    rc = after_launch(h);
+                    if (rc) return rc;
+                    if (n == 1 && ipass == 1) omega = 1.0 / (1.0 - 0.5 * (rjac * rjac));
+                    else omega = 1.0 / (1.0 - 0.25 * (rjac * rjac) * omega);
+                }
+                launch_mix_edges(a, S.partial, S.partial2, nparts, S.ctl, h->stream);
+                rc = after_launch(h);
+                if (rc) return rc;
+            }
+            EllCtl hc{};
+            CUDA_OR_FAIL(cudaMemcpyAsync(&hc, S.ctl, sizeof(hc), cudaMemcpyDeviceToHost, h->stream));
+            CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+            if (hc.done) {
+                inner_total += hc.step;
+                break;
+            }
+            batch = std::min(1024, std::max(32, n / 4));
+        }
+        launch_mix_update(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+    }
+    // parity fill of the solution (the ghosts mirror the first points)
+    SymArgs sy{};
+    sy.G = L.G;
+    sy.nf = 1;
+    sy.st[0] = base_ptr(L, w.u[w.cur]);
+    sy.symr[0] = +1;
+    sy.symz[0] = +1;
+    launch_symmetry(sy, h->stream);
+    rc = after_launch(h);
+    if (rc) return rc;
+    *outer_out = outer;
+    *inner_out = inner_total;
+    *rms_out = rms;
+    return OLLIN_OK;
+}
+
+int mixed_elliptic(ollin_handle* h, WaveSolve& S) {
+    const ollin_params& P = h->P;
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        std::vector<double> ones(L.n, 1.0);
+        CUDA_OR_FAIL(cudaMemcpyAsync(w.u[w.cur], ones.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    }
+    const DLevel& L0 = h->L[0];
+    const double pi = 3.141592653589793;
+    const double rjac = (L0.dz / L0.dr * std::cos(pi / (double)(L0.nr + L0.g))
+                         + L0.dr / L0.dz * std::cos(pi / (double)(L0.nz + L0.g))) / (L0.dz / L0.dr + L0.dr / L0.dz);
+    int outer = 0, inner = 0;
+    double rms = 0.0;
+    int rc = mix_level(h, S, 0, true, rjac, &outer, &inner, &rms);
+    if (rc) return rc;
+    S.steps[0] = outer;
+    S.steps[1] = inner;
+    S.gres = rms;
+    for (int l = 1; l < h->nlev; ++l) {
+        DLevel& F = h->L[l];
+        DLevel& C = h->L[l - 1];
+        InjectArgs a{};
+        a.F = F.G;
+        a.Cg = C.G;
+        a.cin = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.fout = base_ptr(F, S.W[l].u[S.W[l].cur]);
+        a.rminl_f = h->rminl[l]; a.zminl_f = h->zminl[l];
+        a.rminl_c = h->rminl[l - 1]; a.rmaxl_c = h->rmaxl[l - 1];
+        a.zminl_c = h->zminl[l - 1]; a.zmaxl_c = h->zmaxl[l - 1];
+        a.bicubic = P.interp_bicubic;
+        launch_inject(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        int o2 = 0, i2 = 0;
+        double r2 = 0.0;
+        rc = mix_level(h, S, l, false, rjac, &o2, &i2, &r2);
+        if (rc) return rc;
+        S.gres = std::max(S.gres, r2);
+    }
+    for (int l = 1; l < h->nlev; ++l) {
+        DLevel& F = h->L[l];
+        DLevel& C = h->L[l - 1];
+        RestrictArgs a{};
+        a.F = F.G;
+        a.Cg = C.G;
+        a.nf = 1;
+        a.fid[0] = 0;
+        a.fin[0] = base_ptr(F, S.W[l].u[S.W[l].cur]);
+        a.cout[0] = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.rminl_f = h->rminl[l]; a.rmaxl_f = h->rmaxl[l];
+        a.zminl_f = h->zminl[l]; a.zmaxl_f = h->zmaxl[l];
+        a.rminl_c = h->rminl[l - 1]; a.zminl_c = h->zminl[l - 1];
+        a.eqsym = P.eqsym;
+        a.bicubic = P.interp_bicubic;
+        launch_restrict(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+    }
+    return OLLIN_OK;
+}
+
 // The pre-solve part of the elliptic initial data, the solve, and the
 // solution of every level copied to the host (``ell_u``, all points).
 // Scalar pulse (idata_scalarpulse.f90:46-170): the pulse is evaluated here,
@@ -1047,7 +1263,8 @@ int elliptic_data(ollin_handle* h, std::vector<std::vector<double>>& ell_u, std:
             CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
         }
     }
-    rc = (P.ell_solver == OLLIN_ELL_SOR) ? sor_elliptic(h, S) : wave_elliptic(h, S);
+    rc = (P.ell_solver == OLLIN_ELL_SOR) ? sor_elliptic(h, S)
+         : (P.ell_solver == OLLIN_ELL_MIXED) ? mixed_elliptic(h, S) : wave_elliptic(h, S);
     if (rc) return rc;
     h->ell_steps[0] = S.steps[0];
     h->ell_steps[1] = S.steps[1];
