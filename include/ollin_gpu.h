@@ -73,8 +73,8 @@ extern "C" {
 #define OLLIN_ELL_WAVE          1   /* ELL_solver = "wave" (WaveElliptic, the default) */
 #define OLLIN_ELL_SOR           2   /* ELL_solver = "sor"  */
 #define OLLIN_ELL_MIXED         3   /* "mixed": no counterpart in the reference -- the system that "sor"
-                                       converges to, solved by FP64 iterative refinement of FP32 red-black
-                                       relaxation to an RMS residual of ELL_epsilon */
+                                       converges to, solved by FP64 iterative refinement with FP32 multigrid
+                                       corrections, to an RMS residual of ELL_epsilon */
 
 #define OLLIN_PULSE_SHELL       0   /* scalarpulse_type = "shell"     */
 #define OLLIN_PULSE_TORUS       1   /* scalarpulse_type = "torus"     */
@@ -214,7 +214,7 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
  * idata = BrillWave / scalarpulse (wave_elliptic.f90:190-262): steps[0] in
  * the coarse-grid phase, steps[1] in the all-level phase (0 with one level);
  * for SOR the iterations on level 0 and level 1; for "mixed" the FP64
- * refinements and the FP32 sweeps on level 0.  ``gres`` (may be NULL)
+ * refinements and the FP32 V-cycles on level 0.  ``gres`` (may be NULL)
  * receives the final residual.  No counterpart call in the reference, which
  * prints these numbers. */
 int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres);

@@ -330,6 +330,8 @@ __global__ void add_kernel(LevelGeom G, double* out, double c, const double* x) 
 }
 
 // ---- mixed-precision solve of the SOR discretisation --------------------
+// (FP64 residual and update here; the FP32 correction solve is in
+// multigrid.cu)
 // Unknowns u(i,j), 1 <= i <= Nr, 1 <= j <= Nz; ghosts mirror the first
 // interior points (u(1-k,j) = u(k,j), u(i,1-k) = u(i,k)).  Equations:
 //   interior  a_i u(i+1,j) + b_i u(i-1,j) + c (u(i,j+1) + u(i,j-1)) + e u - f = 0
@@ -392,86 +394,6 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
     block_partial(sq, A.partial);
 }
 
-// FP32 red-black relaxation of J d = r on the interior equations; the mirror
-// ghost of the first row/column is folded into the diagonal.
-__global__ void __launch_bounds__(kMixThreads) mix_pass_kernel(const __grid_constant__ MixArgs A) {
-    if (A.skip && *A.skip) return;
-    const LevelGeom& G = A.G;
-    const int nr = G.nr, nz = G.nz;
-    const long ld = G.ld;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int jh = (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    int j = 1;
-    if (((i + j) & 1) != A.parity) ++j;
-    j += 2 * jh;
-    double sq = 0.0;
-    if (i <= nr - 1 && j <= nz - 1) {
-        const size_t o = (size_t)i + (size_t)j * ld;
-        float* d = A.d + o;
-        const float a = A.ca32[i], b = A.cb32[i], c = A.cc32;
-        float diag = A.e32[o];
-        float off = a * d[1] + c * d[ld];
-        if (i > 1) off += b * d[-1]; else diag += b;
-        if (j > 1) off += c * d[-ld]; else diag += c;
-        const float res = A.r32[o] - (off + diag * d[0]);
-        sq = (double)res * (double)res;
-        d[0] = d[0] + (float)A.omega * res / diag;
-    }
-    block_partial(sq, A.partial);
-}
-
-// Robin rows of the correction (two-colour Gauss-Seidel along each edge, then
-// the corner), inner residual norm, stop test: done once the inner residual
-// is below ctl->eps or after ctl->maxiter sweeps.
-__global__ void __launch_bounds__(1024) mix_edges_kernel(const __grid_constant__ MixArgs A, const double* p1,
-                                                         const double* p2, int nparts, EllCtl* ctl) {
-    __shared__ double red[1024];
-    if (ctl->done) return;
-    const LevelGeom& G = A.G;
-    const int nr = G.nr, nz = G.nz;
-    const long ld = G.ld;
-    auto D = [&](int p, int q) -> float& { return A.d[(size_t)mir(p) + (size_t)mir(q) * ld]; };
-    if (A.robin) {
-        const float crn = (float)(G.rcol[nr] / G.dr), czn = (float)(G.zrow[nz] / G.dz);
-        for (int colour = 0; colour < 2; ++colour) {
-            for (int j = 1 + colour + 2 * (int)threadIdx.x; j <= nz - 1; j += 2 * blockDim.x) {
-                const float cz = (float)(G.zrow[j] / G.dz);
-                const float rhs = A.r32[(size_t)nr + (size_t)j * ld] + 0.5f * crn * (4.0f * D(nr - 1, j) - D(nr - 2, j))
-                                  - 0.5f * cz * (D(nr, j + 1) - D(nr, j - 1));
-                D(nr, j) = rhs / (1.0f + 1.5f * crn);
-            }
-            for (int i = 1 + colour + 2 * (int)threadIdx.x; i <= nr - 1; i += 2 * blockDim.x) {
-                const float cr = (float)(G.rcol[i] / G.dr);
-                const float rhs = A.r32[(size_t)i + (size_t)nz * ld] + 0.5f * czn * (4.0f * D(i, nz - 1) - D(i, nz - 2))
-                                  - 0.5f * cr * (D(i + 1, nz) - D(i - 1, nz));
-                D(i, nz) = rhs / (1.0f + 1.5f * czn);
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            const float rhs = A.r32[(size_t)nr + (size_t)nz * ld] + 0.5f * crn * (4.0f * D(nr - 1, nz) - D(nr - 2, nz))
-                              + 0.5f * czn * (4.0f * D(nr, nz - 1) - D(nr, nz - 2));
-            D(nr, nz) = rhs / (1.0f + 1.5f * (crn + czn));
-        }
-    }
-    const int t = threadIdx.x;
-    double acc = 0.0;
-    for (int k = t; k < nparts; k += blockDim.x) acc = acc + p1[k] + p2[k];
-    red[t] = acc;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (t < w) red[t] = red[t] + red[t + w];
-        __syncthreads();
-    }
-    if (t == 0) {
-        const double rms = sqrt(red[0] / (double)((nr - 1) * (nz - 1)));
-        const int step = ctl->step + 1;
-        ctl->step = step;
-        ctl->gres = rms;
-        ctl->done = (rms < ctl->eps || step >= ctl->maxiter) ? 1 : 0;
-    }
-}
-
 // u += d at the unknowns (FP64); the ghosts are filled once the solve ends
 __global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_constant__ MixArgs A) {
     const LevelGeom& G = A.G;
@@ -503,19 +425,6 @@ void launch_mix_resid(const MixArgs& a, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
     dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
     mix_resid_kernel<<<grd, blk, 0, s>>>(a);
-}
-
-void launch_mix_pass(const MixArgs& a, cudaStream_t s) {
-    // (i, jh) grid over the same number of blocks as mix_resid so that the
-    // partial-sum arrays have one size
-    dim3 blk(kMixBX, kMixBY);
-    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
-    mix_pass_kernel<<<grd, blk, 0, s>>>(a);
-}
-
-void launch_mix_edges(const MixArgs& a, const double* partial1, const double* partial2, int nparts, EllCtl* ctl,
-                      cudaStream_t s) {
-    mix_edges_kernel<<<1, 1024, 0, s>>>(a, partial1, partial2, nparts, ctl);
 }
 
 void launch_mix_update(const MixArgs& a, cudaStream_t s) {

@@ -958,41 +958,42 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
 // ---------------------------------------------------------------------------
 // Mixed precision (ELL_solver = "mixed", no counterpart in the reference):
 // the discrete system of sor_elliptic.f90 solved by iterative refinement --
-// FP64 residual and update, FP32 red-black relaxation of each correction to
-// 1e-4 of its residual -- until the FP64 RMS residual of the interior
-// equations is below ELL_epsilon.  Same level sequence as SOR.
+// FP64 residual and update, the correction from FP32 multigrid V-cycles --
+// until the FP64 RMS residual of the interior equations is below
+// ELL_epsilon.  FP32 rounding limits one correction to about 1e-3 of its
+// residual, so each refinement runs a few V-cycles.  Same level sequence as
+// SOR (coarse Robin problem, Dirichlet problems of the finer levels).
 // ---------------------------------------------------------------------------
-int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* outer_out, int* inner_out,
-              double* rms_out) {
+int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_out, int* cycles_out, double* rms_out) {
     const ollin_params& P = h->P;
     DLevel& L = h->L[level];
     WLevel& w = S.W[level];
     const int g = h->g;
     const size_t ncol = (size_t)(L.nr + g);
     std::vector<double> cab(2 * ncol);
-    std::vector<float> cab32(2 * ncol);
     for (int i = 1 - g; i <= L.nr; ++i) {
         const double r = L.rh[i - 1 + g];
         cab[i - 1 + g] = (1.0 / L.dr + 0.5 / r) / L.dr;
         cab[ncol + (i - 1 + g)] = (1.0 / L.dr - 0.5 / r) / L.dr;
-        cab32[i - 1 + g] = (float)cab[i - 1 + g];
-        cab32[ncol + (i - 1 + g)] = (float)cab[ncol + (i - 1 + g)];
     }
     double* dcol = nullptr;
     float* f32 = nullptr;
-    const size_t nf = 3 * L.n + 2 * ncol;
-    if (cudaMalloc(&dcol, 2 * ncol * sizeof(double)) != cudaSuccess || cudaMalloc(&f32, nf * sizeof(float)) != cudaSuccess) {
+    if (cudaMalloc(&dcol, 2 * ncol * sizeof(double)) != cudaSuccess || cudaMalloc(&f32, 3 * L.n * sizeof(float)) != cudaSuccess) {
         cudaFree(dcol);
         return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
     }
-    struct FreeOnExit { double* a; float* b; ~FreeOnExit() { cudaFree(a); cudaFree(b); } } free_all{dcol, f32};
-    float* d = f32;
-    float* r32 = f32 + L.n;
-    float* e32 = f32 + 2 * L.n;
-    float* col32 = f32 + 3 * L.n;
+    MgHierarchy* mg = mg_create(L.nr, L.nz, L.dr, L.dz);
+    struct FreeOnExit {
+        double* a; float* b; MgHierarchy* m;
+        ~FreeOnExit() { cudaFree(a); cudaFree(b); mg_destroy(m); }
+    } free_all{dcol, f32, mg};
+    if (!mg) return fail(OLLIN_ENOMEM, "device allocation failed for the multigrid hierarchy");
     CUDA_OR_FAIL(cudaMemcpyAsync(dcol, cab.data(), 2 * ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CUDA_OR_FAIL(cudaMemcpyAsync(col32, cab32.data(), 2 * ncol * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     CUDA_OR_FAIL(cudaMemsetAsync(f32, 0, 3 * L.n * sizeof(float), h->stream));
+    const size_t off = (size_t)(g - 1) + (size_t)(g - 1) * L.ld;  // FP32 arrays share the level layout
+    float* d = f32 + off;
+    float* r32 = f32 + L.n + off;
+    float* e32 = f32 + 2 * L.n + off;
     const double ec = -2.0 * (1.0 / (L.dr * L.dr) + 1.0 / (L.dz * L.dz));
     double* eaux = w.ua;
     double* e = w.va;
@@ -1003,15 +1004,11 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
     const int nparts = mix_blocks(L.G);
     if (S.nparts < nparts) {
         cudaFree(S.partial);
-        cudaFree(S.partial2);
-        S.partial = S.partial2 = nullptr;
-        if (cudaMalloc(&S.partial, nparts * sizeof(double)) != cudaSuccess ||
-            cudaMalloc(&S.partial2, nparts * sizeof(double)) != cudaSuccess)
+        S.partial = nullptr;
+        if (cudaMalloc(&S.partial, nparts * sizeof(double)) != cudaSuccess)
             return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
         S.nparts = nparts;
     }
-    if (!S.partial2 && cudaMalloc(&S.partial2, S.nparts * sizeof(double)) != cudaSuccess)
-        return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
     MixArgs a{};
     a.G = L.G;
     a.u = base_ptr(L, w.u[w.cur]);
@@ -1020,20 +1017,14 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
     a.ca = dcol + (g - 1);
     a.cb = dcol + ncol + (g - 1);
     a.cc = 1.0 / (L.dz * L.dz);
-    // FP32 arrays use the same (i + j*ld) addressing as the FP64 ones
-    const size_t off = (size_t)(g - 1) + (size_t)(g - 1) * L.ld;
-    a.d = d + off;
-    a.r32 = r32 + off;
-    a.e32 = e32 + off;
-    a.ca32 = col32 + (g - 1);
-    a.cb32 = col32 + ncol + (g - 1);
-    a.cc32 = (float)a.cc;
+    a.d = d;
+    a.r32 = r32;
     a.robin = robin ? 1 : 0;
     a.uinf = 1.0;
-    a.skip = &S.ctl->done;
+    a.partial = S.partial;
     std::vector<double> hp(nparts);
-    int outer = 0, inner_total = 0;
-    double rms = 0.0;
+    int outer = 0, cycles = 0, ncyc = 2;
+    double rms = 0.0, last = 0.0;
     for (;;) {
         if (s5) {
             launch_sor_e(L.G, base_ptr(L, e), base_ptr(L, eaux), base_ptr(L, w.S5), base_ptr(L, w.u[w.cur]), nullptr,
@@ -1041,10 +1032,9 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
             rc = after_launch(h);
             if (rc) return rc;
         }
-        launch_to_float(L.G, e32 + off, a.e64, h->stream);
+        launch_to_float(L.G, e32, a.e64, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
-        a.partial = S.partial;
         launch_mix_resid(a, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
@@ -1054,40 +1044,15 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
         for (double x : hp) sum += x;
         rms = std::sqrt(sum / (double)((L.nr - 1) * (L.nz - 1)));
         if (!(rms >= P.ell_epsilon) || outer >= 60) break;  // converged, NaN, or too many refinements
+        // a refinement that gained less than a decade gets more cycles next time
+        if (outer > 0 && rms > 0.1 * last) ncyc = std::min(ncyc * 2, 16);
+        last = rms;
         ++outer;
-        EllCtl c{};
-        c.maxiter = P.ell_maxiter;
-        c.eps = 1.0e-4 * rms;
-        c.gres = rms;
-        CUDA_OR_FAIL(cudaMemcpyAsync(S.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, h->stream));
-        double omega = 1.0;
-        int n = 0, batch = 32;
-        for (;;) {
-            for (int k = 0; k < batch; ++k) {
-                ++n;
-                for (int ipass = 1; ipass <= 2; ++ipass) {
-                    a.omega = omega;
-                    a.parity = ipass == 1 ? 0 : 1;
-                    a.partial = ipass == 1 ? S.partial : S.partial2;
-                    launch_mix_pass(a, h->stream);
-                    rc = after_launch(h);
-                    if (rc) return rc;
-                    if (n == 1 && ipass == 1) omega = 1.0 / (1.0 - 0.5 * (rjac * rjac));
-                    else omega = 1.0 / (1.0 - 0.25 * (rjac * rjac) * omega);
-                }
-                launch_mix_edges(a, S.partial, S.partial2, nparts, S.ctl, h->stream);
-                rc = after_launch(h);
-                if (rc) return rc;
-            }
-            EllCtl hc{};
-            CUDA_OR_FAIL(cudaMemcpyAsync(&hc, S.ctl, sizeof(hc), cudaMemcpyDeviceToHost, h->stream));
-            CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
-            if (hc.done) {
-                inner_total += hc.step;
-                break;
-            }
-            batch = std::min(1024, std::max(32, n / 4));
-        }
+        mg_load(mg, r32, e32, L.ld, h->stream);
+        mg_solve(mg, a.robin, ncyc, d, L.ld, h->stream);
+        h->launches += 2 + (long long)ncyc * mg_launches_per_cycle(mg, a.robin);
+        CUDA_OR_FAIL(cudaGetLastError());
+        cycles += ncyc;
         launch_mix_update(a, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
@@ -1103,7 +1068,7 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
     rc = after_launch(h);
     if (rc) return rc;
     *outer_out = outer;
-    *inner_out = inner_total;
+    *cycles_out = cycles;
     *rms_out = rms;
     return OLLIN_OK;
 }
@@ -1117,13 +1082,9 @@ int mixed_elliptic(ollin_handle* h, WaveSolve& S) {
         CUDA_OR_FAIL(cudaMemcpyAsync(w.u[w.cur], ones.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     }
-    const DLevel& L0 = h->L[0];
-    const double pi = 3.141592653589793;
-    const double rjac = (L0.dz / L0.dr * std::cos(pi / (double)(L0.nr + L0.g))
-                         + L0.dr / L0.dz * std::cos(pi / (double)(L0.nz + L0.g))) / (L0.dz / L0.dr + L0.dr / L0.dz);
     int outer = 0, inner = 0;
     double rms = 0.0;
-    int rc = mix_level(h, S, 0, true, rjac, &outer, &inner, &rms);
+    int rc = mix_level(h, S, 0, true, &outer, &inner, &rms);
     if (rc) return rc;
     S.steps[0] = outer;
     S.steps[1] = inner;
@@ -1145,7 +1106,7 @@ int mixed_elliptic(ollin_handle* h, WaveSolve& S) {
         if (rc) return rc;
         int o2 = 0, i2 = 0;
         double r2 = 0.0;
-        rc = mix_level(h, S, l, false, rjac, &o2, &i2, &r2);
+        rc = mix_level(h, S, l, false, &o2, &i2, &r2);
         if (rc) return rc;
         S.gres = std::max(S.gres, r2);
     }

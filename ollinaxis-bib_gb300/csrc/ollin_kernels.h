@@ -181,28 +181,30 @@ int launch_sor_finish(const SorFinishArgs& a, cudaStream_t s);
 void launch_add(const LevelGeom& G, double* out, double c, const double* x, cudaStream_t s);
 
 // Mixed-precision solve of the SOR discretisation (the system that the
-// reference's SOR converges to): FP64 residual and update, FP32 red-black
-// relaxation of the correction.  ``robin`` selects the coarse problem (Robin
+// reference's SOR converges to): FP64 residual and update, FP32 multigrid
+// for the correction.  ``robin`` selects the coarse problem (Robin
 // rows at i = Nr and j = Nz are equations) or a fine one (those rows are
 // Dirichlet data).
 struct MixArgs {
     LevelGeom G;
     double* u; const double* e64; const double* f64;
     const double* ca; const double* cb; double cc;   // FP64 coefficients
-    float* d; float* r32; const float* e32;
-    const float* ca32; const float* cb32; float cc32;
+    float* d; float* r32;
     int robin; double uinf;
-    double omega;                                    // inner over-relaxation
-    int parity;
     double* partial;                                 // per-block sums of squares
-    const int* skip;
 };
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
 int mix_blocks(const LevelGeom& G);
-void launch_mix_pass(const MixArgs& a, cudaStream_t s);
-void launch_mix_edges(const MixArgs& a, const double* partial1, const double* partial2, int nparts, EllCtl* ctl,
-                      cudaStream_t s);
 void launch_mix_update(const MixArgs& a, cudaStream_t s);
+
+// FP32 geometric multigrid for the correction equation (multigrid.cu)
+struct MgHierarchy;
+MgHierarchy* mg_create(int n, int m, double dr, double dz);
+void mg_destroy(MgHierarchy* H);
+int mg_levels(const MgHierarchy* H);
+int mg_launches_per_cycle(const MgHierarchy* H, int robin);
+void mg_load(MgHierarchy* H, const float* r, const float* e, long ld, cudaStream_t s);
+void mg_solve(MgHierarchy* H, int robin, int ncycles, float* d, long ld, cudaStream_t s);
 void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s);
 
 void launch_inject(const InjectArgs& a, cudaStream_t s);
