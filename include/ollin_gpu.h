@@ -74,7 +74,8 @@ extern "C" {
 #define OLLIN_ELL_SOR           2   /* ELL_solver = "sor"  */
 #define OLLIN_ELL_MIXED         3   /* "mixed": no counterpart in the reference -- the system that "sor"
                                        converges to, solved by FP64 iterative refinement with FP32 multigrid
-                                       corrections, to an RMS residual of ELL_epsilon */
+                                       corrections, to an RMS residual of ELL_epsilon or the FP64
+                                       rounding floor of the residual, whichever is larger */
 
 #define OLLIN_PULSE_SHELL       0   /* scalarpulse_type = "shell"     */
 #define OLLIN_PULSE_TORUS       1   /* scalarpulse_type = "torus"     */

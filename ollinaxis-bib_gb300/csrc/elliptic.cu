@@ -356,14 +356,15 @@ __device__ __forceinline__ void block_partial(double v, double* out) {
 }
 
 // FP64 residual r = -R(u) at every unknown (zero on Dirichlet rows), its FP32
-// copy, d = 0, and per-block sums of r^2 over the interior equations.
+// copy, d = 0, and per-block sums over the interior equations of r^2 (into
+// partial[b]) and of (e u)^2, the scale of the equation (partial[nblocks+b]).
 __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_constant__ MixArgs A) {
     const LevelGeom& G = A.G;
     const int nr = G.nr, nz = G.nz;
     const long ld = G.ld;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    double sq = 0.0;
+    double sq = 0.0, sc = 0.0;
     if (i <= nr && j <= nz) {
         auto U = [&](int p, int q) { return A.u[(size_t)mir(p) + (size_t)mir(q) * ld]; };
         const size_t o = (size_t)i + (size_t)j * ld;
@@ -373,6 +374,8 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
                              + A.e64[o] * U(i, j) - A.f64[o];
             r = -R;
             sq = r * r;
+            const double eu = A.e64[o] * U(i, j);
+            sc = eu * eu;
         } else if (A.robin) {
             const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
             double R;
@@ -392,6 +395,7 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
         A.d[o] = 0.0f;
     }
     block_partial(sq, A.partial);
+    block_partial(sc, A.partial + gridDim.x * gridDim.y);
 }
 
 // u += d at the unknowns (FP64); the ghosts are filled once the solve ends

@@ -959,10 +959,12 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
 // Mixed precision (ELL_solver = "mixed", no counterpart in the reference):
 // the discrete system of sor_elliptic.f90 solved by iterative refinement --
 // FP64 residual and update, the correction from FP32 multigrid V-cycles --
-// until the FP64 RMS residual of the interior equations is below
-// ELL_epsilon.  FP32 rounding limits one correction to about 1e-3 of its
-// residual, so each refinement runs a few V-cycles.  Same level sequence as
-// SOR (coarse Robin problem, Dirichlet problems of the finer levels).
+// until the RMS residual of the interior equations is below ELL_epsilon or
+// stops falling (the FP64 rounding floor, about 1e-16 of the diagonal terms
+// e*u, which on fine grids lies above 1e-12).  FP32 rounding limits one correction to
+// about 1e-3 of its residual, so each refinement runs a few V-cycles.  Same
+// level sequence as SOR (coarse Robin problem, Dirichlet problems of the
+// finer levels).
 // ---------------------------------------------------------------------------
 int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_out, int* cycles_out, double* rms_out) {
     const ollin_params& P = h->P;
@@ -1002,12 +1004,12 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     if (rc) return rc;
     const bool s5 = P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
     const int nparts = mix_blocks(L.G);
-    if (S.nparts < nparts) {
+    if (S.nparts < 2 * nparts) {
         cudaFree(S.partial);
         S.partial = nullptr;
-        if (cudaMalloc(&S.partial, nparts * sizeof(double)) != cudaSuccess)
+        if (cudaMalloc(&S.partial, 2 * nparts * sizeof(double)) != cudaSuccess)
             return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
-        S.nparts = nparts;
+        S.nparts = 2 * nparts;
     }
     MixArgs a{};
     a.G = L.G;
@@ -1022,8 +1024,8 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     a.robin = robin ? 1 : 0;
     a.uinf = 1.0;
     a.partial = S.partial;
-    std::vector<double> hp(nparts);
-    int outer = 0, cycles = 0, ncyc = 2;
+    std::vector<double> hp(2 * nparts);
+    int outer = 0, cycles = 0, ncyc = 2, flat = 0;
     double rms = 0.0, last = 0.0;
     for (;;) {
         if (s5) {
@@ -1038,14 +1040,20 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         launch_mix_resid(a, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
-        CUDA_OR_FAIL(cudaMemcpyAsync(hp.data(), S.partial, nparts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaMemcpyAsync(hp.data(), S.partial, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
-        double sum = 0.0;
-        for (double x : hp) sum += x;
+        double sum = 0.0, scale = 0.0;
+        for (int k = 0; k < nparts; ++k) { sum += hp[k]; scale += hp[nparts + k]; }
         rms = std::sqrt(sum / (double)((L.nr - 1) * (L.nz - 1)));
+        (void)scale;  // RMS of e*u: the floor is ~1e-16 of it
         if (!(rms >= P.ell_epsilon) || outer >= 60) break;  // converged, NaN, or too many refinements
-        // a refinement that gained less than a decade gets more cycles next time
-        if (outer > 0 && rms > 0.1 * last) ncyc = std::min(ncyc * 2, 16);
+        if (outer > 0) {
+            // at the FP64 floor the residual stops falling
+            flat = (rms > 0.5 * last) ? flat + 1 : 0;
+            if (flat >= 2) break;
+            // a refinement that gained less than a decade gets more cycles next time
+            if (rms > 0.1 * last) ncyc = std::min(ncyc * 2, 16);
+        }
         last = rms;
         ++outer;
         mg_load(mg, r32, e32, L.ld, h->stream);

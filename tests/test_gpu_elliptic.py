@@ -104,8 +104,8 @@ MIXED_BRILL = dict(SOR_BRILL, ell_solver="mixed", ell_epsilon=1e-12)
 
 @pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL], ids=["mixed_pulse_2lev", "mixed_brill_3lev"])
 def test_mixed_precision_solve_matches_fp64_sor(cfg):
-    """ELL_solver = "mixed" (FP64 iterative refinement of FP32 relaxation)
-    solves the discrete system that SOR converges to.  The reference's SOR
+    """ELL_solver = "mixed" (FP64 iterative refinement, FP32 multigrid
+    corrections) solves the discrete system that SOR converges to.  The reference's SOR
     stop test at ELL_epsilon = 1e-8 corresponds to an RMS residual near
     N * 1e-16, so the oracle's FP64 SOR solution is the FP64 solve to compare
     with: the conformal factor agrees to 1e-10 once the FP64 residual of the
@@ -115,8 +115,8 @@ def test_mixed_precision_solve_matches_fp64_sor(cfg):
     o.initial_data()
     e = Evolution(params(cfg))
     e.initial_data()
-    outer, sweeps, rms = e.ell_stats()
-    assert rms < 1e-12 and outer >= 1 and sweeps >= outer
+    outer, cycles, rms = e.ell_stats()
+    assert rms < 1e-12 and outer >= 1 and cycles >= outer
     for lev in o.levels():
         chi = rel_diff(e.download(lev, "chi"), o.get(lev, "chi"))
         dphi = float(abs(e.download(lev, "phi") - o.get(lev, "phi")).max())
