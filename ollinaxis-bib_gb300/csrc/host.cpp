@@ -54,6 +54,12 @@ struct DLevel {
     LevelGeom G{};
     bool last_aux_t0 = true;
     std::vector<double> rh, zh;  // host copies of the coordinates
+    // transfer stencils with the next coarser level (levels >= 1): the
+    // boundary strips this level receives, the overlap it restricts to
+    XferPt* ptab = nullptr;
+    int nptab = 0;
+    XferPt* rtab = nullptr;
+    int nrtab = 0;
 };
 
 }  // namespace
@@ -282,6 +288,98 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
     return a;
 }
 
+// Geometry part of the transfer arguments of level pair (level-1, level).
+ProlongArgs prolong_geometry(ollin_handle* h, int level) {
+    ProlongArgs a{};
+    a.F = h->L[level].G;
+    a.Cg = h->L[level - 1].G;
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
+    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
+    a.bicubic = h->P.interp_bicubic;
+    a.tab = h->L[level].ptab;
+    a.ntab = h->L[level].nptab;
+    return a;
+}
+
+RestrictArgs restrict_geometry(ollin_handle* h, int level) {
+    RestrictArgs a{};
+    a.F = h->L[level].G;
+    a.Cg = h->L[level - 1].G;
+    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
+    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
+    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.eqsym = h->P.eqsym;
+    a.bicubic = h->P.interp_bicubic;
+    a.tab = h->L[level].rtab;
+    a.ntab = h->L[level].nrtab;
+    return a;
+}
+
+// Time weights of finebound.f90:118-145 (the same expressions the oracle
+// evaluates), fixed per launch.
+void prolong_time(ProlongArgs& a, int g) {
+    const double tp = a.tp, t0 = a.t0, tm1 = a.tm1, tl = a.tl;
+    a.imax = (tp == tl) ? g + 2 : g - 1;  // finebound.f90:106-112
+    a.border = (tm1 == 0.0) ? 1 : 2;
+    if (tp == tl) {
+        a.tmode = 0;  // the history weights vanish exactly
+    } else if (a.border == 1) {
+        a.tmode = 1;
+        a.wa = (tl - t0) / (tp - t0);
+        a.wp = (tl - tp) / (t0 - tp);
+    } else {
+        a.tmode = 2;
+        a.wa = ((tl - t0) * (tl - tm1)) / ((tp - t0) * (tp - tm1));
+        a.wp = ((tl - tp) * (tl - tm1)) / ((t0 - tp) * (t0 - tm1));
+        a.wpp = ((tl - tp) * (tl - t0)) / ((tm1 - tp) * (tm1 - t0));
+    }
+}
+
+// Build the transfer stencils of every level pair once.
+int build_transfer_tables(ollin_handle* h) {
+    const int g = h->g;
+    for (int l = 1; l < h->nlev; ++l) {
+        DLevel& F = h->L[l];
+        DLevel& C = h->L[l - 1];
+        F.nptab = prolong_table_size(F.G);
+        if (cudaMalloc(&F.ptab, (size_t)F.nptab * sizeof(XferPt)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the transfer tables");
+        launch_prolong_table(prolong_geometry(h, l), F.ptab, h->stream);
+        int rc = after_launch(h);
+        if (rc) return rc;
+        // the coarse points restrict_kernel writes form a rectangle in (m, n);
+        // find it with the kernel's own expressions, one point wider on each side
+        RestrictArgs ra = restrict_geometry(h, l);
+        const double deltar = (double)(2 * g) * F.dr + 1.0e-10, deltaz = (double)(2 * g) * F.dz + 1.0e-10;
+        const double rmin = (ra.rminl_f < 0.0) ? 0.0 : ra.rminl_f + deltar;
+        const double zmin = (ra.eqsym && ra.zminl_f < 0.0) ? 0.0 : ra.zminl_f + deltaz;
+        const double rmax = ra.rmaxl_f - deltar, zmax = ra.zmaxl_f - deltaz;
+        int m_lo = 1 << 30, m_hi = -1, n_lo = 1 << 30, n_hi = -1;
+        for (int m = 0; m <= C.nr + g - 1; ++m) {
+            const double r0 = ra.rminl_c + (double)m * C.dr;
+            if (r0 > rmin && r0 < rmax) { m_lo = std::min(m_lo, m); m_hi = std::max(m_hi, m); }
+        }
+        for (int n = 0; n <= C.nz + g - 1; ++n) {
+            const double z0 = ra.zminl_c + (double)n * C.dz;
+            if (z0 > zmin && z0 < zmax) { n_lo = std::min(n_lo, n); n_hi = std::max(n_hi, n); }
+        }
+        if (m_hi < 0 || n_hi < 0) { F.nrtab = 0; continue; }
+        m_lo = std::max(0, m_lo - 1); n_lo = std::max(0, n_lo - 1);
+        m_hi = std::min(C.nr + g - 1, m_hi + 1); n_hi = std::min(C.nz + g - 1, n_hi + 1);
+        const int nm = m_hi - m_lo + 1, nn = n_hi - n_lo + 1;
+        F.nrtab = nm * nn;
+        if (cudaMalloc(&F.rtab, (size_t)F.nrtab * sizeof(XferPt)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the transfer tables");
+        launch_restrict_table(ra, F.rtab, m_lo, n_lo, nm, nn, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+    }
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
 int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
     DLevel& F = h->L[level];
     DLevel& C = h->L[level - 1];
@@ -307,10 +405,11 @@ int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
     a.t0 = h->t[level];
     a.tm1 = h->t1[level];
     a.tl = a.t0 + dtw;
-    a.imax = (a.tp == a.tl) ? h->g + 2 : h->g - 1;  // finebound.f90:106-112
-    a.border = (a.tm1 == 0.0) ? 1 : 2;              // finebound.f90:118-122
     a.bicubic = h->P.interp_bicubic;
-    launch_prolong(a, h->stream);
+    a.tab = F.ptab;
+    a.ntab = F.nptab;
+    prolong_time(a, h->g);
+    launch_prolong_tab(a, h->stream);
     return after_launch(h);
 }
 
@@ -331,7 +430,9 @@ int restrict_level(ollin_handle* h, int level) {
     a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
     a.eqsym = h->P.eqsym;
     a.bicubic = h->P.interp_bicubic;
-    launch_restrict(a, h->stream);
+    a.tab = F.rtab;
+    a.ntab = F.nrtab;
+    launch_restrict_tab(a, h->stream);
     return after_launch(h);
 }
 
@@ -596,11 +697,12 @@ int wave_prolong(ollin_handle* h, WaveSolve& S, int level, int out, double dtw) 
     a.t0 = S.t[level];
     a.tm1 = S.t1[level];
     a.tl = a.t0 + dtw;
-    a.imax = (a.tp == a.tl) ? h->g + 2 : h->g - 1;  // finebound.f90:106-112
-    a.border = (a.tm1 == 0.0) ? 1 : 2;
     a.bicubic = h->P.interp_bicubic;
     a.skip = &S.ctl->done;
-    launch_prolong(a, h->stream);
+    a.tab = F.ptab;
+    a.ntab = F.nptab;
+    prolong_time(a, h->g);
+    launch_prolong_tab(a, h->stream);
     return after_launch(h);
 }
 
@@ -622,7 +724,9 @@ int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
     a.eqsym = h->P.eqsym;
     a.bicubic = h->P.interp_bicubic;
     a.skip = &S.ctl->done;
-    launch_restrict(a, h->stream);
+    a.tab = F.rtab;
+    a.ntab = F.nrtab;
+    launch_restrict_tab(a, h->stream);
     return after_launch(h);
 }
 
@@ -1406,6 +1510,11 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
             return rc;
         }
     }
+    rc = build_transfer_tables(h);
+    if (rc) {
+        ollin_gpu_destroy(h);
+        return rc;
+    }
     *out = h;
     return OLLIN_OK;
 }
@@ -1413,8 +1522,11 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
 void ollin_gpu_destroy(ollin_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (DLevel& L : h->L)
+    for (DLevel& L : h->L) {
         if (L.pool) cudaFree(L.pool);
+        if (L.ptab) cudaFree(L.ptab);
+        if (L.rtab) cudaFree(L.rtab);
+    }
     if (h->d_flag) cudaFree(h->d_flag);
     if (h->d_norm) cudaFree(h->d_norm);
     for (cudaEvent_t e : h->ev) cudaEventDestroy(e);

@@ -61,6 +61,18 @@ struct SymArgs {
     const int* skip;             // optional: the launch does nothing while *skip != 0
 };
 
+// One interpolation stencil of a transfer between two levels.  The strip
+// and overlap geometry of a level pair never changes, so the stencils are
+// built once (by the same interp_weights as a direct evaluation) and every
+// transfer launch only applies them.
+struct XferPt {
+    int o_out;           // target element (i + j*ld) in the output level; -1: none
+    int depth;           // prolongation: strip row m (r strip) or n (z strip)
+    int i0, j0, mode;    // source base point; 0 copy, 1 bilinear, 2 bicubic
+    int pad;
+    double w[16];        // bicubic weights [ii+1][jj+1], or auxr, auxz (bilinear)
+};
+
 // Coarse -> fine boundary prolongation (finebound.f90 + bound_interp.inc).
 struct ProlongArgs {
     LevelGeom F;                 // fine level
@@ -76,6 +88,12 @@ struct ProlongArgs {
     double tp, t0, tm1, tl;
     int imax, border, bicubic;
     const int* skip;             // optional: the launch does nothing while *skip != 0
+    // table-driven launch (launch_prolong_tab): stencils of the strips for
+    // imax = ghost+2 and the time weights of finebound.f90:118-145
+    const XferPt* tab;
+    int ntab;
+    int tmode;                   // 0: tp == tl (coarse value), 1: linear, 2: quadratic in time
+    double wa, wp, wpp;          // weights of the coarse value, var_p and the older history
 };
 
 // Fine -> coarse restriction (restrict.f90 + restrict_interp.inc).
@@ -89,6 +107,8 @@ struct RestrictArgs {
     double rminl_c, zminl_c;
     int eqsym, bicubic;
     const int* skip;             // optional: the launch does nothing while *skip != 0
+    const XferPt* tab;           // table-driven launch (launch_restrict_tab)
+    int ntab;
 };
 
 // Interpolation of one grid function of a coarser level to every point of a
@@ -208,6 +228,13 @@ void mg_solve(MgHierarchy* H, int robin, int ncycles, float* d, long ld, cudaStr
 void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s);
 
 void launch_inject(const InjectArgs& a, cudaStream_t s);
+
+// stencil tables of a level pair (built once per handle)
+int prolong_table_size(const LevelGeom& F);
+void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s);
+void launch_prolong_tab(const ProlongArgs& a, cudaStream_t s);
+void launch_restrict_table(const RestrictArgs& a, XferPt* tab, int m_lo, int n_lo, int nm, int nn, cudaStream_t s);
+void launch_restrict_tab(const RestrictArgs& a, cudaStream_t s);
 void launch_wave_stage(const WaveArgs& a, cudaStream_t s);
 int wave_stage_blocks(const LevelGeom& G);
 void launch_wave_residual(const double* partial, int nparts, int nr, int nz, EllCtl* ctl, cudaStream_t s);

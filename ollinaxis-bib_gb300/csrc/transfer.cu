@@ -183,6 +183,134 @@ __global__ void __launch_bounds__(128) restrict_kernel(const __grid_constant__ R
     }
 }
 
+// ---- table-driven transfers ------------------------------------------------
+__device__ void to_xfer(const InterpPt& p, XferPt& x) {
+    x.i0 = p.i0;
+    x.j0 = p.j0;
+    x.mode = p.mode;
+    for (int a = 0; a < 4; ++a)
+        for (int b = 0; b < 4; ++b) x.w[a * 4 + b] = p.w[a][b];
+}
+
+__device__ __forceinline__ double xfer_apply(const LevelGeom& G, const double* f, const XferPt& p) {
+    const long ld = G.ld;
+    if (p.mode == 0) return f[p.i0 + (long)p.j0 * ld];
+    if (p.mode == 1) {
+        const double* b = f + p.i0 + (long)p.j0 * ld;
+        const double ar = p.w[0], az = p.w[1];
+        double v = mul(mul(b[0], sub(1.0, ar)), sub(1.0, az));
+        v = add(v, mul(mul(b[1], ar), sub(1.0, az)));
+        v = add(v, mul(mul(b[ld], sub(1.0, ar)), az));
+        v = add(v, mul(mul(b[1 + ld], ar), az));
+        return v;
+    }
+    double v = 0.0;
+    const double* b = f + (p.i0 - 1) + (long)(p.j0 - 1) * ld;
+#pragma unroll
+    for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) v = add(v, mul(p.w[ii * 4 + jj], b[ii + (long)jj * ld]));
+    return v;
+}
+
+// the strip points of prolong_kernel for imax = ghost+2, in the same order
+__global__ void __launch_bounds__(128) prolong_table_kernel(const __grid_constant__ ProlongArgs a, XferPt* tab) {
+    const LevelGeom& F = a.F;
+    const int g = F.g;
+    const int imax = g + 2;
+    const int nstrip_r = (imax + 1) * (F.nz + g);
+    const int nstrip_z = (imax + 1) * (F.nr + g);
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= nstrip_r + nstrip_z) return;
+    double r0, z0;
+    int depth;
+    if (t < nstrip_r) {
+        const int m = t / (F.nz + g), n = t % (F.nz + g);
+        r0 = sub(a.rmaxl_f, mul((double)m, F.dr));
+        z0 = add(a.zminl_f, mul((double)n, F.dz));
+        depth = m;
+    } else {
+        const int q = t - nstrip_r;
+        const int n = q / (F.nr + g), m = q % (F.nr + g);
+        r0 = add(a.rminl_f, mul((double)m, F.dr));
+        z0 = sub(a.zmaxl_f, mul((double)n, F.dz));
+        depth = n;
+    }
+    XferPt x{};
+    x.depth = depth;
+    const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
+    const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
+    x.o_out = -1;
+    if (i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz) {
+        InterpPt p;
+        interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
+        to_xfer(p, x);
+        x.o_out = i + j * F.ld;
+    }
+    tab[t] = x;
+}
+
+// thread per (stencil, field); the strips of a smaller imax are the entries
+// with depth <= imax
+__global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant__ ProlongArgs a) {
+    if (a.skip && *a.skip) return;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= a.ntab * a.nf) return;
+    const int e = t % a.ntab, k = t / a.ntab;
+    const XferPt& P = a.tab[e];
+    if (P.o_out < 0 || P.depth > a.imax) return;
+    const int f = a.fid[k];
+    const double aux2 = xfer_apply(a.Cg, a.cin[f], P);
+    double v;
+    if (a.tmode == 0) v = aux2;
+    else if (a.tmode == 1) v = add(mul(a.wa, aux2), mul(a.wp, a.fp[f][P.o_out]));
+    else v = add(add(mul(a.wa, aux2), mul(a.wp, a.fp[f][P.o_out])), mul(a.wpp, a.fpp[f][P.o_out]));
+    a.fout[f][P.o_out] = v;
+}
+
+// the coarse points of restrict_kernel inside the overlap rectangle
+// m_lo..m_lo+nm-1, n_lo..n_lo+nn-1
+__global__ void __launch_bounds__(128) restrict_table_kernel(const __grid_constant__ RestrictArgs a, XferPt* tab,
+                                                             int m_lo, int n_lo, int nm, int nn) {
+    const LevelGeom& C = a.Cg;
+    const LevelGeom& F = a.F;
+    const int g = C.g;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= nm * nn) return;
+    const int m = m_lo + t % nm, n = n_lo + t / nm;
+    XferPt x{};
+    x.o_out = -1;
+    const double r0 = add(a.rminl_c, mul((double)m, C.dr));
+    const double z0 = add(a.zminl_c, mul((double)n, C.dz));
+    const double deltar = add(mul((double)(2 * g), F.dr), 1.0e-10);
+    const double deltaz = add(mul((double)(2 * g), F.dz), 1.0e-10);
+    const double rmin = (a.rminl_f < 0.0) ? 0.0 : a.rminl_f + deltar;
+    const double zmin = (a.eqsym && a.zminl_f < 0.0) ? 0.0 : a.zminl_f + deltaz;
+    const double rmax = a.rmaxl_f - deltar, zmax = a.zmaxl_f - deltaz;
+    if (r0 > rmin && r0 < rmax && z0 > zmin && z0 < zmax) {
+        const int i = (int)round((r0 - C.rcol[1 - g]) / C.dr) + 1 - g;
+        const int j = (int)round((z0 - C.zrow[1 - g]) / C.dz) + 1 - g;
+        if (i >= 1 - g && i <= C.nr && j >= 1 - g && j <= C.nz) {
+            InterpPt p;
+            interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p);
+            to_xfer(p, x);
+            x.o_out = i + j * C.ld;
+        }
+    }
+    tab[t] = x;
+}
+
+__global__ void __launch_bounds__(256) restrict_tab_kernel(const __grid_constant__ RestrictArgs a) {
+    if (a.skip && *a.skip) return;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= a.ntab * a.nf) return;
+    const int e = t % a.ntab, k = t / a.ntab;
+    const XferPt& P = a.tab[e];
+    if (P.o_out < 0) return;
+    const int f = a.fid[k];
+    a.cout[f][P.o_out] = xfer_apply(a.F, a.fin[f], P);
+}
+
 // ---- injection: interpolate a coarser level to every point of a finer one --
 // (wave_elliptic.f90:270-328; sor_elliptic.f90:268-320)
 __global__ void __launch_bounds__(128) inject_kernel(const __grid_constant__ InjectArgs a) {
@@ -315,6 +443,28 @@ void launch_symmetry(const SymArgs& a, cudaStream_t s) {
 void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
     const int n = (a.imax + 1) * (a.F.nz + a.F.g) + (a.imax + 1) * (a.F.nr + a.F.g);
     prolong_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
+}
+
+int prolong_table_size(const LevelGeom& F) { return (F.g + 3) * (F.nz + F.g) + (F.g + 3) * (F.nr + F.g); }
+
+void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s) {
+    const int n = prolong_table_size(a.F);
+    prolong_table_kernel<<<(n + 127) / 128, 128, 0, s>>>(a, tab);
+}
+
+void launch_prolong_tab(const ProlongArgs& a, cudaStream_t s) {
+    const long n = (long)a.ntab * a.nf;
+    prolong_tab_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+}
+
+void launch_restrict_table(const RestrictArgs& a, XferPt* tab, int m_lo, int n_lo, int nm, int nn, cudaStream_t s) {
+    const int n = nm * nn;
+    if (n > 0) restrict_table_kernel<<<(n + 127) / 128, 128, 0, s>>>(a, tab, m_lo, n_lo, nm, nn);
+}
+
+void launch_restrict_tab(const RestrictArgs& a, cudaStream_t s) {
+    const long n = (long)a.ntab * a.nf;
+    if (n > 0) restrict_tab_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
 }
 
 void launch_inject(const InjectArgs& a, cudaStream_t s) {
