@@ -29,9 +29,8 @@ __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ 
         a.st[F_CHI][o] = exp(-2.0 * a.st[F_PHI][o]);
     } else {
         const double rc = r * C;
-        double q = (A * B - rc * rc) * H;  // hdet = 1
-        q = cbrt(q);                        // (det)^(1/3)
-        const double iq = 1.0 / q;
+        const double q = (A * B - rc * rc) * H;  // hdet = 1
+        const double iq = rcbrt(q);              // 1/(det)^(1/3)
         A = A * iq; B = B * iq; C = C * iq; H = H * iq;
         a.st[F_A][o] = A; a.st[F_B][o] = B; a.st[F_C][o] = C; a.st[F_H][o] = H;
     }

@@ -23,16 +23,26 @@ __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, 
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 
 // ---- parity ghost fill -------------------------------------------------
+// thread space: the g ghost columns i <= 0 over all rows, then (eqsym) the
+// g ghost rows j <= 0 for i >= 1; the corner points belong to the columns
 __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
     if (a.skip && *a.skip) return;
     const LevelGeom& G = a.G;
     const int g = G.g;
-    // thread space: all points (i,j) with i <= 0 or (eqsym and j <= 0)
-    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    if (i > G.nr || j > G.nz) return;
+    const int ncol = g * (G.nz + g);
+    const int nrow = G.eqsym ? g * G.nr : 0;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= ncol + nrow) return;
+    int i, j;
+    if (t < ncol) {
+        i = 1 - g + t % g;
+        j = 1 - g + t / g;
+    } else {
+        const int q = t - ncol;
+        i = 1 + q % G.nr;
+        j = 1 - g + q / G.nr;
+    }
     const bool gi = i <= 0, gj = G.eqsym && j <= 0;
-    if (!gi && !gj) return;
     const int si = gi ? 1 - i : i, sj = gj ? 1 - j : j;
     const size_t o = (size_t)i + (size_t)j * G.ld, os = (size_t)si + (size_t)sj * G.ld;
     for (int k = 0; k < a.nf; ++k) {
@@ -436,8 +446,8 @@ dim3 full_grid(const LevelGeom& G, dim3 blk) {
 }  // namespace
 
 void launch_symmetry(const SymArgs& a, cudaStream_t s) {
-    dim3 blk(64, 4);
-    symmetry_kernel<<<full_grid(a.G, blk), blk, 0, s>>>(a);
+    const int n = a.G.g * (a.G.nz + a.G.g) + (a.G.eqsym ? a.G.g * a.G.nr : 0);
+    symmetry_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
 }
 
 void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
