@@ -110,7 +110,8 @@ int check_params(const ollin_params& P) {
     if (P.order != 4) return fail(OLLIN_EINVAL, "order must be \"four\" (4)");
     if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
     if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
-    if (!P.eqsym) return fail(OLLIN_EINVAL, "only equatorial symmetry (eqsym) is supported");
+    if (!P.eqsym && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE))
+        return fail(OLLIN_EINVAL, "elliptic initial data needs equatorial symmetry (eqsym) on the device");
     if (P.ghost != 0 && P.ghost != 3) return fail(OLLIN_EINVAL, "ghost must be 3 for order four");
     if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
@@ -140,6 +141,8 @@ int alloc_level(ollin_handle* h, DLevel& L, int level) {
     L.g = g;
     L.nr = P.nrtotal;
     L.nz = P.nztotal;
+    // without equatorial symmetry Nz + ghost is made odd (setupboxes.f90:131-135)
+    if (!P.eqsym && (L.nz + g) % 2 == 0) L.nz += 1;
     L.ld = ((L.nr + g + 31) / 32) * 32;
     L.rows = L.nz + g;
     L.n = (size_t)L.ld * L.rows;
@@ -169,7 +172,9 @@ int alloc_level(ollin_handle* h, DLevel& L, int level) {
         host[(size_t)(L.nr + g) + (i - 1 + g)] = 1.0 / r;
     }
     for (int j = 1 - g; j <= L.nz; ++j) {
-        const double z = ((double)(0 + j) - 0.5) * L.dz;
+        // evolve.f90:57-70: the equator on a cell face (eqsym) or z centred on the box
+        const double z = P.eqsym ? ((double)(0 + j) - 0.5) * L.dz
+                                 : 0.0 + ((double)(0 + j) - 0.5 * (double)(L.nz - g + 1)) * L.dz;
         L.zh[j - 1 + g] = z;
         host[(size_t)(L.nr + g) * 2 + (j - 1 + g)] = z;
     }
@@ -484,7 +489,7 @@ int onestep(ollin_handle* h, int level) {
         if (h->ktime) {
             CUDA_OR_FAIL(cudaEventRecord(h->ev[h->ev_used + 1], h->stream));
             h->ev_used += 2;
-            h->rhs_point_stages += (double)L.nr * (double)L.nz;
+            h->rhs_point_stages += (double)L.nr * (double)(L.nz - L.G.jlo + 1);
             h->rhs_launches++;
         }
         if (level > 0) {
@@ -502,7 +507,7 @@ int onestep(ollin_handle* h, int level) {
     h->t1[level] = h->t[level];
     h->s[level] = h->s[level] + 1;
     h->t[level] = h->t[level] + dt;
-    h->point_updates += (double)L.nr * (double)L.nz;
+    h->point_updates += (double)L.nr * (double)(L.nz - L.G.jlo + 1);
     if (level < h->nlev - 1) {
         int rc = onestep(h, level + 1);
         if (rc) return rc;

@@ -65,11 +65,15 @@ struct SymArgs {
 // and overlap geometry of a level pair never changes, so the stencils are
 // built once (by the same interp_weights as a direct evaluation) and every
 // transfer launch only applies them.
+// o_out of a stencil that writes nothing (offsets of points in rows j <= 0
+// are negative, so no negative value can serve)
+constexpr int kNoPoint = -2147483647 - 1;
+
 struct XferPt {
-    int o_out;           // target element (i + j*ld) in the output level; -1: none
-    int depth;           // prolongation: strip row m (r strip) or n (z strip)
+    int o_out;           // target element (i + j*ld) in the output level; kNoPoint: none
+    int depth;           // prolongation: strip row m (r strip) or n (z strips)
     int i0, j0, mode;    // source base point; 0 copy, 1 bilinear, 2 bicubic
-    int pad;
+    int cover;           // prolongation: a later strip writes this point when imax >= cover
     double w[16];        // bicubic weights [ii+1][jj+1], or auxr, auxz (bilinear)
 };
 

@@ -223,34 +223,51 @@ __device__ __forceinline__ double xfer_apply(const LevelGeom& G, const double* f
     return v;
 }
 
-// the strip points of prolong_kernel for imax = ghost+2, in the same order
+// The strip points of finebound.f90 for imax = ghost+2: the upper r strip
+// (:153-187), the upper z strip (:296-346) and, without equatorial symmetry,
+// the lower z strip (:351-397).  The reference writes the strips in that
+// order, so a point that a later strip also writes takes the later value:
+// ``cover`` is the strip depth from which a later strip reaches the point.
 __global__ void __launch_bounds__(128) prolong_table_kernel(const __grid_constant__ ProlongArgs a, XferPt* tab) {
     const LevelGeom& F = a.F;
     const int g = F.g;
     const int imax = g + 2;
     const int nstrip_r = (imax + 1) * (F.nz + g);
     const int nstrip_z = (imax + 1) * (F.nr + g);
+    const int nstrips_z = F.eqsym ? 1 : 2;
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (t >= nstrip_r + nstrip_z) return;
+    if (t >= nstrip_r + nstrips_z * nstrip_z) return;
     double r0, z0;
-    int depth;
+    int depth, strip;
     if (t < nstrip_r) {
         const int m = t / (F.nz + g), n = t % (F.nz + g);
         r0 = sub(a.rmaxl_f, mul((double)m, F.dr));
         z0 = add(a.zminl_f, mul((double)n, F.dz));
         depth = m;
-    } else {
+        strip = 0;
+    } else if (t < nstrip_r + nstrip_z) {
         const int q = t - nstrip_r;
         const int n = q / (F.nr + g), m = q % (F.nr + g);
         r0 = add(a.rminl_f, mul((double)m, F.dr));
         z0 = sub(a.zmaxl_f, mul((double)n, F.dz));
         depth = n;
+        strip = 1;
+    } else {
+        const int q = t - nstrip_r - nstrip_z;
+        const int n = q / (F.nr + g), m = q % (F.nr + g);
+        r0 = add(a.rminl_f, mul((double)m, F.dr));
+        z0 = add(a.zminl_f, mul((double)n, F.dz));
+        depth = n;
+        strip = 2;
     }
     XferPt x{};
     x.depth = depth;
     const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
     const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
-    x.o_out = -1;
+    x.o_out = kNoPoint;
+    x.cover = 1 << 30;
+    if (strip == 0) x.cover = F.nz - j;                                    // the upper z strip reaches row j
+    if (strip <= 1 && !F.eqsym) x.cover = min(x.cover, j - (1 - g));       // the lower z strip reaches row j
     if (i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz) {
         InterpPt p;
         interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
@@ -268,7 +285,7 @@ __global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant_
     if (t >= a.ntab * a.nf) return;
     const int e = t % a.ntab, k = t / a.ntab;
     const XferPt& P = a.tab[e];
-    if (P.o_out < 0 || P.depth > a.imax) return;
+    if (P.o_out == kNoPoint || P.depth > a.imax || P.cover <= a.imax) return;
     const int f = a.fid[k];
     const double aux2 = xfer_apply(a.Cg, a.cin[f], P);
     double v;
@@ -289,7 +306,7 @@ __global__ void __launch_bounds__(128) restrict_table_kernel(const __grid_consta
     if (t >= nm * nn) return;
     const int m = m_lo + t % nm, n = n_lo + t / nm;
     XferPt x{};
-    x.o_out = -1;
+    x.o_out = kNoPoint;
     const double r0 = add(a.rminl_c, mul((double)m, C.dr));
     const double z0 = add(a.zminl_c, mul((double)n, C.dz));
     const double deltar = add(mul((double)(2 * g), F.dr), 1.0e-10);
@@ -316,7 +333,7 @@ __global__ void __launch_bounds__(256) restrict_tab_kernel(const __grid_constant
     if (t >= a.ntab * a.nf) return;
     const int e = t % a.ntab, k = t / a.ntab;
     const XferPt& P = a.tab[e];
-    if (P.o_out < 0) return;
+    if (P.o_out == kNoPoint) return;
     const int f = a.fid[k];
     a.cout[f][P.o_out] = xfer_apply(a.F, a.fin[f], P);
 }
@@ -455,7 +472,9 @@ void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
     prolong_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
 }
 
-int prolong_table_size(const LevelGeom& F) { return (F.g + 3) * (F.nz + F.g) + (F.g + 3) * (F.nr + F.g); }
+int prolong_table_size(const LevelGeom& F) {
+    return (F.g + 3) * (F.nz + F.g) + (F.eqsym ? 1 : 2) * (F.g + 3) * (F.nr + F.g);
+}
 
 void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s) {
     const int n = prolong_table_size(a.F);

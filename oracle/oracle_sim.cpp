@@ -252,7 +252,7 @@ void finebound(Sim& S, int level, double dtw) {
                     }
                 } else {
                     if (n <= g - 1) {
-                        const auto& H = F.hist[e.name + "_zR"];
+                        const auto& H = F.hist[e.name + (bd == 'z' ? "_zR" : "_zL")];
                         h0 = H[hz(F, ii, n, 0)]; h1 = H[hz(F, ii, n, 1)];
                     }
                 }
@@ -276,7 +276,14 @@ void finebound(Sim& S, int level, double dtw) {
             const double z0 = S.zmaxl[level] - (double)n * S.dzl[level];
             point(r0, z0, m, n, 'z');
         }
-    if (!S.P.eqsym) throw std::runtime_error("oracle: finebound lower-z strip (eqsym=.false.) not restated");
+    // lower z boundary without equatorial symmetry (finebound.f90:351-397)
+    if (!S.P.eqsym)
+        for (int n = 0; n <= jmax; ++n)
+            for (int m = 0; m <= F.Nr + g - 1; ++m) {
+                const double r0 = S.rminl[level] + (double)m * S.drl[level];
+                const double z0 = S.zminl[level] + (double)n * S.dzl[level];
+                point(r0, z0, m, n, 'l');
+            }
 }
 
 // restrict.f90:2-169 with restrict_interp.inc

@@ -44,6 +44,11 @@ CASES = {
                          ilapse="one", mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5,
                          shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, scalardiss=0.02,
                          _steps=[0, 1, 3]),
+    # no equatorial symmetry: the lower z edge is a physical (radiative)
+    # boundary on level 0 and a refinement boundary (lower finebound strip)
+    # on level 1; Gamma-driver shift for the lopsided stencils at both edges
+    "noeqsym_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, eqsym=False,
+                          shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 2]),
     # elliptic initial data (WaveElliptic, the default ELL_solver): a centred
     # scalar pulse solved to convergence on one level
     "ell_pulse_1lev": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.5, dz0=0.5, idata="scalarpulse",

@@ -96,6 +96,26 @@ def test_scalar_field_with_shift():
     run(cfg, 8, check_every=4)
 
 
+def test_no_equatorial_symmetry_three_levels():
+    """eqsym = .false.: the grid spans both signs of z, the lower z edge is
+    a radiative boundary on level 0 and a refinement boundary (the lower
+    finebound strip) on the finer levels; constraint norms as well."""
+    cfg = dict(C1, nrtotal=32, nztotal=32, eqsym=0, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+    o, e, w = run(cfg, 16, check_every=8)
+    for lev in o.levels():
+        o.constraints(lev)
+        for nm in ["ham", "mom_r", "mom_z"]:
+            ng, no = e.norms(lev, nm), o.norms(lev, nm)
+            for k in (2, 3):
+                assert abs(ng[k] - no[k]) <= 1e-8 * abs(no[k]), (lev, nm, k, ng[k], no[k])
+
+
+def test_no_equatorial_symmetry_odd_grid_icn():
+    """Nztotal + ghost even is made odd (setupboxes.f90:131-135); ICN."""
+    cfg = dict(C1, nrtotal=24, nztotal=25, nl0=1, eqsym=0, integrator="icn", icniter=3, dr0=0.25, dz0=0.25)
+    run(cfg, 8, check_every=4)
+
+
 def test_norms_match_oracle():
     o, e = make_pair(dict(C1, nl0=1))
     for _ in range(3):
