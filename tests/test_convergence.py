@@ -1,0 +1,33 @@
+"""Fourth-order self-convergence of the evolution scheme (the oracle, which
+follows the reference's Fortran): with smooth data on one level, trK and phi
+(vacuum gauge pulse) and trK and the scalar field (scalar pulse) converge at
+fourth order; the GPU test in test_gpu_convergence.py checks that the device
+reproduces the same factors."""
+import pytest
+
+from convergence_util import RESOLUTIONS, T_END, config, factors, prepare
+from oracle_bind import Oracle
+from parity_util import params
+
+
+def oracle_origin_values(matter, fields):
+    out = []
+    for n, h in RESOLUTIONS:
+        o = Oracle(params(config(n, h, matter)))
+        o.initial_data()
+        r, z = o.get(0, "r"), o.get(0, "z")
+        prepare(o, matter, lambda nm: o.get(0, nm), lambda nm, v: o.set(0, nm, v))
+        o.initialize()
+        for _ in range(int(round(T_END / (0.25 * h)))):
+            o.step()
+        out.append([o.norms(0, f)[4] for f in fields])
+    return out
+
+
+@pytest.mark.parametrize("matter,fields", [(False, ["trK", "phi"]), (True, ["trK", "scalar_phi"])],
+                         ids=["gauge_pulse", "scalar_pulse"])
+def test_fourth_order_self_convergence(matter, fields):
+    vals = oracle_origin_values(matter, fields)
+    for k, f in enumerate(fields):
+        c = factors([v[k] for v in vals])
+        assert 13.0 < c < 20.0, "%s: convergence factor %.2f (fourth order is 16)" % (f, c)
