@@ -307,9 +307,43 @@ def run_gpu(args):
                 "clocks": clocks}
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(threads=os.cpu_count(), seconds=args.cpu_seconds)
+        if not args.no_elliptic:
+            line["elliptic"] = elliptic_precision()
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
+
+
+def elliptic_precision():
+    """The precision pattern of the Brill-wave configuration: the conformal
+    factor of Holz Brill data (a0 = 1, sigma = 1) on 4 box-in-box levels of
+    1024^2 by the mixed solver (FP32 multigrid corrections, FP64 residual
+    refinement), timed through the C ABI; beside it, on one 256^2 level,
+    the same solve against the FP64 SOR of the reference algorithm."""
+    import numpy as np
+    from ollin.gpu import Evolution
+    from ollin.params import params_from_dict
+    base = dict(eqsym=1, order="four", integrator="rk4", ilapse="one", idata="BrillWave", brill_a0=1.0,
+                brill_sr0=1.0, brill_sz0=1.0, dr0=0.04, dz0=0.04)
+
+    def solve(cfg):
+        e = Evolution(params_from_dict(dict(base, **cfg)))
+        t = time.perf_counter()
+        e.initial_data()
+        dt = time.perf_counter() - t
+        chi = [e.download(lev, "chi") for lev in e.levels()]
+        stats = e.ell_stats()
+        e.close()
+        return dt, stats, chi
+
+    solve(dict(nrtotal=64, nztotal=64, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))  # warm-up
+    t_c3, st_c3, _ = solve(dict(nrtotal=1024, nztotal=1024, nl0=3, ell_solver="mixed", ell_epsilon=1e-12))
+    t_mx, st_mx, chi_mx = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))
+    t_sor, st_sor, chi_sor = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="sor"))
+    return {"workload": "Brill wave a0=1, 4 levels of 1024x1024, dr0=0.04, mixed solver to 1e-12 or the FP64 floor",
+            "seconds": t_c3, "refinements_level0": st_c3[0], "vcycles_level0": st_c3[1], "final_rms_residual": st_c3[2],
+            "vs_fp64_sor_256": {"mixed_seconds": t_mx, "sor_seconds": t_sor, "sor_iterations": st_sor[0],
+                                "max_abs_chi_diff": float(np.max(np.abs(chi_mx[0] - chi_sor[0])))}}
 
 
 def main():
@@ -320,6 +354,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-elliptic", action="store_true", help="skip the mixed-precision elliptic measurement")
     ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
     ap.add_argument("--size", type=int, default=512, help="points per level per direction")
     args = ap.parse_args()

@@ -174,25 +174,28 @@ def generate(outputs, fname):
     repl, reduced = sp.cse(allexprs, symbols=sp.numbered_symbols("c"), optimizations="basic")
     after_cse = sum(cost(e) for _, e in repl) + sum(cost(e) for e in reduced)
     pr = CudaPrinter()
-    # definitions in dependency order (CSE temporaries may use spec temporaries)
-    defs = list(repl) + [(s, e) for (s, _), e in zip(opt, reduced[:len(opt)])]
-    defined = set(syms.values())
-    pending = list(defs)
+    # Emission order: depth-first from each output, every definition placed
+    # just before its first use, so that temporaries live briefly (the
+    # register pressure of the straight-line code follows the text order).
+    defs = dict(list(repl) + [(s, e) for (s, _), e in zip(opt, reduced[:len(opt)])])
+    inputs = set(syms.values())
+    emitted = set()
     lines = []
-    while pending:
-        progress = False
-        rest = []
-        for s, e in pending:
-            if e.free_symbols <= defined:
-                lines.append("    const double %s = %s;" % (s, pr.doprint(e)))
-                defined.add(s)
-                progress = True
-            else:
-                rest.append((s, e))
-        if not progress:
-            raise RuntimeError("cyclic definitions")
-        pending = rest
+
+    def emit(sym):
+        if sym in emitted or sym in inputs:
+            return
+        e = defs[sym]
+        for dep in sorted(e.free_symbols, key=lambda x: x.name):
+            if dep in defs:
+                emit(dep)
+        lines.append("    const double %s = %s;" % (sym, pr.doprint(e)))
+        emitted.add(sym)
+
     for o, e in zip(outputs, reduced[len(opt):]):
+        for dep in sorted(e.free_symbols, key=lambda x: x.name):
+            if dep in defs:
+                emit(dep)
         lines.append("    o.%s = %s;" % (o, pr.doprint(e)))
     return lines, before, after, after_cse
 

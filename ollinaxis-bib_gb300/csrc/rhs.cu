@@ -33,7 +33,7 @@ __device__ __forceinline__ bool nonfinite(double x) {
 
 struct Deriv5 { double r, z, rr, zz, rz; };
 
-template <bool SHIFT, bool SCALAR>
+template <bool SHIFT, bool SCALAR, bool ADVECT>
 #ifndef OLLIN_RHS_THREADS
 #define OLLIN_RHS_THREADS 128
 #endif
@@ -74,7 +74,6 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     const double zero = 0.0, half = 0.5, one = 1.0, two = 2.0, four = 4.0, six = 6.0;
     const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, fourth = 0.25;
     const double smallpi = 3.141592653589793;
-    const double *ft = P.ft;
 
     // ---- state and aux at the point
     const double alpha = val(F_ALPHA), chi = val(F_CHI);
@@ -208,7 +207,6 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     if constexpr (SHIFT) {
         const double br = val(F_BETAR), bz = val(F_BETAZ), dbr = val(F_DTBETAR), dbz = val(F_DTBETAZ);
         const Deriv5 dbR = D5(F_BETAR), dbZ = D5(F_BETAZ);
-        const bool adv = P.shiftadvect != 0;
         const bool negr = br <= 0.0, negz = bz <= 0.0;
         // Advection term beta^r D_r f + beta^z D_z f with lopsided derivatives
         // (derivadvect.f90).  Inside i = 4-ghost..Nr-3 the two upwind
@@ -223,10 +221,15 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         };
         auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * dadv(p, 1, i, nr, g, negr, G.idr, false); };
         auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ld, j, nz, g, negz, G.idz, true); };
+        // shiftadvect is a template parameter: with it on, the centred
+        // derivatives need not stay live for this block
         auto ADV = [&](int f, double dr_, double dz_) {
-            if (!adv) return br * dr_ + bz * dz_;
-            const double* p = A.in[f] + o;
-            return ladv_r(p) + ladv_z(p);
+            if constexpr (!ADVECT) {
+                return br * dr_ + bz * dz_;
+            } else {
+                const double* p = A.in[f] + o;
+                return ladv_r(p) + ladv_z(p);
+            }
         };
         // DD_beta_rr = d/dr (beta_r / r): first derivative of beta_r/r
         double DD_beta_rr;
@@ -356,9 +359,8 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         if (P.driveradv) {
             const double br = val(F_BETAR), bz = val(F_BETAZ);
             const bool negr = br <= 0.0, negz = bz <= 0.0;
-            const bool adv = P.shiftadvect != 0;
-            auto DAr = [&](int f) { return adv ? dadv(A.in[f] + o, 1, i, nr, g, negr, G.idr, false) : Dr(f); };
-            auto DAz = [&](int f) { return adv ? dadv(A.in[f] + o, ld, j, nz, g, negz, G.idz, true) : Dz(f); };
+            auto DAr = [&](int f) { return ADVECT ? dadv(A.in[f] + o, 1, i, nr, g, negr, G.idr, false) : Dr(f); };
+            auto DAz = [&](int f) { return ADVECT ? dadv(A.in[f] + o, ld, j, nz, g, negz, G.idz, true) : Dz(f); };
             s_dbr = s_dbr + br * (DAr(F_DTBETAR) - DAr(F_DLR)) + bz * (DAz(F_DTBETAR) - DAz(F_DLR));
             s_dbz = s_dbz + br * (DAr(F_DTBETAZ) - DAr(F_DLZ)) + bz * (DAz(F_DTBETAZ) - DAz(F_DLZ));
         }
@@ -434,11 +436,13 @@ void launch_rhs(const StageArgs& a, cudaStream_t s) {
     dim3 blk(32, OLLIN_RHS_THREADS / 32);
     const int nj = a.G.nz - a.G.jlo + 1;
     dim3 grd((a.G.nr + blk.x - 1) / blk.x, (nj + blk.y - 1) / blk.y);
-    const bool sh = a.P.shift != 0, sc = a.P.scalar != 0;
-    if (!sh && !sc) rhs_kernel<false, false><<<grd, blk, 0, s>>>(a);
-    else if (sh && !sc) rhs_kernel<true, false><<<grd, blk, 0, s>>>(a);
-    else if (!sh && sc) rhs_kernel<false, true><<<grd, blk, 0, s>>>(a);
-    else rhs_kernel<true, true><<<grd, blk, 0, s>>>(a);
+    const bool sh = a.P.shift != 0, sc = a.P.scalar != 0, ad = a.P.shiftadvect != 0;
+    if (!sh && !sc) rhs_kernel<false, false, false><<<grd, blk, 0, s>>>(a);
+    else if (!sh && sc) rhs_kernel<false, true, false><<<grd, blk, 0, s>>>(a);
+    else if (!sc && ad) rhs_kernel<true, false, true><<<grd, blk, 0, s>>>(a);
+    else if (!sc) rhs_kernel<true, false, false><<<grd, blk, 0, s>>>(a);
+    else if (ad) rhs_kernel<true, true, true><<<grd, blk, 0, s>>>(a);
+    else rhs_kernel<true, true, false><<<grd, blk, 0, s>>>(a);
 }
 
 }  // namespace ollin
