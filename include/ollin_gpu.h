@@ -47,6 +47,9 @@ extern "C" {
 #define OLLIN_SLICING_HARMONIC  1   /* slicing = "harmonic"   */
 #define OLLIN_SLICING_SHOCKAVOID 2  /* slicing = "shockavoid" */
 #define OLLIN_SLICING_STATIC    3   /* slicing = "static"     */
+#define OLLIN_SLICING_MAXIMAL   4   /* slicing = "maximal": no lapse or trK source; the
+                                     * host calls ollin_gpu_maximal_slicing after each
+                                     * coarse step (evolve.f90:388-393) */
 
 #define OLLIN_SHIFT_NONE        0   /* shift = "none"         */
 #define OLLIN_SHIFT_ZERO        1   /* shift = "zero"         */
@@ -85,6 +88,8 @@ extern "C" {
 #define OLLIN_ILAPSE_ISOTROPIC  1   /* ilapse = "isotropic" */
 #define OLLIN_ILAPSE_PSIMINUS2  2   /* ilapse = "psiminus2" */
 #define OLLIN_ILAPSE_PSIMINUS4  3   /* ilapse = "psiminus4" */
+#define OLLIN_ILAPSE_MAXIMAL    4   /* ilapse = "maximal": alpha = 1 until the host's
+                                     * first ollin_gpu_maximal_slicing (evolve.f90:228) */
 
 /*
  * Parsed parameters, field for field the values of the reference's
@@ -196,7 +201,7 @@ int ollin_gpu_initial_data(ollin_handle* h);
 int ollin_gpu_initialize(ollin_handle* h);
 
 /* Recompute auxiliary quantities of one level after the host changed its
- * state (e.g. an elliptic lapse).  Replaces: call auxiliary
+ * state (uploaded arrays).  Replaces: call auxiliary
  * (src/base/auxiliary.f90:26-56) for the current grid. */
 int ollin_gpu_aux(ollin_handle* h, int level);
 
@@ -211,13 +216,32 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
  * Derived fields (OLLIN_F_HAM ...) are computed first (constraints.f90:55-149). */
 int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
 
+/* Maximal slicing on every level: solve lap(alpha) = (K_ij K^ij +
+ * 4 pi (rho + S)) alpha with the physical Laplacian of the conformal metric
+ * and alpha -> 1 far away, by the solver of ELL_solver (wave or sor), and
+ * replace the lapse.  Replaces: call maximalslicing
+ * (src/geometry/maximalslicing.f90:3-175), which the host calls at
+ * src/base/evolve.f90:228-230 (after ollin_gpu_initialize, when slicing or
+ * ilapse is "maximal" or maximalevery /= 0) and :388-393 (after
+ * ollin_gpu_coarse_step, when slicing = "maximal" or every maximalevery
+ * steps).  ``va_max`` (may be NULL): the largest |va_rp|, |va_zp| over all
+ * levels that the host's last analysis_geometry/cfl call left, which
+ * wave_elliptic.f90:211-263 folds into its time step; NULL stands for the
+ * zero arrays of a run that has not called either.  Like the reference, the
+ * call recomputes only the lapse and its first and second derivatives: the
+ * next stage of each level still sees the covariant second derivatives,
+ * Laplacian, falpha and advective derivatives of the lapse before the solve.
+ * Needs eqsym; OLLIN_EINVAL for ELL_solver = "mixed". */
+int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
+
 /* Iterations of the elliptic solve run by ollin_gpu_initial_data for
  * idata = BrillWave / scalarpulse (wave_elliptic.f90:190-262): steps[0] in
  * the coarse-grid phase, steps[1] in the all-level phase (0 with one level);
  * for SOR the iterations on level 0 and level 1; for "mixed" the FP64
  * refinements and the FP32 V-cycles on level 0.  ``gres`` (may be NULL)
- * receives the final residual.  No counterpart call in the reference, which
- * prints these numbers. */
+ * receives the final residual; after ollin_gpu_maximal_slicing, the numbers
+ * of that solve.  No counterpart call in the reference, which prints these
+ * numbers. */
 int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres);
 
 /* Total point-updates performed by this handle so far (interior points of

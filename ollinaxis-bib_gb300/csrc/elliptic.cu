@@ -23,6 +23,7 @@ namespace {
 
 constexpr int kWaveBX = 32, kWaveBY = 4, kWaveThreads = kWaveBX * kWaveBY;
 
+template <bool PHYS>
 __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_constant__ WaveArgs A) {
     __shared__ double red[kWaveThreads];
     if (A.skip && *A.skip) return;  // the same value for the whole grid
@@ -41,8 +42,25 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_c
         const int pcr = pclass(mi, nr, g), pcz = pclass(mj, nz, g);
         const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
         const double cr2 = G.idr * G.idr * (1.0 / 12.0), cz2 = G.idz * G.idz * (1.0 / 12.0);
-        // flat Laplacian in (r, z) with the axis term (wave_elliptic.f90:593-597)
-        double s = (d2(u, 1, pcr, cr2) + d2(u, ld, pcz, cz2)) + d1(u, 1, pcr, cr1) * G.ircol[mi];
+        double s;
+        if constexpr (!PHYS) {
+            // flat Laplacian in (r, z) with the axis term (wave_elliptic.f90:593-597)
+            s = (d2(u, 1, pcr, cr2) + d2(u, ld, pcz, cz2)) + d1(u, 1, pcr, cr1) * G.ircol[mi];
+        } else {
+            // physical Laplacian of the conformal metric (wave_elliptic.f90:
+            // 781-812); the hdet terms vanish (hdet = 1)
+            const WavePhys& q = A.ph;
+            const double ur = d1(u, 1, pcr, cr1), uz = d1(u, ld, pcz, cz1);
+            const double urr = d2(u, 1, pcr, cr2), uzz = d2(u, ld, pcz, cz2);
+            const double urz = d2rz(u, ld, mi, mj, nr, nz, g, G.idr * G.idz);
+            const double gA = q.gA[om], gB = q.gB[om], gC = q.gC[om];
+            const double r = G.rcol[mi], rgC = r * gC;
+            s = gA * urr + gB * uzz + ((2.0 * r) * gC) * urz;
+            s = s + ur * q.P1[om] + uz * q.P2[om];
+            s = s + (gA * ur) / r + gC * uz;
+            s = s + 2.0 * (q.Drphi[om] * (gA * ur + rgC * uz) + q.Dzphi[om] * (gB * uz + rgC * ur));
+            s = s / q.psi4[om];
+        }
         const double uc = ld_(u);
         double u5 = uc * uc;
         u5 = u5 * u5;
@@ -319,6 +337,193 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
     }
 }
 
+// ---- maximal slicing (maximalslicing.f90) -----------------------------------
+constexpr int kMaxBX = 32, kMaxBY = 4, kMaxThreads = kMaxBX * kMaxBY;
+
+// Coefficients of the physical Laplacian and the source S1 at every point
+// (MaxCoeffArgs); per-block maxima of the light speeds sqrt|g^ii/psi4| for
+// the wave solver's time step (wave_elliptic.f90:193-263).  A derivative at
+// a ghost point is the parity image of the derivative at the mirror point,
+// as the symmetry fill of derivatives.f90:91-99 and :212-216 leaves it: the
+// r derivative changes sign across the axis for an even function and takes
+// the function's z parity across the equator, and the other way round for
+// the z derivative.
+__global__ void __launch_bounds__(kMaxThreads) max_coeff_kernel(const __grid_constant__ MaxCoeffArgs A) {
+    __shared__ double red[2][kMaxThreads];
+    const LevelGeom& G = A.G;
+    const int g = G.g, nr = G.nr, nz = G.nz;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    double vr = 0.0, vz = 0.0;
+    if (i <= nr && j <= nz) {
+        const long ld = G.ld;
+        const bool gr = i < 1, gz = G.eqsym && j < 1;
+        const int mi = gr ? 1 - i : i, mj = gz ? 1 - j : j;
+        const size_t o = (size_t)i + (size_t)j * ld, om = (size_t)mi + (size_t)mj * ld;
+        const int pcr = pclass(mi, nr, g), pcz = pclass(mj, nz, g);
+        const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
+        // parities: g_A, g_B, phi, chi even in r and z; g_C even in r, odd in z
+        const double er = gr ? -1.0 : 1.0;  // r derivative of an r-even function
+        const double ez = gz ? -1.0 : 1.0;  // z derivative of a z-even function
+        const double DrgA = d1(A.gA + om, 1, pcr, cr1) * er;
+        const double DzgB = d1(A.gB + om, ld, pcz, cz1) * ez;
+        const double DrgC = d1(A.gC + om, 1, pcr, cr1) * er * (gz ? -1.0 : 1.0);
+        const double DzgC = d1(A.gC + om, ld, pcz, cz1);
+        const double r = G.rcol[i], gC = A.gC[o];
+        A.P1[o] = DrgA + r * DzgC;
+        A.P2[o] = (DzgB + r * DrgC) + gC;
+        double Drphi, Dzphi, psi4;
+        if (A.t0) {
+            Drphi = d1(A.phi + om, 1, pcr, cr1) * er;
+            Dzphi = d1(A.phi + om, ld, pcz, cz1) * ez;
+            const double p = exp(A.phi[o]);
+            psi4 = (p * p) * (p * p);
+        } else {
+            const double chm = A.chi[om];
+            Drphi = (-(d1(A.chi + om, 1, pcr, cr1) * er) / chm) * 0.5;
+            Dzphi = (-(d1(A.chi + om, ld, pcz, cz1) * ez) / chm) * 0.5;
+            const double p = exp(-log(A.chi[o]) * 0.5);
+            psi4 = (p * p) * (p * p);
+        }
+        A.Drphi[o] = Drphi;
+        A.Dzphi[o] = Dzphi;
+        A.psi4[o] = psi4;
+        const double tk = A.trK[om];
+        double s1 = -(A.KT2[om] + (1.0 / 3.0) * (tk * tk));
+        if (A.rhos) s1 = s1 - 4.0 * 3.141592653589793 * A.rhos[om];
+        A.S1[o] = s1;
+        vr = sqrt(fabs(A.gA[o] / psi4));
+        vz = sqrt(fabs(A.gB[o] / psi4));
+    }
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    red[0][t] = vr;
+    red[1][t] = vz;
+    __syncthreads();
+    for (int w = kMaxThreads / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            red[0][t] = fmax(red[0][t], red[0][t + w]);
+            red[1][t] = fmax(red[1][t], red[1][t + w]);
+        }
+        __syncthreads();
+    }
+    const int b = blockIdx.y * gridDim.x + blockIdx.x;
+    if (t == 0) { A.vmax[2 * b] = red[0][0]; A.vmax[2 * b + 1] = red[1][0]; }
+}
+
+// SOR stencil of the physical Laplacian at every point, in the expression
+// order of sor_elliptic.f90:168-262 / :371-448 (explicitly rounded)
+__global__ void __launch_bounds__(128) sor_coeff_kernel(const __grid_constant__ SorCoeffArgs A) {
+    const LevelGeom& G = A.G;
+    const int g = G.g;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    const WavePhys& q = A.ph;
+    const double dr = G.dr, dz = G.dz, r = G.rcol[i];
+    const double gA = q.gA[o], gB = q.gB[o], gC = q.gC[o], ps = q.psi4[o];
+    const double Drp = q.Drphi[o], Dzp = q.Dzphi[o];
+    auto dv = [](double x, double y) { return __ddiv_rn(x, y); };
+    double a = dv(mrn(gA, arn(dv(1.0, dr), dv(0.5, r))), dr);
+    double b = dv(mrn(gA, srn(dv(1.0, dr), dv(0.5, r))), dr);
+    double c = dv(gB, mrn(dz, dz));
+    double d = dv(gB, mrn(dz, dz));
+    double e = mrn(-2.0, arn(dv(gA, mrn(dr, dr)), dv(gB, mrn(dz, dz))));
+    const double hr = mrn(mrn(0.5, r), gC);
+    const double diag = A.fine ? dv(dv(hr, dr), dz) : dv(hr, mrn(dr, dz));
+    double cg = diag, ch = diag, ci = -diag, cj = -diag;
+    const double t1 = dv(mrn(0.5, q.P1[o]), dr), t2 = dv(mrn(0.5, q.P2[o]), dz);
+    a = arn(a, t1); b = srn(b, t1);
+    c = arn(c, t2); d = srn(d, t2);
+    const double t3 = dv(mrn(0.5, gC), dz);
+    c = arn(c, t3); d = srn(d, t3);
+    const double rgC = mrn(r, gC);
+    const double t4 = dv(arn(mrn(gA, Drp), mrn(rgC, Dzp)), dr);
+    const double t5 = dv(arn(mrn(gB, Dzp), mrn(rgC, Drp)), dz);
+    a = arn(a, t4); b = srn(b, t4);
+    c = arn(c, t5); d = srn(d, t5);
+    A.a[o] = dv(a, ps); A.b[o] = dv(b, ps); A.c[o] = dv(c, ps); A.d[o] = dv(d, ps);
+    A.e[o] = arn(dv(e, ps), A.S1[o]);
+    cg = dv(cg, ps); ch = dv(ch, ps); ci = dv(ci, ps); cj = dv(cj, ps);
+    A.cg[o] = cg; A.ch[o] = ch; A.ci[o] = ci; A.cj[o] = cj;
+    if (cg != 0.0 || ch != 0.0 || ci != 0.0 || cj != 0.0) atomicOr(A.diag_nonzero, 1ull);
+}
+
+// residual of the nine-point stencil at one point, in the order of
+// sor_elliptic.f90:660-666, and the update of u
+__device__ __forceinline__ double sor_phys_update(const SorPhysPassArgs& A, size_t o, long ld, bool diag) {
+    double* u = A.u + o;
+    const double ev = A.e[o];
+    double r = mrn(A.a[o], u[1]);
+    r = arn(r, mrn(A.b[o], u[-1]));
+    r = arn(r, mrn(A.c[o], u[ld]));
+    r = arn(r, mrn(A.d[o], u[-ld]));
+    if (diag) {
+        r = arn(r, mrn(A.cg[o], u[1 + ld]));
+        r = arn(r, mrn(A.ch[o], u[-1 - ld]));
+        r = arn(r, mrn(A.ci[o], u[1 - ld]));
+        r = arn(r, mrn(A.cj[o], u[-1 + ld]));
+    }
+    r = arn(r, mrn(ev, u[0]));
+    r = srn(r, A.f[o]);
+    u[0] = srn(u[0], __ddiv_rn(mrn(A.omega, r), ev));
+    return mrn(r, r);
+}
+
+// A pass when every diagonal coefficient is zero: the points of one colour
+// are then independent, as for the flat Laplacian
+__global__ void __launch_bounds__(kSorThreads) sor_phys_pass_kernel(const __grid_constant__ SorPhysPassArgs A) {
+    __shared__ double red[kSorThreads];
+    if (A.skip && *A.skip) return;
+    const LevelGeom& G = A.G;
+    const int g = G.g;
+    const int i = 2 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int jh = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    int j = 2 - g;
+    if (((i + j) & 1) != A.parity) ++j;
+    j += 2 * jh;
+    double res = 0.0;
+    if (i <= G.nr - 1 && j <= G.nz - 1) res = sor_phys_update(A, (size_t)i + (size_t)j * G.ld, G.ld, false);
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    red[t] = res;
+    __syncthreads();
+    for (int w = kSorThreads / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    if (t == 0) A.partial[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
+}
+
+// A pass with nonzero diagonal coefficients: they couple a point to the
+// points of its own colour in the neighbouring columns, which the loop of
+// sor_elliptic.f90:648-676 (i outer) has already updated (i-1) or not yet
+// (i+1).  One block sweeps the columns in that order; within a column the
+// points are independent.
+constexpr int kSeqThreads = 1024;
+__global__ void __launch_bounds__(kSeqThreads) sor_phys_pass_seq_kernel(const __grid_constant__ SorPhysPassArgs A) {
+    __shared__ double red[kSeqThreads];
+    if (A.skip && *A.skip) return;
+    const LevelGeom& G = A.G;
+    const int g = G.g;
+    const long ld = G.ld;
+    double res = 0.0;
+    for (int i = 2 - g; i <= G.nr - 1; ++i) {
+        int j0 = 2 - g;
+        if (((i + j0) & 1) != A.parity) ++j0;
+        for (int j = j0 + 2 * (int)threadIdx.x; j <= G.nz - 1; j += 2 * kSeqThreads)
+            res = res + sor_phys_update(A, (size_t)i + (size_t)j * ld, ld, true);
+        __syncthreads();
+    }
+    const int t = threadIdx.x;
+    red[t] = res;
+    __syncthreads();
+    for (int w = kSeqThreads / 2; w > 0; w >>= 1) {
+        if (t < w) red[t] = red[t] + red[t + w];
+        __syncthreads();
+    }
+    if (t == 0) A.partial[0] = red[0];
+}
+
 // out = c + x at every point
 __global__ void add_kernel(LevelGeom G, double* out, double c, const double* x) {
     const int g = G.g;
@@ -487,7 +692,36 @@ int wave_stage_blocks(const LevelGeom& G) {
 void launch_wave_stage(const WaveArgs& a, cudaStream_t s) {
     dim3 blk(kWaveBX, kWaveBY);
     dim3 grd((a.G.nr + a.G.g + kWaveBX - 1) / kWaveBX, (a.G.nz + a.G.g + kWaveBY - 1) / kWaveBY);
-    wave_stage_kernel<<<grd, blk, 0, s>>>(a);
+    if (a.physical) wave_stage_kernel<true><<<grd, blk, 0, s>>>(a);
+    else wave_stage_kernel<false><<<grd, blk, 0, s>>>(a);
+}
+
+int max_coeff_blocks(const LevelGeom& G) {
+    const int nx = (G.nr + G.g + kMaxBX - 1) / kMaxBX, ny = (G.nz + G.g + kMaxBY - 1) / kMaxBY;
+    return nx * ny;
+}
+
+void launch_max_coeffs(const MaxCoeffArgs& a, cudaStream_t s) {
+    dim3 blk(kMaxBX, kMaxBY);
+    dim3 grd((a.G.nr + a.G.g + kMaxBX - 1) / kMaxBX, (a.G.nz + a.G.g + kMaxBY - 1) / kMaxBY);
+    max_coeff_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_sor_coeffs(const SorCoeffArgs& a, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((a.G.nr + a.G.g + blk.x - 1) / blk.x, (a.G.nz + a.G.g + blk.y - 1) / blk.y);
+    sor_coeff_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_sor_phys_pass(const SorPhysPassArgs& a, cudaStream_t s) {
+    const int ni = a.G.nr + a.G.g - 2, nj = (a.G.nz + a.G.g - 2 + 1) / 2;
+    dim3 blk(kSorBX, kSorBY);
+    dim3 grd((ni + kSorBX - 1) / kSorBX, (nj + kSorBY - 1) / kSorBY);
+    sor_phys_pass_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_sor_phys_pass_seq(const SorPhysPassArgs& a, cudaStream_t s) {
+    sor_phys_pass_seq_kernel<<<1, kSeqThreads, 0, s>>>(a);
 }
 
 void launch_wave_residual(const double* partial, int nparts, int nr, int nz, EllCtl* ctl, cudaStream_t s) {

@@ -25,7 +25,7 @@ import sympy as sp
 INPUTS = [
     "r", "ir", "alpha", "chi", "Ac", "Bc", "Hc", "Cc", "trK", "kA", "kB", "kC", "kH",
     "Dlr", "Dlz", "gA", "gB", "gH", "gC", "lam", "Alam", "glam", "DDr", "DDz", "ipsi4", "eta",
-    "da_r", "da_z", "da_rr", "da_zz", "da_rz",
+    "da_r", "da_z", "da_rr", "da_zz", "da_rz", "dan_r", "dan_z",
     "dA_r", "dA_z", "dA_rr", "dA_zz", "dA_rz",
     "dB_r", "dB_z", "dB_rr", "dB_zz", "dB_rz",
     "dH_r", "dH_z", "dH_rr", "dH_zz", "dH_rz",
@@ -214,9 +214,13 @@ def algebra(x, let):
     out["s_KTA"] = alpha * (trK * kA - two * KT2_A) + (-D2A + alpha * RA) * ipsi4 - third * Ac * trterm
     out["s_KTB"] = alpha * (trK * kB - two * KT2_B) + (-D2B + alpha * RB) * ipsi4 - third * Bc * trterm
     out["s_KTC"] = alpha * (trK * kC - two * KT2_C) + (-D2C + alpha * RC) * ipsi4 - third * Cc * trterm
-    out["s_Dlr"] = -two * (KT_up_rr * da_r + KT_up_rz * da_z) - two * alpha * DIVA_KT_r \
+    # the lapse gradient of the Delta sources is the one maximalslicing.f90
+    # recomputes (dan_*); D2cov_alpha and Lapla_alpha above keep the values of
+    # the last ``auxiliary`` call (da_*); the two differ only in the first
+    # stage after a maximal-slicing solve
+    out["s_Dlr"] = -two * (KT_up_rr * x.dan_r + KT_up_rz * x.dan_z) - two * alpha * DIVA_KT_r \
         + x.eta * alpha * (DIV_KT_r + six * (KT_up_rr * Dr_phi + KT_up_rz * Dz_phi) - two * third * (gA * x.Dr_trK + r * gC * x.Dz_trK))
-    out["s_Dlz"] = -two * (KT_up_rz * da_r + KT_up_zz * da_z) - two * alpha * DIVA_KT_z \
+    out["s_Dlz"] = -two * (KT_up_rz * x.dan_r + KT_up_zz * x.dan_z) - two * alpha * DIVA_KT_z \
         + x.eta * alpha * (DIV_KT_z + six * (KT_up_rz * Dr_phi + KT_up_zz * Dz_phi) - two * third * (r * gC * x.Dr_trK + gB * x.Dz_trK))
     # constraints (constraints.f90:55-149), vacuum part
     out["ham"] = RSCAL - KT2 + two * third * trK ** 2

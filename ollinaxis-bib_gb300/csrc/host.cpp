@@ -60,6 +60,10 @@ struct DLevel {
     int nptab = 0;
     XferPt* rtab = nullptr;
     int nrtab = 0;
+    // the lapse of the last ``auxiliary`` call, kept while a maximal-slicing
+    // solve has replaced the lapse and no ``auxiliary`` has run since
+    double* alpha_aux = nullptr;
+    bool alpha_stale = false;
 };
 
 }  // namespace
@@ -118,7 +122,8 @@ int check_params(const ollin_params& P) {
     if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
     if (P.shift != OLLIN_SHIFT_NONE && P.shift != OLLIN_SHIFT_GAMMADRIVER2)
         return fail(OLLIN_EINVAL, "shift must be none or Gammadriver2");
-    if (P.slicing < 0 || P.slicing > 3) return fail(OLLIN_EINVAL, "unknown slicing");
+    if (P.slicing < 0 || P.slicing > OLLIN_SLICING_MAXIMAL) return fail(OLLIN_EINVAL, "unknown slicing");
+    if (P.ilapse < OLLIN_ILAPSE_ONE || P.ilapse > OLLIN_ILAPSE_MAXIMAL) return fail(OLLIN_EINVAL, "unknown ilapse");
     if (P.integrator != OLLIN_INTEGRATOR_RK4 && P.integrator != OLLIN_INTEGRATOR_ICN) return fail(OLLIN_EINVAL, "unknown integrator");
     if (P.integrator == OLLIN_INTEGRATOR_ICN && P.icniter < 1) return fail(OLLIN_EINVAL, "icniter must be positive");
     if (P.mattertype != OLLIN_MATTER_VACUUM && P.mattertype != OLLIN_MATTER_SCALAR) return fail(OLLIN_EINVAL, "unknown mattertype");
@@ -268,6 +273,7 @@ int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0) {
         if (rc) return rc;
     }
     L.last_aux_t0 = t0;
+    L.alpha_stale = false;
     return OLLIN_OK;
 }
 
@@ -290,7 +296,15 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
     a.level0 = L.level == 0;
     a.rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
     a.nanflag = h->d_flag;
+    a.alpha_aux = L.alpha_stale ? base_ptr(L, L.alpha_aux) : nullptr;
     return a;
+}
+
+// the right-hand side of a stage: the ordinary kernels, or the ones that read
+// the lapse quantities of the last ``auxiliary`` call from alpha_aux
+void launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
+    if (a.alpha_aux) launch_rhs_stale(a, s);
+    else launch_rhs(a, s);
 }
 
 // Geometry part of the transfer arguments of level pair (level-1, level).
@@ -483,7 +497,7 @@ int onestep(ollin_handle* h, int level) {
             }
             CUDA_OR_FAIL(cudaEventRecord(h->ev[h->ev_used], h->stream));
         }
-        launch_rhs(a, h->stream);
+        launch_stage_rhs(a, h->stream);
         int rc = after_launch(h);
         if (rc) return rc;
         if (h->ktime) {
@@ -575,7 +589,7 @@ int analysis(ollin_handle* h, int level) {
     DLevel& L = h->L[level];
     StageArgs a = stage_args(h, L, L.cur, L.cur, L.last_aux_t0);
     a.analysis = 1;
-    launch_rhs(a, h->stream);
+    launch_stage_rhs(a, h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
     launch_ham_edges(L.G, base_ptr(L, L.aux[X_HAM]), h->stream);
@@ -604,6 +618,9 @@ struct WLevel {
     double* S0 = nullptr; double* S1 = nullptr; double* S5 = nullptr;
     int cur = 0, p = 1, pp = 2;
     double dt = 0;
+    // physical Laplacian (maximal slicing): P1, P2, Drphi, Dzphi, psi4
+    double* cpool = nullptr;
+    WavePhys ph{};
 };
 
 struct WaveSolve {
@@ -623,8 +640,9 @@ struct WaveSolve {
         std::vector<double> t, t1, t2;
         std::vector<long> s;
     };
+    bool physical = false;  // type = 'physical' (maximal slicing)
     ~WaveSolve() {
-        for (WLevel& w : W) cudaFree(w.pool);
+        for (WLevel& w : W) { cudaFree(w.pool); cudaFree(w.cpool); }
         cudaFree(ctl);
         cudaFree(partial);
         cudaFree(partial2);
@@ -736,6 +754,7 @@ int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
 }
 
 // wave_elliptic.f90:347-770 (recursive subroutine wavestep), type = 'flat'
+// or 'physical'
 int wavestep(ollin_handle* h, WaveSolve& S, int level) {
     const ollin_params& P = h->P;
     DLevel& L = h->L[level];
@@ -778,6 +797,8 @@ int wavestep(ollin_handle* h, WaveSolve& S, int level) {
         a.niter = niter;
         a.res_partial = (level == 0 && iter == niter) ? S.partial : nullptr;
         a.skip = &S.ctl->done;
+        a.physical = S.physical ? 1 : 0;
+        a.ph = w.ph;
         launch_wave_stage(a, h->stream);
         int rc = after_launch(h);
         if (rc) return rc;
@@ -906,7 +927,10 @@ int wave_elliptic(ollin_handle* h, WaveSolve& S) {
 // below, then restriction back down.  The iteration is in place; batches of
 // iterations are queued and turned into no-ops by the device stop flag.
 // ---------------------------------------------------------------------------
+int sor_level_physical(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* iters);
+
 int sor_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* iters) {
+    if (S.physical) return sor_level_physical(h, S, level, robin, rjac, iters);
     const ollin_params& P = h->P;
     DLevel& L = h->L[level];
     WLevel& w = S.W[level];
@@ -971,6 +995,95 @@ int sor_level(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac,
             f.partial1 = S.partial;
             f.partial2 = S.partial2;
             f.nparts = sor_pass_blocks(L.G);
+            f.robin = robin ? 1 : 0;
+            f.uinf = 1.0;
+            f.ctl = S.ctl;
+            if (launch_sor_finish(f, h->stream))
+                return fail(OLLIN_ECUDA, "SOR boundary kernel: shared memory for the Robin edges not available");
+            rc = after_launch(h);
+            if (rc) return rc;
+        }
+        EllCtl hc{};
+        CUDA_OR_FAIL(cudaMemcpyAsync(&hc, S.ctl, sizeof(hc), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        if (hc.done) {
+            *iters = hc.step;
+            S.gres = hc.gres;
+            return OLLIN_OK;
+        }
+        batch = std::min(1024, std::max(64, n / 4));
+    }
+}
+
+// sor on one level with the nine-point stencil of the physical Laplacian
+// (maximal slicing, S5 = 0 so the diagonal stays fixed).  While every
+// diagonal coefficient is zero the colours decouple and the pass runs over
+// all points at once; otherwise one block sweeps the columns in the
+// reference's order.
+int sor_level_physical(ollin_handle* h, WaveSolve& S, int level, bool robin, double rjac, int* iters) {
+    const ollin_params& P = h->P;
+    DLevel& L = h->L[level];
+    WLevel& w = S.W[level];
+    double* pool = nullptr;
+    unsigned long long* dflag = nullptr;
+    if (cudaMalloc(&pool, 9 * L.n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dflag, sizeof(unsigned long long)) != cudaSuccess) {
+        cudaFree(pool);
+        return fail(OLLIN_ENOMEM, "device allocation failed for the SOR coefficients");
+    }
+    struct FreeOnExit { void* a; void* b; ~FreeOnExit() { cudaFree(a); cudaFree(b); } } fr{pool, dflag};
+    CUDA_OR_FAIL(cudaMemsetAsync(pool, 0, 9 * L.n * sizeof(double), h->stream));
+    CUDA_OR_FAIL(cudaMemsetAsync(dflag, 0, sizeof(unsigned long long), h->stream));
+    double* arr[9];
+    for (int k = 0; k < 9; ++k) arr[k] = pool + (size_t)k * L.n;
+    SorCoeffArgs c{};
+    c.G = L.G;
+    c.ph = w.ph;
+    c.S1 = base_ptr(L, w.S1);
+    c.fine = level > 0 ? 1 : 0;
+    c.a = base_ptr(L, arr[0]); c.b = base_ptr(L, arr[1]); c.c = base_ptr(L, arr[2]); c.d = base_ptr(L, arr[3]);
+    c.e = base_ptr(L, arr[4]);
+    c.cg = base_ptr(L, arr[5]); c.ch = base_ptr(L, arr[6]); c.ci = base_ptr(L, arr[7]); c.cj = base_ptr(L, arr[8]);
+    c.diag_nonzero = dflag;
+    launch_sor_coeffs(c, h->stream);
+    int rc = after_launch(h);
+    if (rc) return rc;
+    unsigned long long hdiag = 0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(&hdiag, dflag, sizeof(hdiag), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    const bool seq = hdiag != 0;
+    EllCtl ctl{};
+    ctl.maxiter = P.ell_maxiter; ctl.eps = P.ell_epsilon; ctl.gres = 1.0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(S.ctl, &ctl, sizeof(ctl), cudaMemcpyHostToDevice, h->stream));
+    double omega = 1.0;
+    int n = 0, batch = 64;
+    for (;;) {
+        for (int k = 0; k < batch; ++k) {
+            ++n;
+            for (int ipass = 1; ipass <= 2; ++ipass) {
+                SorPhysPassArgs a{};
+                a.G = L.G;
+                a.u = base_ptr(L, w.u[w.cur]);
+                a.a = c.a; a.b = c.b; a.c = c.c; a.d = c.d; a.e = c.e;
+                a.cg = c.cg; a.ch = c.ch; a.ci = c.ci; a.cj = c.cj;
+                a.f = base_ptr(L, w.S0);
+                a.omega = omega;
+                a.parity = ipass == 1 ? 0 : 1;
+                a.partial = ipass == 1 ? S.partial : S.partial2;
+                a.skip = &S.ctl->done;
+                if (seq) launch_sor_phys_pass_seq(a, h->stream);
+                else launch_sor_phys_pass(a, h->stream);
+                rc = after_launch(h);
+                if (rc) return rc;
+                if (n == 1 && ipass == 1) omega = 1.0 / (1.0 - 0.5 * (rjac * rjac));
+                else omega = 1.0 / (1.0 - 0.25 * (rjac * rjac) * omega);
+            }
+            SorFinishArgs f{};
+            f.G = L.G;
+            f.u = base_ptr(L, w.u[w.cur]);
+            f.partial1 = S.partial;
+            f.partial2 = S.partial2;
+            f.nparts = seq ? 1 : sor_pass_blocks(L.G);
             f.robin = robin ? 1 : 0;
             f.uinf = 1.0;
             f.ctl = S.ctl;
@@ -1440,6 +1553,98 @@ int initial_data(ollin_handle* h) {
     return OLLIN_OK;
 }
 
+// maximalslicing.f90:3-175 on every level: lap(alpha) = (K_ij K^ij +
+// 4 pi (rho + S)) alpha with the physical Laplacian of the conformal metric,
+// solved by the elliptic solver of ELL_solver ('physical', init 'one'), then
+// alpha = ell_u.  The reference recomputes the lapse's first and second
+// derivatives and nothing else, so until a level's next ``auxiliary`` the
+// right-hand side reads the other lapse quantities from the lapse before the
+// solve (DLevel::alpha_aux).  va_max: the largest slicing speeds (r, z) that
+// the caller's last analysis left in va_rp/va_zp, or null for none.
+int maximal_slicing(ollin_handle* h, const double* va_max) {
+    const ollin_params& P = h->P;
+    if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
+    if (!P.eqsym) return fail(OLLIN_EINVAL, "maximal slicing on the device needs equatorial symmetry (eqsym)");
+    if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
+        return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave or sor");
+    // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)
+    for (int l = 0; l < h->nlev; ++l) {
+        int rc = analysis(h, l);
+        if (rc) return rc;
+    }
+    WaveSolve S;
+    int rc = wave_alloc(h, S);
+    if (rc) return rc;
+    S.physical = true;
+    double vrmax = 0.0, vzmax = 0.0;
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        const int nb = max_coeff_blocks(L.G);
+        if (cudaMalloc(&w.cpool, (5 * L.n + 2 * (size_t)nb) * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the maximal-slicing coefficients");
+        CUDA_OR_FAIL(cudaMemsetAsync(w.cpool, 0, (5 * L.n + 2 * (size_t)nb) * sizeof(double), h->stream));
+        double* q[5];
+        for (int k = 0; k < 5; ++k) q[k] = w.cpool + (size_t)k * L.n;
+        double* vmax = w.cpool + 5 * L.n;
+        MaxCoeffArgs a{};
+        a.G = L.G;
+        a.gA = base_ptr(L, L.aux[X_GA]); a.gB = base_ptr(L, L.aux[X_GB]); a.gC = base_ptr(L, L.aux[X_GC]);
+        a.chi = base_ptr(L, L.slot[L.cur][F_CHI]);
+        a.phi = base_ptr(L, L.slot[L.cur][F_PHI]);
+        a.trK = base_ptr(L, L.slot[L.cur][F_TRK]);
+        a.KT2 = base_ptr(L, L.aux[X_KT2]);
+        a.rhos = h->scalar ? base_ptr(L, L.aux[X_RHOS]) : nullptr;
+        a.t0 = L.last_aux_t0 ? 1 : 0;
+        a.S1 = base_ptr(L, w.S1);
+        a.P1 = base_ptr(L, q[0]); a.P2 = base_ptr(L, q[1]);
+        a.Drphi = base_ptr(L, q[2]); a.Dzphi = base_ptr(L, q[3]); a.psi4 = base_ptr(L, q[4]);
+        a.vmax = vmax;
+        launch_max_coeffs(a, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        w.ph.gA = a.gA; w.ph.gB = a.gB; w.ph.gC = a.gC;
+        w.ph.P1 = a.P1; w.ph.P2 = a.P2; w.ph.Drphi = a.Drphi; w.ph.Dzphi = a.Dzphi; w.ph.psi4 = a.psi4;
+        std::vector<double> hv(2 * (size_t)nb);
+        CUDA_OR_FAIL(cudaMemcpyAsync(hv.data(), vmax, hv.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        // wave_elliptic.f90:211-258: maxima over the level, then over levels
+        double vr = 0.0, vz = 0.0;
+        for (int b = 0; b < nb; ++b) { vr = std::max(vr, hv[2 * b]); vz = std::max(vz, hv[2 * b + 1]); }
+        if (va_max) { vr = std::max(vr, std::fabs(va_max[0])); vz = std::max(vz, std::fabs(va_max[1])); }
+        vrmax = std::max(vrmax, vr);
+        vzmax = std::max(vzmax, vz);
+    }
+    if (P.ell_solver == OLLIN_ELL_WAVE) {
+        // wave_elliptic.f90:263-271
+        const double dt0 = P.we_dtfac * std::min(std::min(P.dr0, P.dz0), std::min(P.dr0 / vrmax, P.dz0 / vzmax));
+        for (int l = 0; l < h->nlev; ++l) S.W[l].dt = dt0 / (double)(1L << l);
+        rc = wave_elliptic(h, S);
+    } else {
+        rc = sor_elliptic(h, S);
+    }
+    if (rc) return rc;
+    // alpha = ell_u (maximalslicing.f90:148-154)
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        WLevel& w = S.W[l];
+        if (!L.alpha_aux && cudaMalloc(&L.alpha_aux, L.n * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the lapse of the last auxiliary call");
+        // a second solve before any ``auxiliary`` keeps the older lapse
+        if (!L.alpha_stale)
+            CUDA_OR_FAIL(cudaMemcpyAsync(L.alpha_aux, L.slot[L.cur][F_ALPHA], L.n * sizeof(double),
+                                         cudaMemcpyDeviceToDevice, h->stream));
+        CUDA_OR_FAIL(cudaMemcpyAsync(L.slot[L.cur][F_ALPHA], w.u[w.cur], L.n * sizeof(double), cudaMemcpyDeviceToDevice,
+                                     h->stream));
+        L.alpha_stale = true;
+    }
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    h->ell_steps[0] = S.steps[0];
+    h->ell_steps[1] = S.steps[1];
+    h->ell_gres = S.gres;
+    return OLLIN_OK;
+}
+
 }  // namespace
 
 // =============================================================================
@@ -1531,6 +1736,7 @@ void ollin_gpu_destroy(ollin_handle* h) {
         if (L.pool) cudaFree(L.pool);
         if (L.ptab) cudaFree(L.ptab);
         if (L.rtab) cudaFree(L.rtab);
+        if (L.alpha_aux) cudaFree(L.alpha_aux);
     }
     if (h->d_flag) cudaFree(h->d_flag);
     if (h->d_norm) cudaFree(h->d_norm);
@@ -1719,6 +1925,11 @@ int ollin_gpu_kernel_stats(ollin_handle* h, double* rhs_ms, long long* launches,
 }
 
 void* ollin_gpu_stream(const ollin_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    return maximal_slicing(h, va_max);
+}
 
 int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres) {
     if (!h || !steps) return fail(OLLIN_EINVAL, "null argument");

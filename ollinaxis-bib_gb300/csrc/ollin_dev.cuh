@@ -36,6 +36,7 @@ enum AuxField : int {
     X_GDR, X_GDZ,                  // Dr_g_A + r Dz_g_C, Dz_g_B + r Dr_g_C (scalar-field source)
     // derived output arrays (analysis)
     X_HAM, X_MOMR, X_MOMZ, X_RSCAL, X_KT2, X_LAPLA,
+    X_RHOS,                        // rho + trS (scalar field; source of maximal slicing)
     NAUX
 };
 

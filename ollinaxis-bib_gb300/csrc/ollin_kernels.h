@@ -40,6 +40,12 @@ struct StageArgs {
     double dtw, weight;
     int analysis;                // 1: write ham/mom/RSCAL/KT2/Lapla_alpha instead of updating
     unsigned int* nanflag;       // set to 1 if a non-finite source is produced
+    // The lapse of the level's last ``auxiliary`` call when a maximal-slicing
+    // solve has replaced the lapse since (launch_rhs_stale only): the
+    // covariant second derivatives, Laplacian, falpha and advective
+    // derivatives of the lapse come from it, the lapse itself and the
+    // gradient that maximalslicing.f90:156-170 recomputes from the new one.
+    const double* alpha_aux;
 };
 
 // Pointwise auxiliary quantities (auxiliary_geometry.f90 pointwise parts).
@@ -137,6 +143,32 @@ struct EllCtl {
     double gres;   // residual of the last iteration
 };
 
+// Coefficients of the physical Laplacian of the conformal metric that both
+// elliptic solvers use for maximal slicing (wave_elliptic.f90:781-812,
+// sor_elliptic.f90:168-262), at every point of a level; derivatives at the
+// ghost points follow the parity fill of derivatives.f90.  hdet = 1 and its
+// derivatives vanish after ``initial`` with factorhdet, so the determinant
+// terms drop out exactly.
+struct MaxCoeffArgs {
+    LevelGeom G;
+    const double* gA; const double* gB; const double* gC;  // inverse conformal metric
+    const double* chi; const double* phi;                  // conformal factor
+    const double* trK; const double* KT2; const double* rhos;  // rhos may be null (vacuum)
+    int t0;                                                // phi-based conformal factor
+    double* S1;                                            // -(K_ij K^ij + 4 pi (rho + S))
+    double* P1;                                            // Dr_g_A + r Dz_g_C
+    double* P2;                                            // Dz_g_B + r Dr_g_C + g_C
+    double* Drphi; double* Dzphi; double* psi4;
+    double* vmax;                                          // [2*block]: per-block max sqrt|g^rr/psi4|, sqrt|g^zz/psi4|
+};
+
+// The physical-Laplacian coefficients of one wave stage.
+struct WavePhys {
+    const double* gA; const double* gB; const double* gC;
+    const double* P1; const double* P2;
+    const double* Drphi; const double* Dzphi; const double* psi4;
+};
+
 // One WaveElliptic stage on one level (wave_elliptic.f90:505-700):
 // sources, dissipation, parity, radiative boundary, accumulate and update of
 // (u, v) at every point including ghosts.
@@ -153,6 +185,8 @@ struct WaveArgs {
     int rk4, iter, niter;
     double* res_partial;   // level 0, last stage: per-block sums of sell_v^2
     const int* skip;
+    int physical;          // type = 'physical' (coefficients in ph)
+    WavePhys ph;
 };
 
 // Scalar-pulse coefficients (idata_scalarpulse.f90:108-170): xi = grad phi,
@@ -178,6 +212,32 @@ struct SorPassArgs {
     double omega;
     int parity;
     double* partial;                     // per-block sums of resid^2
+    const int* skip;
+};
+
+// Per-point coefficients of the SOR stencil for the physical Laplacian
+// (sor_elliptic.f90:168-262 on the coarse grid, :371-448 on finer grids,
+// which divide by dr and dz in turn): a..d axial, g..j diagonal, e the
+// diagonal including S1.
+struct SorCoeffArgs {
+    LevelGeom G;
+    WavePhys ph;
+    const double* S1;
+    int fine;
+    double* a; double* b; double* c; double* d; double* e;
+    double* cg; double* ch; double* ci; double* cj;
+    unsigned long long* diag_nonzero;  // set when any diagonal coefficient is not zero
+};
+
+// A red-black pass with the nine-point stencil of the physical Laplacian.
+struct SorPhysPassArgs {
+    LevelGeom G;
+    double* u;
+    const double* a; const double* b; const double* c; const double* d; const double* e; const double* f;
+    const double* cg; const double* ch; const double* ci; const double* cj;
+    double omega;
+    int parity;
+    double* partial;
     const int* skip;
 };
 
@@ -246,6 +306,13 @@ void launch_pulse_xi(const PulseCoeffArgs& a, cudaStream_t s);
 void launch_pulse_coeffs(const PulseCoeffArgs& a, cudaStream_t s);
 
 void launch_rhs(const StageArgs& a, cudaStream_t s);
+void launch_rhs_stale(const StageArgs& a, cudaStream_t s);
+// maximal slicing (elliptic.cu)
+int max_coeff_blocks(const LevelGeom& G);
+void launch_max_coeffs(const MaxCoeffArgs& a, cudaStream_t s);
+void launch_sor_coeffs(const SorCoeffArgs& a, cudaStream_t s);
+void launch_sor_phys_pass(const SorPhysPassArgs& a, cudaStream_t s);
+void launch_sor_phys_pass_seq(const SorPhysPassArgs& a, cudaStream_t s);
 void launch_aux_point(const AuxArgs& a, cudaStream_t s);
 void launch_aux_deriv(const AuxArgs& a, cudaStream_t s);
 void launch_symmetry(const SymArgs& a, cudaStream_t s);

@@ -72,6 +72,7 @@ def load(build_if_missing=True):
     L.ollin_gpu_fp64_rate.restype = ctypes.c_double
     L.ollin_gpu_kernel_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
+    L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     _lib = L
     return L
 
@@ -164,6 +165,16 @@ class Evolution:
 
     def kernel_timing(self, enable=True):
         self._check(self.L.ollin_gpu_kernel_timing(self.h, 1 if enable else 0))
+
+    def maximal_slicing(self, va_max=None):
+        """maximalslicing.f90 on every level (ollin_gpu_maximal_slicing);
+        va_max = (r, z) maxima of the slicing speeds of the host's last
+        analysis, or None."""
+        if va_max is None:
+            self._check(self.L.ollin_gpu_maximal_slicing(self.h, None))
+        else:
+            v = np.asarray(va_max, dtype=np.float64)
+            self._check(self.L.ollin_gpu_maximal_slicing(self.h, v.ctypes.data))
 
     def ell_stats(self):
         """(coarse-phase iterations, all-level iterations, final residual) of

@@ -43,7 +43,7 @@ class Params(ctypes.Structure):
 
 
 INTEGRATOR = {"rk4": 0, "icn": 1}
-SLICING = {"1+log": 0, "harmonic": 1, "shockavoid": 2, "static": 3}
+SLICING = {"1+log": 0, "harmonic": 1, "shockavoid": 2, "static": 3, "maximal": 4}
 SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3}
 BOUND = {"radiative": 0, "none": 1}
 MATTER = {"vacuum": 0, "scalar": 1}
@@ -52,7 +52,7 @@ IDATA = {"minkowski": 0, "schwarzschild": 1, "BrillLindquist": 2, "BrillWave": 3
 ELL_SOLVER = {"none": 0, "wave": 1, "sor": 2, "mixed": 3}
 PULSE = {"shell": 0, "torus": 1, "Baumgarte": 2}
 BRILLTYPE = {"Holz": 0}
-ILAPSE = {"one": 0, "isotropic": 1, "psiminus2": 2, "psiminus4": 3}
+ILAPSE = {"one": 0, "isotropic": 1, "psiminus2": 2, "psiminus4": 3, "maximal": 4}
 
 # field ids of enum ollin_field
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
@@ -106,7 +106,7 @@ _RENAME = {"Nrtotal": "nrtotal", "Nztotal": "nztotal", "Nl0": "nl0", "BH1mass": 
            "ELL_solver": "ell_solver", "ELL_maxiter": "ell_maxiter", "ELL_epsilon": "ell_epsilon",
            "WE_method": "we_method", "WE_maxiter": "we_maxiter", "WE_eta": "we_eta",
            "WE_diss": "we_diss", "WE_dtfac": "we_dtfac", "WE_epsilon": "we_epsilon"}
-_IGNORED = {"Nt", "Ninfo", "ELL_verbose", "ELL_Noutput", "WE_verbose", "WE_Noutput", "Noutput0D", "Noutput1D", "Noutput2D", "outvars0D", "outvars1D",
+_IGNORED = {"Nt", "maximalevery", "Ninfo", "ELL_verbose", "ELL_Noutput", "WE_verbose", "WE_Noutput", "Noutput0D", "Noutput1D", "Noutput2D", "outvars0D", "outvars1D",
             "outvars2D", "directory", "Nb", "checkpoint", "outparallel", "commenttype"}
 
 

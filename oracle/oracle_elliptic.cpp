@@ -9,7 +9,9 @@
 //   src/elliptic/sor_elliptic.f90    (red-black SOR with Chebyshev
 //       acceleration and Robin / Dirichlet boundaries),
 //   src/matter/idata_scalarpulse.f90 and src/geometry/idata_brillwave.f90
-// for the flat Laplacian that both initial-data routines use, box 0 only.
+// for the flat Laplacian that both initial-data routines use, and
+//   src/geometry/maximalslicing.f90 with the physical Laplacian of the
+//   conformal metric (type = 'physical' in both solvers), box 0 only.
 // Arithmetic follows the Fortran expression order of those files.
 #include <cmath>
 #include <stdexcept>
@@ -26,9 +28,10 @@ namespace {
 const double kPi = 3.141592653589793;  // acos(-1.d0)
 
 // ---------------------------------------------------------------------------
-// wave_elliptic.f90:347-770 (subroutine wavestep), type = 'flat'
+// wave_elliptic.f90:347-770 (subroutine wavestep), type = 'flat' or
+// 'physical'
 // ---------------------------------------------------------------------------
-void wavestep(Sim& S, int level, int Nlmax) {
+void wavestep(Sim& S, int level, int Nlmax, bool physical) {
     const ollin_params& P = S.P;
     Level& L = S.L[level];
     currentgrid(S, L);
@@ -63,12 +66,28 @@ void wavestep(Sim& S, int level, int Nlmax) {
         diff1z(L, u, Dz_u, +1);
         diff2r(L, u, Drr_u, +1);
         diff2z(L, u, Dzz_u, +1);
+        if (physical) diff2rz(L, u, L.a("Drz_ell_u"), +1, +1);
         diff1r(L, v, Dr_v, +1);
         diff1z(L, v, Dz_v, +1);
         su = v;
         for (int j = 1 - g; j <= Nz; ++j)
             for (int i = 1 - g; i <= Nr; ++i) {
-                double s = Drr_u(i, j) + Dzz_u(i, j) + Dr_u(i, j) / r(i, j);
+                double s;
+                if (!physical) {
+                    s = Drr_u(i, j) + Dzz_u(i, j) + Dr_u(i, j) / r(i, j);
+                } else {  // wave_elliptic.f90:781-812
+                    const double gA = L.a("g_A")(i, j), gB = L.a("g_B")(i, j), gC = L.a("g_C")(i, j);
+                    const double rr = r(i, j), ur = Dr_u(i, j), uz = Dz_u(i, j);
+                    s = gA * Drr_u(i, j) + gB * Dzz_u(i, j) + 2.0 * rr * gC * L.a("Drz_ell_u")(i, j);
+                    s = s + ur * (L.a("Dr_g_A")(i, j) + rr * L.a("Dz_g_C")(i, j))
+                          + uz * (L.a("Dz_g_B")(i, j) + rr * L.a("Dr_g_C")(i, j) + gC);
+                    s = s + gA * ur / rr + gC * uz + 0.5 * L.a("ihdet")(i, j)
+                          * (L.a("Dr_hdet")(i, j) * (gA * ur + rr * gC * uz)
+                             + L.a("Dz_hdet")(i, j) * (gB * uz + rr * gC * ur));
+                    s = s + 2.0 * (L.a("Dr_phi")(i, j) * (gA * ur + rr * gC * uz)
+                                   + L.a("Dz_phi")(i, j) * (gB * uz + rr * gC * ur));
+                    s = s / L.a("psi4")(i, j);
+                }
                 s = s + S1(i, j) * u(i, j) + S5(i, j) * p5(u(i, j)) - S0(i, j);
                 s = s - P.we_eta * v(i, j);
                 sv(i, j) = s;
@@ -90,8 +109,8 @@ void wavestep(Sim& S, int level, int Nlmax) {
     S.s[level] = S.s[level] + 1;
     S.t[level] = S.t[level] + dt;
     if (level < Nlmax) {
-        wavestep(S, level + 1, Nlmax);
-        wavestep(S, level + 1, Nlmax);
+        wavestep(S, level + 1, Nlmax, physical);
+        wavestep(S, level + 1, Nlmax, physical);
     }
     if (Nlmax > 0) {
         if (L.ownaxis) symmetries_r(S, L);
@@ -106,8 +125,11 @@ void wavestep(Sim& S, int level, int Nlmax) {
     }
 }
 
-// wave_elliptic.f90:2-345 with type = 'flat', init = 'one'
-void wave_elliptic(Sim& S) {
+// wave_elliptic.f90:2-345 with init = 'one'.  For the physical Laplacian the
+// time step follows the largest speed sqrt|g^ii/psi4| over all levels and the
+// largest slicing speeds va_max[0..1] (r, z) that the caller's last analysis
+// left in va_rp/va_zp (:193-263).
+void wave_elliptic(Sim& S, bool physical, const double* va_max) {
     const ollin_params& P = S.P;
     const int nlev = (int)S.L.size();
     // the time counters are borrowed and given back (wave_elliptic.f90:95-103, 330-340)
@@ -124,7 +146,29 @@ void wave_elliptic(Sim& S) {
         for (double& x : L.a("ell_v").v) x = 0.0;
         for (double& x : L.a("ell_u").v) x = 1.0;
     }
-    const double dt0 = P.we_dtfac * std::min(P.dr0, P.dz0);
+    double dt0 = P.we_dtfac * std::min(P.dr0, P.dz0);
+    if (physical) {
+        double vrmax = 0.0, vzmax = 0.0;
+        for (Level& L : S.L) {
+            double vr = 0.0, vz = 0.0;
+            const int g = L.g;
+            Arr& gA = L.a("g_A"); Arr& gB = L.a("g_B"); Arr& psi4 = L.a("psi4");
+            const double var = va_max ? std::fabs(va_max[0]) : 0.0, vaz = va_max ? std::fabs(va_max[1]) : 0.0;
+            for (int j = 1 - g; j <= L.Nz; ++j)
+                for (int i = 1 - g; i <= L.Nr; ++i) {
+                    const double vlr = std::sqrt(std::fabs(gA(i, j) / psi4(i, j)));
+                    const double vlz = std::sqrt(std::fabs(gB(i, j) / psi4(i, j)));
+                    if (std::fabs(vlr) > vr) vr = std::fabs(vlr);
+                    if (std::fabs(vlz) > vz) vz = std::fabs(vlz);
+                    if (var > vr) vr = var;
+                    if (vaz > vz) vz = vaz;
+                }
+            if (std::fabs(vr) > vrmax) vrmax = std::fabs(vr);
+            if (std::fabs(vz) > vzmax) vzmax = std::fabs(vz);
+        }
+        const double cfac = P.we_dtfac;
+        dt0 = cfac * std::min(std::min(P.dr0, P.dz0), std::min(P.dr0 / vrmax, P.dz0 / vzmax));
+    }
     for (int l = 0; l < nlev; ++l) S.L[l].dt = dt0 / (double)(1L << l);
     const int Nlmax_old = S.Nlmax;
     int Nlmax = (S.Nlmax > 0) ? 0 : S.Nlmax;
@@ -136,7 +180,7 @@ void wave_elliptic(Sim& S) {
         Level& L0 = S.L[0];
         while (step < miniter || (gres > P.we_epsilon && step < P.we_maxiter)) {
             step = step + 1;
-            wavestep(S, 0, Nlmax);
+            wavestep(S, 0, Nlmax, physical);
             Arr& sv = L0.a("sell_v");
             double lres = 0.0;
             for (int j = 1; j <= L0.Nz - L0.g; ++j)
@@ -194,8 +238,8 @@ struct SorArr {
 };
 
 // subroutine sor (sor_elliptic.f90:562-802); returns the iteration count
-int sor(Sim& S, Level& L, SorArr& a, SorArr& b, SorArr& c, SorArr& d, SorArr& e, SorArr& f, SorArr& u,
-        int imax, int jmax, double rjac, double uinf, bool robin) {
+int sor(Sim& S, Level& L, SorArr& a, SorArr& b, SorArr& c, SorArr& d, SorArr& e, SorArr& f, SorArr& cg,
+        SorArr& ch, SorArr& ci, SorArr& cj, SorArr& u, int imax, int jmax, double rjac, double uinf, bool robin) {
     const ollin_params& P = S.P;
     const int g = L.g;
     Arr& r = L.a("r"); Arr& z = L.a("z"); Arr& S5 = L.a("ell_S5");
@@ -210,11 +254,13 @@ int sor(Sim& S, Level& L, SorArr& a, SorArr& b, SorArr& c, SorArr& d, SorArr& e,
             int jsw = isw;
             for (int i = 2; i <= imax - 1; ++i) {
                 for (int j = jsw + 1; j <= jmax - 1; j += 2) {
-                    // the diagonal couplings g,h,i,j are zero for the flat Laplacian
+                    // the diagonal couplings g,h,i,j are zero for the flat
+                    // Laplacian; for the physical one they couple points of
+                    // the same colour, so the loop order matters
                     const double resid = a(i, j) * u(i + 1, j) + b(i, j) * u(i - 1, j)
                         + c(i, j) * u(i, j + 1) + d(i, j) * u(i, j - 1)
-                        + 0.0 * u(i + 1, j + 1) + 0.0 * u(i - 1, j - 1)
-                        + 0.0 * u(i + 1, j - 1) + 0.0 * u(i - 1, j + 1)
+                        + cg(i, j) * u(i + 1, j + 1) + ch(i, j) * u(i - 1, j - 1)
+                        + ci(i, j) * u(i + 1, j - 1) + cj(i, j) * u(i - 1, j + 1)
                         + e(i, j) * u(i, j) - f(i, j);
                     anorm = anorm + p2(resid);
                     u(i, j) = u(i, j) - omega * resid / e(i, j);
@@ -257,7 +303,50 @@ int sor(Sim& S, Level& L, SorArr& a, SorArr& b, SorArr& c, SorArr& d, SorArr& e,
     return P.ell_maxiter;
 }
 
-void sor_elliptic(Sim& S) {
+// sor_elliptic.f90:154-262 (coarse grid, dr*dz) and :371-448 (finer grids,
+// /dr/dz): coefficients of the physical Laplacian at one point
+static void sor_physical_coeffs(Level& L, int i, int j, bool fine, double& a, double& b, double& c, double& d,
+                                double& e, double& cg, double& ch, double& ci, double& cj) {
+    const double one = 1.0, half = 0.5, two = 2.0;
+    const double dr = L.dr, dz = L.dz;
+    const double gA = L.a("g_A")(i, j), gB = L.a("g_B")(i, j), gC = L.a("g_C")(i, j), r = L.a("r")(i, j);
+    const double Dr_g_A = L.a("Dr_g_A")(i, j), Dz_g_C = L.a("Dz_g_C")(i, j);
+    const double Dz_g_B = L.a("Dz_g_B")(i, j), Dr_g_C = L.a("Dr_g_C")(i, j);
+    const double ihdet = L.a("ihdet")(i, j), Dr_hdet = L.a("Dr_hdet")(i, j), Dz_hdet = L.a("Dz_hdet")(i, j);
+    const double Dr_phi = L.a("Dr_phi")(i, j), Dz_phi = L.a("Dz_phi")(i, j), psi4 = L.a("psi4")(i, j);
+    a = gA * (one / dr + half / r) / dr;
+    b = gA * (one / dr - half / r) / dr;
+    c = gB / p2(dz);
+    d = gB / p2(dz);
+    e = -two * (gA / p2(dr) + gB / p2(dz));
+    if (!fine) {
+        cg = +0.5 * r * gC / (dr * dz);
+        ch = +0.5 * r * gC / (dr * dz);
+        ci = -0.5 * r * gC / (dr * dz);
+        cj = -0.5 * r * gC / (dr * dz);
+    } else {
+        cg = +0.5 * r * gC / dr / dz;
+        ch = +0.5 * r * gC / dr / dz;
+        ci = -0.5 * r * gC / dr / dz;
+        cj = -0.5 * r * gC / dr / dz;
+    }
+    a = a + half * (Dr_g_A + r * Dz_g_C) / dr;
+    b = b - half * (Dr_g_A + r * Dz_g_C) / dr;
+    c = c + half * (Dz_g_B + r * Dr_g_C + gC) / dz;
+    d = d - half * (Dz_g_B + r * Dr_g_C + gC) / dz;
+    a = a + 0.25 * ihdet * (gA * Dr_hdet + r * gC * Dz_hdet) / dr;
+    b = b - 0.25 * ihdet * (gA * Dr_hdet + r * gC * Dz_hdet) / dr;
+    c = c + 0.5 * gC / dz + 0.25 * ihdet * (gB * Dz_hdet + r * gC * Dr_hdet) / dz;
+    d = d - 0.5 * gC / dz - 0.25 * ihdet * (gB * Dz_hdet + r * gC * Dr_hdet) / dz;
+    a = a + (gA * Dr_phi + r * gC * Dz_phi) / dr;
+    b = b - (gA * Dr_phi + r * gC * Dz_phi) / dr;
+    c = c + (gB * Dz_phi + r * gC * Dr_phi) / dz;
+    d = d - (gB * Dz_phi + r * gC * Dr_phi) / dz;
+    a = a / psi4; b = b / psi4; c = c / psi4; d = d / psi4; e = e / psi4;
+    cg = cg / psi4; ch = ch / psi4; ci = ci / psi4; cj = cj / psi4;
+}
+
+void sor_elliptic(Sim& S, bool physical) {
     const ollin_params& P = S.P;
     const int nlev = (int)S.L.size();
     for (Level& L : S.L)
@@ -274,20 +363,28 @@ void sor_elliptic(Sim& S) {
         const int imax = L.Nr + g, jmax = L.Nz + g;
         SorArr a(imax, jmax, 0.0), b(imax, jmax, 0.0), c(imax, jmax, 0.0), d(imax, jmax, 0.0), e(imax, jmax, 1.0),
             f(imax, jmax, 0.0), u(imax, jmax, 0.0);
+        SorArr cg(imax, jmax, 0.0), ch(imax, jmax, 0.0), ci(imax, jmax, 0.0), cj(imax, jmax, 0.0);
         Arr& r = L.a("r"); Arr& S1 = L.a("ell_S1"); Arr& S0 = L.a("ell_S0"); Arr& eu = L.a("ell_u");
         const double one = 1.0, half = 0.5, two = 2.0;
         const double dr = L.dr, dz = L.dz;
         for (int i = 1 - g; i <= L.Nr; ++i)
             for (int j = 1 - g; j <= L.Nz; ++j) {
                 u(i + g, j + g) = eu(i, j);
-                a(i + g, j + g) = (one / dr + half / r(i, j)) / dr;
-                b(i + g, j + g) = (one / dr - half / r(i, j)) / dr;
-                c(i + g, j + g) = one / p2(dz);
-                d(i + g, j + g) = one / p2(dz);
-                e(i + g, j + g) = -two * (one / p2(dr) + one / p2(dz)) + S1(i, j);
+                if (!physical) {
+                    a(i + g, j + g) = (one / dr + half / r(i, j)) / dr;
+                    b(i + g, j + g) = (one / dr - half / r(i, j)) / dr;
+                    c(i + g, j + g) = one / p2(dz);
+                    d(i + g, j + g) = one / p2(dz);
+                    e(i + g, j + g) = -two * (one / p2(dr) + one / p2(dz)) + S1(i, j);
+                } else {
+                    sor_physical_coeffs(L, i, j, level > 0, a(i + g, j + g), b(i + g, j + g), c(i + g, j + g),
+                                        d(i + g, j + g), e(i + g, j + g), cg(i + g, j + g), ch(i + g, j + g),
+                                        ci(i + g, j + g), cj(i + g, j + g));
+                    e(i + g, j + g) = e(i + g, j + g) + S1(i, j);
+                }
                 f(i + g, j + g) = S0(i, j);
             }
-        const int n = sor(S, L, a, b, c, d, e, f, u, imax, jmax, rjac, 1.0, robin);
+        const int n = sor(S, L, a, b, c, d, e, f, cg, ch, ci, cj, u, imax, jmax, rjac, 1.0, robin);
         for (int i = 1 - g; i <= L.Nr; ++i)
             for (int j = 1 - g; j <= L.Nz; ++j) eu(i, j) = u(i + g, j + g);
         return n;
@@ -318,8 +415,8 @@ void sor_elliptic(Sim& S) {
 }
 
 void ell_solve(Sim& S) {
-    if (S.P.ell_solver == OLLIN_ELL_WAVE) wave_elliptic(S);
-    else if (S.P.ell_solver == OLLIN_ELL_SOR) sor_elliptic(S);
+    if (S.P.ell_solver == OLLIN_ELL_WAVE) wave_elliptic(S, false, nullptr);
+    else if (S.P.ell_solver == OLLIN_ELL_SOR) sor_elliptic(S, false);
     else throw std::runtime_error("elliptic initial data needs ELL_solver = wave or sor");
 }
 
@@ -430,6 +527,44 @@ void idata_brillwave(Sim& S) {
             Dr_.v[k] = (one - one / A.v[k]) / r.v[k];
             Dz_.v[k] = zero;
         }
+    }
+}
+
+// maximalslicing.f90:3-175: lap(alpha) = (K_ij K^ij + 4 pi (rho + S)) alpha
+// with the physical Laplacian, alpha -> 1 far away; then the lapse
+// derivatives that ``auxiliary`` would give, and nothing else (the other
+// auxiliary quantities of the lapse keep the values of the last
+// ``auxiliary`` call)
+void maximalslicing(Sim& S, const double* va_max) {
+    const ollin_params& P = S.P;
+    const double zero = 0.0, smallpi = std::acos(-1.0);
+    for (Level& L : S.L) {
+        currentgrid(S, L);
+        Arr& S0 = L.a("ell_S0"); Arr& S1 = L.a("ell_S1"); Arr& S5 = L.a("ell_S5"); Arr& K2 = L.a("K2");
+        for (size_t k = 0; k < S0.v.size(); ++k) {
+            S0.v[k] = zero;
+            S5.v[k] = zero;
+            S1.v[k] = -K2.v[k];
+        }
+        if (P.mattertype != OLLIN_MATTER_VACUUM) {
+            Arr& rho = L.a("rho"); Arr& trS = L.a("trS");
+            for (size_t k = 0; k < S1.v.size(); ++k) S1.v[k] = S1.v[k] - 4.0 * smallpi * (rho.v[k] + trS.v[k]);
+        }
+    }
+    if (P.ell_solver == OLLIN_ELL_WAVE) wave_elliptic(S, true, va_max);
+    else if (P.ell_solver == OLLIN_ELL_SOR) sor_elliptic(S, true);
+    else throw std::runtime_error("maximal slicing needs ELL_solver = wave or sor");
+    for (Level& L : S.L) L.a("alpha").v = L.a("ell_u").v;
+    for (Level& L : S.L) {
+        currentgrid(S, L);
+        Arr& alpha = L.a("alpha"); Arr& Dr_alpha = L.a("Dr_alpha"); Arr& r = L.a("r"); Arr& aux = L.a("auxarray");
+        diff1r(L, alpha, Dr_alpha, +1);
+        diff1z(L, alpha, L.a("Dz_alpha"), +1);
+        diff2r(L, alpha, L.a("Drr_alpha"), +1);
+        diff2z(L, alpha, L.a("Dzz_alpha"), +1);
+        diff2rz(L, alpha, L.a("Drz_alpha"), +1, +1);
+        for (size_t k = 0; k < aux.v.size(); ++k) aux.v[k] = Dr_alpha.v[k] / r.v[k];
+        diff1r(L, aux, L.a("DD_alphar"), +1);
     }
 }
 

@@ -354,7 +354,8 @@ void auxiliary_geometry(Sim& S, Level& L) {
     // ---- Bona-Masso function (:100-168)
     R(falpha);
     switch (P.slicing) {
-        case OLLIN_SLICING_STATIC: ALL falpha(i, j) = 0.0; break;
+        case OLLIN_SLICING_STATIC:
+        case OLLIN_SLICING_MAXIMAL: ALL falpha(i, j) = 0.0; break;
         case OLLIN_SLICING_HARMONIC: ALL falpha(i, j) = p2(alpha(i, j)) * P.gauge_f; break;
         case OLLIN_SLICING_1PLUSLOG: ALL falpha(i, j) = alpha(i, j) * P.gauge_f; break;
         case OLLIN_SLICING_SHOCKAVOID: ALL falpha(i, j) = p2(alpha(i, j)) + (P.gauge_f - 1.0); break;
@@ -996,7 +997,8 @@ void sources_geometry(Sim& S, Level& L) {
         }
     }
     // trK (:196-252)
-    if (P.slicing == OLLIN_SLICING_STATIC && false) {
+    if (P.slicing == OLLIN_SLICING_MAXIMAL) {  // :200-204
+        ALL strK(i, j) = zero;
     } else {
         ALL strK(i, j) = -Lapla_alpha(i, j);
         ALL strK(i, j) = strK(i, j) + alpha(i, j) * K2(i, j);
@@ -1109,7 +1111,7 @@ void sources_geometry(Sim& S, Level& L) {
 void sources_lapse(Sim& S, Level& L) {
     GRID_DIMS;
     R(salpha); R(falpha); R(trK); R(alpha);
-    if (S.P.slicing == OLLIN_SLICING_STATIC) {
+    if (S.P.slicing == OLLIN_SLICING_STATIC || S.P.slicing == OLLIN_SLICING_MAXIMAL) {
         ALL salpha(i, j) = 0.0;
     } else {
         ALL salpha(i, j) = -falpha(i, j) * trK(i, j);
@@ -1230,7 +1232,7 @@ void radiative_geometry(Sim& S, Level& L) {
     R(KTA); R(sKTA); R(Dr_KTA); R(Dz_KTA);
     R(KTB); R(sKTB); R(Dr_KTB); R(Dz_KTB);
     R(KTC); R(sKTC); R(Dr_KTC); R(Dz_KTC);
-    radbound(L, trK, strK, Dr_trK, Dz_trK, va, var0);
+    if (P.slicing != OLLIN_SLICING_MAXIMAL) radbound(L, trK, strK, Dr_trK, Dz_trK, va, var0);  // :70-76
     radbound(L, KTA, sKTA, Dr_KTA, Dz_KTA, vl, var0);
     radbound(L, KTB, sKTB, Dr_KTB, Dz_KTB, vl, var0);
     for (int j = 1 - g; j <= Nz; ++j) {

@@ -589,6 +589,11 @@ int ollin_oracle_aux(ollin_oracle* o, int level) {
     }
 }
 
+// maximalslicing (evolve.f90:228-230 and :388-393); va_max (r, z) may be null
+int ollin_oracle_maximal_slicing(ollin_oracle* o, const double* va_max) {
+    try { maximalslicing(o->S, va_max); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }
+}
+
 int ollin_oracle_constraints(ollin_oracle* o, int level) {
     try { constraints(o->S, o->S.L[level]); return 0; } catch (const std::exception& e) { g_oracle_err = e.what(); return 1; }
 }

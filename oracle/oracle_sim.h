@@ -51,6 +51,7 @@ void diff1r(Level& L, const Arr& f, Arr& d, int symr);
 void diff1z(Level& L, const Arr& f, Arr& d, int symz);
 void diff2r(Level& L, const Arr& f, Arr& d, int symr);
 void diff2z(Level& L, const Arr& f, Arr& d, int symz);
+void diff2rz(Level& L, const Arr& f, Arr& d, int symr, int symz);
 void dissipation(Level& L, const Arr& ev, Arr& src, int symr, int symz, double diss);
 void radbound(Level& L, const Arr& ev, Arr& src, const Arr& Dr_var, const Arr& Dz_var, double v, double var0);
 void potential(Sim& S, Level& L);
@@ -70,6 +71,7 @@ void restrict_(Sim& S, int level);
 // elliptic initial data (oracle_elliptic.cpp)
 void idata_scalarpulse(Sim& S);
 void idata_brillwave(Sim& S);
+void maximalslicing(Sim& S, const double* va_max);
 
 // solver statistics of the last elliptic solve: iterations of each phase
 struct EllStats { int steps[2] = {0, 0}; int phases = 0; double gres = 0.0; };

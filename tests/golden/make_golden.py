@@ -68,6 +68,29 @@ CASES = {
     "ell_sor_2lev": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
                          ilapse="one", mattertype="scalar", scalar_a0=0.05, ell_solver="sor",
                          scalardiss=0.02, _steps=[0], _elliptic=True),
+    # maximal slicing (maximalslicing.f90, physical Laplacian).  Time-symmetric
+    # vacuum data have K_ij = 0 and a maximal lapse of exactly 1, and so does
+    # a static massless scalar field (rho + S = 0), so the cases solve where
+    # the source is not zero.  Initial maximal lapse on a massive scalar pulse
+    # (rho + S = -2V, a small amplitude: the source then has the sign that
+    # makes the damped wave equation grow, and must stay below the lowest
+    # eigenvalue of the Laplacian on the grid), then 1+log evolution: the
+    # first stage of each level sees the new lapse and its derivatives but
+    # the other auxiliary quantities of the old one; WaveElliptic capped
+    "max_ilapse_pulse": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                             ilapse="maximal", mattertype="scalar", scalarpotential="phi2", scalar_mass=1.0,
+                             scalar_a0=0.02, scalar_r0=2.0, scalar_z0=2.0, scalardiss=0.02, we_maxiter=200,
+                             _steps=[0, 1], _elliptic=True),
+    # maximalevery = 1 on Schwarzschild data: a (trivial) solve at t = 0, then
+    # one after every coarse step, where K_ij is no longer zero
+    "max_every_wave": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.25, dz0=0.25, maximalevery=1,
+                           we_maxiter=120, _steps=[0, 1, 2], _elliptic=True),
+    # slicing = maximal with SOR after every coarse step; the Gamma-driver
+    # shift makes C, and so the mixed (same-colour) couplings of the SOR
+    # stencil, nonzero after the first step
+    "max_slicing_sor": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, ilapse="one",
+                            slicing="maximal", ell_solver="sor", shift="Gammadriver2", drivercsi=0.75,
+                            drivereta=2.0, _steps=[0, 1, 2], _elliptic=True),
 }
 
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
@@ -110,7 +133,9 @@ def run_case(refdir, name, cfg):
             ph, xr, xz, pi = scalar_pulse(r, z)
             for nm, v in zip(["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"], [ph, xr, xz, pi]):
                 sim.set_field(lev, nm, v)
+    ini_iters = wave_iters[0]
     sim.initialize()
+    max_iters = [wave_iters[0] - ini_iters]
     names = list(FIELDS)
     if cfg.get("shift", "none") != "none":
         names += SHIFT_FIELDS
@@ -118,7 +143,8 @@ def run_case(refdir, name, cfg):
         names += SCALAR_FIELDS
     out = {}
     if elliptic:
-        out["wave_iterations"] = np.array(wave_iters[0])
+        out["wave_iterations"] = np.array(ini_iters)
+        out["max_wave_iterations_s0"] = np.array(max_iters[0])
         for lev in sim.levels():
             for nm in ("psi", "ell_u", "ell_S1"):
                 out["ell_L%d_%s" % (lev, nm)] = sim.field(lev, nm)
@@ -128,6 +154,12 @@ def run_case(refdir, name, cfg):
             t0 = time.time()
             sim.step()
             done += 1
+            # evolve.f90:388-393
+            me = int(cfg.get("maximalevery", 0))
+            if cfg.get("slicing") == "maximal" or (me != 0 and done % me == 0):
+                before = wave_iters[0]
+                sim.maximal_slicing()
+                out["max_wave_iterations_s%d" % done] = np.array(wave_iters[0] - before)
             print("  %s: step %d in %.1fs" % (name, done, time.time() - t0), flush=True)
         for lev in sim.levels():
             for nm in names:

@@ -41,6 +41,7 @@ SOURCES = [
     "src/matter/scalar.f90",
     "src/elliptic/wave_elliptic.f90", "src/elliptic/sor_elliptic.f90",
     "src/matter/idata_scalarpulse.f90", "src/geometry/idata_brillwave.f90",
+    "src/geometry/maximalslicing.f90",
 ]
 GENERATED = ["saveold.f90", "accumulate.f90", "update.f90", "symmetries_r.f90",
              "symmetries_z.f90"]
@@ -326,11 +327,16 @@ class RefSim:
                 self.use(lev)
                 M.dtbeta_r[...] = M.drivercsi * M.delta_r
                 M.dtbeta_z[...] = M.drivercsi * M.delta_z
+        # evolve.f90:228-230; no analysis has run, so va_rp/va_zp are zero
         if M.slicing == "maximal" or M.ilapse == "maximal" or M.maximalevery != 0:
-            raise NotImplementedError("maximal slicing is outside the golden-vector scope")
+            F.maximalslicing()
 
     def step(self):
         self.prog.F.onestep(0)
+
+    def maximal_slicing(self):
+        """call maximalslicing, as evolve.f90:388-393 does after a coarse step."""
+        self.prog.F.maximalslicing()
 
     def field(self, level, name):
         """Interior+ghost copy of a grid array (Fortran (i,j) -> [i+g-1, j+g-1])."""

@@ -41,6 +41,7 @@ def lib():
         L.ollin_oracle_set.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int]
         L.ollin_oracle_aux.argtypes = [vp, ctypes.c_int]
         L.ollin_oracle_constraints.argtypes = [vp, ctypes.c_int]
+        L.ollin_oracle_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
         L.ollin_oracle_norms.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p]
         L.ollin_oracle_point_updates.argtypes = [vp]
         L.ollin_oracle_point_updates.restype = ctypes.c_double
@@ -108,6 +109,15 @@ class Oracle:
 
     def constraints(self, level):
         self._check(self.L.ollin_oracle_constraints(self.h, level))
+
+    def maximal_slicing(self, va_max=None):
+        """maximalslicing.f90 on every level; va_max = (r, z) maxima of the
+        slicing speeds of the last analysis, or None."""
+        if va_max is None:
+            self._check(self.L.ollin_oracle_maximal_slicing(self.h, None))
+        else:
+            v = np.asarray(va_max, dtype=np.float64)
+            self._check(self.L.ollin_oracle_maximal_slicing(self.h, v.ctypes.data))
 
     def norms(self, level, name):
         out = np.zeros(5)

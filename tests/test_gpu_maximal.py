@@ -1,0 +1,126 @@
+"""Maximal slicing on the GPU (ollin_gpu_maximal_slicing, C ABI) against the
+oracle's restatement of maximalslicing.f90: the lapse after each solve, the
+iteration counts of the wave solver, and the evolution that follows, whose
+first stage on each level reads the lapse quantities of the last
+``auxiliary`` call as the reference's does.
+
+The host sequence is that of evolve.f90: a solve after ``initialize`` when
+slicing or ilapse is "maximal" or maximalevery /= 0 (:228-230), and after a
+coarse step when slicing is "maximal" or every maximalevery steps
+(:388-393).
+
+Bound: the lapse of a solve agrees to rounding (about 1e-13; the device
+forms the coefficient derivatives with folded stencil constants) and the
+wave iteration counts are equal.  Fields after a solve are held to 1e-9
+normwise: trK starts from zero, so the relative difference of the small
+trK a step later amplifies the rounding of the lapse's second derivatives
+(observed 2e-10)."""
+import pytest
+
+from oracle_bind import Oracle, ell_stats
+from parity_util import field_list, params, rel_diff, tol_for
+
+pytestmark = pytest.mark.gpu
+
+BASE = dict(eqsym=1, order="four", integrator="rk4", slicing="1+log", gauge_f=2.0, geodiss=0.02, dtfac=0.25,
+            boundtype="radiative")
+
+# initial maximal lapse on a massive scalar pulse (source 4 pi (rho + S) =
+# -8 pi V: small, since with this sign a larger source makes the damped wave
+# equation grow), wave solver on two levels, then 1+log evolution
+PULSE = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse", ilapse="maximal",
+             mattertype="scalar", scalarpotential="phi2", scalar_mass=1.0, scalar_a0=0.02, scalar_r0=2.0,
+             scalar_z0=2.0, scalardiss=0.02, we_maxiter=200)
+# a solve after every coarse step of a Schwarzschild puncture (K_ij /= 0
+# after the first step)
+EVERY = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.25, dz0=0.25, idata="schwarzschild", bh1mass=1.0,
+             ilapse="psiminus2", maximalevery=1, we_maxiter=150)
+# slicing = maximal with SOR and the Gamma-driver shift: C /= 0 after the
+# first step, so the SOR stencil couples points of one colour
+SOR_SHIFT = dict(BASE, nrtotal=20, nztotal=20, nl0=0, dr0=0.25, dz0=0.25, idata="schwarzschild", bh1mass=1.0,
+                 ilapse="one", slicing="maximal", ell_solver="sor", shift="Gammadriver2", drivercsi=0.75,
+                 drivereta=2.0)
+# SOR on two levels with C = 0 (the colours decouple), scalar pulse
+SOR_PULSE = dict(PULSE, nrtotal=20, nztotal=20, ell_solver="sor", we_maxiter=100000)
+
+
+def maximal_due(cfg, step):
+    me = int(cfg.get("maximalevery", 0))
+    if step == 0:
+        return cfg.get("slicing") == "maximal" or cfg.get("ilapse") == "maximal" or me != 0
+    return cfg.get("slicing") == "maximal" or (me != 0 and step % me == 0)
+
+
+def solve_both(o, e, cfg, va_max, tag):
+    o.maximal_slicing(va_max)
+    e.maximal_slicing(va_max)
+    o0, o1, _, _ = ell_stats()
+    g0, g1, _ = e.ell_stats()
+    if cfg.get("ell_solver", "wave") == "wave":
+        assert (g0, g1) == (o0, o1), "%s: iterations gpu %s oracle %s" % (tag, (g0, g1), (o0, o1))
+    for lev in o.levels():
+        d = rel_diff(e.download(lev, "alpha"), o.get(lev, "alpha"))
+        assert d <= tol_for("alpha"), "%s level %d alpha: rel diff %.3e" % (tag, lev, d)
+
+
+TOL = 1e-9
+
+
+def compare(o, e, cfg, tag):
+    for lev in o.levels():
+        for nm in field_list(cfg):
+            d = rel_diff(e.download(lev, nm), o.get(lev, nm))
+            assert d <= max(TOL, tol_for(nm)), "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
+
+
+def run(cfg, steps, va_max=None):
+    from ollin.gpu import Evolution
+    p = params(cfg)
+    o, e = Oracle(p), Evolution(p)
+    o.initial_data()
+    e.initial_data()
+    o.initialize()
+    e.initialize()
+    assert maximal_due(cfg, 0)
+    solve_both(o, e, cfg, va_max, "t=0")
+    for k in range(1, steps + 1):
+        assert o.step() == e.step()
+        compare(o, e, cfg, "step %d" % k)
+        if maximal_due(cfg, k):
+            solve_both(o, e, cfg, va_max, "after step %d" % k)
+    return o, e
+
+
+def test_initial_maximal_lapse_scalar_pulse():
+    o, e = run(PULSE, 2)
+    a = e.download(0, "alpha")
+    assert a.max() > 1.001  # the source is not zero: a nontrivial lapse
+
+
+def test_maximal_every_step_wave():
+    run(EVERY, 3)
+
+
+def test_maximal_every_step_with_speeds():
+    """The slicing speeds of the host's last analysis enter the wave
+    solver's time step (wave_elliptic.f90:211-263)."""
+    run(dict(EVERY, nl0=0), 2, va_max=(1.7, 1.3))
+
+
+def test_maximal_slicing_sor_with_shift():
+    o, e = run(SOR_SHIFT, 3)
+    # maximal slicing keeps trK = 0 (strK = 0, no radiative boundary)
+    assert abs(e.download(0, "trK")).max() == 0.0
+
+
+def test_maximal_lapse_sor_two_levels():
+    run(SOR_PULSE, 1)
+
+
+def test_mixed_solver_is_rejected():
+    from ollin.gpu import Evolution, OllinError
+    e = Evolution(params(dict(EVERY, ell_solver="mixed")))
+    e.initial_data()
+    e.initialize()
+    with pytest.raises(OllinError):
+        e.maximal_slicing()

@@ -134,6 +134,65 @@ def test_oracle_elliptic_data_matches_reference_fortran(name):
 # differences of the initial data stay at the 1e-13 level through them.
 ELL_TOL = 1e-9
 
+MAX_CASES = ["max_ilapse_pulse", "max_every_wave", "max_slicing_sor"]
+
+
+def maximal_due(cfg, step):
+    """evolve.f90:228 (step 0) and :388-391 (after coarse step ``step``)."""
+    me = int(cfg.get("maximalevery", 0))
+    if step == 0:
+        return cfg.get("slicing") == "maximal" or cfg.get("ilapse") == "maximal" or me != 0
+    return cfg.get("slicing") == "maximal" or (me != 0 and step % me == 0)
+
+
+@pytest.mark.parametrize("name", MAX_CASES)
+def test_oracle_maximal_slicing_matches_reference_fortran(name):
+    """maximalslicing.f90 (physical Laplacian in wave_elliptic.f90 or
+    sor_elliptic.f90) executed by the reference's own Fortran at t = 0
+    (evolve.f90:228-230) and, for slicing = maximal, after every coarse step
+    (:388-393): the lapse solution and source on every level, the wave
+    iteration count, and the evolved state at the stored steps."""
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture %s not generated" % name)
+    d, meta = load(name)
+    cfg = ell_cfg(meta)
+    o = Oracle(params(cfg))
+    o.initial_data()
+    o.initialize()
+    wave = cfg.get("ell_solver", "wave") == "wave"
+
+    def solve(step):
+        o.maximal_slicing()
+        s0, s1, phases, _ = ell_stats()
+        if wave:
+            ref = int(d["max_wave_iterations_s%d" % step])
+            assert s0 + s1 == ref, (step, s0, s1, ref)
+
+    assert maximal_due(cfg, 0)
+    solve(0)
+    for lev in o.levels():
+        for nm in ("ell_u", "ell_S1"):
+            ref = d["ell_L%d_%s" % (lev, nm)]
+            got = o.get(lev, nm)
+            scale = max(np.abs(ref).max(), 1e-300)
+            err = np.abs(got - ref).max() / scale
+            assert err <= ELL_TOL, "%s level %d %s: rel %.3e" % (name, lev, nm, err)
+    done = 0
+    for target in meta["steps"]:
+        while done < target:
+            o.step()
+            done += 1
+            if maximal_due(cfg, done):
+                solve(done)
+        for lev in o.levels():
+            for nm in meta["fields"]:
+                ref = d["s%d_L%d_%s" % (done, lev, nm)]
+                got = o.get(lev, nm)
+                scale = max(np.abs(ref).max(), 1e-300)
+                err = np.abs(got - ref).max() / scale
+                assert err <= ELL_TOL, "%s step %d level %d %s: rel %.3e" % (name, done, lev, nm, err)
+
 
 def test_golden_fixture_inventory():
     for name in CASES:
