@@ -144,6 +144,13 @@ typedef struct ollin_params {
     int    brilltype;          /* 0 = "Holz" */
     double scalar_a0, scalar_r0, scalar_z0, scalar_sr0, scalar_sz0;
     double brill_a0, brill_sr0, brill_sz0;
+    /* refinement boxes (appended; param.f90:115-139, setupboxes.f90): box 0
+     * is the base grid with Nl0 levels above it, boxes 1..nb have levels
+     * 1..nl[b-1] of nrbox x nzbox points centred at (rbox, zbox) */
+    int    nb;                 /* Nb, 0..3 */
+    int    nl[3];              /* Nl1, Nl2, Nl3 */
+    int    nrbox[3], nzbox[3]; /* Nrbox1..3, Nzbox1..3 */
+    double rbox[3], zbox[3];   /* rbox1..3, zbox1..3 (before the alignment of setupboxes.f90:186-206) */
 } ollin_params;
 
 /* Evolved and auxiliary fields addressable by upload/download.  The names are

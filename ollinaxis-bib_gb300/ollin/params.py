@@ -39,6 +39,9 @@ class Params(ctypes.Structure):
         ("scalar_a0", ctypes.c_double), ("scalar_r0", ctypes.c_double), ("scalar_z0", ctypes.c_double),
         ("scalar_sr0", ctypes.c_double), ("scalar_sz0", ctypes.c_double),
         ("brill_a0", ctypes.c_double), ("brill_sr0", ctypes.c_double), ("brill_sz0", ctypes.c_double),
+        ("nb", ctypes.c_int), ("nl", ctypes.c_int * 3),
+        ("nrbox", ctypes.c_int * 3), ("nzbox", ctypes.c_int * 3),
+        ("rbox", ctypes.c_double * 3), ("zbox", ctypes.c_double * 3),
     ]
 
 
@@ -95,6 +98,9 @@ def default_params():
     p.scalar_a0, p.scalar_r0, p.scalar_z0 = _single(0.0), _single(0.0), _single(0.0)
     p.scalar_sr0, p.scalar_sz0 = _single(1.0), _single(1.0)
     p.brill_a0, p.brill_sr0, p.brill_sz0 = _single(0.0), _single(1.0), _single(1.0)
+    p.nb = 0
+    for k in range(3):
+        p.nl[k], p.nrbox[k], p.nzbox[k], p.rbox[k], p.zbox[k] = 0, 1, 1, 0.0, 0.0
     return p
 
 
@@ -107,7 +113,7 @@ _RENAME = {"Nrtotal": "nrtotal", "Nztotal": "nztotal", "Nl0": "nl0", "BH1mass": 
            "WE_method": "we_method", "WE_maxiter": "we_maxiter", "WE_eta": "we_eta",
            "WE_diss": "we_diss", "WE_dtfac": "we_dtfac", "WE_epsilon": "we_epsilon"}
 _IGNORED = {"Nt", "maximalevery", "Ninfo", "ELL_verbose", "ELL_Noutput", "WE_verbose", "WE_Noutput", "Noutput0D", "Noutput1D", "Noutput2D", "outvars0D", "outvars1D",
-            "outvars2D", "directory", "Nb", "checkpoint", "outparallel", "commenttype"}
+            "outvars2D", "directory", "checkpoint", "outparallel", "commenttype"}
 
 
 def set_param(p, name, value):
@@ -133,6 +139,16 @@ def set_param(p, name, value):
     m = re.match(r"^ft([1-8])$", name)
     if m:
         p.ft[int(m.group(1)) - 1] = float(value)
+        return
+    if name == "Nb":
+        p.nb = int(float(str(value)))
+        return
+    # the per-box parameters Nl1..3, Nrbox1..3, Nzbox1..3, rbox1..3, zbox1..3
+    m = re.match(r"^(Nl|Nrbox|Nzbox|rbox|zbox)([1-3])$", name)
+    if m:
+        arr = getattr(p, m.group(1).lower())
+        v = str(value).strip().replace("d", "e").replace("D", "e")
+        arr[int(m.group(2)) - 1] = float(v) if m.group(1) in ("rbox", "zbox") else int(float(v))
         return
     if not hasattr(p, name):
         raise ValueError("unknown parameter %s" % name)

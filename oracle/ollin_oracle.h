@@ -22,6 +22,7 @@ int ollin_oracle_set(ollin_oracle* o, int level, const char* name, const double*
 int ollin_oracle_aux(ollin_oracle* o, int level);
 int ollin_oracle_constraints(ollin_oracle* o, int level);
 int ollin_oracle_maximal_slicing(ollin_oracle* o, const double* va_max);
+int ollin_oracle_grid(const ollin_oracle* o, int gid, int* box, int* level);
 int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]);
 double ollin_oracle_point_updates(const ollin_oracle* o);
 /* iteration counts of the last elliptic solve on this thread: steps[0] of

@@ -131,6 +131,7 @@ void wavestep(Sim& S, int level, int Nlmax, bool physical) {
 // left in va_rp/va_zp (:193-263).
 void wave_elliptic(Sim& S, bool physical, const double* va_max) {
     const ollin_params& P = S.P;
+    if (S.Nb > 0) throw std::runtime_error("oracle: the elliptic solvers are restated for box 0 only");
     const int nlev = (int)S.L.size();
     // the time counters are borrowed and given back (wave_elliptic.f90:95-103, 330-340)
     const auto s_ext = S.s; const auto t_ext = S.t, t1_ext = S.t1, t2_ext = S.t2;
@@ -348,6 +349,7 @@ static void sor_physical_coeffs(Level& L, int i, int j, bool fine, double& a, do
 
 void sor_elliptic(Sim& S, bool physical) {
     const ollin_params& P = S.P;
+    if (S.Nb > 0) throw std::runtime_error("oracle: the elliptic solvers are restated for box 0 only");
     const int nlev = (int)S.L.size();
     for (Level& L : S.L)
         for (double& x : L.a("ell_u").v) x = 1.0;

@@ -30,7 +30,15 @@ static void setup(Sim& S) {
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) throw std::runtime_error("oracle: lagrangian+factorhdet+evolveH only");
     if (P.evolveKTH) throw std::runtime_error("oracle: evolveKTH unsupported");
     S.g = P.ghost ? P.ghost : 3;
-    S.Nlmax = P.nl0;
+    const int g = S.g;
+    // setupboxes.f90:25-80: boxes and their levels
+    if (P.nb < 0 || P.nb > 3) throw std::runtime_error("The number of refinement boxes must be between 0 and 3");
+    S.Nb = P.nb;
+    S.Nl[0] = P.nl0;
+    for (int b = 1; b <= 3; ++b) S.Nl[b] = P.nl[b - 1];
+    S.Nlmax = 0;
+    for (int b = 0; b <= 3; ++b) S.Nlmax = std::max(S.Nlmax, S.Nl[b]);
+    if (S.Nb > 0 && S.Nlmax == 0) throw std::runtime_error("If you choose Nb>0 you must also have Nl>0 for at least one box");
     const int L = S.Nlmax;
     const double dt0 = P.dtfac * std::min(P.dr0, P.dz0);
     S.dtl.resize(L + 1); S.drl.resize(L + 1); S.dzl.resize(L + 1);
@@ -39,32 +47,83 @@ static void setup(Sim& S) {
         S.drl[l] = P.dr0 / (double)(1 << l);
         S.dzl[l] = P.dz0 / (double)(1 << l);
     }
-    int nz = P.nztotal;
-    if (!P.eqsym && (nz + S.g) % 2 == 0) nz += 1;  // setupboxes.f90:131-135
-    S.t.assign(L + 1, 0.0); S.t1.assign(L + 1, 0.0); S.t2.assign(L + 1, 0.0); S.s.assign(L + 1, 0);
-    S.rminl.resize(L + 1); S.rmaxl.resize(L + 1); S.zminl.resize(L + 1); S.zmaxl.resize(L + 1);
-    S.L.resize(L + 1);
-    const int g = S.g;
-    for (int l = 0; l <= L; ++l) {
-        Level& lv = S.L[l];
-        lv.level = l; lv.g = g; lv.Nr = P.nrtotal; lv.Nz = nz;
+    // box sizes and centres (setupboxes.f90:131-206)
+    int Nrbox[4], Nzbox[4];
+    Nrbox[0] = P.nrtotal;
+    Nzbox[0] = P.nztotal;
+    if (!P.eqsym && (Nzbox[0] + g) % 2 == 0) Nzbox[0] += 1;
+    for (int b = 1; b <= 3; ++b) { Nrbox[b] = P.nrbox[b - 1]; Nzbox[b] = P.nzbox[b - 1]; }
+    for (int b = 0; b <= S.Nb; ++b)
+        if (Nrbox[b] < 2 + g || Nzbox[b] < 2 + g)
+            throw std::runtime_error("The values of (Nrtotal,Nztotal,Nrbox,Nzbox) should be greater than 2 plus the number of ghost zones");
+    S.rbox[0] = 0.0; S.zbox[0] = 0.0;
+    for (int b = 1; b <= 3; ++b) { S.rbox[b] = P.rbox[b - 1]; S.zbox[b] = P.zbox[b - 1]; }
+    for (int b = 1; b <= S.Nb; ++b) {
+        const double d1r = S.drl[std::min(1, L)], d1z = S.dzl[std::min(1, L)];
+        if (S.rbox[b] != 0.0) S.rbox[b] = ((double)(long)(S.rbox[b] / d1r) + 0.5) * d1r;
+        if (S.zbox[b] != 0.0) {
+            if (P.eqsym) S.zbox[b] = ((double)(long)(S.zbox[b] / d1z) + 0.5) * d1z;
+            else S.zbox[b] = (double)(long)(S.zbox[b] / d1z) * d1z;
+        }
+    }
+    for (int b = 1; b <= S.Nb; ++b) {  // setupboxes.f90:210-285
+        const double d1r = S.drl[std::min(1, L)], d1z = S.dzl[std::min(1, L)];
+        if (S.rbox[b] < 0.0) throw std::runtime_error("rbox must be larger than or equal to 0 for all refinement boxes");
+        if (S.rbox[b] > 0.0 && S.rbox[b] - 0.5 * Nrbox[b] * d1r <= 0.0)
+            throw std::runtime_error("Refinement box extends to negative values of r");
+        if (S.rbox[b] + 0.5 * Nrbox[b] * d1r >= (Nrbox[0] - g) * P.dr0)
+            throw std::runtime_error("Refinement box extends beyond base grid in r direction");
+        if (P.eqsym) {
+            if (S.zbox[b] < 0.0) throw std::runtime_error("For equatorial symmetry zbox must be larger than or equal to 0");
+            if (S.zbox[b] > 0.0 && S.zbox[b] - 0.5 * Nzbox[b] * d1z <= 0.0)
+                throw std::runtime_error("Refinement box extends to negative values of z");
+            if (S.zbox[b] + 0.5 * Nzbox[b] * d1z >= (Nzbox[0] - g) * P.dz0)
+                throw std::runtime_error("Refinement box extends beyond base grid in z direction");
+        } else {
+            if (S.zbox[b] - 0.5 * Nzbox[b] * d1z <= -0.5 * (Nzbox[0] - g) * P.dz0 ||
+                S.zbox[b] + 0.5 * Nzbox[b] * d1z >= 0.5 * (Nzbox[0] - g) * P.dz0)
+                throw std::runtime_error("Refinement box extends beyond base grid in z direction");
+        }
+    }
+    // grids: box 0 levels 0..Nl0, then boxes 1..Nb levels 1..Nl(b)
+    std::vector<std::pair<int, int>> grids;
+    for (int l = 0; l <= S.Nl[0]; ++l) grids.push_back({0, l});
+    for (int b = 1; b <= S.Nb; ++b)
+        for (int l = 1; l <= S.Nl[b]; ++l) grids.push_back({b, l});
+    const int ng = (int)grids.size();
+    S.t.assign(ng, 0.0); S.t1.assign(ng, 0.0); S.t2.assign(ng, 0.0); S.s.assign(ng, 0);
+    S.rminl.resize(ng); S.rmaxl.resize(ng); S.zminl.resize(ng); S.zmaxl.resize(ng);
+    S.L.resize(ng);
+    for (int k = 0; k < ng; ++k) {
+        const int b = grids[k].first, l = grids[k].second;
+        Level& lv = S.L[k];
+        lv.gid = k;
+        lv.level = l; lv.box = b; lv.g = g; lv.Nr = Nrbox[b]; lv.Nz = Nzbox[b];
+        // finebound/restrict partner: level 1 of any box talks to the base grid
+        lv.parent = -1;
+        if (l > 0) {
+            const int pb = (l == 1) ? 0 : b;
+            for (int q = 0; q < ng; ++q)
+                if (grids[q].first == pb && grids[q].second == l - 1) lv.parent = q;
+        }
         lv.dr = S.drl[l]; lv.dz = S.dzl[l]; lv.dt = S.dtl[l];
         lv.eqsym = P.eqsym != 0;
-        lv.ownaxis = true;
-        lv.ownequator = P.eqsym != 0;  // main.f90:393-424 (box 0, one process)
+        lv.ownaxis = S.rbox[b] == 0.0;                         // main.f90:393-403
+        lv.ownequator = P.eqsym != 0 && S.zbox[b] == 0.0;      // main.f90:412-424
         Arr& r = lv.a("r"); Arr& z = lv.a("z"); Arr& rr = lv.a("rr");
         for (int j = 1 - g; j <= lv.Nz; ++j)
             for (int i = 1 - g; i <= lv.Nr; ++i) {  // evolve.f90:42-70
-                r(i, j) = ((double)(0 + i) - 0.5) * lv.dr;
-                if (P.eqsym) z(i, j) = ((double)(0 + j) - 0.5) * lv.dz;
-                else z(i, j) = 0.0 + ((double)(0 + j) - 0.5 * (double)(lv.Nz - g + 1)) * lv.dz;
+                if (S.rbox[b] == 0.0) r(i, j) = ((double)(0 + i) - 0.5) * lv.dr;
+                else r(i, j) = S.rbox[b] + ((double)(0 + i) - 0.5 * (double)(lv.Nr - g + 1)) * lv.dr;
+                if (P.eqsym && S.zbox[b] == 0.0) z(i, j) = ((double)(0 + j) - 0.5) * lv.dz;
+                else z(i, j) = S.zbox[b] + ((double)(0 + j) - 0.5 * (double)(lv.Nz - g + 1)) * lv.dz;
             }
         for (int j = 1 - g; j <= lv.Nz; ++j)
             for (int i = 1 - g; i <= lv.Nr; ++i) rr(i, j) = std::sqrt(p2(r(i, j)) + p2(z(i, j)));
-        S.rminl[l] = r(1 - g, 0);
-        S.rmaxl[l] = r(lv.Nr, 0);
-        S.zminl[l] = z(0, 1 - g);
-        S.zmaxl[l] = z(0, lv.Nz);
+        S.rminl[k] = r(1 - g, 0);
+        S.rmaxl[k] = r(lv.Nr, 0);
+        S.zminl[k] = z(0, 1 - g);
+        S.zmaxl[k] = z(0, lv.Nz);
     }
     // EVOLVE arrays in generated update.f90 order, with their parity tags
     // (src/base/arrays.config:154-1045)
@@ -97,7 +156,7 @@ static void setup(Sim& S) {
 static inline size_t hr(const Level& L, int m, int j, int k) { return (size_t)m + (size_t)L.g * ((size_t)(j - 1 + L.g) + (size_t)(L.Nz + L.g) * k); }
 static inline size_t hz(const Level& L, int i, int n, int k) { return (size_t)(i - 1 + L.g) + (size_t)(L.Nr + L.g) * ((size_t)n + (size_t)L.g * k); }
 
-void currentgrid(Sim& S, Level& L) { L.time = S.t[L.level]; }
+void currentgrid(Sim& S, Level& L) { L.time = S.t[L.gid]; }
 
 // ---------------------------------------------------------------------------
 // generated per-array routines
@@ -165,14 +224,16 @@ void symmetries_z(Sim& S, Level& L) {
 }
 
 // ---------------------------------------------------------------------------
-// interp.f90:2-270 -- value of one grid function of (box 0, level) at (r0,z0)
+// interp.f90:2-270 -- value of one grid function of grid ``gid`` (a box and
+// level) at (r0,z0)
 // ---------------------------------------------------------------------------
-double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
-    Level& L = S.L[level];
+double interp(Sim& S, int gid, const Arr& var, double r0, double z0) {
+    Level& L = S.L[gid];
     const int g = L.g;
+    const int level = L.level;
     const double small = 1.0e-10;
-    const double rmin = S.rminl[level] - small, rmax = S.rmaxl[level];
-    const double zmin = S.zminl[level] - small, zmax = S.zmaxl[level];
+    const double rmin = S.rminl[gid] - small, rmax = S.rmaxl[gid];
+    const double zmin = S.zminl[gid] - small, zmax = S.zmaxl[gid];
     if (r0 < rmin || r0 > rmax || z0 < zmin || z0 > zmax)
         throw std::runtime_error("interp: interpolating point is outside the local grid");
     Arr& r = L.a("r"); Arr& z = L.a("z");
@@ -181,8 +242,8 @@ double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
     const int j0 = (int)((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
     const double deltaz = z0 - z(0, j0);
     if (deltar == 0.0 && deltaz == 0.0) return var(i0, j0);
-    const bool forcelinear = ((S.rmaxl[level] - r0) < S.drl[level]) || ((S.zmaxl[level] - z0) < S.dzl[level])
-        || ((r0 - S.rminl[level]) < S.drl[level]) || ((z0 - S.zminl[level]) < S.dzl[level]);
+    const bool forcelinear = ((S.rmaxl[gid] - r0) < S.drl[level]) || ((S.zmaxl[gid] - z0) < S.dzl[level])
+        || ((r0 - S.rminl[gid]) < S.drl[level]) || ((z0 - S.zminl[gid]) < S.dzl[level]);
     double fa[4][4];
     if (forcelinear) {
         for (int i = 0; i <= 1; ++i)
@@ -215,27 +276,30 @@ double interp(Sim& S, int level, const Arr& var, double r0, double z0) {
 }
 
 // ---------------------------------------------------------------------------
-// finebound.f90:2-407 (all=.true.) with the generated bound_interp.inc
+// finebound.f90:2-407 (all=.true.) with the generated bound_interp.inc, for
+// grid ``gid`` from its parent (box 0's level 0 for level 1)
 // ---------------------------------------------------------------------------
-void finebound(Sim& S, int level, double dtw) {
-    Level& F = S.L[level];
+void finebound(Sim& S, int gid, double dtw) {
+    Level& F = S.L[gid];
     const int g = F.g;
-    const int bbox_level = level - 1;
-    const double tp = S.t[level - 1], t0 = S.t[level], tm1 = S.t1[level];
+    const int level = F.level;
+    const int pg = F.parent;
+    const double tp = S.t[pg], t0 = S.t[gid], tm1 = S.t1[gid];
     const double tl = t0 + dtw;
     const int imax = (tp == tl) ? g + 2 : g - 1;
     const int jmax = imax;
     const int border = (tm1 == 0.0) ? 1 : 2;
     Arr& r = F.a("r"); Arr& z = F.a("z");
-    Level& Cl = S.L[bbox_level];
+    Level& Cl = S.L[pg];
 
-    // one strip point: all evolving variables (bound_interp.inc)
+    // one strip point: all evolving variables (bound_interp.inc); bd is the
+    // strip: 'R' (rR), 'L' (rL), 'z' (zR), 'l' (zL)
     auto point = [&](double r0, double z0, int m, int n, char bd) {
         const int ii = (int)nint_((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
         const int jj = (int)nint_((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
         const bool flag1 = (ii >= 1 - g) && (ii <= F.Nr) && (jj >= 1 - g) && (jj <= F.Nz);
         for (const EvolvedVar& e : S.evolved) {
-            const double aux2 = interp(S, bbox_level, Cl.a(e.name), r0, z0);
+            const double aux2 = interp(S, pg, Cl.a(e.name), r0, z0);
             if (!flag1) continue;
             Arr& v = F.a(e.name);
             if (border == 1) {
@@ -245,9 +309,9 @@ void finebound(Sim& S, int level, double dtw) {
                 // (m or n > ghost-1, reachable only when tp == tl) carries a
                 // zero weight in the reference and contributes nothing here
                 double h0 = 0.0, h1 = 0.0;
-                if (bd == 'r') {
+                if (bd == 'R' || bd == 'L') {
                     if (m <= g - 1) {
-                        const auto& H = F.hist[e.name + "_rR"];
+                        const auto& H = F.hist[e.name + (bd == 'R' ? "_rR" : "_rL")];
                         h0 = H[hr(F, m, jj, 0)]; h1 = H[hr(F, m, jj, 1)];
                     }
                 } else {
@@ -265,63 +329,89 @@ void finebound(Sim& S, int level, double dtw) {
     // upper r boundary (finebound.f90:153-187)
     for (int m = 0; m <= imax; ++m)
         for (int n = 0; n <= F.Nz + g - 1; ++n) {
-            const double r0 = S.rmaxl[level] - (double)m * S.drl[level];
-            const double z0 = S.zminl[level] + (double)n * S.dzl[level];
-            point(r0, z0, m, n, 'r');
+            const double r0 = S.rmaxl[gid] - (double)m * S.drl[level];
+            const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
+            point(r0, z0, m, n, 'R');
         }
+    // lower r boundary of a box off the axis (finebound.f90:246-285)
+    if (F.box > 0 && S.rbox[F.box] != 0.0)
+        for (int m = 0; m <= imax; ++m)
+            for (int n = 0; n <= F.Nz + g - 1; ++n) {
+                const double r0 = S.rminl[gid] + (double)m * S.drl[level];
+                const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
+                point(r0, z0, m, n, 'L');
+            }
     // upper z boundary (finebound.f90:296-316)
     for (int n = 0; n <= jmax; ++n)
         for (int m = 0; m <= F.Nr + g - 1; ++m) {
-            const double r0 = S.rminl[level] + (double)m * S.drl[level];
-            const double z0 = S.zmaxl[level] - (double)n * S.dzl[level];
+            const double r0 = S.rminl[gid] + (double)m * S.drl[level];
+            const double z0 = S.zmaxl[gid] - (double)n * S.dzl[level];
             point(r0, z0, m, n, 'z');
         }
-    // lower z boundary without equatorial symmetry (finebound.f90:351-397)
-    if (!S.P.eqsym)
+    // lower z boundary without equatorial symmetry or off the equator
+    // (finebound.f90:351-397)
+    if (!S.P.eqsym || (F.box > 0 && S.zbox[F.box] != 0.0))
         for (int n = 0; n <= jmax; ++n)
             for (int m = 0; m <= F.Nr + g - 1; ++m) {
-                const double r0 = S.rminl[level] + (double)m * S.drl[level];
-                const double z0 = S.zminl[level] + (double)n * S.dzl[level];
+                const double r0 = S.rminl[gid] + (double)m * S.drl[level];
+                const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
                 point(r0, z0, m, n, 'l');
             }
 }
 
-// restrict.f90:2-169 with restrict_interp.inc
-void restrict_(Sim& S, int level) {
-    Level& F = S.L[level];
-    Level& Cl = S.L[level - 1];
+// restrict.f90:2-169 with restrict_interp.inc: grid ``gid`` into its parent
+void restrict_(Sim& S, int gid) {
+    Level& F = S.L[gid];
+    const int pg = F.parent;
+    Level& Cl = S.L[pg];
     const int g = F.g;
+    const int level = F.level;
     const double deltar = (double)(2 * g) * S.drl[level] + 1.0e-10;
     const double deltaz = (double)(2 * g) * S.dzl[level] + 1.0e-10;
     Arr& rc = Cl.a("r"); Arr& zc = Cl.a("z");
     for (int n = 0; n <= Cl.Nz + g - 1; ++n)
         for (int m = 0; m <= Cl.Nr + g - 1; ++m) {
-            const double r0 = S.rminl[level - 1] + (double)m * S.drl[level - 1];
-            const double z0 = S.zminl[level - 1] + (double)n * S.dzl[level - 1];
-            const double rmin = (S.rminl[level] < 0.0) ? 0.0 : S.rminl[level] + deltar;
-            const double zmin = (S.P.eqsym && S.zminl[level] < 0.0) ? 0.0 : S.zminl[level] + deltaz;
-            const double rmax = S.rmaxl[level] - deltar;
-            const double zmax = S.zmaxl[level] - deltaz;
+            const double r0 = S.rminl[pg] + (double)m * S.drl[level - 1];
+            const double z0 = S.zminl[pg] + (double)n * S.dzl[level - 1];
+            const double rmin = (S.rminl[gid] < 0.0) ? 0.0 : S.rminl[gid] + deltar;
+            const double zmin = (S.P.eqsym && S.zminl[gid] < 0.0) ? 0.0 : S.zminl[gid] + deltaz;
+            const double rmax = S.rmaxl[gid] - deltar;
+            const double zmax = S.zmaxl[gid] - deltaz;
             if (r0 > rmin && r0 < rmax && z0 > zmin && z0 < zmax) {
                 const int i = (int)nint_((r0 - rc(1 - g, 0)) / S.drl[level - 1]) + 1 - g;
                 const int j = (int)nint_((z0 - zc(0, 1 - g)) / S.dzl[level - 1]) + 1 - g;
                 const bool flag1 = (i >= 1 - g) && (i <= Cl.Nr) && (j >= 1 - g) && (j <= Cl.Nz);
                 for (const EvolvedVar& e : S.evolved) {
-                    const double aux2 = interp(S, level, F.a(e.name), r0, z0);
+                    const double aux2 = interp(S, gid, F.a(e.name), r0, z0);
                     if (flag1) Cl.a(e.name)(i, j) = aux2;
                 }
             }
         }
 }
 
+// syncboxes.f90:48-52: grids of two boxes on one level that overlap copy
+// each other's data there; the copy is not restated, so overlapping boxes
+// are refused
+void check_no_intersection(Sim& S, int level) {
+    for (Level& a : S.L)
+        for (Level& b : S.L) {
+            if (a.level != level || b.level != level || a.box >= b.box) continue;
+            const int p = a.gid, q = b.gid;
+            const bool apart = S.rmaxl[p] < S.rminl[q] || S.rmaxl[q] < S.rminl[p] || S.zmaxl[p] < S.zminl[q] ||
+                               S.zmaxl[q] < S.zminl[p];
+            if (!apart) throw std::runtime_error("oracle: refinement boxes intersect (syncboxes is not restated)");
+        }
+}
+
 // ---------------------------------------------------------------------------
-// onestep.f90:2-522 (box 0 only; Nb = 0 so syncboxes never runs)
+// onestep.f90:2-522: every box that has this level, one step each, then
+// the finer levels twice, then the restriction of each box into its parent
 // ---------------------------------------------------------------------------
-static void onestep(Sim& S, int level) {
+static void step_grid(Sim& S, Level& L) {
     const ollin_params& P = S.P;
     const bool rk4 = P.integrator == OLLIN_INTEGRATOR_RK4;
     const bool matter = P.mattertype != OLLIN_MATTER_VACUUM;
-    Level& L = S.L[level];
+    const int gid = L.gid;
     currentgrid(S, L);
     saveold(S, L);
     const int niter = rk4 ? 4 : P.icniter;
@@ -342,35 +432,43 @@ static void onestep(Sim& S, int level) {
         sources_lapse(S, L);
         if (P.shift != OLLIN_SHIFT_NONE) sources_shift(S, L);
         if (matter) sources_scalar(S, L);
-        if (level == 0 && P.boundtype == OLLIN_BOUND_RADIATIVE) radiative_geometry(S, L);
+        if (L.level == 0 && P.boundtype == OLLIN_BOUND_RADIATIVE) radiative_geometry(S, L);
         if (rk4) accumulate(S, L, iter, niter, weight);
         update(S, L, dtw);
-        if (level > 0) finebound(S, level, dtw);
+        if (L.level > 0) finebound(S, gid, dtw);
         if (L.ownaxis) symmetries_r(S, L);
         if (L.eqsym && L.ownequator) symmetries_z(S, L);
         auxiliary(S, L);
     }
-    S.t2[level] = S.t1[level];
-    S.t1[level] = S.t[level];
-    S.s[level] = S.s[level] + 1;
-    S.t[level] = S.t[level] + dt;
+    S.t2[gid] = S.t1[gid];
+    S.t1[gid] = S.t[gid];
+    S.s[gid] = S.s[gid] + 1;
+    S.t[gid] = S.t[gid] + dt;
     S.point_updates += (double)L.Nr * (double)(L.eqsym ? L.Nz : L.Nz + L.g);
+}
+
+static void onestep(Sim& S, int level) {
+    // boxes in order 0..Nb (level 0 exists on box 0 only)
+    for (Level& L : S.L)
+        if (L.level == level) step_grid(S, L);
     if (level < S.Nlmax) {
         onestep(S, level + 1);
         onestep(S, level + 1);
     }
-    if (level > 0 && S.s[level] % 2 == 0) {
-        restrict_(S, level);
-        Level& Cl = S.L[level - 1];
-        currentgrid(S, Cl);
-        if (Cl.ownaxis) symmetries_r(S, Cl);
-        if (Cl.eqsym && Cl.ownequator) symmetries_z(S, Cl);
-        auxiliary(S, Cl);
+    if (level > 0) check_no_intersection(S, level);
+    if (level > 0) {
+        for (Level& F : S.L) {
+            if (F.level != level || S.s[F.gid] % 2 != 0) continue;
+            restrict_(S, F.gid);
+            Level& Cl = S.L[F.parent];
+            currentgrid(S, Cl);
+            if (Cl.ownaxis) symmetries_r(S, Cl);
+            if (Cl.eqsym && Cl.ownequator) symmetries_z(S, Cl);
+            auxiliary(S, Cl);
+        }
     }
 }
 
-// ---------------------------------------------------------------------------
-// initial.f90:59-218, 528-645 for minkowski / schwarzschild / Brill-Lindquist
 // ---------------------------------------------------------------------------
 static void initial(Sim& S) {
     const ollin_params& P = S.P;
@@ -458,7 +556,7 @@ static void initial(Sim& S) {
     }
 }
 
-// evolve.f90:128-195 (box 0, no maximal slicing); ``initial`` runs first
+// evolve.f90:128-219 (no maximal slicing); ``initial`` runs first
 static void initialize(Sim& S) {
     for (Level& L : S.L) {
         currentgrid(S, L);
@@ -475,6 +573,7 @@ static void initialize(Sim& S) {
             for (size_t q = 0; q < b.v.size(); ++q) { b.v[q] = S.P.drivercsi * dr_.v[q]; bz.v[q] = S.P.drivercsi * dz_.v[q]; }
         }
     }
+    for (int level = 1; level <= S.Nlmax; ++level) check_no_intersection(S, level);  // :211-219
 }
 
 // save0Ddata.f90:221-288 and the origin value at :370-374
@@ -492,7 +591,7 @@ static void norms(Sim& S, int level, const Arr& v, double out[5]) {
             nm2 = nm2 + p2(aux);
         }
     out[0] = vmax; out[1] = vmin; out[2] = nm1; out[3] = std::sqrt(nm2 / NN);
-    out[4] = interp(S, level, v, 0.0, 0.0);
+    out[4] = (L.box == 0) ? interp(S, level, v, 0.0, 0.0) : 0.0;  // origin data for box 0 only (:372-374)
 }
 
 }  // namespace oracle
@@ -554,6 +653,13 @@ int ollin_oracle_dims(const ollin_oracle* o, int level, int* nr, int* nz, int* g
 }
 
 double ollin_oracle_time(const ollin_oracle* o, int level) { return o->S.t[level]; }
+
+int ollin_oracle_grid(const ollin_oracle* o, int gid, int* box, int* level) {
+    if (gid < 0 || gid >= (int)o->S.L.size()) return 1;
+    *box = o->S.L[gid].box;
+    *level = o->S.L[gid].level;
+    return 0;
+}
 
 // Copy grid function ``name`` of ``level`` into ``a`` (column-major,
 // leading dimension ld_r, element (1-ghost,1-ghost) first).

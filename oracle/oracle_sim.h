@@ -12,6 +12,8 @@ namespace oracle {
 
 struct Level {
     int level = 0, g = 3, Nr = 0, Nz = 0;
+    int box = 0, parent = -1;  // refinement box; grid of the next coarser level (finebound/restrict)
+    int gid = 0;               // index in Sim::L
     double dr = 0, dz = 0, dt = 0, time = 0;
     bool ownaxis = true, ownequator = true, eqsym = true;
     std::unordered_map<std::string, Arr> arrs;
@@ -29,9 +31,14 @@ struct EvolvedVar {
     int symr, symz;
 };
 
+// The grids are box 0's levels 0..Nl0 (grid index = level), then levels
+// 1..Nl(b) of boxes b = 1..Nb; t, t1, t2, s and the extents rminl.. are per
+// grid, dtl, drl, dzl per level.
 struct Sim {
     ollin_params P;
-    int g = 3, Nlmax = 0;
+    int g = 3, Nlmax = 0, Nb = 0;
+    int Nl[4] = {0, 0, 0, 0};
+    double rbox[4] = {0, 0, 0, 0}, zbox[4] = {0, 0, 0, 0};
     std::vector<Level> L;
     std::vector<double> t, t1, t2, dtl, drl, dzl, rminl, rmaxl, zminl, zmaxl;
     std::vector<long> s;

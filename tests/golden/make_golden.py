@@ -68,6 +68,17 @@ CASES = {
     "ell_sor_2lev": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
                          ilapse="one", mattertype="scalar", scalar_a0=0.05, ell_solver="sor",
                          scalardiss=0.02, _steps=[0], _elliptic=True),
+    # refinement boxes (Nb > 0) that do not overlap, box 0 the base grid
+    # alone: box 1 on the axis above the equator (its lower z edge is a
+    # refinement boundary, finebound.f90:361-397) with two levels, box 2 a
+    # ring on the equator (lower r edge, finebound.f90:246-285)
+    "box_two": dict(BASE, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=2, Nl1=2, Nrbox1=12,
+                    Nzbox1=12, zbox1=6.0, Nl2=1, Nrbox2=10, Nzbox2=10, rbox2=8.0, _steps=[0, 1, 2]),
+    # a ring off the equator (both lower edges and their corner) with the
+    # Gamma-driver shift
+    "box_ring_shift": dict(BASE, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=10,
+                           Nzbox1=10, rbox1=5.0, zbox1=5.0, shift="Gammadriver2", drivercsi=0.75,
+                           drivereta=2.0, _steps=[0, 1, 2]),
     # maximal slicing (maximalslicing.f90, physical Laplacian).  Time-symmetric
     # vacuum data have K_ij = 0 and a maximal lapse of exactly 1, and so does
     # a static massless scalar field (rho + S = 0), so the cases solve where
@@ -168,8 +179,8 @@ def run_case(refdir, name, cfg):
                 sim.analysis(lev)
                 for nm in DERIVED:
                     out["s%d_L%d_%s" % (done, lev, nm)] = sim.field(lev, nm)
-            out["s%d_L%d_time" % (done, lev)] = np.array(float(sim.M.t[0, lev]))
-    meta = dict(cfg, steps=steps, fields=names)
+            out["s%d_L%d_time" % (done, lev)] = np.array(sim.time(lev))
+    meta = dict(cfg, steps=steps, fields=names, grids=[list(sim.box_level(k)) for k in sim.levels()])
     out["meta"] = np.array(json.dumps(meta))
     return out
 

@@ -163,7 +163,7 @@ class RefSim:
         prog.load(texts, extra_functions=("interp",))
         prog.define("currentgrid", self._currentgrid)
         prog.define("syncall", lambda: None)
-        prog.define("syncboxes", self._unsupported("syncboxes"))
+        prog.define("syncboxes", self._syncboxes)
         prog.define("save1dvariable", lambda *a: None)
         prog.define("save2dvariable", lambda *a: None)
         prog.define("sync", lambda *a: None)
@@ -192,12 +192,13 @@ class RefSim:
         if M.ghost == 0:
             s("ghost", 2 if M.order == "two" else 3)
         g = M.ghost
-        if M.nb != 0:
-            raise NotImplementedError("golden vectors cover box 0 only")
+        nb = int(M.nb)
+        if nb < 0 or nb > 3:
+            raise ValueError("The number of refinement boxes must be between 0 and 3")
         nl = _int_array((0,), (3,))
         nl[0], nl[1], nl[2], nl[3] = M.nl0, M.nl1, M.nl2, M.nl3
         s("nl", nl)
-        s("nlmax", int(nl.max()))
+        s("nlmax", int(max(nl[b] for b in range(nb + 1))))
         L = M.nlmax
         s("dt0", np.float64(M.dtfac * min(M.dr0, M.dz0)))
         drl = fs.falloc((0,), (L,))
@@ -212,68 +213,114 @@ class RefSim:
         s("dtl", dtl)
         if not M.eqsym and (M.nztotal + g) % 2 == 0:
             s("nztotal", M.nztotal + 1)
+        # box sizes and centres, setupboxes.f90:143-206
         nrbox = _int_array((0,), (3,), 1)
         nzbox = _int_array((0,), (3,), 1)
         nrbox[0] = M.nrtotal
         nzbox[0] = M.nztotal
-        s("nrbox", nrbox)
-        s("nzbox", nzbox)
         rbox = fs.falloc((0,), (3,))
         zbox = fs.falloc((0,), (3,))
+        for b in range(1, 4):
+            nrbox[b] = getattr(M, "nrbox%d" % b)
+            nzbox[b] = getattr(M, "nzbox%d" % b)
+            rbox[b] = np.float64(getattr(M, "rbox%d" % b))
+            zbox[b] = np.float64(getattr(M, "zbox%d" % b))
+        for b in range(1, nb + 1):
+            if rbox[b] != 0.0:
+                rbox[b] = (np.float64(int(rbox[b] / drl[1])) + 0.5) * drl[1]
+            if zbox[b] != 0.0:
+                if M.eqsym:
+                    zbox[b] = (np.float64(int(zbox[b] / dzl[1])) + 0.5) * dzl[1]
+                else:
+                    zbox[b] = np.float64(int(zbox[b] / dzl[1])) * dzl[1]
+        s("nrbox", nrbox)
+        s("nzbox", nzbox)
         s("rbox", rbox)
         s("zbox", zbox)
         for nm in ("s",):
-            s(nm, _int_array((0, 0), (0, L)))
+            s(nm, _int_array((0, 0), (nb, L)))
         for nm in ("t", "t1", "t2", "rminl", "rmaxl", "zminl", "zmaxl"):
-            s(nm, fs.falloc((0, 0), (0, L)))
-        nrl = _int_array((0, 0), (0, 0))
-        nzl = _int_array((0, 0), (0, 0))
-        nrl[0, 0] = M.nrtotal
-        nzl[0, 0] = M.nztotal
+            s(nm, fs.falloc((0, 0), (nb, L)))
+        nrl = _int_array((0, 0), (nb, 0))
+        nzl = _int_array((0, 0), (nb, 0))
+        for b in range(nb + 1):
+            nrl[b, 0] = nrbox[b]
+            nzl[b, 0] = nzbox[b]
         s("nrl", nrl)
         s("nzl", nzl)
-        s("nrmaxl", _int_array((0,), (0,), M.nrtotal))
-        s("nzmaxl", _int_array((0,), (0,), M.nztotal))
-        s("nminl_r", _int_array((0, 0), (0, 0)))
-        s("nminl_z", _int_array((0, 0), (0, 0)))
-        axis = _int_array((0, 0), (0, 0), 1)
-        eqz = _int_array((0, 0), (0, 0), 1 if M.eqsym else -1)
-        origin = _int_array((0, 0), (0, 0), 1 if M.eqsym else -1)
-        if not M.eqsym:
-            # main.f90:405-424: equator ownership from the z-coordinate of the
-            # grid rows (only row j with z in {0, dz0/2} counts)
-            for j in range(1, M.nztotal - g + 1):
-                aux = (float(j) - 0.5 * float(M.nztotal - g + 1)) * M.dz0
-                if aux == 0.0 or aux == 0.5 * M.dz0:
-                    eqz[0, 0] = j
-                    origin[0, 0] = j
-                    break
+        nrmaxl = _int_array((0,), (nb,))
+        nzmaxl = _int_array((0,), (nb,))
+        for b in range(nb + 1):
+            nrmaxl[b] = nrbox[b]
+            nzmaxl[b] = nzbox[b]
+        s("nrmaxl", nrmaxl)
+        s("nzmaxl", nzmaxl)
+        s("nminl_r", _int_array((0, 0), (nb, 0)))
+        s("nminl_z", _int_array((0, 0), (nb, 0)))
+        # main.f90:380-460: the axis belongs to boxes with rbox = 0, the
+        # equator to boxes with zbox = 0
+        axis = _int_array((0, 0), (nb, 0), -1)
+        eqz = _int_array((0, 0), (nb, 0), -1)
+        origin = _int_array((0, 0), (nb, 0), -1)
+        for b in range(nb + 1):
+            if rbox[b] == 0.0:
+                axis[b, 0] = 1
+            if zbox[b] == 0.0:
+                if M.eqsym:
+                    eqz[b, 0] = 1
+                    origin[b, 0] = 1
+                else:
+                    for j in range(1, nzbox[b] - g + 1):
+                        aux = (float(j) - 0.5 * float(nzbox[b] - g + 1)) * M.dz0
+                        if aux == 0.0 or aux == 0.5 * M.dz0:
+                            eqz[b, 0] = j
+                            origin[b, 0] = j
+                            break
         s("axis", axis)
         s("eqz", eqz)
         s("origin", origin)
-        grid = _obj_array((0, 0), (0, L))
-        for lev in range(L + 1):
-            grid[0, lev] = GridFuncs(g, M.nrtotal, M.nztotal)
+        grid = _obj_array((0, 0), (nb, L))
+        self.grids = []
+        for b in range(nb + 1):
+            for lev in range(min(1, b), int(nl[b]) + 1):
+                grid[b, lev] = GridFuncs(g, int(nrbox[b]), int(nzbox[b]))
+                self.grids.append((b, lev))
+        # grid order of the library and the oracle: box 0, then boxes 1..Nb
+        self.grids.sort(key=lambda bl: (bl[0] != 0, bl[0], bl[1]))
         s("grid", grid)
-        # coordinates (evolve.f90:42-97), single process, box 0
-        for lev in range(L + 1):
-            gf = grid[0, lev]
+        # coordinates (evolve.f90:42-97), single process
+        for b, lev in self.grids:
+            gf = grid[b, lev]
             dr, dz = drl[lev], dzl[lev]
             r = gf.r
             z = gf.z
-            for i in range(1 - g, M.nrtotal + 1):
-                fs.fset(r, (i, slice(None, None)), (np.float64(0 + i) - 0.5) * dr)
-            for j in range(1 - g, M.nztotal + 1):
-                if M.eqsym:
+            nrb, nzb = int(nrbox[b]), int(nzbox[b])
+            for i in range(1 - g, nrb + 1):
+                if rbox[b] == 0.0:
+                    v = (np.float64(0 + i) - 0.5) * dr
+                else:
+                    v = rbox[b] + (np.float64(0 + i) - 0.5 * np.float64(nrb - g + 1)) * dr
+                fs.fset(r, (i, slice(None, None)), v)
+            for j in range(1 - g, nzb + 1):
+                if M.eqsym and zbox[b] == 0.0:
                     v = (np.float64(0 + j) - 0.5) * dz
                 else:
-                    v = 0.0 + (np.float64(0 + j) - 0.5 * np.float64(M.nztotal - g + 1)) * dz
+                    v = zbox[b] + (np.float64(0 + j) - 0.5 * np.float64(nzb - g + 1)) * dz
                 fs.fset(z, (slice(None, None), j), v)
             gf.rr[...] = np.sqrt(r ** 2 + z ** 2)
-            self.M.rminl[0, lev] = fs.fget(r, (1 - g, 0))
-            self.M.rmaxl[0, lev] = fs.fget(r, (M.nrtotal, 0))
-            self.M.zminl[0, lev] = fs.fget(z, (0, 1 - g))
-            self.M.zmaxl[0, lev] = fs.fget(z, (0, M.nztotal))
+            self.M.rminl[b, lev] = fs.fget(r, (1 - g, 0))
+            self.M.rmaxl[b, lev] = fs.fget(r, (nrb, 0))
+            self.M.zminl[b, lev] = fs.fget(z, (0, 1 - g))
+            self.M.zmaxl[b, lev] = fs.fget(z, (0, nzb))
+
+    def _syncboxes(self, b1, b2, level, all_):
+        """syncboxes.f90:48-52: boxes that do not overlap on a level do
+        nothing; the overlap copy is outside the golden-vector scope."""
+        M = self.M
+        if (M.rmaxl[b1, level] < M.rminl[b2, level] or M.rmaxl[b2, level] < M.rminl[b1, level] or
+                M.zmaxl[b1, level] < M.zminl[b2, level] or M.zmaxl[b2, level] < M.zminl[b1, level]):
+            return
+        raise NotImplementedError("intersecting refinement boxes are outside the golden-vector scope")
 
     def _currentgrid(self, box, level, localgrid):
         M = self.M
@@ -295,19 +342,29 @@ class RefSim:
     # driver (evolve.f90:104-219 and the main loop :357-381)
     # ------------------------------------------------------------------
     def levels(self):
-        return range(self.M.nlmax + 1)
+        """Grid indices: box 0's levels, then the levels of boxes 1..Nb."""
+        return range(len(self.grids))
 
-    def use(self, level):
-        self._currentgrid(0, level, self.M.grid[0, level])
+    def box_level(self, gid):
+        return self.grids[gid]
+
+    def use(self, gid):
+        b, lev = self.grids[gid]
+        self._currentgrid(b, lev, self.M.grid[b, lev])
+
+    def time(self, gid):
+        b, lev = self.grids[gid]
+        return float(self.M.t[b, lev])
 
     def initial(self):
         """call initial (evolve.f90:124)."""
         M, F = self.M, self.prog.F
-        object.__setattr__(M, "s", _int_array((0, 0), (0, M.nlmax)))
+        object.__setattr__(M, "s", _int_array((0, 0), (int(M.nb), M.nlmax)))
         F.initial()
 
-    def set_field(self, level, name, values):
-        a = getattr(self.M.grid[0, level], fs.pyname(name.lower()))
+    def set_field(self, gid, name, values):
+        b, lev = self.grids[gid]
+        a = getattr(self.M.grid[b, lev], fs.pyname(name.lower()))
         a.view(np.ndarray)[...] = values
 
     def initialize(self):
@@ -327,6 +384,12 @@ class RefSim:
                 self.use(lev)
                 M.dtbeta_r[...] = M.drivercsi * M.delta_r
                 M.dtbeta_z[...] = M.drivercsi * M.delta_z
+        # evolve.f90:211-219: boxes that overlap on a level synchronise
+        for level in range(1, int(M.nlmax) + 1):
+            for b1 in range(int(M.nb) + 1):
+                for b2 in range(int(M.nb) + 1):
+                    if b1 != b2 and M.nl[b1] >= level and M.nl[b2] >= level:
+                        self._syncboxes(b1, b2, level, True)
         # evolve.f90:228-230; no analysis has run, so va_rp/va_zp are zero
         if M.slicing == "maximal" or M.ilapse == "maximal" or M.maximalevery != 0:
             F.maximalslicing()
@@ -340,9 +403,11 @@ class RefSim:
 
     def field(self, level, name):
         """Interior+ghost copy of a grid array (Fortran (i,j) -> [i+g-1, j+g-1])."""
-        a = getattr(self.M.grid[0, level], fs.pyname(name.lower()))
+        b, lev = self.grids[level]
+        a = getattr(self.M.grid[b, lev], fs.pyname(name.lower()))
         return np.array(a.view(np.ndarray), copy=True)
 
-    def analysis(self, level):
-        self.use(level)
-        self.prog.F.constraints(0, level)
+    def analysis(self, gid):
+        self.use(gid)
+        b, lev = self.grids[gid]
+        self.prog.F.constraints(b, lev)

@@ -42,6 +42,7 @@ def lib():
         L.ollin_oracle_aux.argtypes = [vp, ctypes.c_int]
         L.ollin_oracle_constraints.argtypes = [vp, ctypes.c_int]
         L.ollin_oracle_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
+        L.ollin_oracle_grid.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.ollin_oracle_norms.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p]
         L.ollin_oracle_point_updates.argtypes = [vp]
         L.ollin_oracle_point_updates.restype = ctypes.c_double
@@ -103,6 +104,13 @@ class Oracle:
         nr, nz, g = self.dims(level)
         a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).T)
         self._check(self.L.ollin_oracle_set(self.h, level, name.encode(), a.ctypes.data, nr + g))
+
+    def grid(self, gid):
+        """(box, level) of grid ``gid``."""
+        b, l = ctypes.c_int(), ctypes.c_int()
+        if self.L.ollin_oracle_grid(self.h, gid, ctypes.byref(b), ctypes.byref(l)):
+            raise RuntimeError("oracle: bad grid %d" % gid)
+        return b.value, l.value
 
     def aux(self, level):
         self._check(self.L.ollin_oracle_aux(self.h, level))

@@ -11,7 +11,7 @@ from oracle_bind import Oracle, ell_stats
 from parity_util import params, scalar_pulse
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["c1_small", "c2_small", "icn_harmonic", "scalar_shift", "noeqsym_shift"]
+CASES = ["c1_small", "c2_small", "icn_harmonic", "scalar_shift", "noeqsym_shift", "box_two", "box_ring_shift"]
 
 # The oracle restates the reference statement by statement; the remaining
 # differences come from libm (exp/log/pow) last-bit differences amplified by
@@ -26,7 +26,7 @@ def load(name):
 
 
 def cfg_of(meta):
-    skip = {"steps", "fields"}
+    skip = {"steps", "fields", "grids"}
     cfg = {k: v for k, v in meta.items() if k not in skip}
     cfg["eqsym"] = 1 if cfg.get("eqsym") else 0
     return cfg
@@ -45,6 +45,8 @@ def test_oracle_matches_reference_fortran(name):
             for nm, v in zip(["scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"], scalar_pulse(r, z)):
                 o.set(lev, nm, v)
     o.initialize()
+    if "grids" in meta:  # the grid order (box, level) is the reference's
+        assert [list(o.grid(k)) for k in o.levels()] == meta["grids"]
     done = 0
     worst = 0.0
     for target in meta["steps"]:
@@ -53,10 +55,16 @@ def test_oracle_matches_reference_fortran(name):
             done += 1
         for lev in o.levels():
             assert o.time(lev) == float(d["s%d_L%d_time" % (done, lev)])
+            level = meta["grids"][lev][1] if "grids" in meta else lev
+            h2 = (cfg["dr0"] / 2 ** level) * (cfg["dz0"] / 2 ** level)
             for nm in meta["fields"]:
                 ref = d["s%d_L%d_%s" % (done, lev, nm)]
                 got = o.get(lev, nm)
                 scale = max(np.abs(ref).max(), 1e-300)
+                if nm in ("lambda", "Alambda"):
+                    # (A - H)/r^2 and (KTA - KTH)/r^2: near zero far from the
+                    # puncture, with the fields' rounding divided by r^2 ~ dr^2
+                    scale = max(scale, 1e-3 / h2)
                 err = np.abs(got - ref).max() / scale
                 worst = max(worst, err)
                 assert err <= TOL, "%s step %d level %d %s: rel %.3e" % (name, done, lev, nm, err)
@@ -70,7 +78,12 @@ def test_oracle_matches_reference_fortran(name):
                     # mom_r/mom_z as computed, the comparison covers i,j >= 1
                     g = 3
                     ref_i, got_i = ref[g:, g:], got[g:, g:]
-                    scale = max(np.abs(ref_i).max(), 1e-300)
+                    # curvature quantities are sums of second differences:
+                    # far from the puncture (refinement boxes off the
+                    # centre) they are small, while the rounding of the
+                    # fields (libm last bits) enters divided by dr dz, so
+                    # the error is also measured against 1e-3/(dr dz)
+                    scale = max(np.abs(ref_i).max(), 1e-3 / h2)
                     err = np.abs(got_i - ref_i).max() / scale
                     assert err <= TOL, "%s step %d level %d %s: rel %.3e" % (name, done, lev, nm, err)
     print("%s: worst relative difference %.2e" % (name, worst))
