@@ -1675,6 +1675,10 @@ void ollin_params_default(ollin_params* p) {
     p->scalarpulse_type = OLLIN_PULSE_SHELL; p->brilltype = 0;
     p->scalar_a0 = 0.0; p->scalar_r0 = 0.0; p->scalar_z0 = 0.0; p->scalar_sr0 = 1.0; p->scalar_sz0 = 1.0;
     p->brill_a0 = 0.0; p->brill_sr0 = 1.0; p->brill_sz0 = 1.0;
+    p->nb = 0;  // param.f90:114-139
+    for (int b = 0; b < 3; ++b) {
+        p->nl[b] = 0; p->nrbox[b] = 1; p->nzbox[b] = 1; p->rbox[b] = 0.0; p->zbox[b] = 0.0;
+    }
 }
 
 const char* ollin_gpu_last_error(void) { return g_err.c_str(); }

@@ -39,7 +39,7 @@ def test_default_parameters_match_param_module():
     q = default_params()
     for f, _ in Params._fields_:
         a, b = getattr(p, f), getattr(q, f)
-        if f == "ft":
+        if f in ("ft", "nl", "nrbox", "nzbox", "rbox", "zbox"):
             a, b = list(a), list(b)
         assert a == b, f
     # a literal without a d-exponent in param.f90 is single precision
