@@ -171,12 +171,13 @@ enum ollin_field {
 
 /* One level's geometry (box 0): arrays are (1-ghost:nr, 1-ghost:nz). */
 typedef struct ollin_level_desc {
-    int    level;
+    int    level;                   /* refinement level of the grid */
     int    nr, nz, ghost;
     double dr, dz, dt;
     double rmin, rmax, zmin, zmax;  /* rminl/rmaxl/zminl/zmaxl incl. ghosts (evolve.f90:75-92) */
-    double time;                    /* t(0,level) */
-    int    steps;                   /* s(0,level) */
+    double time;                    /* t(box,level) */
+    int    steps;                   /* s(box,level) */
+    int    box;                     /* refinement box (appended) */
 } ollin_level_desc;
 
 typedef struct ollin_handle ollin_handle;
@@ -189,7 +190,12 @@ void ollin_params_default(ollin_params* p);
 int ollin_gpu_create(const ollin_params* p, ollin_handle** out);
 void ollin_gpu_destroy(ollin_handle* h);
 
-/* Level geometry and clocks. */
+/* Grid geometry and clocks.  The ``level`` argument of this and every other
+ * entry point is a grid index: box 0's levels 0..Nl0 first (so with Nb = 0
+ * it is the refinement level), then levels 1..Nl(b) of boxes b = 1..Nb, the
+ * order of the reference's ``do box=0,Nb; do level=min(1,box),Nl(box)``
+ * loops (e.g. src/base/evolve.f90:157-167).  ollin_gpu_num_levels counts
+ * the grids; ollin_level_desc gives each one's box and level. */
 int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out);
 int ollin_gpu_num_levels(const ollin_handle* h);
 

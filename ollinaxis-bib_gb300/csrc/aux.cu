@@ -49,11 +49,15 @@ __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ 
     a.aux[X_GLAM][o] = C * C - B * lam;
 }
 
-// DelDef_r/z from first derivatives of the inverse metric, interior points
-// (:1085-1094); at t = 0 they overwrite Delta_r/z (:1088-1094).
+// DelDef_r/z from first derivatives of the inverse metric (:1085-1094); at
+// t = 0 they overwrite Delta_r/z (:1088-1094).  Rows from jlo (the ghost rows
+// of a grid that does not own the equator take the one-sided z stencils of
+// derivatives.f90:179-212); on a grid off the axis the ghost columns as well,
+// where the reference's diff1r leaves the r derivatives unset: they are zero
+// here, as in an execution that starts them from zero.
 __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ AuxArgs a) {
     const LevelGeom& G = a.G;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = (G.axis ? 1 : 1 - G.g) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const long ld = G.ld;
@@ -61,9 +65,10 @@ __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ 
     const int kr = pclass(i, G.nr, G.g), kz = pclass(j, G.nz, G.g);
     const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
     const double r = G.rcol[i];
-    const double Dr_gA = d1(a.aux[X_GA] + o, 1, kr, cr1);
+    const bool rg = i < 1;  // a ghost column of a grid off the axis
+    const double Dr_gA = rg ? 0.0 : d1(a.aux[X_GA] + o, 1, kr, cr1);
     const double Dz_gB = d1(a.aux[X_GB] + o, ld, kz, cz1);
-    const double Dr_gC = d1(a.aux[X_GC] + o, 1, kr, cr1);
+    const double Dr_gC = rg ? 0.0 : d1(a.aux[X_GC] + o, 1, kr, cr1);
     const double Dz_gC = d1(a.aux[X_GC] + o, ld, kz, cz1);
     const double glam = a.aux[X_GLAM][o], gC = a.aux[X_GC][o];
     const double ddr = -Dr_gA - r * Dz_gC - r * glam;
@@ -90,7 +95,8 @@ void launch_aux_point(const AuxArgs& a, cudaStream_t s) {
 
 void launch_aux_deriv(const AuxArgs& a, cudaStream_t s) {
     dim3 blk(64, 4);
-    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
+    const int ni = a.G.axis ? a.G.nr : a.G.nr + a.G.g;
+    dim3 grd((ni + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
     aux_deriv_kernel<<<grd, blk, 0, s>>>(a);
 }
 

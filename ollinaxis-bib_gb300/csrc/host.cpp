@@ -43,6 +43,7 @@ constexpr int kSlots = 4;
 
 struct DLevel {
     int level = 0, nr = 0, nz = 0, g = 3, ld = 0, rows = 0;
+    int box = 0, parent = -1;  // refinement box; grid of the next coarser level
     size_t n = 0;  // elements per grid function
     double dr = 0, dz = 0, dt = 0;
     double* pool = nullptr;
@@ -70,7 +71,11 @@ struct DLevel {
 
 struct ollin_handle {
     ollin_params P{};
-    int g = 3, nlev = 0;
+    // grids: box 0's levels 0..Nl0 (index = level), then levels 1..Nl(b) of
+    // boxes b = 1..Nb; nlev counts the grids, t..zmaxl are per grid
+    int g = 3, nlev = 0, nb = 0, nlmax = 0;
+    int nl[4] = {0, 0, 0, 0}, nrbox[4] = {0, 0, 0, 0}, nzbox[4] = {0, 0, 0, 0};
+    double rbox[4] = {0, 0, 0, 0}, zbox[4] = {0, 0, 0, 0};
     std::vector<DLevel> L;
     std::vector<double> t, t1, t2, rminl, rmaxl, zminl, zmaxl;
     std::vector<long> s;
@@ -136,18 +141,81 @@ int check_params(const ollin_params& P) {
         P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
         return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave, sor or mixed)");
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
+    if (P.nb < 0 || P.nb > 3) return fail(OLLIN_EINVAL, "The number of refinement boxes must be between 0 and 3");
+    if (P.nb > 0 && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE))
+        return fail(OLLIN_EINVAL, "elliptic initial data on the device needs Nb = 0");
+    for (int b = 0; b < P.nb; ++b)
+        if (P.nl[b] < 0 || P.nl[b] >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl of a refinement box out of range");
     return OLLIN_OK;
 }
 
-int alloc_level(ollin_handle* h, DLevel& L, int level) {
+// setupboxes.f90:25-285: box sizes, centres aligned with the fine grids,
+// sanity checks; then the grid list of the handle
+int setup_boxes(ollin_handle* h) {
     const ollin_params& P = h->P;
     const int g = h->g;
-    L.level = level;
+    h->nb = P.nb;
+    h->nl[0] = P.nl0;
+    for (int b = 1; b <= 3; ++b) h->nl[b] = P.nl[b - 1];
+    h->nlmax = 0;
+    for (int b = 0; b <= h->nb; ++b) h->nlmax = std::max(h->nlmax, h->nl[b]);
+    if (h->nb > 0 && h->nlmax == 0) return fail(OLLIN_EINVAL, "If you choose Nb>0 you must also have Nl>0 for at least one box");
+    h->nrbox[0] = P.nrtotal;
+    h->nzbox[0] = P.nztotal;
+    if (!P.eqsym && (h->nzbox[0] + g) % 2 == 0) h->nzbox[0] += 1;  // setupboxes.f90:131-135
+    for (int b = 1; b <= 3; ++b) { h->nrbox[b] = P.nrbox[b - 1]; h->nzbox[b] = P.nzbox[b - 1]; }
+    for (int b = 0; b <= h->nb; ++b)
+        if (h->nrbox[b] < 2 + g || h->nzbox[b] < 2 + g)
+            return fail(OLLIN_EINVAL, "The values of (Nrtotal,Nztotal,Nrbox,Nzbox) should be greater than 2 plus the number of ghost zones");
+    const double d1r = P.dr0 / 2.0, d1z = P.dz0 / 2.0;  // drl(1), dzl(1)
+    h->rbox[0] = 0.0; h->zbox[0] = 0.0;
+    for (int b = 1; b <= 3; ++b) { h->rbox[b] = P.rbox[b - 1]; h->zbox[b] = P.zbox[b - 1]; }
+    for (int b = 1; b <= h->nb; ++b) {
+        if (h->rbox[b] != 0.0) h->rbox[b] = ((double)(long)(h->rbox[b] / d1r) + 0.5) * d1r;
+        if (h->zbox[b] != 0.0)
+            h->zbox[b] = P.eqsym ? ((double)(long)(h->zbox[b] / d1z) + 0.5) * d1z : (double)(long)(h->zbox[b] / d1z) * d1z;
+        const double rb = h->rbox[b], zb = h->zbox[b];
+        if (rb < 0.0) return fail(OLLIN_EINVAL, "rbox must be larger than or equal to 0 for all refinement boxes");
+        if (rb > 0.0 && rb - 0.5 * h->nrbox[b] * d1r <= 0.0) return fail(OLLIN_EINVAL, "Refinement box extends to negative values of r");
+        if (rb + 0.5 * h->nrbox[b] * d1r >= (h->nrbox[0] - g) * P.dr0)
+            return fail(OLLIN_EINVAL, "Refinement box extends beyond base grid in r direction");
+        if (P.eqsym) {
+            if (zb < 0.0) return fail(OLLIN_EINVAL, "For equatorial symmetry zbox must be larger than or equal to 0");
+            if (zb > 0.0 && zb - 0.5 * h->nzbox[b] * d1z <= 0.0) return fail(OLLIN_EINVAL, "Refinement box extends to negative values of z");
+            if (zb + 0.5 * h->nzbox[b] * d1z >= (h->nzbox[0] - g) * P.dz0)
+                return fail(OLLIN_EINVAL, "Refinement box extends beyond base grid in z direction");
+        } else if (zb - 0.5 * h->nzbox[b] * d1z <= -0.5 * (h->nzbox[0] - g) * P.dz0 ||
+                   zb + 0.5 * h->nzbox[b] * d1z >= 0.5 * (h->nzbox[0] - g) * P.dz0) {
+            return fail(OLLIN_EINVAL, "Refinement box extends beyond base grid in z direction");
+        }
+    }
+    std::vector<std::pair<int, int>> grids;
+    for (int l = 0; l <= h->nl[0]; ++l) grids.push_back({0, l});
+    for (int b = 1; b <= h->nb; ++b)
+        for (int l = 1; l <= h->nl[b]; ++l) grids.push_back({b, l});
+    h->nlev = (int)grids.size();
+    h->L.resize(h->nlev);
+    for (int k = 0; k < h->nlev; ++k) {
+        DLevel& L = h->L[k];
+        L.box = grids[k].first;
+        L.level = grids[k].second;
+        L.parent = -1;
+        if (L.level > 0) {
+            const int pb = L.level == 1 ? 0 : L.box;  // finebound.f90:66-70
+            for (int q = 0; q < h->nlev; ++q)
+                if (grids[q].first == pb && grids[q].second == L.level - 1) L.parent = q;
+        }
+    }
+    return OLLIN_OK;
+}
+
+int alloc_level(ollin_handle* h, DLevel& L, int gid) {
+    const ollin_params& P = h->P;
+    const int g = h->g;
+    const int level = L.level, box = L.box;
     L.g = g;
-    L.nr = P.nrtotal;
-    L.nz = P.nztotal;
-    // without equatorial symmetry Nz + ghost is made odd (setupboxes.f90:131-135)
-    if (!P.eqsym && (L.nz + g) % 2 == 0) L.nz += 1;
+    L.nr = h->nrbox[box];
+    L.nz = h->nzbox[box];
     L.ld = ((L.nr + g + 31) / 32) * 32;
     L.rows = L.nz + g;
     L.n = (size_t)L.ld * L.rows;
@@ -166,20 +234,24 @@ int alloc_level(ollin_handle* h, DLevel& L, int level) {
     for (int f = 0; f < NFIELDS; ++f) { L.acc[f] = q; q += L.n; }
     for (int x = 0; x < NAUX; ++x) { L.aux[x] = q; q += L.n; }
     L.coords = q;
-    // coordinates (evolve.f90:42-70, box 0, one process)
+    // coordinates (evolve.f90:42-70, one process): the axis on a cell face
+    // for boxes on it, else centred on the box
     L.rh.resize(L.nr + g);
     L.zh.resize(L.nz + g);
     std::vector<double> host(ncoord);
+    const double rb = h->rbox[box], zb = h->zbox[box];
     for (int i = 1 - g; i <= L.nr; ++i) {
-        const double r = ((double)(0 + i) - 0.5) * L.dr;
+        const double r = (rb == 0.0) ? ((double)(0 + i) - 0.5) * L.dr
+                                     : rb + ((double)(0 + i) - 0.5 * (double)(L.nr - g + 1)) * L.dr;
         L.rh[i - 1 + g] = r;
         host[i - 1 + g] = r;
         host[(size_t)(L.nr + g) + (i - 1 + g)] = 1.0 / r;
     }
     for (int j = 1 - g; j <= L.nz; ++j) {
-        // evolve.f90:57-70: the equator on a cell face (eqsym) or z centred on the box
-        const double z = P.eqsym ? ((double)(0 + j) - 0.5) * L.dz
-                                 : 0.0 + ((double)(0 + j) - 0.5 * (double)(L.nz - g + 1)) * L.dz;
+        // evolve.f90:57-70: the equator on a cell face (eqsym, boxes on it) or
+        // z centred on the box
+        const double z = (P.eqsym && zb == 0.0) ? ((double)(0 + j) - 0.5) * L.dz
+                                                : zb + ((double)(0 + j) - 0.5 * (double)(L.nz - g + 1)) * L.dz;
         L.zh[j - 1 + g] = z;
         host[(size_t)(L.nr + g) * 2 + (j - 1 + g)] = z;
     }
@@ -188,16 +260,20 @@ int alloc_level(ollin_handle* h, DLevel& L, int level) {
     LevelGeom& G = L.G;
     G.nr = L.nr; G.nz = L.nz; G.g = g; G.ld = L.ld;
     G.eqsym = P.eqsym ? 1 : 0;
-    G.jlo = P.eqsym ? 1 : 1 - g;
+    G.axis = rb == 0.0 ? 1 : 0;                        // main.f90:393-403
+    G.equator = (P.eqsym && zb == 0.0) ? 1 : 0;        // main.f90:412-424
+    G.lower_r = (box > 0 && rb != 0.0) ? 1 : 0;        // finebound.f90:246
+    G.lower_z = (!P.eqsym || (box > 0 && zb != 0.0)) ? 1 : 0;  // finebound.f90:361
+    G.jlo = G.equator ? 1 : 1 - g;
     G.dr = L.dr; G.dz = L.dz; G.dt = L.dt;
     G.idr = 1.0 / L.dr; G.idz = 1.0 / L.dz;
     G.rcol = L.coords + (g - 1);                 // rcol[i] for i >= 1-g
     G.ircol = L.coords + (L.nr + g) + (g - 1);
     G.zrow = L.coords + 2 * (L.nr + g) + (g - 1);
-    h->rminl[level] = L.rh[0];
-    h->rmaxl[level] = L.rh[L.nr - 1 + g];
-    h->zminl[level] = L.zh[0];
-    h->zmaxl[level] = L.zh[L.nz - 1 + g];
+    h->rminl[gid] = L.rh[0];
+    h->rmaxl[gid] = L.rh[L.nr - 1 + g];
+    h->zminl[gid] = L.zh[0];
+    h->zmaxl[gid] = L.zh[L.nz - 1 + g];
     L.cur = 0; L.p = 1; L.pp = 2;
     return OLLIN_OK;
 }
@@ -307,32 +383,35 @@ void launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
     else launch_rhs(a, s);
 }
 
-// Geometry part of the transfer arguments of level pair (level-1, level).
-ProlongArgs prolong_geometry(ollin_handle* h, int level) {
+// Geometry part of the transfer arguments of grid ``gid`` and its parent
+// (the next coarser level of its box, or box 0's level 0 for level 1).
+ProlongArgs prolong_geometry(ollin_handle* h, int gid) {
+    const int pg = h->L[gid].parent;
     ProlongArgs a{};
-    a.F = h->L[level].G;
-    a.Cg = h->L[level - 1].G;
-    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
-    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
-    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
+    a.F = h->L[gid].G;
+    a.Cg = h->L[pg].G;
+    a.rminl_f = h->rminl[gid]; a.rmaxl_f = h->rmaxl[gid];
+    a.zminl_f = h->zminl[gid]; a.zmaxl_f = h->zmaxl[gid];
+    a.rminl_c = h->rminl[pg]; a.rmaxl_c = h->rmaxl[pg];
+    a.zminl_c = h->zminl[pg]; a.zmaxl_c = h->zmaxl[pg];
     a.bicubic = h->P.interp_bicubic;
-    a.tab = h->L[level].ptab;
-    a.ntab = h->L[level].nptab;
+    a.tab = h->L[gid].ptab;
+    a.ntab = h->L[gid].nptab;
     return a;
 }
 
-RestrictArgs restrict_geometry(ollin_handle* h, int level) {
+RestrictArgs restrict_geometry(ollin_handle* h, int gid) {
+    const int pg = h->L[gid].parent;
     RestrictArgs a{};
-    a.F = h->L[level].G;
-    a.Cg = h->L[level - 1].G;
-    a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
-    a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.F = h->L[gid].G;
+    a.Cg = h->L[pg].G;
+    a.rminl_f = h->rminl[gid]; a.rmaxl_f = h->rmaxl[gid];
+    a.zminl_f = h->zminl[gid]; a.zmaxl_f = h->zmaxl[gid];
+    a.rminl_c = h->rminl[pg]; a.zminl_c = h->zminl[pg];
     a.eqsym = h->P.eqsym;
     a.bicubic = h->P.interp_bicubic;
-    a.tab = h->L[level].rtab;
-    a.ntab = h->L[level].nrtab;
+    a.tab = h->L[gid].rtab;
+    a.ntab = h->L[gid].nrtab;
     return a;
 }
 
@@ -356,12 +435,13 @@ void prolong_time(ProlongArgs& a, int g) {
     }
 }
 
-// Build the transfer stencils of every level pair once.
+// Build the transfer stencils of every grid and its parent once.
 int build_transfer_tables(ollin_handle* h) {
     const int g = h->g;
-    for (int l = 1; l < h->nlev; ++l) {
+    for (int l = 0; l < h->nlev; ++l) {
         DLevel& F = h->L[l];
-        DLevel& C = h->L[l - 1];
+        if (F.parent < 0) continue;
+        DLevel& C = h->L[F.parent];
         F.nptab = prolong_table_size(F.G);
         if (cudaMalloc(&F.ptab, (size_t)F.nptab * sizeof(XferPt)) != cudaSuccess)
             return fail(OLLIN_ENOMEM, "device allocation failed for the transfer tables");
@@ -396,12 +476,28 @@ int build_transfer_tables(ollin_handle* h) {
         if (rc) return rc;
     }
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    // a stencil that would leave its source grid marks the layout as unusable
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& F = h->L[l];
+        for (int k = 0; k < 2; ++k) {
+            const XferPt* t = k == 0 ? F.ptab : F.rtab;
+            const int n = k == 0 ? F.nptab : F.nrtab;
+            if (!t || n == 0) continue;
+            std::vector<XferPt> host(n);
+            CUDA_OR_FAIL(cudaMemcpy(host.data(), t, (size_t)n * sizeof(XferPt), cudaMemcpyDeviceToHost));
+            for (const XferPt& x : host)
+                if (x.mode == -1)
+                    return fail(OLLIN_EINVAL, "grid " + std::to_string(l) + ": a boundary or restriction point lies too close to "
+                                              "the edge of the grid it interpolates from (interp.f90:146-157)");
+        }
+    }
     return OLLIN_OK;
 }
 
 int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
     DLevel& F = h->L[level];
-    DLevel& C = h->L[level - 1];
+    const int pg = F.parent;
+    DLevel& C = h->L[pg];
     ProlongArgs a{};
     a.F = F.G;
     a.Cg = C.G;
@@ -418,9 +514,9 @@ int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
     }
     a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
     a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
-    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
-    a.tp = h->t[level - 1];
+    a.rminl_c = h->rminl[pg]; a.rmaxl_c = h->rmaxl[pg];
+    a.zminl_c = h->zminl[pg]; a.zmaxl_c = h->zmaxl[pg];
+    a.tp = h->t[pg];
     a.t0 = h->t[level];
     a.tm1 = h->t1[level];
     a.tl = a.t0 + dtw;
@@ -434,7 +530,8 @@ int prolong(ollin_handle* h, int level, int out_slot, double dtw) {
 
 int restrict_level(ollin_handle* h, int level) {
     DLevel& F = h->L[level];
-    DLevel& C = h->L[level - 1];
+    const int pg = F.parent;
+    DLevel& C = h->L[pg];
     RestrictArgs a{};
     a.F = F.G;
     a.Cg = C.G;
@@ -446,7 +543,7 @@ int restrict_level(ollin_handle* h, int level) {
     }
     a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
     a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.rminl_c = h->rminl[pg]; a.zminl_c = h->zminl[pg];
     a.eqsym = h->P.eqsym;
     a.bicubic = h->P.interp_bicubic;
     a.tab = F.rtab;
@@ -455,8 +552,8 @@ int restrict_level(ollin_handle* h, int level) {
     return after_launch(h);
 }
 
-// onestep.f90:2-522 for box 0
-int onestep(ollin_handle* h, int level) {
+// One time step of one grid (the body of the box loop of onestep.f90:73-388).
+int step_grid(ollin_handle* h, int level) {
     DLevel& L = h->L[level];
     const bool rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
     const bool t0 = h->t[level] == 0.0;  // currentgrid: time = t(box,level)
@@ -506,7 +603,7 @@ int onestep(ollin_handle* h, int level) {
             h->rhs_point_stages += (double)L.nr * (double)(L.nz - L.G.jlo + 1);
             h->rhs_launches++;
         }
-        if (level > 0) {
+        if (L.level > 0) {
             rc = prolong(h, level, out_slot, dtw);
             if (rc) return rc;
         }
@@ -521,22 +618,57 @@ int onestep(ollin_handle* h, int level) {
     h->t1[level] = h->t[level];
     h->s[level] = h->s[level] + 1;
     h->t[level] = h->t[level] + dt;
-    h->point_updates += (double)L.nr * (double)(L.nz - L.G.jlo + 1);
-    if (level < h->nlev - 1) {
+    h->point_updates += (double)L.nr * (double)(L.nz - (L.G.eqsym ? 1 : 1 - L.g) + 1);
+    return OLLIN_OK;
+}
+
+// onestep.f90:2-522: a step of every box that has this level (boxes 0..Nb),
+// two steps of the next level, then each box restricts into its parent
+// with the parent's symmetries and ``auxiliary`` (:472-514).  Boxes that
+// overlap are refused at create, so ``syncboxes`` (:446-466) has nothing
+// to copy.
+int onestep(ollin_handle* h, int level) {
+    for (int k = 0; k < h->nlev; ++k) {
+        if (h->L[k].level != level) continue;
+        int rc = step_grid(h, k);
+        if (rc) return rc;
+    }
+    if (level < h->nlmax) {
         int rc = onestep(h, level + 1);
         if (rc) return rc;
         rc = onestep(h, level + 1);
         if (rc) return rc;
     }
-    if (level > 0 && h->s[level] % 2 == 0) {
-        int rc = restrict_level(h, level);
-        if (rc) return rc;
-        DLevel& C = h->L[level - 1];
-        rc = do_symmetry(h, C, C.cur, active_fields(h, false));
-        if (rc) return rc;
-        rc = do_aux(h, C, C.cur, h->t[level - 1] == 0.0);
-        if (rc) return rc;
+    if (level > 0) {
+        for (int k = 0; k < h->nlev; ++k) {
+            if (h->L[k].level != level || h->s[k] % 2 != 0) continue;
+            int rc = restrict_level(h, k);
+            if (rc) return rc;
+            const int pg = h->L[k].parent;
+            DLevel& C = h->L[pg];
+            rc = do_symmetry(h, C, C.cur, active_fields(h, false));
+            if (rc) return rc;
+            rc = do_aux(h, C, C.cur, h->t[pg] == 0.0);
+            if (rc) return rc;
+        }
     }
+    return OLLIN_OK;
+}
+
+// syncboxes.f90:48-52 on every level: the grids of two boxes on one level
+// may not overlap (their overlap copy, which also carries the auxiliary
+// arrays, is not built)
+int check_boxes_apart(ollin_handle* h) {
+    for (int a = 0; a < h->nlev; ++a)
+        for (int b = a + 1; b < h->nlev; ++b) {
+            if (h->L[a].level != h->L[b].level || h->L[a].box == h->L[b].box) continue;
+            const bool apart = h->rmaxl[a] < h->rminl[b] || h->rmaxl[b] < h->rminl[a] || h->zmaxl[a] < h->zminl[b] ||
+                               h->zmaxl[b] < h->zminl[a];
+            if (!apart)
+                return fail(OLLIN_EINVAL, "refinement boxes " + std::to_string(h->L[a].box) + " and " +
+                                              std::to_string(h->L[b].box) + " overlap on level " +
+                                              std::to_string(h->L[a].level) + " (syncboxes is not supported)");
+        }
     return OLLIN_OK;
 }
 
@@ -1565,6 +1697,7 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     const ollin_params& P = h->P;
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
     if (!P.eqsym) return fail(OLLIN_EINVAL, "maximal slicing on the device needs equatorial symmetry (eqsym)");
+    if (h->nb > 0) return fail(OLLIN_EINVAL, "maximal slicing on the device needs Nb = 0");
     if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
         return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave or sor");
     // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)
@@ -1694,7 +1827,6 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
     auto* h = new ollin_handle();
     h->P = *p;
     h->g = 3;
-    h->nlev = p->nl0 + 1;
     h->shift = p->shift == OLLIN_SHIFT_GAMMADRIVER2;
     h->scalar = p->mattertype == OLLIN_MATTER_SCALAR;
     h->phys = make_phys(*p);
@@ -1704,6 +1836,11 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
         for (int f : {F_BETAR, F_BETAZ, F_DTBETAR, F_DTBETAZ}) h->fields.push_back(f);
     if (h->scalar)
         for (int f : {F_SPHI, F_SXIR, F_SXIZ, F_SPI}) h->fields.push_back(f);
+    rc = setup_boxes(h);
+    if (rc) {
+        delete h;
+        return rc;
+    }
     const int L = h->nlev;
     h->t.assign(L, 0.0); h->t1.assign(L, 0.0); h->t2.assign(L, 0.0); h->s.assign(L, 0);
     h->rminl.resize(L); h->rmaxl.resize(L); h->zminl.resize(L); h->zmaxl.resize(L);
@@ -1716,13 +1853,17 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
         return fail(OLLIN_ENOMEM, "device allocation failed");
     }
     cudaMemsetAsync(h->d_flag, 0, 64, h->stream);
-    h->L.resize(L);
     for (int l = 0; l < L; ++l) {
         rc = alloc_level(h, h->L[l], l);
         if (rc) {
             ollin_gpu_destroy(h);
             return rc;
         }
+    }
+    rc = check_boxes_apart(h);
+    if (rc) {
+        ollin_gpu_destroy(h);
+        return rc;
     }
     rc = build_transfer_tables(h);
     if (rc) {
@@ -1754,7 +1895,8 @@ int ollin_gpu_num_levels(const ollin_handle* h) { return h ? h->nlev : 0; }
 int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out) {
     if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad level");
     const DLevel& L = h->L[level];
-    out->level = level; out->nr = L.nr; out->nz = L.nz; out->ghost = L.g;
+    out->level = L.level; out->nr = L.nr; out->nz = L.nz; out->ghost = L.g;
+    out->box = L.box;
     out->dr = L.dr; out->dz = L.dz; out->dt = L.dt;
     out->rmin = h->rminl[level]; out->rmax = h->rmaxl[level];
     out->zmin = h->zminl[level]; out->zmax = h->zmaxl[level];
@@ -1887,8 +2029,9 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
             src = base_ptr(L, L.aux[X_RSCAL]);
         }
     }
-    launch_norms(L.G, src, h->P.interp_bicubic, h->rminl[level], h->zminl[level], h->rmaxl[level], h->zmaxl[level],
-                 h->d_norm, h->stream);
+    // the origin value only for box 0 (save0Ddata.f90:370-374)
+    launch_norms(L.G, src, L.box == 0 ? h->P.interp_bicubic : -1, h->rminl[level], h->zminl[level], h->rmaxl[level],
+                 h->zmaxl[level], h->d_norm, h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
     double res[6];

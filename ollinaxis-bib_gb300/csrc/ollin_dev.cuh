@@ -43,8 +43,12 @@ enum AuxField : int {
 // Geometry of one level as seen by a kernel.
 struct LevelGeom {
     int nr, nz, g, ld;   // Nr, Nz, ghost, leading dimension
-    int jlo;             // first z-row with a source: 1 (eqsym) or 1-g
-    int eqsym;
+    int jlo;             // first z-row with a source: 1 (the grid owns the equator) or 1-g
+    int eqsym;           // equatorial symmetry of the run (param eqsym)
+    int axis, equator;   // the grid's ghosts are the axis / equator parity images
+                         // (main.f90:380-460: boxes with rbox = 0 / zbox = 0)
+    int lower_r, lower_z;  // the lower r / z edge is a refinement boundary
+                           // (finebound.f90:246-285, :361-397)
     double dr, dz, dt;
     double idr, idz;     // 1/dr, 1/dz
     const double* rcol;  // r(i) for i = 1-g..nr   (indexed rcol[i])

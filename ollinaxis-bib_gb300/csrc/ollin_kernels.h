@@ -316,7 +316,6 @@ void launch_sor_phys_pass_seq(const SorPhysPassArgs& a, cudaStream_t s);
 void launch_aux_point(const AuxArgs& a, cudaStream_t s);
 void launch_aux_deriv(const AuxArgs& a, cudaStream_t s);
 void launch_symmetry(const SymArgs& a, cudaStream_t s);
-void launch_prolong(const ProlongArgs& a, cudaStream_t s);
 void launch_restrict(const RestrictArgs& a, cudaStream_t s);
 void launch_norms(const LevelGeom& G, const double* f, int origin_bicubic, double rminl, double zminl,
                   double rmaxl, double zmaxl, double* dev_out, cudaStream_t s);

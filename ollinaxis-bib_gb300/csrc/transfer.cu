@@ -23,14 +23,17 @@ __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, 
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 
 // ---- parity ghost fill -------------------------------------------------
-// thread space: the g ghost columns i <= 0 over all rows, then (eqsym) the
-// g ghost rows j <= 0 for i >= 1; the corner points belong to the columns
+// thread space: the g ghost columns i <= 0 over all rows (grids that own the
+// axis), then the g ghost rows j <= 0 (grids that own the equator) for the
+// columns not filled already; a corner point belongs to the columns when the
+// grid owns the axis
 __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
     if (a.skip && *a.skip) return;
     const LevelGeom& G = a.G;
     const int g = G.g;
-    const int ncol = g * (G.nz + g);
-    const int nrow = G.eqsym ? g * G.nr : 0;
+    const int ncol = G.axis ? g * (G.nz + g) : 0;
+    const int i0 = G.axis ? 1 : 1 - g, ni = G.nr - i0 + 1;
+    const int nrow = G.equator ? g * ni : 0;
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= ncol + nrow) return;
     int i, j;
@@ -39,10 +42,10 @@ __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ S
         j = 1 - g + t / g;
     } else {
         const int q = t - ncol;
-        i = 1 + q % G.nr;
-        j = 1 - g + q / G.nr;
+        i = i0 + q % ni;
+        j = 1 - g + q / ni;
     }
-    const bool gi = i <= 0, gj = G.eqsym && j <= 0;
+    const bool gi = G.axis && i <= 0, gj = G.equator && j <= 0;
     const int si = gi ? 1 - i : i, sj = gj ? 1 - j : j;
     const size_t o = (size_t)i + (size_t)j * G.ld, os = (size_t)si + (size_t)sj * G.ld;
     for (int k = 0; k < a.nf; ++k) {
@@ -60,26 +63,33 @@ struct InterpPt {
     double w[4][4];
 };
 
-__device__ void interp_weights(const LevelGeom& G, double rminl, double rmaxl, double zminl, double zmaxl,
+// Returns false (and mode -1) when the stencil would leave the grid, which
+// a consistent box layout never asks for (interp.f90:146-157 reports it and
+// reads on); the callers turn that into an error instead of a stray read.
+__device__ bool interp_weights(const LevelGeom& G, double rminl, double rmaxl, double zminl, double zmaxl,
                                double r0, double z0, int bicubic, InterpPt& p) {
     const int g = G.g;
     const double dr = G.dr, dz = G.dz;
     const double r1 = G.rcol[1 - g], z1 = G.zrow[1 - g];
     p.i0 = (int)((r0 - r1) / dr) + 1 - g;
-    const double deltar = r0 - G.rcol[p.i0];
     p.j0 = (int)((z0 - z1) / dz) + 1 - g;
+    p.mode = -1;
+    if (p.i0 < 1 - g || p.i0 > G.nr || p.j0 < 1 - g || p.j0 > G.nz) return false;
+    const double deltar = r0 - G.rcol[p.i0];
     const double deltaz = z0 - G.zrow[p.j0];
-    if (deltar == 0.0 && deltaz == 0.0) { p.mode = 0; return; }
+    if (deltar == 0.0 && deltaz == 0.0) { p.mode = 0; return true; }
     const bool forcelinear = ((rmaxl - r0) < dr) || ((zmaxl - z0) < dz) || ((r0 - rminl) < dr) || ((z0 - zminl) < dz);
     const double auxr = deltar / dr, auxz = deltaz / dz;
     if (!bicubic || forcelinear) {
+        if (p.i0 + 1 > G.nr || p.j0 + 1 > G.nz) return false;
         // factors kept separate: the reference multiplies left to right,
         // fa(0,0)*(1-auxr)*(1-auxz) + fa(1,0)*auxr*(1-auxz) + ...
         p.mode = 1;
         p.w[0][0] = auxr;
         p.w[0][1] = auxz;
-        return;
+        return true;
     }
+    if (p.i0 - 1 < 1 - g || p.i0 + 2 > G.nr || p.j0 - 1 < 1 - g || p.j0 + 2 > G.nz) return false;
     p.mode = 2;
     for (int ii = -1; ii <= 2; ++ii)
         for (int jj = -1; jj <= 2; ++jj) {
@@ -94,6 +104,7 @@ __device__ void interp_weights(const LevelGeom& G, double rminl, double rmaxl, d
             }
             p.w[ii + 1][jj + 1] = aux;
         }
+    return true;
 }
 
 __device__ double interp_apply(const LevelGeom& G, const double* f, const InterpPt& p) {
@@ -114,54 +125,6 @@ __device__ double interp_apply(const LevelGeom& G, const double* f, const Interp
         for (int jj = -1; jj <= 2; ++jj)
             v = add(v, mul(p.w[ii + 1][jj + 1], f[(p.i0 + ii) + (long)(p.j0 + jj) * ld]));
     return v;
-}
-
-// ---- prolongation ----------------------------------------------------------
-// Thread space: the upper-r strip (imax+1) x (Nz+g) followed by the upper-z
-// strip (jmax+1) x (Nr+g); corner points are written by both strips with the
-// same value, as in the reference.
-__global__ void __launch_bounds__(128) prolong_kernel(const __grid_constant__ ProlongArgs a) {
-    if (a.skip && *a.skip) return;
-    const LevelGeom& F = a.F;
-    const int g = F.g;
-    const int nstrip_r = (a.imax + 1) * (F.nz + g);
-    const int nstrip_z = (a.imax + 1) * (F.nr + g);
-    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (t >= nstrip_r + nstrip_z) return;
-    double r0, z0;
-    if (t < nstrip_r) {
-        const int m = t / (F.nz + g), n = t % (F.nz + g);
-        r0 = sub(a.rmaxl_f, mul((double)m, F.dr));
-        z0 = add(a.zminl_f, mul((double)n, F.dz));
-    } else {
-        const int q = t - nstrip_r;
-        const int n = q / (F.nr + g), m = q % (F.nr + g);
-        r0 = add(a.rminl_f, mul((double)m, F.dr));
-        z0 = sub(a.zmaxl_f, mul((double)n, F.dz));
-    }
-    const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
-    const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
-    if (!(i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz)) return;
-    InterpPt p;
-    interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
-    const size_t o = (size_t)i + (size_t)j * F.ld;
-    const double tp = a.tp, t0 = a.t0, tm1 = a.tm1, tl = a.tl;
-    for (int k = 0; k < a.nf; ++k) {
-        const int f = a.fid[k];
-        const double aux2 = interp_apply(a.Cg, a.cin[f], p);
-        double v;
-        if (tp == tl) {
-            v = aux2;  // the history weights vanish exactly
-        } else if (a.border == 1) {
-            v = add(mul((tl - t0) / (tp - t0), aux2), mul((tl - tp) / (t0 - tp), a.fp[f][o]));
-        } else {
-            const double w0 = ((tl - t0) * (tl - tm1)) / ((tp - t0) * (tp - tm1));
-            const double w1 = ((tl - tp) * (tl - tm1)) / ((t0 - tp) * (t0 - tm1));
-            const double w2 = ((tl - tp) * (tl - t0)) / ((tm1 - tp) * (tm1 - t0));
-            v = add(add(mul(w0, aux2), mul(w1, a.fp[f][o])), mul(w2, a.fpp[f][o]));
-        }
-        a.fout[f][o] = v;
-    }
 }
 
 // ---- restriction -----------------------------------------------------------
@@ -185,7 +148,7 @@ __global__ void __launch_bounds__(128) restrict_kernel(const __grid_constant__ R
     const int j = (int)round((z0 - C.zrow[1 - g]) / C.dz) + 1 - g;
     if (!(i >= 1 - g && i <= C.nr && j >= 1 - g && j <= C.nz)) return;
     InterpPt p;
-    interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p);
+    if (!interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p)) return;
     const size_t o = (size_t)i + (size_t)j * C.ld;
     for (int k = 0; k < a.nf; ++k) {
         const int f = a.fid[k];
@@ -228,37 +191,37 @@ __device__ __forceinline__ double xfer_apply(const LevelGeom& G, const double* f
 // the lower z strip (:351-397).  The reference writes the strips in that
 // order, so a point that a later strip also writes takes the later value:
 // ``cover`` is the strip depth from which a later strip reaches the point.
+// Strips in the order finebound.f90 writes them: upper r (rR), lower r (rL,
+// boxes off the axis), upper z (zR), lower z (zL, without equatorial
+// symmetry or off the equator), each (imax+1) deep for imax = ghost+2.
+// ``cover`` is the smallest imax at which a later strip writes the same
+// point, so that the last writer wins as in the reference.
 __global__ void __launch_bounds__(128) prolong_table_kernel(const __grid_constant__ ProlongArgs a, XferPt* tab) {
     const LevelGeom& F = a.F;
     const int g = F.g;
     const int imax = g + 2;
     const int nstrip_r = (imax + 1) * (F.nz + g);
     const int nstrip_z = (imax + 1) * (F.nr + g);
-    const int nstrips_z = F.eqsym ? 1 : 2;
+    const int nr_strips = F.lower_r ? 2 : 1, nz_strips = F.lower_z ? 2 : 1;
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    if (t >= nstrip_r + nstrips_z * nstrip_z) return;
+    if (t >= nr_strips * nstrip_r + nz_strips * nstrip_z) return;
     double r0, z0;
-    int depth, strip;
-    if (t < nstrip_r) {
-        const int m = t / (F.nz + g), n = t % (F.nz + g);
-        r0 = sub(a.rmaxl_f, mul((double)m, F.dr));
+    int depth, strip;  // 0 rR, 1 rL, 2 zR, 3 zL
+    if (t < nr_strips * nstrip_r) {
+        const int q = t % nstrip_r;
+        const int m = q / (F.nz + g), n = q % (F.nz + g);
+        strip = t / nstrip_r;
+        r0 = strip == 0 ? sub(a.rmaxl_f, mul((double)m, F.dr)) : add(a.rminl_f, mul((double)m, F.dr));
         z0 = add(a.zminl_f, mul((double)n, F.dz));
         depth = m;
-        strip = 0;
-    } else if (t < nstrip_r + nstrip_z) {
-        const int q = t - nstrip_r;
-        const int n = q / (F.nr + g), m = q % (F.nr + g);
-        r0 = add(a.rminl_f, mul((double)m, F.dr));
-        z0 = sub(a.zmaxl_f, mul((double)n, F.dz));
-        depth = n;
-        strip = 1;
     } else {
-        const int q = t - nstrip_r - nstrip_z;
+        const int q0 = t - nr_strips * nstrip_r;
+        const int q = q0 % nstrip_z;
         const int n = q / (F.nr + g), m = q % (F.nr + g);
+        strip = 2 + q0 / nstrip_z;
         r0 = add(a.rminl_f, mul((double)m, F.dr));
-        z0 = add(a.zminl_f, mul((double)n, F.dz));
+        z0 = strip == 2 ? sub(a.zmaxl_f, mul((double)n, F.dz)) : add(a.zminl_f, mul((double)n, F.dz));
         depth = n;
-        strip = 2;
     }
     XferPt x{};
     x.depth = depth;
@@ -266,13 +229,17 @@ __global__ void __launch_bounds__(128) prolong_table_kernel(const __grid_constan
     const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
     x.o_out = kNoPoint;
     x.cover = 1 << 30;
-    if (strip == 0) x.cover = F.nz - j;                                    // the upper z strip reaches row j
-    if (strip <= 1 && !F.eqsym) x.cover = min(x.cover, j - (1 - g));       // the lower z strip reaches row j
+    if (strip < 1 && F.lower_r) x.cover = min(x.cover, i - (1 - g));  // rL reaches column i
+    if (strip < 2) x.cover = min(x.cover, F.nz - j);                   // zR reaches row j
+    if (strip < 3 && F.lower_z) x.cover = min(x.cover, j - (1 - g));  // zL reaches row j
     if (i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz) {
         InterpPt p;
-        interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
-        to_xfer(p, x);
-        x.o_out = i + j * F.ld;
+        if (interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p)) {
+            to_xfer(p, x);
+            x.o_out = i + j * F.ld;
+        } else {
+            x.mode = -1;  // the host refuses the layout
+        }
     }
     tab[t] = x;
 }
@@ -319,9 +286,12 @@ __global__ void __launch_bounds__(128) restrict_table_kernel(const __grid_consta
         const int j = (int)round((z0 - C.zrow[1 - g]) / C.dz) + 1 - g;
         if (i >= 1 - g && i <= C.nr && j >= 1 - g && j <= C.nz) {
             InterpPt p;
-            interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p);
-            to_xfer(p, x);
-            x.o_out = i + j * C.ld;
+            if (interp_weights(F, a.rminl_f, a.rmaxl_f, a.zminl_f, a.zmaxl_f, r0, z0, a.bicubic, p)) {
+                to_xfer(p, x);
+                x.o_out = i + j * C.ld;
+            } else {
+                x.mode = -1;
+            }
         }
     }
     tab[t] = x;
@@ -352,7 +322,7 @@ __global__ void __launch_bounds__(128) inject_kernel(const __grid_constant__ Inj
     const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
     if (!(i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz)) return;
     InterpPt p;
-    interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p);
+    if (!interp_weights(a.Cg, a.rminl_c, a.rmaxl_c, a.zminl_c, a.zmaxl_c, r0, z0, a.bicubic, p)) return;
     a.fout[(size_t)i + (size_t)j * F.ld] = interp_apply(a.Cg, a.cin, p);
 }
 
@@ -396,9 +366,12 @@ __global__ void __launch_bounds__(512) norms_kernel(LevelGeom G, const double* f
         out[1] = smin[0];
         out[2] = snm1[0];
         out[3] = sqrt(snm2[0] / (double)npts);
-        InterpPt p;
-        interp_weights(G, rminl, rmaxl, zminl, zmaxl, 0.0, 0.0, bicubic, p);
-        out[4] = interp_apply(G, f, p);
+        if (bicubic >= 0) {
+            InterpPt p;
+            out[4] = interp_weights(G, rminl, rmaxl, zminl, zmaxl, 0.0, 0.0, bicubic, p) ? interp_apply(G, f, p) : 0.0;
+        } else {
+            out[4] = 0.0;  // save0Ddata.f90:370-374 writes origin data for box 0 only
+        }
         out[5] = snan[0] ? 1.0 : 0.0;
     }
 }
@@ -418,10 +391,11 @@ __global__ void ham_edges_kernel(LevelGeom G, double* h) {
     __syncthreads();
     for (int i = 1 - g + (int)threadIdx.x; i <= G.nr; i += blockDim.x) H(i, G.nz) = H(i, G.nz - 1);
     __syncthreads();
-    for (int j = 1 - g + (int)threadIdx.x; j <= G.nz; j += blockDim.x)
-        for (int ii = 1; ii <= g; ++ii) H(1 - ii, j) = H(ii, j);
+    if (G.axis)
+        for (int j = 1 - g + (int)threadIdx.x; j <= G.nz; j += blockDim.x)
+            for (int ii = 1; ii <= g; ++ii) H(1 - ii, j) = H(ii, j);
     __syncthreads();
-    if (G.eqsym)
+    if (G.equator)
         for (int i = 1 - g + (int)threadIdx.x; i <= G.nr; i += blockDim.x)
             for (int jj = 1; jj <= g; ++jj) H(i, 1 - jj) = H(i, jj);
 }
@@ -463,17 +437,15 @@ dim3 full_grid(const LevelGeom& G, dim3 blk) {
 }  // namespace
 
 void launch_symmetry(const SymArgs& a, cudaStream_t s) {
-    const int n = a.G.g * (a.G.nz + a.G.g) + (a.G.eqsym ? a.G.g * a.G.nr : 0);
+    const int n = (a.G.axis ? a.G.g * (a.G.nz + a.G.g) : 0) +
+                  (a.G.equator ? a.G.g * (a.G.axis ? a.G.nr : a.G.nr + a.G.g) : 0);
+    if (n == 0) return;
     symmetry_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
 }
 
-void launch_prolong(const ProlongArgs& a, cudaStream_t s) {
-    const int n = (a.imax + 1) * (a.F.nz + a.F.g) + (a.imax + 1) * (a.F.nr + a.F.g);
-    prolong_kernel<<<(n + 127) / 128, 128, 0, s>>>(a);
-}
 
 int prolong_table_size(const LevelGeom& F) {
-    return (F.g + 3) * (F.nz + F.g) + (F.eqsym ? 1 : 2) * (F.g + 3) * (F.nr + F.g);
+    return (F.lower_r ? 2 : 1) * (F.g + 3) * (F.nz + F.g) + (F.lower_z ? 2 : 1) * (F.g + 3) * (F.nr + F.g);
 }
 
 void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s) {

@@ -29,7 +29,8 @@ class LevelDesc(ctypes.Structure):
     _fields_ = [("level", ctypes.c_int), ("nr", ctypes.c_int), ("nz", ctypes.c_int), ("ghost", ctypes.c_int),
                 ("dr", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
                 ("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("zmin", ctypes.c_double),
-                ("zmax", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_int)]
+                ("zmax", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_int),
+                ("box", ctypes.c_int)]
 
 
 def library_path():
@@ -135,6 +136,11 @@ class Evolution:
         d = LevelDesc()
         self._check(self.L.ollin_gpu_level_desc(self.h, level, ctypes.byref(d)))
         return d
+
+    def grid(self, gid):
+        """(box, level) of grid ``gid``."""
+        d = self.desc(gid)
+        return d.box, d.level
 
     def download(self, level, name):
         """(Nr+g, Nz+g) array indexed [i+g-1, j+g-1] for Fortran (i, j)."""

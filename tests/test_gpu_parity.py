@@ -116,6 +116,57 @@ def test_no_equatorial_symmetry_odd_grid_icn():
     run(cfg, 8, check_every=4)
 
 
+# refinement boxes (Nb > 0): box 0 is the base grid; box 1 on the axis above
+# the equator with two levels (lower z edge from finebound), box 2 a ring on
+# the equator (lower r edge); and a ring off both, with the shift
+BOXES = dict(C1, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=2, Nl1=2, Nrbox1=12, Nzbox1=12, zbox1=6.0,
+             Nl2=1, Nrbox2=10, Nzbox2=10, rbox2=8.0)
+RING = dict(C1, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=10, Nzbox1=10, rbox1=5.0,
+            zbox1=5.0, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+
+
+@pytest.mark.parametrize("cfg", [BOXES, RING], ids=["axis_and_ring_boxes", "ring_off_equator_shift"])
+def test_refinement_boxes(cfg):
+    """Box loops of onestep.f90 (every box of a level, restriction of each box
+    into box 0's level 0 or its own coarser level), the lower-edge strips of
+    finebound.f90 and the box coordinates of evolve.f90:42-70; grids in the
+    reference's box order, constraint norms with the origin value for box 0
+    only."""
+    o, e = make_pair(cfg)
+    for k in range(1, 9):
+        assert o.step() == e.step()
+        if k % 4:
+            continue
+        for lev in o.levels():
+            d = e.desc(lev)
+            for nm in field_list(cfg):
+                a, b = e.download(lev, nm), o.get(lev, nm)
+                scale = max(float(abs(b).max()), 1e-300)
+                if nm in ("lambda", "Alambda"):
+                    # (A - H)/r^2 is near zero far from the puncture and
+                    # carries the fields' rounding divided by r^2 ~ dr^2
+                    scale = max(scale, 1e-3 / (d.dr * d.dz))
+                err = float(abs(a - b).max()) / scale
+                assert err <= tol_for(nm), "step %d grid %d %s: rel diff %.3e" % (k, lev, nm, err)
+    for lev in o.levels():
+        assert e.grid(lev) == o.grid(lev)
+        o.constraints(lev)
+        for nm in ["ham", "mom_r", "mom_z"]:
+            ng, no = e.norms(lev, nm), o.norms(lev, nm)
+            # the norms cover i, j >= 1: near zero far from the puncture, so
+            # the bound is absolute at the scale of the curvature terms
+            scale = max(abs(no[2]), 1e-6)
+            for k in (2, 3, 4):
+                assert abs(ng[k] - no[k]) <= 1e-8 * scale, (lev, nm, k, ng[k], no[k])
+
+
+def test_overlapping_boxes_are_refused():
+    from ollin.gpu import Evolution, OllinError
+    cfg = dict(BOXES, nl0=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
+    with pytest.raises(OllinError):
+        Evolution(params(cfg))
+
+
 def test_norms_match_oracle():
     o, e = make_pair(dict(C1, nl0=1))
     for _ in range(3):
