@@ -11,6 +11,7 @@
 //   of src/base/save0Ddata.f90:221-288,370-374.
 // It exposes a C API (ollin_oracle.h) with the same parameter struct as the
 // GPU library so that one harness drives both.
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <stdexcept>
@@ -389,18 +390,58 @@ void restrict_(Sim& S, int gid) {
         }
 }
 
-// syncboxes.f90:48-52: grids of two boxes on one level that overlap copy
-// each other's data there; the copy is not restated, so overlapping boxes
-// are refused
-void check_no_intersection(Sim& S, int level) {
-    for (Level& a : S.L)
-        for (Level& b : S.L) {
-            if (a.level != level || b.level != level || a.box >= b.box) continue;
-            const int p = a.gid, q = b.gid;
-            const bool apart = S.rmaxl[p] < S.rminl[q] || S.rmaxl[q] < S.rminl[p] || S.zmaxl[p] < S.zminl[q] ||
-                               S.zmaxl[q] < S.zminl[p];
-            if (!apart) throw std::runtime_error("oracle: refinement boxes intersect (syncboxes is not restated)");
+// syncboxes.f90:2-243 with the generated intersect_interp.inc: grid ``p``
+// (box b1) takes every EVOLVE and AUXILIARY array that is not NOSYNC from
+// grid ``q`` (box b2, same level) on its strips up to 3*ghost deep, at the
+// points well inside q.  Arrays the reference does not declare (the var_p,
+// accumulator and source copies) are overwritten before they are read, so
+// every array but the NOSYNC coordinates and scratch is taken.
+void syncboxes(Sim& S, int p, int q) {
+    Level& A = S.L[p];
+    Level& B = S.L[q];
+    if (S.rmaxl[p] < S.rminl[q] || S.rmaxl[q] < S.rminl[p] || S.zmaxl[p] < S.zminl[q] || S.zmaxl[q] < S.zminl[p]) return;
+    const int g = A.g, level = A.level;
+    const int imax = 3 * g, jmax = 3 * g;
+    const double deltar = (double)(3 * g) * S.drl[level], deltaz = (double)(3 * g) * S.dzl[level];
+    Arr& r = A.a("r"); Arr& z = A.a("z");
+    std::vector<std::string> names;
+    for (auto& kv : A.arrs) {
+        const std::string& n = kv.first;
+        if (n == "r" || n == "z" || n == "rr" || n == "auxarray" || n == "Dr_auxarray" || n == "Dz_auxarray") continue;
+        if (B.arrs.find(n) == B.arrs.end()) continue;
+        names.push_back(n);
+    }
+    std::sort(names.begin(), names.end());
+    auto point = [&](double r0, double z0) {
+        if (!(r0 >= S.rminl[q] + deltar && r0 <= S.rmaxl[q] - deltar && z0 >= S.zminl[q] + deltaz &&
+              z0 <= S.zmaxl[q] - deltaz))
+            return;
+        const int i = (int)nint_((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
+        const int j = (int)nint_((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
+        const bool flag1 = (i >= 1 - g) && (i <= A.Nr) && (j >= 1 - g) && (j <= A.Nz);
+        for (const std::string& n : names) {
+            const double aux2 = interp(S, q, B.a(n), r0, z0);
+            if (flag1) A.a(n)(i, j) = aux2;
         }
+    };
+    for (int m = 0; m <= imax; ++m)  // upper r (:60-104)
+        for (int n = 0; n <= A.Nz + g - 1; ++n) point(S.rmaxl[p] - (double)m * S.drl[level], S.zminl[p] + (double)n * S.dzl[level]);
+    if (A.box > 0 && S.rbox[A.box] != 0.0)  // lower r (:109-141)
+        for (int m = 0; m <= imax; ++m)
+            for (int n = 0; n <= A.Nz + g - 1; ++n) point(S.rminl[p] + (double)m * S.drl[level], S.zminl[p] + (double)n * S.dzl[level]);
+    for (int n = 0; n <= jmax; ++n)  // upper z (:145-177)
+        for (int m = 0; m <= A.Nr + g - 1; ++m) point(S.rminl[p] + (double)m * S.drl[level], S.zmaxl[p] - (double)n * S.dzl[level]);
+    if (!S.P.eqsym || (A.box > 0 && S.zbox[A.box] != 0.0))  // lower z (:181-213)
+        for (int n = 0; n <= jmax; ++n)
+            for (int m = 0; m <= A.Nr + g - 1; ++m) point(S.rminl[p] + (double)m * S.drl[level], S.zminl[p] + (double)n * S.dzl[level]);
+}
+
+// onestep.f90:446-466 and evolve.f90:211-219: every ordered pair of boxes
+// that has the level, box 0 first
+void sync_level(Sim& S, int level) {
+    for (Level& A : S.L)
+        for (Level& B : S.L)
+            if (A.level == level && B.level == level && A.box != B.box) syncboxes(S, A.gid, B.gid);
 }
 
 // ---------------------------------------------------------------------------
@@ -455,7 +496,7 @@ static void onestep(Sim& S, int level) {
         onestep(S, level + 1);
         onestep(S, level + 1);
     }
-    if (level > 0) check_no_intersection(S, level);
+    if (level > 0) sync_level(S, level);
     if (level > 0) {
         for (Level& F : S.L) {
             if (F.level != level || S.s[F.gid] % 2 != 0) continue;
@@ -573,7 +614,7 @@ static void initialize(Sim& S) {
             for (size_t q = 0; q < b.v.size(); ++q) { b.v[q] = S.P.drivercsi * dr_.v[q]; bz.v[q] = S.P.drivercsi * dz_.v[q]; }
         }
     }
-    for (int level = 1; level <= S.Nlmax; ++level) check_no_intersection(S, level);  // :211-219
+    for (int level = 1; level <= S.Nlmax; ++level) sync_level(S, level);  // :211-219
 }
 
 // save0Ddata.f90:221-288 and the origin value at :370-374

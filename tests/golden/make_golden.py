@@ -79,6 +79,10 @@ CASES = {
     "box_ring_shift": dict(BASE, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=10,
                            Nzbox1=10, rbox1=5.0, zbox1=5.0, shift="Gammadriver2", drivercsi=0.75,
                            drivereta=2.0, _steps=[0, 1, 2]),
+    # boxes that overlap on level 1 (syncboxes.f90 with intersect_interp.inc):
+    # box 0's level 1 around the origin and box 1 on the axis above it
+    "box_overlap": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,
+                        Nzbox1=16, zbox1=4.0, _steps=[0, 1, 2]),
     # maximal slicing (maximalslicing.f90, physical Laplacian).  Time-symmetric
     # vacuum data have K_ij = 0 and a maximal lapse of exactly 1, and so does
     # a static massless scalar field (rho + S = 0), so the cases solve where

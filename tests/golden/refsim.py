@@ -41,7 +41,7 @@ SOURCES = [
     "src/matter/scalar.f90",
     "src/elliptic/wave_elliptic.f90", "src/elliptic/sor_elliptic.f90",
     "src/matter/idata_scalarpulse.f90", "src/geometry/idata_brillwave.f90",
-    "src/geometry/maximalslicing.f90",
+    "src/geometry/maximalslicing.f90", "src/base/syncboxes.f90",
 ]
 GENERATED = ["saveold.f90", "accumulate.f90", "update.f90", "symmetries_r.f90",
              "symmetries_z.f90"]
@@ -163,7 +163,6 @@ class RefSim:
         prog.load(texts, extra_functions=("interp",))
         prog.define("currentgrid", self._currentgrid)
         prog.define("syncall", lambda: None)
-        prog.define("syncboxes", self._syncboxes)
         prog.define("save1dvariable", lambda *a: None)
         prog.define("save2dvariable", lambda *a: None)
         prog.define("sync", lambda *a: None)
@@ -313,15 +312,6 @@ class RefSim:
             self.M.zminl[b, lev] = fs.fget(z, (0, 1 - g))
             self.M.zmaxl[b, lev] = fs.fget(z, (0, nzb))
 
-    def _syncboxes(self, b1, b2, level, all_):
-        """syncboxes.f90:48-52: boxes that do not overlap on a level do
-        nothing; the overlap copy is outside the golden-vector scope."""
-        M = self.M
-        if (M.rmaxl[b1, level] < M.rminl[b2, level] or M.rmaxl[b2, level] < M.rminl[b1, level] or
-                M.zmaxl[b1, level] < M.zminl[b2, level] or M.zmaxl[b2, level] < M.zminl[b1, level]):
-            return
-        raise NotImplementedError("intersecting refinement boxes are outside the golden-vector scope")
-
     def _currentgrid(self, box, level, localgrid):
         M = self.M
         s = lambda k, v: object.__setattr__(M, k, v)
@@ -389,7 +379,7 @@ class RefSim:
             for b1 in range(int(M.nb) + 1):
                 for b2 in range(int(M.nb) + 1):
                     if b1 != b2 and M.nl[b1] >= level and M.nl[b2] >= level:
-                        self._syncboxes(b1, b2, level, True)
+                        F.syncboxes(b1, b2, level, True)
         # evolve.f90:228-230; no analysis has run, so va_rp/va_zp are zero
         if M.slicing == "maximal" or M.ilapse == "maximal" or M.maximalevery != 0:
             F.maximalslicing()
