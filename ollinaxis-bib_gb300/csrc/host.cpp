@@ -13,6 +13,7 @@
 // The boundary history var_bound_* of the reference is the strip of the
 // state at the start of the current (p) and previous (pp) step, so it is read
 // straight from those slots.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -65,6 +66,23 @@ struct DLevel {
     // solve has replaced the lapse and no ``auxiliary`` has run since
     double* alpha_aux = nullptr;
     bool alpha_stale = false;
+    // syncboxes: this grid's state before the copies of its level (kept for
+    // the partner's next first stage and its own), the map of the points
+    // another box copies onto it (offset in the partner's state, or -1), the
+    // partner grid, and whether the copy has happened since the last
+    // ``auxiliary``
+    double* snap = nullptr;
+    int* smap = nullptr;
+    int spartner = -1;
+    bool sync_pending = false;
+};
+
+// One ``syncboxes`` copy onto grid p from grid q (same level), in the order
+// of onestep.f90:452-464.
+struct SyncPair {
+    int p = -1, q = -1;
+    XferPt* tab = nullptr;
+    int ntab = 0;
 };
 
 }  // namespace
@@ -77,6 +95,7 @@ struct ollin_handle {
     int nl[4] = {0, 0, 0, 0}, nrbox[4] = {0, 0, 0, 0}, nzbox[4] = {0, 0, 0, 0};
     double rbox[4] = {0, 0, 0, 0}, zbox[4] = {0, 0, 0, 0};
     std::vector<DLevel> L;
+    std::vector<SyncPair> sync;  // nonempty copies, in the reference's order
     std::vector<double> t, t1, t2, rminl, rmaxl, zminl, zmaxl;
     std::vector<long> s;
     std::vector<int> fields;  // active field slots
@@ -350,6 +369,7 @@ int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0) {
     }
     L.last_aux_t0 = t0;
     L.alpha_stale = false;
+    L.sync_pending = false;
     return OLLIN_OK;
 }
 
@@ -373,6 +393,15 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
     a.rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
     a.nanflag = h->d_flag;
     a.alpha_aux = L.alpha_stale ? base_ptr(L, L.alpha_aux) : nullptr;
+    if (L.sync_pending) {
+        const DLevel& Q = h->L[L.spartner];
+        a.smap = L.smap + (L.g - 1) + (size_t)(L.g - 1) * L.ld;
+        for (int f = 0; f < NFIELDS; ++f) {
+            a.xa[f] = base_ptr(L, L.snap + (size_t)f * L.n);
+            a.xb[f] = base_ptr(Q, Q.snap + (size_t)f * Q.n);
+        }
+        a.xb_ld = Q.ld;
+    }
     return a;
 }
 
@@ -380,6 +409,7 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
 // the lapse quantities of the last ``auxiliary`` call from alpha_aux
 void launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
     if (a.alpha_aux) launch_rhs_stale(a, s);
+    else if (a.smap) launch_rhs_sync(a, s);
     else launch_rhs(a, s);
 }
 
@@ -622,11 +652,12 @@ int step_grid(ollin_handle* h, int level) {
     return OLLIN_OK;
 }
 
+int sync_level(ollin_handle* h, int level);
+
 // onestep.f90:2-522: a step of every box that has this level (boxes 0..Nb),
-// two steps of the next level, then each box restricts into its parent
-// with the parent's symmetries and ``auxiliary`` (:472-514).  Boxes that
-// overlap are refused at create, so ``syncboxes`` (:446-466) has nothing
-// to copy.
+// two steps of the next level, the ``syncboxes`` copies between boxes that
+// overlap on this level (:446-466), then each box restricts into its parent
+// with the parent's symmetries and ``auxiliary`` (:472-514).
 int onestep(ollin_handle* h, int level) {
     for (int k = 0; k < h->nlev; ++k) {
         if (h->L[k].level != level) continue;
@@ -640,6 +671,8 @@ int onestep(ollin_handle* h, int level) {
         if (rc) return rc;
     }
     if (level > 0) {
+        int rc = sync_level(h, level);  // onestep.f90:446-466
+        if (rc) return rc;
         for (int k = 0; k < h->nlev; ++k) {
             if (h->L[k].level != level || h->s[k] % 2 != 0) continue;
             int rc = restrict_level(h, k);
@@ -655,23 +688,152 @@ int onestep(ollin_handle* h, int level) {
     return OLLIN_OK;
 }
 
-// syncboxes.f90:48-52 on every level: the grids of two boxes on one level
-// may not overlap (their overlap copy, which also carries the auxiliary
-// arrays, is not built)
-int check_boxes_apart(ollin_handle* h) {
-    for (int a = 0; a < h->nlev; ++a)
-        for (int b = a + 1; b < h->nlev; ++b) {
-            if (h->L[a].level != h->L[b].level || h->L[a].box == h->L[b].box) continue;
-            const bool apart = h->rmaxl[a] < h->rminl[b] || h->rmaxl[b] < h->rminl[a] || h->zmaxl[a] < h->zminl[b] ||
-                               h->zmaxl[b] < h->zminl[a];
-            if (!apart)
-                return fail(OLLIN_EINVAL, "refinement boxes " + std::to_string(h->L[a].box) + " and " +
-                                              std::to_string(h->L[b].box) + " overlap on level " +
-                                              std::to_string(h->L[a].level) + " (syncboxes is not supported)");
+// ``syncboxes`` tables of every ordered pair of boxes on a level that
+// overlap (onestep.f90:446-466).  The device reproduces the copy and, for
+// the next first stage, the auxiliary quantities it carries: that needs each
+// copied point to coincide with a node of the partner, one partner per grid,
+// and no copied point to be read by a later copy of the same level.
+int build_sync_tables(ollin_handle* h) {
+    for (int level = 1; level <= h->nlmax; ++level)
+        for (int p = 0; p < h->nlev; ++p) {
+            if (h->L[p].level != level) continue;
+            for (int q = 0; q < h->nlev; ++q) {
+                if (q == p || h->L[q].level != level) continue;
+                if (h->rmaxl[p] < h->rminl[q] || h->rmaxl[q] < h->rminl[p] || h->zmaxl[p] < h->zminl[q] ||
+                    h->zmaxl[q] < h->zminl[p])
+                    continue;  // syncboxes.f90:48-52
+                DLevel& P = h->L[p];
+                SyncTableArgs a{};
+                a.P = P.G; a.Q = h->L[q].G;
+                a.rminl_p = h->rminl[p]; a.rmaxl_p = h->rmaxl[p]; a.zminl_p = h->zminl[p]; a.zmaxl_p = h->zmaxl[p];
+                a.rminl_q = h->rminl[q]; a.rmaxl_q = h->rmaxl[q]; a.zminl_q = h->zminl[q]; a.zmaxl_q = h->zmaxl[q];
+                a.bicubic = h->P.interp_bicubic;
+                const int n = sync_table_size(P.G);
+                std::vector<XferPt> host(n);
+                XferPt* tab = nullptr;
+                if (cudaMalloc(&tab, (size_t)n * sizeof(XferPt)) != cudaSuccess)
+                    return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes tables");
+                launch_sync_table(a, tab, h->stream);
+                int rc = after_launch(h);
+                if (rc) { cudaFree(tab); return rc; }
+                CUDA_OR_FAIL(cudaMemcpyAsync(host.data(), tab, (size_t)n * sizeof(XferPt), cudaMemcpyDeviceToHost, h->stream));
+                CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+                int used = 0;
+                for (const XferPt& x : host) {
+                    if (x.mode == -1) { cudaFree(tab); return fail(OLLIN_EINVAL, "syncboxes: a stencil leaves the partner box"); }
+                    if (x.o_out == kNoPoint) continue;
+                    ++used;
+                    if (x.depth < 0) {
+                        cudaFree(tab);
+                        return fail(OLLIN_EINVAL, "overlapping boxes whose grid points do not coincide are not supported");
+                    }
+                }
+                if (used == 0) { cudaFree(tab); continue; }
+                if (P.spartner >= 0 && P.spartner != q) {
+                    cudaFree(tab);
+                    return fail(OLLIN_EINVAL, "a grid that overlaps two other boxes on one level is not supported");
+                }
+                P.spartner = q;
+                std::vector<int> map(P.n, -1);
+                for (const XferPt& x : host)
+                    if (x.o_out != kNoPoint) map[(size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld] = x.depth;
+                if (!P.smap && cudaMalloc(&P.smap, P.n * sizeof(int)) != cudaSuccess) {
+                    cudaFree(tab);
+                    return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes map");
+                }
+                CUDA_OR_FAIL(cudaMemcpy(P.smap, map.data(), P.n * sizeof(int), cudaMemcpyHostToDevice));
+                SyncPair sp;
+                sp.p = p; sp.q = q; sp.tab = tab; sp.ntab = n;
+                h->sync.push_back(sp);
+            }
+        }
+    // a later copy of the level may not read a point an earlier one wrote
+    for (size_t k = 0; k < h->sync.size(); ++k)
+        for (size_t e = k + 1; e < h->sync.size(); ++e) {
+            const SyncPair& w = h->sync[k];
+            const SyncPair& r = h->sync[e];
+            if (r.q != w.p) continue;
+            std::vector<XferPt> hr(r.ntab);
+            std::vector<int> map(h->L[w.p].n);
+            CUDA_OR_FAIL(cudaMemcpy(hr.data(), r.tab, (size_t)r.ntab * sizeof(XferPt), cudaMemcpyDeviceToHost));
+            CUDA_OR_FAIL(cudaMemcpy(map.data(), h->L[w.p].smap, map.size() * sizeof(int), cudaMemcpyDeviceToHost));
+            const DLevel& W = h->L[w.p];
+            const size_t shift = (size_t)(W.g - 1) + (size_t)(W.g - 1) * W.ld;
+            for (const XferPt& x : hr) {
+                if (x.o_out == kNoPoint) continue;
+                for (int di = -1; di <= 2; ++di)
+                    for (int dj = -1; dj <= 2; ++dj) {
+                        const long o = (long)(x.i0 + di) + (long)(x.j0 + dj) * W.ld + (long)shift;
+                        if (o >= 0 && o < (long)W.n && map[(size_t)o] >= 0)
+                            return fail(OLLIN_EINVAL, "syncboxes: a copy reads points another copy of the level wrote");
+                    }
+            }
+        }
+    for (const SyncPair& sp : h->sync)
+        for (int g2 : {sp.p, sp.q}) {
+            DLevel& G = h->L[g2];
+            if (!G.snap && cudaMalloc(&G.snap, (size_t)NFIELDS * G.n * sizeof(double)) != cudaSuccess)
+                return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes state");
         }
     return OLLIN_OK;
 }
 
+// The copies of one level (syncboxes.f90): the state of every grid involved
+// is kept first, then each copy takes the evolved fields and the stored
+// auxiliary quantities, and the targets' next first stage reads the kept
+// states (StageArgs::smap).
+int sync_level(ollin_handle* h, int level) {
+    bool any = false;
+    for (const SyncPair& sp : h->sync)
+        if (h->L[sp.p].level == level) any = true;
+    if (!any) return OLLIN_OK;
+    std::vector<int> kept;
+    for (const SyncPair& sp : h->sync) {
+        if (h->L[sp.p].level != level) continue;
+        for (int g2 : {sp.p, sp.q}) {
+            if (std::find(kept.begin(), kept.end(), g2) != kept.end()) continue;
+            kept.push_back(g2);
+            DLevel& G = h->L[g2];
+            for (int f : h->fields)
+                CUDA_OR_FAIL(cudaMemcpyAsync(G.snap + (size_t)f * G.n, G.slot[G.cur][f], G.n * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, h->stream));
+        }
+    }
+    static const int kSyncAux[] = {X_GA, X_GB, X_GH, X_GC, X_KTH, X_LAM, X_ALAM, X_GLAM, X_DELDEFR, X_DELDEFZ, X_GDR, X_GDZ};
+    for (const SyncPair& sp : h->sync) {
+        if (h->L[sp.p].level != level) continue;
+        DLevel& P = h->L[sp.p];
+        DLevel& Q = h->L[sp.q];
+        for (int part = 0; part < 2; ++part) {
+            RestrictArgs a{};
+            a.F = Q.G;
+            a.Cg = P.G;
+            a.nf = 0;
+            if (part == 0) {
+                for (int f : active_fields(h, h->t[sp.p] == 0.0)) {
+                    a.fid[a.nf] = a.nf;
+                    a.fin[a.nf] = base_ptr(Q, Q.slot[Q.cur][f]);
+                    a.cout[a.nf] = base_ptr(P, P.slot[P.cur][f]);
+                    ++a.nf;
+                }
+            } else {
+                for (int x : kSyncAux) {
+                    a.fid[a.nf] = a.nf;
+                    a.fin[a.nf] = base_ptr(Q, Q.aux[x]);
+                    a.cout[a.nf] = base_ptr(P, P.aux[x]);
+                    ++a.nf;
+                }
+            }
+            a.tab = sp.tab;
+            a.ntab = sp.ntab;
+            launch_restrict_tab(a, h->stream);
+            int rc = after_launch(h);
+            if (rc) return rc;
+        }
+        P.sync_pending = true;
+    }
+    return OLLIN_OK;
+}
 int internal_field(int field, bool* is_aux) {
     *is_aux = false;
     switch (field) {
@@ -1860,7 +2022,7 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
             return rc;
         }
     }
-    rc = check_boxes_apart(h);
+    rc = build_sync_tables(h);
     if (rc) {
         ollin_gpu_destroy(h);
         return rc;
@@ -1882,7 +2044,10 @@ void ollin_gpu_destroy(ollin_handle* h) {
         if (L.ptab) cudaFree(L.ptab);
         if (L.rtab) cudaFree(L.rtab);
         if (L.alpha_aux) cudaFree(L.alpha_aux);
+        if (L.snap) cudaFree(L.snap);
+        if (L.smap) cudaFree(L.smap);
     }
+    for (SyncPair& sp : h->sync) cudaFree(sp.tab);
     if (h->d_flag) cudaFree(h->d_flag);
     if (h->d_norm) cudaFree(h->d_norm);
     for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
@@ -1978,6 +2143,10 @@ int ollin_gpu_initialize(ollin_handle* h) {
             int rc = after_launch(h);
             if (rc) return rc;
         }
+    }
+    for (int level = 1; level <= h->nlmax; ++level) {  // evolve.f90:211-219
+        int rc = sync_level(h, level);
+        if (rc) return rc;
     }
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     h->initialized = true;

@@ -46,6 +46,22 @@ struct StageArgs {
     // derivatives of the lapse come from it, the lapse itself and the
     // gradient that maximalslicing.f90:156-170 recomputes from the new one.
     const double* alpha_aux;
+    // The first stage after ``syncboxes`` copied another box's data onto this
+    // grid (launch_rhs_sync only): smap[o] >= 0 marks a copied point and its
+    // offset in the partner's state xb (leading dimension xb_ld); the other
+    // points read this grid's state before the copy, xa.
+    const int* smap;
+    const double* xa[NFIELDS];
+    const double* xb[NFIELDS];
+    long xb_ld;
+};
+
+// Table of a ``syncboxes`` copy onto grid P from grid Q of the same level.
+struct SyncTableArgs {
+    LevelGeom P, Q;
+    double rminl_p, rmaxl_p, zminl_p, zmaxl_p;
+    double rminl_q, rmaxl_q, zminl_q, zmaxl_q;
+    int bicubic;
 };
 
 // Pointwise auxiliary quantities (auxiliary_geometry.f90 pointwise parts).
@@ -307,6 +323,9 @@ void launch_pulse_coeffs(const PulseCoeffArgs& a, cudaStream_t s);
 
 void launch_rhs(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale(const StageArgs& a, cudaStream_t s);
+void launch_rhs_sync(const StageArgs& a, cudaStream_t s);
+int sync_table_size(const LevelGeom& P);
+void launch_sync_table(const SyncTableArgs& a, XferPt* tab, cudaStream_t s);
 // maximal slicing (elliptic.cu)
 int max_coeff_blocks(const LevelGeom& G);
 void launch_max_coeffs(const MaxCoeffArgs& a, cudaStream_t s);

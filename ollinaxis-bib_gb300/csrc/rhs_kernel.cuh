@@ -34,7 +34,7 @@ __device__ __forceinline__ bool nonfinite(double x) {
 
 struct Deriv5 { double r, z, rr, zz, rz; };
 
-template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE>
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
 #ifndef OLLIN_RHS_THREADS
 #define OLLIN_RHS_THREADS 128
 #endif
@@ -54,21 +54,38 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
     const double cr2 = G.idr * G.idr * (1.0 / 12.0), cz2 = G.idz * G.idz * (1.0 / 12.0);
     const double idrz = G.idr * G.idz;
-    const int pcr = pclass(i, nr, g), pcz = pclass(j, nz, g);
+    // The state the derivatives and the point values of this stage are taken
+    // from: the stage input, except in the first stage after ``syncboxes``
+    // (SYNC), whose auxiliary quantities the reference still holds from
+    // before the copy -- the grid's own state before it at the points not
+    // copied, the partner box's state (a point well inside it, so interior
+    // stencils) at the copied ones.  Dissipation reads the stage input.
+    const double* const* X = A.in;
+    size_t ox = o;
+    long ldx = ld;
+    bool xin = false;  // a copied point: stencils of the partner's interior
+    if constexpr (SYNC) {
+        const int m = A.smap[o];
+        if (m >= 0) { X = A.xb; ox = (size_t)m; ldx = A.xb_ld; xin = true; }
+        else X = A.xa;
+    }
+    const int pcr = xin ? 0 : pclass(i, nr, g), pcz = xin ? 0 : pclass(j, nz, g);
+    // edge position of the mixed derivative: an interior point when copied
+    const int ir_ = xin ? 4 : i, jr_ = xin ? 4 : j, nr_ = xin ? (1 << 20) : nr, nz_ = xin ? (1 << 20) : nz;
 
-    auto val = [&](int f) { return ld_(A.in[f] + o); };
+    auto val = [&](int f) { return ld_(X[f] + ox); };
     auto D5p = [&](const double* p) {
         Deriv5 d;
         d.r = d1(p, 1, pcr, cr1);
-        d.z = d1(p, ld, pcz, cz1);
+        d.z = d1(p, ldx, pcz, cz1);
         d.rr = d2(p, 1, pcr, cr2);
-        d.zz = d2(p, ld, pcz, cz2);
-        d.rz = d2rz(p, ld, i, j, nr, nz, g, idrz);
+        d.zz = d2(p, ldx, pcz, cz2);
+        d.rz = d2rz(p, ldx, ir_, jr_, nr_, nz_, g, idrz);
         return d;
     };
-    auto D5 = [&](int f) { return D5p(A.in[f] + o); };
-    auto Dr = [&](int f) { return d1(A.in[f] + o, 1, pcr, cr1); };
-    auto Dz = [&](int f) { return d1(A.in[f] + o, ld, pcz, cz1); };
+    auto D5 = [&](int f) { return D5p(X[f] + ox); };
+    auto Dr = [&](int f) { return d1(X[f] + ox, 1, pcr, cr1); };
+    auto Dz = [&](int f) { return d1(X[f] + ox, ldx, pcz, cz1); };
     auto aux = [&](int x) { return ld_(A.aux[x] + o); };
 
     const double r = G.rcol[i], ir = G.ircol[i];
@@ -226,14 +243,14 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         // stencils are one 5-point sum taken with the stride pointing against
         // the shift, and beta times its scale is -|beta|/(12 h) for either
         // sign, so each field costs one stencil and one FMA per direction.
-        const bool lint_r = (i >= 4 - g && i <= nr - 3), lint_z = (j >= 4 - g && j <= nz - 3);
-        const long lsr = negr ? -1 : 1, lsz = negz ? -ld : ld;
+        const bool lint_r = xin || (i >= 4 - g && i <= nr - 3), lint_z = xin || (j >= 4 - g && j <= nz - 3);
+        const long lsr = negr ? -1 : 1, lsz = negz ? -ldx : ldx;
         const double kr = -fabs(br) * (G.idr * (1.0 / 12.0)), kz = -fabs(bz) * (G.idz * (1.0 / 12.0));
         auto lop = [&](const double* p, long st) {
             return 3.0 * ld_(p - st) + 10.0 * ld_(p) - 18.0 * ld_(p + st) + 6.0 * ld_(p + 2 * st) - ld_(p + 3 * st);
         };
         auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * dadv(p, 1, i, nr, g, negr, G.idr, false); };
-        auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ld, j, nz, g, negz, G.idz, true); };
+        auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ldx, j, nz, g, negz, G.idz, true); };
         // shiftadvect is a template parameter: with it on, the centred
         // derivatives need not stay live for this block
         auto ADVp = [&](const double* p, double dr_, double dz_) {
@@ -244,11 +261,11 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
                 return ladv_r(p) + ladv_z(p);
             }
         };
-        auto ADV = [&](int f, double dr_, double dz_) { return ADVp(A.in[f] + o, dr_, dz_); };
+        auto ADV = [&](int f, double dr_, double dz_) { return ADVp(X[f] + ox, dr_, dz_); };
         // DD_beta_rr = d/dr (beta_r / r): first derivative of beta_r/r
         double DD_beta_rr;
         {
-            const double* pb = A.in[F_BETAR] + o;
+            const double* pb = X[F_BETAR] + ox;
             const double* ic = G.ircol + i;
             auto q = [&](int m) { return ld_(pb + m) * ic[m]; };
             if (pcr == 0) DD_beta_rr = cr1 * (8.0 * (q(1) - q(-1)) - (q(2) - q(-2)));
@@ -287,7 +304,7 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         s_Dlz = s_Dlz + two * rgC * dbZ.rz + gA * dbZ.rr + gB * dbZ.zz + gH * Drbz * ir;
         s_Dlz = s_Dlz + third * (rgC * Dr_DIV_beta + gB * Dz_DIV_beta) + Dlz * tdb;
         if (bona_masso)
-            s_alpha = s_alpha + ADVp(STALE ? A.alpha_aux + o : A.in[F_ALPHA] + o, dao.r, dao.z);
+            s_alpha = s_alpha + ADVp(STALE ? A.alpha_aux + o : X[F_ALPHA] + ox, dao.r, dao.z);
         s_br = dbr;
         s_bz = dbz;
         if (P.driveradv) {
@@ -298,7 +315,7 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         if constexpr (SCALAR) {
             // auxiliary_matter.f90 always forms lopsided derivatives for the
             // scalar field when a shift is present (independent of shiftadvect)
-            auto LADV = [&](int f) { const double* p = A.in[f] + o; return ladv_r(p) + ladv_z(p); };
+            auto LADV = [&](int f) { const double* p = X[f] + ox; return ladv_r(p) + ladv_z(p); };
             const double sxr = val(F_SXIR), sxz = val(F_SXIZ);
             s_sphi = s_sphi + br * sxr + bz * sxz;
             s_sxr = s_sxr + LADV(F_SXIR) + sxr * Drb + sxz * Drbz;
@@ -375,8 +392,12 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         if (P.driveradv) {
             const double br = val(F_BETAR), bz = val(F_BETAZ);
             const bool negr = br <= 0.0, negz = bz <= 0.0;
-            auto DAr = [&](int f) { return ADVECT ? dadv(A.in[f] + o, 1, i, nr, g, negr, G.idr, false) : Dr(f); };
-            auto DAz = [&](int f) { return ADVECT ? dadv(A.in[f] + o, ld, j, nz, g, negz, G.idz, true) : Dz(f); };
+            auto DAr = [&](int f) {
+                return ADVECT ? dadv(X[f] + ox, 1, xin ? 4 : i, xin ? (1 << 20) : nr, g, negr, G.idr, false) : Dr(f);
+            };
+            auto DAz = [&](int f) {
+                return ADVECT ? dadv(X[f] + ox, ldx, xin ? 4 : j, xin ? (1 << 20) : nz, g, negz, G.idz, true) : Dz(f);
+            };
             s_dbr = s_dbr + br * (DAr(F_DTBETAR) - DAr(F_DLR)) + bz * (DAz(F_DTBETAR) - DAz(F_DLR));
             s_dbz = s_dbz + br * (DAr(F_DTBETAZ) - DAr(F_DLZ)) + bz * (DAz(F_DTBETAZ) - DAz(F_DLZ));
         }

@@ -244,6 +244,60 @@ __global__ void __launch_bounds__(128) prolong_table_kernel(const __grid_constan
     tab[t] = x;
 }
 
+// ``syncboxes`` (syncboxes.f90:48-216): the strips of grid P up to 3*ghost
+// deep in the order rR, rL (P off the axis), zR, zL (P off the equator or no
+// equatorial symmetry), at the points well inside grid Q, interpolated from
+// Q (intersect_interp.inc).  ``depth`` holds the offset of the Q node the
+// point coincides with (to rounding), or -1.
+__global__ void __launch_bounds__(128) sync_table_kernel(const __grid_constant__ SyncTableArgs a, XferPt* tab) {
+    const LevelGeom& F = a.P;
+    const LevelGeom& Q = a.Q;
+    const int g = F.g;
+    const int imax = 3 * g;
+    const int nstrip_r = (imax + 1) * (F.nz + g);
+    const int nstrip_z = (imax + 1) * (F.nr + g);
+    const int nr_strips = F.lower_r ? 2 : 1, nz_strips = F.lower_z ? 2 : 1;
+    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (t >= nr_strips * nstrip_r + nz_strips * nstrip_z) return;
+    double r0, z0;
+    if (t < nr_strips * nstrip_r) {
+        const int q = t % nstrip_r;
+        const int m = q / (F.nz + g), n = q % (F.nz + g);
+        r0 = (t < nstrip_r) ? sub(a.rmaxl_p, mul((double)m, F.dr)) : add(a.rminl_p, mul((double)m, F.dr));
+        z0 = add(a.zminl_p, mul((double)n, F.dz));
+    } else {
+        const int q0 = t - nr_strips * nstrip_r;
+        const int q = q0 % nstrip_z;
+        const int n = q / (F.nr + g), m = q % (F.nr + g);
+        r0 = add(a.rminl_p, mul((double)m, F.dr));
+        z0 = (q0 < nstrip_z) ? sub(a.zmaxl_p, mul((double)n, F.dz)) : add(a.zminl_p, mul((double)n, F.dz));
+    }
+    XferPt x{};
+    x.o_out = kNoPoint;
+    x.depth = -1;
+    const double deltar = mul((double)(3 * g), F.dr), deltaz = mul((double)(3 * g), F.dz);
+    if (r0 >= add(a.rminl_q, deltar) && r0 <= sub(a.rmaxl_q, deltar) && z0 >= add(a.zminl_q, deltaz) &&
+        z0 <= sub(a.zmaxl_q, deltaz)) {
+        const int i = (int)round((r0 - F.rcol[1 - g]) / F.dr) + 1 - g;
+        const int j = (int)round((z0 - F.zrow[1 - g]) / F.dz) + 1 - g;
+        if (i >= 1 - g && i <= F.nr && j >= 1 - g && j <= F.nz) {
+            InterpPt p;
+            if (interp_weights(Q, a.rminl_q, a.rmaxl_q, a.zminl_q, a.zmaxl_q, r0, z0, a.bicubic, p)) {
+                to_xfer(p, x);
+                x.o_out = i + j * F.ld;
+                // the coinciding Q node
+                const double er = (r0 - Q.rcol[p.i0]) / Q.dr, ez = (z0 - Q.zrow[p.j0]) / Q.dz;
+                const int ni = fabs(er) < 1e-9 ? p.i0 : (fabs(er - 1.0) < 1e-9 ? p.i0 + 1 : -1 << 30);
+                const int nj = fabs(ez) < 1e-9 ? p.j0 : (fabs(ez - 1.0) < 1e-9 ? p.j0 + 1 : -1 << 30);
+                if (ni >= 1 - g && ni <= Q.nr && nj >= 1 - g && nj <= Q.nz) x.depth = ni + nj * Q.ld;
+            } else {
+                x.mode = -1;
+            }
+        }
+    }
+    tab[t] = x;
+}
+
 // thread per (stencil, field); the strips of a smaller imax are the entries
 // with depth <= imax
 __global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant__ ProlongArgs a) {
@@ -446,6 +500,15 @@ void launch_symmetry(const SymArgs& a, cudaStream_t s) {
 
 int prolong_table_size(const LevelGeom& F) {
     return (F.lower_r ? 2 : 1) * (F.g + 3) * (F.nz + F.g) + (F.lower_z ? 2 : 1) * (F.g + 3) * (F.nr + F.g);
+}
+
+int sync_table_size(const LevelGeom& P) {
+    return (P.lower_r ? 2 : 1) * (3 * P.g + 1) * (P.nz + P.g) + (P.lower_z ? 2 : 1) * (3 * P.g + 1) * (P.nr + P.g);
+}
+
+void launch_sync_table(const SyncTableArgs& a, XferPt* tab, cudaStream_t s) {
+    const int n = sync_table_size(a.P);
+    sync_table_kernel<<<(n + 127) / 128, 128, 0, s>>>(a, tab);
 }
 
 void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s) {

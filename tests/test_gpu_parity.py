@@ -165,11 +165,40 @@ def test_refinement_boxes(cfg):
                 assert abs(ng[k] - no[k]) <= 1e-8 * scale, (lev, nm, k, ng[k], no[k])
 
 
-def test_overlapping_boxes_are_refused():
+# box 0's level 1 around the origin and box 1 on the axis above it overlap
+# on level 1 (syncboxes.f90)
+OVERLAP = dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
+
+
+@pytest.mark.parametrize("cfg", [OVERLAP, dict(OVERLAP, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)],
+                         ids=["overlap", "overlap_shift"])
+def test_overlapping_boxes(cfg):
+    """syncboxes copies the evolved and auxiliary arrays of the partner box
+    on each box's strips; the next first stage reads the auxiliary
+    quantities from before the copy (the own grid) and from the partner at
+    the copied points."""
+    o, e = make_pair(cfg)
+    for k in range(1, 7):
+        assert o.step() == e.step()
+        got = {(lev, nm): e.download(lev, nm) for lev in o.levels() for nm in field_list(cfg)}
+        ref = {(lev, nm): o.get(lev, nm) for lev in o.levels() for nm in field_list(cfg)}
+        for nm in field_list(cfg):
+            hscale = max(float(abs(ref[(lev, nm)]).max()) for lev in o.levels())
+            for lev in o.levels():
+                d = e.desc(lev)
+                scale = max(hscale, 1e-300)
+                if nm in ("lambda", "Alambda"):
+                    scale = max(scale, 1e-3 / (d.dr * d.dz))
+                err = float(abs(got[(lev, nm)] - ref[(lev, nm)]).max()) / scale
+                assert err <= tol_for(nm), "step %d grid %d %s: rel diff %.3e" % (k, lev, nm, err)
+
+
+def test_overlap_between_staggered_grids_is_refused():
+    """With Nzbox - ghost + 1 odd the box's z nodes fall between those of box
+    0, so syncboxes interpolates; the device copies coinciding nodes only."""
     from ollin.gpu import Evolution, OllinError
-    cfg = dict(BOXES, nl0=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
     with pytest.raises(OllinError):
-        Evolution(params(cfg))
+        Evolution(params(dict(OVERLAP, Nzbox1=17)))
 
 
 def test_norms_match_oracle():
