@@ -759,14 +759,13 @@ int build_sync_tables(ollin_handle* h) {
             CUDA_OR_FAIL(cudaMemcpy(map.data(), h->L[w.p].smap, map.size() * sizeof(int), cudaMemcpyDeviceToHost));
             const DLevel& W = h->L[w.p];
             const size_t shift = (size_t)(W.g - 1) + (size_t)(W.g - 1) * W.ld;
+            // the copy reads the node it coincides with (the other weights
+            // of a near-node stencil are rounding)
             for (const XferPt& x : hr) {
                 if (x.o_out == kNoPoint) continue;
-                for (int di = -1; di <= 2; ++di)
-                    for (int dj = -1; dj <= 2; ++dj) {
-                        const long o = (long)(x.i0 + di) + (long)(x.j0 + dj) * W.ld + (long)shift;
-                        if (o >= 0 && o < (long)W.n && map[(size_t)o] >= 0)
-                            return fail(OLLIN_EINVAL, "syncboxes: a copy reads points another copy of the level wrote");
-                    }
+                const size_t o = (size_t)x.depth + shift;
+                if (o < W.n && map[o] >= 0)
+                    return fail(OLLIN_EINVAL, "syncboxes: a copy reads a point another copy of the level wrote");
             }
         }
     for (const SyncPair& sp : h->sync)
