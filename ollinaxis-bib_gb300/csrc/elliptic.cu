@@ -575,12 +575,21 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
         const size_t o = (size_t)i + (size_t)j * ld;
         double r = 0.0;
         if (i <= nr - 1 && j <= nz - 1) {
-            const double R = A.ca[i] * U(i + 1, j) + A.cb[i] * U(i - 1, j) + A.cc * (U(i, j + 1) + U(i, j - 1))
-                             + A.e64[o] * U(i, j) - A.f64[o];
+            double R;
+            if (!A.pa) {
+                R = A.ca[i] * U(i + 1, j) + A.cb[i] * U(i - 1, j) + A.cc * (U(i, j + 1) + U(i, j - 1))
+                    + A.e64[o] * U(i, j) - A.f64[o];
+            } else {
+                R = A.pa[o] * U(i + 1, j) + A.pb[o] * U(i - 1, j) + A.pc[o] * U(i, j + 1) + A.pd[o] * U(i, j - 1)
+                    + A.pg[o] * U(i + 1, j + 1) + A.ph[o] * U(i - 1, j - 1) + A.pi[o] * U(i + 1, j - 1)
+                    + A.pj[o] * U(i - 1, j + 1) + A.e64[o] * U(i, j) - A.f64[o];
+            }
             r = -R;
             sq = r * r;
             const double eu = A.e64[o] * U(i, j);
             sc = eu * eu;
+            // the flat correction equation sees the physical operator times psi^4
+            if (A.pa) r = r * A.psi4[o];
         } else if (A.robin) {
             const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
             double R;
@@ -614,6 +623,17 @@ __global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_co
     A.u[o] = A.u[o] + (double)A.d[o];
 }
 
+// diagonal of the flat correction operator for the physical Laplacian:
+// the flat stencil's centre plus psi^4 S1
+__global__ void mix_diag_phys_kernel(LevelGeom G, float* e32, double ec, const double* S1, const double* psi4) {
+    const int g = G.g;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    e32[o] = (float)(ec + S1[o] * psi4[o]);
+}
+
 __global__ void to_float_kernel(LevelGeom G, float* out, const double* in) {
     const int g = G.g;
     const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -640,6 +660,13 @@ void launch_mix_update(const MixArgs& a, cudaStream_t s) {
     dim3 blk(32, 4);
     dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz + blk.y - 1) / blk.y);
     mix_update_kernel<<<grd, blk, 0, s>>>(a);
+}
+
+void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const double* S1, const double* psi4,
+                          cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+    mix_diag_phys_kernel<<<grd, blk, 0, s>>>(G, e32, ec, S1, psi4);
 }
 
 void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s) {

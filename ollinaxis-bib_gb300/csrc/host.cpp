@@ -1517,7 +1517,7 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     launch_add(L.G, base_ptr(L, eaux), ec, base_ptr(L, w.S1), h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
-    const bool s5 = P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
+    const bool s5 = !S.physical && P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
     const int nparts = mix_blocks(L.G);
     if (S.nparts < 2 * nparts) {
         cudaFree(S.partial);
@@ -1526,10 +1526,37 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
             return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
         S.nparts = 2 * nparts;
     }
+    // maximal slicing: the nine-point stencil of the physical Laplacian
+    double* phys = nullptr;
+    struct FreePhys { double* p; ~FreePhys() { cudaFree(p); } } free_phys{nullptr};
+    if (S.physical) {
+        if (cudaMalloc(&phys, (9 * L.n + 1) * sizeof(double)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
+        free_phys.p = phys;
+        CUDA_OR_FAIL(cudaMemsetAsync(phys, 0, (9 * L.n + 1) * sizeof(double), h->stream));
+    }
     MixArgs a{};
     a.G = L.G;
     a.u = base_ptr(L, w.u[w.cur]);
     a.e64 = base_ptr(L, s5 ? e : eaux);
+    if (S.physical) {
+        double* q[9];
+        for (int k = 0; k < 9; ++k) q[k] = base_ptr(L, phys + (size_t)k * L.n);
+        SorCoeffArgs c{};
+        c.G = L.G;
+        c.ph = w.ph;
+        c.S1 = base_ptr(L, w.S1);
+        c.fine = level > 0 ? 1 : 0;
+        c.a = q[0]; c.b = q[1]; c.c = q[2]; c.d = q[3]; c.e = q[4];
+        c.cg = q[5]; c.ch = q[6]; c.ci = q[7]; c.cj = q[8];
+        c.diag_nonzero = reinterpret_cast<unsigned long long*>(phys + 9 * L.n);  // not needed here
+        launch_sor_coeffs(c, h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        a.pa = q[0]; a.pb = q[1]; a.pc = q[2]; a.pd = q[3]; a.e64 = q[4];
+        a.pg = q[5]; a.ph = q[6]; a.pi = q[7]; a.pj = q[8];
+        a.psi4 = w.ph.psi4;
+    }
     a.f64 = base_ptr(L, w.S0);
     a.ca = dcol + (g - 1);
     a.cb = dcol + ncol + (g - 1);
@@ -1549,7 +1576,8 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
             rc = after_launch(h);
             if (rc) return rc;
         }
-        launch_to_float(L.G, e32, a.e64, h->stream);
+        if (S.physical) launch_mix_diag_phys(L.G, e32, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
+        else launch_to_float(L.G, e32, a.e64, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
         launch_mix_resid(a, h->stream);
@@ -1859,8 +1887,8 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
     if (!P.eqsym) return fail(OLLIN_EINVAL, "maximal slicing on the device needs equatorial symmetry (eqsym)");
     if (h->nb > 0) return fail(OLLIN_EINVAL, "maximal slicing on the device needs Nb = 0");
-    if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
-        return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave or sor");
+    if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
+        return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor or mixed");
     // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)
     for (int l = 0; l < h->nlev; ++l) {
         int rc = analysis(h, l);
@@ -1914,8 +1942,10 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
         const double dt0 = P.we_dtfac * std::min(std::min(P.dr0, P.dz0), std::min(P.dr0 / vrmax, P.dz0 / vzmax));
         for (int l = 0; l < h->nlev; ++l) S.W[l].dt = dt0 / (double)(1L << l);
         rc = wave_elliptic(h, S);
-    } else {
+    } else if (P.ell_solver == OLLIN_ELL_SOR) {
         rc = sor_elliptic(h, S);
+    } else {
+        rc = mixed_elliptic(h, S);
     }
     if (rc) return rc;
     // alpha = ell_u (maximalslicing.f90:148-154)

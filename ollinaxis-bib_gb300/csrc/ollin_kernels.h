@@ -292,7 +292,15 @@ struct MixArgs {
     float* d; float* r32;
     int robin; double uinf;
     double* partial;                                 // per-block sums of squares
+    // physical Laplacian (maximal slicing): the per-point nine-point stencil
+    // of sor_elliptic.f90 (pa..pj; e64 its diagonal) and psi^4, by which the
+    // interior residual is scaled for the flat FP32 correction
+    const double* pa; const double* pb; const double* pc; const double* pd;
+    const double* pg; const double* ph; const double* pi; const double* pj;
+    const double* psi4;
 };
+void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const double* S1, const double* psi4,
+                          cudaStream_t s);
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
 int mix_blocks(const LevelGeom& G);
 void launch_mix_update(const MixArgs& a, cudaStream_t s);
