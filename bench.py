@@ -336,14 +336,39 @@ def elliptic_precision():
         e.close()
         return dt, stats, chi
 
+    def maximal(cfg):
+        """Brill data, one coarse step (K_ij no longer zero), then the
+        maximal-slicing lapse (maximalslicing.f90)."""
+        e = Evolution(params_from_dict(dict(base, maximalevery=1, slicing="1+log", gauge_f=2.0, **cfg)))
+        e.initial_data()
+        e.initialize()
+        e.maximal_slicing()
+        e.step()
+        t = time.perf_counter()
+        e.maximal_slicing()
+        dt = time.perf_counter() - t
+        alpha = e.download(0, "alpha")
+        stats = e.ell_stats()
+        e.close()
+        return dt, stats, alpha
+
     solve(dict(nrtotal=64, nztotal=64, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))  # warm-up
     t_c3, st_c3, _ = solve(dict(nrtotal=1024, nztotal=1024, nl0=3, ell_solver="mixed", ell_epsilon=1e-12))
     t_mx, st_mx, chi_mx = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))
     t_sor, st_sor, chi_sor = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="sor"))
+    tm_c3, sm_c3, a_c3 = maximal(dict(nrtotal=1024, nztotal=1024, nl0=3, ell_solver="mixed", ell_epsilon=1e-12))
+    tm_mx, sm_mx, a_mx = maximal(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))
+    tm_sor, sm_sor, a_sor = maximal(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="sor"))
     return {"workload": "Brill wave a0=1, 4 levels of 1024x1024, dr0=0.04, mixed solver to 1e-12 or the FP64 floor",
             "seconds": t_c3, "refinements_level0": st_c3[0], "vcycles_level0": st_c3[1], "final_rms_residual": st_c3[2],
             "vs_fp64_sor_256": {"mixed_seconds": t_mx, "sor_seconds": t_sor, "sor_iterations": st_sor[0],
-                                "max_abs_chi_diff": float(np.max(np.abs(chi_mx[0] - chi_sor[0])))}}
+                                "max_abs_chi_diff": float(np.max(np.abs(chi_mx[0] - chi_sor[0])))},
+            "maximal_slicing": {"workload": "the same data after one coarse step, maximal lapse by the mixed solver",
+                                "seconds": tm_c3, "refinements_level0": sm_c3[0], "vcycles_level0": sm_c3[1],
+                                "final_rms_residual": sm_c3[2], "min_alpha": float(a_c3.min()),
+                                "vs_fp64_sor_256": {"mixed_seconds": tm_mx, "sor_seconds": tm_sor,
+                                                    "sor_iterations": sm_sor[0],
+                                                    "max_abs_alpha_diff": float(np.max(np.abs(a_mx - a_sor)))}}}
 
 
 def main():
