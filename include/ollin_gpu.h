@@ -244,7 +244,9 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
  * call recomputes only the lapse and its first and second derivatives: the
  * next stage of each level still sees the covariant second derivatives,
  * Laplacian, falpha and advective derivatives of the lapse before the solve.
- * Needs eqsym; OLLIN_EINVAL for ELL_solver = "mixed". */
+ * ELL_solver = "mixed" solves the same discrete system as "sor" with FP64
+ * residuals and FP32 multigrid corrections (no counterpart in the reference).
+ * Needs eqsym and Nb = 0. */
 int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
 
 /* Iterations of the elliptic solve run by ollin_gpu_initial_data for
