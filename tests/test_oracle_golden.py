@@ -209,7 +209,9 @@ def test_oracle_maximal_slicing_matches_reference_fortran(name):
 
 
 def test_golden_fixture_inventory():
-    for name in CASES:
+    """Every fixture the tests name is committed (the elliptic and maximal
+    slicing tests would otherwise skip)."""
+    for name in CASES + ELL_CASES + MAX_CASES:
         d, meta = load(name)
         assert meta["steps"][0] == 0 and len(meta["fields"]) >= 16
         assert "s0_L0_alpha" in d
