@@ -309,6 +309,8 @@ def run_gpu(args):
             line["cpu_baseline"] = cpu_baseline(threads=os.cpu_count(), seconds=args.cpu_seconds)
         if not args.no_elliptic:
             line["elliptic"] = elliptic_precision()
+        if not args.no_batch:
+            line["batch"] = batch_throughput()
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
@@ -371,6 +373,59 @@ def elliptic_precision():
                                                     "max_abs_alpha_diff": float(np.max(np.abs(a_mx - a_sor)))}}}
 
 
+def batch_throughput(n=32, steps=2, seed=7):
+    """The batching pattern: n independent massless scalar-field shells
+    (phi = a exp(-(r - 5)^2), a log-uniform in [0.01, 0.1], seeded; elliptic
+    initial data by the mixed solver), grids of 64^2 to 128^2 per level with
+    2-3 levels (seeded mix), advanced one coarse step at a time either one
+    evolution after another or all together (ollin_gpu_coarse_step_many,
+    every step queued on its own stream).  Host wall time, launches included."""
+    import numpy as np
+    from ollin.gpu import Evolution, step_many
+    from ollin.params import params_from_dict
+    rng = np.random.default_rng(seed)
+    cfgs = []
+    for _ in range(n):
+        size = int(rng.choice([64, 96, 128]))
+        cfgs.append(dict(nrtotal=size, nztotal=size, nl0=int(rng.integers(1, 3)), dr0=16.0 / size, dz0=16.0 / size,
+                         eqsym=1, order="four", integrator="rk4", dtfac=0.25, boundtype="radiative",
+                         idata="scalarpulse", mattertype="scalar", scalarpotential="none", scalarpulse_type="shell",
+                         scalar_a0=float(np.exp(rng.uniform(np.log(0.01), np.log(0.1)))), scalar_r0=5.0,
+                         scalar_sr0=1.0, scalar_sz0=1.0, ilapse="one", slicing="1+log", gauge_f=2.0,
+                         geodiss=0.02, scalardiss=0.02, ell_solver="mixed", ell_epsilon=1e-12))
+
+    def build():
+        es = []
+        for c in cfgs:
+            e = Evolution(params_from_dict(c))
+            e.initial_data()
+            e.initialize()
+            es.append(e)
+        return es
+
+    seq, bat = build(), build()
+    for e in seq:  # warm-up
+        e.step()
+    step_many(bat)
+    p0 = sum(e.point_updates() for e in seq)
+    t = time.perf_counter()
+    for _ in range(steps):
+        for e in seq:
+            e.step()
+    t_seq = time.perf_counter() - t
+    pu = sum(e.point_updates() for e in seq) - p0
+    t = time.perf_counter()
+    for _ in range(steps):
+        step_many(bat)
+    t_bat = time.perf_counter() - t
+    same = all(np.array_equal(a.download(0, "trK"), b.download(0, "trK")) for a, b in zip(seq, bat))
+    for e in seq + bat:
+        e.close()
+    return {"workload": "%d massless scalar shells, 64^2-128^2 x 2-3 levels (seeded), %d coarse steps each" % (n, steps),
+            "sequential_point_updates_per_s": pu / t_seq, "batched_point_updates_per_s": pu / t_bat,
+            "speedup": t_seq / t_bat, "identical_results": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -380,6 +435,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-elliptic", action="store_true", help="skip the mixed-precision elliptic measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched small-evolution measurement")
     ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
     ap.add_argument("--size", type=int, default=512, help="points per level per direction")
     args = ap.parse_args()

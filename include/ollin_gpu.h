@@ -223,6 +223,15 @@ int ollin_gpu_aux(ollin_handle* h, int level);
  * src/base/evolve.f90:381).  ``t_out`` (may be NULL) receives t(0,0). */
 int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
 
+/* One coarse step of each of ``n`` independent evolutions (handles on the
+ * same device).  All steps are queued, each on its handle's stream, before
+ * any is waited for, so the kernels of small grids run side by side; the
+ * results are those of n ollin_gpu_coarse_step calls.  ``t_out`` (may be
+ * NULL) receives each t(0,0).  No counterpart in the reference, which runs
+ * one evolution per process (a host batching independent runs calls this
+ * in its loop over them). */
+int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out);
+
 /* Constraint norms and 0-D statistics of one field of one level, the five
  * numbers of save0Dvariable (src/base/save0Ddata.f90:221-288):
  * out[0]=max, out[1]=min, out[2]=nm1 (max |f|), out[3]=nm2 (RMS), out[4]=origin value.

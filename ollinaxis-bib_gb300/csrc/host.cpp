@@ -2204,6 +2204,36 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
     return OLLIN_OK;
 }
 
+int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out) {
+    if (!hs || n < 0) return fail(OLLIN_EINVAL, "bad handle array");
+    for (int k = 0; k < n; ++k) {
+        if (!hs[k]) return fail(OLLIN_EINVAL, "null handle");
+        if (!hs[k]->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
+    }
+    // every evolution's step is queued on its own stream before any is
+    // waited for, so the steps of small grids run side by side
+    int first = OLLIN_OK;
+    std::string first_msg;
+    for (int k = 0; k < n && first == OLLIN_OK; ++k) {
+        int rc = onestep(hs[k], 0);
+        if (rc) { first = rc; first_msg = g_err; }
+    }
+    for (int k = 0; k < n; ++k) {
+        ollin_handle* h = hs[k];
+        unsigned int flag = 0;
+        const bool ok = cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream) == cudaSuccess &&
+                        cudaStreamSynchronize(h->stream) == cudaSuccess;
+        if (first == OLLIN_OK && !ok) { first = OLLIN_ECUDA; first_msg = "stream synchronisation failed"; }
+        if (first == OLLIN_OK && flag) {
+            first = OLLIN_ENAN;
+            first_msg = "non-finite value produced by evolution " + std::to_string(k);
+        }
+        if (t_out) t_out[k] = h->t[0];
+    }
+    if (first != OLLIN_OK) return fail(first, first_msg);
+    return OLLIN_OK;
+}
+
 int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
     if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
     DLevel& L = h->L[level];

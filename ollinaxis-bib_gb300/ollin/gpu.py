@@ -74,6 +74,7 @@ def load(build_if_missing=True):
     L.ollin_gpu_kernel_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
+    L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     _lib = L
     return L
 
@@ -195,3 +196,17 @@ class Evolution:
         ms, n, pts = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
         self._check(self.L.ollin_gpu_kernel_stats(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(pts)))
         return ms.value, n.value, pts.value
+
+
+def step_many(evolutions):
+    """One coarse step of every evolution, queued side by side on their
+    streams (ollin_gpu_coarse_step_many); returns each t(0,0)."""
+    if not evolutions:
+        return []
+    L = evolutions[0].L
+    hs = (ctypes.c_void_p * len(evolutions))(*[e.h.value for e in evolutions])
+    t = np.zeros(len(evolutions))
+    rc = L.ollin_gpu_coarse_step_many(hs, len(evolutions), t.ctypes.data)
+    if rc != 0:
+        raise OllinError(rc, L.ollin_gpu_last_error().decode())
+    return list(t)
