@@ -251,21 +251,6 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         };
         auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * dadv(p, 1, i, nr, g, negr, G.idr, false); };
         auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ldx, j, nz, g, negz, G.idz, true); };
-        // Inside both ranges the two stencils share the centre, and with
-        // kr3 = 3 kr the r part is kr3 (f(-s) - 6 f(s) + 2 f(2s)) - kr f(3s):
-        // nine FP64 operations per field instead of twelve.
-        const double kr3 = 3.0 * kr, kz3 = 3.0 * kz, k10 = 10.0 * (kr + kz);
-        auto ladv_rz = [&](const double* p) {
-            double acc = k10 * ld_(p);
-            double sr = fma(-6.0, ld_(p + lsr), ld_(p - lsr));
-            sr = fma(2.0, ld_(p + 2 * lsr), sr);
-            acc = fma(kr3, sr, acc);
-            acc = fma(-kr, ld_(p + 3 * lsr), acc);
-            double sz = fma(-6.0, ld_(p + lsz), ld_(p - lsz));
-            sz = fma(2.0, ld_(p + 2 * lsz), sz);
-            acc = fma(kz3, sz, acc);
-            return fma(-kz, ld_(p + 3 * lsz), acc);
-        };
         // shiftadvect is a template parameter: with it on, the centred
         // derivatives need not stay live for this block
         auto ADVp = [&](const double* p, double dr_, double dz_) {
@@ -273,7 +258,7 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
                 (void)p;
                 return br * dr_ + bz * dz_;
             } else {
-                return (lint_r && lint_z) ? ladv_rz(p) : ladv_r(p) + ladv_z(p);
+                return ladv_r(p) + ladv_z(p);
             }
         };
         auto ADV = [&](int f, double dr_, double dz_) { return ADVp(X[f] + ox, dr_, dz_); };
@@ -330,10 +315,7 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         if constexpr (SCALAR) {
             // auxiliary_matter.f90 always forms lopsided derivatives for the
             // scalar field when a shift is present (independent of shiftadvect)
-            auto LADV = [&](int f) {
-                const double* p = X[f] + ox;
-                return (lint_r && lint_z) ? ladv_rz(p) : ladv_r(p) + ladv_z(p);
-            };
+            auto LADV = [&](int f) { const double* p = X[f] + ox; return ladv_r(p) + ladv_z(p); };
             const double sxr = val(F_SXIR), sxz = val(F_SXIZ);
             s_sphi = s_sphi + br * sxr + bz * sxz;
             s_sxr = s_sxr + LADV(F_SXIR) + sxr * Drb + sxz * Drbz;
