@@ -39,3 +39,14 @@ def test_unknown_values_are_refused():
         params_from_par("shift = Gammadriver1\n")
     with pytest.raises(ValueError):
         params_from_par("nosuchparameter = 3\n")
+
+
+def test_refinement_box_parameters():
+    """Nb, Nl1..3, Nrbox1..3, Nzbox1..3, rbox1..3, zbox1..3 (param.f90:114-139)."""
+    p = params_from_par("Nb = 2\nNl1 = 2\nNrbox1 = 12\nNzbox1 = 14\nzbox1 = 6.0\nNl2 = 1\nrbox2 = 8.d0\n"
+                        "slicing = maximal\nilapse = maximal\nmaximalevery = 4\n")
+    assert p.nb == 2
+    assert list(p.nl) == [2, 1, 0]
+    assert list(p.nrbox) == [12, 1, 1] and list(p.nzbox) == [14, 1, 1]
+    assert list(p.rbox) == [0.0, 8.0, 0.0] and list(p.zbox) == [6.0, 0.0, 0.0]
+    assert p.slicing == SLICING["maximal"]
