@@ -77,8 +77,9 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_c
             if (diss_z) s = s - kd * ko6(v, ld);
         }
         // radiative boundary with unit speed and zero asymptotic value
-        // (radbound(1.d0, 0.d0), radbound.f90:46-70)
-        if (mi == nr || mj == nz) {
+        // (radbound(1.d0, 0.d0), radbound.f90:46-70), also on the lower z
+        // edge without equatorial symmetry
+        if (mi == nr || mj == nz || (!G.eqsym && mj == 1 - g)) {
             const double r = G.rcol[mi], z = G.zrow[mj];
             const double rr = sqrt(r * r + z * z);
             s = -(r * d1(v, 1, pcr, cr1) + z * d1(v, ld, pcz, cz1) + (ld_(v) - 0.0)) / rr;
@@ -137,11 +138,12 @@ __global__ void __launch_bounds__(256) wave_residual_kernel(const double* partia
 }
 
 // scalar_xi_r = diff1r(+1), scalar_xi_z = diff1z(+1) of scalar_phi at the
-// interior points; the ghosts follow from the parity fill
+// interior points (without equatorial symmetry the lower rows too, one-sided
+// in z); the other ghosts follow from the parity fill
 __global__ void __launch_bounds__(128) pulse_xi_kernel(const __grid_constant__ PulseCoeffArgs a) {
     const LevelGeom& G = a.G;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const long ld = G.ld;
     const size_t o = (size_t)i + (size_t)j * ld;
@@ -775,7 +777,7 @@ void launch_wave_residual(const double* partial, int nparts, int nr, int nz, Ell
 
 void launch_pulse_xi(const PulseCoeffArgs& a, cudaStream_t s) {
     dim3 blk(32, 4);
-    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz + blk.y - 1) / blk.y);
+    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
     pulse_xi_kernel<<<grd, blk, 0, s>>>(a);
 }
 

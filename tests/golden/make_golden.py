@@ -79,6 +79,14 @@ CASES = {
     "box_ring_shift": dict(BASE, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=10,
                            Nzbox1=10, rbox1=5.0, zbox1=5.0, shift="Gammadriver2", drivercsi=0.75,
                            drivereta=2.0, _steps=[0, 1, 2]),
+    # elliptic data and maximal slicing without equatorial symmetry (the
+    # wave solver's radiative boundary on the lower z edge as well)
+    "ell_pulse_noeqsym": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, eqsym=False,
+                              idata="scalarpulse", ilapse="one", mattertype="scalar", scalar_a0=0.05,
+                              scalar_r0=2.0, scalar_z0=1.0, scalardiss=0.02, we_maxiter=150, _steps=[0, 1],
+                              _elliptic=True),
+    "max_noeqsym_wave": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, eqsym=False,
+                             maximalevery=1, we_maxiter=150, _steps=[0, 1], _elliptic=True),
     # boxes that overlap on level 1 (syncboxes.f90 with intersect_interp.inc):
     # box 0's level 1 around the origin and box 1 on the axis above it
     "box_overlap": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,

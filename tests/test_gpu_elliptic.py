@@ -27,6 +27,11 @@ BRILL_3LEV = dict(BASE, nrtotal=32, nztotal=32, nl0=2, dr0=0.25, dz0=0.25, idata
                   brill_a0=1.0, we_maxiter=150)
 BRILL_RK4 = dict(BASE, nrtotal=24, nztotal=24, nl0=0, dr0=0.25, dz0=0.25, idata="BrillWave",
                  brill_a0=4.0, we_method="rk4", we_eta=0.5)
+# without equatorial symmetry: the pulse off the equator, the radiative
+# boundary of the wave solver on the lower z edge too
+PULSE_NOEQSYM = dict(BASE, eqsym=0, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                     mattertype="scalar", scalar_a0=0.05, scalar_r0=2.0, scalar_z0=1.0, scalardiss=0.02,
+                     we_maxiter=200)
 
 
 def solve_pair(cfg):
@@ -47,8 +52,8 @@ def check_fields(o, e, cfg, names, tag):
             assert d <= tol_for(nm), "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
 
 
-@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4],
-                         ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped"])
+@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM],
+                         ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped", "pulse_no_eqsym"])
 def test_elliptic_data_matches_oracle(cfg):
     o, e, (o0, o1, ophases, ogres), (g0, g1, ggres) = solve_pair(cfg)
     assert (g0, g1) == (o0, o1), "iterations gpu %s oracle %s" % ((g0, g1), (o0, o1))

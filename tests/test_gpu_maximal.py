@@ -101,6 +101,10 @@ def test_maximal_every_step_wave():
     run(EVERY, 3)
 
 
+def test_maximal_every_step_without_equatorial_symmetry():
+    run(dict(EVERY, eqsym=0, nl0=0), 2)
+
+
 def test_maximal_every_step_with_speeds():
     """The slicing speeds of the host's last analysis enter the wave
     solver's time step (wave_elliptic.f90:211-263)."""

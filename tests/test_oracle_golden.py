@@ -90,7 +90,7 @@ def test_oracle_matches_reference_fortran(name):
     print("%s: worst relative difference %.2e" % (name, worst))
 
 
-ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev"]
+ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev", "ell_pulse_noeqsym"]
 
 
 def ell_cfg(meta):
@@ -148,7 +148,7 @@ def test_oracle_elliptic_data_matches_reference_fortran(name):
 # differences of the initial data stay at the 1e-13 level through them.
 ELL_TOL = 1e-9
 
-MAX_CASES = ["max_ilapse_pulse", "max_every_wave", "max_slicing_sor"]
+MAX_CASES = ["max_ilapse_pulse", "max_every_wave", "max_slicing_sor", "max_noeqsym_wave"]
 
 
 def maximal_due(cfg, step):
