@@ -162,8 +162,9 @@ int check_params(const ollin_params& P) {
         return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave, sor or mixed)");
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     if (P.nb < 0 || P.nb > 3) return fail(OLLIN_EINVAL, "The number of refinement boxes must be between 0 and 3");
-    if (P.nb > 0 && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE))
-        return fail(OLLIN_EINVAL, "elliptic initial data on the device needs Nb = 0");
+    if (P.nb > 0 && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
+        P.ell_solver != OLLIN_ELL_WAVE)
+        return fail(OLLIN_EINVAL, "elliptic initial data with refinement boxes needs ELL_solver = wave on the device");
     for (int b = 0; b < P.nb; ++b)
         if (P.nl[b] < 0 || P.nl[b] >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl of a refinement box out of range");
     return OLLIN_OK;
@@ -971,7 +972,7 @@ int wave_alloc(ollin_handle* h, WaveSolve& S) {
         for (int k = 0; k < kSlots; ++k) { w.v[k] = q; q += L.n; }
         w.ua = q; q += L.n; w.va = q; q += L.n;
         w.S0 = q; q += L.n; w.S1 = q; q += L.n; w.S5 = q; q += L.n;
-        w.dt = dt0 / (double)(1L << l);
+        w.dt = dt0 / (double)(1L << L.level);
     }
     S.nparts = wave_stage_blocks(h->L[0].G);
     if (cudaMalloc(&S.ctl, sizeof(EllCtl)) != cudaSuccess || cudaMalloc(&S.partial, S.nparts * sizeof(double)) != cudaSuccess)
@@ -994,9 +995,10 @@ int wave_symmetry(ollin_handle* h, WaveSolve& S, int level) {
 
 int wave_prolong(ollin_handle* h, WaveSolve& S, int level, int out, double dtw) {
     DLevel& F = h->L[level];
-    DLevel& C = h->L[level - 1];
+    const int pg = F.parent;
+    DLevel& C = h->L[pg];
     WLevel& wf = S.W[level];
-    WLevel& wc = S.W[level - 1];
+    WLevel& wc = S.W[pg];
     ProlongArgs a{};
     a.F = F.G;
     a.Cg = C.G;
@@ -1008,9 +1010,9 @@ int wave_prolong(ollin_handle* h, WaveSolve& S, int level, int out, double dtw) 
     a.cin[0] = base_ptr(C, wc.u[wc.cur]); a.cin[1] = base_ptr(C, wc.v[wc.cur]);
     a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
     a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.rmaxl_c = h->rmaxl[level - 1];
-    a.zminl_c = h->zminl[level - 1]; a.zmaxl_c = h->zmaxl[level - 1];
-    a.tp = S.t[level - 1];
+    a.rminl_c = h->rminl[pg]; a.rmaxl_c = h->rmaxl[pg];
+    a.zminl_c = h->zminl[pg]; a.zmaxl_c = h->zmaxl[pg];
+    a.tp = S.t[pg];
     a.t0 = S.t[level];
     a.tm1 = S.t1[level];
     a.tl = a.t0 + dtw;
@@ -1025,9 +1027,10 @@ int wave_prolong(ollin_handle* h, WaveSolve& S, int level, int out, double dtw) 
 
 int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
     DLevel& F = h->L[level];
-    DLevel& C = h->L[level - 1];
+    const int pg = F.parent;
+    DLevel& C = h->L[pg];
     WLevel& wf = S.W[level];
-    WLevel& wc = S.W[level - 1];
+    WLevel& wc = S.W[pg];
     RestrictArgs a{};
     a.F = F.G;
     a.Cg = C.G;
@@ -1037,7 +1040,7 @@ int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
     a.cout[0] = base_ptr(C, wc.u[wc.cur]); a.cout[1] = base_ptr(C, wc.v[wc.cur]);
     a.rminl_f = h->rminl[level]; a.rmaxl_f = h->rmaxl[level];
     a.zminl_f = h->zminl[level]; a.zmaxl_f = h->zmaxl[level];
-    a.rminl_c = h->rminl[level - 1]; a.zminl_c = h->zminl[level - 1];
+    a.rminl_c = h->rminl[pg]; a.zminl_c = h->zminl[pg];
     a.eqsym = h->P.eqsym;
     a.bicubic = h->P.interp_bicubic;
     a.skip = &S.ctl->done;
@@ -1047,9 +1050,9 @@ int wave_restrict(ollin_handle* h, WaveSolve& S, int level) {
     return after_launch(h);
 }
 
-// wave_elliptic.f90:347-770 (recursive subroutine wavestep), type = 'flat'
-// or 'physical'
-int wavestep(ollin_handle* h, WaveSolve& S, int level) {
+// One step of one grid in wave_elliptic.f90:578-1005 (the body of the box
+// loop of subroutine wavestep), type = 'flat' or 'physical'
+int wave_grid_step(ollin_handle* h, WaveSolve& S, int level) {
     const ollin_params& P = h->P;
     DLevel& L = h->L[level];
     WLevel& w = S.W[level];
@@ -1096,7 +1099,7 @@ int wavestep(ollin_handle* h, WaveSolve& S, int level) {
         launch_wave_stage(a, h->stream);
         int rc = after_launch(h);
         if (rc) return rc;
-        if (level > 0) {
+        if (L.level > 0) {
             rc = wave_prolong(h, S, level, out, dtw);
             if (rc) return rc;
         }
@@ -1107,22 +1110,61 @@ int wavestep(ollin_handle* h, WaveSolve& S, int level) {
     S.t1[level] = S.t[level];
     S.s[level] = S.s[level] + 1;
     S.t[level] = S.t[level] + dt;
+    return OLLIN_OK;
+}
+
+// wave_elliptic.f90:578-1160 (recursive subroutine wavestep): a step of every
+// box that has the level, the next level twice, the parity fills,
+// ``syncboxes`` of ell_u and ell_v between boxes that overlap (plain copies:
+// the solver differentiates ell_u afresh in every stage), and the
+// restriction of each box into its parent.
+int wavestep(ollin_handle* h, WaveSolve& S, int level) {
+    for (int k = 0; k < h->nlev; ++k) {
+        if (h->L[k].level != level) continue;
+        int rc = wave_grid_step(h, S, k);
+        if (rc) return rc;
+    }
     if (level < S.Nlmax) {
         int rc = wavestep(h, S, level + 1);
         if (rc) return rc;
         rc = wavestep(h, S, level + 1);
         if (rc) return rc;
     }
-    if (S.Nlmax > 0) {
-        int rc = wave_symmetry(h, S, level);
-        if (rc) return rc;
-    }
-    if (level > 0 && S.s[level] % 2 == 0) {
-        int rc = wave_restrict(h, S, level);
-        if (rc) return rc;
-        rc = wave_symmetry(h, S, level - 1);
-        if (rc) return rc;
-    }
+    if (S.Nlmax > 0)
+        for (int k = 0; k < h->nlev; ++k) {
+            if (h->L[k].level != level) continue;
+            int rc = wave_symmetry(h, S, k);
+            if (rc) return rc;
+        }
+    if (level > 0)
+        for (const SyncPair& sp : h->sync) {
+            if (h->L[sp.p].level != level) continue;
+            DLevel& P = h->L[sp.p];
+            DLevel& Q = h->L[sp.q];
+            WLevel& wp = S.W[sp.p];
+            WLevel& wq = S.W[sp.q];
+            RestrictArgs a{};
+            a.F = Q.G;
+            a.Cg = P.G;
+            a.nf = 2;
+            a.fid[0] = 0; a.fid[1] = 1;
+            a.fin[0] = base_ptr(Q, wq.u[wq.cur]); a.fin[1] = base_ptr(Q, wq.v[wq.cur]);
+            a.cout[0] = base_ptr(P, wp.u[wp.cur]); a.cout[1] = base_ptr(P, wp.v[wp.cur]);
+            a.tab = sp.tab;
+            a.ntab = sp.ntab;
+            a.skip = &S.ctl->done;
+            launch_restrict_tab(a, h->stream);
+            int rc = after_launch(h);
+            if (rc) return rc;
+        }
+    if (level > 0)
+        for (int k = 0; k < h->nlev; ++k) {
+            if (h->L[k].level != level || S.s[k] % 2 != 0) continue;
+            int rc = wave_restrict(h, S, k);
+            if (rc) return rc;
+            rc = wave_symmetry(h, S, h->L[k].parent);
+            if (rc) return rc;
+        }
     return OLLIN_OK;
 }
 
@@ -1180,7 +1222,7 @@ int wave_elliptic(ollin_handle* h, WaveSolve& S) {
         CUDA_OR_FAIL(cudaMemsetAsync(w.v[w.cur], 0, L.n * sizeof(double), h->stream));
         CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     }
-    const int Nlmax_old = h->nlev - 1;
+    const int Nlmax_old = h->nlmax;
     S.Nlmax = Nlmax_old > 0 ? 0 : Nlmax_old;
     for (int phase = 0;; ++phase) {
         int steps = 0;
@@ -1888,7 +1930,8 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
     if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE)
         return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave on the device");
-    if (h->nb > 0) return fail(OLLIN_EINVAL, "maximal slicing on the device needs Nb = 0");
+    if (h->nb > 0 && P.ell_solver != OLLIN_ELL_WAVE)
+        return fail(OLLIN_EINVAL, "maximal slicing with refinement boxes needs ELL_solver = wave on the device");
     if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
         return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor or mixed");
     // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)
@@ -1942,7 +1985,7 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     if (P.ell_solver == OLLIN_ELL_WAVE) {
         // wave_elliptic.f90:263-271
         const double dt0 = P.we_dtfac * std::min(std::min(P.dr0, P.dz0), std::min(P.dr0 / vrmax, P.dz0 / vzmax));
-        for (int l = 0; l < h->nlev; ++l) S.W[l].dt = dt0 / (double)(1L << l);
+        for (int l = 0; l < h->nlev; ++l) S.W[l].dt = dt0 / (double)(1L << h->L[l].level);
         rc = wave_elliptic(h, S);
     } else if (P.ell_solver == OLLIN_ELL_SOR) {
         rc = sor_elliptic(h, S);

@@ -31,9 +31,9 @@ const double kPi = 3.141592653589793;  // acos(-1.d0)
 // wave_elliptic.f90:347-770 (subroutine wavestep), type = 'flat' or
 // 'physical'
 // ---------------------------------------------------------------------------
-void wavestep(Sim& S, int level, int Nlmax, bool physical) {
+static void wave_grid_step(Sim& S, Level& L, bool physical) {
     const ollin_params& P = S.P;
-    Level& L = S.L[level];
+    const int level = L.level, gid = L.gid;
     currentgrid(S, L);
     // ell_u_p = ell_u, ell_v_p = ell_v and the boundary history
     // (wave_elliptic.f90:421-473): the generic saveold over S.evolved
@@ -102,27 +102,46 @@ void wavestep(Sim& S, int level, int Nlmax, bool physical) {
         radbound(L, v, sv, Dr_v, Dz_v, 1.0, 0.0);
         if (rk4) accumulate(S, L, iter, niter, weight);
         update(S, L, dtw);
-        if (level > 0) finebound(S, level, dtw);
+        if (level > 0) finebound(S, gid, dtw);
     }
-    S.t2[level] = S.t1[level];
-    S.t1[level] = S.t[level];
-    S.s[level] = S.s[level] + 1;
-    S.t[level] = S.t[level] + dt;
+    S.t2[gid] = S.t1[gid];
+    S.t1[gid] = S.t[gid];
+    S.s[gid] = S.s[gid] + 1;
+    S.t[gid] = S.t[gid] + dt;
+}
+
+// wave_elliptic.f90:578-1160 (recursive subroutine wavestep): every box that
+// has the level, then the finer level twice, parity fills, ``syncboxes`` of
+// ell_u and ell_v between boxes that overlap, restriction into the parents
+void wavestep(Sim& S, int level, int Nlmax, bool physical) {
+    for (Level& L : S.L)
+        if (L.level == level) wave_grid_step(S, L, physical);
     if (level < Nlmax) {
         wavestep(S, level + 1, Nlmax, physical);
         wavestep(S, level + 1, Nlmax, physical);
     }
-    if (Nlmax > 0) {
-        if (L.ownaxis) symmetries_r(S, L);
-        if (L.eqsym && L.ownequator) symmetries_z(S, L);
-    }
-    if (level > 0 && S.s[level] % 2 == 0) {
-        restrict_(S, level);
-        Level& Cl = S.L[level - 1];
-        currentgrid(S, Cl);
-        if (Cl.ownaxis) symmetries_r(S, Cl);
-        if (Cl.eqsym && Cl.ownequator) symmetries_z(S, Cl);
-    }
+    if (Nlmax > 0)
+        for (Level& L : S.L) {
+            if (L.level != level) continue;
+            if (L.ownaxis) symmetries_r(S, L);
+            if (L.eqsym && L.ownequator) symmetries_z(S, L);
+        }
+    if (level > 0)
+        for (Level& A : S.L)
+            for (Level& B : S.L)
+                if (A.level == level && B.level == level && A.box != B.box) {
+                    syncboxes(S, A.gid, B.gid, {"ell_u"});
+                    syncboxes(S, A.gid, B.gid, {"ell_v"});
+                }
+    if (level > 0)
+        for (Level& F : S.L) {
+            if (F.level != level || S.s[F.gid] % 2 != 0) continue;
+            restrict_(S, F.gid);
+            Level& Cl = S.L[F.parent];
+            currentgrid(S, Cl);
+            if (Cl.ownaxis) symmetries_r(S, Cl);
+            if (Cl.eqsym && Cl.ownequator) symmetries_z(S, Cl);
+        }
 }
 
 // wave_elliptic.f90:2-345 with init = 'one'.  For the physical Laplacian the
@@ -131,7 +150,6 @@ void wavestep(Sim& S, int level, int Nlmax, bool physical) {
 // left in va_rp/va_zp (:193-263).
 void wave_elliptic(Sim& S, bool physical, const double* va_max) {
     const ollin_params& P = S.P;
-    if (S.Nb > 0) throw std::runtime_error("oracle: the elliptic solvers are restated for box 0 only");
     const int nlev = (int)S.L.size();
     // the time counters are borrowed and given back (wave_elliptic.f90:95-103, 330-340)
     const auto s_ext = S.s; const auto t_ext = S.t, t1_ext = S.t1, t2_ext = S.t2;
@@ -170,7 +188,7 @@ void wave_elliptic(Sim& S, bool physical, const double* va_max) {
         const double cfac = P.we_dtfac;
         dt0 = cfac * std::min(std::min(P.dr0, P.dz0), std::min(P.dr0 / vrmax, P.dz0 / vzmax));
     }
-    for (int l = 0; l < nlev; ++l) S.L[l].dt = dt0 / (double)(1L << l);
+    for (int l = 0; l < nlev; ++l) S.L[l].dt = dt0 / (double)(1L << S.L[l].level);
     const int Nlmax_old = S.Nlmax;
     int Nlmax = (S.Nlmax > 0) ? 0 : S.Nlmax;
     g_ell_stats = EllStats();
@@ -196,15 +214,16 @@ void wave_elliptic(Sim& S, bool physical, const double* va_max) {
         if (step != P.ell_maxiter && Nlmax != Nlmax_old) {
             Nlmax = Nlmax_old;
             for (double& x : L0.a("ell_v").v) x = 0.0;
-            // inject the coarse solution into every finer level (:270-328)
-            for (int level = 1; level < nlev; ++level) {
-                Level& F = S.L[level];
+            // inject the coarse solution into every finer grid (:270-328)
+            for (int gid = 1; gid < nlev; ++gid) {
+                Level& F = S.L[gid];
+                const int level = F.level;
                 Arr& r = F.a("r"); Arr& z = F.a("z");
                 Arr& u = F.a("ell_u");
                 for (int m = 0; m <= F.Nr + F.g - 1; ++m)
                     for (int n = 0; n <= F.Nz + F.g - 1; ++n) {
-                        const double r0 = S.rminl[level] + (double)m * S.drl[level];
-                        const double z0 = S.zminl[level] + (double)n * S.dzl[level];
+                        const double r0 = S.rminl[gid] + (double)m * S.drl[level];
+                        const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
                         const int i = (int)nint_((r0 - r(1 - F.g, 0)) / S.drl[level]) + 1 - F.g;
                         const int j = (int)nint_((z0 - z(0, 1 - F.g)) / S.dzl[level]) + 1 - F.g;
                         const bool flag1 = (i >= 1 - F.g) && (i <= F.Nr) && (j >= 1 - F.g) && (j <= F.Nz);

@@ -396,7 +396,7 @@ void restrict_(Sim& S, int gid) {
 // points well inside q.  Arrays the reference does not declare (the var_p,
 // accumulator and source copies) are overwritten before they are read, so
 // every array but the NOSYNC coordinates and scratch is taken.
-void syncboxes(Sim& S, int p, int q) {
+void syncboxes(Sim& S, int p, int q, const std::vector<std::string>& only) {
     Level& A = S.L[p];
     Level& B = S.L[q];
     if (S.rmaxl[p] < S.rminl[q] || S.rmaxl[q] < S.rminl[p] || S.zmaxl[p] < S.zminl[q] || S.zmaxl[q] < S.zminl[p]) return;
@@ -405,7 +405,8 @@ void syncboxes(Sim& S, int p, int q) {
     const double deltar = (double)(3 * g) * S.drl[level], deltaz = (double)(3 * g) * S.dzl[level];
     Arr& r = A.a("r"); Arr& z = A.a("z");
     std::vector<std::string> names;
-    for (auto& kv : A.arrs) {
+    if (!only.empty()) names = only;  // a single variable (all = .false.)
+    else for (auto& kv : A.arrs) {
         const std::string& n = kv.first;
         if (n == "r" || n == "z" || n == "rr" || n == "auxarray" || n == "Dr_auxarray" || n == "Dz_auxarray") continue;
         if (B.arrs.find(n) == B.arrs.end()) continue;
@@ -441,7 +442,7 @@ void syncboxes(Sim& S, int p, int q) {
 void sync_level(Sim& S, int level) {
     for (Level& A : S.L)
         for (Level& B : S.L)
-            if (A.level == level && B.level == level && A.box != B.box) syncboxes(S, A.gid, B.gid);
+            if (A.level == level && B.level == level && A.box != B.box) syncboxes(S, A.gid, B.gid, {});
 }
 
 // ---------------------------------------------------------------------------

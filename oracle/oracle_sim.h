@@ -74,6 +74,9 @@ void symmetries_z(Sim& S, Level& L);
 double interp(Sim& S, int level, const Arr& var, double r0, double z0);
 void finebound(Sim& S, int level, double dtw);
 void restrict_(Sim& S, int level);
+// syncboxes.f90 onto grid p from grid q: every synchronised array, or only
+// the named ones (the single-variable mode of the elliptic solver)
+void syncboxes(Sim& S, int p, int q, const std::vector<std::string>& only);
 
 // elliptic initial data (oracle_elliptic.cpp)
 void idata_scalarpulse(Sim& S);

@@ -87,6 +87,13 @@ CASES = {
                               _elliptic=True),
     "max_noeqsym_wave": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, eqsym=False,
                              maximalevery=1, we_maxiter=150, _steps=[0, 1], _elliptic=True),
+    # elliptic data with refinement boxes: the wave solver's box loops and its
+    # syncboxes of ell_u and ell_v (wave_elliptic.f90:1059-1082), on the
+    # overlapping layout below
+    "ell_pulse_boxes": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,
+                            Nzbox1=16, zbox1=4.0, idata="scalarpulse", ilapse="one", mattertype="scalar",
+                            scalar_a0=0.05, scalar_r0=2.0, scalar_z0=3.0, scalardiss=0.02, we_maxiter=100,
+                            _steps=[0, 1], _elliptic=True),
     # boxes that overlap on level 1 (syncboxes.f90 with intersect_interp.inc):
     # box 0's level 1 around the origin and box 1 on the axis above it
     "box_overlap": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,

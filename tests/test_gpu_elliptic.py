@@ -52,8 +52,16 @@ def check_fields(o, e, cfg, names, tag):
             assert d <= tol_for(nm), "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
 
 
-@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM],
-                         ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped", "pulse_no_eqsym"])
+# refinement boxes: box 0's level 1 and a box above it that overlap (the
+# wave solver's syncboxes of ell_u and ell_v)
+PULSE_BOXES = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16,
+                   zbox1=4.0, idata="scalarpulse", mattertype="scalar", scalar_a0=0.05, scalar_r0=2.0,
+                   scalar_z0=3.0, scalardiss=0.02, we_maxiter=120)
+
+
+@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM, PULSE_BOXES],
+                         ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped", "pulse_no_eqsym",
+                              "pulse_boxes"])
 def test_elliptic_data_matches_oracle(cfg):
     o, e, (o0, o1, ophases, ogres), (g0, g1, ggres) = solve_pair(cfg)
     assert (g0, g1) == (o0, o1), "iterations gpu %s oracle %s" % ((g0, g1), (o0, o1))
