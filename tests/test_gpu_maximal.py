@@ -105,6 +105,12 @@ def test_maximal_every_step_without_equatorial_symmetry():
     run(dict(EVERY, eqsym=0, nl0=0), 2)
 
 
+def test_maximal_every_step_with_refinement_boxes():
+    """Box 0's level 1 and an overlapping box above it: the wave solver's box
+    loops and syncboxes, then the stale lapse of the next stage on each grid."""
+    run(dict(EVERY, nl0=1, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0), 2)
+
+
 def test_maximal_every_step_with_speeds():
     """The slicing speeds of the host's last analysis enter the wave
     solver's time step (wave_elliptic.f90:211-263)."""
