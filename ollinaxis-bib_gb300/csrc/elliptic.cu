@@ -359,31 +359,46 @@ __global__ void __launch_bounds__(kMaxThreads) max_coeff_kernel(const __grid_con
     double vr = 0.0, vz = 0.0;
     if (i <= nr && j <= nz) {
         const long ld = G.ld;
-        const bool gr = i < 1, gz = G.eqsym && j < 1;
+        // a ghost column of a grid off the axis keeps r derivatives of zero
+        // (diff1r leaves them unset there); ghost rows of a grid that does
+        // not own the equator take the one-sided z stencils
+        const bool gr = G.axis && i < 1, gz = G.equator && j < 1, r0 = !G.axis && i < 1;
         const int mi = gr ? 1 - i : i, mj = gz ? 1 - j : j;
         const size_t o = (size_t)i + (size_t)j * ld, om = (size_t)mi + (size_t)mj * ld;
-        const int pcr = pclass(mi, nr, g), pcz = pclass(mj, nz, g);
+        // the arrays the derivatives are taken from: the live ones, or after
+        // syncboxes the state before the copy (or the partner's, at a
+        // copied point: interior stencils there)
+        const double* src[5] = {A.gA, A.gB, A.gC, A.chi, A.phi};
+        size_t os = om;
+        long lds = ld;
+        bool xin = false;
+        if (A.smap) {
+            const int m = A.smap[om];
+            for (int k = 0; k < 5; ++k) src[k] = m >= 0 ? A.xb[k] : A.xa[k];
+            if (m >= 0) { os = (size_t)m; lds = A.xb_ld; xin = true; }
+        }
+        const int pcr = xin ? 0 : pclass(mi, nr, g), pcz = xin ? 0 : pclass(mj, nz, g);
         const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
         // parities: g_A, g_B, phi, chi even in r and z; g_C even in r, odd in z
         const double er = gr ? -1.0 : 1.0;  // r derivative of an r-even function
         const double ez = gz ? -1.0 : 1.0;  // z derivative of a z-even function
-        const double DrgA = d1(A.gA + om, 1, pcr, cr1) * er;
-        const double DzgB = d1(A.gB + om, ld, pcz, cz1) * ez;
-        const double DrgC = d1(A.gC + om, 1, pcr, cr1) * er * (gz ? -1.0 : 1.0);
-        const double DzgC = d1(A.gC + om, ld, pcz, cz1);
+        const double DrgA = r0 ? 0.0 : d1(src[0] + os, 1, pcr, cr1) * er;
+        const double DzgB = d1(src[1] + os, lds, pcz, cz1) * ez;
+        const double DrgC = r0 ? 0.0 : d1(src[2] + os, 1, pcr, cr1) * er * (gz ? -1.0 : 1.0);
+        const double DzgC = d1(src[2] + os, lds, pcz, cz1);
         const double r = G.rcol[i], gC = A.gC[o];
         A.P1[o] = DrgA + r * DzgC;
         A.P2[o] = (DzgB + r * DrgC) + gC;
         double Drphi, Dzphi, psi4;
         if (A.t0) {
-            Drphi = d1(A.phi + om, 1, pcr, cr1) * er;
-            Dzphi = d1(A.phi + om, ld, pcz, cz1) * ez;
+            Drphi = r0 ? 0.0 : d1(src[4] + os, 1, pcr, cr1) * er;
+            Dzphi = d1(src[4] + os, lds, pcz, cz1) * ez;
             const double p = exp(A.phi[o]);
             psi4 = (p * p) * (p * p);
         } else {
-            const double chm = A.chi[om];
-            Drphi = (-(d1(A.chi + om, 1, pcr, cr1) * er) / chm) * 0.5;
-            Dzphi = (-(d1(A.chi + om, ld, pcz, cz1) * ez) / chm) * 0.5;
+            const double chm = src[3][os];
+            Drphi = r0 ? 0.0 : (-(d1(src[3] + os, 1, pcr, cr1) * er) / chm) * 0.5;
+            Dzphi = (-(d1(src[3] + os, lds, pcz, cz1) * ez) / chm) * 0.5;
             const double p = exp(-log(A.chi[o]) * 0.5);
             psi4 = (p * p) * (p * p);
         }

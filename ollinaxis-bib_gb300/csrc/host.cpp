@@ -408,9 +408,11 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
 }
 
 // the right-hand side of a stage: the ordinary kernels, or the ones that read
-// the lapse quantities of the last ``auxiliary`` call from alpha_aux
+// the lapse quantities of the last ``auxiliary`` call from alpha_aux, the
+// derivatives from the state kept from before ``syncboxes``, or both
 void launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
-    if (a.alpha_aux) launch_rhs_stale(a, s);
+    if (a.alpha_aux && a.smap) launch_rhs_stale_sync(a, s);
+    else if (a.alpha_aux) launch_rhs_stale(a, s);
     else if (a.smap) launch_rhs_sync(a, s);
     else launch_rhs(a, s);
 }
@@ -773,7 +775,7 @@ int build_sync_tables(ollin_handle* h) {
     for (const SyncPair& sp : h->sync)
         for (int g2 : {sp.p, sp.q}) {
             DLevel& G = h->L[g2];
-            if (!G.snap && cudaMalloc(&G.snap, (size_t)NFIELDS * G.n * sizeof(double)) != cudaSuccess)
+            if (!G.snap && cudaMalloc(&G.snap, (size_t)(NFIELDS + 3) * G.n * sizeof(double)) != cudaSuccess)
                 return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes state");
         }
     return OLLIN_OK;
@@ -797,6 +799,11 @@ int sync_level(ollin_handle* h, int level) {
             DLevel& G = h->L[g2];
             for (int f : h->fields)
                 CUDA_OR_FAIL(cudaMemcpyAsync(G.snap + (size_t)f * G.n, G.slot[G.cur][f], G.n * sizeof(double),
+                                             cudaMemcpyDeviceToDevice, h->stream));
+            // and the inverse metric the maximal-slicing coefficients differentiate
+            static const int kGSlots[3] = {X_GA, X_GB, X_GC};
+            for (int k = 0; k < 3; ++k)
+                CUDA_OR_FAIL(cudaMemcpyAsync(G.snap + (size_t)(NFIELDS + k) * G.n, G.aux[kGSlots[k]], G.n * sizeof(double),
                                              cudaMemcpyDeviceToDevice, h->stream));
         }
     }
@@ -1963,6 +1970,16 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
         a.KT2 = base_ptr(L, L.aux[X_KT2]);
         a.rhos = h->scalar ? base_ptr(L, L.aux[X_RHOS]) : nullptr;
         a.t0 = L.last_aux_t0 ? 1 : 0;
+        if (L.sync_pending) {
+            const DLevel& Q = h->L[L.spartner];
+            a.smap = L.smap + (L.g - 1) + (size_t)(L.g - 1) * L.ld;
+            const int slots[5] = {NFIELDS, NFIELDS + 1, NFIELDS + 2, F_CHI, F_PHI};
+            for (int k = 0; k < 5; ++k) {
+                a.xa[k] = base_ptr(L, L.snap + (size_t)slots[k] * L.n);
+                a.xb[k] = base_ptr(Q, Q.snap + (size_t)slots[k] * Q.n);
+            }
+            a.xb_ld = Q.ld;
+        }
         a.S1 = base_ptr(L, w.S1);
         a.P1 = base_ptr(L, q[0]); a.P2 = base_ptr(L, q[1]);
         a.Drphi = base_ptr(L, q[2]); a.Dzphi = base_ptr(L, q[3]); a.psi4 = base_ptr(L, q[4]);

@@ -41,13 +41,13 @@ struct StageArgs {
     int analysis;                // 1: write ham/mom/RSCAL/KT2/Lapla_alpha instead of updating
     unsigned int* nanflag;       // set to 1 if a non-finite source is produced
     // The lapse of the level's last ``auxiliary`` call when a maximal-slicing
-    // solve has replaced the lapse since (launch_rhs_stale only): the
+    // solve has replaced the lapse since (launch_rhs_stale, _stale_sync): the
     // covariant second derivatives, Laplacian, falpha and advective
     // derivatives of the lapse come from it, the lapse itself and the
     // gradient that maximalslicing.f90:156-170 recomputes from the new one.
     const double* alpha_aux;
     // The first stage after ``syncboxes`` copied another box's data onto this
-    // grid (launch_rhs_sync only): smap[o] >= 0 marks a copied point and its
+    // grid (launch_rhs_sync, _stale_sync): smap[o] >= 0 marks a copied point and its
     // offset in the partner's state xb (leading dimension xb_ld); the other
     // points read this grid's state before the copy, xa.
     const int* smap;
@@ -176,6 +176,13 @@ struct MaxCoeffArgs {
     double* P2;                                            // Dz_g_B + r Dr_g_C + g_C
     double* Drphi; double* Dzphi; double* psi4;
     double* vmax;                                          // [2*block]: per-block max sqrt|g^rr/psi4|, sqrt|g^zz/psi4|
+    // after ``syncboxes`` (as StageArgs::smap): the derivatives come from the
+    // grid's state before the copy (xa) or the partner's (xb) at the copied
+    // points; order g_A, g_B, g_C, chi, phi
+    const int* smap;
+    const double* xa[5];
+    const double* xb[5];
+    long xb_ld;
 };
 
 // The physical-Laplacian coefficients of one wave stage.
@@ -332,6 +339,7 @@ void launch_pulse_coeffs(const PulseCoeffArgs& a, cudaStream_t s);
 void launch_rhs(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale(const StageArgs& a, cudaStream_t s);
 void launch_rhs_sync(const StageArgs& a, cudaStream_t s);
+void launch_rhs_stale_sync(const StageArgs& a, cudaStream_t s);
 int sync_table_size(const LevelGeom& P);
 void launch_sync_table(const SyncTableArgs& a, XferPt* tab, cudaStream_t s);
 // maximal slicing (elliptic.cu)

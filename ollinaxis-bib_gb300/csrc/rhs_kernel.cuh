@@ -94,7 +94,9 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     const double smallpi = 3.141592653589793;
 
     // ---- state and aux at the point
-    const double alpha = val(F_ALPHA), chi = val(F_CHI);
+    // after a maximal-slicing solve the lapse itself is the solver's (the
+    // current state), whatever the derivatives are taken from
+    const double alpha = (STALE && SYNC) ? ld_(A.in[F_ALPHA] + o) : val(F_ALPHA), chi = val(F_CHI);
     const double Ac = val(F_A), Bc = val(F_B), Hc = val(F_H), Cc = val(F_C);
     const double trK = val(F_TRK), kA = val(F_KTA), kB = val(F_KTB), kC = val(F_KTC);
     const double Dlr = val(F_DLR), Dlz = val(F_DLZ);
@@ -103,14 +105,30 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     const double DDr = aux(X_DELDEFR), DDz = aux(X_DELDEFZ);
 
     // ---- derivatives
-    const Deriv5 da = D5(F_ALPHA);
     // the lapse as the last ``auxiliary`` call saw it: the same as alpha
-    // except in the first stage after a maximal-slicing solve (STALE)
-    Deriv5 dao = da;
+    // except in the first stage after a maximal-slicing solve (STALE), whose
+    // first derivatives ``maximalslicing`` recomputed on this grid's own
+    // stencils; with SYNC as well, the old lapse's derivatives are those of
+    // the state kept from before the copies
+    Deriv5 da, dao;
     double alpha_o = alpha;
-    if constexpr (STALE) {
+    if constexpr (STALE && SYNC) {
+        const int kr = pclass(i, nr, g), kz = pclass(j, nz, g);
+        const double* p = A.in[F_ALPHA] + o;
+        da.r = d1(p, 1, kr, cr1);
+        da.z = d1(p, ld, kz, cz1);
+        da.rr = d2(p, 1, kr, cr2);
+        da.zz = d2(p, ld, kz, cz2);
+        da.rz = d2rz(p, ld, i, j, nr, nz, g, idrz);
+        dao = D5(F_ALPHA);
+        alpha_o = ld_(A.alpha_aux + o);
+    } else if constexpr (STALE) {
+        da = D5(F_ALPHA);
         dao = D5p(A.alpha_aux + o);
         alpha_o = ld_(A.alpha_aux + o);
+    } else {
+        da = D5(F_ALPHA);
+        dao = da;
     }
     const Deriv5 dA = D5(F_A), dB = D5(F_B), dH = D5(F_H), dC = D5(F_C);
     const double Dr_trK = Dr(F_TRK), Dz_trK = Dz(F_TRK);
@@ -304,7 +322,7 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
         s_Dlz = s_Dlz + two * rgC * dbZ.rz + gA * dbZ.rr + gB * dbZ.zz + gH * Drbz * ir;
         s_Dlz = s_Dlz + third * (rgC * Dr_DIV_beta + gB * Dz_DIV_beta) + Dlz * tdb;
         if (bona_masso)
-            s_alpha = s_alpha + ADVp(STALE ? A.alpha_aux + o : X[F_ALPHA] + ox, dao.r, dao.z);
+            s_alpha = s_alpha + ADVp(STALE && !SYNC ? A.alpha_aux + o : X[F_ALPHA] + ox, dao.r, dao.z);
         s_br = dbr;
         s_bz = dbz;
         if (P.driveradv) {

@@ -111,6 +111,13 @@ def test_maximal_every_step_with_refinement_boxes():
     run(dict(EVERY, nl0=1, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0), 2)
 
 
+def test_initial_maximal_lapse_scalar_pulse_with_refinement_boxes():
+    """The solve right after ``initialize`` (whose t = 0 syncboxes is still
+    pending) on a scalar pulse: the first stage on the box grids reads the
+    kept pre-copy state and the solved lapse together."""
+    run(dict(PULSE, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0), 1)
+
+
 def test_maximal_every_step_with_speeds():
     """The slicing speeds of the host's last analysis enter the wave
     solver's time step (wave_elliptic.f90:211-263)."""
