@@ -311,6 +311,8 @@ def run_gpu(args):
             line["elliptic"] = elliptic_precision()
         if not args.no_batch:
             line["batch"] = batch_throughput()
+        if not args.no_serve:
+            line["serving"] = serving()
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
@@ -426,6 +428,113 @@ def batch_throughput(n=32, steps=2, seed=7):
             "speedup": t_seq / t_bat, "identical_results": bool(same)}
 
 
+def serving_requests(rng, n):
+    """A seeded mix of the request types of the serving workload: Schwarzschild
+    punctures (3 levels), massless scalar shells (2-3 levels, mixed-precision
+    elliptic data) and Brill waves (A = 1, 2 levels, mixed-precision elliptic
+    data), 64^2 to 128^2 per level, each with its end time."""
+    import numpy as np
+    common = dict(eqsym=1, order="four", integrator="rk4", dtfac=0.25, boundtype="radiative", slicing="1+log",
+                  gauge_f=2.0, geodiss=0.02, ell_solver="mixed", ell_epsilon=1e-12)
+    out = []
+    for _ in range(n):
+        kind = int(rng.integers(0, 3))
+        size = int(rng.choice([64, 96, 128]))
+        if kind == 0:
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=2, dr0=12.8 / size, dz0=12.8 / size,
+                       idata="schwarzschild", bh1mass=1.0, ilapse="psiminus2")
+            t_end = float(rng.uniform(1.0, 3.0))
+        elif kind == 1:
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=int(rng.integers(1, 3)), dr0=16.0 / size,
+                       dz0=16.0 / size, idata="scalarpulse", mattertype="scalar", scalarpotential="none",
+                       scalarpulse_type="shell", scalar_a0=float(np.exp(rng.uniform(np.log(0.01), np.log(0.1)))),
+                       scalar_r0=5.0, scalar_sr0=1.0, scalar_sz0=1.0, ilapse="one", scalardiss=0.02)
+            t_end = float(rng.uniform(2.0, 6.0))
+        else:
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=1, dr0=8.0 / size, dz0=8.0 / size,
+                       idata="BrillWave", brill_a0=1.0, ilapse="one")
+            t_end = float(rng.uniform(1.0, 3.0))
+        out.append((kind, cfg, t_end))
+    return out
+
+
+def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
+    """The serving pattern through the request loop (ollin_server_*):
+      * plain: the requests one at a time (max_active = 1), all queued at 0;
+      * batched: the same requests with up to 64 running together;
+      * served: Poisson arrivals (seeded) at ``load`` x the batched rate, plus a
+        bisection chain on the shell amplitude whose next request is submitted
+        when the previous one finishes (collapse = smallest lapse < 0.05).
+    Latency is finish minus submission, host wall clock.  Every request's
+    norms must agree between the plain and the served runs."""
+    import numpy as np
+    from ollin.gpu import Server
+    from ollin.params import params_from_dict
+    rng = np.random.default_rng(seed)
+    reqs = serving_requests(rng, n)
+
+    def closed(max_active):
+        s = Server(budget, max_active=max_active)
+        for k, (_, cfg, t_end) in enumerate(reqs):
+            s.submit(k, params_from_dict(cfg), t_end, 0.05 if cfg.get("mattertype") == "scalar" else 0.0)
+        t = time.perf_counter()
+        res = s.drain()
+        dt = time.perf_counter() - t
+        s.close()
+        return dt, {r.id: r for r in res}
+
+    t_plain, plain = closed(1)
+    t_bat, bat = closed(64)
+    rate = load * n / t_bat
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
+    chain_cfg = dict(reqs[0][1]) if reqs[0][0] == 1 else None
+    if chain_cfg is None:
+        chain_cfg = next(dict(c) for kd, c, _ in reqs if kd == 1)
+    lo, hi = 0.01, 0.1
+    s = Server(budget, max_active=64)
+    res, nxt, t0, pending_chain, chain_done = {}, 0, time.perf_counter(), None, 0
+    peak_run = 0
+    while len(res) < n + chain:
+        now = time.perf_counter() - t0
+        while nxt < n and arrivals[nxt] <= now:
+            _, cfg, t_end = reqs[nxt]
+            s.submit(nxt, params_from_dict(cfg), t_end, 0.05 if cfg.get("mattertype") == "scalar" else 0.0)
+            nxt += 1
+        if pending_chain is None and chain_done < chain:
+            a = float(np.sqrt(lo * hi))
+            pending_chain = (1000 + chain_done, a)
+            s.submit(1000 + chain_done, params_from_dict(dict(chain_cfg, scalar_a0=a)), 4.0, 0.05)
+        a_run, _ = s.tick()
+        peak_run = max(peak_run, a_run)
+        for r in s.poll():
+            res[r.id] = r
+            if pending_chain and r.id == pending_chain[0]:
+                if r.collapsed:
+                    hi = pending_chain[1]
+                else:
+                    lo = pending_chain[1]
+                pending_chain, chain_done = None, chain_done + 1
+        if a_run == 0 and nxt < n and pending_chain is None and chain_done >= chain:
+            time.sleep(max(0.0, min(0.01, arrivals[nxt] - (time.perf_counter() - t0))))
+    t_served = time.perf_counter() - t0
+    used, peak = s.usage()
+    s.close()
+    lat = np.array([res[k].t_done - res[k].t_submit for k in range(n)])
+    svc = np.array([plain[k].t_done - plain[k].t_admit for k in range(n)])
+    same = all(np.array_equal(plain[k].norms(), res[k].norms()) and plain[k].steps == res[k].steps
+               for k in range(n))
+    ok = all(r.status == 0 for r in list(res.values()) + list(plain.values()) + list(bat.values()))
+    return {"workload": "%d requests: Schwarzschild punctures, massless scalar shells, Brill waves; 64^2-128^2 "
+                        "x 2-3 levels, t_end 1-6 (seeded); + a %d-step bisection chain on the shell amplitude"
+                        % (n, chain),
+            "budget_bytes": budget, "peak_reserved_bytes": peak, "most_running": peak_run,
+            "plain_runs_per_s": n / t_plain, "batched_runs_per_s": n / t_bat, "batched_vs_plain": t_plain / t_bat,
+            "served": {"arrival_rate_per_s": rate, "runs_per_s": (n + chain) / t_served,
+                       "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99))},
+            "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99))},
+            "bisection_bracket": [lo, hi], "all_ok": bool(ok), "identical_results": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -436,6 +545,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-elliptic", action="store_true", help="skip the mixed-precision elliptic measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched small-evolution measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the request-loop measurement")
     ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
     ap.add_argument("--size", type=int, default=512, help="points per level per direction")
     args = ap.parse_args()

@@ -22,10 +22,13 @@
  *    the leading dimension in elements (``Nr+ghost`` for an unpadded array).
  *  - One handle = one evolution = one CUDA stream.  Device memory is owned by
  *    the handle.  Handles are independent; several may live at once.
- *  - Only box 0 (Nb = 0, concentric box-in-box levels) is supported.
+ *  - Refinement boxes Nb = 0..3 (setupboxes.f90); a ``level`` argument is a
+ *    grid index: box 0's levels, then each further box's levels.
  */
 #ifndef OLLIN_GPU_H
 #define OLLIN_GPU_H
+
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -231,6 +234,80 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
  * one evolution per process (a host batching independent runs calls this
  * in its loop over them). */
 int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out);
+
+/* One coarse step split in two, for callers that overlap several evolutions
+ * (the request loop below): ollin_gpu_step_begin queues ``onestep(0)`` on the
+ * handle's stream and returns without waiting; ollin_gpu_step_end waits for
+ * it, checks for non-finite values and gives the coarse time.  Between the
+ * two the caller may queue work on other handles.  Every begin needs its end,
+ * also when begin failed (the end then waits for what was queued). */
+int ollin_gpu_step_begin(ollin_handle* h);
+int ollin_gpu_step_end(ollin_handle* h, double* t_out);
+
+/* Device bytes an evolution with parameters ``p`` holds from create to
+ * destroy (``resident``), and the most its elliptic solves (initial data,
+ * maximal slicing) add while they run (``transient``).  An upper bound that
+ * includes the 2 MiB granularity of large allocations; no device work.  No
+ * counterpart in the reference (one run per process). */
+int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transient);
+
+/* ---------------------------------------------------------------------------
+ * Request loop (continuous batching of evolutions; no counterpart in the
+ * reference, whose evolve.f90 runs one evolution per process).
+ *
+ * Requests are submitted as parameter sets with an end time.  Each call to
+ * ollin_server_tick (1) queues one coarse step of every running evolution,
+ * each on its own stream, (2) admits waiting requests, in arrival order and
+ * first fit, while their footprint (resident + transient) fits in the device
+ * budget next to the running ones' resident bytes and a slot is free -- their
+ * initial data, ``initialize`` and any initial maximal-slicing solve run on
+ * their own streams while the steps of (1) run -- and (3) waits for the
+ * steps, checks the lapse against the request's collapse threshold and
+ * retires evolutions that reached their end time, collapsed or failed.  A
+ * retired evolution's handle is destroyed; its summary is kept for
+ * ollin_server_poll.  Each evolution's arithmetic is that of a lone run:
+ * running in the mix changes only when its steps happen.
+ * ------------------------------------------------------------------------- */
+typedef struct ollin_server ollin_server;
+
+#define OLLIN_RESULT_MAXGRIDS 8
+typedef struct ollin_result {
+    long long id;       /* the caller's request id */
+    int    status;      /* OLLIN_OK, or the code that ended the evolution */
+    int    collapsed;   /* 1: the smallest lapse fell below the request's threshold */
+    int    steps;       /* coarse steps taken */
+    int    ngrids;      /* grids of the evolution (norms below for the first OLLIN_RESULT_MAXGRIDS) */
+    double t;           /* coarse time reached */
+    double min_alpha;   /* smallest lapse at the last check (every coarse step with a threshold, else at the end) */
+    double t_submit, t_admit, t_done;  /* seconds since ollin_server_create */
+    size_t bytes;       /* resident + transient bytes reserved for it */
+    double l2[OLLIN_RESULT_MAXGRIDS][4];  /* per grid at the end: L2 norms of alpha, phi, trK, ham (save0Ddata.f90:221-288) */
+} ollin_result;
+
+/* ``budget``: device bytes the server's evolutions may hold; ``max_active``:
+ * evolutions stepped together (>= 1). */
+int ollin_server_create(size_t budget, int max_active, ollin_server** out);
+void ollin_server_destroy(ollin_server* s);
+/* Queue a request: evolve ``p`` (copied) to coarse time ``t_end`` (rounded to
+ * whole coarse steps), with the maximal-slicing solves of evolve.f90:228-230
+ * and :388-393 (``maximalevery`` is the par-file value; slicing or ilapse
+ * "maximal" in ``p`` also count), stopping early when the smallest lapse over
+ * all grids falls below ``collapse_alpha`` (0: no check).  A request that
+ * could never fit the budget is rejected at once with OLLIN_ENOMEM; bad
+ * parameters give OLLIN_EINVAL. */
+int ollin_server_submit(ollin_server* s, long long id, const ollin_params* p, int maximalevery, double t_end,
+                        double collapse_alpha);
+/* One round of the loop; ``n_active``/``n_waiting`` (may be null) give the
+ * counts after it.  Failures of single evolutions end up in their results;
+ * the return value is nonzero only for a failure of the loop itself. */
+int ollin_server_tick(ollin_server* s, int* n_active, int* n_waiting);
+/* Move up to ``max`` finished results, oldest first, into ``out``; ``n_out``
+ * gets the number moved. */
+int ollin_server_poll(ollin_server* s, ollin_result* out, int max, int* n_out);
+/* Device bytes reserved now and at most so far by the server's evolutions. */
+int ollin_server_usage(const ollin_server* s, size_t* used, size_t* peak);
+/* Message for the last failure of an ollin_server_* call on the calling thread. */
+const char* ollin_server_last_error(void);
 
 /* Constraint norms and 0-D statistics of one field of one level, the five
  * numbers of save0Dvariable (src/base/save0Ddata.f90:221-288):

@@ -106,6 +106,7 @@ struct ollin_handle {
     double point_updates = 0;
     long long launches = 0;
     bool initialized = false;
+    bool step_queued = false;  // ollin_gpu_step_begin ran, ollin_gpu_step_end not yet
     bool shift = false, scalar = false;
     PhysParams phys{};
     // optional per-launch timing of the right-hand-side kernel
@@ -2263,6 +2264,61 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     if (flag) return fail(OLLIN_ENAN, "non-finite value produced by the evolution");
     if (t_out) *t_out = h->t[0];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_step_begin(ollin_handle* h) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
+    if (h->step_queued) return fail(OLLIN_ESTATE, "a step is already queued on this handle");
+    int rc = onestep(h, 0);
+    // queued work runs to its end whatever happened: the next end waits for it
+    h->step_queued = true;
+    return rc;
+}
+
+int ollin_gpu_step_end(ollin_handle* h, double* t_out) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    if (!h->step_queued) return fail(OLLIN_ESTATE, "no step is queued on this handle");
+    h->step_queued = false;
+    unsigned int flag = 0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    if (flag) return fail(OLLIN_ENAN, "non-finite value produced by the evolution");
+    if (t_out) *t_out = h->t[0];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transient) {
+    if (!p || !resident || !transient) return fail(OLLIN_EINVAL, "null argument");
+    int rc = check_params(*p);
+    if (rc) return rc;
+    ollin_handle tmp;  // the grid list only: no device work
+    tmp.P = *p;
+    tmp.g = 3;
+    rc = setup_boxes(&tmp);
+    if (rc) return rc;
+    // a maximal-slicing solve may run whenever the caller asks (maximalevery
+    // is the caller's): count its arrays for every run that can have one
+    const bool maximal = true;
+    const bool elliptic = maximal || p->idata == OLLIN_IDATA_SCALARPULSE || p->idata == OLLIN_IDATA_BRILLWAVE;
+    const size_t page = (size_t)2 << 20;  // allocation granularity of large cudaMalloc blocks
+    size_t res = 4 * page, tr = 0;
+    for (const DLevel& L : tmp.L) {
+        const int g = tmp.g, nr = tmp.nrbox[L.box], nz = tmp.nzbox[L.box];
+        const size_t n = (size_t)(((nr + g + 31) / 32) * 32) * (size_t)(nz + g);
+        const size_t narrays = (size_t)kSlots * NFIELDS + NFIELDS + NAUX;
+        res += (narrays * n + (size_t)(nr + g) * 2 + (size_t)(nz + g) + 64) * sizeof(double) + page;
+        res += 2 * page;                                  // transfer tables
+        if (tmp.nb > 0) res += ((NFIELDS + 3) * n + n) * sizeof(double) + 2 * page;  // syncboxes state and map
+        if (maximal) res += n * sizeof(double) + page;  // the lapse of the last auxiliary call
+        // the elliptic solver's arrays while a solve runs: 13 arrays of the
+        // wave solver's state and sources, 5 of coefficients, and for SOR and
+        // the mixed solver their stencil, residual and FP32 hierarchy (below 22)
+        if (elliptic) tr += 40 * n * sizeof(double) + 4 * page;
+    }
+    *resident = res;
+    *transient = tr;
     return OLLIN_OK;
 }
 

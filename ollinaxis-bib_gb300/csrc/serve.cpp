@@ -1,0 +1,274 @@
+// Request loop over evolutions: continuous batching on one GPU.
+//
+// The reference runs one evolution per process (src/base/evolve.f90); there
+// is nothing to mirror here but its per-evolution sequence, which each
+// admitted request follows: initial data (``initial``, with its elliptic
+// solve), ``initialize`` (evolve.f90:128-219), an initial maximal-slicing
+// solve where evolve.f90:228-230 makes one, then ``onestep(0)`` per coarse
+// step with the solves of :388-393, and at the end the 0-D norms of
+// save0Ddata.f90:221-288.
+//
+// Design (one host thread, one stream per evolution):
+//   * admission by device bytes: a request's footprint (resident while it
+//     runs, plus what its elliptic solves add while they run) must fit in the
+//     budget beside the resident bytes of the running evolutions;
+//   * a tick queues one coarse step of every running evolution before it
+//     waits for any, so small grids fill the GPU together; the set-up of
+//     newly admitted requests is queued after those steps, on the new
+//     requests' own streams, so it overlaps them;
+//   * nothing is shared between evolutions on the device, so a result does
+//     not depend on which other requests ran beside it.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <deque>
+#include <string>
+#include <vector>
+
+#include "../../include/ollin_gpu.h"
+
+namespace {
+
+thread_local std::string s_err;
+
+int sfail(int code, const std::string& msg) {
+    s_err = msg;
+    return code;
+}
+
+struct Request {
+    long long id = 0;
+    ollin_params p{};
+    int nsteps = 0;           // coarse steps to the end time
+    double collapse = 0.0;    // smallest-lapse threshold (0: none)
+    int maximalevery = 0;     // param maximalevery
+    size_t resident = 0, transient = 0;
+    double t_submit = 0.0;
+};
+
+struct Running {
+    Request r;
+    ollin_handle* h = nullptr;
+    double t_admit = 0.0;
+    int steps = 0;
+    double t = 0.0;
+    double min_alpha = 1.0;
+    bool queued = false;  // a step_begin waits for its step_end
+};
+
+double min_lapse(ollin_handle* h, double* out_min) {
+    double m = HUGE_VAL;
+    const int n = ollin_gpu_num_levels(h);
+    for (int l = 0; l < n; ++l) {
+        double nm[5];
+        int rc = ollin_gpu_norms(h, l, OLLIN_F_ALPHA, nm);
+        if (rc) return rc;
+        m = std::min(m, nm[1]);
+    }
+    *out_min = m;
+    return OLLIN_OK;
+}
+
+bool maximal_at_start(const Request& r) {  // evolve.f90:228-230
+    return r.p.slicing == OLLIN_SLICING_MAXIMAL || r.p.ilapse == OLLIN_ILAPSE_MAXIMAL || r.maximalevery != 0;
+}
+
+bool maximal_after(const Request& r, int step) {  // evolve.f90:388-393
+    return r.p.slicing == OLLIN_SLICING_MAXIMAL || (r.maximalevery != 0 && step % r.maximalevery == 0);
+}
+
+}  // namespace
+
+struct ollin_server {
+    size_t budget = 0;
+    int max_active = 1;
+    size_t used = 0, peak = 0;
+    std::deque<Request> waiting;
+    std::vector<Running> running;
+    std::deque<ollin_result> done;
+    std::chrono::steady_clock::time_point t0;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+
+    ollin_result result_of(const Request& r, int status) const {
+        ollin_result x{};
+        x.id = r.id;
+        x.status = status;
+        x.t_submit = r.t_submit;
+        x.bytes = r.resident + r.transient;
+        x.min_alpha = NAN;
+        return x;
+    }
+
+    // ends a running evolution: final norms, then the handle goes
+    void retire(size_t k, int status, bool collapsed) {
+        Running& e = running[k];
+        if (e.queued) {  // its queued work finishes before the handle goes
+            double t;
+            ollin_gpu_step_end(e.h, &t);
+            e.queued = false;
+        }
+        ollin_result x = result_of(e.r, status);
+        x.t_admit = e.t_admit;
+        x.collapsed = collapsed ? 1 : 0;
+        x.steps = e.steps;
+        x.t = e.t;
+        x.min_alpha = e.min_alpha;
+        x.ngrids = ollin_gpu_num_levels(e.h);
+        if (status == OLLIN_OK) {
+            static const int fields[4] = {OLLIN_F_ALPHA, OLLIN_F_PHI, OLLIN_F_TRK, OLLIN_F_HAM};
+            for (int l = 0; l < std::min(x.ngrids, OLLIN_RESULT_MAXGRIDS) && x.status == OLLIN_OK; ++l)
+                for (int f = 0; f < 4; ++f) {
+                    double nm[5];
+                    int rc = ollin_gpu_norms(e.h, l, fields[f], nm);
+                    if (rc) { x.status = rc; break; }
+                    x.l2[l][f] = nm[3];
+                }
+            if (x.status == OLLIN_OK && e.r.collapse <= 0.0) {
+                double m;
+                if (min_lapse(e.h, &m) == OLLIN_OK) x.min_alpha = m;
+            }
+        }
+        ollin_gpu_destroy(e.h);
+        x.t_done = now();
+        used -= e.r.resident;
+        done.push_back(x);
+        running.erase(running.begin() + (long)k);
+    }
+
+    // create, initial data, initialize and the first maximal solve of one
+    // request, queued on its own stream
+    int start(Request& r, Running& e) {
+        int rc = ollin_gpu_create(&r.p, &e.h);
+        if (rc) { e.h = nullptr; return rc; }
+        rc = ollin_gpu_initial_data(e.h);
+        if (!rc) rc = ollin_gpu_initialize(e.h);
+        if (!rc && maximal_at_start(r)) rc = ollin_gpu_maximal_slicing(e.h, nullptr);
+        if (!rc && r.collapse > 0.0) rc = min_lapse(e.h, &e.min_alpha);
+        return rc;
+    }
+
+    void admit() {
+        for (auto it = waiting.begin(); it != waiting.end() && (int)running.size() < max_active;) {
+            if (used + it->resident + it->transient > budget) { ++it; continue; }  // first fit
+            Request r = *it;
+            it = waiting.erase(it);
+            Running e;
+            e.r = r;
+            e.t_admit = now();
+            used += r.resident;
+            peak = std::max(peak, used + r.transient);
+            int rc = start(r, e);
+            if (rc) {
+                if (e.h) ollin_gpu_destroy(e.h);
+                used -= r.resident;
+                ollin_result x = result_of(r, rc);
+                x.t_admit = e.t_admit;
+                x.t_done = now();
+                done.push_back(x);
+                continue;
+            }
+            running.push_back(e);
+        }
+    }
+};
+
+extern "C" {
+
+int ollin_server_create(size_t budget, int max_active, ollin_server** out) {
+    if (!out || max_active < 1) return sfail(OLLIN_EINVAL, "bad argument");
+    auto* s = new ollin_server();
+    s->budget = budget;
+    s->max_active = max_active;
+    s->t0 = std::chrono::steady_clock::now();
+    *out = s;
+    return OLLIN_OK;
+}
+
+void ollin_server_destroy(ollin_server* s) {
+    if (!s) return;
+    while (!s->running.empty()) s->retire(s->running.size() - 1, OLLIN_ESTATE, false);
+    delete s;
+}
+
+int ollin_server_submit(ollin_server* s, long long id, const ollin_params* p, int maximalevery, double t_end,
+                        double collapse_alpha) {
+    if (!s || !p || !(t_end >= 0.0) || maximalevery < 0) return sfail(OLLIN_EINVAL, "bad argument");
+    Request r;
+    r.id = id;
+    r.p = *p;
+    r.collapse = collapse_alpha;
+    r.maximalevery = maximalevery;
+    r.t_submit = s->now();
+    int rc = ollin_gpu_footprint(p, &r.resident, &r.transient);
+    if (rc) return sfail(rc, ollin_gpu_last_error());
+    if (r.resident + r.transient > s->budget) return sfail(OLLIN_ENOMEM, "the request can never fit the device budget");
+    const double dt0 = p->dtfac * std::min(p->dr0, p->dz0);  // setupboxes.f90:121-125
+    r.nsteps = (int)std::ceil(t_end / dt0 - 1e-9);
+    s->waiting.push_back(r);
+    return OLLIN_OK;
+}
+
+int ollin_server_tick(ollin_server* s, int* n_active, int* n_waiting) {
+    if (!s) return sfail(OLLIN_EINVAL, "null server");
+    // (1) one coarse step of every running evolution, queued before any wait
+    std::vector<int> rc(s->running.size(), OLLIN_OK);
+    for (size_t k = 0; k < s->running.size(); ++k) {
+        Running& e = s->running[k];
+        if (e.steps >= e.r.nsteps) continue;
+        rc[k] = ollin_gpu_step_begin(e.h);
+        e.queued = true;
+    }
+    // (2) admissions: their set-up overlaps the steps on the device
+    const size_t nrun = s->running.size();
+    s->admit();
+    // (3) the steps' ends, the solves that follow a step, the checks
+    std::vector<std::pair<size_t, std::pair<int, bool>>> retire;
+    for (size_t k = 0; k < nrun; ++k) {
+        Running& e = s->running[k];
+        int r = rc[k];
+        if (e.queued) {
+            double t = e.t;
+            const int re = ollin_gpu_step_end(e.h, &t);
+            e.queued = false;
+            if (!r) r = re;
+            if (!r) { e.t = t; e.steps += 1; }
+        }
+        if (!r && maximal_after(e.r, e.steps)) r = ollin_gpu_maximal_slicing(e.h, nullptr);
+        bool collapsed = false;
+        if (!r && e.r.collapse > 0.0) {
+            r = min_lapse(e.h, &e.min_alpha);
+            collapsed = !r && e.min_alpha < e.r.collapse;
+        }
+        if (r || collapsed || e.steps >= e.r.nsteps) retire.push_back({k, {r, collapsed}});
+    }
+    for (size_t q = retire.size(); q-- > 0;) s->retire(retire[q].first, retire[q].second.first, retire[q].second.second);
+    // a request that finished at once (nsteps = 0) retires on the next tick
+    if (n_active) *n_active = (int)s->running.size();
+    if (n_waiting) *n_waiting = (int)s->waiting.size();
+    return OLLIN_OK;
+}
+
+int ollin_server_poll(ollin_server* s, ollin_result* out, int max, int* n_out) {
+    if (!s || (!out && max > 0) || !n_out) return sfail(OLLIN_EINVAL, "bad argument");
+    int n = 0;
+    while (n < max && !s->done.empty()) {
+        out[n++] = s->done.front();
+        s->done.pop_front();
+    }
+    *n_out = n;
+    return OLLIN_OK;
+}
+
+int ollin_server_usage(const ollin_server* s, size_t* used, size_t* peak) {
+    if (!s || !used || !peak) return sfail(OLLIN_EINVAL, "bad argument");
+    *used = s->used;
+    *peak = s->peak;
+    return OLLIN_OK;
+}
+
+const char* ollin_server_last_error(void) { return s_err.c_str(); }
+
+}  // extern "C"

@@ -75,6 +75,18 @@ def load(build_if_missing=True):
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_step_begin.argtypes = [vp]
+    L.ollin_gpu_step_end.argtypes = [vp, dp]
+    sp = ctypes.POINTER(ctypes.c_size_t)
+    L.ollin_gpu_footprint.argtypes = [ctypes.c_void_p, sp, sp]
+    L.ollin_server_create.argtypes = [ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(vp)]
+    L.ollin_server_destroy.argtypes = [vp]
+    L.ollin_server_submit.argtypes = [vp, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_double]
+    L.ollin_server_tick.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+    L.ollin_server_poll.argtypes = [vp, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.ollin_server_usage.argtypes = [vp, sp, sp]
+    L.ollin_server_last_error.restype = ctypes.c_char_p
     _lib = L
     return L
 
@@ -210,3 +222,86 @@ def step_many(evolutions):
     if rc != 0:
         raise OllinError(rc, L.ollin_gpu_last_error().decode())
     return list(t)
+
+
+def footprint(params):
+    """(resident, transient) device bytes of an evolution (ollin_gpu_footprint)."""
+    L = load()
+    r, t = ctypes.c_size_t(), ctypes.c_size_t()
+    rc = L.ollin_gpu_footprint(ctypes.byref(params), ctypes.byref(r), ctypes.byref(t))
+    if rc:
+        raise OllinError(rc, L.ollin_gpu_last_error().decode())
+    return r.value, t.value
+
+
+RESULT_MAXGRIDS = 8
+
+
+class Result(ctypes.Structure):
+    """ollin_result: the summary of one finished request."""
+    _fields_ = [("id", ctypes.c_longlong), ("status", ctypes.c_int), ("collapsed", ctypes.c_int),
+                ("steps", ctypes.c_int), ("ngrids", ctypes.c_int), ("t", ctypes.c_double),
+                ("min_alpha", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_done", ctypes.c_double), ("bytes", ctypes.c_size_t),
+                ("l2", (ctypes.c_double * 4) * RESULT_MAXGRIDS)]
+
+    def norms(self):
+        """(ngrids, 4) array: L2 norms of alpha, phi, trK, ham per grid."""
+        n = min(self.ngrids, RESULT_MAXGRIDS)
+        return np.array([[self.l2[g][k] for k in range(4)] for g in range(n)])
+
+
+class Server:
+    """The request loop of the C ABI (ollin_server_*): continuous batching of
+    evolutions on the current device, admitted against a byte budget."""
+
+    def __init__(self, budget_bytes, max_active=64):
+        self.L = load()
+        h = ctypes.c_void_p()
+        self._check(self.L.ollin_server_create(int(budget_bytes), int(max_active), ctypes.byref(h)))
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            raise OllinError(rc, self.L.ollin_server_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.ollin_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, rid, params, t_end, collapse_alpha=0.0, maximalevery=0):
+        self._check(self.L.ollin_server_submit(self.h, int(rid), ctypes.byref(params), int(maximalevery),
+                                               float(t_end), float(collapse_alpha)))
+
+    def tick(self):
+        """One round; returns (running, waiting)."""
+        a, w = ctypes.c_int(), ctypes.c_int()
+        self._check(self.L.ollin_server_tick(self.h, ctypes.byref(a), ctypes.byref(w)))
+        return a.value, w.value
+
+    def poll(self, max_results=256):
+        buf = (Result * max_results)()
+        n = ctypes.c_int()
+        self._check(self.L.ollin_server_poll(self.h, buf, max_results, ctypes.byref(n)))
+        return [buf[k] for k in range(n.value)]
+
+    def usage(self):
+        u, p = ctypes.c_size_t(), ctypes.c_size_t()
+        self._check(self.L.ollin_server_usage(self.h, ctypes.byref(u), ctypes.byref(p)))
+        return u.value, p.value
+
+    def drain(self):
+        """Tick until nothing runs or waits; return every result."""
+        out = []
+        while True:
+            a, w = self.tick()
+            out += self.poll()
+            if a == 0 and w == 0:
+                return out + self.poll()
