@@ -521,6 +521,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
     s.close()
     lat = np.array([res[k].t_done - res[k].t_submit for k in range(n)])
     svc = np.array([plain[k].t_done - plain[k].t_admit for k in range(n)])
+    setup = np.array([plain[k].t_ready - plain[k].t_admit for k in range(n)])
     same = all(np.array_equal(plain[k].norms(), res[k].norms()) and plain[k].steps == res[k].steps
                for k in range(n))
     ok = all(r.status == 0 for r in list(res.values()) + list(plain.values()) + list(bat.values()))
@@ -531,7 +532,8 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
             "plain_runs_per_s": n / t_plain, "batched_runs_per_s": n / t_bat, "batched_vs_plain": t_plain / t_bat,
             "served": {"arrival_rate_per_s": rate, "runs_per_s": (n + chain) / t_served,
                        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99))},
-            "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99))},
+            "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99)),
+                              "setup_share": float(setup.sum() / svc.sum())},
             "bisection_bracket": [lo, hi], "all_ok": bool(ok), "identical_results": bool(same)}
 
 

@@ -243,6 +243,9 @@ int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out);
  * also when begin failed (the end then waits for what was queued). */
 int ollin_gpu_step_begin(ollin_handle* h);
 int ollin_gpu_step_end(ollin_handle* h, double* t_out);
+/* 1 when ollin_gpu_step_end would not wait (the queued step has finished, or
+ * none is queued), 0 while the step runs.  Does not block. */
+int ollin_gpu_step_ready(const ollin_handle* h);
 
 /* Device bytes an evolution with parameters ``p`` holds from create to
  * destroy (``resident``), and the most its elliptic solves (initial data,
@@ -255,16 +258,19 @@ int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transie
  * Request loop (continuous batching of evolutions; no counterpart in the
  * reference, whose evolve.f90 runs one evolution per process).
  *
- * Requests are submitted as parameter sets with an end time.  Each call to
- * ollin_server_tick (1) queues one coarse step of every running evolution,
- * each on its own stream, (2) admits waiting requests, in arrival order and
- * first fit, while their footprint (resident + transient) fits in the device
- * budget next to the running ones' resident bytes and a slot is free -- their
- * initial data, ``initialize`` and any initial maximal-slicing solve run on
- * their own streams while the steps of (1) run -- and (3) waits for the
- * steps, checks the lapse against the request's collapse threshold and
- * retires evolutions that reached their end time, collapsed or failed.  A
- * retired evolution's handle is destroyed; its summary is kept for
+ * Requests are submitted as parameter sets with an end time.  Every running
+ * evolution always has one coarse step queued on its own stream; no
+ * evolution waits for another.  Each call to ollin_server_tick (1) takes
+ * every evolution whose step has finished, runs the maximal-slicing solve
+ * that follows the step if any, checks the lapse against the request's
+ * collapse threshold, and either retires it (end time reached, collapsed or
+ * failed) or queues its next step; (2) admits waiting requests, in arrival
+ * order and first fit, while their footprint (resident + transient) fits in
+ * the device budget next to the running ones' resident bytes and a slot is
+ * free -- their initial data, ``initialize`` and any initial maximal-slicing
+ * solve run on their own streams while the queued steps run.  A tick that
+ * finds nothing to do waits until some step finishes.  A retired
+ * evolution's handle is destroyed; its summary is kept for
  * ollin_server_poll.  Each evolution's arithmetic is that of a lone run:
  * running in the mix changes only when its steps happen.
  * ------------------------------------------------------------------------- */
@@ -279,7 +285,8 @@ typedef struct ollin_result {
     int    ngrids;      /* grids of the evolution (norms below for the first OLLIN_RESULT_MAXGRIDS) */
     double t;           /* coarse time reached */
     double min_alpha;   /* smallest lapse at the last check (every coarse step with a threshold, else at the end) */
-    double t_submit, t_admit, t_done;  /* seconds since ollin_server_create */
+    double t_submit, t_admit, t_ready, t_done;  /* seconds since ollin_server_create: submitted,
+                                                  admitted, set up (initial data done), finished */
     size_t bytes;       /* resident + transient bytes reserved for it */
     double l2[OLLIN_RESULT_MAXGRIDS][4];  /* per grid at the end: L2 norms of alpha, phi, trK, ham (save0Ddata.f90:221-288) */
 } ollin_result;

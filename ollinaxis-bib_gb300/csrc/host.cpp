@@ -2277,6 +2277,12 @@ int ollin_gpu_step_begin(ollin_handle* h) {
     return rc;
 }
 
+int ollin_gpu_step_ready(const ollin_handle* h) {
+    if (!h || !h->step_queued) return 1;
+    // an error also counts as finished: ollin_gpu_step_end reports it
+    return cudaStreamQuery(h->stream) == cudaErrorNotReady ? 0 : 1;
+}
+
 int ollin_gpu_step_end(ollin_handle* h, double* t_out) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     if (!h->step_queued) return fail(OLLIN_ESTATE, "no step is queued on this handle");

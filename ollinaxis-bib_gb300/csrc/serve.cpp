@@ -12,17 +12,26 @@
 //   * admission by device bytes: a request's footprint (resident while it
 //     runs, plus what its elliptic solves add while they run) must fit in the
 //     budget beside the resident bytes of the running evolutions;
-//   * a tick queues one coarse step of every running evolution before it
-//     waits for any, so small grids fill the GPU together; the set-up of
-//     newly admitted requests is queued after those steps, on the new
-//     requests' own streams, so it overlaps them;
+//   * every running evolution keeps one coarse step queued on its stream;
+//     a step that has finished is followed at once by the next, without
+//     waiting for the other evolutions, so grids of different sizes keep
+//     the GPU filled together; the set-up of newly admitted requests runs on
+//     their own streams beside the queued steps;
 //   * nothing is shared between evolutions on the device, so a result does
-//     not depend on which other requests ran beside it.
+//     not depend on which other requests ran beside it;
+//   * small grids make a coarse step a few hundred short kernels, so issuing
+//     them binds the loop: the steps of different evolutions are issued from
+//     several host threads at once (each evolution from one thread at a time;
+//     a handle's state is touched by no one else meanwhile).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <deque>
+#include <functional>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/ollin_gpu.h"
@@ -49,11 +58,12 @@ struct Request {
 struct Running {
     Request r;
     ollin_handle* h = nullptr;
-    double t_admit = 0.0;
+    double t_admit = 0.0, t_ready = 0.0;
     int steps = 0;
     double t = 0.0;
     double min_alpha = 1.0;
     bool queued = false;  // a step_begin waits for its step_end
+    int begin_rc = OLLIN_OK;
 };
 
 double min_lapse(ollin_handle* h, double* out_min) {
@@ -68,6 +78,66 @@ double min_lapse(ollin_handle* h, double* out_min) {
     *out_min = m;
     return OLLIN_OK;
 }
+
+// Host threads that run one job per index; the calling thread takes part.
+class Workers {
+  public:
+    explicit Workers(int n) {
+        for (int k = 0; k < n; ++k) th_.emplace_back([this] { loop(); });
+    }
+    ~Workers() {
+        {
+            std::lock_guard<std::mutex> g(m_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        for (std::thread& t : th_) t.join();
+    }
+    // f(0) .. f(n-1), each once; returns when all have returned
+    void run(int n, const std::function<void(int)>& f) {
+        if (n <= 0) return;
+        std::unique_lock<std::mutex> g(m_);
+        job_ = &f;
+        n_ = n;
+        next_ = 0;
+        left_ = n;
+        ++gen_;
+        cv_.notify_all();
+        work(g);
+        done_.wait(g, [this] { return left_ == 0; });
+        job_ = nullptr;
+    }
+
+  private:
+    // takes and runs indices until none is left (called with the lock held)
+    void work(std::unique_lock<std::mutex>& g) {
+        while (job_ && next_ < n_) {
+            const int k = next_++;
+            const std::function<void(int)>* f = job_;
+            g.unlock();
+            (*f)(k);
+            g.lock();
+            if (--left_ == 0) done_.notify_all();
+        }
+    }
+    void loop() {
+        std::unique_lock<std::mutex> g(m_);
+        unsigned long seen = gen_;
+        for (;;) {
+            cv_.wait(g, [&] { return stop_ || gen_ != seen; });
+            if (stop_) return;
+            seen = gen_;
+            work(g);
+        }
+    }
+    std::vector<std::thread> th_;
+    std::mutex m_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)>* job_ = nullptr;
+    int n_ = 0, next_ = 0, left_ = 0;
+    unsigned long gen_ = 0;
+    bool stop_ = false;
+};
 
 bool maximal_at_start(const Request& r) {  // evolve.f90:228-230
     return r.p.slicing == OLLIN_SLICING_MAXIMAL || r.p.ilapse == OLLIN_ILAPSE_MAXIMAL || r.maximalevery != 0;
@@ -87,6 +157,7 @@ struct ollin_server {
     std::vector<Running> running;
     std::deque<ollin_result> done;
     std::chrono::steady_clock::time_point t0;
+    Workers* workers = nullptr;  // issue threads besides the caller's
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -112,6 +183,7 @@ struct ollin_server {
         }
         ollin_result x = result_of(e.r, status);
         x.t_admit = e.t_admit;
+        x.t_ready = e.t_ready;
         x.collapsed = collapsed ? 1 : 0;
         x.steps = e.steps;
         x.t = e.t;
@@ -170,6 +242,7 @@ struct ollin_server {
                 done.push_back(x);
                 continue;
             }
+            e.t_ready = now();
             running.push_back(e);
         }
     }
@@ -183,6 +256,9 @@ int ollin_server_create(size_t budget, int max_active, ollin_server** out) {
     s->budget = budget;
     s->max_active = max_active;
     s->t0 = std::chrono::steady_clock::now();
+    const int hw = (int)std::thread::hardware_concurrency();
+    const int nthreads = std::max(0, std::min({hw > 0 ? hw : 1, max_active, 8}) - 1);
+    s->workers = new Workers(nthreads);
     *out = s;
     return OLLIN_OK;
 }
@@ -190,6 +266,7 @@ int ollin_server_create(size_t budget, int max_active, ollin_server** out) {
 void ollin_server_destroy(ollin_server* s) {
     if (!s) return;
     while (!s->running.empty()) s->retire(s->running.size() - 1, OLLIN_ESTATE, false);
+    delete s->workers;
     delete s;
 }
 
@@ -213,39 +290,50 @@ int ollin_server_submit(ollin_server* s, long long id, const ollin_params* p, in
 
 int ollin_server_tick(ollin_server* s, int* n_active, int* n_waiting) {
     if (!s) return sfail(OLLIN_EINVAL, "null server");
-    // (1) one coarse step of every running evolution, queued before any wait
-    std::vector<int> rc(s->running.size(), OLLIN_OK);
-    for (size_t k = 0; k < s->running.size(); ++k) {
-        Running& e = s->running[k];
-        if (e.steps >= e.r.nsteps) continue;
-        rc[k] = ollin_gpu_step_begin(e.h);
-        e.queued = true;
-    }
-    // (2) admissions: their set-up overlaps the steps on the device
-    const size_t nrun = s->running.size();
-    s->admit();
-    // (3) the steps' ends, the solves that follow a step, the checks
-    std::vector<std::pair<size_t, std::pair<int, bool>>> retire;
-    for (size_t k = 0; k < nrun; ++k) {
-        Running& e = s->running[k];
-        int r = rc[k];
-        if (e.queued) {
-            double t = e.t;
-            const int re = ollin_gpu_step_end(e.h, &t);
-            e.queued = false;
-            if (!r) r = re;
-            if (!r) { e.t = t; e.steps += 1; }
+    for (int spin = 0;; ++spin) {
+        // (1) every evolution whose step finished: the step's end, the solve
+        //     that follows it, the checks, then its next step
+        const size_t nrun = s->running.size();
+        std::vector<int> rc(nrun, OLLIN_OK);
+        std::vector<char> coll(nrun, 0), fin(nrun, 0), moved(nrun, 0);
+        std::vector<int> ready;  // found on this thread: waking the others costs more than a query
+        for (size_t k = 0; k < nrun; ++k)
+            if (!s->running[k].queued || ollin_gpu_step_ready(s->running[k].h)) ready.push_back((int)k);
+        s->workers->run((int)ready.size(), [&](int q) {
+            const int k = ready[(size_t)q];
+            Running& e = s->running[(size_t)k];
+            if (e.queued) {
+                double t = e.t;
+                int r = ollin_gpu_step_end(e.h, &t);
+                e.queued = false;
+                if (e.begin_rc) r = e.begin_rc;
+                if (!r) { e.t = t; e.steps += 1; }
+                if (!r && maximal_after(e.r, e.steps)) r = ollin_gpu_maximal_slicing(e.h, nullptr);
+                if (!r && e.r.collapse > 0.0) {
+                    r = min_lapse(e.h, &e.min_alpha);
+                    coll[(size_t)k] = !r && e.min_alpha < e.r.collapse;
+                }
+                rc[(size_t)k] = r;
+            }
+            moved[(size_t)k] = 1;
+            if (rc[(size_t)k] || coll[(size_t)k] || e.steps >= e.r.nsteps) { fin[(size_t)k] = 1; return; }
+            e.begin_rc = ollin_gpu_step_begin(e.h);
+            e.queued = true;
+        });
+        bool progressed = false;
+        for (size_t q = nrun; q-- > 0;) {
+            progressed = progressed || moved[q];
+            if (fin[q]) s->retire(q, rc[q], coll[q] != 0);
         }
-        if (!r && maximal_after(e.r, e.steps)) r = ollin_gpu_maximal_slicing(e.h, nullptr);
-        bool collapsed = false;
-        if (!r && e.r.collapse > 0.0) {
-            r = min_lapse(e.h, &e.min_alpha);
-            collapsed = !r && e.min_alpha < e.r.collapse;
-        }
-        if (r || collapsed || e.steps >= e.r.nsteps) retire.push_back({k, {r, collapsed}});
+        // (2) admissions: their set-up overlaps the queued steps
+        const size_t before = s->running.size() + s->done.size();
+        s->admit();
+        progressed = progressed || s->running.size() + s->done.size() != before;
+        if (progressed || s->running.empty()) break;
+        // nothing finished yet: wait a little for the queued steps
+        if (spin > 64) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        else std::this_thread::yield();
     }
-    for (size_t q = retire.size(); q-- > 0;) s->retire(retire[q].first, retire[q].second.first, retire[q].second.second);
-    // a request that finished at once (nsteps = 0) retires on the next tick
     if (n_active) *n_active = (int)s->running.size();
     if (n_waiting) *n_waiting = (int)s->waiting.size();
     return OLLIN_OK;

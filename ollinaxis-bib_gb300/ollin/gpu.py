@@ -241,7 +241,7 @@ class Result(ctypes.Structure):
     """ollin_result: the summary of one finished request."""
     _fields_ = [("id", ctypes.c_longlong), ("status", ctypes.c_int), ("collapsed", ctypes.c_int),
                 ("steps", ctypes.c_int), ("ngrids", ctypes.c_int), ("t", ctypes.c_double),
-                ("min_alpha", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("min_alpha", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_ready", ctypes.c_double),
                 ("t_done", ctypes.c_double), ("bytes", ctypes.c_size_t),
                 ("l2", (ctypes.c_double * 4) * RESULT_MAXGRIDS)]
 
