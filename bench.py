@@ -459,9 +459,11 @@ def serving_requests(rng, n):
 
 
 def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
-    """The serving pattern through the request loop (ollin_server_*):
+    """The serving pattern through the request loop (ollin_server_*), coarse
+    steps launched as captured graphs unless stated:
       * plain: the requests one at a time (max_active = 1), all queued at 0;
-      * batched: the same requests with up to 64 running together;
+      * batched: the same requests with up to 64 running together (and again
+        with direct launches);
       * served: Poisson arrivals (seeded) at ``load`` x the batched rate, plus a
         bisection chain on the shell amplitude whose next request is submitted
         when the previous one finishes (collapse = smallest lapse < 0.05).
@@ -473,8 +475,8 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
     rng = np.random.default_rng(seed)
     reqs = serving_requests(rng, n)
 
-    def closed(max_active):
-        s = Server(budget, max_active=max_active)
+    def closed(max_active, graphs=True, reqs=reqs):
+        s = Server(budget, max_active=max_active, graphs=graphs)
         for k, (_, cfg, t_end) in enumerate(reqs):
             s.submit(k, params_from_dict(cfg), t_end, 0.05 if cfg.get("mattertype") == "scalar" else 0.0)
         t = time.perf_counter()
@@ -485,6 +487,17 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
 
     t_plain, plain = closed(1)
     t_bat, bat = closed(64)
+    t_direct, _ = closed(64, graphs=False)
+    pu = sum(r.point_updates for r in plain.values())
+    # the small end of the mix alone: 32 punctures of 3 levels of 64^2 (the
+    # plain-method configuration's grids), where one evolution fills a few
+    # SMs and the plain path is bound by kernel latency
+    small = [(0, dict(reqs[0][1] if reqs[0][0] == 0 else next(c for kd, c, _ in reqs if kd == 0),
+                      nrtotal=64, nztotal=64, dr0=0.2, dz0=0.2), 2.0)] * 32
+    t_sp, sp = closed(1, reqs=small)
+    t_sb, _ = closed(64, reqs=small)
+    t_sd, _ = closed(64, graphs=False, reqs=small)
+    pu_s = sum(r.point_updates for r in sp.values())
     rate = load * n / t_bat
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
     chain_cfg = dict(reqs[0][1]) if reqs[0][0] == 1 else None
@@ -530,6 +543,12 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
                         % (n, chain),
             "budget_bytes": budget, "peak_reserved_bytes": peak, "most_running": peak_run,
             "plain_runs_per_s": n / t_plain, "batched_runs_per_s": n / t_bat, "batched_vs_plain": t_plain / t_bat,
+            "batched_direct_launch_runs_per_s": n / t_direct,
+            "plain_point_updates_per_s": pu / t_plain, "batched_point_updates_per_s": pu / t_bat,
+            "small_grids": {"workload": "32 Schwarzschild punctures, 3 levels of 64^2, t_end 2 (40 coarse steps)",
+                            "plain_runs_per_s": 32 / t_sp, "batched_runs_per_s": 32 / t_sb,
+                            "batched_vs_plain": t_sp / t_sb, "batched_direct_launch_runs_per_s": 32 / t_sd,
+                            "batched_point_updates_per_s": pu_s / t_sb},
             "served": {"arrival_rate_per_s": rate, "runs_per_s": (n + chain) / t_served,
                        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99))},
             "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99)),

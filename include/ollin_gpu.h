@@ -246,6 +246,11 @@ int ollin_gpu_step_end(ollin_handle* h, double* t_out);
 /* 1 when ollin_gpu_step_end would not wait (the queued step has finished, or
  * none is queued), 0 while the step runs.  Does not block. */
 int ollin_gpu_step_ready(const ollin_handle* h);
+/* enable = 1: ollin_gpu_step_begin records the coarse step by stream capture
+ * and launches it as one CUDA graph (same kernels, arguments and order, so
+ * the same results); 0: direct launches (the default); -1: leave as is.
+ * ``stats`` (may be null) gets the graphs instantiated and updated so far. */
+int ollin_gpu_step_graphs(ollin_handle* h, int enable, long long stats[2]);
 
 /* Device bytes an evolution with parameters ``p`` holds from create to
  * destroy (``resident``), and the most its elliptic solves (initial data,
@@ -289,6 +294,7 @@ typedef struct ollin_result {
                                                   admitted, set up (initial data done), finished */
     size_t bytes;       /* resident + transient bytes reserved for it */
     double l2[OLLIN_RESULT_MAXGRIDS][4];  /* per grid at the end: L2 norms of alpha, phi, trK, ham (save0Ddata.f90:221-288) */
+    double point_updates;                 /* grid points advanced by one full step, summed over its steps */
 } ollin_result;
 
 /* ``budget``: device bytes the server's evolutions may hold; ``max_active``:
@@ -311,6 +317,9 @@ int ollin_server_tick(ollin_server* s, int* n_active, int* n_waiting);
 /* Move up to ``max`` finished results, oldest first, into ``out``; ``n_out``
  * gets the number moved. */
 int ollin_server_poll(ollin_server* s, ollin_result* out, int max, int* n_out);
+/* Whether evolutions admitted from now on step as captured graphs
+ * (ollin_gpu_step_graphs; on by default). */
+int ollin_server_set_graphs(ollin_server* s, int enable);
 /* Device bytes reserved now and at most so far by the server's evolutions. */
 int ollin_server_usage(const ollin_server* s, size_t* used, size_t* peak);
 /* Message for the last failure of an ollin_server_* call on the calling thread. */

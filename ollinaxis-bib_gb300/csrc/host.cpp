@@ -107,6 +107,11 @@ struct ollin_handle {
     long long launches = 0;
     bool initialized = false;
     bool step_queued = false;  // ollin_gpu_step_begin ran, ollin_gpu_step_end not yet
+    // ollin_gpu_step_graphs: a coarse step is captured and replayed as one
+    // graph launch (the executable graph is updated in place each step)
+    bool graphs = false;
+    cudaGraphExec_t gexec = nullptr;
+    long long graph_updates = 0, graph_instantiations = 0;
     bool shift = false, scalar = false;
     PhysParams phys{};
     // optional per-launch timing of the right-hand-side kernel
@@ -2143,6 +2148,7 @@ void ollin_gpu_destroy(ollin_handle* h) {
     if (h->d_flag) cudaFree(h->d_flag);
     if (h->d_norm) cudaFree(h->d_norm);
     for (cudaEvent_t e : h->ev) cudaEventDestroy(e);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -2267,14 +2273,63 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
     return OLLIN_OK;
 }
 
+// One coarse step recorded by stream capture into a graph and launched as
+// one unit: the kernels, their arguments and their order are those of the
+// direct launches, so the results are the same bit for bit; what changes is
+// that the driver gets one submission instead of a few hundred.  The step's
+// scalars (times, interpolation weights, slot pointers) differ from step to
+// step, so each step is captured again and the executable graph updated in
+// place; a step whose launch structure differs from the last (the first
+// steps, a maximal solve's stale lapse, a syncboxes copy) instantiates anew.
+static int captured_step(ollin_handle* h) {
+    CUDA_OR_FAIL(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = onestep(h, 0);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->stream, &g);
+    if (rc || ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : fail(OLLIN_ECUDA, std::string("step capture: ") + cudaGetErrorString(ec));
+    }
+    if (h->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(h->gexec, g, &info) == cudaSuccess) {
+            h->graph_updates++;
+        } else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+    }
+    if (!h->gexec) {
+        const cudaError_t ei = cudaGraphInstantiate(&h->gexec, g, 0);
+        if (ei != cudaSuccess) {
+            h->gexec = nullptr;
+            cudaGraphDestroy(g);
+            return fail(OLLIN_ECUDA, std::string("graph instantiation: ") + cudaGetErrorString(ei));
+        }
+        h->graph_instantiations++;
+    }
+    cudaGraphDestroy(g);
+    CUDA_OR_FAIL(cudaGraphLaunch(h->gexec, h->stream));
+    return OLLIN_OK;
+}
+
 int ollin_gpu_step_begin(ollin_handle* h) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
     if (h->step_queued) return fail(OLLIN_ESTATE, "a step is already queued on this handle");
-    int rc = onestep(h, 0);
+    int rc = h->graphs && !h->ktime ? captured_step(h) : onestep(h, 0);
     // queued work runs to its end whatever happened: the next end waits for it
     h->step_queued = true;
     return rc;
+}
+
+int ollin_gpu_step_graphs(ollin_handle* h, int enable, long long* stats) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    if (enable >= 0) h->graphs = enable != 0;
+    if (stats) { stats[0] = h->graph_instantiations; stats[1] = h->graph_updates; }
+    return OLLIN_OK;
 }
 
 int ollin_gpu_step_ready(const ollin_handle* h) {

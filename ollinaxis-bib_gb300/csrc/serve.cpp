@@ -158,6 +158,7 @@ struct ollin_server {
     std::deque<ollin_result> done;
     std::chrono::steady_clock::time_point t0;
     Workers* workers = nullptr;  // issue threads besides the caller's
+    int graphs = 1;              // coarse steps as captured graphs (ollin_gpu_step_graphs)
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -189,6 +190,7 @@ struct ollin_server {
         x.t = e.t;
         x.min_alpha = e.min_alpha;
         x.ngrids = ollin_gpu_num_levels(e.h);
+        x.point_updates = ollin_gpu_point_updates(e.h);
         if (status == OLLIN_OK) {
             static const int fields[4] = {OLLIN_F_ALPHA, OLLIN_F_PHI, OLLIN_F_TRK, OLLIN_F_HAM};
             for (int l = 0; l < std::min(x.ngrids, OLLIN_RESULT_MAXGRIDS) && x.status == OLLIN_OK; ++l)
@@ -215,6 +217,7 @@ struct ollin_server {
     int start(Request& r, Running& e) {
         int rc = ollin_gpu_create(&r.p, &e.h);
         if (rc) { e.h = nullptr; return rc; }
+        ollin_gpu_step_graphs(e.h, graphs, nullptr);
         rc = ollin_gpu_initial_data(e.h);
         if (!rc) rc = ollin_gpu_initialize(e.h);
         if (!rc && maximal_at_start(r)) rc = ollin_gpu_maximal_slicing(e.h, nullptr);
@@ -347,6 +350,12 @@ int ollin_server_poll(ollin_server* s, ollin_result* out, int max, int* n_out) {
         s->done.pop_front();
     }
     *n_out = n;
+    return OLLIN_OK;
+}
+
+int ollin_server_set_graphs(ollin_server* s, int enable) {
+    if (!s) return sfail(OLLIN_EINVAL, "null server");
+    s->graphs = enable != 0;
     return OLLIN_OK;
 }
 

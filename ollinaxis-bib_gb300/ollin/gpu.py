@@ -87,6 +87,8 @@ def load(build_if_missing=True):
     L.ollin_server_poll.argtypes = [vp, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.ollin_server_usage.argtypes = [vp, sp, sp]
     L.ollin_server_last_error.restype = ctypes.c_char_p
+    L.ollin_server_set_graphs.argtypes = [vp, ctypes.c_int]
+    L.ollin_gpu_step_graphs.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
     _lib = L
     return L
 
@@ -185,6 +187,21 @@ class Evolution:
     def kernel_timing(self, enable=True):
         self._check(self.L.ollin_gpu_kernel_timing(self.h, 1 if enable else 0))
 
+    def step_graphs(self, enable=None):
+        """Turn graph-captured steps on/off (None: leave); returns
+        (graphs instantiated, graph updates) so far."""
+        st = (ctypes.c_longlong * 2)()
+        self._check(self.L.ollin_gpu_step_graphs(self.h, -1 if enable is None else int(bool(enable)), st))
+        return st[0], st[1]
+
+    def step_begin(self):
+        self._check(self.L.ollin_gpu_step_begin(self.h))
+
+    def step_end(self):
+        t = ctypes.c_double()
+        self._check(self.L.ollin_gpu_step_end(self.h, ctypes.byref(t)))
+        return t.value
+
     def maximal_slicing(self, va_max=None):
         """maximalslicing.f90 on every level (ollin_gpu_maximal_slicing);
         va_max = (r, z) maxima of the slicing speeds of the host's last
@@ -243,7 +260,7 @@ class Result(ctypes.Structure):
                 ("steps", ctypes.c_int), ("ngrids", ctypes.c_int), ("t", ctypes.c_double),
                 ("min_alpha", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double), ("t_ready", ctypes.c_double),
                 ("t_done", ctypes.c_double), ("bytes", ctypes.c_size_t),
-                ("l2", (ctypes.c_double * 4) * RESULT_MAXGRIDS)]
+                ("l2", (ctypes.c_double * 4) * RESULT_MAXGRIDS), ("point_updates", ctypes.c_double)]
 
     def norms(self):
         """(ngrids, 4) array: L2 norms of alpha, phi, trK, ham per grid."""
@@ -255,11 +272,12 @@ class Server:
     """The request loop of the C ABI (ollin_server_*): continuous batching of
     evolutions on the current device, admitted against a byte budget."""
 
-    def __init__(self, budget_bytes, max_active=64):
+    def __init__(self, budget_bytes, max_active=64, graphs=True):
         self.L = load()
         h = ctypes.c_void_p()
         self._check(self.L.ollin_server_create(int(budget_bytes), int(max_active), ctypes.byref(h)))
         self.h = h
+        self._check(self.L.ollin_server_set_graphs(self.h, 1 if graphs else 0))
 
     def _check(self, rc):
         if rc != 0:
