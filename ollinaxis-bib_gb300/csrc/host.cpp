@@ -2216,10 +2216,8 @@ int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_
 
 int ollin_gpu_initial_data(ollin_handle* h) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
-    const ollin_params& P = h->P;
-    (void)P;
-    // scalar-field slots start at zero; a scalar pulse needs the elliptic
-    // solve of idata_scalarpulse.f90 and is uploaded by the caller
+    // analytic data, or the elliptic solve of idata_scalarpulse.f90 /
+    // idata_brillwave.f90 on the device
     return initial_data(h);
 }
 

@@ -109,3 +109,20 @@ def test_collapse_threshold_stops_early():
     assert out[0].status == 0 and out[0].collapsed == 1 and out[0].steps == 1 and out[0].min_alpha < 0.05
     assert out[1].status == 0 and out[1].collapsed == 0 and out[1].min_alpha > 0.5
     assert out[1].steps == int(np.ceil(0.8 / (0.25 * 0.4) - 1e-9))
+
+
+def test_a_failing_request_ends_alone():
+    """An unstable Courant factor (dtfac = 3) makes the evolution overflow
+    within a few steps: its request ends with OLLIN_ENAN, and the request
+    running beside it is unaffected."""
+    from ollin.gpu import Server
+    good = (dict(C1, nrtotal=32, nztotal=32, nl0=1), 0, 0.5, 0.0)
+    s = Server(1 << 36, max_active=1)
+    submit_all(s, [good])
+    (alone,) = s.drain()
+    s = Server(1 << 36, max_active=4)
+    submit_all(s, [(dict(C1, nrtotal=24, nztotal=24, nl0=0, dtfac=3.0), 0, 5.0, 0.0), good])
+    out = {r.id: r for r in s.drain()}
+    assert out[0].status == 3 and 0 < out[0].steps < 10
+    assert out[1].status == 0 and np.array_equal(out[1].norms(), alone.norms())
+    assert s.usage()[0] == 0
