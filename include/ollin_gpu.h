@@ -235,6 +235,11 @@ int ollin_gpu_coarse_step(ollin_handle* h, double* t_out);
  * in its loop over them). */
 int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out);
 
+/* The smallest lapse over every grid (the minimum of save0Ddata.f90:221-288 on
+ * each grid's interior, then over grids): one queued reduction per grid, one
+ * copy, one wait.  OLLIN_ENAN if a lapse is NaN. */
+int ollin_gpu_min_lapse(ollin_handle* h, double* out);
+
 /* One coarse step split in two, for callers that overlap several evolutions
  * (the request loop below): ollin_gpu_step_begin queues ``onestep(0)`` on the
  * handle's stream and returns without waiting; ollin_gpu_step_end waits for

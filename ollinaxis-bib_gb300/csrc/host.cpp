@@ -327,6 +327,10 @@ PhysParams make_phys(const ollin_params& P) {
 }
 
 // ---- kernel launch helpers ---------------------------------------------------
+// d_norm: 8 result slots per grid, then the first pass's block partials
+size_t norm_scratch(const ollin_handle* h) { return 8 * (size_t)h->nlev + 5 * (size_t)kNormMaxBlocks; }
+double* norm_partials(const ollin_handle* h) { return h->d_norm + 8 * (size_t)h->nlev; }
+
 int after_launch(ollin_handle* h) {
     h->launches++;
     cudaError_t e = cudaGetLastError();
@@ -2107,7 +2111,7 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
         delete h;
         return fail(OLLIN_ECUDA, "cudaStreamCreate failed");
     }
-    if (cudaMalloc(&h->d_flag, 64) != cudaSuccess || cudaMalloc(&h->d_norm, 8 * sizeof(double)) != cudaSuccess) {
+    if (cudaMalloc(&h->d_flag, 64) != cudaSuccess || cudaMalloc(&h->d_norm, norm_scratch(h) * sizeof(double)) != cudaSuccess) {
         ollin_gpu_destroy(h);
         return fail(OLLIN_ENOMEM, "device allocation failed");
     }
@@ -2436,7 +2440,7 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
     }
     // the origin value only for box 0 (save0Ddata.f90:370-374)
     launch_norms(L.G, src, L.box == 0 ? h->P.interp_bicubic : -1, h->rminl[level], h->zminl[level], h->rmaxl[level],
-                 h->zmaxl[level], h->d_norm, h->stream);
+                 h->zmaxl[level], h->d_norm, norm_partials(h), h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
     double res[6];
@@ -2444,6 +2448,28 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     if (res[5] != 0.0) return fail(OLLIN_ENAN, "NaN found in the field (save0Ddata.f90:229-264)");
     for (int k = 0; k < 5; ++k) out[k] = res[k];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_min_lapse(ollin_handle* h, double* out) {
+    if (!h || !out) return fail(OLLIN_EINVAL, "null argument");
+    // every grid's statistics queued, then one copy and one wait
+    for (int l = 0; l < h->nlev; ++l) {
+        DLevel& L = h->L[l];
+        launch_norms(L.G, base_ptr(L, L.slot[L.cur][F_ALPHA]), -1, 0.0, 0.0, 0.0, 0.0, h->d_norm + 8 * (size_t)l,
+                     norm_partials(h), h->stream);
+        int rc = after_launch(h);
+        if (rc) return rc;
+    }
+    std::vector<double> res(8 * (size_t)h->nlev);
+    CUDA_OR_FAIL(cudaMemcpyAsync(res.data(), h->d_norm, res.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    double m = HUGE_VAL;
+    for (int l = 0; l < h->nlev; ++l) {
+        if (res[8 * (size_t)l + 5] != 0.0) return fail(OLLIN_ENAN, "NaN found in the lapse");
+        m = std::min(m, res[8 * (size_t)l + 1]);
+    }
+    *out = m;
     return OLLIN_OK;
 }
 

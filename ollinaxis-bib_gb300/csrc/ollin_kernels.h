@@ -352,8 +352,13 @@ void launch_aux_point(const AuxArgs& a, cudaStream_t s);
 void launch_aux_deriv(const AuxArgs& a, cudaStream_t s);
 void launch_symmetry(const SymArgs& a, cudaStream_t s);
 void launch_restrict(const RestrictArgs& a, cudaStream_t s);
+// 0-D statistics: max, min, max|f|, RMS, origin value, NaN flag into
+// dev_out[0..5]; ``partials`` holds 5 doubles per block of the first pass
+// (at most kNormMaxBlocks blocks).
+constexpr int kNormThreads = 256, kNormMaxBlocks = 4 * 152;
+int norm_blocks(const LevelGeom& G);
 void launch_norms(const LevelGeom& G, const double* f, int origin_bicubic, double rminl, double zminl,
-                  double rmaxl, double zmaxl, double* dev_out, cudaStream_t s);
+                  double rmaxl, double zmaxl, double* dev_out, double* partials, cudaStream_t s);
 void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s);
 void launch_gammadriver_init(const LevelGeom& G, double* dtbr, double* dtbz, const double* dlr,
                              const double* dlz, double csi, cudaStream_t s);

@@ -66,18 +66,7 @@ struct Running {
     int begin_rc = OLLIN_OK;
 };
 
-double min_lapse(ollin_handle* h, double* out_min) {
-    double m = HUGE_VAL;
-    const int n = ollin_gpu_num_levels(h);
-    for (int l = 0; l < n; ++l) {
-        double nm[5];
-        int rc = ollin_gpu_norms(h, l, OLLIN_F_ALPHA, nm);
-        if (rc) return rc;
-        m = std::min(m, nm[1]);
-    }
-    *out_min = m;
-    return OLLIN_OK;
-}
+int min_lapse(ollin_handle* h, double* out_min) { return ollin_gpu_min_lapse(h, out_min); }
 
 // Host threads that run one job per index; the calling thread takes part.
 class Workers {

@@ -12,6 +12,8 @@
 //    fixed-order block reduction.
 // The transfer arithmetic uses explicitly rounded operations (no FMA
 // contraction) so that it reproduces the reference's sequence of roundings.
+#include <algorithm>
+
 #include "ollin_kernels.h"
 
 namespace ollin {
@@ -381,52 +383,92 @@ __global__ void __launch_bounds__(128) inject_kernel(const __grid_constant__ Inj
 }
 
 // ---- 0-D statistics (save0Ddata.f90:221-288, origin value :370-374) --------
-// One block; each thread walks the points in a fixed order and the partial
-// results are combined in a fixed tree, so the result does not depend on
-// scheduling.
-__global__ void __launch_bounds__(512) norms_kernel(LevelGeom G, const double* f, int bicubic,
-                                                    double rminl, double zminl, double rmaxl, double zmaxl,
-                                                    double* out) {
-    __shared__ double smax[512], smin[512], snm1[512], snm2[512];
-    __shared__ int snan[512];
+// Two passes, both deterministic: the partial pass gives each of nb blocks a
+// fixed set of points (a grid-stride walk) and combines its threads by warp
+// shuffles in a fixed tree, then its 8 warps in a fixed order; the final
+// pass combines the nb partials the same way in one block.  So the result
+// depends on the grid size only, never on scheduling.  (The reference sums
+// in loop order; the tree order changes the sum of squares by rounding
+// only.)
+struct NormAcc {
+    double vmax, vmin, nm1, nm2;
+    int nan;
+};
+
+__device__ __forceinline__ NormAcc norm_combine(NormAcc a, const NormAcc& b) {
+    a.vmax = fmax(a.vmax, b.vmax);
+    a.vmin = fmin(a.vmin, b.vmin);
+    a.nm1 = fmax(a.nm1, b.nm1);
+    a.nm2 = a.nm2 + b.nm2;
+    a.nan |= b.nan;
+    return a;
+}
+
+// the block's threads combined into thread 0 (blockDim.x == kNormThreads)
+__device__ __forceinline__ NormAcc norm_block(NormAcc a) {
+    __shared__ NormAcc warp_acc[kNormThreads / 32];
+    for (int off = 16; off > 0; off >>= 1) {
+        NormAcc b;
+        b.vmax = __shfl_down_sync(0xffffffffu, a.vmax, off);
+        b.vmin = __shfl_down_sync(0xffffffffu, a.vmin, off);
+        b.nm1 = __shfl_down_sync(0xffffffffu, a.nm1, off);
+        b.nm2 = __shfl_down_sync(0xffffffffu, a.nm2, off);
+        b.nan = __shfl_down_sync(0xffffffffu, a.nan, off);
+        a = norm_combine(a, b);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_acc[warp] = a;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        a = warp_acc[0];
+        for (int w = 1; w < kNormThreads / 32; ++w) a = norm_combine(a, warp_acc[w]);
+    }
+    return a;
+}
+
+__global__ void __launch_bounds__(kNormThreads) norms_partial_kernel(LevelGeom G, const double* f, double* part) {
     const int ni = G.nr - G.g, nj = G.nz - G.g;
     const long npts = (long)ni * nj;
-    double vmax = -1.0e10, vmin = 1.0e10, nm1 = 0.0, nm2 = 0.0;
-    int nan = 0;
-    for (long q = threadIdx.x; q < npts; q += blockDim.x) {
+    NormAcc a{-1.0e10, 1.0e10, 0.0, 0.0, 0};
+    for (long q = blockIdx.x * (long)kNormThreads + threadIdx.x; q < npts; q += (long)gridDim.x * kNormThreads) {
         const int i = 1 + (int)(q % ni), j = 1 + (int)(q / ni);
         const double v = f[(size_t)i + (size_t)j * G.ld];
-        if (v != v) nan = 1;
-        vmax = fmax(vmax, v);
-        vmin = fmin(vmin, v);
-        nm1 = fmax(nm1, fabs(v));
-        nm2 = nm2 + v * v;
+        if (v != v) a.nan = 1;
+        a.vmax = fmax(a.vmax, v);
+        a.vmin = fmin(a.vmin, v);
+        a.nm1 = fmax(a.nm1, fabs(v));
+        a.nm2 = a.nm2 + v * v;
     }
-    smax[threadIdx.x] = vmax; smin[threadIdx.x] = vmin; snm1[threadIdx.x] = nm1; snm2[threadIdx.x] = nm2;
-    snan[threadIdx.x] = nan;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) {
-            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + w]);
-            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + w]);
-            snm1[threadIdx.x] = fmax(snm1[threadIdx.x], snm1[threadIdx.x + w]);
-            snm2[threadIdx.x] = snm2[threadIdx.x] + snm2[threadIdx.x + w];
-            snan[threadIdx.x] |= snan[threadIdx.x + w];
-        }
-        __syncthreads();
-    }
+    a = norm_block(a);
     if (threadIdx.x == 0) {
-        out[0] = smax[0];
-        out[1] = smin[0];
-        out[2] = snm1[0];
-        out[3] = sqrt(snm2[0] / (double)npts);
+        double* p = part + 5 * (size_t)blockIdx.x;
+        p[0] = a.vmax; p[1] = a.vmin; p[2] = a.nm1; p[3] = a.nm2; p[4] = a.nan ? 1.0 : 0.0;
+    }
+}
+
+__global__ void __launch_bounds__(kNormThreads) norms_final_kernel(LevelGeom G, const double* f, int bicubic,
+                                                                   double rminl, double zminl, double rmaxl,
+                                                                   double zmaxl, const double* part, int nb,
+                                                                   double* out) {
+    NormAcc a{-1.0e10, 1.0e10, 0.0, 0.0, 0};
+    for (int b = threadIdx.x; b < nb; b += kNormThreads) {
+        const double* p = part + 5 * (size_t)b;
+        a = norm_combine(a, NormAcc{p[0], p[1], p[2], p[3], p[4] != 0.0 ? 1 : 0});
+    }
+    a = norm_block(a);
+    if (threadIdx.x == 0) {
+        const long npts = (long)(G.nr - G.g) * (G.nz - G.g);
+        out[0] = a.vmax;
+        out[1] = a.vmin;
+        out[2] = a.nm1;
+        out[3] = sqrt(a.nm2 / (double)npts);
         if (bicubic >= 0) {
             InterpPt p;
             out[4] = interp_weights(G, rminl, rmaxl, zminl, zmaxl, 0.0, 0.0, bicubic, p) ? interp_apply(G, f, p) : 0.0;
         } else {
             out[4] = 0.0;  // save0Ddata.f90:370-374 writes origin data for box 0 only
         }
-        out[5] = snan[0] ? 1.0 : 0.0;
+        out[5] = a.nan ? 1.0 : 0.0;
     }
 }
 
@@ -543,9 +585,17 @@ void launch_restrict(const RestrictArgs& a, cudaStream_t s) {
     restrict_kernel<<<grd, blk, 0, s>>>(a);
 }
 
+int norm_blocks(const LevelGeom& G) {
+    const long npts = (long)(G.nr - G.g) * (G.nz - G.g);
+    const long nb = (npts + 4L * kNormThreads - 1) / (4L * kNormThreads);  // about 4 points per thread
+    return (int)std::max(1L, std::min((long)kNormMaxBlocks, nb));
+}
+
 void launch_norms(const LevelGeom& G, const double* f, int bicubic, double rminl, double zminl,
-                  double rmaxl, double zmaxl, double* dev_out, cudaStream_t s) {
-    norms_kernel<<<1, 512, 0, s>>>(G, f, bicubic, rminl, zminl, rmaxl, zmaxl, dev_out);
+                  double rmaxl, double zmaxl, double* dev_out, double* partials, cudaStream_t s) {
+    const int nb = norm_blocks(G);
+    norms_partial_kernel<<<nb, kNormThreads, 0, s>>>(G, f, partials);
+    norms_final_kernel<<<1, kNormThreads, 0, s>>>(G, f, bicubic, rminl, zminl, rmaxl, zmaxl, partials, nb, dev_out);
 }
 
 void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s) {

@@ -75,6 +75,7 @@ def load(build_if_missing=True):
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_min_lapse.argtypes = [vp, dp]
     L.ollin_gpu_step_begin.argtypes = [vp]
     L.ollin_gpu_step_end.argtypes = [vp, dp]
     sp = ctypes.POINTER(ctypes.c_size_t)
@@ -193,6 +194,11 @@ class Evolution:
         st = (ctypes.c_longlong * 2)()
         self._check(self.L.ollin_gpu_step_graphs(self.h, -1 if enable is None else int(bool(enable)), st))
         return st[0], st[1]
+
+    def min_lapse(self):
+        out = ctypes.c_double()
+        self._check(self.L.ollin_gpu_min_lapse(self.h, ctypes.byref(out)))
+        return out.value
 
     def step_begin(self):
         self._check(self.L.ollin_gpu_step_begin(self.h))

@@ -126,3 +126,17 @@ def test_a_failing_request_ends_alone():
     assert out[0].status == 3 and 0 < out[0].steps < 10
     assert out[1].status == 0 and np.array_equal(out[1].norms(), alone.norms())
     assert s.usage()[0] == 0
+
+
+def test_min_lapse_is_the_smallest_level_minimum():
+    """ollin_gpu_min_lapse (one copy for all grids) against the minima of the
+    per-grid statistics, on a box hierarchy and after steps."""
+    from ollin.gpu import Evolution
+    cfg = dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.25, dz0=0.25, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0)
+    e = Evolution(params(cfg))
+    e.initial_data()
+    e.initialize()
+    for _ in range(3):
+        e.step()
+        m = min(e.norms(lev, "alpha")[1] for lev in e.levels())
+        assert e.min_lapse() == m
