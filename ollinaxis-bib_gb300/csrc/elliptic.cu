@@ -142,13 +142,15 @@ __global__ void __launch_bounds__(256) wave_residual_kernel(const double* partia
 // in z); the other ghosts follow from the parity fill
 __global__ void __launch_bounds__(128) pulse_xi_kernel(const __grid_constant__ PulseCoeffArgs a) {
     const LevelGeom& G = a.G;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    // on a grid off the axis the ghost columns too: diff1z covers them, while
+    // diff1r leaves xi_r there unset (zero in data that start from zero)
+    const int i = (G.axis ? 1 : 1 - G.g) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const long ld = G.ld;
     const size_t o = (size_t)i + (size_t)j * ld;
     const double* f = a.sphi + o;
-    a.xir[o] = d1(f, 1, pclass(i, G.nr, G.g), G.idr * (1.0 / 12.0));
+    a.xir[o] = i < 1 ? 0.0 : d1(f, 1, pclass(i, G.nr, G.g), G.idr * (1.0 / 12.0));
     a.xiz[o] = d1(f, ld, pclass(j, G.nz, G.g), G.idz * (1.0 / 12.0));
 }
 
@@ -324,11 +326,14 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
         }
     }
     __syncthreads();
-    // parity fill: axis first over all rows, then the equator (:772-784)
-    for (int j = 1 - g + (int)threadIdx.x; j <= nz; j += blockDim.x)
-        for (int i = 1; i <= g; ++i) U(1 - i, j) = U(i, j);
+    // parity fill: axis first over all rows, then the equator (:772-784),
+    // on a grid that owns them (a refinement box off the axis or the
+    // equator keeps its interpolated ghosts as Dirichlet values)
+    if (G.axis)
+        for (int j = 1 - g + (int)threadIdx.x; j <= nz; j += blockDim.x)
+            for (int i = 1; i <= g; ++i) U(1 - i, j) = U(i, j);
     __syncthreads();
-    if (G.eqsym)
+    if (G.equator)
         for (int i = 1 - g + (int)threadIdx.x; i <= nr; i += blockDim.x)
             for (int j = 1; j <= g; ++j) U(i, 1 - j) = U(i, j);
     if (threadIdx.x == 0) {
@@ -792,7 +797,8 @@ void launch_wave_residual(const double* partial, int nparts, int nr, int nz, Ell
 
 void launch_pulse_xi(const PulseCoeffArgs& a, cudaStream_t s) {
     dim3 blk(32, 4);
-    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
+    const int ni = a.G.axis ? a.G.nr : a.G.nr + a.G.g;
+    dim3 grd((ni + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
     pulse_xi_kernel<<<grd, blk, 0, s>>>(a);
 }
 

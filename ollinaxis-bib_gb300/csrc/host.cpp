@@ -169,8 +169,8 @@ int check_params(const ollin_params& P) {
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     if (P.nb < 0 || P.nb > 3) return fail(OLLIN_EINVAL, "The number of refinement boxes must be between 0 and 3");
     if (P.nb > 0 && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
-        P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "elliptic initial data with refinement boxes needs ELL_solver = wave on the device");
+        P.ell_solver == OLLIN_ELL_MIXED)
+        return fail(OLLIN_EINVAL, "elliptic initial data with refinement boxes needs ELL_solver = wave or sor");
     for (int b = 0; b < P.nb; ++b)
         if (P.nl[b] < 0 || P.nl[b] >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl of a refinement box out of range");
     return OLLIN_OK;
@@ -1462,8 +1462,9 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
     // the Robin edges are staged in shared memory (six doubles per edge point)
     if (sor_finish_smem(h->L[0].G) > (size_t)200 * 1024)
         return fail(OLLIN_EINVAL, "ELL_solver = sor on the device supports Nrtotal + Nztotal up to 4260");
-    // partial sums of the two passes (every level has the same dimensions)
-    const int nparts = sor_pass_blocks(h->L[0].G);
+    // partial sums of the two passes (the largest grid's count)
+    int nparts = 1;
+    for (const DLevel& L : h->L) nparts = std::max(nparts, sor_pass_blocks(L.G));
     if (S.nparts < nparts) {
         cudaFree(S.partial);
         S.partial = nullptr;
@@ -1488,17 +1489,21 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
                          + L0.dr / L0.dz * std::cos(pi / (double)(L0.nz + L0.g))) / (L0.dz / L0.dr + L0.dr / L0.dz);
     int rc = sor_level(h, S, 0, true, rjac, &S.steps[0]);
     if (rc) return rc;
-    for (int l = 1; l < h->nlev; ++l) {  // sor_elliptic.f90:268-530
+    // sor_elliptic.f90:293-491: every box, levels 1..Nl(box), in the grid
+    // list's order; each grid starts from and is bounded by interpolation
+    // from its parent (box 0's level 0 for level 1, else its box's coarser level)
+    for (int l = 1; l < h->nlev; ++l) {
         DLevel& F = h->L[l];
-        DLevel& C = h->L[l - 1];
+        const int pl = F.parent;
+        DLevel& C = h->L[pl];
         InjectArgs a{};
         a.F = F.G;
         a.Cg = C.G;
-        a.cin = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.cin = base_ptr(C, S.W[pl].u[S.W[pl].cur]);
         a.fout = base_ptr(F, S.W[l].u[S.W[l].cur]);
         a.rminl_f = h->rminl[l]; a.zminl_f = h->zminl[l];
-        a.rminl_c = h->rminl[l - 1]; a.rmaxl_c = h->rmaxl[l - 1];
-        a.zminl_c = h->zminl[l - 1]; a.zmaxl_c = h->zmaxl[l - 1];
+        a.rminl_c = h->rminl[pl]; a.rmaxl_c = h->rmaxl[pl];
+        a.zminl_c = h->zminl[pl]; a.zmaxl_c = h->zmaxl[pl];
         a.bicubic = P.interp_bicubic;
         launch_inject(a, h->stream);
         rc = after_launch(h);
@@ -1508,19 +1513,20 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
         if (rc) return rc;
         if (l == 1) S.steps[1] = it;
     }
-    for (int l = 1; l < h->nlev; ++l) {  // sor_elliptic.f90:534-555
+    for (int l = 1; l < h->nlev; ++l) {  // sor_elliptic.f90:497-521, the same order
         DLevel& F = h->L[l];
-        DLevel& C = h->L[l - 1];
+        const int pl = F.parent;
+        DLevel& C = h->L[pl];
         RestrictArgs a{};
         a.F = F.G;
         a.Cg = C.G;
         a.nf = 1;
         a.fid[0] = 0;
         a.fin[0] = base_ptr(F, S.W[l].u[S.W[l].cur]);
-        a.cout[0] = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.cout[0] = base_ptr(C, S.W[pl].u[S.W[pl].cur]);
         a.rminl_f = h->rminl[l]; a.rmaxl_f = h->rmaxl[l];
         a.zminl_f = h->zminl[l]; a.zmaxl_f = h->zmaxl[l];
-        a.rminl_c = h->rminl[l - 1]; a.zminl_c = h->zminl[l - 1];
+        a.rminl_c = h->rminl[pl]; a.zminl_c = h->zminl[pl];
         a.eqsym = P.eqsym;
         a.bicubic = P.interp_bicubic;
         launch_restrict(a, h->stream);
@@ -1947,8 +1953,8 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
     if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE)
         return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave on the device");
-    if (h->nb > 0 && P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "maximal slicing with refinement boxes needs ELL_solver = wave on the device");
+    if (h->nb > 0 && P.ell_solver == OLLIN_ELL_MIXED)
+        return fail(OLLIN_EINVAL, "maximal slicing with refinement boxes needs ELL_solver = wave or sor");
     if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
         return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor or mixed");
     // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)

@@ -368,7 +368,6 @@ static void sor_physical_coeffs(Level& L, int i, int j, bool fine, double& a, do
 
 void sor_elliptic(Sim& S, bool physical) {
     const ollin_params& P = S.P;
-    if (S.Nb > 0) throw std::runtime_error("oracle: the elliptic solvers are restated for box 0 only");
     const int nlev = (int)S.L.size();
     for (Level& L : S.L)
         for (double& x : L.a("ell_u").v) x = 1.0;
@@ -398,7 +397,7 @@ void sor_elliptic(Sim& S, bool physical) {
                     d(i + g, j + g) = one / p2(dz);
                     e(i + g, j + g) = -two * (one / p2(dr) + one / p2(dz)) + S1(i, j);
                 } else {
-                    sor_physical_coeffs(L, i, j, level > 0, a(i + g, j + g), b(i + g, j + g), c(i + g, j + g),
+                    sor_physical_coeffs(L, i, j, L.level > 0, a(i + g, j + g), b(i + g, j + g), c(i + g, j + g),
                                         d(i + g, j + g), e(i + g, j + g), cg(i + g, j + g), ch(i + g, j + g),
                                         ci(i + g, j + g), cj(i + g, j + g));
                     e(i + g, j + g) = e(i + g, j + g) + S1(i, j);
@@ -414,24 +413,29 @@ void sor_elliptic(Sim& S, bool physical) {
     g_ell_stats.phases = 1;
     const auto evolved_ext = S.evolved;
     S.evolved = {{"ell_u", +1, +1}};
-    for (int level = 1; level < nlev; ++level) {
-        Level& F = S.L[level];
+    // sor_elliptic.f90:293-491: every box, levels 1..Nl(box) in order (the
+    // grid list's order), each started and bounded by interpolation from its
+    // parent (box 0's level 0 for level 1, else the box's own coarser level)
+    for (int gid = 1; gid < nlev; ++gid) {
+        Level& F = S.L[gid];
+        const int level = F.level;
         Arr& r = F.a("r"); Arr& z = F.a("z"); Arr& u = F.a("ell_u");
         for (int m = 0; m <= F.Nr + F.g - 1; ++m)
             for (int n = 0; n <= F.Nz + F.g - 1; ++n) {
-                const double r0 = S.rminl[level] + (double)m * S.drl[level];
-                const double z0 = S.zminl[level] + (double)n * S.dzl[level];
+                const double r0 = S.rminl[gid] + (double)m * S.drl[level];
+                const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
                 const int i = (int)nint_((r0 - r(1 - F.g, 0)) / S.drl[level]) + 1 - F.g;
                 const int j = (int)nint_((z0 - z(0, 1 - F.g)) / S.dzl[level]) + 1 - F.g;
                 const bool flag1 = (i >= 1 - F.g) && (i <= F.Nr) && (j >= 1 - F.g) && (j <= F.Nz);
-                const double aux1 = interp(S, level - 1, S.L[level - 1].a("ell_u"), r0, z0);
+                const double aux1 = interp(S, F.parent, S.L[F.parent].a("ell_u"), r0, z0);
                 if (flag1) u(i, j) = aux1;
             }
-        const int n = solve_level(level, false);
-        if (level == 1) g_ell_stats.steps[1] = n;
+        const int n = solve_level(gid, false);
+        if (gid == 1) g_ell_stats.steps[1] = n;
         g_ell_stats.phases = 2;
     }
-    for (int level = 1; level < nlev; ++level) restrict_(S, level);
+    // :497-521: restriction in the same order (level 1 into level 0 first)
+    for (int gid = 1; gid < nlev; ++gid) restrict_(S, gid);
     S.evolved = evolved_ext;
 }
 

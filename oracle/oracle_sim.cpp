@@ -395,7 +395,10 @@ void restrict_(Sim& S, int gid) {
 // grid ``q`` (box b2, same level) on its strips up to 3*ghost deep, at the
 // points well inside q.  Arrays the reference does not declare (the var_p,
 // accumulator and source copies) are overwritten before they are read, so
-// every array but the NOSYNC coordinates and scratch is taken.
+// every array is taken but the NOSYNC coordinates and scratch and the
+// arrays of INTENT = ELLIPTIC or OUTPUT (prl/arrays.pl:1431 generates the
+// copies for EVOLVE and AUXILIARY only): the elliptic solution ell_u, ell_v
+// and the constraint outputs.
 void syncboxes(Sim& S, int p, int q, const std::vector<std::string>& only) {
     Level& A = S.L[p];
     Level& B = S.L[q];
@@ -409,6 +412,9 @@ void syncboxes(Sim& S, int p, int q, const std::vector<std::string>& only) {
     else for (auto& kv : A.arrs) {
         const std::string& n = kv.first;
         if (n == "r" || n == "z" || n == "rr" || n == "auxarray" || n == "Dr_auxarray" || n == "Dz_auxarray") continue;
+        if (n == "ell_u" || n == "ell_v" || n == "ham" || n == "mom_r" || n == "mom_z" || n == "mom_p" ||
+            n == "CDelta_r" || n == "CDelta_z" || n == "CDelta_p" || n == "Clambda" || n == "CAlambda")
+            continue;
         if (B.arrs.find(n) == B.arrs.end()) continue;
         names.push_back(n);
     }

@@ -94,6 +94,16 @@ CASES = {
                             Nzbox1=16, zbox1=4.0, idata="scalarpulse", ilapse="one", mattertype="scalar",
                             scalar_a0=0.05, scalar_r0=2.0, scalar_z0=3.0, scalardiss=0.02, we_maxiter=100,
                             _steps=[0, 1], _elliptic=True),
+    # the SOR solver with refinement boxes (sor_elliptic.f90:293-521): every
+    # box's levels interpolated from their parents in order, then restricted
+    # in the same order; box 1 on the axis above box 0's level 1.  The
+    # reference sizes its SOR work arrays (sor_elliptic.f90:52) by the grid
+    # current at entry, the last box's last level, so the box is as large as
+    # box 0 (a smaller one overruns them)
+    "ell_sor_boxes": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,
+                          Nzbox1=16, zbox1=3.0, idata="scalarpulse", ilapse="one", mattertype="scalar",
+                          scalar_a0=0.05, scalar_r0=2.0, scalar_z0=3.0, ell_solver="sor", scalardiss=0.02,
+                          _steps=[0], _elliptic=True),
     # boxes that overlap on level 1 (syncboxes.f90 with intersect_interp.inc):
     # box 0's level 1 around the origin and box 1 on the axis above it
     "box_overlap": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,

@@ -95,8 +95,21 @@ SOR_BRILL = dict(BASE, nrtotal=32, nztotal=32, nl0=2, dr0=0.25, dz0=0.25, idata=
                  brill_a0=1.0, ell_solver="sor")
 
 
-@pytest.mark.parametrize("cfg", [SOR_2LEV, SOR_POTENTIAL, SOR_BRILL],
-                         ids=["sor_pulse_2lev", "sor_pulse_potential", "sor_brill_3lev"])
+# SOR with refinement boxes (sor_elliptic.f90:293-521): the layout of the
+# executed-reference fixture (a box as large as box 0), and a smaller box
+# off the axis, where the reference's work arrays (sized by the last box)
+# would be overrun and only the oracle's restatement defines the result
+SOR_BOXES = dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16,
+                 zbox1=3.0, idata="scalarpulse", mattertype="scalar", scalar_a0=0.05, scalar_r0=2.0,
+                 scalar_z0=3.0, scalardiss=0.02, ell_solver="sor")
+SOR_RING = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=2, Nrbox1=12, Nzbox1=12,
+                rbox1=5.0, zbox1=5.0, idata="scalarpulse", mattertype="scalar", scalar_a0=0.05, scalar_r0=4.0,
+                scalar_z0=4.0, scalardiss=0.02, ell_solver="sor")
+
+
+@pytest.mark.parametrize("cfg", [SOR_2LEV, SOR_POTENTIAL, SOR_BRILL, SOR_BOXES, SOR_RING],
+                         ids=["sor_pulse_2lev", "sor_pulse_potential", "sor_brill_3lev", "sor_boxes",
+                              "sor_ring_two_levels"])
 def test_sor_data_matches_oracle(cfg):
     """SOR (sor_elliptic.f90): the red-black sweeps and the sequential Robin
     boundary reproduce the reference's arithmetic; the residual norm that

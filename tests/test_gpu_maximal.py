@@ -134,6 +134,13 @@ def test_maximal_lapse_sor_two_levels():
     run(SOR_PULSE, 1)
 
 
+def test_maximal_slicing_sor_with_refinement_boxes():
+    """SOR's box loops (sor_elliptic.f90:293-521) for the physical
+    Laplacian: box 0's level 1 and an overlapping box above it, a solve after
+    every step (so right after each syncboxes)."""
+    run(dict(EVERY, nl0=1, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0, ell_solver="sor"), 2)
+
+
 @pytest.mark.parametrize("cfg", [EVERY, dict(SOR_SHIFT, slicing="1+log", maximalevery=1)],
                          ids=["schwarzschild_two_levels", "shift_c_nonzero"])
 def test_maximal_lapse_mixed_precision_matches_fp64_sor(cfg):

@@ -91,7 +91,7 @@ def test_oracle_matches_reference_fortran(name):
 
 
 ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev", "ell_pulse_noeqsym",
-             "ell_pulse_boxes"]
+             "ell_pulse_boxes", "ell_sor_boxes"]
 
 
 def ell_cfg(meta):
