@@ -59,9 +59,17 @@ PULSE_BOXES = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, 
                    scalar_z0=3.0, scalardiss=0.02, we_maxiter=120)
 
 
-@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM, PULSE_BOXES],
+# a ring off the axis and the equator with two levels: the wave solver's
+# lower r and z strips, and the pulse's xi on the ring's ghost columns
+PULSE_RING = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=2, Nrbox1=12, Nzbox1=12,
+                  rbox1=5.0, zbox1=5.0, idata="scalarpulse", mattertype="scalar", scalar_a0=0.05, scalar_r0=4.0,
+                  scalar_z0=4.0, scalardiss=0.02, we_maxiter=120)
+
+
+@pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM, PULSE_BOXES,
+                                 PULSE_RING],
                          ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped", "pulse_no_eqsym",
-                              "pulse_boxes"])
+                              "pulse_boxes", "pulse_ring"])
 def test_elliptic_data_matches_oracle(cfg):
     o, e, (o0, o1, ophases, ogres), (g0, g1, ggres) = solve_pair(cfg)
     assert (g0, g1) == (o0, o1), "iterations gpu %s oracle %s" % ((g0, g1), (o0, o1))
