@@ -1708,15 +1708,16 @@ int mixed_elliptic(ollin_handle* h, WaveSolve& S) {
     S.gres = rms;
     for (int l = 1; l < h->nlev; ++l) {
         DLevel& F = h->L[l];
-        DLevel& C = h->L[l - 1];
+        const int pl = F.parent;
+        DLevel& C = h->L[pl];
         InjectArgs a{};
         a.F = F.G;
         a.Cg = C.G;
-        a.cin = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.cin = base_ptr(C, S.W[pl].u[S.W[pl].cur]);
         a.fout = base_ptr(F, S.W[l].u[S.W[l].cur]);
         a.rminl_f = h->rminl[l]; a.zminl_f = h->zminl[l];
-        a.rminl_c = h->rminl[l - 1]; a.rmaxl_c = h->rmaxl[l - 1];
-        a.zminl_c = h->zminl[l - 1]; a.zmaxl_c = h->zmaxl[l - 1];
+        a.rminl_c = h->rminl[pl]; a.rmaxl_c = h->rmaxl[pl];
+        a.zminl_c = h->zminl[pl]; a.zmaxl_c = h->zmaxl[pl];
         a.bicubic = P.interp_bicubic;
         launch_inject(a, h->stream);
         rc = after_launch(h);
@@ -1729,17 +1730,18 @@ int mixed_elliptic(ollin_handle* h, WaveSolve& S) {
     }
     for (int l = 1; l < h->nlev; ++l) {
         DLevel& F = h->L[l];
-        DLevel& C = h->L[l - 1];
+        const int pl = F.parent;
+        DLevel& C = h->L[pl];
         RestrictArgs a{};
         a.F = F.G;
         a.Cg = C.G;
         a.nf = 1;
         a.fid[0] = 0;
         a.fin[0] = base_ptr(F, S.W[l].u[S.W[l].cur]);
-        a.cout[0] = base_ptr(C, S.W[l - 1].u[S.W[l - 1].cur]);
+        a.cout[0] = base_ptr(C, S.W[pl].u[S.W[pl].cur]);
         a.rminl_f = h->rminl[l]; a.rmaxl_f = h->rmaxl[l];
         a.zminl_f = h->zminl[l]; a.zmaxl_f = h->zmaxl[l];
-        a.rminl_c = h->rminl[l - 1]; a.zminl_c = h->zminl[l - 1];
+        a.rminl_c = h->rminl[pl]; a.zminl_c = h->zminl[pl];
         a.eqsym = P.eqsym;
         a.bicubic = P.interp_bicubic;
         launch_restrict(a, h->stream);
