@@ -313,6 +313,7 @@ def run_gpu(args):
             line["batch"] = batch_throughput()
         if not args.no_serve:
             line["serving"] = serving()
+            line["plain_small"] = plain_small()
         print(json.dumps(line))
     if pg is not None:
         pg.destroy_process_group()
@@ -426,6 +427,38 @@ def batch_throughput(n=32, steps=2, seed=7):
     return {"workload": "%d massless scalar shells, 64^2-128^2 x 2-3 levels (seeded), %d coarse steps each" % (n, steps),
             "sequential_point_updates_per_s": pu / t_seq, "batched_point_updates_per_s": pu / t_bat,
             "speedup": t_seq / t_bat, "identical_results": bool(same)}
+
+
+def plain_small():
+    """The plain-method small configuration end to end on the device: the
+    Schwarzschild puncture on 3 levels of 64^2 (finest dr 0.05), RK4, evolved
+    to t = 10M (200 coarse steps) through ollin_gpu_coarse_step, with direct
+    launches and with each step launched as a captured graph (the same
+    kernels and arguments: the final norms agree bit for bit)."""
+    import numpy as np
+    from ollin.gpu import Evolution
+    from ollin.params import params_from_dict
+    cfg = dict(nrtotal=64, nztotal=64, nl0=2, dr0=0.2, dz0=0.2, eqsym=1, idata="schwarzschild", bh1mass=1.0,
+               ilapse="psiminus2", slicing="1+log", gauge_f=2.0, shift="none", integrator="rk4", order="four",
+               geodiss=0.02, dtfac=0.25, boundtype="radiative")
+    out, norms = {}, []
+    for graphs in (False, True):
+        e = Evolution(params_from_dict(cfg))
+        e.initial_data()
+        e.initialize()
+        e.step_graphs(graphs)
+        for _ in range(3):  # warm-up: first steps and kernel loading
+            e.step()
+        t = time.perf_counter()
+        for _ in range(197):
+            e.step()
+        dt = time.perf_counter() - t
+        out["graphs" if graphs else "direct"] = {"seconds_for_197_steps": dt, "ms_per_coarse_step": 1e3 * dt / 197}
+        norms.append(np.array([e.norms(lev, "alpha") for lev in e.levels()]))
+        e.close()
+    out["workload"] = "Schwarzschild puncture, 3 levels of 64^2, RK4 to t = 10M (3 warm-up + 197 timed coarse steps)"
+    out["identical_results"] = bool(np.array_equal(norms[0], norms[1]))
+    return out
 
 
 def serving_requests(rng, n):

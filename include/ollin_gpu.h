@@ -251,7 +251,8 @@ int ollin_gpu_step_end(ollin_handle* h, double* t_out);
 /* 1 when ollin_gpu_step_end would not wait (the queued step has finished, or
  * none is queued), 0 while the step runs.  Does not block. */
 int ollin_gpu_step_ready(const ollin_handle* h);
-/* enable = 1: ollin_gpu_step_begin records the coarse step by stream capture
+/* enable = 1: ollin_gpu_step_begin (and ollin_gpu_coarse_step,
+ * ollin_gpu_coarse_step_many) records the coarse step by stream capture
  * and launches it as one CUDA graph (same kernels, arguments and order, so
  * the same results); 0: direct launches (the default); -1: leave as is.
  * ``stats`` (may be null) gets the graphs instantiated and updated so far. */

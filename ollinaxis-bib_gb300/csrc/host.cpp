@@ -2165,6 +2165,8 @@ void ollin_gpu_destroy(ollin_handle* h) {
     delete h;
 }
 
+static int captured_step(ollin_handle* h);
+
 int ollin_gpu_num_levels(const ollin_handle* h) { return h ? h->nlev : 0; }
 
 int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out) {
@@ -2273,7 +2275,7 @@ int ollin_gpu_aux(ollin_handle* h, int level) {
 int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
-    int rc = onestep(h, 0);
+    int rc = h->graphs && !h->ktime ? captured_step(h) : onestep(h, 0);
     if (rc) return rc;
     unsigned int flag = 0;
     CUDA_OR_FAIL(cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream));
@@ -2404,7 +2406,7 @@ int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out) {
     int first = OLLIN_OK;
     std::string first_msg;
     for (int k = 0; k < n && first == OLLIN_OK; ++k) {
-        int rc = onestep(hs[k], 0);
+        int rc = hs[k]->graphs && !hs[k]->ktime ? captured_step(hs[k]) : onestep(hs[k], 0);
         if (rc) { first = rc; first_msg = g_err; }
     }
     for (int k = 0; k < n; ++k) {

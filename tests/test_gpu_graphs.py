@@ -54,3 +54,22 @@ def test_graph_steps_equal_direct_steps(name):
     if not every:
         assert upd >= 3  # steady steps reuse the executable graph
     assert direct.step_graphs() == (0, 0)
+
+
+def test_coarse_step_honours_graph_mode():
+    """ollin_gpu_coarse_step launches the captured graph too."""
+    from ollin.gpu import Evolution
+    cfg = CASES["puncture_3_levels"][0]
+    ev = []
+    for graphs in (False, True):
+        e = Evolution(params(cfg))
+        e.initial_data()
+        e.initialize()
+        e.step_graphs(graphs)
+        ev.append(e)
+    for _ in range(5):
+        assert ev[0].step() == ev[1].step()
+    for lev in ev[0].levels():
+        for nm in field_list(cfg):
+            assert np.array_equal(ev[0].download(lev, nm), ev[1].download(lev, nm)), (lev, nm)
+    assert sum(ev[1].step_graphs()) == 5
