@@ -251,6 +251,14 @@ int ollin_gpu_step_end(ollin_handle* h, double* t_out);
 /* 1 when ollin_gpu_step_end would not wait (the queued step has finished, or
  * none is queued), 0 while the step runs.  Does not block. */
 int ollin_gpu_step_ready(const ollin_handle* h);
+/* enable = 1 (the default): the kernels of a coarse step are launched as a
+ * programmatic dependent chain -- each may be scheduled while its
+ * predecessor runs and waits on the device for it -- which shortens the gaps
+ * between the short kernels of small grids; 0: ordinary launches (what the
+ * request loop and ollin_gpu_coarse_step_many with n > 1 use: evolutions
+ * running side by side fill the SMs already).
+ * Results are the same either way. */
+int ollin_gpu_step_chaining(ollin_handle* h, int enable);
 /* enable = 1: ollin_gpu_step_begin (and ollin_gpu_coarse_step,
  * ollin_gpu_coarse_step_many) records the coarse step by stream capture
  * and launches it as one CUDA graph (same kernels, arguments and order, so

@@ -18,6 +18,7 @@ namespace {
 //   lambda, Alambda from their definitions        (:767-773, nolambda)
 //   g_lambda = C^2 - B lambda                     (:816-821)
 __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ AuxArgs a) {
+    chain_enter();
     const LevelGeom& G = a.G;
     const int i = 1 - G.g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 - G.g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
@@ -56,6 +57,7 @@ __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ 
 // where the reference's diff1r leaves the r derivatives unset: they are zero
 // here, as in an execution that starts them from zero.
 __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ AuxArgs a) {
+    chain_enter();
     const LevelGeom& G = a.G;
     const int i = (G.axis ? 1 : 1 - G.g) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
@@ -90,14 +92,14 @@ __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ 
 void launch_aux_point(const AuxArgs& a, cudaStream_t s) {
     dim3 blk(64, 4);
     dim3 grd((a.G.nr + a.G.g + blk.x - 1) / blk.x, (a.G.nz + a.G.g + blk.y - 1) / blk.y);
-    aux_point_kernel<<<grd, blk, 0, s>>>(a);
+    launch_chained(aux_point_kernel, grd, blk, s, a);
 }
 
 void launch_aux_deriv(const AuxArgs& a, cudaStream_t s) {
     dim3 blk(64, 4);
     const int ni = a.G.axis ? a.G.nr : a.G.nr + a.G.g;
     dim3 grd((ni + blk.x - 1) / blk.x, (a.G.nz - a.G.jlo + 1 + blk.y - 1) / blk.y);
-    aux_deriv_kernel<<<grd, blk, 0, s>>>(a);
+    launch_chained(aux_deriv_kernel, grd, blk, s, a);
 }
 
 }  // namespace ollin

@@ -25,6 +25,10 @@
 
 using namespace ollin;
 
+namespace ollin {
+thread_local bool g_chain_launch = false;
+}
+
 namespace {
 
 thread_local std::string g_err;
@@ -110,6 +114,9 @@ struct ollin_handle {
     // ollin_gpu_step_graphs: a coarse step is captured and replayed as one
     // graph launch (the executable graph is updated in place each step)
     bool graphs = false;
+    // ollin_gpu_step_chaining: the kernels of a step launched as a
+    // programmatic dependent chain (on by default)
+    bool chain = true;
     cudaGraphExec_t gexec = nullptr;
     long long graph_updates = 0, graph_instantiations = 0;
     bool shift = false, scalar = false;
@@ -2275,7 +2282,9 @@ int ollin_gpu_aux(ollin_handle* h, int level) {
 int ollin_gpu_coarse_step(ollin_handle* h, double* t_out) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
+    g_chain_launch = h->chain;
     int rc = h->graphs && !h->ktime ? captured_step(h) : onestep(h, 0);
+    g_chain_launch = false;
     if (rc) return rc;
     unsigned int flag = 0;
     CUDA_OR_FAIL(cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream));
@@ -2331,10 +2340,18 @@ int ollin_gpu_step_begin(ollin_handle* h) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
     if (h->step_queued) return fail(OLLIN_ESTATE, "a step is already queued on this handle");
+    g_chain_launch = h->chain;
     int rc = h->graphs && !h->ktime ? captured_step(h) : onestep(h, 0);
+    g_chain_launch = false;
     // queued work runs to its end whatever happened: the next end waits for it
     h->step_queued = true;
     return rc;
+}
+
+int ollin_gpu_step_chaining(ollin_handle* h, int enable) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    h->chain = enable != 0;
+    return OLLIN_OK;
 }
 
 int ollin_gpu_step_graphs(ollin_handle* h, int enable, long long* stats) {
@@ -2406,7 +2423,11 @@ int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out) {
     int first = OLLIN_OK;
     std::string first_msg;
     for (int k = 0; k < n && first == OLLIN_OK; ++k) {
+        // side by side the evolutions fill the SMs: ordinary launches (a
+        // chained successor's waiting blocks would take room from the others)
+        g_chain_launch = n == 1 && hs[k]->chain;
         int rc = hs[k]->graphs && !hs[k]->ktime ? captured_step(hs[k]) : onestep(hs[k], 0);
+        g_chain_launch = false;
         if (rc) { first = rc; first_msg = g_err; }
     }
     for (int k = 0; k < n; ++k) {

@@ -13,6 +13,37 @@
 
 namespace ollin {
 
+// Programmatic dependent launch (sm_90+): the kernels of a level step are a
+// chain of short dependent grids.  A kernel launched with launch_chained may
+// be scheduled while its predecessor on the stream is still running; it
+// first waits (griddepcontrol.wait) until that grid has completed and its
+// writes are visible, so it reads and writes nothing early.  Then it lets
+// its own successor be scheduled.  Both instructions are no-ops for a kernel
+// launched the ordinary way.
+__device__ __forceinline__ void chain_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Whether launch_chained adds the programmatic attribute (per host thread:
+// set from the handle being stepped).  Off, the launch is an ordinary one.
+extern thread_local bool g_chain_launch;
+
+template <typename... KArgs, typename... Args>
+inline void launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = g_chain_launch ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 constexpr int kMaxLevels = 12;
 
 // Evolved fields kept on the device (a subset of the reference's EVOLVE

@@ -42,6 +42,7 @@ template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
 #define OLLIN_RHS_MINBLOCKS 3
 #endif
 __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_kernel(const __grid_constant__ StageArgs A) {
+    chain_enter();
     const LevelGeom& G = A.G;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);

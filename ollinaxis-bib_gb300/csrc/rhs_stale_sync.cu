@@ -15,12 +15,12 @@ void launch_rhs_stale_sync(const StageArgs& a, cudaStream_t s) {
     const int nj = a.G.nz - a.G.jlo + 1;
     dim3 grd((a.G.nr + blk.x - 1) / blk.x, (nj + blk.y - 1) / blk.y);
     const bool sh = a.P.shift != 0, sc = a.P.scalar != 0, ad = a.P.shiftadvect != 0;
-    if (!sh && !sc) rhs_kernel<false, false, false, true, true><<<grd, blk, 0, s>>>(a);
-    else if (!sh && sc) rhs_kernel<false, true, false, true, true><<<grd, blk, 0, s>>>(a);
-    else if (!sc && ad) rhs_kernel<true, false, true, true, true><<<grd, blk, 0, s>>>(a);
-    else if (!sc) rhs_kernel<true, false, false, true, true><<<grd, blk, 0, s>>>(a);
-    else if (ad) rhs_kernel<true, true, true, true, true><<<grd, blk, 0, s>>>(a);
-    else rhs_kernel<true, true, false, true, true><<<grd, blk, 0, s>>>(a);
+    if (!sh && !sc) launch_chained(rhs_kernel<false, false, false, true, true>, grd, blk, s, a);
+    else if (!sh && sc) launch_chained(rhs_kernel<false, true, false, true, true>, grd, blk, s, a);
+    else if (!sc && ad) launch_chained(rhs_kernel<true, false, true, true, true>, grd, blk, s, a);
+    else if (!sc) launch_chained(rhs_kernel<true, false, false, true, true>, grd, blk, s, a);
+    else if (ad) launch_chained(rhs_kernel<true, true, true, true, true>, grd, blk, s, a);
+    else launch_chained(rhs_kernel<true, true, false, true, true>, grd, blk, s, a);
 }
 
 }  // namespace ollin

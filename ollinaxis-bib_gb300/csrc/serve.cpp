@@ -207,6 +207,9 @@ struct ollin_server {
         int rc = ollin_gpu_create(&r.p, &e.h);
         if (rc) { e.h = nullptr; return rc; }
         ollin_gpu_step_graphs(e.h, graphs, nullptr);
+        // evolutions side by side fill the SMs themselves; a chained
+        // successor's blocks waiting on an SM would only take room from them
+        ollin_gpu_step_chaining(e.h, 0);
         rc = ollin_gpu_initial_data(e.h);
         if (!rc) rc = ollin_gpu_initialize(e.h);
         if (!rc && maximal_at_start(r)) rc = ollin_gpu_maximal_slicing(e.h, nullptr);

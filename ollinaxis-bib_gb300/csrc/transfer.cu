@@ -30,6 +30,7 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 // columns not filled already; a corner point belongs to the columns when the
 // grid owns the axis
 __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
+    chain_enter();
     if (a.skip && *a.skip) return;
     const LevelGeom& G = a.G;
     const int g = G.g;
@@ -303,6 +304,7 @@ __global__ void __launch_bounds__(128) sync_table_kernel(const __grid_constant__
 // thread per (stencil, field); the strips of a smaller imax are the entries
 // with depth <= imax
 __global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant__ ProlongArgs a) {
+    chain_enter();
     if (a.skip && *a.skip) return;
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= a.ntab * a.nf) return;
@@ -354,6 +356,7 @@ __global__ void __launch_bounds__(128) restrict_table_kernel(const __grid_consta
 }
 
 __global__ void __launch_bounds__(256) restrict_tab_kernel(const __grid_constant__ RestrictArgs a) {
+    chain_enter();
     if (a.skip && *a.skip) return;
     const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     if (t >= a.ntab * a.nf) return;
@@ -536,7 +539,7 @@ void launch_symmetry(const SymArgs& a, cudaStream_t s) {
     const int n = (a.G.axis ? a.G.g * (a.G.nz + a.G.g) : 0) +
                   (a.G.equator ? a.G.g * (a.G.axis ? a.G.nr : a.G.nr + a.G.g) : 0);
     if (n == 0) return;
-    symmetry_kernel<<<(n + 255) / 256, 256, 0, s>>>(a);
+    launch_chained(symmetry_kernel, dim3((n + 255) / 256), dim3(256), s, a);
 }
 
 
@@ -560,7 +563,7 @@ void launch_prolong_table(const ProlongArgs& a, XferPt* tab, cudaStream_t s) {
 
 void launch_prolong_tab(const ProlongArgs& a, cudaStream_t s) {
     const long n = (long)a.ntab * a.nf;
-    prolong_tab_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    launch_chained(prolong_tab_kernel, dim3((unsigned)((n + 255) / 256)), dim3(256), s, a);
 }
 
 void launch_restrict_table(const RestrictArgs& a, XferPt* tab, int m_lo, int n_lo, int nm, int nn, cudaStream_t s) {
@@ -570,7 +573,7 @@ void launch_restrict_table(const RestrictArgs& a, XferPt* tab, int m_lo, int n_l
 
 void launch_restrict_tab(const RestrictArgs& a, cudaStream_t s) {
     const long n = (long)a.ntab * a.nf;
-    if (n > 0) restrict_tab_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a);
+    if (n > 0) launch_chained(restrict_tab_kernel, dim3((unsigned)((n + 255) / 256)), dim3(256), s, a);
 }
 
 void launch_inject(const InjectArgs& a, cudaStream_t s) {

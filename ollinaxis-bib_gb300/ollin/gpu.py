@@ -90,6 +90,7 @@ def load(build_if_missing=True):
     L.ollin_server_last_error.restype = ctypes.c_char_p
     L.ollin_server_set_graphs.argtypes = [vp, ctypes.c_int]
     L.ollin_gpu_step_graphs.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_step_chaining.argtypes = [vp, ctypes.c_int]
     _lib = L
     return L
 
@@ -199,6 +200,10 @@ class Evolution:
         out = ctypes.c_double()
         self._check(self.L.ollin_gpu_min_lapse(self.h, ctypes.byref(out)))
         return out.value
+
+    def step_chaining(self, enable):
+        """Programmatic dependent chaining of a step's kernels (on by default)."""
+        self._check(self.L.ollin_gpu_step_chaining(self.h, int(bool(enable))))
 
     def step_begin(self):
         self._check(self.L.ollin_gpu_step_begin(self.h))

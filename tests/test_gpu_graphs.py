@@ -73,3 +73,23 @@ def test_coarse_step_honours_graph_mode():
         for nm in field_list(cfg):
             assert np.array_equal(ev[0].download(lev, nm), ev[1].download(lev, nm)), (lev, nm)
     assert sum(ev[1].step_graphs()) == 5
+
+
+@pytest.mark.parametrize("name", ["puncture_3_levels", "overlapping_boxes"])
+def test_chained_launches_equal_ordinary_launches(name):
+    """The kernels of a step as a programmatic dependent chain (each waits on
+    the device for its predecessor) give the fields of ordinary launches."""
+    from ollin.gpu import Evolution
+    cfg, _ = CASES[name]
+    ev = []
+    for chain in (False, True):
+        e = Evolution(params(cfg))
+        e.initial_data()
+        e.initialize()
+        e.step_chaining(chain)
+        ev.append(e)
+    for _ in range(4):
+        assert ev[0].step() == ev[1].step()
+    for lev in ev[0].levels():
+        for nm in field_list(cfg):
+            assert np.array_equal(ev[0].download(lev, nm), ev[1].download(lev, nm)), (lev, nm)
