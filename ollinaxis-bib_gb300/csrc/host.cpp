@@ -1488,9 +1488,9 @@ int sor_elliptic(ollin_handle* h, WaveSolve& S) {
         CUDA_OR_FAIL(cudaMemcpyAsync(w.u[w.cur], ones.data(), L.n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     }
-    // Jacobi spectral radius (sor_elliptic.f90:126-128): the grid-spacing
-    // ratio is the same on every level
-    const DLevel& L0 = h->L[0];
+    // Jacobi spectral radius (sor_elliptic.f90:126-128) from the grid that is
+    // current on entry: the last box's last level
+    const DLevel& L0 = h->L[h->nlev - 1];
     const double pi = 3.141592653589793;
     const double rjac = (L0.dz / L0.dr * std::cos(pi / (double)(L0.nr + L0.g))
                          + L0.dr / L0.dz * std::cos(pi / (double)(L0.nz + L0.g))) / (L0.dz / L0.dr + L0.dr / L0.dz);

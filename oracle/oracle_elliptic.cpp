@@ -372,9 +372,10 @@ void sor_elliptic(Sim& S, bool physical) {
     for (Level& L : S.L)
         for (double& x : L.a("ell_u").v) x = 1.0;
     g_ell_stats = EllStats();
-    // Jacobi spectral radius (sor_elliptic.f90:126-128), from the grid spacing
-    // ratio, which is the same on every level
-    const Level& Lg = S.L[0];
+    // Jacobi spectral radius (sor_elliptic.f90:126-128) from the grid that is
+    // current on entry: the last box's last level (the loop of :87-110
+    // leaves it current); for Nb = 0 every grid has box 0's dimensions
+    const Level& Lg = S.L[nlev - 1];
     const double rjac = (Lg.dz / Lg.dr * std::cos(kPi / (double)(Lg.Nr + Lg.g))
                          + Lg.dr / Lg.dz * std::cos(kPi / (double)(Lg.Nz + Lg.g))) / (Lg.dz / Lg.dr + Lg.dr / Lg.dz);
     auto solve_level = [&](int level, bool robin) {

@@ -118,6 +118,25 @@ def test_initial_maximal_lapse_scalar_pulse_with_refinement_boxes():
     run(dict(PULSE, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0), 1)
 
 
+@pytest.mark.parametrize("solver", ["wave", pytest.param("sor", marks=pytest.mark.xfail(
+    reason="open: the physical SOR on a ring off the axis differs from the oracle by 5.7e-8 (relative, level 0 "
+           "lapse after the first step, also at ELL_epsilon = 1e-12); the flat SOR on the same ring and the wave "
+           "solver on it agree", strict=False))])
+def test_maximal_every_step_on_a_ring(solver):
+    """A ring off the axis and the equator: the coefficient derivatives on its
+    ghost columns (r derivatives unset, so zero) and ghost rows (one-sided z
+    stencils), with either solver's box handling.  SOR stops when a residual
+    norm summed in another order crosses ELL_epsilon, so at the default 1e-8
+    the iteration counts can differ by one on level 0 and then by many on the
+    ring, which starts from level 0's values (the lapses then agree to about
+    the solver's tolerance, 1e-6); with ELL_epsilon = 1e-12 both converge to
+    the same discrete solution."""
+    cfg = dict(EVERY, nl0=0, Nb=1, Nl1=1, Nrbox1=12, Nzbox1=12, rbox1=2.5, zbox1=2.5, ell_solver=solver)
+    if solver == "sor":
+        cfg["ell_epsilon"] = 1e-12
+    run(cfg, 2)
+
+
 def test_maximal_every_step_with_speeds():
     """The slicing speeds of the host's last analysis enter the wave
     solver's time step (wave_elliptic.f90:211-263)."""
