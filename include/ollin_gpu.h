@@ -8,7 +8,7 @@
  * ``src/base/evolve.f90:381`` plus the t=0 preparation of
  * ``src/base/evolve.f90:128-195`` (symmetries, ``auxiliary`` on every level,
  * Gamma-driver initialisation).  A Fortran host binds these entry points with
- * ISO_C_BINDING (see INTEGRATION.md); all arguments are plain pointers,
+ * ISO_C_BINDING; all arguments are plain pointers,
  * integers and doubles.
  *
  * Conventions
