@@ -589,6 +589,36 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
             "bisection_bracket": [lo, hi], "all_ok": bool(ok), "identical_results": bool(same)}
 
 
+OP_NAMES = ["DFMA", "DADD", "DMUL", "DDIV", "sqrt", "cbrt", "exp", "log", "FFMA (FP32)"]
+
+
+def probe(args):
+    """Stand-alone measurements behind the committed profile summaries:
+    ``fp64`` prints the operation-rate table (ollin_gpu_op_rate);
+    ``norms`` runs ollin_gpu_norms on the lapse of one 1024x1024
+    Schwarzschild level five times (the launches an ncu capture of
+    norms_partial_kernel selects from)."""
+    import torch
+    from ollin.gpu import Evolution, load
+    from ollin.params import params_from_dict
+    L = load()
+    L.ollin_gpu_op_rate.argtypes = [ctypes.c_int]
+    L.ollin_gpu_op_rate.restype = ctypes.c_double
+    if args.probe == "fp64":
+        rates = {nm: L.ollin_gpu_op_rate(k) for k, nm in enumerate(OP_NAMES)}
+        dfma = rates["DFMA"]
+        print(json.dumps({"probe": "fp64", "ops_per_s": rates,
+                          "cost_vs_dfma": {nm: dfma / v if v > 0 else None for nm, v in rates.items()}}))
+    else:
+        e = Evolution(params_from_dict(dict(WORKLOAD, nl0=0, nrtotal=1024, nztotal=1024, shift="none")))
+        e.initial_data()
+        e.initialize()
+        out = [e.norms(0, "alpha") for _ in range(5)]
+        torch.cuda.synchronize()
+        e.close()
+        print(json.dumps({"probe": "norms", "alpha_norms": [float(x) for x in out[-1]]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -602,9 +632,13 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop measurement")
     ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
     ap.add_argument("--size", type=int, default=512, help="points per level per direction")
+    ap.add_argument("--probe", choices=["fp64", "norms"], default=None,
+                    help="print a stand-alone measurement (operation rates, or the norms launches) and exit")
     args = ap.parse_args()
     WORKLOAD.update(nl0=args.levels - 1, nrtotal=args.size, nztotal=args.size)
-    if args.impl == "reference":
+    if args.probe:
+        probe(args)
+    elif args.impl == "reference":
         if args.steps > 3:
             args.steps = 3  # bounded CPU sample per timed region
         run_reference(args)

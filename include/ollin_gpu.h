@@ -397,6 +397,14 @@ int ollin_gpu_kernel_stats(ollin_handle* h, double* rhs_ms, long long* launches,
  * No counterpart in the reference. */
 double ollin_gpu_fp64_rate(void);
 
+/* Measured rate (operations per second, whole device) of one arithmetic
+ * operation: 0 DFMA, 1 DADD, 2 DMUL, 3 DDIV, 4 sqrt, 5 cbrt, 6 exp, 7 log
+ * (all FP64), 8 FP32 FMA.  Eight independent chains per thread, 8 blocks of
+ * 256 threads per SM.  Returns -1 for an unknown op or on failure.  No
+ * counterpart in the reference: it prices the FP64 operations of the
+ * right-hand side. */
+double ollin_gpu_op_rate(int op);
+
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);
 
@@ -406,21 +414,24 @@ const char* ollin_gpu_last_error(void);
  * grid function that the caller already holds in device memory, computed
  * without allocating anything.  No counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc -- hosts whose device memory comes
- * from their own allocator or pool, code inside a stream capture, tools that
- * may only read.
+ * from their own allocator or pool, regions where an allocation would
+ * synchronise the device, tools that may only read.
  *
  * d_field points at element (1-ghost, 1-ghost) of a column-major
  * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost must be 3
  * and the grid equatorially symmetric (box-0 coordinates r = (i-1/2) dr,
- * z = (j-1/2) dz).  ``stream`` is a cudaStream_t or NULL; the call returns
- * after the result has reached ``out`` (host memory).
+ * z = (j-1/2) dz); eqsym = 0 is refused with OLLIN_EINVAL.  ``stream`` is a
+ * cudaStream_t or NULL; the call returns after the result has reached ``out``
+ * (host memory).  out[4] is the bicubic origin value, which is
+ * save0Dvariable's for interporder = "bicubic" (the default) only.
  *
  * Limit: nz - ghost <= 8192 interior rows (larger grids get OLLIN_EINVAL).
  * The intermediate results live in one fixed 320 KiB device array that is
  * part of the library image, so every GPU that loads the library holds it
  * until the process exits.  The first call on a device looks up that array's
- * device address (with the device current); make that first call before any
- * stream capture.  All calls share the array and it keeps the last call's
+ * device address (with the device current) and keeps it for the life of the
+ * process, so it must not be called on a device after cudaDeviceReset; make
+ * that first call before any stream capture.  All calls share the array and it keeps the last call's
  * contents; every slot a call reads is written earlier in the same call, so
  * no clearing is needed, but calls whose work overlaps on the GPU (other
  * threads or streams, at the same time) race on it and must be serialised by

@@ -87,7 +87,64 @@ __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ 
     }
 }
 
+// KT2 and (scalar field) rho + trS on the ghost columns i = 1-g..0 of a grid
+// that does not own the axis.  The reference forms both with whole-array
+// statements, so they exist at every point (auxiliary_geometry.f90:1022-1031
+// for KT2, the non-angmom branch; stressenergy.f90:65-205 for rho and trS);
+// the fused constraint pass starts at i = 1 because its derivative stencils
+// would leave the grid, and maximal slicing's SOR sweeps the ghost columns of
+// such a grid (sor_elliptic.f90:648, i = 2..imax-1) with S1 = -K2 there.
+// Expression order: the reference's.
+__global__ void __launch_bounds__(128) ghost_kt2_kernel(const __grid_constant__ StageArgs A) {
+    const LevelGeom& G = A.G;
+    const int g = G.g;
+    const int i = 1 - g + (int)threadIdx.x;
+    const int j = 1 - g + (int)(blockIdx.x * blockDim.y + threadIdx.y);
+    if (i > 0 || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * (size_t)G.ld;
+    const double r = G.rcol[i], r2 = r * r;
+    const double gA = A.aux[X_GA][o], gB = A.aux[X_GB][o], gH = A.aux[X_GH][o], gC = A.aux[X_GC][o];
+    const double kA = A.in[F_KTA][o], kB = A.in[F_KTB][o], kC = A.in[F_KTC][o], kH = A.aux[X_KTH][o];
+    const double KT2_A = (2.0 * kA * gC * kC + kC * kC * gB) * r2 + gA * (kA * kA);
+    const double KT2_B = (kC * kC * gA + 2.0 * kC * gC * kB) * r2 + gB * (kB * kB);
+    const double KT2_H = (kH * kH) * gH;
+    const double KT2_C = (kC * kC) * gC * r2 + kA * gA * kC + kA * gC * kB + kC * gB * kB;
+    A.auxw[X_KT2][o] = gA * KT2_A + gB * KT2_B + gH * KT2_H + 2.0 * gC * KT2_C * r2;
+    if (!A.P.scalar) return;
+    // 1/psi^4 as the right-hand side forms it (from phi at t = 0, else chi^2)
+    double ps4;
+    if (A.t0) {
+        const double psi = exp(A.in[F_PHI][o]);
+        const double psi2 = psi * psi;
+        ps4 = 1.0 / (psi2 * psi2);
+    } else {
+        const double chi = A.in[F_CHI][o];
+        ps4 = chi * chi;
+    }
+    const double sphi = A.in[F_SPHI][o], sxr = A.in[F_SXIR][o], sxz = A.in[F_SXIZ][o], spi = A.in[F_SPI][o];
+    const double m2 = A.P.scalar_mass * A.P.scalar_mass;
+    double V = 0.0;
+    if (A.P.potential == 1) V = 0.5 * m2 * (sphi * sphi);
+    else if (A.P.potential == 2) V = 0.5 * m2 * (sphi * sphi) + 0.25 * A.P.scalar_lambda * ((sphi * sphi) * (sphi * sphi));
+    const double grad2 = (gA * (sxr * sxr) + gB * (sxz * sxz) + 2.0 * r * gC * sxr * sxz) * ps4;
+    const double rho = 0.5 * ((spi * spi) + grad2) + V;
+    const double auxs = 0.5 * ((spi * spi) - grad2) - V;
+    const double psi4 = 1.0 / ps4;
+    const double S_A = (sxr * sxr) + A.in[F_A][o] * psi4 * auxs;
+    const double S_B = (sxz * sxz) + A.in[F_B][o] * psi4 * auxs;
+    const double S_C = sxr * sxz * G.ircol[i] + A.in[F_C][o] * psi4 * auxs;
+    const double S_H = A.in[F_H][o] * psi4 * auxs;
+    const double trS = (gA * S_A + gB * S_B + gH * S_H + 2.0 * r2 * gC * S_C) * ps4;
+    A.auxw[X_RHOS][o] = rho + trS;
+}
+
 }  // namespace
+
+void launch_ghost_kt2(const StageArgs& a, cudaStream_t s) {
+    if (a.G.axis) return;
+    dim3 blk(4, 32);  // x: the g ghost columns; y: rows
+    ghost_kt2_kernel<<<(a.G.nz + a.G.g + blk.y - 1) / blk.y, blk, 0, s>>>(a);
+}
 
 void launch_aux_point(const AuxArgs& a, cudaStream_t s) {
     dim3 blk(64, 4);

@@ -911,6 +911,9 @@ int analysis(ollin_handle* h, int level) {
     launch_stage_rhs(a, h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
+    launch_ghost_kt2(a, h->stream);
+    rc = after_launch(h);
+    if (rc) return rc;
     launch_ham_edges(L.G, base_ptr(L, L.aux[X_HAM]), h->stream);
     rc = after_launch(h);
     if (rc) return rc;
@@ -2507,6 +2510,8 @@ int ollin_gpu_min_lapse(ollin_handle* h, double* out) {
 double ollin_gpu_point_updates(const ollin_handle* h) { return h ? h->point_updates : 0.0; }
 
 double ollin_gpu_fp64_rate(void) { return measure_fp64_dfma_rate(0); }
+
+double ollin_gpu_op_rate(int op) { return measure_op_rate(op, 0); }
 
 int ollin_gpu_kernel_timing(ollin_handle* h, int enable) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");

@@ -3,12 +3,16 @@
 //
 // Who needs it: callers that cannot call cudaMalloc -- a Fortran host that
 // hands over arrays from its own CUDA allocator or from a memory pool it
-// manages, code running inside a stream capture or a region where allocation
-// would synchronise the device, or tools that may only read memory.  They
-// own the field and the 5-number result; the reduction's intermediate
-// results live in a fixed-size array that is part of this library's device
-// image, reserved when the library is loaded and held by every GPU that loads
-// it until the process exits.
+// manages and must not have a second allocator carve device memory beside
+// it, a region where an allocation would synchronise the device, or tools
+// that may only read memory.  They own the field and the 5-number result; the
+// reduction's intermediate results live in a fixed-size array that is part
+// of this library's device image, reserved when the library is loaded and
+// held by every GPU that loads it until the process exits.
+//
+// The origin value is the 4x4 bicubic interpolation of save0Dvariable with
+// interporder = "bicubic" (the reference's default); with "bilinear" the
+// fifth number differs from the reference's, the other four do not.
 //
 // The statistics are those of save0Dvariable (src/base/save0Ddata.f90:221-288,
 // origin value at :370-374), computed in two fixed-order passes so that the
@@ -81,7 +85,7 @@ __global__ void __launch_bounds__(256) rows_kernel(const double* __restrict__ f,
 // (interp.f90:146-263 at r0 = z0 = 0, which lies one cell from the axis and
 // the equator and uses the 4x4 stencil).
 __global__ void __launch_bounds__(256) final_kernel(const double* __restrict__ f, int nr, int nz, int g, long ld,
-                                                    double dr, double dz, int eqsym, double* scratch) {
+                                                    double dr, double dz, double* scratch) {
     __shared__ double smax[256], smin[256], snm1[256], snm2[256];
     __shared__ int snan[256];
     const int nrows = nz - g;
@@ -115,9 +119,10 @@ __global__ void __launch_bounds__(256) final_kernel(const double* __restrict__ f
         out[1] = smin[0];
         out[2] = snm1[0];
         out[3] = sqrt(snm2[0] / npts);
-        // origin value: interp(box 0, level, 0, 0)
+        // origin value: interp(box 0, level, 0, 0); the grid is equatorially
+        // symmetric (the entry point refuses anything else)
         const double r1 = rcoord(1 - g, dr);
-        const double z1 = eqsym ? rcoord(1 - g, dz) : 0.0;
+        const double z1 = rcoord(1 - g, dz);
         const int i0 = (int)((0.0 - r1) / dr) + 1 - g;
         const int j0 = (int)((0.0 - z1) / dz) + 1 - g;
         const double auxr = (0.0 - rcoord(i0, dr)) / dr;
@@ -150,7 +155,10 @@ int noalloc_fail(int code, const char* msg) {
 }
 
 // Address of the scratch array on the current device: looked up once per
-// device, with that device current.
+// device, with that device current, and cached for the life of the process.
+// The cache does not survive cudaDeviceReset (the address belongs to the
+// destroyed context), so a caller that resets a device must not call this
+// entry point on it afterwards.
 int scratch_for_current_device(double** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return noalloc_fail(OLLIN_ECUDA, "cudaGetDevice failed");
@@ -184,10 +192,19 @@ int ollin_gpu_norms_noalloc(const double* d_field, int nr, int nz, int ghost, in
     double* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
+    // An error left pending by the caller's earlier work is reported as such,
+    // not charged to these launches.
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess) {
+        snprintf(g_noalloc_err, sizeof(g_noalloc_err), "a CUDA error from earlier work is pending: %s",
+                 cudaGetErrorString(pending));
+        return OLLIN_ECUDA;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     rows_kernel<<<nz - ghost, 256, 0, s>>>(d_field, nr, ghost, (long)ld_r, scratch);
-    final_kernel<<<1, 256, 0, s>>>(d_field, nr, nz, ghost, (long)ld_r, dr, dz, eqsym, scratch);
-    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(OLLIN_ECUDA, "kernel launch failed");
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(OLLIN_ECUDA, "launch of the row pass failed");
+    final_kernel<<<1, 256, 0, s>>>(d_field, nr, nz, ghost, (long)ld_r, dr, dz, scratch);
+    if (cudaGetLastError() != cudaSuccess) return noalloc_fail(OLLIN_ECUDA, "launch of the final pass failed");
     double res[6];
     if (cudaMemcpyAsync(res, scratch + (size_t)kMaxRows * kRowSlots, sizeof(res), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)

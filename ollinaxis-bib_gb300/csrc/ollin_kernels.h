@@ -337,6 +337,9 @@ void launch_pulse_xi(const PulseCoeffArgs& a, cudaStream_t s);
 void launch_pulse_coeffs(const PulseCoeffArgs& a, cudaStream_t s);
 
 void launch_rhs(const StageArgs& a, cudaStream_t s);
+// KT2 (and rho + trS) on the ghost columns of a grid off the axis; no-op on a
+// grid that owns the axis.
+void launch_ghost_kt2(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale(const StageArgs& a, cudaStream_t s);
 void launch_rhs_sync(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale_sync(const StageArgs& a, cudaStream_t s);
@@ -364,6 +367,9 @@ void launch_gammadriver_init(const LevelGeom& G, double* dtbr, double* dtbz, con
                              const double* dlz, double csi, cudaStream_t s);
 // DFMA instructions per second of this GPU (all SMs, independent chains).
 double measure_fp64_dfma_rate(cudaStream_t s);
+// Operations per second of one entry of the rate table (0 DFMA, 1 DADD, 2 DMUL,
+// 3 DDIV, 4 sqrt, 5 cbrt, 6 exp, 7 log, 8 FP32 FMA); -1 on failure.
+double measure_op_rate(int op, cudaStream_t s);
 void launch_phi_from_chi(const LevelGeom& G, const double* chi, double* out, cudaStream_t s);
 
 }  // namespace ollin

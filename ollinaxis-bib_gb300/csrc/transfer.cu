@@ -529,6 +529,55 @@ __global__ void fp64_probe_kernel(double* out, int iters, double seed) {
     out[gid] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+// One operation of the rate table, applied to one chain value.  Every chain
+// stays bounded and finite: the divide alternates between two values, sqrt,
+// cbrt and exp(-x) converge to fixed points, log(x + 2) converges to 1.146.
+template <int OP>
+__device__ __forceinline__ double probe_op(double a, double m, double c) {
+    if constexpr (OP == 0) return fma(a, m, c);
+    else if constexpr (OP == 1) return a + c;
+    else if constexpr (OP == 2) return a * m;
+    else if constexpr (OP == 3) return m / a;
+    else if constexpr (OP == 4) return sqrt(a);
+    else if constexpr (OP == 5) return cbrt(a);
+    else if constexpr (OP == 6) return exp(-a);
+    else return log(a + 2.0);
+}
+
+template <int OP>
+__global__ void op_probe_kernel(double* out, int iters, double seed) {
+    const int gid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    double a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = seed + 0.1 * u + gid * 1e-9;
+    const double m = 0.999999, c = 1e-7;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a[u] = probe_op<OP>(a[u], m, c);
+    }
+    double t = 0.0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t += a[u];
+    out[gid] = t;
+}
+
+// FP32 FMA chains, for the FP32/FP64 rate ratio.
+__global__ void ffma_probe_kernel(double* out, int iters, double seed) {
+    const int gid = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    float a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = (float)seed + 0.1f * u + gid * 1e-6f;
+    const float m = 0.9999f, c = 1e-4f;
+    for (int k = 0; k < iters; ++k) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) a[u] = fmaf(a[u], m, c);
+    }
+    float t = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t += a[u];
+    out[gid] = (double)t;
+}
+
 dim3 full_grid(const LevelGeom& G, dim3 blk) {
     return dim3((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
 }
@@ -616,19 +665,35 @@ void launch_phi_from_chi(const LevelGeom& G, const double* chi, double* out, cud
     phi_from_chi_kernel<<<full_grid(G, blk), blk, 0, s>>>(G, chi, out);
 }
 
-double measure_fp64_dfma_rate(cudaStream_t s) {
+double measure_op_rate(int op, cudaStream_t s) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = sms * 8, threads = 256, iters = 4096;
+    // the slow operations get fewer iterations, so every launch lasts ~1-10 ms
+    static const int kIters[9] = {4096, 4096, 4096, 1024, 1024, 512, 512, 256, 65536};
+    if (op < 0 || op > 8) return -1.0;
+    const int blocks = sms * 8, threads = 256, iters = kIters[op];
     double* out = nullptr;
     if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
+    auto launch = [&](int n) {
+        switch (op) {
+            case 0: fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 1: op_probe_kernel<1><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 2: op_probe_kernel<2><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 3: op_probe_kernel<3><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 4: op_probe_kernel<4><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 5: op_probe_kernel<5><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 6: op_probe_kernel<6><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            case 7: op_probe_kernel<7><<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+            default: ffma_probe_kernel<<<blocks, threads, 0, s>>>(out, n, 0.5); break;
+        }
+    };
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, 16, 0.5);
+    launch(16);
     cudaEventRecord(e0, s);
-    fp64_probe_kernel<<<blocks, threads, 0, s>>>(out, iters, 0.5);
+    launch(iters);
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -636,7 +701,10 @@ double measure_fp64_dfma_rate(cudaStream_t s) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(out);
+    if (cudaGetLastError() != cudaSuccess || !(ms > 0.f)) return -1.0;
     return (double)blocks * threads * iters * 8.0 / (ms * 1e-3);
 }
+
+double measure_fp64_dfma_rate(cudaStream_t s) { return measure_op_rate(0, s); }
 
 }  // namespace ollin

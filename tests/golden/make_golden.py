@@ -2,9 +2,10 @@
 reference's own Fortran evolution path (src/base/onestep.f90 and everything
 it calls, plus initial.f90 and constraints.f90) through ``ftn_subset``.
 
-Run from the repository root in a container that has the reference mounted:
+Run from the repository root in a container that has the reference checked
+out, giving its directory as the first argument or in OLLIN_REFERENCE_DIR:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference checkout> [case ...]
 
 Each fixture stores, for a small box-in-box configuration, the reference's
 grid functions (all points including ghosts, Fortran (i,j) at [i+g-1, j+g-1])
@@ -215,7 +216,10 @@ def run_case(refdir, name, cfg):
 
 
 def main():
-    refdir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("OLLIN_REFERENCE_DIR")
+    if not refdir or not os.path.isdir(os.path.join(refdir, "src", "base")):
+        sys.exit("usage: make_golden.py <reference checkout> [case ...] "
+                 "(or set OLLIN_REFERENCE_DIR); the directory must hold src/base/onestep.f90")
     only = sys.argv[2:]
     for name, cfg in CASES.items():
         if only and name not in only:

@@ -44,6 +44,20 @@ def rel_diff(a, b):
     return float(np.max(np.abs(a - b))) / scale
 
 
+# Pointwise relative difference: |gpu - oracle| / max(|oracle|, floor), with
+# the floor POINT_FLOOR x max|oracle| of that field on that level, so that
+# points where a field crosses zero (C, KTC, Delta_z, beta_z are zero on the
+# axis and the equator and tiny far out) are measured against a millionth of
+# the field's scale instead of their own vanishing value.
+POINT_FLOOR = 1e-6
+
+
+def point_rel_diff(a, b, floor=POINT_FLOOR):
+    scale = max(float(np.max(np.abs(b))), 1e-300)
+    den = np.maximum(np.abs(b), floor * scale)
+    return float(np.max(np.abs(a - b) / den))
+
+
 def scalar_pulse(r, z, a0=0.05):
     ph = a0 * np.exp(-(r ** 2 + z ** 2))
     return ph, -2.0 * r * ph, -2.0 * z * ph, np.zeros_like(ph)

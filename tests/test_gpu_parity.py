@@ -6,7 +6,8 @@ import numpy as np
 import pytest
 
 from oracle_bind import Oracle
-from parity_util import (C1, coords, field_list, params, rel_diff, scalar_pulse, tol_for)
+from parity_util import (C1, POINT_FLOOR, coords, field_list, params, point_rel_diff, rel_diff, scalar_pulse,
+                         tol_for)
 
 pytestmark = pytest.mark.gpu
 
@@ -30,9 +31,12 @@ def make_pair(cfg):
     return o, e
 
 
-def compare(o, e, cfg, tag=""):
+def compare(o, e, cfg, tag="", point_tol=None, stats=None):
     """Largest normwise relative difference over the evolved fields; every
-    field is held to its bound (tol_for)."""
+    field is held to its bound (tol_for).  With ``point_tol`` the pointwise
+    relative difference (parity_util.point_rel_diff) of every evolved field
+    but lambda, Alambda and KTH is held to it as well; ``stats`` collects
+    the worst pointwise figure per field."""
     worst = 0.0
     for lev in o.levels():
         for nm in field_list(cfg):
@@ -41,20 +45,43 @@ def compare(o, e, cfg, tag=""):
             d = rel_diff(a, b)
             if nm not in ("lambda", "Alambda", "KTH"):
                 worst = max(worst, d)
+                pd = point_rel_diff(a, b)
+                if stats is not None:
+                    stats[nm] = max(stats.get(nm, 0.0), pd)
+                if point_tol is not None:
+                    assert pd <= point_tol, "%s level %d %s: pointwise rel diff %.3e (floor %.0e of max)" % (
+                        tag, lev, nm, pd, POINT_FLOOR)
             assert d <= tol_for(nm), "%s level %d %s: rel diff %.3e" % (tag, lev, nm, d)
     return worst
 
 
-def run(cfg, steps, check_every=None):
+def run(cfg, steps, check_every=None, point_tol=None, stats=None):
     o, e = make_pair(cfg)
-    compare(o, e, cfg, tag="t=0")
+    compare(o, e, cfg, tag="t=0", point_tol=point_tol, stats=stats)
     worst = 0.0
     for k in range(1, steps + 1):
         to, te = o.step(), e.step()
         assert to == te
         if check_every and k % check_every == 0 or k == steps:
-            worst = max(worst, compare(o, e, cfg, tag="step %d" % k))
+            worst = max(worst, compare(o, e, cfg, tag="step %d" % k, point_tol=point_tol, stats=stats))
     return o, e, worst
+
+
+def report(tag, stats):
+    print("%s pointwise (floor %.0e of max): %s" % (tag, POINT_FLOOR,
+                                                    " ".join("%s=%.1e" % kv for kv in sorted(stats.items()))))
+
+
+def check_constraint_norms(o, e):
+    """L2 (nm2) and max-abs (nm1) of ham, mom_r, mom_z on every level within
+    1e-8 relative of the oracle's."""
+    for lev in o.levels():
+        o.constraints(lev)
+        for nm in ["ham", "mom_r", "mom_z"]:
+            ng = e.norms(lev, nm)
+            no = o.norms(lev, nm)
+            for k in (2, 3):
+                assert abs(ng[k] - no[k]) <= 1e-8 * abs(no[k]), (lev, nm, k, ng[k], no[k])
 
 
 def test_c1_single_level_20_steps():
@@ -66,16 +93,28 @@ def test_c1_single_level_20_steps():
 def test_c1_three_levels_to_t10():
     """The plain small configuration (3 box-in-box levels of 64x64) over its
     whole run, 200 coarse steps (t = 10M): fields and constraint norms."""
-    o, e, w = run(dict(C1), 200, check_every=25)
+    stats = {}
+    o, e, w = run(dict(C1), 200, check_every=25, stats=stats)
     print("C1 200 steps worst field rel diff %.2e" % w)
-    for lev in o.levels():
-        o.constraints(lev)
-        for nm in ["ham", "mom_r", "mom_z"]:
-            ng = e.norms(lev, nm)
-            no = o.norms(lev, nm)
-            # L2 (nm2) and max-abs (nm1) of the constraints
-            for k in (2, 3):
-                assert abs(ng[k] - no[k]) <= 1e-8 * abs(no[k]), (lev, nm, k, ng[k], no[k])
+    report("C1 200 steps", stats)
+    check_constraint_norms(o, e)
+
+
+# The large plain configuration exactly as bench.py times it: the puncture
+# with the Gamma-driver-2 shift on 6 box-in-box levels of 512x512 (finest
+# dr = 0.00625), six-deep recursion (32 finest steps per coarse step)
+C2 = dict(C1, nrtotal=512, nztotal=512, nl0=5, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+
+
+def test_c2_headline_configuration_two_coarse_steps():
+    """Two coarse steps of the benchmarked configuration (2 x 16.5 M
+    point-updates): every evolved field on every level, normwise and
+    pointwise, and the constraint norms per level."""
+    stats = {}
+    o, e, w = run(dict(C2), 2, check_every=1, stats=stats)
+    print("C2 2 coarse steps worst field rel diff %.2e" % w)
+    report("C2 2 coarse steps", stats)
+    check_constraint_norms(o, e)
 
 
 def test_gammadriver_shift_three_levels():
