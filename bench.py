@@ -139,59 +139,103 @@ def sum_over_ranks(pg, x):
     return float(t.item())
 
 
-def cpu_baseline(threads=None, seconds=10.0):
-    """The oracle (CPU restatement of the reference, C++ -O2) on one 512x512
-    level of the same physics, timed for roughly ``seconds`` of work."""
-    if threads is not None:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_hierarchy(cfg):
+    """The oracle (CPU restatement of the reference, C++ -O2, OpenMP loops)
+    set up on ``cfg`` through the reference's sequence: initial data,
+    ``initialize``."""
     from oracle_bind import Oracle
     from ollin.params import params_from_dict
-    cfg = dict(WORKLOAD, nl0=0)
     o = Oracle(params_from_dict(cfg))
     o.initial_data()
     o.initialize()
-    o.step()  # warm-up
+    return o
+
+
+def time_oracle_steps(o, min_seconds, min_steps=1, max_steps=None):
+    """Coarse steps of ``o`` until at least ``min_seconds`` and ``min_steps``
+    have passed (or ``max_steps``); returns (steps, seconds, point-updates)."""
     pu0 = o.point_updates()
-    t0 = time.time()
+    t0 = time.perf_counter()
     n = 0
     while True:
         o.step()
         n += 1
-        if time.time() - t0 >= seconds or n >= 50:
+        dt = time.perf_counter() - t0
+        if (dt >= min_seconds and n >= min_steps) or (max_steps is not None and n >= max_steps):
             break
-    dt = time.time() - t0
-    v = (o.point_updates() - pu0) / dt
-    return {"value": v, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", "1")), "kind": "port",
-            "sample": "%d RK4 steps of one 512x512 level (Gammadriver2, 1+log, FP64), %.1f s" % (n, dt)}
+    return n, dt, o.point_updates() - pu0
+
+
+def cpu_baseline(seconds=10.0):
+    """The oracle on the host cores: the whole benchmarked hierarchy (6
+    levels of 512^2, every level's steps, prolongation, restriction and
+    recursion of onestep) with all cores, timed over whole coarse steps after
+    one untimed coarse step; beside it one core on one 512^2 level of the same
+    physics (a whole coarse step on one core takes minutes)."""
+    from oracle_bind import set_threads
+    cores = set_threads(host_cores())
+    o = oracle_hierarchy(dict(WORKLOAD))
+    o.step()  # untimed: the first step's time == 0 branches
+    n, dt, pu = time_oracle_steps(o, seconds)
+    del o
+    one = set_threads(1)
+    s = oracle_hierarchy(dict(WORKLOAD, nl0=0))
+    s.step()
+    n1, dt1, pu1 = time_oracle_steps(s, seconds / 2.0, min_steps=2)
+    del s
+    set_threads(cores)
+    nlev = WORKLOAD["nl0"] + 1
+    return {"value": pu / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d whole coarse step(s) of the %d-level %dx%d hierarchy (Gammadriver2, 1+log, RK4, FP64), "
+                      "%.1f s, after one untimed coarse step" % (n, nlev, WORKLOAD["nrtotal"], WORKLOAD["nztotal"], dt),
+            "single_thread": {"value": pu1 / dt1, "unit": UNIT, "cores": one,
+                              "sample": "%d RK4 steps of one %dx%d level of the same physics on one core, %.1f s"
+                                        % (n1, WORKLOAD["nrtotal"], WORKLOAD["nztotal"], dt1)}}
+
+
+# Largest number of coarse steps the reference arm times (one coarse step of
+# the 6-level hierarchy takes several seconds on the host cores).
+REFERENCE_MAX_STEPS = 30
 
 
 def run_reference(args):
+    """The reference's CPU path (the oracle restatement; the Fortran cannot be
+    built on these hosts) on the same workload as the GPU arm: whole coarse
+    steps of the 6-level hierarchy with every host core.  One untimed coarse
+    step stands in for the warm-up (a CPU needs no more); the timed steps are
+    the requested ones, up to REFERENCE_MAX_STEPS."""
     world, rank, _, pg = dist_setup(args)
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    from oracle_bind import Oracle
-    from ollin.params import params_from_dict
-    cfg = dict(WORKLOAD, nl0=0)
-    o = Oracle(params_from_dict(cfg))
-    o.initial_data()
-    o.initialize()
-    for _ in range(args.warmup):
+    from oracle_bind import set_threads
+    threads = set_threads(host_cores())
+    o = oracle_hierarchy(dict(WORKLOAD))
+    warm = min(args.warmup, 1)
+    for _ in range(warm):
         o.step()
-    pu0 = o.point_updates()
-    t0 = time.time()
-    for _ in range(args.steps):
-        o.step()
-    dt = time.time() - t0
-    v = (o.point_updates() - pu0) / dt
-    sample = "%d RK4 steps of one 512x512 level of the workload's physics per timed region" % args.steps
+    timed = min(args.steps, REFERENCE_MAX_STEPS)
+    n, dt, pu = time_oracle_steps(o, 0.0, min_steps=timed, max_steps=timed)
+    v = pu / dt
+    nlev = WORKLOAD["nl0"] + 1
+    sample = ("%d whole coarse steps of the %d-level %dx%d hierarchy per timed region, after %d untimed"
+              % (n, nlev, WORKLOAD["nrtotal"], WORKLOAD["nztotal"], warm))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+            "steps": n, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / n,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (analytic Schwarzschild initial data)", "config": config_dict(args),
+            "timed_seconds": dt, "warmup_steps_run": warm,
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if n != args.steps:
+        line["steps_note"] = "timed %d of the %d requested coarse steps (cap %d)" % (n, args.steps,
+                                                                                  REFERENCE_MAX_STEPS)
     print(json.dumps(line))
 
 
@@ -306,7 +350,7 @@ def run_gpu(args):
                              "rhs_share_of_step": (rhs_ms / max(ms_local, 1e-9))},
                 "clocks": clocks}
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(threads=os.cpu_count(), seconds=args.cpu_seconds)
+            line["cpu_baseline"] = cpu_baseline(seconds=args.cpu_seconds)
         if not args.no_elliptic:
             line["elliptic"] = elliptic_precision()
         if not args.no_batch:
@@ -320,16 +364,24 @@ def run_gpu(args):
 
 
 def elliptic_precision():
-    """The precision pattern of the Brill-wave configuration: the conformal
-    factor of Holz Brill data (a0 = 1, sigma = 1) on 4 box-in-box levels of
-    1024^2 by the mixed solver (FP32 multigrid corrections, FP64 residual
-    refinement), timed through the C ABI; beside it, on one 256^2 level,
-    the same solve against the FP64 SOR of the reference algorithm."""
+    """The precision pattern of the Brill-wave configuration (Holz data,
+    sigma = 1, dr0 = 0.04, 4 box-in-box levels of 1024^2) for a0 = 1, 4, 5:
+      * the conformal factor by the mixed solver (FP32 multigrid corrections,
+        FP64 residual refinement) and by the all-FP64 solve of the same
+        system (ELL_solver = fp64mg: FP64 multigrid corrections), timed
+        through the C ABI; the error is max |chi_mixed - chi_fp64| over all
+        levels;
+      * after one coarse step (K_ij no longer zero), the maximal-slicing
+        lapse by both, and max |alpha_mixed - alpha_fp64|;
+    and on one 256^2 level, where the reference's FP64 SOR converges, the
+    mixed and FP64 multigrid solves against that SOR."""
     import numpy as np
     from ollin.gpu import Evolution
     from ollin.params import params_from_dict
     base = dict(eqsym=1, order="four", integrator="rk4", ilapse="one", idata="BrillWave", brill_a0=1.0,
-                brill_sr0=1.0, brill_sz0=1.0, dr0=0.04, dz0=0.04)
+                brill_sr0=1.0, brill_sz0=1.0, dr0=0.04, dz0=0.04, ell_epsilon=1e-12)
+    c3 = dict(nrtotal=1024, nztotal=1024, nl0=3)
+    one = dict(nrtotal=256, nztotal=256, nl0=0)
 
     def solve(cfg):
         e = Evolution(params_from_dict(dict(base, **cfg)))
@@ -342,8 +394,9 @@ def elliptic_precision():
         return dt, stats, chi
 
     def maximal(cfg):
-        """Brill data, one coarse step (K_ij no longer zero), then the
-        maximal-slicing lapse (maximalslicing.f90)."""
+        """Brill data, the maximal lapse, one coarse step, then the
+        maximal-slicing lapse again (maximalslicing.f90), every solve by the
+        solver of cfg: the whole precision pattern against the all-FP64 one."""
         e = Evolution(params_from_dict(dict(base, maximalevery=1, slicing="1+log", gauge_f=2.0, **cfg)))
         e.initial_data()
         e.initialize()
@@ -352,28 +405,42 @@ def elliptic_precision():
         t = time.perf_counter()
         e.maximal_slicing()
         dt = time.perf_counter() - t
-        alpha = e.download(0, "alpha")
+        alpha = [e.download(lev, "alpha") for lev in e.levels()]
         stats = e.ell_stats()
         e.close()
         return dt, stats, alpha
 
-    solve(dict(nrtotal=64, nztotal=64, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))  # warm-up
-    t_c3, st_c3, _ = solve(dict(nrtotal=1024, nztotal=1024, nl0=3, ell_solver="mixed", ell_epsilon=1e-12))
-    t_mx, st_mx, chi_mx = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))
-    t_sor, st_sor, chi_sor = solve(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="sor"))
-    tm_c3, sm_c3, a_c3 = maximal(dict(nrtotal=1024, nztotal=1024, nl0=3, ell_solver="mixed", ell_epsilon=1e-12))
-    tm_mx, sm_mx, a_mx = maximal(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="mixed", ell_epsilon=1e-12))
-    tm_sor, sm_sor, a_sor = maximal(dict(nrtotal=256, nztotal=256, nl0=0, ell_solver="sor"))
-    return {"workload": "Brill wave a0=1, 4 levels of 1024x1024, dr0=0.04, mixed solver to 1e-12 or the FP64 floor",
-            "seconds": t_c3, "refinements_level0": st_c3[0], "vcycles_level0": st_c3[1], "final_rms_residual": st_c3[2],
-            "vs_fp64_sor_256": {"mixed_seconds": t_mx, "sor_seconds": t_sor, "sor_iterations": st_sor[0],
-                                "max_abs_chi_diff": float(np.max(np.abs(chi_mx[0] - chi_sor[0])))},
-            "maximal_slicing": {"workload": "the same data after one coarse step, maximal lapse by the mixed solver",
-                                "seconds": tm_c3, "refinements_level0": sm_c3[0], "vcycles_level0": sm_c3[1],
-                                "final_rms_residual": sm_c3[2], "min_alpha": float(a_c3.min()),
-                                "vs_fp64_sor_256": {"mixed_seconds": tm_mx, "sor_seconds": tm_sor,
-                                                    "sor_iterations": sm_sor[0],
-                                                    "max_abs_alpha_diff": float(np.max(np.abs(a_mx - a_sor)))}}}
+    def maxdiff(x, y):
+        return float(max(np.max(np.abs(a - b)) for a, b in zip(x, y)))
+
+    solve(dict(nrtotal=64, nztotal=64, nl0=0, ell_solver="mixed"))  # warm-up
+    out = {"workload": "Holz Brill wave, sigma = 1, dr0 = 0.04, 4 levels of 1024x1024; mixed solver (FP32 multigrid "
+                       "corrections, FP64 residual) against the FP64 solve of the same system (FP64 multigrid "
+                       "corrections), each to an RMS residual of 1e-12 or its FP64 floor",
+           "cases": []}
+    for a0 in (1.0, 4.0, 5.0):
+        cfg = dict(c3, brill_a0=a0)
+        tm, sm, chim = solve(dict(cfg, ell_solver="mixed"))
+        tf, sf, chif = solve(dict(cfg, ell_solver="fp64mg"))
+        mtm, msm, am = maximal(dict(cfg, ell_solver="mixed"))
+        mtf, msf, af = maximal(dict(cfg, ell_solver="fp64mg"))
+        out["cases"].append({
+            "a0": a0,
+            "psi": {"mixed_seconds": tm, "fp64_seconds": tf, "mixed_refinements_level0": sm[0],
+                    "mixed_vcycles_level0": sm[1], "mixed_rms_residual": sm[2], "fp64_rms_residual": sf[2],
+                    "max_abs_chi_error": maxdiff(chim, chif)},
+            "maximal_lapse": {"mixed_seconds": mtm, "fp64_seconds": mtf, "mixed_rms_residual": msm[2],
+                              "fp64_rms_residual": msf[2], "max_abs_alpha_error": maxdiff(am, af),
+                              "min_alpha": float(min(a.min() for a in am))}})
+    t_mx, _, chi_mx = solve(dict(one, ell_solver="mixed"))
+    t_64, _, chi_64 = solve(dict(one, ell_solver="fp64mg"))
+    t_sor, st_sor, chi_sor = solve(dict(one, ell_solver="sor", ell_epsilon=1e-8))
+    out["vs_fp64_sor_256"] = {"mixed_seconds": t_mx, "fp64mg_seconds": t_64, "sor_seconds": t_sor,
+                              "sor_iterations": st_sor[0], "mixed_max_abs_chi_diff": maxdiff(chi_mx, chi_sor),
+                              "fp64mg_max_abs_chi_diff": maxdiff(chi_64, chi_sor)}
+    out["max_abs_error"] = max(max(c["psi"]["max_abs_chi_error"], c["maximal_lapse"]["max_abs_alpha_error"])
+                               for c in out["cases"])
+    return out
 
 
 def batch_throughput(n=32, steps=2, seed=7):
@@ -639,8 +706,6 @@ def main():
     if args.probe:
         probe(args)
     elif args.impl == "reference":
-        if args.steps > 3:
-            args.steps = 3  # bounded CPU sample per timed region
         run_reference(args)
     else:
         run_gpu(args)

@@ -82,6 +82,9 @@ extern "C" {
                                        converges to, solved by FP64 iterative refinement with FP32 multigrid
                                        corrections, to an RMS residual of ELL_epsilon or the FP64
                                        rounding floor of the residual, whichever is larger */
+#define OLLIN_ELL_FP64MG        4   /* "fp64mg": no counterpart in the reference -- the same solve as "mixed"
+                                       with FP64 multigrid corrections: the all-FP64 solve of the system
+                                       that the mixed-precision solve's error is measured against */
 
 #define OLLIN_PULSE_SHELL       0   /* scalarpulse_type = "shell"     */
 #define OLLIN_PULSE_TORUS       1   /* scalarpulse_type = "torus"     */

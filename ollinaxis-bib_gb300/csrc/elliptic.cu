@@ -633,8 +633,13 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
             }
             r = -R;
         }
-        A.r32[o] = (float)r;
-        A.d[o] = 0.0f;
+        if (A.d64) {
+            A.r64[o] = r;
+            A.d64[o] = 0.0;
+        } else {
+            A.r32[o] = (float)r;
+            A.d[o] = 0.0f;
+        }
     }
     block_partial(sq, A.partial);
     block_partial(sc, A.partial + gridDim.x * gridDim.y);
@@ -648,15 +653,17 @@ __global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_co
     const int lim_r = A.robin ? G.nr : G.nr - 1, lim_z = A.robin ? G.nz : G.nz - 1;
     if (i > lim_r || j > lim_z) return;  // Dirichlet rows keep their data
     const size_t o = (size_t)i + (size_t)j * G.ld;
-    if (A.psi4) A.u[o] = A.u[o] + (double)A.d[o] / sqrt(sqrt(A.psi4[o]));  // du = dv/psi
-    else A.u[o] = A.u[o] + (double)A.d[o];
+    const double dv = A.d64 ? A.d64[o] : (double)A.d[o];
+    if (A.psi4) A.u[o] = A.u[o] + dv / sqrt(sqrt(A.psi4[o]));  // du = dv/psi
+    else A.u[o] = A.u[o] + dv;
 }
 
 // diagonal of the flat correction operator for the physical Laplacian in
 // dv = psi du: the flat stencil's centre plus psi^4 S1 - lap(psi)/psi, with
 // the flat second-order Laplacian (axis term included) of psi; points on the
 // outer edges keep the flat centre plus psi^4 S1
-__global__ void mix_diag_phys_kernel(LevelGeom G, float* e32, double ec, const double* S1, const double* psi4) {
+template <typename T>
+__global__ void mix_diag_phys_kernel(LevelGeom G, T* e32, double ec, const double* S1, const double* psi4) {
     const int g = G.g;
     const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
@@ -671,7 +678,16 @@ __global__ void mix_diag_phys_kernel(LevelGeom G, float* e32, double ec, const d
                            + (P(1, 0) - P(-1, 0)) / (2.0 * G.dr) * G.ircol[i];
         e = e - lap / p0;
     }
-    e32[o] = (float)e;
+    e32[o] = (T)e;
+}
+
+__global__ void copy64_kernel(LevelGeom G, double* out, const double* in) {
+    const int g = G.g;
+    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    out[o] = in[o];
 }
 
 __global__ void to_float_kernel(LevelGeom G, float* out, const double* in) {
@@ -706,7 +722,20 @@ void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const doubl
                           cudaStream_t s) {
     dim3 blk(32, 4);
     dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
-    mix_diag_phys_kernel<<<grd, blk, 0, s>>>(G, e32, ec, S1, psi4);
+    mix_diag_phys_kernel<float><<<grd, blk, 0, s>>>(G, e32, ec, S1, psi4);
+}
+
+void launch_mix_diag_phys64(const LevelGeom& G, double* e, double ec, const double* S1, const double* psi4,
+                            cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+    mix_diag_phys_kernel<double><<<grd, blk, 0, s>>>(G, e, ec, S1, psi4);
+}
+
+void launch_copy64(const LevelGeom& G, double* out, const double* in, cudaStream_t s) {
+    dim3 blk(32, 4);
+    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
+    copy64_kernel<<<grd, blk, 0, s>>>(G, out, in);
 }
 
 void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s) {

@@ -171,12 +171,13 @@ int check_params(const ollin_params& P) {
     if (P.idata == OLLIN_IDATA_SCALARPULSE && P.mattertype != OLLIN_MATTER_SCALAR)
         return fail(OLLIN_EINVAL, "Scalar pulse initial data needs scalar field type matter.");
     if ((P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) && P.ell_solver != OLLIN_ELL_WAVE &&
-        P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
-        return fail(OLLIN_EINVAL, "elliptic initial data needs an elliptic solver (ELL_solver = wave, sor or mixed)");
+        P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED && P.ell_solver != OLLIN_ELL_FP64MG)
+        return fail(OLLIN_EINVAL,
+                    "elliptic initial data needs an elliptic solver (ELL_solver = wave, sor, mixed or fp64mg)");
     if (P.idata == OLLIN_IDATA_BRILLWAVE && P.brilltype != 0) return fail(OLLIN_EINVAL, "brilltype must be Holz");
     if (P.nb < 0 || P.nb > 3) return fail(OLLIN_EINVAL, "The number of refinement boxes must be between 0 and 3");
     if (P.nb > 0 && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
-        P.ell_solver == OLLIN_ELL_MIXED)
+        (P.ell_solver == OLLIN_ELL_MIXED || P.ell_solver == OLLIN_ELL_FP64MG))
         return fail(OLLIN_EINVAL, "elliptic initial data with refinement boxes needs ELL_solver = wave or sor");
     for (int b = 0; b < P.nb; ++b)
         if (P.nl[b] < 0 || P.nl[b] >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl of a refinement box out of range");
@@ -1569,24 +1570,33 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         cab[i - 1 + g] = (1.0 / L.dr + 0.5 / r) / L.dr;
         cab[ncol + (i - 1 + g)] = (1.0 / L.dr - 0.5 / r) / L.dr;
     }
+    // the correction's precision: FP32 ("mixed") or FP64 ("fp64mg", the
+    // all-FP64 solve of the same system)
+    const bool fp64 = P.ell_solver == OLLIN_ELL_FP64MG;
+    const size_t csize = fp64 ? sizeof(double) : sizeof(float);
     double* dcol = nullptr;
-    float* f32 = nullptr;
-    if (cudaMalloc(&dcol, 2 * ncol * sizeof(double)) != cudaSuccess || cudaMalloc(&f32, 3 * L.n * sizeof(float)) != cudaSuccess) {
+    void* cbuf = nullptr;
+    if (cudaMalloc(&dcol, 2 * ncol * sizeof(double)) != cudaSuccess || cudaMalloc(&cbuf, 3 * L.n * csize) != cudaSuccess) {
         cudaFree(dcol);
         return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
     }
-    MgHierarchy* mg = mg_create(L.nr, L.nz, L.dr, L.dz);
+    MgHierarchy* mg = mg_create(L.nr, L.nz, L.dr, L.dz, fp64 ? 1 : 0);
     struct FreeOnExit {
-        double* a; float* b; MgHierarchy* m;
+        double* a; void* b; MgHierarchy* m;
         ~FreeOnExit() { cudaFree(a); cudaFree(b); mg_destroy(m); }
-    } free_all{dcol, f32, mg};
+    } free_all{dcol, cbuf, mg};
     if (!mg) return fail(OLLIN_ENOMEM, "device allocation failed for the multigrid hierarchy");
     CUDA_OR_FAIL(cudaMemcpyAsync(dcol, cab.data(), 2 * ncol * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    CUDA_OR_FAIL(cudaMemsetAsync(f32, 0, 3 * L.n * sizeof(float), h->stream));
-    const size_t off = (size_t)(g - 1) + (size_t)(g - 1) * L.ld;  // FP32 arrays share the level layout
-    float* d = f32 + off;
-    float* r32 = f32 + L.n + off;
-    float* e32 = f32 + 2 * L.n + off;
+    CUDA_OR_FAIL(cudaMemsetAsync(cbuf, 0, 3 * L.n * csize, h->stream));
+    const size_t off = (size_t)(g - 1) + (size_t)(g - 1) * L.ld;  // correction arrays share the level layout
+    float* f32 = fp64 ? nullptr : (float*)cbuf;
+    double* f64 = fp64 ? (double*)cbuf : nullptr;
+    float* d = fp64 ? nullptr : f32 + off;
+    float* r32 = fp64 ? nullptr : f32 + L.n + off;
+    float* e32 = fp64 ? nullptr : f32 + 2 * L.n + off;
+    double* d64 = fp64 ? f64 + off : nullptr;
+    double* r64 = fp64 ? f64 + L.n + off : nullptr;
+    double* e64c = fp64 ? f64 + 2 * L.n + off : nullptr;
     const double ec = -2.0 * (1.0 / (L.dr * L.dr) + 1.0 / (L.dz * L.dz));
     double* eaux = w.ua;
     double* e = w.va;
@@ -1639,6 +1649,8 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     a.cc = 1.0 / (L.dz * L.dz);
     a.d = d;
     a.r32 = r32;
+    a.d64 = d64;
+    a.r64 = r64;
     a.robin = robin ? 1 : 0;
     a.uinf = 1.0;
     a.partial = S.partial;
@@ -1652,8 +1664,13 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
             rc = after_launch(h);
             if (rc) return rc;
         }
-        if (S.physical) launch_mix_diag_phys(L.G, e32, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
-        else launch_to_float(L.G, e32, a.e64, h->stream);
+        if (S.physical) {
+            if (fp64) launch_mix_diag_phys64(L.G, e64c, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
+            else launch_mix_diag_phys(L.G, e32, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
+        } else {
+            if (fp64) launch_copy64(L.G, e64c, a.e64, h->stream);
+            else launch_to_float(L.G, e32, a.e64, h->stream);
+        }
         rc = after_launch(h);
         if (rc) return rc;
         launch_mix_resid(a, h->stream);
@@ -1675,8 +1692,13 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         }
         last = rms;
         ++outer;
-        mg_load(mg, r32, e32, L.ld, h->stream);
-        mg_solve(mg, a.robin, ncyc, d, L.ld, h->stream);
+        if (fp64) {
+            mg_load(mg, r64, e64c, L.ld, h->stream);
+            mg_solve(mg, a.robin, ncyc, d64, L.ld, h->stream);
+        } else {
+            mg_load(mg, r32, e32, L.ld, h->stream);
+            mg_solve(mg, a.robin, ncyc, d, L.ld, h->stream);
+        }
         h->launches += 2 + (long long)ncyc * mg_launches_per_cycle(mg, a.robin);
         CUDA_OR_FAIL(cudaGetLastError());
         cycles += ncyc;
@@ -1854,7 +1876,8 @@ int elliptic_data(ollin_handle* h, std::vector<std::vector<double>>& ell_u, std:
         }
     }
     rc = (P.ell_solver == OLLIN_ELL_SOR) ? sor_elliptic(h, S)
-         : (P.ell_solver == OLLIN_ELL_MIXED) ? mixed_elliptic(h, S) : wave_elliptic(h, S);
+         : (P.ell_solver == OLLIN_ELL_MIXED || P.ell_solver == OLLIN_ELL_FP64MG) ? mixed_elliptic(h, S)
+                                                                                  : wave_elliptic(h, S);
     if (rc) return rc;
     h->ell_steps[0] = S.steps[0];
     h->ell_steps[1] = S.steps[1];
@@ -1965,10 +1988,11 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
     if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE)
         return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave on the device");
-    if (h->nb > 0 && P.ell_solver == OLLIN_ELL_MIXED)
+    if (h->nb > 0 && (P.ell_solver == OLLIN_ELL_MIXED || P.ell_solver == OLLIN_ELL_FP64MG))
         return fail(OLLIN_EINVAL, "maximal slicing with refinement boxes needs ELL_solver = wave or sor");
-    if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED)
-        return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor or mixed");
+    if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED &&
+        P.ell_solver != OLLIN_ELL_FP64MG)
+        return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor, mixed or fp64mg");
     // K_ij K^ij and rho + S of the current state (the last ``auxiliary``)
     for (int l = 0; l < h->nlev; ++l) {
         int rc = analysis(h, l);

@@ -297,6 +297,9 @@ struct MixArgs {
     double* u; const double* e64; const double* f64;
     const double* ca; const double* cb; double cc;   // FP64 coefficients
     float* d; float* r32;
+    // FP64 correction (ELL_solver = "fp64mg"): when d64 is set the residual
+    // goes to r64 and the correction comes from d64 instead of r32/d
+    double* d64; double* r64;
     int robin; double uinf;
     double* partial;                                 // per-block sums of squares
     // physical Laplacian (maximal slicing): the per-point nine-point stencil
@@ -308,19 +311,23 @@ struct MixArgs {
 };
 void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const double* S1, const double* psi4,
                           cudaStream_t s);
+void launch_mix_diag_phys64(const LevelGeom& G, double* e, double ec, const double* S1, const double* psi4,
+                            cudaStream_t s);
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
 int mix_blocks(const LevelGeom& G);
 void launch_mix_update(const MixArgs& a, cudaStream_t s);
 
-// FP32 geometric multigrid for the correction equation (multigrid.cu)
+// Geometric multigrid for the correction equation (multigrid.cu), FP32 or
+// FP64 (fp64 = 1); r, e and d are arrays of that precision
 struct MgHierarchy;
-MgHierarchy* mg_create(int n, int m, double dr, double dz);
+MgHierarchy* mg_create(int n, int m, double dr, double dz, int fp64);
 void mg_destroy(MgHierarchy* H);
 int mg_levels(const MgHierarchy* H);
 int mg_launches_per_cycle(const MgHierarchy* H, int robin);
-void mg_load(MgHierarchy* H, const float* r, const float* e, long ld, cudaStream_t s);
-void mg_solve(MgHierarchy* H, int robin, int ncycles, float* d, long ld, cudaStream_t s);
+void mg_load(MgHierarchy* H, const void* r, const void* e, long ld, cudaStream_t s);
+void mg_solve(MgHierarchy* H, int robin, int ncycles, void* d, long ld, cudaStream_t s);
 void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s);
+void launch_copy64(const LevelGeom& G, double* out, const double* in, cudaStream_t s);
 
 void launch_inject(const InjectArgs& a, cudaStream_t s);
 

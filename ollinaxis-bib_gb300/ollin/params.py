@@ -52,7 +52,7 @@ BOUND = {"radiative": 0, "none": 1}
 MATTER = {"vacuum": 0, "scalar": 1}
 POTENTIAL = {"none": 0, "phi2": 1, "phi4": 2}
 IDATA = {"minkowski": 0, "schwarzschild": 1, "BrillLindquist": 2, "BrillWave": 3, "scalarpulse": 4}
-ELL_SOLVER = {"none": 0, "wave": 1, "sor": 2, "mixed": 3}
+ELL_SOLVER = {"none": 0, "wave": 1, "sor": 2, "mixed": 3, "fp64mg": 4}
 PULSE = {"shell": 0, "torus": 1, "Baumgarte": 2}
 BRILLTYPE = {"Holz": 0}
 ILAPSE = {"one": 0, "isotropic": 1, "psiminus2": 2, "psiminus4": 3, "maximal": 4}

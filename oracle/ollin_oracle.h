@@ -25,6 +25,10 @@ int ollin_oracle_maximal_slicing(ollin_oracle* o, const double* va_max);
 int ollin_oracle_grid(const ollin_oracle* o, int gid, int* box, int* level);
 int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]);
 double ollin_oracle_point_updates(const ollin_oracle* o);
+/* OpenMP threads of the oracle's loops from now on (>= 1), and the current
+ * number; the CPU baselines time one and all host cores in one process */
+void ollin_oracle_set_threads(int n);
+int ollin_oracle_max_threads(void);
 /* iteration counts of the last elliptic solve on this thread: steps[0] of
  * the coarse phase, steps[1] of the all-level phase (0 if there was none) */
 int ollin_oracle_ell_stats(int steps[2], double* gres);

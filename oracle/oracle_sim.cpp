@@ -11,6 +11,8 @@
 //   of src/base/save0Ddata.f90:221-288,370-374.
 // It exposes a C API (ollin_oracle.h) with the same parameter struct as the
 // GPU library so that one harness drives both.
+#include <omp.h>
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -766,6 +768,10 @@ int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[
 }
 
 double ollin_oracle_point_updates(const ollin_oracle* o) { return o->S.point_updates; }
+
+void ollin_oracle_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+
+int ollin_oracle_max_threads(void) { return omp_get_max_threads(); }
 
 int ollin_oracle_ell_stats(int steps[2], double* gres) {
     steps[0] = g_ell_stats.steps[0];

@@ -48,6 +48,8 @@ def lib():
         L.ollin_oracle_point_updates.restype = ctypes.c_double
         L.ollin_oracle_last_error.restype = ctypes.c_char_p
         L.ollin_oracle_ell_stats.argtypes = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]
+        L.ollin_oracle_set_threads.argtypes = [ctypes.c_int]
+        L.ollin_oracle_max_threads.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -143,3 +145,9 @@ def ell_stats():
     gres = ctypes.c_double()
     phases = lib().ollin_oracle_ell_stats(steps, ctypes.byref(gres))
     return steps[0], steps[1], phases, gres.value
+
+
+def set_threads(n):
+    """OpenMP threads of the oracle from now on."""
+    lib().ollin_oracle_set_threads(int(n))
+    return lib().ollin_oracle_max_threads()

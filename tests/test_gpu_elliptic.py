@@ -134,16 +134,20 @@ def test_sor_data_matches_oracle(cfg):
 
 MIXED_2LEV = dict(SOR_2LEV, ell_solver="mixed", ell_epsilon=1e-12)
 MIXED_BRILL = dict(SOR_BRILL, ell_solver="mixed", ell_epsilon=1e-12)
+FP64MG_2LEV = dict(MIXED_2LEV, ell_solver="fp64mg")
+FP64MG_BRILL = dict(MIXED_BRILL, ell_solver="fp64mg")
 
 
-@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL], ids=["mixed_pulse_2lev", "mixed_brill_3lev"])
+@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL],
+                         ids=["mixed_pulse_2lev", "mixed_brill_3lev", "fp64mg_pulse_2lev", "fp64mg_brill_3lev"])
 def test_mixed_precision_solve_matches_fp64_sor(cfg):
     """ELL_solver = "mixed" (FP64 iterative refinement, FP32 multigrid
-    corrections) solves the discrete system that SOR converges to.  The reference's SOR
+    corrections) and "fp64mg" (the same with FP64 multigrid corrections)
+    solve the discrete system that SOR converges to.  The reference's SOR
     stop test at ELL_epsilon = 1e-8 corresponds to an RMS residual near
     N * 1e-16, so the oracle's FP64 SOR solution is the FP64 solve to compare
     with: the conformal factor agrees to 1e-10 once the FP64 residual of the
-    mixed solve is below 1e-12."""
+    solve is below 1e-12."""
     from ollin.gpu import Evolution
     o = Oracle(params(dict(cfg, ell_solver="sor", ell_epsilon=1e-8)))
     o.initial_data()
@@ -157,3 +161,34 @@ def test_mixed_precision_solve_matches_fp64_sor(cfg):
         assert chi <= 1e-10 and dphi <= 1e-10, "level %d: chi rel %.2e, phi abs %.2e" % (lev, chi, dphi)
         for nm in ("A", "B", "H", "C", "alpha"):
             assert rel_diff(e.download(lev, nm), o.get(lev, nm)) <= 1e-10
+
+
+@pytest.mark.parametrize("a0", [1.0, 4.0, 5.0])
+def test_precision_pattern_against_fp64_solve(a0):
+    """The Brill-wave precision configuration at reduced size (2 levels of
+    256^2, dr0 = 0.16, so the same physical extent as 4 levels of 1024^2 at
+    0.04 on the coarse level): the conformal factor of the mixed solver
+    against the all-FP64 multigrid solve of the same system, then the
+    maximal-slicing lapse after one coarse step, every solve by each solver;
+    both agree to 1e-10 (max abs)."""
+    from ollin.gpu import Evolution
+    base = dict(eqsym=1, order="four", integrator="rk4", ilapse="one", idata="BrillWave", brill_a0=a0,
+                brill_sr0=1.0, brill_sz0=1.0, nrtotal=256, nztotal=256, nl0=1, dr0=0.16, dz0=0.16,
+                ell_epsilon=1e-12, maximalevery=1, slicing="1+log", gauge_f=2.0)
+    res = {}
+    for solver in ("mixed", "fp64mg"):
+        e = Evolution(params(dict(base, ell_solver=solver)))
+        e.initial_data()
+        assert e.ell_stats()[2] < 1e-11
+        chi = [e.download(lev, "chi") for lev in e.levels()]
+        e.initialize()
+        e.maximal_slicing()
+        e.step()
+        e.maximal_slicing()
+        alpha = [e.download(lev, "alpha") for lev in e.levels()]
+        res[solver] = (chi, alpha)
+        e.close()
+    for k, nm in enumerate(("chi", "alpha")):
+        err = max(float(abs(a - b).max()) for a, b in zip(res["mixed"][k], res["fp64mg"][k]))
+        print("a0 = %g: max |%s_mixed - %s_fp64| = %.2e" % (a0, nm, nm, err))
+        assert err <= 1e-10, (nm, err)
