@@ -443,57 +443,86 @@ def elliptic_precision():
     return out
 
 
-def batch_throughput(n=32, steps=2, seed=7):
-    """The batching pattern: n independent massless scalar-field shells
-    (phi = a exp(-(r - 5)^2), a log-uniform in [0.01, 0.1], seeded; elliptic
-    initial data by the mixed solver), grids of 64^2 to 128^2 per level with
-    2-3 levels (seeded mix), advanced one coarse step at a time either one
-    evolution after another or all together (ollin_gpu_coarse_step_many,
-    every step queued on its own stream).  Host wall time, launches included."""
+def c4_configs(n, seed):
+    """The batching configuration's seeded mix: massless scalar-field shells
+    phi = a exp(-(r - 5)^2) (r0 = 5, s = 1), a log-uniform in [0.01, 0.1],
+    grids of 64^2 to 512^2 per level (multiples of 64) with 2-5 levels, a
+    16 M square coarse domain (dr0 = 16/N), elliptic data by the mixed solver."""
     import numpy as np
-    from ollin.gpu import Evolution, step_many
-    from ollin.params import params_from_dict
     rng = np.random.default_rng(seed)
     cfgs = []
     for _ in range(n):
-        size = int(rng.choice([64, 96, 128]))
-        cfgs.append(dict(nrtotal=size, nztotal=size, nl0=int(rng.integers(1, 3)), dr0=16.0 / size, dz0=16.0 / size,
+        size = int(64 * rng.integers(1, 9))
+        cfgs.append(dict(nrtotal=size, nztotal=size, nl0=int(rng.integers(1, 5)), dr0=16.0 / size, dz0=16.0 / size,
                          eqsym=1, order="four", integrator="rk4", dtfac=0.25, boundtype="radiative",
                          idata="scalarpulse", mattertype="scalar", scalarpotential="none", scalarpulse_type="shell",
                          scalar_a0=float(np.exp(rng.uniform(np.log(0.01), np.log(0.1)))), scalar_r0=5.0,
                          scalar_sr0=1.0, scalar_sz0=1.0, ilapse="one", slicing="1+log", gauge_f=2.0,
                          geodiss=0.02, scalardiss=0.02, ell_solver="mixed", ell_epsilon=1e-12))
+    return cfgs
 
-    def build():
-        es = []
-        for c in cfgs:
-            e = Evolution(params_from_dict(c))
-            e.initial_data()
-            e.initialize()
-            es.append(e)
-        return es
 
-    seq, bat = build(), build()
-    for e in seq:  # warm-up
-        e.step()
-    step_many(bat)
-    p0 = sum(e.point_updates() for e in seq)
-    t = time.perf_counter()
-    for _ in range(steps):
-        for e in seq:
+def batch_throughput(n=256, steps=1, seed=7):
+    """The batching configuration (256 seeded scalar-field shells, 64^2-512^2
+    per level, 2-5 levels), t_end cut to ``steps`` coarse steps per run:
+      * plain: each evolution alone, set up, then its steps timed by
+        themselves (host wall clock, launches included);
+      * batched: all n set up, then every coarse step of all of them queued
+        together (ollin_gpu_coarse_step_many, one stream each).
+    The bound: batching cannot beat the FP64 ceiling of the device, the rate
+    R of the large single instance; plain run i at rate r_i leaves the rest
+    of the device idle, so batched/plain <= sum(t_i) / (sum(pu_i) / R)."""
+    import numpy as np
+    from ollin.gpu import Evolution, step_many
+    from ollin.params import params_from_dict
+    cfgs = c4_configs(n, seed)
+
+    def setup(c):
+        e = Evolution(params_from_dict(c))
+        e.initial_data()
+        e.initialize()
+        return e
+
+    w = setup(cfgs[0])  # warm-up: kernel loading
+    w.step()
+    w.close()
+    t_plain, pu_plain, digest_plain = [], [], []
+    t_setup = time.perf_counter()
+    for c in cfgs:
+        e = setup(c)
+        p0 = e.point_updates()
+        t = time.perf_counter()
+        for _ in range(steps):
             e.step()
-    t_seq = time.perf_counter() - t
-    pu = sum(e.point_updates() for e in seq) - p0
+        t_plain.append(time.perf_counter() - t)
+        pu_plain.append(e.point_updates() - p0)
+        digest_plain.append(e.norms(0, "trK"))
+        e.close()
+    t_setup = time.perf_counter() - t_setup - sum(t_plain)
+    es = [setup(c) for c in cfgs]
+    p0 = sum(e.point_updates() for e in es)
     t = time.perf_counter()
     for _ in range(steps):
-        step_many(bat)
+        step_many(es)
     t_bat = time.perf_counter() - t
-    same = all(np.array_equal(a.download(0, "trK"), b.download(0, "trK")) for a, b in zip(seq, bat))
-    for e in seq + bat:
+    pu_bat = sum(e.point_updates() for e in es) - p0
+    same = all(np.array_equal(a, e.norms(0, "trK")) for a, e in zip(digest_plain, es))
+    for e in es:
         e.close()
-    return {"workload": "%d massless scalar shells, 64^2-128^2 x 2-3 levels (seeded), %d coarse steps each" % (n, steps),
-            "sequential_point_updates_per_s": pu / t_seq, "batched_point_updates_per_s": pu / t_bat,
-            "speedup": t_seq / t_bat, "identical_results": bool(same)}
+    t_plain = np.array(t_plain)
+    pu = float(sum(pu_plain))
+    rate_plain = np.array(pu_plain) / t_plain
+    return {"workload": "%d massless scalar shells (a log-uniform in [0.01, 0.1], seeded), 64^2-512^2 per level x 2-5 "
+                        "levels, elliptic data by the mixed solver; t_end cut to %d coarse step(s) per run"
+                        % (n, steps),
+            "plain_runs_per_s": n / float(t_plain.sum()), "batched_runs_per_s": n / t_bat,
+            "speedup": float(t_plain.sum()) / t_bat,
+            "plain_point_updates_per_s": pu / float(t_plain.sum()), "batched_point_updates_per_s": pu_bat / t_bat,
+            "plain_run_seconds_p50": float(np.percentile(t_plain, 50)),
+            "plain_run_seconds_p99": float(np.percentile(t_plain, 99)),
+            "plain_rate_p50": float(np.percentile(rate_plain, 50)),
+            "setup_seconds_per_run": t_setup / n,
+            "identical_results": bool(same)}
 
 
 def plain_small():

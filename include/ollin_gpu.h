@@ -408,6 +408,48 @@ double ollin_gpu_fp64_rate(void);
  * right-hand side. */
 double ollin_gpu_op_rate(int op);
 
+/*
+ * Restart data: replaces checkpointsave / checkpointrestart
+ * (src/base/checkpoint.f90:2-328, :338-700).  A reference checkpoint holds,
+ * per grid, every evolved array, its boundary history var_bound_{rL,rR,zL,zR}
+ * (:253-300) and the clocks t, t1, t2.  On the device the history lives in
+ * whole time levels of the state: ``which`` = 0 is the current state, 1 the
+ * state at the start of the level's last step (history level 0 on the
+ * strips), 2 the start of the step before (history level 1); history level
+ * 2 of the reference is never read by finebound's time interpolation.
+ * A restart is: ollin_gpu_create, ollin_gpu_upload_slot of every evolved
+ * field for which = 0, 1, 2, ollin_gpu_set_clocks of every grid, then
+ * ollin_gpu_initialize, which runs what evolve.f90:128-219 runs after
+ * checkpointrestart: parity fill, ``auxiliary`` (with the t > 0 branches,
+ * since t is no longer 0), the Gamma-driver reset dtbeta = drivercsi Delta
+ * (:174-195, as the reference does on a restart) and the t = 0 syncboxes.
+ * That ``auxiliary`` call projects A, B, C, H onto unit determinant once
+ * more, as the reference's does, which can move them by an ulp; for a
+ * continuation bit for bit use ollin_gpu_resume instead of
+ * ollin_gpu_initialize.
+ * Fields: the ids accepted by ollin_gpu_upload.  ld_r as for ollin_gpu_upload.
+ */
+int ollin_gpu_download_slot(ollin_handle* h, int level, int field, int which, double* a, int ld_r);
+int ollin_gpu_upload_slot(ollin_handle* h, int level, int field, int which, const double* a, int ld_r);
+/* Resume a suspended evolution instead of restarting it: after the slots and
+ * clocks of a running evolution (t > 0 on every grid) have been uploaded,
+ * recompute the auxiliary quantities of that state without projecting it
+ * onto unit determinant again and without the Gamma-driver reset, and mark
+ * the handle initialized.  The evolution then continues bit for bit as if
+ * never interrupted (an ``auxiliary`` call, as ollin_gpu_initialize makes,
+ * re-applies factordet and moves A, B, C, H by an ulp).  No counterpart in
+ * the reference: it lets a host evict an evolution's state to host memory
+ * and bring it back.  Not for a state suspended between a maximal-slicing
+ * solve or a syncboxes copy and the next coarse step (their pending stale
+ * quantities are not part of the slots). */
+int ollin_gpu_resume(ollin_handle* h);
+/* out = {t, t1, t2, s} of grid ``level`` (prl/arrays.pl:54-58; s is the
+ * level's step count, whose parity decides restriction, onestep.f90:472). */
+int ollin_gpu_get_clocks(ollin_handle* h, int level, double out[4]);
+/* Sets {t, t1, t2, s} of a grid; only before ollin_gpu_initialize
+ * (OLLIN_ESTATE afterwards).  s must be a whole number. */
+int ollin_gpu_set_clocks(ollin_handle* h, int level, const double in[4]);
+
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);
 

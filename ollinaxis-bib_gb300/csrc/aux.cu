@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ 
     double A = a.st[F_A][o], B = a.st[F_B][o], C = a.st[F_C][o], H = a.st[F_H][o];
     if (a.t0) {
         a.st[F_CHI][o] = exp(-2.0 * a.st[F_PHI][o]);
-    } else {
+    } else if (a.project) {
         const double rc = r * C;
         const double q = (A * B - rc * rc) * H;  // hdet = 1
         const double iq = rcbrt(q);              // 1/(det)^(1/3)

@@ -370,13 +370,14 @@ std::vector<int> active_fields(const ollin_handle* h, bool with_phi) {
 
 // ``auxiliary`` on one level's current slot (auxiliary_geometry.f90 parts
 // that feed the right-hand side).
-int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0) {
+int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0, bool project = true) {
     AuxArgs a{};
     a.G = L.G;
     for (int f = 0; f < NFIELDS; ++f) a.st[f] = base_ptr(L, L.slot[slot][f]);
     for (int x = 0; x < NAUX; ++x) a.aux[x] = base_ptr(L, L.aux[x]);
     a.t0 = t0 ? 1 : 0;
     a.scalar = h->scalar ? 1 : 0;
+    a.project = project ? 1 : 0;
     launch_aux_point(a, h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
@@ -2262,6 +2263,66 @@ int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_
     return OLLIN_OK;
 }
 
+// The three time levels of an evolved field the next coarse step reads:
+// slot 0 the current state, 1 the state at the start of the level's last
+// step (the reference's var_bound_*(...,0) on the boundary strips), 2 the
+// start of the step before (var_bound_*(...,1)).
+static int history_slot(const DLevel& L, int which) {
+    return which == 0 ? L.cur : which == 1 ? L.p : which == 2 ? L.pp : -1;
+}
+
+int ollin_gpu_download_slot(ollin_handle* h, int level, int field, int which, double* a, int ld_r) {
+    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    bool is_aux;
+    const int f = internal_field(field, &is_aux);
+    if (f < 0 || is_aux || !field_active(h, f)) return fail(OLLIN_EINVAL, "not an evolved field of these parameters");
+    const int sl = history_slot(L, which);
+    if (sl < 0) return fail(OLLIN_EINVAL, "slot must be 0 (current), 1 or 2 (history)");
+    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
+    CUDA_OR_FAIL(cudaMemcpy2DAsync(a, (size_t)ld_r * sizeof(double), L.slot[sl][f], (size_t)L.ld * sizeof(double),
+                                   (size_t)(L.nr + L.g) * sizeof(double), (size_t)(L.nz + L.g), cudaMemcpyDeviceToHost,
+                                   h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_upload_slot(ollin_handle* h, int level, int field, int which, const double* a, int ld_r) {
+    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    bool is_aux;
+    const int f = internal_field(field, &is_aux);
+    if (f < 0 || is_aux || !field_active(h, f)) return fail(OLLIN_EINVAL, "not an evolved field of these parameters");
+    const int sl = history_slot(L, which);
+    if (sl < 0) return fail(OLLIN_EINVAL, "slot must be 0 (current), 1 or 2 (history)");
+    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
+    CUDA_OR_FAIL(cudaMemcpy2DAsync(L.slot[sl][f], (size_t)L.ld * sizeof(double), a, (size_t)ld_r * sizeof(double),
+                                   (size_t)(L.nr + L.g) * sizeof(double), (size_t)(L.nz + L.g), cudaMemcpyHostToDevice,
+                                   h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_get_clocks(ollin_handle* h, int level, double out[4]) {
+    if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    out[0] = h->t[level];
+    out[1] = h->t1[level];
+    out[2] = h->t2[level];
+    out[3] = (double)h->s[level];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_set_clocks(ollin_handle* h, int level, const double in[4]) {
+    if (!h || !in || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    if (h->initialized) return fail(OLLIN_ESTATE, "clocks are set before ollin_gpu_initialize (a restart)");
+    if (!(in[3] >= 0.0) || in[3] != std::floor(in[3])) return fail(OLLIN_EINVAL, "the step count must be a whole number");
+    h->t[level] = in[0];
+    h->t1[level] = in[1];
+    h->t2[level] = in[2];
+    h->s[level] = (long)in[3];
+    return OLLIN_OK;
+}
+
 int ollin_gpu_initial_data(ollin_handle* h) {
     if (!h) return fail(OLLIN_EINVAL, "null handle");
     // analytic data, or the elliptic solve of idata_scalarpulse.f90 /
@@ -2290,6 +2351,22 @@ int ollin_gpu_initialize(ollin_handle* h) {
     }
     for (int level = 1; level <= h->nlmax; ++level) {  // evolve.f90:211-219
         int rc = sync_level(h, level);
+        if (rc) return rc;
+    }
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    h->initialized = true;
+    return OLLIN_OK;
+}
+
+int ollin_gpu_resume(ollin_handle* h) {
+    if (!h) return fail(OLLIN_EINVAL, "null handle");
+    if (h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_resume replaces ollin_gpu_initialize");
+    for (int l = 0; l < h->nlev; ++l)
+        if (h->t[l] == 0.0) return fail(OLLIN_EINVAL, "resume needs the clocks of a running evolution (t > 0)");
+    // the auxiliary quantities of the uploaded state, which the last
+    // ``auxiliary`` call of the suspended evolution already projected
+    for (int l = 0; l < h->nlev; ++l) {
+        int rc = do_aux(h, h->L[l], h->L[l].cur, false, false);
         if (rc) return rc;
     }
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));

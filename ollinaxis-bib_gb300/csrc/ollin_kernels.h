@@ -71,6 +71,10 @@ struct AuxArgs {
     double* aux[NAUX];
     int t0;
     int scalar;
+    // t > 0: 1 projects A, B, C, H onto unit determinant in place (factordet,
+    // every ``auxiliary`` call of the reference); 0 takes the state as it is
+    // (a resumed state that the last ``auxiliary`` call already projected)
+    int project;
 };
 
 // Parity ghost fill of the evolved fields (generated symmetries_r/_z).

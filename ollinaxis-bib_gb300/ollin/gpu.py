@@ -91,6 +91,11 @@ def load(build_if_missing=True):
     L.ollin_server_set_graphs.argtypes = [vp, ctypes.c_int]
     L.ollin_gpu_step_graphs.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
     L.ollin_gpu_step_chaining.argtypes = [vp, ctypes.c_int]
+    L.ollin_gpu_download_slot.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.ollin_gpu_upload_slot.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.ollin_gpu_get_clocks.argtypes = [vp, ctypes.c_int, dp]
+    L.ollin_gpu_resume.argtypes = [vp]
+    L.ollin_gpu_set_clocks.argtypes = [vp, ctypes.c_int, dp]
     _lib = L
     return L
 
@@ -137,6 +142,11 @@ class Evolution:
     def initialize(self):
         self._check(self.L.ollin_gpu_initialize(self.h))
 
+    def resume(self):
+        """After upload_slot/set_clocks of a suspended evolution: continue it
+        bit for bit (ollin_gpu_resume), instead of ``initialize``."""
+        self._check(self.L.ollin_gpu_resume(self.h))
+
     def aux(self, level):
         self._check(self.L.ollin_gpu_aux(self.h, level))
 
@@ -171,6 +181,34 @@ class Evolution:
         d = self.desc(level)
         a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).T)
         self._check(self.L.ollin_gpu_upload(self.h, level, field_id(name), a.ctypes.data, d.nr + d.ghost))
+
+    # restart data (checkpoint.f90) ---------------------------------------------
+    def download_slot(self, level, name, which):
+        """Time level ``which`` of an evolved field: 0 the current state, 1
+        the start of the level's last step, 2 the start of the step before
+        (on the boundary strips: the reference's var_bound_*(..., 0) and
+        (..., 1))."""
+        d = self.desc(level)
+        a = np.zeros((d.nz + d.ghost, d.nr + d.ghost), dtype=np.float64)
+        self._check(self.L.ollin_gpu_download_slot(self.h, level, field_id(name), which, a.ctypes.data,
+                                                   d.nr + d.ghost))
+        return np.ascontiguousarray(a.T)
+
+    def upload_slot(self, level, name, which, arr):
+        d = self.desc(level)
+        a = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).T)
+        self._check(self.L.ollin_gpu_upload_slot(self.h, level, field_id(name), which, a.ctypes.data,
+                                                 d.nr + d.ghost))
+
+    def clocks(self, level):
+        """(t, t1, t2, s) of a grid."""
+        out = np.zeros(4)
+        self._check(self.L.ollin_gpu_get_clocks(self.h, level, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
+
+    def set_clocks(self, level, clocks):
+        v = np.ascontiguousarray(np.asarray(clocks, dtype=np.float64))
+        self._check(self.L.ollin_gpu_set_clocks(self.h, level, v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
 
     def norms(self, level, name):
         out = np.zeros(5)

@@ -49,10 +49,14 @@ void diff1r(Level& L, const Arr& f, Arr& d, int symr) {
 void diff1z(Level& L, const Arr& f, Arr& d, int symz) {
     GRID_DIMS;
     const double idz = 1.0 / L.dz;
+    // the interior rows with r innermost (contiguous), then the edge rows and
+    // the equator fill: every point gets the statement the reference gives it
+#pragma omp parallel for schedule(static)
+    for (int j = 3 - g; j <= Nz - 2; ++j)
+        for (int i = 1 - g; i <= Nr; ++i)
+            d(i, j) = idz * (8.0 * (f(i, j + 1) - f(i, j - 1)) - (f(i, j + 2) - f(i, j - 2))) / 12.0;
 #pragma omp parallel for schedule(static)
     for (int i = 1 - g; i <= Nr; ++i) {
-        for (int j = 3 - g; j <= Nz - 2; ++j)
-            d(i, j) = idz * (8.0 * (f(i, j + 1) - f(i, j - 1)) - (f(i, j + 2) - f(i, j - 2))) / 12.0;
         int j = 2 - g;
         d(i, j) = -idz * (3.0 * f(i, j - 1) + 10.0 * f(i, j) - 18.0 * f(i, j + 1) + 6.0 * f(i, j + 2) - f(i, j + 3)) / 12.0;
         j = 1 - g;
@@ -90,9 +94,11 @@ void diff2z(Level& L, const Arr& f, Arr& d, int symz) {
     const double idz = 1.0 / L.dz;
     const double idz2 = idz * idz;
 #pragma omp parallel for schedule(static)
-    for (int i = 1 - g; i <= Nr; ++i) {
-        for (int j = 3 - g; j <= Nz - 2; ++j)
+    for (int j = 3 - g; j <= Nz - 2; ++j)
+        for (int i = 1 - g; i <= Nr; ++i)
             d(i, j) = -idz2 * (30.0 * f(i, j) - 16.0 * (f(i, j + 1) + f(i, j - 1)) + f(i, j + 2) + f(i, j - 2)) / 12.0;
+#pragma omp parallel for schedule(static)
+    for (int i = 1 - g; i <= Nr; ++i) {
         int j = 2 - g;
         d(i, j) = idz2 * (10.0 * f(i, j - 1) - 15.0 * f(i, j) - 4.0 * f(i, j + 1) + 14.0 * f(i, j + 2) - 6.0 * f(i, j + 3) + f(i, j + 4)) / 12.0;
         j = 1 - g;
@@ -215,13 +221,15 @@ void diffadvz(Level& L, const Arr& f, Arr& d, int symz) {
     const Arr& beta_z = L.a("beta_z");
     const double idz = 1.0 / L.dz;
 #pragma omp parallel for schedule(static)
-    for (int i = 1 - g; i <= Nr; ++i) {
-        for (int j = 4 - g; j <= Nz - 3; ++j) {
+    for (int j = 4 - g; j <= Nz - 3; ++j)
+        for (int i = 1 - g; i <= Nr; ++i) {
             if (beta_z(i, j) <= 0.0)
                 d(i, j) = +0.25 * idz * (3.0 * f(i, j + 1) + 10.0 * f(i, j) - 18.0 * f(i, j - 1) + 6.0 * f(i, j - 2) - f(i, j - 3)) / 3.0;
             else
                 d(i, j) = -0.25 * idz * (3.0 * f(i, j - 1) + 10.0 * f(i, j) - 18.0 * f(i, j + 1) + 6.0 * f(i, j + 2) - f(i, j + 3)) / 3.0;
         }
+#pragma omp parallel for schedule(static)
+    for (int i = 1 - g; i <= Nr; ++i) {
         int j = 3 - g;
         if (beta_z(i, j) <= 0.0)
             d(i, j) = -0.25 * idz * (3.0 * f(i, j - 1) + 10.0 * f(i, j) - 18.0 * f(i, j + 1) + 6.0 * f(i, j + 2) - f(i, j + 3)) / 3.0;

@@ -193,11 +193,19 @@ void accumulate(Sim& S, Level& L, int k, int niter, double w) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& a = L.a(e.name + "_a"); Arr& s = L.a("s" + e.name);
         const size_t n = a.v.size();
+        double* av = a.v.data();
+        double* sv = s.v.data();
         if (!last) {
-            if (first) for (size_t q = 0; q < n; ++q) a.v[q] = w * s.v[q];
-            else for (size_t q = 0; q < n; ++q) a.v[q] = a.v[q] + w * s.v[q];
+            if (first) {
+#pragma omp parallel for schedule(static)
+                for (size_t q = 0; q < n; ++q) av[q] = w * sv[q];
+            } else {
+#pragma omp parallel for schedule(static)
+                for (size_t q = 0; q < n; ++q) av[q] = av[q] + w * sv[q];
+            }
         } else {
-            for (size_t q = 0; q < n; ++q) s.v[q] = a.v[q] + w * s.v[q];
+#pragma omp parallel for schedule(static)
+            for (size_t q = 0; q < n; ++q) sv[q] = av[q] + w * sv[q];
         }
     }
 }
@@ -206,7 +214,11 @@ void update(Sim& S, Level& L, double dtw) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name); Arr& vp = L.a(e.name + "_p"); Arr& s = L.a("s" + e.name);
         const size_t n = v.v.size();
-        for (size_t q = 0; q < n; ++q) v.v[q] = vp.v[q] + dtw * s.v[q];
+        double* vv = v.v.data();
+        const double* pv = vp.v.data();
+        const double* sv = s.v.data();
+#pragma omp parallel for schedule(static)
+        for (size_t q = 0; q < n; ++q) vv[q] = pv[q] + dtw * sv[q];
     }
 }
 
@@ -230,21 +242,23 @@ void symmetries_z(Sim& S, Level& L) {
 // interp.f90:2-270 -- value of one grid function of grid ``gid`` (a box and
 // level) at (r0,z0)
 // ---------------------------------------------------------------------------
-double interp(Sim& S, int gid, const Arr& var, double r0, double z0) {
-    Level& L = S.L[gid];
+// The interpolation itself, with the grid's coordinate arrays already
+// resolved (no map lookups: safe inside the parallel loops below); returns
+// false when (r0, z0) lies outside the grid.
+static bool interp_at(const Sim& S, int gid, const Arr& r, const Arr& z, const Arr& var, double r0, double z0,
+                      double* out) {
+    const Level& L = S.L[gid];
     const int g = L.g;
     const int level = L.level;
     const double small = 1.0e-10;
     const double rmin = S.rminl[gid] - small, rmax = S.rmaxl[gid];
     const double zmin = S.zminl[gid] - small, zmax = S.zmaxl[gid];
-    if (r0 < rmin || r0 > rmax || z0 < zmin || z0 > zmax)
-        throw std::runtime_error("interp: interpolating point is outside the local grid");
-    Arr& r = L.a("r"); Arr& z = L.a("z");
+    if (r0 < rmin || r0 > rmax || z0 < zmin || z0 > zmax) return false;
     const int i0 = (int)((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
     const double deltar = r0 - r(i0, 0);
     const int j0 = (int)((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
     const double deltaz = z0 - z(0, j0);
-    if (deltar == 0.0 && deltaz == 0.0) return var(i0, j0);
+    if (deltar == 0.0 && deltaz == 0.0) { *out = var(i0, j0); return true; }
     const bool forcelinear = ((S.rmaxl[gid] - r0) < S.drl[level]) || ((S.zmaxl[gid] - z0) < S.dzl[level])
         || ((r0 - S.rminl[gid]) < S.drl[level]) || ((z0 - S.zminl[gid]) < S.dzl[level]);
     double fa[4][4];
@@ -258,8 +272,9 @@ double interp(Sim& S, int gid, const Arr& var, double r0, double z0) {
     const double auxr = deltar / S.drl[level];
     const double auxz = deltaz / S.dzl[level];
     if (!S.P.interp_bicubic || forcelinear) {
-        return fa[1][1] * (1.0 - auxr) * (1.0 - auxz) + fa[2][1] * auxr * (1.0 - auxz)
+        *out = fa[1][1] * (1.0 - auxr) * (1.0 - auxz) + fa[2][1] * auxr * (1.0 - auxz)
             + fa[1][2] * (1.0 - auxr) * auxz + fa[2][2] * auxr * auxz;
+        return true;
     }
     double res = 0.0;
     for (int i = -1; i <= 2; ++i)
@@ -275,7 +290,16 @@ double interp(Sim& S, int gid, const Arr& var, double r0, double z0) {
             }
             res = res + aux * fa[i + 1][j + 1];
         }
-    return res;
+    *out = res;
+    return true;
+}
+
+double interp(Sim& S, int gid, const Arr& var, double r0, double z0) {
+    Level& L = S.L[gid];
+    double v = 0.0;
+    if (!interp_at(S, gid, L.a("r"), L.a("z"), var, r0, z0, &v))
+        throw std::runtime_error("interp: interpolating point is outside the local grid");
+    return v;
 }
 
 // ---------------------------------------------------------------------------
@@ -294,6 +318,28 @@ void finebound(Sim& S, int gid, double dtw) {
     const int border = (tm1 == 0.0) ? 1 : 2;
     Arr& r = F.a("r"); Arr& z = F.a("z");
     Level& Cl = S.L[pg];
+    const Arr& rc = Cl.a("r");
+    const Arr& zc = Cl.a("z");
+    // every array the strips touch, resolved once (the point loops below run
+    // in parallel and must not touch the name maps)
+    struct VarRefs {
+        Arr* fine; const Arr* coarse; const Arr* vp;
+        const std::vector<double>* h[4];  // rR, rL, zR, zL
+    };
+    std::vector<VarRefs> vars;
+    for (const EvolvedVar& e : S.evolved) {
+        VarRefs x{};
+        x.fine = &F.a(e.name);
+        x.coarse = &Cl.a(e.name);
+        x.vp = &F.a(e.name + "_p");
+        const char* sfx[4] = {"_rR", "_rL", "_zR", "_zL"};
+        for (int k = 0; k < 4; ++k) {
+            auto it = F.hist.find(e.name + sfx[k]);
+            x.h[k] = it == F.hist.end() ? nullptr : &it->second;
+        }
+        vars.push_back(x);
+    }
+    int outside = 0;
 
     // one strip point: all evolving variables (bound_interp.inc); bd is the
     // strip: 'R' (rR), 'L' (rL), 'z' (zR), 'l' (zL)
@@ -301,12 +347,17 @@ void finebound(Sim& S, int gid, double dtw) {
         const int ii = (int)nint_((r0 - r(1 - g, 0)) / S.drl[level]) + 1 - g;
         const int jj = (int)nint_((z0 - z(0, 1 - g)) / S.dzl[level]) + 1 - g;
         const bool flag1 = (ii >= 1 - g) && (ii <= F.Nr) && (jj >= 1 - g) && (jj <= F.Nz);
-        for (const EvolvedVar& e : S.evolved) {
-            const double aux2 = interp(S, pg, Cl.a(e.name), r0, z0);
+        for (const VarRefs& x : vars) {
+            double aux2 = 0.0;
+            if (!interp_at(S, pg, rc, zc, *x.coarse, r0, z0, &aux2)) {
+#pragma omp atomic write
+                outside = 1;
+                return;
+            }
             if (!flag1) continue;
-            Arr& v = F.a(e.name);
+            Arr& v = *x.fine;
             if (border == 1) {
-                v(ii, jj) = (tl - t0) / (tp - t0) * aux2 + (tl - tp) / (t0 - tp) * F.a(e.name + "_p")(ii, jj);
+                v(ii, jj) = (tl - t0) / (tp - t0) * aux2 + (tl - tp) / (t0 - tp) * (*x.vp)(ii, jj);
             } else {
                 // history terms; an index beyond the declared history depth
                 // (m or n > ghost-1, reachable only when tp == tl) carries a
@@ -314,12 +365,12 @@ void finebound(Sim& S, int gid, double dtw) {
                 double h0 = 0.0, h1 = 0.0;
                 if (bd == 'R' || bd == 'L') {
                     if (m <= g - 1) {
-                        const auto& H = F.hist[e.name + (bd == 'R' ? "_rR" : "_rL")];
+                        const auto& H = *x.h[bd == 'R' ? 0 : 1];
                         h0 = H[hr(F, m, jj, 0)]; h1 = H[hr(F, m, jj, 1)];
                     }
                 } else {
                     if (n <= g - 1) {
-                        const auto& H = F.hist[e.name + (bd == 'z' ? "_zR" : "_zL")];
+                        const auto& H = *x.h[bd == 'z' ? 2 : 3];
                         h0 = H[hz(F, ii, n, 0)]; h1 = H[hz(F, ii, n, 1)];
                     }
                 }
@@ -329,37 +380,46 @@ void finebound(Sim& S, int gid, double dtw) {
             }
         }
     };
+    // The strips are written in the reference's order (a later strip wins at
+    // the corners they share); within a strip every point is its own.
     // upper r boundary (finebound.f90:153-187)
-    for (int m = 0; m <= imax; ++m)
-        for (int n = 0; n <= F.Nz + g - 1; ++n) {
+#pragma omp parallel for schedule(static)
+    for (int n = 0; n <= F.Nz + g - 1; ++n)
+        for (int m = 0; m <= imax; ++m) {
             const double r0 = S.rmaxl[gid] - (double)m * S.drl[level];
             const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
             point(r0, z0, m, n, 'R');
         }
     // lower r boundary of a box off the axis (finebound.f90:246-285)
-    if (F.box > 0 && S.rbox[F.box] != 0.0)
-        for (int m = 0; m <= imax; ++m)
-            for (int n = 0; n <= F.Nz + g - 1; ++n) {
+    if (F.box > 0 && S.rbox[F.box] != 0.0) {
+#pragma omp parallel for schedule(static)
+        for (int n = 0; n <= F.Nz + g - 1; ++n)
+            for (int m = 0; m <= imax; ++m) {
                 const double r0 = S.rminl[gid] + (double)m * S.drl[level];
                 const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
                 point(r0, z0, m, n, 'L');
             }
+    }
     // upper z boundary (finebound.f90:296-316)
-    for (int n = 0; n <= jmax; ++n)
-        for (int m = 0; m <= F.Nr + g - 1; ++m) {
+#pragma omp parallel for schedule(static)
+    for (int m = 0; m <= F.Nr + g - 1; ++m)
+        for (int n = 0; n <= jmax; ++n) {
             const double r0 = S.rminl[gid] + (double)m * S.drl[level];
             const double z0 = S.zmaxl[gid] - (double)n * S.dzl[level];
             point(r0, z0, m, n, 'z');
         }
     // lower z boundary without equatorial symmetry or off the equator
     // (finebound.f90:351-397)
-    if (!S.P.eqsym || (F.box > 0 && S.zbox[F.box] != 0.0))
-        for (int n = 0; n <= jmax; ++n)
-            for (int m = 0; m <= F.Nr + g - 1; ++m) {
+    if (!S.P.eqsym || (F.box > 0 && S.zbox[F.box] != 0.0)) {
+#pragma omp parallel for schedule(static)
+        for (int m = 0; m <= F.Nr + g - 1; ++m)
+            for (int n = 0; n <= jmax; ++n) {
                 const double r0 = S.rminl[gid] + (double)m * S.drl[level];
                 const double z0 = S.zminl[gid] + (double)n * S.dzl[level];
                 point(r0, z0, m, n, 'l');
             }
+    }
+    if (outside) throw std::runtime_error("interp: interpolating point is outside the local grid");
 }
 
 // restrict.f90:2-169 with restrict_interp.inc: grid ``gid`` into its parent
@@ -372,6 +432,13 @@ void restrict_(Sim& S, int gid) {
     const double deltar = (double)(2 * g) * S.drl[level] + 1.0e-10;
     const double deltaz = (double)(2 * g) * S.dzl[level] + 1.0e-10;
     Arr& rc = Cl.a("r"); Arr& zc = Cl.a("z");
+    const Arr& rf = F.a("r");
+    const Arr& zf = F.a("z");
+    std::vector<std::pair<const Arr*, Arr*>> vars;
+    for (const EvolvedVar& e : S.evolved) vars.emplace_back(&F.a(e.name), &Cl.a(e.name));
+    int outside = 0;
+    // every coarse point is written at most once: the rows run in parallel
+#pragma omp parallel for schedule(dynamic, 4)
     for (int n = 0; n <= Cl.Nz + g - 1; ++n)
         for (int m = 0; m <= Cl.Nr + g - 1; ++m) {
             const double r0 = S.rminl[pg] + (double)m * S.drl[level - 1];
@@ -384,12 +451,18 @@ void restrict_(Sim& S, int gid) {
                 const int i = (int)nint_((r0 - rc(1 - g, 0)) / S.drl[level - 1]) + 1 - g;
                 const int j = (int)nint_((z0 - zc(0, 1 - g)) / S.dzl[level - 1]) + 1 - g;
                 const bool flag1 = (i >= 1 - g) && (i <= Cl.Nr) && (j >= 1 - g) && (j <= Cl.Nz);
-                for (const EvolvedVar& e : S.evolved) {
-                    const double aux2 = interp(S, gid, F.a(e.name), r0, z0);
-                    if (flag1) Cl.a(e.name)(i, j) = aux2;
+                for (const auto& fc : vars) {
+                    double aux2 = 0.0;
+                    if (!interp_at(S, gid, rf, zf, *fc.first, r0, z0, &aux2)) {
+#pragma omp atomic write
+                        outside = 1;
+                        break;
+                    }
+                    if (flag1) (*fc.second)(i, j) = aux2;
                 }
             }
         }
+    if (outside) throw std::runtime_error("interp: interpolating point is outside the local grid");
 }
 
 // syncboxes.f90:2-243 with the generated intersect_interp.inc: grid ``p``

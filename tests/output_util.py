@@ -1,0 +1,31 @@
+"""The reference's 0-D records computed straight from a golden fixture's
+grid functions (outputs of the reference's own Fortran): the statistics of
+save0Dvariable (src/base/save0Ddata.f90:221-288) restated with NumPy, and the
+value at the origin by the 4x4 Lagrange interpolation of interp.f90, whose
+weights at the origin (half a cell from the axis and the equator on every
+box-0 level) are (-1, 9, 9, -1)/16 on i, j = -1..2."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+OUT_NAMES = ("alpha", "phi", "trK", "ham")
+
+
+def load_fixture(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    cfg = {k: v for k, v in meta.items() if k not in ("steps", "fields", "grids")}
+    cfg["eqsym"] = 1 if cfg.get("eqsym") else 0
+    return d, meta, cfg
+
+
+def fixture_stats(a, g=3):
+    """(max, min, max|f|, RMS, origin) of a[i+g-1, j+g-1] over i = 1..Nr-g,
+    j = 1..Nz-g."""
+    inner = a[g:-g, g:-g]
+    w = np.array([-1.0, 9.0, 9.0, -1.0]) / 16.0
+    origin = float(w @ a[g - 2:g + 2, g - 2:g + 2] @ w)
+    return (float(inner.max()), float(inner.min()), float(np.abs(inner).max()),
+            float(np.sqrt(np.mean(inner ** 2))), origin)

@@ -1,0 +1,151 @@
+"""Output and restart compatibility of the GPU path (C ABI).
+
+* 0-D records (src/base/save0Ddata.f90:297-403): the ``(2ES20.8E3)`` lines
+  written from ollin_gpu_norms of the evolved state equal, character for
+  character, the lines computed from the reference-executed fixture c1_small.
+* Restart (src/base/checkpoint.f90): every evolved field's three time levels
+  (current state and the two step starts that hold the boundary history of
+  :253-300) and the clocks t, t1, t2, s are downloaded after some coarse
+  steps and uploaded into a new handle.  ollin_gpu_resume continues the
+  evolution bit for bit; ollin_gpu_initialize runs the reference's
+  post-restart sequence instead (``auxiliary`` re-projects the metric, and
+  with the Gamma-driver shift dtbeta = drivercsi Delta, evolve.f90:174-195),
+  which stays within rounding of the uninterrupted evolution."""
+import numpy as np
+import pytest
+
+from ollin.output import Save0D, header, lines
+from output_util import OUT_NAMES, fixture_stats, load_fixture
+from parity_util import C1, params
+
+pytestmark = pytest.mark.gpu
+
+EVOLVED = ["alpha", "chi", "phi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTC", "Delta_r", "Delta_z"]
+SHIFT = ["beta_r", "beta_z", "dtbeta_r", "dtbeta_z"]
+
+
+def test_gpu_records_match_reference_fixture(tmp_path):
+    from ollin.gpu import Evolution
+    d, meta, cfg = load_fixture("c1_small")
+    e = Evolution(params(cfg))
+    e.initial_data()
+    e.initialize()
+    writer = Save0D(str(tmp_path), OUT_NAMES)
+    expect = {}
+    done = 0
+    for target in meta["steps"]:
+        while done < target:
+            e.step()
+            done += 1
+        if all(("s%d_L%d_ham" % (done, lev)) in d for lev in e.levels()):
+            writer.write(e)
+        for lev in e.levels():
+            t = float(d["s%d_L%d_time" % (done, lev)])
+            assert e.clocks(lev)[0] == t
+            for nm in OUT_NAMES:
+                key = "s%d_L%d_%s" % (done, lev, nm)
+                if key not in d:  # constraints are stored at the first and last snapshot
+                    continue
+                ref = lines(t, fixture_stats(d[key]))
+                assert lines(t, e.norms(lev, nm)) == ref, (done, lev, nm)
+                for kind, rec in ref.items():
+                    expect.setdefault((nm, lev, kind), []).append(rec)
+    for (nm, lev, kind), recs in expect.items():
+        text = (tmp_path / ("%s_b0l%d_%s.tl" % (nm, lev, kind))).read_text().splitlines()
+        assert text == [header(nm, kind)] + recs
+    e.close()
+
+
+def _restart_copy(src, cfg, names, resume):
+    from ollin.gpu import Evolution
+    dst = Evolution(params(cfg))
+    for lev in src.levels():
+        for nm in names:
+            for which in (0, 1, 2):
+                dst.upload_slot(lev, nm, which, src.download_slot(lev, nm, which))
+        dst.set_clocks(lev, src.clocks(lev))
+    if resume:
+        dst.resume()
+    else:
+        dst.initialize()
+    return dst
+
+
+def _worst(a, b, names, tag, exact):
+    worst = 0.0
+    for lev in a.levels():
+        assert np.array_equal(a.clocks(lev), b.clocks(lev)), (tag, lev)
+        for nm in names:
+            for which in (0, 1, 2):
+                x, y = a.download_slot(lev, nm, which), b.download_slot(lev, nm, which)
+                if exact:
+                    assert np.array_equal(x, y), "%s level %d %s slot %d: max diff %.3e" % (
+                        tag, lev, nm, which, float(np.abs(x - y).max()))
+                else:
+                    worst = max(worst, float(np.abs(x - y).max()) / max(float(np.abs(x).max()), 1e-300))
+    return worst
+
+
+def _run(shift):
+    from ollin.gpu import Evolution
+    cfg = dict(C1, nrtotal=48, nztotal=48)
+    names = list(EVOLVED)
+    if shift:
+        cfg.update(shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
+        names += SHIFT
+    x = Evolution(params(cfg))
+    x.initial_data()
+    x.initialize()
+    for _ in range(5):
+        x.step()
+    return x, cfg, names
+
+
+@pytest.mark.parametrize("shift", [False, True], ids=["puncture", "puncture_gammadriver2"])
+def test_resume_continues_bit_for_bit(shift):
+    """ollin_gpu_resume: the suspended evolution's three time levels and
+    clocks in a new handle continue bit for bit, shift included."""
+    x, cfg, names = _run(shift)
+    y = _restart_copy(x, cfg, names, resume=True)
+    _worst(x, y, names, "after resume", exact=True)
+    for _ in range(7):
+        assert x.step() == y.step()
+    _worst(x, y, names, "7 coarse steps after resume", exact=True)
+    for lev in x.levels():
+        assert np.array_equal(x.norms(lev, "ham"), y.norms(lev, "ham"))
+    x.close()
+    y.close()
+
+
+@pytest.mark.parametrize("shift", [False, True], ids=["puncture", "puncture_gammadriver2"])
+def test_restart_follows_the_reference(shift):
+    """A reference-style restart (ollin_gpu_initialize after the upload):
+    ``auxiliary`` projects A, B, C, H onto unit determinant once more, which
+    moves them by an ulp, and with the Gamma driver dtbeta is reset to
+    drivercsi Delta (evolve.f90:174-195), as in the reference.  With dtbeta
+    uploaded again the restarted evolution stays within 1e-12 (normwise) of
+    the uninterrupted one over the next 7 coarse steps."""
+    x, cfg, names = _run(shift)
+    y = _restart_copy(x, cfg, names, resume=False)
+    if shift:
+        for lev in x.levels():
+            for db, dl in (("dtbeta_r", "Delta_r"), ("dtbeta_z", "Delta_z")):
+                assert np.array_equal(y.download_slot(lev, db, 0), 0.75 * y.download_slot(lev, dl, 0))
+            for db in ("dtbeta_r", "dtbeta_z"):
+                y.upload_slot(lev, db, 0, x.download_slot(lev, db, 0))
+    for _ in range(7):
+        assert x.step() == y.step()
+    w = _worst(x, y, names, "7 coarse steps after restart", exact=False)
+    assert w <= 1e-12, w
+    x.close()
+    y.close()
+
+
+def test_clocks_only_before_initialize():
+    from ollin.gpu import Evolution, OllinError
+    e = Evolution(params(dict(C1, nl0=0)))
+    e.initial_data()
+    e.initialize()
+    with pytest.raises(OllinError):
+        e.set_clocks(0, [1.0, 0.5, 0.0, 2.0])
+    e.close()
