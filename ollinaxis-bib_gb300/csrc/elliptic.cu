@@ -610,14 +610,6 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
             sq = r * r;
             const double eu = A.e64[o] * U(i, j);
             sc = eu * eu;
-            // the correction is solved for psi du with the flat operator:
-            // for a conformally flat metric psi^5 (physical Laplacian)(dv/psi)
-            // = (flat Laplacian - lap(psi)/psi) dv, so the right-hand side is
-            // psi^5 r (mix_diag_phys_kernel, mix_update_kernel)
-            if (A.pa) {
-                const double p4 = A.psi4[o];
-                r = r * (p4 * sqrt(sqrt(p4)));
-            }
         } else if (A.robin) {
             const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
             double R;
@@ -653,50 +645,7 @@ __global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_co
     const int lim_r = A.robin ? G.nr : G.nr - 1, lim_z = A.robin ? G.nz : G.nz - 1;
     if (i > lim_r || j > lim_z) return;  // Dirichlet rows keep their data
     const size_t o = (size_t)i + (size_t)j * G.ld;
-    const double dv = A.d64 ? A.d64[o] : (double)A.d[o];
-    if (A.psi4) A.u[o] = A.u[o] + dv / sqrt(sqrt(A.psi4[o]));  // du = dv/psi
-    else A.u[o] = A.u[o] + dv;
-}
-
-// diagonal of the flat correction operator for the physical Laplacian in
-// dv = psi du: the flat stencil's centre plus psi^4 S1 - lap(psi)/psi, with
-// the flat second-order Laplacian (axis term included) of psi; points on the
-// outer edges keep the flat centre plus psi^4 S1
-template <typename T>
-__global__ void mix_diag_phys_kernel(LevelGeom G, T* e32, double ec, const double* S1, const double* psi4) {
-    const int g = G.g;
-    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    if (i > G.nr || j > G.nz) return;
-    const long ld = G.ld;
-    const size_t o = (size_t)i + (size_t)j * ld;
-    double e = ec + S1[o] * psi4[o];
-    if (i >= 2 - g && i <= G.nr - 1 && j >= 2 - g && j <= G.nz - 1) {
-        auto P = [&](int di, int dj) { return sqrt(sqrt(psi4[o + di + (long)dj * ld])); };
-        const double p0 = P(0, 0);
-        const double lap = (P(1, 0) - 2.0 * p0 + P(-1, 0)) / (G.dr * G.dr) + (P(0, 1) - 2.0 * p0 + P(0, -1)) / (G.dz * G.dz)
-                           + (P(1, 0) - P(-1, 0)) / (2.0 * G.dr) * G.ircol[i];
-        e = e - lap / p0;
-    }
-    e32[o] = (T)e;
-}
-
-__global__ void copy64_kernel(LevelGeom G, double* out, const double* in) {
-    const int g = G.g;
-    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    if (i > G.nr || j > G.nz) return;
-    const size_t o = (size_t)i + (size_t)j * G.ld;
-    out[o] = in[o];
-}
-
-__global__ void to_float_kernel(LevelGeom G, float* out, const double* in) {
-    const int g = G.g;
-    const int i = 1 - g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 - g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    if (i > G.nr || j > G.nz) return;
-    const size_t o = (size_t)i + (size_t)j * G.ld;
-    out[o] = (float)in[o];
+    A.u[o] = A.u[o] + (A.d64 ? A.d64[o] : (double)A.d[o]);
 }
 
 }  // namespace
@@ -716,32 +665,6 @@ void launch_mix_update(const MixArgs& a, cudaStream_t s) {
     dim3 blk(32, 4);
     dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz + blk.y - 1) / blk.y);
     mix_update_kernel<<<grd, blk, 0, s>>>(a);
-}
-
-void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const double* S1, const double* psi4,
-                          cudaStream_t s) {
-    dim3 blk(32, 4);
-    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
-    mix_diag_phys_kernel<float><<<grd, blk, 0, s>>>(G, e32, ec, S1, psi4);
-}
-
-void launch_mix_diag_phys64(const LevelGeom& G, double* e, double ec, const double* S1, const double* psi4,
-                            cudaStream_t s) {
-    dim3 blk(32, 4);
-    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
-    mix_diag_phys_kernel<double><<<grd, blk, 0, s>>>(G, e, ec, S1, psi4);
-}
-
-void launch_copy64(const LevelGeom& G, double* out, const double* in, cudaStream_t s) {
-    dim3 blk(32, 4);
-    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
-    copy64_kernel<<<grd, blk, 0, s>>>(G, out, in);
-}
-
-void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s) {
-    dim3 blk(32, 4);
-    dim3 grd((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
-    to_float_kernel<<<grd, blk, 0, s>>>(G, out, in);
 }
 
 void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const double* S5, const double* u,

@@ -1594,10 +1594,8 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     double* f64 = fp64 ? (double*)cbuf : nullptr;
     float* d = fp64 ? nullptr : f32 + off;
     float* r32 = fp64 ? nullptr : f32 + L.n + off;
-    float* e32 = fp64 ? nullptr : f32 + 2 * L.n + off;
     double* d64 = fp64 ? f64 + off : nullptr;
     double* r64 = fp64 ? f64 + L.n + off : nullptr;
-    double* e64c = fp64 ? f64 + 2 * L.n + off : nullptr;
     const double ec = -2.0 * (1.0 / (L.dr * L.dr) + 1.0 / (L.dz * L.dz));
     double* eaux = w.ua;
     double* e = w.va;
@@ -1642,7 +1640,6 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         if (rc) return rc;
         a.pa = q[0]; a.pb = q[1]; a.pc = q[2]; a.pd = q[3]; a.e64 = q[4];
         a.pg = q[5]; a.ph = q[6]; a.pi = q[7]; a.pj = q[8];
-        a.psi4 = w.ph.psi4;
     }
     a.f64 = base_ptr(L, w.S0);
     a.ca = dcol + (g - 1);
@@ -1655,6 +1652,14 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     a.robin = robin ? 1 : 0;
     a.uinf = 1.0;
     a.partial = S.partial;
+    // the five-point part of the level's stencil, which the multigrid
+    // coarsens (the variable coefficients of the physical Laplacian included)
+    MgStencil ms{};
+    ms.pa = a.pa; ms.pb = a.pb; ms.pc = a.pc; ms.pd = a.pd;
+    ms.ca = a.ca; ms.cb = a.cb; ms.cc = a.cc;
+    ms.e = a.e64;
+    ms.ld = L.ld;
+    ms.dr = L.dr; ms.dz = L.dz;
     std::vector<double> hp(2 * nparts);
     int outer = 0, cycles = 0, ncyc = 2, flat = 0;
     double rms = 0.0, last = 0.0;
@@ -1665,15 +1670,6 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
             rc = after_launch(h);
             if (rc) return rc;
         }
-        if (S.physical) {
-            if (fp64) launch_mix_diag_phys64(L.G, e64c, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
-            else launch_mix_diag_phys(L.G, e32, ec, base_ptr(L, w.S1), w.ph.psi4, h->stream);
-        } else {
-            if (fp64) launch_copy64(L.G, e64c, a.e64, h->stream);
-            else launch_to_float(L.G, e32, a.e64, h->stream);
-        }
-        rc = after_launch(h);
-        if (rc) return rc;
         launch_mix_resid(a, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
@@ -1693,13 +1689,13 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         }
         last = rms;
         ++outer;
-        if (fp64) {
-            mg_load(mg, r64, e64c, L.ld, h->stream);
-            mg_solve(mg, a.robin, ncyc, d64, L.ld, h->stream);
-        } else {
-            mg_load(mg, r32, e32, L.ld, h->stream);
-            mg_solve(mg, a.robin, ncyc, d, L.ld, h->stream);
+        // the operator once, or every refinement when S5 u^4 enters the diagonal
+        if (outer == 1 || s5) {
+            mg_load_operator(mg, ms, h->stream);
+            h->launches += mg_levels(mg);
         }
+        mg_set_rhs(mg, fp64 ? (const void*)r64 : (const void*)r32, L.ld, h->stream);
+        mg_solve(mg, a.robin, ncyc, fp64 ? (void*)d64 : (void*)d, L.ld, h->stream);
         h->launches += 2 + (long long)ncyc * mg_launches_per_cycle(mg, a.robin);
         CUDA_OR_FAIL(cudaGetLastError());
         cycles += ncyc;

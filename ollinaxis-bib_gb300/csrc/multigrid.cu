@@ -4,20 +4,26 @@
 // FP64 gives the all-FP64 solve of that system that the mixed solve's error is
 // measured against.
 //
-// Grid k of the hierarchy has n x m cells, cell centres r_I = (I-1/2) Hr,
-// z_J = (J-1/2) Hz, Hr = 2^k dr.  Its equations are those of the level
-// itself re-discretised with spacing H:
-//   interior I <= n-1, J <= m-1:
-//     a_I d(I+1,J) + b_I d(I-1,J) + cz (d(I,J+1) + d(I,J-1)) + e_IJ d = r
-//     with d(0,J) = d(1,J), d(I,0) = d(I,1) (axis and equator mirrors)
-//   Robin rows I = n / J = m (coarse problem), zero rows otherwise (the
-//   Dirichlet problems of the finer refinement levels).
-// Cell (I,J) of grid k+1 covers cells 2I-1..2I x 2J-1..2J of grid k:
-// restriction averages the four residuals (the two Robin residuals on a
-// boundary row), prolongation is bilinear in the cell centres (9/16, 3/16,
-// 3/16, 1/16).  Smoother: red-black Gauss-Seidel, Robin rows by two-colour
-// Gauss-Seidel along each edge.  Arrays are compact, (n+2) x (m+2) with one
-// ghost layer: element (I,J) at [I + J (n+2)].
+// J is the five-point part of the level's stencil with variable coefficients
+// (the physical Laplacian of maximal slicing has g^rr/psi^4 and g^zz/psi^4
+// varying by orders of magnitude in a strong Brill wave; the flat Laplacian of
+// the initial data is the case krr = kzz = 1, vr = vz = 0):
+//   aE d(I+1,J) + aW d(I-1,J) + aN d(I,J+1) + aS d(I,J-1) + e d(I,J) = r
+//   aE = krr (1/Hr + 1/(2 r_I))/Hr + vr/(2Hr),  aW = krr (1/Hr - 1/(2 r_I))/Hr - vr/(2Hr)
+//   aN = kzz/Hz^2 + vz/(2Hz),                    aS = kzz/Hz^2 - vz/(2Hz)
+//   e  = -2 (krr/Hr^2 + kzz/Hz^2) + s
+// per cell of a grid of n x m cells, cell centres r_I = (I-1/2) Hr,
+// z_J = (J-1/2) Hz, Hr = 2^k dr, with d(0,J) = d(1,J), d(I,0) = d(I,1) (axis
+// and equator mirrors); Robin rows I = n / J = m on the coarse problem, zero
+// rows on the Dirichlet problems of the finer refinement levels.  The nine-
+// point couplings of a metric with g^rz /= 0 are left to the FP64 residual of
+// the outer iteration.
+// Cell (I,J) of grid k+1 covers cells 2I-1..2I x 2J-1..2J of grid k: the
+// coefficient fields and the residual are averaged (the two Robin residuals
+// on a boundary row), prolongation is bilinear in the cell centres (9/16,
+// 3/16, 3/16, 1/16).  Smoother: red-black Gauss-Seidel, Robin rows by
+// two-colour Gauss-Seidel along each edge.  Arrays are compact, (n+2) x (m+2)
+// with one ghost layer: element (I,J) at [I + J (n+2)].
 #include <vector>
 
 #include "ollin_kernels.h"
@@ -29,8 +35,9 @@ namespace {
 template <typename T>
 struct Grid {
     int n, m, ld;
-    T hr, hz;            // spacings
-    T* d; T* r; T* e;
+    T hr, hz;                            // spacings
+    T* d; T* r;                          // correction, right-hand side
+    T* krr; T* kzz; T* vr; T* vz; T* s;  // coefficient fields
 };
 
 __device__ __forceinline__ int mirror(int k) { return k < 1 ? 1 - k : k; }
@@ -38,14 +45,32 @@ __device__ __forceinline__ int mirror(int k) { return k < 1 ? 1 - k : k; }
 template <typename T>
 __device__ __forceinline__ T Dv(const Grid<T>& G, int i, int j) { return G.d[mirror(i) + mirror(j) * G.ld]; }
 
+template <typename T>
+struct Stencil { T e, w, n, s, c; };
+
+template <typename T>
+__device__ __forceinline__ Stencil<T> stencil(const Grid<T>& G, int i, int j) {
+    const int o = i + j * G.ld;
+    const T ri = ((T)i - T(0.5)) * G.hr;
+    const T krr = G.krr[o], kzz = G.kzz[o];
+    const T ihr = T(1.0) / G.hr, ihz = T(1.0) / G.hz;
+    const T ur = T(0.5) * G.vr[o] * ihr, uz = T(0.5) * G.vz[o] * ihz;
+    Stencil<T> q;
+    q.e = krr * (ihr + T(0.5) / ri) * ihr + ur;
+    q.w = krr * (ihr - T(0.5) / ri) * ihr - ur;
+    q.n = kzz * ihz * ihz + uz;
+    q.s = kzz * ihz * ihz - uz;
+    q.c = T(-2.0) * (krr * ihr * ihr + kzz * ihz * ihz) + G.s[o];
+    return q;
+}
+
 // residual of one interior equation
 template <typename T>
 __device__ __forceinline__ T interior_res(const Grid<T>& G, int i, int j) {
-    const T ri = ((T)i - T(0.5)) * G.hr;
-    const T a = (T(1.0) / G.hr + T(0.5) / ri) / G.hr, b = (T(1.0) / G.hr - T(0.5) / ri) / G.hr;
-    const T cz = T(1.0) / (G.hz * G.hz);
+    const Stencil<T> q = stencil(G, i, j);
     const int o = i + j * G.ld;
-    return G.r[o] - (a * Dv(G, i + 1, j) + b * Dv(G, i - 1, j) + cz * (Dv(G, i, j + 1) + Dv(G, i, j - 1)) + G.e[o] * G.d[o]);
+    return G.r[o] - (q.e * Dv(G, i + 1, j) + q.w * Dv(G, i - 1, j) + q.n * Dv(G, i, j + 1) + q.s * Dv(G, i, j - 1)
+                     + q.c * G.d[o]);
 }
 
 // residual of a Robin row (coarse problem); cr = r_n/Hr = n - 1/2, cz = J - 1/2
@@ -69,6 +94,19 @@ __device__ __forceinline__ T robin_res(const Grid<T>& G, int i, int j) {
     return G.r[i + j * G.ld] - lhs;
 }
 
+// Gauss-Seidel update of one interior cell (the mirrored neighbours across
+// the axis and the equator fold into the diagonal)
+template <typename T>
+__device__ __forceinline__ void relax(const Grid<T>& G, int i, int j) {
+    const Stencil<T> q = stencil(G, i, j);
+    const int o = i + j * G.ld;
+    T diag = q.c;
+    T off = q.e * G.d[o + 1] + q.n * G.d[o + G.ld];
+    if (i > 1) off += q.w * G.d[o - 1]; else diag += q.w;
+    if (j > 1) off += q.s * G.d[o - G.ld]; else diag += q.s;
+    G.d[o] = (G.r[o] - off) / diag;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) mg_smooth_kernel(Grid<T> G, int parity) {
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -77,20 +115,13 @@ __global__ void __launch_bounds__(128) mg_smooth_kernel(Grid<T> G, int parity) {
     if (((i + j) & 1) != parity) ++j;
     j += 2 * jh;
     if (i > G.n - 1 || j > G.m - 1) return;
-    const T ri = ((T)i - T(0.5)) * G.hr;
-    const T a = (T(1.0) / G.hr + T(0.5) / ri) / G.hr, b = (T(1.0) / G.hr - T(0.5) / ri) / G.hr;
-    const T cz = T(1.0) / (G.hz * G.hz);
-    const int o = i + j * G.ld;
-    T diag = G.e[o];
-    T off = a * G.d[o + 1] + cz * G.d[o + G.ld];
-    if (i > 1) off += b * G.d[o - 1]; else diag += b;
-    if (j > 1) off += cz * G.d[o - G.ld]; else diag += cz;
-    G.d[o] = (G.r[o] - off) / diag;
+    relax(G, i, j);
 }
 
-// Robin rows: two-colour Gauss-Seidel along each edge, then the corner
+// Robin rows, two-colour Gauss-Seidel along each edge, then the corner
+// (called by every thread of one block)
 template <typename T>
-__global__ void __launch_bounds__(1024) mg_edges_kernel(Grid<T> G) {
+__device__ void robin_sweep(const Grid<T>& G) {
     const int n = G.n, m = G.m;
     const T cr = (T)n - T(0.5), czn = (T)m - T(0.5);
     auto D = [&](int i, int j) -> T& { return G.d[mirror(i) + mirror(j) * G.ld]; };
@@ -110,51 +141,27 @@ __global__ void __launch_bounds__(1024) mg_edges_kernel(Grid<T> G) {
     if (threadIdx.x == 0)
         D(n, m) = (G.r[n + m * G.ld] + T(0.5) * cr * (T(4.0) * D(n - 1, m) - D(n - 2, m)) + T(0.5) * czn * (T(4.0) * D(n, m - 1) - D(n, m - 2)))
                   / (T(1.0) + T(1.5) * (cr + czn));
+    __syncthreads();
 }
+
+template <typename T>
+__global__ void __launch_bounds__(1024) mg_edges_kernel(Grid<T> G) { robin_sweep(G); }
 
 // coarsest grid: one block runs all the sweeps
 template <typename T>
 __global__ void __launch_bounds__(1024) mg_coarse_kernel(Grid<T> G, int robin, int sweeps) {
     const int n = G.n, m = G.m;
-    const T cz2 = T(1.0) / (G.hz * G.hz);
-    const T cr = (T)n - T(0.5), czn = (T)m - T(0.5);
-    auto D = [&](int i, int j) -> T& { return G.d[mirror(i) + mirror(j) * G.ld]; };
     const int ncell = (n - 1) * (m - 1);
     for (int sw = 0; sw < sweeps; ++sw) {
         for (int parity = 0; parity < 2; ++parity) {
             for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
                 const int i = 1 + c % (n - 1), j = 1 + c / (n - 1);
                 if (((i + j) & 1) != parity) continue;
-                const T ri = ((T)i - T(0.5)) * G.hr;
-                const T a = (T(1.0) / G.hr + T(0.5) / ri) / G.hr, b = (T(1.0) / G.hr - T(0.5) / ri) / G.hr;
-                const int o = i + j * G.ld;
-                T diag = G.e[o];
-                T off = a * G.d[o + 1] + cz2 * G.d[o + G.ld];
-                if (i > 1) off += b * G.d[o - 1]; else diag += b;
-                if (j > 1) off += cz2 * G.d[o - G.ld]; else diag += cz2;
-                G.d[o] = (G.r[o] - off) / diag;
+                relax(G, i, j);
             }
             __syncthreads();
         }
-        if (robin) {
-            for (int colour = 0; colour < 2; ++colour) {
-                for (int j = 1 + colour + 2 * (int)threadIdx.x; j <= m - 1; j += 2 * blockDim.x) {
-                    const T cz = (T)j - T(0.5);
-                    D(n, j) = (G.r[n + j * G.ld] + T(0.5) * cr * (T(4.0) * D(n - 1, j) - D(n - 2, j)) - T(0.5) * cz * (D(n, j + 1) - D(n, j - 1)))
-                              / (T(1.0) + T(1.5) * cr);
-                }
-                for (int i = 1 + colour + 2 * (int)threadIdx.x; i <= n - 1; i += 2 * blockDim.x) {
-                    const T crr = (T)i - T(0.5);
-                    D(i, m) = (G.r[i + m * G.ld] + T(0.5) * czn * (T(4.0) * D(i, m - 1) - D(i, m - 2)) - T(0.5) * crr * (D(i + 1, m) - D(i - 1, m)))
-                              / (T(1.0) + T(1.5) * czn);
-                }
-                __syncthreads();
-            }
-            if (threadIdx.x == 0)
-                D(n, m) = (G.r[n + m * G.ld] + T(0.5) * cr * (T(4.0) * D(n - 1, m) - D(n - 2, m)) + T(0.5) * czn * (T(4.0) * D(n, m - 1) - D(n, m - 2)))
-                          / (T(1.0) + T(1.5) * (cr + czn));
-            __syncthreads();
-        }
+        if (robin) robin_sweep(G);
     }
 }
 
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(128) mg_restrict_kernel(Grid<T> F, Grid<T> C, 
     T v = T(0.0);
     if (!bI && !bJ) {
         v = T(0.25) * (interior_res(F, 2 * I - 1, 2 * J - 1) + interior_res(F, 2 * I, 2 * J - 1)
-                     + interior_res(F, 2 * I - 1, 2 * J) + interior_res(F, 2 * I, 2 * J));
+                       + interior_res(F, 2 * I - 1, 2 * J) + interior_res(F, 2 * I, 2 * J));
     } else if (robin) {
         if (bI && bJ) v = robin_res(F, F.n, F.m);
         else if (bI) v = T(0.5) * (robin_res(F, F.n, 2 * J - 1) + robin_res(F, F.n, 2 * J));
@@ -197,22 +204,50 @@ __global__ void __launch_bounds__(128) mg_prolong_kernel(Grid<T> F, Grid<T> C, i
     F.d[i + j * F.ld] += v;
 }
 
-// grid-k diagonal from the one below: average of S1 plus the constant part
+// coefficient fields of grid C: averages over the four children in grid F
 template <typename T>
-__global__ void __launch_bounds__(128) mg_diag_kernel(Grid<T> F, Grid<T> C) {
+__global__ void __launch_bounds__(128) mg_coarsen_kernel(Grid<T> F, Grid<T> C) {
     const int I = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int J = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (I > C.n || J > C.m) return;
-    const T ef = -T(2.0) * (T(1.0) / (F.hr * F.hr) + T(1.0) / (F.hz * F.hz));
-    const T ec = -T(2.0) * (T(1.0) / (C.hr * C.hr) + T(1.0) / (C.hz * C.hz));
-    auto s1 = [&](int p, int q) { return F.e[p + q * F.ld] - ef; };
-    const T avg = T(0.25) * (s1(2 * I - 1, 2 * J - 1) + s1(2 * I, 2 * J - 1) + s1(2 * I - 1, 2 * J) + s1(2 * I, 2 * J));
-    C.e[I + J * C.ld] = ec + avg;
+    const int a = (2 * I - 1) + (2 * J - 1) * F.ld, b = a + 1, c = a + F.ld, d = c + 1;
+    const int o = I + J * C.ld;
+    C.krr[o] = T(0.25) * (F.krr[a] + F.krr[b] + F.krr[c] + F.krr[d]);
+    C.kzz[o] = T(0.25) * (F.kzz[a] + F.kzz[b] + F.kzz[c] + F.kzz[d]);
+    C.vr[o] = T(0.25) * (F.vr[a] + F.vr[b] + F.vr[c] + F.vr[d]);
+    C.vz[o] = T(0.25) * (F.vz[a] + F.vz[b] + F.vz[c] + F.vz[d]);
+    C.s[o] = T(0.25) * (F.s[a] + F.s[b] + F.s[c] + F.s[d]);
 }
 
-// grid 0 from the level's arrays (level layout: element (i,j) at [i + j*ld])
+// grid 0 from the level's FP64 five-point stencil (level layout: element
+// (i,j) at [i + j*ld]): krr = (a+b) dr^2/2, vr = (a-b) dr - krr/r,
+// kzz = (c+d) dz^2/2, vz = (c-d) dz, s = e + 2 (krr/dr^2 + kzz/dz^2)
 template <typename T>
-__global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, const T* r, const T* e, long ld) {
+__global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, MgStencil S) {
+    const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.n + 1 || j > G.m + 1) return;
+    const int o = i + j * G.ld;
+    const bool in = i >= 1 && i <= G.n && j >= 1 && j <= G.m;
+    if (!in) {
+        G.krr[o] = T(0.0); G.kzz[o] = T(0.0); G.vr[o] = T(0.0); G.vz[o] = T(0.0); G.s[o] = T(0.0);
+        return;
+    }
+    const size_t q = (size_t)i + (size_t)j * S.ld;
+    const double a = S.pa ? S.pa[q] : S.ca[i], b = S.pb ? S.pb[q] : S.cb[i];
+    const double c = S.pc ? S.pc[q] : S.cc, d = S.pd ? S.pd[q] : S.cc;
+    const double dr = S.dr, dz = S.dz, ri = ((double)i - 0.5) * dr;
+    const double krr = (a + b) * (dr * dr) * 0.5, kzz = (c + d) * (dz * dz) * 0.5;
+    G.krr[o] = (T)krr;
+    G.kzz[o] = (T)kzz;
+    G.vr[o] = (T)((a - b) * dr - krr / ri);
+    G.vz[o] = (T)((c - d) * dz);
+    G.s[o] = (T)(S.e[q] + 2.0 * (krr / (dr * dr) + kzz / (dz * dz)));
+}
+
+// the right-hand side of grid 0 (the hierarchy's precision, level layout); d = 0
+template <typename T>
+__global__ void __launch_bounds__(128) mg_rhs_kernel(Grid<T> G, const T* r, long ld) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.n + 1 || j > G.m + 1) return;
@@ -220,7 +255,6 @@ __global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, const T* r, con
     G.d[o] = T(0.0);
     const bool in = i >= 1 && i <= G.n && j >= 1 && j <= G.m;
     G.r[o] = in ? r[(size_t)i + (size_t)j * ld] : T(0.0);
-    G.e[o] = in ? e[(size_t)i + (size_t)j * ld] : T(0.0);
 }
 
 template <typename T>
@@ -234,11 +268,7 @@ __global__ void __launch_bounds__(128) mg_store_kernel(Grid<T> G, T* d, long ld)
 template <typename T>
 dim3 cells(const Grid<T>& G, dim3 blk) { return dim3((G.n + blk.x - 1) / blk.x, (G.m + blk.y - 1) / blk.y); }
 
-}  // namespace
-
 // ---- host side of the hierarchy ---------------------------------------------
-namespace {
-
 template <typename T>
 struct MgGrids {
     std::vector<Grid<T>> g;
@@ -253,7 +283,7 @@ struct MgGrids {
             G.n = nn; G.m = mm; G.ld = nn + 2;
             G.hr = (T)hr; G.hz = (T)hz;
             g.push_back(G);
-            total += (size_t)3 * (nn + 2) * (mm + 2);
+            total += (size_t)7 * (nn + 2) * (mm + 2);
             if ((nn & 1) || (mm & 1) || nn / 2 < 4 || mm / 2 < 4) break;
             nn /= 2; mm /= 2; hr *= 2.0; hz *= 2.0;
         }
@@ -261,17 +291,24 @@ struct MgGrids {
         T* q = pool;
         for (Grid<T>& G : g) {
             const size_t sz = (size_t)(G.n + 2) * (G.m + 2);
-            G.d = q; q += sz; G.r = q; q += sz; G.e = q; q += sz;
+            G.d = q; q += sz; G.r = q; q += sz;
+            G.krr = q; q += sz; G.kzz = q; q += sz; G.vr = q; q += sz; G.vz = q; q += sz; G.s = q; q += sz;
         }
         cudaMemset(pool, 0, total * sizeof(T));
         return true;
     }
 
-    void load(const T* r, const T* e, long ld, cudaStream_t s) {
+    void load(const MgStencil& S, cudaStream_t s) {
         dim3 blk(32, 4);
         const Grid<T>& G0 = g[0];
-        mg_load_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, r, e, ld);
-        for (size_t k = 1; k < g.size(); ++k) mg_diag_kernel<T><<<cells(g[k], blk), blk, 0, s>>>(g[k - 1], g[k]);
+        mg_load_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, S);
+        for (size_t k = 1; k < g.size(); ++k) mg_coarsen_kernel<T><<<cells(g[k], blk), blk, 0, s>>>(g[k - 1], g[k]);
+    }
+
+    void rhs(const T* r, long ld, cudaStream_t s) {
+        dim3 blk(32, 4);
+        const Grid<T>& G0 = g[0];
+        mg_rhs_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, r, ld);
     }
 
     void smooth(const Grid<T>& G, int robin, int sweeps, cudaStream_t s) {
@@ -335,11 +372,14 @@ void mg_destroy(MgHierarchy* H) {
 
 int mg_levels(const MgHierarchy* H) { return (int)(H->fp64 ? H->d.g.size() : H->f.g.size()); }
 
-// load r, e of the level (the hierarchy's precision, level layout), build the
-// coarse diagonals
-void mg_load(MgHierarchy* H, const void* r, const void* e, long ld, cudaStream_t s) {
-    if (H->fp64) H->d.load((const double*)r, (const double*)e, ld, s);
-    else H->f.load((const float*)r, (const float*)e, ld, s);
+void mg_load_operator(MgHierarchy* H, const MgStencil& S, cudaStream_t s) {
+    if (H->fp64) H->d.load(S, s);
+    else H->f.load(S, s);
+}
+
+void mg_set_rhs(MgHierarchy* H, const void* r, long ld, cudaStream_t s) {
+    if (H->fp64) H->d.rhs((const double*)r, ld, s);
+    else H->f.rhs((const float*)r, ld, s);
 }
 
 int mg_launches_per_cycle(const MgHierarchy* H, int robin) {
@@ -348,7 +388,6 @@ int mg_launches_per_cycle(const MgHierarchy* H, int robin) {
     return (L - 1) * (4 * per_sweep + 2) + 1;
 }
 
-// ncycles V-cycles from d = 0; the correction is stored into d (level layout)
 void mg_solve(MgHierarchy* H, int robin, int ncycles, void* d, long ld, cudaStream_t s) {
     if (H->fp64) H->d.solve(robin, ncycles, (double*)d, ld, s);
     else H->f.solve(robin, ncycles, (float*)d, ld, s);

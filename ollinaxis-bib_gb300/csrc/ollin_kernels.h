@@ -307,31 +307,36 @@ struct MixArgs {
     int robin; double uinf;
     double* partial;                                 // per-block sums of squares
     // physical Laplacian (maximal slicing): the per-point nine-point stencil
-    // of sor_elliptic.f90 (pa..pj; e64 its diagonal) and psi^4, by which the
-    // interior residual is scaled for the flat FP32 correction
+    // of sor_elliptic.f90 (pa..pj; e64 its diagonal)
     const double* pa; const double* pb; const double* pc; const double* pd;
     const double* pg; const double* ph; const double* pi; const double* pj;
-    const double* psi4;
 };
-void launch_mix_diag_phys(const LevelGeom& G, float* e32, double ec, const double* S1, const double* psi4,
-                          cudaStream_t s);
-void launch_mix_diag_phys64(const LevelGeom& G, double* e, double ec, const double* S1, const double* psi4,
-                            cudaStream_t s);
+
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
 int mix_blocks(const LevelGeom& G);
 void launch_mix_update(const MixArgs& a, cudaStream_t s);
 
+// The FP64 five-point stencil of a level as the multigrid reads it (level
+// layout, element (i,j) at [i + j*ld]): per-point east/west/north/south
+// coefficients pa..pd, or the flat Laplacian's per-column ca/cb and constant
+// cc when pa is null; the diagonal e.
+struct MgStencil {
+    const double* pa; const double* pb; const double* pc; const double* pd;
+    const double* ca; const double* cb; double cc;
+    const double* e;
+    long ld;
+    double dr, dz;
+};
 // Geometric multigrid for the correction equation (multigrid.cu), FP32 or
-// FP64 (fp64 = 1); r, e and d are arrays of that precision
+// FP64 (fp64 = 1); r and d are arrays of that precision
 struct MgHierarchy;
 MgHierarchy* mg_create(int n, int m, double dr, double dz, int fp64);
 void mg_destroy(MgHierarchy* H);
 int mg_levels(const MgHierarchy* H);
 int mg_launches_per_cycle(const MgHierarchy* H, int robin);
-void mg_load(MgHierarchy* H, const void* r, const void* e, long ld, cudaStream_t s);
+void mg_load_operator(MgHierarchy* H, const MgStencil& S, cudaStream_t s);
+void mg_set_rhs(MgHierarchy* H, const void* r, long ld, cudaStream_t s);
 void mg_solve(MgHierarchy* H, int robin, int ncycles, void* d, long ld, cudaStream_t s);
-void launch_to_float(const LevelGeom& G, float* out, const double* in, cudaStream_t s);
-void launch_copy64(const LevelGeom& G, double* out, const double* in, cudaStream_t s);
 
 void launch_inject(const InjectArgs& a, cudaStream_t s);
 

@@ -185,6 +185,9 @@ def test_precision_pattern_against_fp64_solve(a0):
         e.maximal_slicing()
         e.step()
         e.maximal_slicing()
+        rms = e.ell_stats()[2]
+        print("a0 = %g, %s: maximal-slicing RMS residual %.2e" % (a0, solver, rms))
+        assert rms < 1e-10, (solver, rms)
         alpha = [e.download(lev, "alpha") for lev in e.levels()]
         res[solver] = (chi, alpha)
         e.close()
