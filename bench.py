@@ -473,7 +473,7 @@ def batch_throughput(n=256, steps=1, seed=7):
     R of the large single instance; plain run i at rate r_i leaves the rest
     of the device idle, so batched/plain <= sum(t_i) / (sum(pu_i) / R)."""
     import numpy as np
-    from ollin.gpu import Evolution, step_many
+    from ollin.gpu import Evolution, step_fused, step_many
     from ollin.params import params_from_dict
     cfgs = c4_configs(n, seed)
 
@@ -507,21 +507,39 @@ def batch_throughput(n=256, steps=1, seed=7):
     t_bat = time.perf_counter() - t
     pu_bat = sum(e.point_updates() for e in es) - p0
     same = all(np.array_equal(a, e.norms(0, "trK")) for a, e in zip(digest_plain, es))
+    # the same evolutions' next steps with every kernel fused over all of them
+    step_fused(es)  # warm-up: the fused launch tables
+    p0 = sum(e.point_updates() for e in es)
+    t = time.perf_counter()
+    for _ in range(steps):
+        step_fused(es)
+    t_fused = time.perf_counter() - t
+    pu_fused = sum(e.point_updates() for e in es) - p0
     for e in es:
         e.close()
     t_plain = np.array(t_plain)
     pu = float(sum(pu_plain))
     rate_plain = np.array(pu_plain) / t_plain
+    # the FP64 ceiling of this physics (no shift, scalar field): the rate of
+    # the mix's largest evolutions stepped alone, which fill the device
+    ceiling = float(np.max(rate_plain))
+    bound = float(t_plain.sum()) / (pu / ceiling)
     return {"workload": "%d massless scalar shells (a log-uniform in [0.01, 0.1], seeded), 64^2-512^2 per level x 2-5 "
                         "levels, elliptic data by the mixed solver; t_end cut to %d coarse step(s) per run"
                         % (n, steps),
             "plain_runs_per_s": n / float(t_plain.sum()), "batched_runs_per_s": n / t_bat,
             "speedup": float(t_plain.sum()) / t_bat,
             "plain_point_updates_per_s": pu / float(t_plain.sum()), "batched_point_updates_per_s": pu_bat / t_bat,
+            "fused_point_updates_per_s": pu_fused / t_fused,
+            "fused_speedup": float(t_plain.sum()) / t_fused * (pu_fused / pu),
+            "fused_runs_per_s": n / t_fused * (pu_fused / pu),
             "plain_run_seconds_p50": float(np.percentile(t_plain, 50)),
             "plain_run_seconds_p99": float(np.percentile(t_plain, 99)),
             "plain_rate_p50": float(np.percentile(rate_plain, 50)),
             "setup_seconds_per_run": t_setup / n,
+            "ceiling_point_updates_per_s": ceiling,
+            "ceiling_note": "the fastest plain run of the mix (a large evolution alone fills the device)",
+            "speedup_bound_from_plain_occupancy": bound,
             "identical_results": bool(same)}
 
 
@@ -558,38 +576,49 @@ def plain_small():
 
 
 def serving_requests(rng, n):
-    """A seeded mix of the request types of the serving workload: Schwarzschild
-    punctures (3 levels), massless scalar shells (2-3 levels, mixed-precision
-    elliptic data) and Brill waves (A = 1, 2 levels, mixed-precision elliptic
-    data), 64^2 to 128^2 per level, each with its end time."""
+    """A seeded mix of the serving configuration's request types: Schwarzschild
+    punctures (the plain-method configuration's physics), Brill waves
+    (A in {1, 4, 5}) and massless scalar shells (a log-uniform in
+    [0.01, 0.1]), both with elliptic data by the mixed solver; grids of 64^2
+    to 1024^2 per level with 2-6 levels; t_end uniform in [5, 40]."""
     import numpy as np
     common = dict(eqsym=1, order="four", integrator="rk4", dtfac=0.25, boundtype="radiative", slicing="1+log",
                   gauge_f=2.0, geodiss=0.02, ell_solver="mixed", ell_epsilon=1e-12)
     out = []
     for _ in range(n):
         kind = int(rng.integers(0, 3))
-        size = int(rng.choice([64, 96, 128]))
+        size = int(rng.choice([64, 128, 256, 512, 1024]))
+        nl0 = int(rng.integers(1, 6))
+        t_end = float(rng.uniform(5.0, 40.0))
         if kind == 0:
-            cfg = dict(common, nrtotal=size, nztotal=size, nl0=2, dr0=12.8 / size, dz0=12.8 / size,
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=nl0, dr0=12.8 / size, dz0=12.8 / size,
                        idata="schwarzschild", bh1mass=1.0, ilapse="psiminus2")
-            t_end = float(rng.uniform(1.0, 3.0))
         elif kind == 1:
-            cfg = dict(common, nrtotal=size, nztotal=size, nl0=int(rng.integers(1, 3)), dr0=16.0 / size,
-                       dz0=16.0 / size, idata="scalarpulse", mattertype="scalar", scalarpotential="none",
-                       scalarpulse_type="shell", scalar_a0=float(np.exp(rng.uniform(np.log(0.01), np.log(0.1)))),
-                       scalar_r0=5.0, scalar_sr0=1.0, scalar_sz0=1.0, ilapse="one", scalardiss=0.02)
-            t_end = float(rng.uniform(2.0, 6.0))
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=nl0, dr0=40.96 / size, dz0=40.96 / size,
+                       idata="BrillWave", brill_a0=float(rng.choice([1.0, 4.0, 5.0])), brill_sr0=1.0, brill_sz0=1.0,
+                       ilapse="one")
         else:
-            cfg = dict(common, nrtotal=size, nztotal=size, nl0=1, dr0=8.0 / size, dz0=8.0 / size,
-                       idata="BrillWave", brill_a0=1.0, ilapse="one")
-            t_end = float(rng.uniform(1.0, 3.0))
+            cfg = dict(common, nrtotal=size, nztotal=size, nl0=nl0, dr0=16.0 / size, dz0=16.0 / size,
+                       idata="scalarpulse", mattertype="scalar", scalarpotential="none", scalarpulse_type="shell",
+                       scalar_a0=float(np.exp(rng.uniform(np.log(0.01), np.log(0.1)))), scalar_r0=5.0,
+                       scalar_sr0=1.0, scalar_sz0=1.0, ilapse="one", scalardiss=0.02)
         out.append((kind, cfg, t_end))
     return out
 
 
-def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
-    """The serving pattern through the request loop (ollin_server_*), coarse
-    steps launched as captured graphs unless stated:
+def request_point_updates(cfg, t_end):
+    """Point-updates of a request evolved to t_end (RK4 steps of every level)."""
+    import numpy as np
+    dt0 = cfg["dtfac"] * min(cfg["dr0"], cfg["dz0"])
+    steps = max(1, int(np.ceil(t_end / dt0 - 1e-9)))
+    return steps * cfg["nrtotal"] * cfg["nztotal"] * (2 ** (cfg["nl0"] + 1) - 1)
+
+
+def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
+    """The serving pattern through the request loop (ollin_server_*) on the
+    serving configuration's mix, coarse steps launched as captured graphs
+    unless stated.  Every t_end is multiplied by one factor chosen so that the
+    mix totals ``work`` point-updates (stated in the result):
       * plain: the requests one at a time (max_active = 1), all queued at 0;
       * batched: the same requests with up to 64 running together (and again
         with direct launches);
@@ -597,12 +626,18 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
         bisection chain on the shell amplitude whose next request is submitted
         when the previous one finishes (collapse = smallest lapse < 0.05).
     Latency is finish minus submission, host wall clock.  Every request's
-    norms must agree between the plain and the served runs."""
+    norms must agree between the plain and the served runs.  The bound on
+    batched/plain is the plain runs' step time over the time the fastest
+    request's rate (a large grid alone fills the device) needs for their
+    point-updates."""
     import numpy as np
     from ollin.gpu import Server
     from ollin.params import params_from_dict
     rng = np.random.default_rng(seed)
-    reqs = serving_requests(rng, n)
+    raw = serving_requests(rng, n)
+    full = sum(request_point_updates(c, t) for _, c, t in raw)
+    scale = work / full
+    reqs = [(k, c, t * scale) for k, c, t in raw]
 
     def closed(max_active, graphs=True, reqs=reqs):
         s = Server(budget, max_active=max_active, graphs=graphs)
@@ -618,20 +653,24 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
     t_bat, bat = closed(64)
     t_direct, _ = closed(64, graphs=False)
     pu = sum(r.point_updates for r in plain.values())
+    step_time = sum(plain[k].t_done - plain[k].t_ready for k in range(n))
+    # the ceiling: the fastest request of the mix stepped alone (a large grid
+    # fills the device); batching cannot beat it on average
+    ceiling = max(plain[k].point_updates / max(plain[k].t_done - plain[k].t_ready, 1e-9) for k in range(n))
+    bound = step_time / (pu / ceiling)
     # the small end of the mix alone: 32 punctures of 3 levels of 64^2 (the
     # plain-method configuration's grids), where one evolution fills a few
     # SMs and the plain path is bound by kernel latency
-    small = [(0, dict(reqs[0][1] if reqs[0][0] == 0 else next(c for kd, c, _ in reqs if kd == 0),
-                      nrtotal=64, nztotal=64, dr0=0.2, dz0=0.2), 2.0)] * 32
+    small_cfg = dict(next(c for kd, c, _ in reqs if kd == 0), nrtotal=64, nztotal=64, nl0=2, dr0=0.2, dz0=0.2)
+    small = [(0, small_cfg, 2.0)] * 32
     t_sp, sp = closed(1, reqs=small)
     t_sb, _ = closed(64, reqs=small)
     t_sd, _ = closed(64, graphs=False, reqs=small)
     pu_s = sum(r.point_updates for r in sp.values())
     rate = load * n / t_bat
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
-    chain_cfg = dict(reqs[0][1]) if reqs[0][0] == 1 else None
-    if chain_cfg is None:
-        chain_cfg = next(dict(c) for kd, c, _ in reqs if kd == 1)
+    chain_cfg = dict(next(c for kd, c, _ in reqs if kd == 2))
+    chain_t = float(np.median([t for kd, _, t in reqs if kd == 2]))
     lo, hi = 0.01, 0.1
     s = Server(budget, max_active=64)
     res, nxt, t0, pending_chain, chain_done = {}, 0, time.perf_counter(), None, 0
@@ -645,7 +684,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
         if pending_chain is None and chain_done < chain:
             a = float(np.sqrt(lo * hi))
             pending_chain = (1000 + chain_done, a)
-            s.submit(1000 + chain_done, params_from_dict(dict(chain_cfg, scalar_a0=a)), 4.0, 0.05)
+            s.submit(1000 + chain_done, params_from_dict(dict(chain_cfg, scalar_a0=a)), chain_t, 0.05)
         a_run, _ = s.tick()
         peak_run = max(peak_run, a_run)
         for r in s.poll():
@@ -667,13 +706,18 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
     same = all(np.array_equal(plain[k].norms(), res[k].norms()) and plain[k].steps == res[k].steps
                for k in range(n))
     ok = all(r.status == 0 for r in list(res.values()) + list(plain.values()) + list(bat.values()))
-    return {"workload": "%d requests: Schwarzschild punctures, massless scalar shells, Brill waves; 64^2-128^2 "
-                        "x 2-3 levels, t_end 1-6 (seeded); + a %d-step bisection chain on the shell amplitude"
-                        % (n, chain),
-            "budget_bytes": budget, "peak_reserved_bytes": peak, "most_running": peak_run,
+    kinds = [kd for kd, _, _ in reqs]
+    return {"workload": "%d requests (%d punctures, %d Brill waves, %d scalar shells), 64^2-1024^2 x 2-6 levels "
+                        "(seeded), t_end in [5, 40] x %.2e (the mix scaled to %.2g point-updates); + a %d-step "
+                        "bisection chain on the shell amplitude" % (n, kinds.count(0), kinds.count(1), kinds.count(2),
+                                                                     scale, work, chain),
+            "t_end_scale": scale, "budget_bytes": budget, "peak_reserved_bytes": peak, "most_running": peak_run,
             "plain_runs_per_s": n / t_plain, "batched_runs_per_s": n / t_bat, "batched_vs_plain": t_plain / t_bat,
             "batched_direct_launch_runs_per_s": n / t_direct,
             "plain_point_updates_per_s": pu / t_plain, "batched_point_updates_per_s": pu / t_bat,
+            "ceiling_point_updates_per_s": ceiling,
+            "ceiling_note": "the fastest request of the plain run, stepped alone",
+            "speedup_bound_from_plain_occupancy": bound,
             "small_grids": {"workload": "32 Schwarzschild punctures, 3 levels of 64^2, t_end 2 (40 coarse steps)",
                             "plain_runs_per_s": 32 / t_sp, "batched_runs_per_s": 32 / t_sb,
                             "batched_vs_plain": t_sp / t_sb, "batched_direct_launch_runs_per_s": 32 / t_sd,
@@ -683,36 +727,6 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8):
             "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99)),
                               "setup_share": float(setup.sum() / svc.sum())},
             "bisection_bracket": [lo, hi], "all_ok": bool(ok), "identical_results": bool(same)}
-
-
-OP_NAMES = ["DFMA", "DADD", "DMUL", "DDIV", "sqrt", "cbrt", "exp", "log", "FFMA (FP32)"]
-
-
-def probe(args):
-    """Stand-alone measurements behind the committed profile summaries:
-    ``fp64`` prints the operation-rate table (ollin_gpu_op_rate);
-    ``norms`` runs ollin_gpu_norms on the lapse of one 1024x1024
-    Schwarzschild level five times (the launches an ncu capture of
-    norms_partial_kernel selects from)."""
-    import torch
-    from ollin.gpu import Evolution, load
-    from ollin.params import params_from_dict
-    L = load()
-    L.ollin_gpu_op_rate.argtypes = [ctypes.c_int]
-    L.ollin_gpu_op_rate.restype = ctypes.c_double
-    if args.probe == "fp64":
-        rates = {nm: L.ollin_gpu_op_rate(k) for k, nm in enumerate(OP_NAMES)}
-        dfma = rates["DFMA"]
-        print(json.dumps({"probe": "fp64", "ops_per_s": rates,
-                          "cost_vs_dfma": {nm: dfma / v if v > 0 else None for nm, v in rates.items()}}))
-    else:
-        e = Evolution(params_from_dict(dict(WORKLOAD, nl0=0, nrtotal=1024, nztotal=1024, shift="none")))
-        e.initial_data()
-        e.initialize()
-        out = [e.norms(0, "alpha") for _ in range(5)]
-        torch.cuda.synchronize()
-        e.close()
-        print(json.dumps({"probe": "norms", "alpha_norms": [float(x) for x in out[-1]]}))
 
 
 def main():

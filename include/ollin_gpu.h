@@ -450,6 +450,22 @@ int ollin_gpu_get_clocks(ollin_handle* h, int level, double out[4]);
  * (OLLIN_ESTATE afterwards).  s must be a whole number. */
 int ollin_gpu_set_clocks(ollin_handle* h, int level, const double in[4]);
 
+/*
+ * One coarse step of n independent evolutions with every kernel of the step
+ * issued once for all of them.  Each evolution's step is recorded (the host
+ * logic of onestep as usual, the launches kept instead of issued); evolutions
+ * whose steps launch the same kernels in the same order form a group, and each
+ * kernel of a group's sequence runs as one multi-instance launch whose blocks
+ * are the blocks of every member's launch, each block reading its evolution's
+ * argument struct from device memory (one upload per call).  The kernels and
+ * arguments are those of ollin_gpu_coarse_step, so the results are the same
+ * bit for bit; a step is some 150 launches for the whole batch instead of per
+ * evolution.  Evolutions with syncboxes copies in their steps are stepped on
+ * their own streams.  Returns after every evolution's step has finished.
+ * No counterpart in the reference (it runs one evolution per process).
+ */
+int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out);
+
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);
 

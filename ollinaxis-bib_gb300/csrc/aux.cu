@@ -17,11 +17,10 @@ namespace {
 //   KTH from tracelessness                        (:747-753)
 //   lambda, Alambda from their definitions        (:767-773, nolambda)
 //   g_lambda = C^2 - B lambda                     (:816-821)
-__global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ AuxArgs a) {
-    chain_enter();
+__device__ __forceinline__ void aux_point_body(const AuxArgs& a, unsigned bx, unsigned by) {
     const LevelGeom& G = a.G;
-    const int i = 1 - G.g + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 - G.g + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = 1 - G.g + (int)(bx * blockDim.x + threadIdx.x);
+    const int j = 1 - G.g + (int)(by * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const size_t o = (size_t)i + (size_t)j * (size_t)G.ld;
     const double r = G.rcol[i];
@@ -50,17 +49,21 @@ __global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ 
     a.aux[X_GLAM][o] = C * C - B * lam;
 }
 
+__global__ void __launch_bounds__(256) aux_point_kernel(const __grid_constant__ AuxArgs a) {
+    chain_enter();
+    aux_point_body(a, blockIdx.x, blockIdx.y);
+}
+
 // DelDef_r/z from first derivatives of the inverse metric (:1085-1094); at
 // t = 0 they overwrite Delta_r/z (:1088-1094).  Rows from jlo (the ghost rows
 // of a grid that does not own the equator take the one-sided z stencils of
 // derivatives.f90:179-212); on a grid off the axis the ghost columns as well,
 // where the reference's diff1r leaves the r derivatives unset: they are zero
 // here, as in an execution that starts them from zero.
-__global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ AuxArgs a) {
-    chain_enter();
+__device__ __forceinline__ void aux_deriv_body(const AuxArgs& a, unsigned bx, unsigned by) {
     const LevelGeom& G = a.G;
-    const int i = (G.axis ? 1 : 1 - G.g) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = (G.axis ? 1 : 1 - G.g) + (int)(bx * blockDim.x + threadIdx.x);
+    const int j = G.jlo + (int)(by * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const long ld = G.ld;
     const size_t o = (size_t)i + (size_t)j * (size_t)ld;
@@ -85,6 +88,11 @@ __global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ 
         a.st[F_DLR][o] = ddr;
         a.st[F_DLZ][o] = ddz;
     }
+}
+
+__global__ void __launch_bounds__(256) aux_deriv_kernel(const __grid_constant__ AuxArgs a) {
+    chain_enter();
+    aux_deriv_body(a, blockIdx.x, blockIdx.y);
 }
 
 // KT2 and (scalar field) rho + trS on the ghost columns i = 1-g..0 of a grid
@@ -137,6 +145,9 @@ __global__ void __launch_bounds__(128) ghost_kt2_kernel(const __grid_constant__ 
     const double trS = (gA * S_A + gB * S_B + gH * S_H + 2.0 * r2 * gC * S_C) * ps4;
     A.auxw[X_RHOS][o] = rho + trS;
 }
+
+const MultiRegistration reg_aux_point((const void*)aux_point_kernel, multi_launch<AuxArgs, aux_point_body, 256, 1>);
+const MultiRegistration reg_aux_deriv((const void*)aux_deriv_kernel, multi_launch<AuxArgs, aux_deriv_body, 256, 1>);
 
 }  // namespace
 

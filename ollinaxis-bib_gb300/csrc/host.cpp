@@ -17,7 +17,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/ollin_gpu.h"
@@ -27,6 +30,17 @@ using namespace ollin;
 
 namespace ollin {
 thread_local bool g_chain_launch = false;
+thread_local LaunchRecorder* g_recorder = nullptr;
+
+static std::unordered_map<const void*, MultiLaunchFn>& multi_registry() {
+    static std::unordered_map<const void*, MultiLaunchFn> m;
+    return m;
+}
+void register_multi(const void* kernel, MultiLaunchFn fn) { multi_registry()[kernel] = fn; }
+MultiLaunchFn multi_for(const void* kernel) {
+    auto it = multi_registry().find(kernel);
+    return it == multi_registry().end() ? nullptr : it->second;
+}
 }
 
 namespace {
@@ -2535,6 +2549,161 @@ int ollin_gpu_coarse_step_many(ollin_handle* const* hs, int n, double* t_out) {
         unsigned int flag = 0;
         const bool ok = cudaMemcpyAsync(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost, h->stream) == cudaSuccess &&
                         cudaStreamSynchronize(h->stream) == cudaSuccess;
+        if (first == OLLIN_OK && !ok) { first = OLLIN_ECUDA; first_msg = "stream synchronisation failed"; }
+        if (first == OLLIN_OK && flag) {
+            first = OLLIN_ENAN;
+            first_msg = "non-finite value produced by evolution " + std::to_string(k);
+        }
+        if (t_out) t_out[k] = h->t[0];
+    }
+    if (first != OLLIN_OK) return fail(first, first_msg);
+    return OLLIN_OK;
+}
+
+namespace {
+
+// Host (pinned) and device buffers of the fused launches' argument tables,
+// kept between calls and grown on demand.
+struct FusedWorkspace {
+    std::mutex mu;
+    unsigned char* host = nullptr;
+    unsigned char* dev = nullptr;
+    size_t cap = 0;
+    cudaStream_t upload = nullptr;
+    cudaEvent_t ready = nullptr;
+};
+FusedWorkspace g_fused;
+
+size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+}  // namespace
+
+int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
+    if (!hs || n < 0) return fail(OLLIN_EINVAL, "bad handle array");
+    for (int k = 0; k < n; ++k) {
+        if (!hs[k]) return fail(OLLIN_EINVAL, "null handle");
+        if (!hs[k]->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
+    }
+    // 1. every evolution's coarse step, recorded instead of launched (the host
+    //    logic of onestep runs as usual: slots, clocks, time weights); an
+    //    evolution with syncboxes copies (device-to-device copies in its step)
+    //    is stepped on its own stream instead
+    std::vector<LaunchRecorder> rec(n);
+    std::vector<int> direct;
+    for (int k = 0; k < n; ++k) {
+        ollin_handle* h = hs[k];
+        if (!h->sync.empty()) { direct.push_back(k); continue; }
+        g_chain_launch = false;
+        g_recorder = &rec[k];
+        const int rc = onestep(h, 0);
+        g_recorder = nullptr;
+        if (rc) return rc;
+        for (const LaunchRec& r : rec[k].recs)
+            if (!multi_for(r.kernel)) return fail(OLLIN_ECUDA, "a step kernel has no fused twin");
+    }
+    for (int k : direct) {
+        g_chain_launch = false;
+        const int rc = onestep(hs[k], 0);
+        if (rc) return rc;
+    }
+    // 2. evolutions whose steps launch the same kernels with the same block
+    //    shapes in the same order form a group; each position of a group's
+    //    sequence becomes one launch over all its members' blocks
+    using Sig = std::vector<std::pair<const void*, unsigned>>;
+    std::map<Sig, std::vector<int>> groups;
+    for (int k = 0; k < n; ++k) {
+        Sig sig;
+        for (const LaunchRec& r : rec[k].recs) sig.emplace_back(r.kernel, r.block.x | (r.block.y << 16));
+        if (!sig.empty()) groups[sig].push_back(k);
+    }
+    // 3. the argument structs, block offsets and grid widths of every fused
+    //    launch in one buffer, uploaded in one copy
+    struct Fused { MultiLaunchFn fn; size_t args, boff, gx; int n, total; dim3 block; };
+    std::vector<std::vector<Fused>> plan;
+    size_t bytes = 0;
+    for (auto& [sig, mem] : groups) {
+        std::vector<Fused> seq;
+        for (size_t p = 0; p < sig.size(); ++p) {
+            const LaunchRec& r0 = rec[mem[0]].recs[p];
+            Fused f{};
+            f.fn = multi_for(r0.kernel);
+            f.n = (int)mem.size();
+            f.block = r0.block;
+            f.args = bytes; bytes = align16(bytes + r0.args.size() * mem.size());
+            f.boff = bytes; bytes = align16(bytes + sizeof(int) * (mem.size() + 1));
+            f.gx = bytes; bytes = align16(bytes + sizeof(int) * mem.size());
+            seq.push_back(f);
+        }
+        plan.push_back(std::move(seq));
+    }
+    std::lock_guard<std::mutex> lock(g_fused.mu);
+    if (bytes > g_fused.cap) {
+        cudaFreeHost(g_fused.host);
+        cudaFree(g_fused.dev);
+        g_fused.host = nullptr; g_fused.dev = nullptr; g_fused.cap = 0;
+        const size_t cap = bytes + bytes / 2 + 4096;
+        if (cudaHostAlloc((void**)&g_fused.host, cap, cudaHostAllocDefault) != cudaSuccess ||
+            cudaMalloc((void**)&g_fused.dev, cap) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "allocation of the fused launch tables failed");
+        g_fused.cap = cap;
+    }
+    if (!g_fused.upload) {
+        CUDA_OR_FAIL(cudaStreamCreateWithFlags(&g_fused.upload, cudaStreamNonBlocking));
+        CUDA_OR_FAIL(cudaEventCreateWithFlags(&g_fused.ready, cudaEventDisableTiming));
+    }
+    {
+        size_t gi = 0;
+        for (auto& [sig, mem] : groups) {
+            for (size_t p = 0; p < sig.size(); ++p) {
+                Fused& f = plan[gi][p];
+                int* boff = (int*)(g_fused.host + f.boff);
+                int* gx = (int*)(g_fused.host + f.gx);
+                int total = 0;
+                for (size_t m = 0; m < mem.size(); ++m) {
+                    const LaunchRec& r = rec[mem[m]].recs[p];
+                    memcpy(g_fused.host + f.args + m * r.args.size(), r.args.data(), r.args.size());
+                    boff[m] = total;
+                    gx[m] = (int)r.grid.x;
+                    total += (int)(r.grid.x * r.grid.y);
+                }
+                boff[mem.size()] = total;
+                f.total = total;
+            }
+            ++gi;
+        }
+    }
+    if (bytes > 0) {
+        CUDA_OR_FAIL(cudaMemcpyAsync(g_fused.dev, g_fused.host, bytes, cudaMemcpyHostToDevice, g_fused.upload));
+        CUDA_OR_FAIL(cudaEventRecord(g_fused.ready, g_fused.upload));
+    }
+    // 4. each group's launches in order on its first member's stream
+    {
+        size_t gi = 0;
+        for (auto& [sig, mem] : groups) {
+            cudaStream_t st = hs[mem[0]]->stream;
+            CUDA_OR_FAIL(cudaStreamWaitEvent(st, g_fused.ready, 0));
+            for (const Fused& f : plan[gi]) {
+                if (f.total == 0) continue;
+                f.fn(g_fused.dev + f.args, (const int*)(g_fused.dev + f.boff), (const int*)(g_fused.dev + f.gx), f.n,
+                     f.total, f.block, st);
+            }
+            CUDA_OR_FAIL(cudaGetLastError());
+            ++gi;
+        }
+    }
+    // 5. wait for every group and every evolution stepped alone; NaN checks
+    int first = OLLIN_OK;
+    std::string first_msg;
+    for (auto& [sig, mem] : groups)
+        if (cudaStreamSynchronize(hs[mem[0]]->stream) != cudaSuccess && first == OLLIN_OK) {
+            first = OLLIN_ECUDA;
+            first_msg = "fused launches failed";
+        }
+    for (int k = 0; k < n; ++k) {
+        ollin_handle* h = hs[k];
+        unsigned int flag = 0;
+        const bool ok = cudaStreamSynchronize(h->stream) == cudaSuccess &&
+                        cudaMemcpy(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost) == cudaSuccess;
         if (first == OLLIN_OK && !ok) { first = OLLIN_ECUDA; first_msg = "stream synchronisation failed"; }
         if (first == OLLIN_OK && flag) {
             first = OLLIN_ENAN;

@@ -10,6 +10,9 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
+
+#include <vector>
 
 namespace ollin {
 
@@ -29,8 +32,80 @@ __device__ __forceinline__ void chain_enter() {
 // set from the handle being stepped).  Off, the launch is an ordinary one.
 extern thread_local bool g_chain_launch;
 
+// ---- fused launches of many evolutions --------------------------------------
+// While a recorder is set on the host thread, launch_chained records each
+// step-path launch (the kernel, its shape and its one argument struct)
+// instead of issuing it.  The fused coarse step of many evolutions records
+// every evolution's step this way, then issues each kernel once for all of
+// them: a multi-instance kernel (multi_kernel below) whose blocks are the
+// blocks of every evolution's launch, each reading its own argument struct
+// from device memory.
+struct LaunchRec {
+    const void* kernel;
+    dim3 grid, block;
+    std::vector<unsigned char> args;
+};
+struct LaunchRecorder {
+    std::vector<LaunchRec> recs;
+};
+extern thread_local LaunchRecorder* g_recorder;
+
+// Issues one multi-instance launch: ``n`` argument structs at dargs (device),
+// block offsets boff[0..n] and grid widths gx[0..n-1] (device), ``total``
+// blocks of shape ``block``.
+using MultiLaunchFn = void (*)(const void* dargs, const int* boff, const int* gx, int n, int total, dim3 block,
+                               cudaStream_t s);
+// The multi-instance twin of a kernel (registered at load time by the file
+// that defines both); null if the kernel has none.
+void register_multi(const void* kernel, MultiLaunchFn fn);
+MultiLaunchFn multi_for(const void* kernel);
+
+// The body of a step-path kernel run for the blocks of every evolution of a
+// fused launch: block b belongs to the evolution k with boff[k] <= b <
+// boff[k+1], and is block (local % gx[k], local / gx[k]) of its own launch.
+template <typename Args, void (*Body)(const Args&, unsigned, unsigned), int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) multi_kernel(const Args* __restrict__ args,
+                                                              const int* __restrict__ boff,
+                                                              const int* __restrict__ gx, int n) {
+    const int b = (int)blockIdx.x;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(boff + mid) <= b) lo = mid;
+        else hi = mid - 1;
+    }
+    const int local = b - __ldg(boff + lo);
+    const int w = __ldg(gx + lo);
+    Body(args[lo], (unsigned)(local % w), (unsigned)(local / w));
+}
+
+template <typename Args, void (*Body)(const Args&, unsigned, unsigned), int THREADS, int MINB>
+void multi_launch(const void* dargs, const int* boff, const int* gx, int n, int total, dim3 block, cudaStream_t s) {
+    multi_kernel<Args, Body, THREADS, MINB><<<total, block, 0, s>>>((const Args*)dargs, boff, gx, n);
+}
+
+// Registers kernel -> its multi-instance twin when the library loads.
+struct MultiRegistration {
+    MultiRegistration(const void* kernel, MultiLaunchFn fn) { register_multi(kernel, fn); }
+};
+
 template <typename... KArgs, typename... Args>
 inline void launch_chained(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+    if constexpr (sizeof...(Args) == 1) {
+        if (g_recorder) {
+            LaunchRec r;
+            r.kernel = (const void*)kernel;
+            r.grid = grid;
+            r.block = block;
+            auto put = [&](const auto& a) {
+                r.args.resize(sizeof(a));
+                memcpy(r.args.data(), &a, sizeof(a));
+            };
+            (put(args), ...);
+            g_recorder->recs.push_back(std::move(r));
+            return;
+        }
+    }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = block;

@@ -18,4 +18,19 @@ void launch_rhs(const StageArgs& a, cudaStream_t s) {
     else launch_chained(rhs_kernel<true, true, false, false>, grd, blk, s, a);
 }
 
+namespace {
+// the fused multi-instance twins of the six instantiations above
+struct MultiRegs {
+    MultiRegs() {
+        register_rhs_multi<false, false, false, false>();
+        register_rhs_multi<false, true, false, false>();
+        register_rhs_multi<true, false, true, false>();
+        register_rhs_multi<true, false, false, false>();
+        register_rhs_multi<true, true, true, false>();
+        register_rhs_multi<true, true, false, false>();
+    }
+};
+const MultiRegs multi_regs;
+}  // namespace
+
 }  // namespace ollin

@@ -34,18 +34,20 @@ __device__ __forceinline__ bool nonfinite(double x) {
 
 struct Deriv5 { double r, z, rr, zz, rz; };
 
-template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
 #ifndef OLLIN_RHS_THREADS
 #define OLLIN_RHS_THREADS 128
 #endif
 #ifndef OLLIN_RHS_MINBLOCKS
 #define OLLIN_RHS_MINBLOCKS 3
 #endif
-__global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_kernel(const __grid_constant__ StageArgs A) {
-    chain_enter();
+// (bx, by) is the block's position in its own launch's grid: blockIdx for an
+// ordinary launch, or the block of this evolution in a fused multi-instance
+// launch (multi_kernel)
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+__device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsigned by) {
     const LevelGeom& G = A.G;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = G.jlo + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = 1 + (int)(bx * blockDim.x + threadIdx.x);
+    const int j = G.jlo + (int)(by * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const int g = G.g, nr = G.nr, nz = G.nz;
     const long ld = G.ld;
@@ -490,6 +492,20 @@ __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_ke
     if constexpr (SCALAR) { upd(F_SPHI, s_sphi); upd(F_SXIR, s_sxr); upd(F_SXIZ, s_sxz); upd(F_SPI, s_spi); }
     if (bad && A.nanflag) atomicOr(A.nanflag, 1u);
     (void)zero; (void)phi_c;
+}
+
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+__global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_kernel(const __grid_constant__ StageArgs A) {
+    chain_enter();
+    rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC>(A, blockIdx.x, blockIdx.y);
+}
+
+// the fused multi-instance twin of one instantiation
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+void register_rhs_multi() {
+    register_multi((const void*)rhs_kernel<SHIFT, SCALAR, ADVECT, STALE, SYNC>,
+                   multi_launch<StageArgs, rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC>, OLLIN_RHS_THREADS,
+                                OLLIN_RHS_MINBLOCKS>);
 }
 
 }  // namespace

@@ -23,4 +23,19 @@ void launch_rhs_stale(const StageArgs& a, cudaStream_t s) {
     else launch_chained(rhs_kernel<true, true, false, true>, grd, blk, s, a);
 }
 
+namespace {
+// the fused multi-instance twins of the six instantiations above
+struct MultiRegs {
+    MultiRegs() {
+        register_rhs_multi<false, false, false, true>();
+        register_rhs_multi<false, true, false, true>();
+        register_rhs_multi<true, false, true, true>();
+        register_rhs_multi<true, false, false, true>();
+        register_rhs_multi<true, true, true, true>();
+        register_rhs_multi<true, true, false, true>();
+    }
+};
+const MultiRegs multi_regs;
+}  // namespace
+
 }  // namespace ollin

@@ -29,15 +29,14 @@ __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, 
 // axis), then the g ghost rows j <= 0 (grids that own the equator) for the
 // columns not filled already; a corner point belongs to the columns when the
 // grid owns the axis
-__global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
-    chain_enter();
+__device__ __forceinline__ void symmetry_body(const SymArgs& a, unsigned bx, unsigned) {
     if (a.skip && *a.skip) return;
     const LevelGeom& G = a.G;
     const int g = G.g;
     const int ncol = G.axis ? g * (G.nz + g) : 0;
     const int i0 = G.axis ? 1 : 1 - g, ni = G.nr - i0 + 1;
     const int nrow = G.equator ? g * ni : 0;
-    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int t = (int)(bx * blockDim.x + threadIdx.x);
     if (t >= ncol + nrow) return;
     int i, j;
     if (t < ncol) {
@@ -58,6 +57,11 @@ __global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ S
         if (gj && a.symz[k] < 0) v = -v;
         f[o] = v;
     }
+}
+
+__global__ void __launch_bounds__(256) symmetry_kernel(const __grid_constant__ SymArgs a) {
+    chain_enter();
+    symmetry_body(a, blockIdx.x, blockIdx.y);
 }
 
 // ---- interp.f90 on the device ---------------------------------------------
@@ -303,10 +307,9 @@ __global__ void __launch_bounds__(128) sync_table_kernel(const __grid_constant__
 
 // thread per (stencil, field); the strips of a smaller imax are the entries
 // with depth <= imax
-__global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant__ ProlongArgs a) {
-    chain_enter();
+__device__ __forceinline__ void prolong_tab_body(const ProlongArgs& a, unsigned bx, unsigned) {
     if (a.skip && *a.skip) return;
-    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int t = (int)(bx * blockDim.x + threadIdx.x);
     if (t >= a.ntab * a.nf) return;
     const int e = t % a.ntab, k = t / a.ntab;
     const XferPt& P = a.tab[e];
@@ -318,6 +321,11 @@ __global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant_
     else if (a.tmode == 1) v = add(mul(a.wa, aux2), mul(a.wp, a.fp[f][P.o_out]));
     else v = add(add(mul(a.wa, aux2), mul(a.wp, a.fp[f][P.o_out])), mul(a.wpp, a.fpp[f][P.o_out]));
     a.fout[f][P.o_out] = v;
+}
+
+__global__ void __launch_bounds__(256) prolong_tab_kernel(const __grid_constant__ ProlongArgs a) {
+    chain_enter();
+    prolong_tab_body(a, blockIdx.x, blockIdx.y);
 }
 
 // the coarse points of restrict_kernel inside the overlap rectangle
@@ -355,16 +363,20 @@ __global__ void __launch_bounds__(128) restrict_table_kernel(const __grid_consta
     tab[t] = x;
 }
 
-__global__ void __launch_bounds__(256) restrict_tab_kernel(const __grid_constant__ RestrictArgs a) {
-    chain_enter();
+__device__ __forceinline__ void restrict_tab_body(const RestrictArgs& a, unsigned bx, unsigned) {
     if (a.skip && *a.skip) return;
-    const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int t = (int)(bx * blockDim.x + threadIdx.x);
     if (t >= a.ntab * a.nf) return;
     const int e = t % a.ntab, k = t / a.ntab;
     const XferPt& P = a.tab[e];
     if (P.o_out == kNoPoint) return;
     const int f = a.fid[k];
     a.cout[f][P.o_out] = xfer_apply(a.F, a.fin[f], P);
+}
+
+__global__ void __launch_bounds__(256) restrict_tab_kernel(const __grid_constant__ RestrictArgs a) {
+    chain_enter();
+    restrict_tab_body(a, blockIdx.x, blockIdx.y);
 }
 
 // ---- injection: interpolate a coarser level to every point of a finer one --
@@ -581,6 +593,12 @@ __global__ void ffma_probe_kernel(double* out, int iters, double seed) {
 dim3 full_grid(const LevelGeom& G, dim3 blk) {
     return dim3((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
 }
+
+const MultiRegistration reg_symmetry((const void*)symmetry_kernel, multi_launch<SymArgs, symmetry_body, 256, 1>);
+const MultiRegistration reg_prolong((const void*)prolong_tab_kernel,
+                                    multi_launch<ProlongArgs, prolong_tab_body, 256, 1>);
+const MultiRegistration reg_restrict((const void*)restrict_tab_kernel,
+                                     multi_launch<RestrictArgs, restrict_tab_body, 256, 1>);
 
 }  // namespace
 

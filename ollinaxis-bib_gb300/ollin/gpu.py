@@ -75,6 +75,7 @@ def load(build_if_missing=True):
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_coarse_step_fused.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.ollin_gpu_min_lapse.argtypes = [vp, dp]
     L.ollin_gpu_step_begin.argtypes = [vp]
     L.ollin_gpu_step_end.argtypes = [vp, dp]
@@ -285,6 +286,20 @@ def step_many(evolutions):
     hs = (ctypes.c_void_p * len(evolutions))(*[e.h.value for e in evolutions])
     t = np.zeros(len(evolutions))
     rc = L.ollin_gpu_coarse_step_many(hs, len(evolutions), t.ctypes.data)
+    if rc != 0:
+        raise OllinError(rc, L.ollin_gpu_last_error().decode())
+    return list(t)
+
+
+def step_fused(evolutions):
+    """One coarse step of every evolution with each kernel of the step issued
+    once for all of them (ollin_gpu_coarse_step_fused); returns each t(0,0)."""
+    if not evolutions:
+        return []
+    L = evolutions[0].L
+    hs = (ctypes.c_void_p * len(evolutions))(*[e.h.value for e in evolutions])
+    t = np.zeros(len(evolutions))
+    rc = L.ollin_gpu_coarse_step_fused(hs, len(evolutions), t.ctypes.data)
     if rc != 0:
         raise OllinError(rc, L.ollin_gpu_last_error().decode())
     return list(t)
