@@ -364,8 +364,9 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
  * next stage of each level still sees the covariant second derivatives,
  * Laplacian, falpha and advective derivatives of the lapse before the solve.
  * ELL_solver = "mixed" solves the same discrete system as "sor" with FP64
- * residuals and FP32 multigrid corrections (no counterpart in the reference).
- * Needs eqsym and Nb = 0. */
+ * residuals and FP32 multigrid corrections, "fp64mg" with FP64 ones (no
+ * counterpart in the reference); both need eqsym and Nb = 0.  "wave" and
+ * "sor" work without equatorial symmetry too. */
 int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
 
 /* Iterations of the elliptic solve run by ollin_gpu_initial_data for

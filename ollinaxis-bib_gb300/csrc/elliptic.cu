@@ -286,7 +286,11 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
         double* Pz = Hr + nj;              // uinf + 0.5 cz (4 u(i,Nz-1) - u(i,Nz-2))
         double* Qz = Pz + ni;              // old u(i+1, Nz)
         double* Hz = Qz + ni;              // 0.5 r(i)/dr
-        const double crn = G.rcol[nr] / G.dr, czn = G.zrow[nz] / G.dz;
+        // without equatorial symmetry the lower z edge as well (:724-736)
+        const bool lower = !G.eqsym;
+        double* Pl = Hz + ni;              // uinf - 0.5 czl (4 u(i,2-g) - u(i,3-g))
+        double* Ql = Pl + ni;              // old u(i+1, 1-g)
+        const double crn = G.rcol[nr] / G.dr, czn = G.zrow[nz] / G.dz, czl = G.zrow[1 - g] / G.dz;
         for (int j = 2 - g + (int)threadIdx.x; j <= nz - 1; j += blockDim.x) {
             const int k = j + g - 1;
             Pr[k] = arn(A.uinf, mrn(mrn(0.5, crn), srn(mrn(4.0, U(nr - 1, j)), U(nr - 2, j))));
@@ -298,6 +302,10 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
             Pz[k] = arn(A.uinf, mrn(mrn(0.5, czn), srn(mrn(4.0, U(i, nz - 1)), U(i, nz - 2))));
             Qz[k] = U(i + 1, nz);
             Hz[k] = mrn(0.5, G.rcol[i] / G.dr);
+            if (lower) {
+                Pl[k] = srn(A.uinf, mrn(mrn(0.5, czl), srn(mrn(4.0, U(i, 2 - g)), U(i, 3 - g))));
+                Ql[k] = U(i + 1, 1 - g);
+            }
         }
         __syncthreads();
         if (threadIdx.x == 0) {  // r edge, j upwards
@@ -314,15 +322,30 @@ __global__ void __launch_bounds__(1024) sor_finish_kernel(const __grid_constant_
                 prev = __ddiv_rn(srn(Pz[k], mrn(Hz[k], srn(Qz[k], prev))), den);
                 Pz[k] = prev;
             }
+        } else if (threadIdx.x == 64 && lower) {  // lower z edge, i outwards
+            const double den = srn(1.0, mrn(1.5, czl));
+            double prev = U(1 - g, 1 - g);
+            for (int k = 1; k <= nr - 2 + g; ++k) {  // i = 2-g .. nr-1
+                prev = __ddiv_rn(srn(Pl[k], mrn(Hz[k], srn(Ql[k], prev))), den);
+                Pl[k] = prev;
+            }
         }
         __syncthreads();
         for (int j = 2 - g + (int)threadIdx.x; j <= nz - 1; j += blockDim.x) U(nr, j) = Pr[j + g - 1];
-        for (int i = 2 - g + (int)threadIdx.x; i <= nr - 1; i += blockDim.x) U(i, nz) = Pz[i + g - 1];
+        for (int i = 2 - g + (int)threadIdx.x; i <= nr - 1; i += blockDim.x) {
+            U(i, nz) = Pz[i + g - 1];
+            if (lower) U(i, 1 - g) = Pl[i + g - 1];
+        }
         __syncthreads();
-        if (threadIdx.x == 0) {  // upper corner (:748-756)
+        if (threadIdx.x == 0) {  // upper corner (:738-745)
             double v = arn(A.uinf, mrn(mrn(0.5, crn), srn(mrn(4.0, U(nr - 1, nz)), U(nr - 2, nz))));
             v = arn(v, mrn(mrn(0.5, czn), srn(mrn(4.0, U(nr, nz - 1)), U(nr, nz - 2))));
             U(nr, nz) = __ddiv_rn(v, arn(1.0, mrn(1.5, arn(crn, czn))));
+            if (lower) {  // lower corner (:747-756)
+                double w = arn(A.uinf, mrn(mrn(0.5, crn), srn(mrn(4.0, U(nr - 1, 1 - g)), U(nr - 2, 1 - g))));
+                w = srn(w, mrn(mrn(0.5, czl), srn(mrn(4.0, U(nr, 2 - g)), U(nr, 3 - g))));
+                U(nr, 1 - g) = __ddiv_rn(w, arn(1.0, mrn(1.5, srn(crn, czl))));
+            }
         }
     }
     __syncthreads();
@@ -686,7 +709,9 @@ void launch_sor_pass(const SorPassArgs& a, cudaStream_t s) {
     sor_pass_kernel<<<grd, blk, 0, s>>>(a);
 }
 
-size_t sor_finish_smem(const LevelGeom& G) { return (size_t)3 * ((G.nz + G.g) + (G.nr + G.g)) * sizeof(double); }
+size_t sor_finish_smem(const LevelGeom& G) {
+    return (size_t)(3 * (G.nz + G.g) + (G.eqsym ? 3 : 5) * (G.nr + G.g)) * sizeof(double);
+}
 
 int launch_sor_finish(const SorFinishArgs& a, cudaStream_t s) {
     const size_t smem = a.robin ? sor_finish_smem(a.G) : 0;

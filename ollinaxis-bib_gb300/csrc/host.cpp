@@ -166,8 +166,9 @@ int check_params(const ollin_params& P) {
     if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
     if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
     if (!P.eqsym && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
-        P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "elliptic initial data without equatorial symmetry needs ELL_solver = wave on the device");
+        P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
+        return fail(OLLIN_EINVAL,
+                    "elliptic initial data without equatorial symmetry needs ELL_solver = wave or sor on the device");
     if (P.ghost != 0 && P.ghost != 3) return fail(OLLIN_EINVAL, "ghost must be 3 for order four");
     if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
@@ -1997,8 +1998,8 @@ int initial_data(ollin_handle* h) {
 int maximal_slicing(ollin_handle* h, const double* va_max) {
     const ollin_params& P = h->P;
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
-    if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE)
-        return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave on the device");
+    if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
+        return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave or sor on the device");
     if (h->nb > 0 && (P.ell_solver == OLLIN_ELL_MIXED || P.ell_solver == OLLIN_ELL_FP64MG))
         return fail(OLLIN_EINVAL, "maximal slicing with refinement boxes needs ELL_solver = wave or sor");
     if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED &&

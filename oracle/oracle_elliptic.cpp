@@ -306,11 +306,26 @@ int sor(Sim& S, Level& L, SorArr& a, SorArr& b, SorArr& c, SorArr& d, SorArr& e,
                 u(i, jmax) = (uinf + 0.5 * cz * (4.0 * u(i, jmax - 1) - u(i, jmax - 2))
                               - 0.5 * cr * (u(i + 1, jmax) - u(i - 1, jmax))) / (1.0 + 1.5 * cz);
             }
-            if (!L.eqsym) throw std::runtime_error("oracle: sor lower-z Robin boundary (eqsym=.false.) not restated");
+            // lower z edge without equatorial symmetry (sor_elliptic.f90:724-736)
+            if (!L.eqsym) {
+                cz = z(1, 1 - g) / L.dz;
+                for (int i = 2; i <= imax - 1; ++i) {
+                    cr = r(i - g, 1) / L.dr;
+                    u(i, 1) = (uinf - 0.5 * cz * (4.0 * u(i, 2) - u(i, 3))
+                               - 0.5 * cr * (u(i + 1, 1) - u(i - 1, 1))) / (1.0 - 1.5 * cz);
+                }
+            }
             cr = r(imax - g, jmax - g) / L.dr;
             cz = z(imax - g, jmax - g) / L.dz;
             u(imax, jmax) = (uinf + 0.5 * cr * (4.0 * u(imax - 1, jmax) - u(imax - 2, jmax))
                              + 0.5 * cz * (4.0 * u(imax, jmax - 1) - u(imax, jmax - 2))) / (1.0 + 1.5 * (cr + cz));
+            // lower corner (:748-756)
+            if (!L.eqsym) {
+                cr = r(imax - g, 1 - g) / L.dr;
+                cz = z(imax - g, 1 - g) / L.dz;
+                u(imax, 1) = (uinf + 0.5 * cr * (4.0 * u(imax - 1, 1) - u(imax - 2, 1))
+                              - 0.5 * cz * (4.0 * u(imax, 2) - u(imax, 3))) / (1.0 + 1.5 * (cr - cz));
+            }
         }
         if (L.ownaxis)
             for (int i = 1; i <= g; ++i)

@@ -132,6 +132,15 @@ CASES = {
     "max_slicing_sor": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, ilapse="one",
                             slicing="maximal", ell_solver="sor", shift="Gammadriver2", drivercsi=0.75,
                             drivereta=2.0, _steps=[0, 1, 2], _elliptic=True),
+    # SOR without equatorial symmetry: the Robin condition on the lower z edge
+    # and the lower corner (sor_elliptic.f90:724-756), for the elliptic data
+    # (flat Laplacian, two levels) and for maximal slicing every step
+    "ell_sor_noeqsym": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, eqsym=False,
+                            idata="scalarpulse", ilapse="one", mattertype="scalar", scalar_a0=0.05,
+                            scalar_r0=2.0, scalar_z0=1.0, ell_solver="sor", scalardiss=0.02, _steps=[0, 1],
+                            _elliptic=True),
+    "max_noeqsym_sor": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, eqsym=False,
+                            maximalevery=1, ell_solver="sor", _steps=[0, 1], _elliptic=True),
 }
 
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",

@@ -115,9 +115,19 @@ SOR_RING = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1
                 scalar_z0=4.0, scalardiss=0.02, ell_solver="sor")
 
 
-@pytest.mark.parametrize("cfg", [SOR_2LEV, SOR_POTENTIAL, SOR_BRILL, SOR_BOXES, SOR_RING],
+# without equatorial symmetry: the Robin condition on the lower z edge and
+# the lower corner (sor_elliptic.f90:724-756), the layout of the
+# executed-reference fixture ell_sor_noeqsym and a Brill wave on three levels
+SOR_NOEQSYM = dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.5, dz0=0.5, eqsym=0, idata="scalarpulse",
+                   mattertype="scalar", scalar_a0=0.05, scalar_r0=2.0, scalar_z0=1.0, scalardiss=0.02,
+                   ell_solver="sor")
+SOR_BRILL_NOEQSYM = dict(SOR_BRILL, eqsym=0, nztotal=48)
+
+
+@pytest.mark.parametrize("cfg", [SOR_2LEV, SOR_POTENTIAL, SOR_BRILL, SOR_BOXES, SOR_RING, SOR_NOEQSYM,
+                                 SOR_BRILL_NOEQSYM],
                          ids=["sor_pulse_2lev", "sor_pulse_potential", "sor_brill_3lev", "sor_boxes",
-                              "sor_ring_two_levels"])
+                              "sor_ring_two_levels", "sor_pulse_no_eqsym", "sor_brill_no_eqsym"])
 def test_sor_data_matches_oracle(cfg):
     """SOR (sor_elliptic.f90): the red-black sweeps and the sequential Robin
     boundary reproduce the reference's arithmetic; the residual norm that

@@ -101,8 +101,11 @@ def test_maximal_every_step_wave():
     run(EVERY, 3)
 
 
-def test_maximal_every_step_without_equatorial_symmetry():
-    run(dict(EVERY, eqsym=0, nl0=0), 2)
+@pytest.mark.parametrize("solver", ["wave", "sor"])
+def test_maximal_every_step_without_equatorial_symmetry(solver):
+    """Without equatorial symmetry: the wave solver's radiative lower edge, or
+    SOR's Robin lower edge and lower corner (sor_elliptic.f90:724-756)."""
+    run(dict(EVERY, eqsym=0, nl0=0, ell_solver=solver), 2)
 
 
 def test_maximal_every_step_with_refinement_boxes():

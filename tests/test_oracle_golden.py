@@ -91,7 +91,7 @@ def test_oracle_matches_reference_fortran(name):
 
 
 ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev", "ell_pulse_noeqsym",
-             "ell_pulse_boxes", "ell_sor_boxes"]
+             "ell_pulse_boxes", "ell_sor_boxes", "ell_sor_noeqsym"]
 
 
 def ell_cfg(meta):
@@ -148,7 +148,7 @@ def test_oracle_elliptic_data_matches_reference_fortran(name):
 # differences of the initial data stay at the 1e-13 level through them.
 ELL_TOL = 1e-9
 
-MAX_CASES = ["max_ilapse_pulse", "max_every_wave", "max_slicing_sor", "max_noeqsym_wave"]
+MAX_CASES = ["max_ilapse_pulse", "max_every_wave", "max_slicing_sor", "max_noeqsym_wave", "max_noeqsym_sor"]
 
 
 def maximal_due(cfg, step):
