@@ -473,7 +473,7 @@ def batch_throughput(n=256, steps=1, seed=7):
     R of the large single instance; plain run i at rate r_i leaves the rest
     of the device idle, so batched/plain <= sum(t_i) / (sum(pu_i) / R)."""
     import numpy as np
-    from ollin.gpu import Evolution, step_fused, step_many
+    from ollin.gpu import SCHEDULES, Evolution, step_auto, step_fused, step_many
     from ollin.params import params_from_dict
     cfgs = c4_configs(n, seed)
 
@@ -515,6 +515,16 @@ def batch_throughput(n=256, steps=1, seed=7):
         step_fused(es)
     t_fused = time.perf_counter() - t
     pu_fused = sum(e.point_updates() for e in es) - p0
+    # the schedule autotuner on the same batch: two live steps under each
+    # schedule, then its choice, timed
+    for _ in range(6):
+        step_auto(es)
+    p0 = sum(e.point_updates() for e in es)
+    t = time.perf_counter()
+    for _ in range(steps):
+        _, sched = step_auto(es)
+    t_auto = time.perf_counter() - t
+    pu_auto = sum(e.point_updates() for e in es) - p0
     for e in es:
         e.close()
     t_plain = np.array(t_plain)
@@ -533,6 +543,8 @@ def batch_throughput(n=256, steps=1, seed=7):
             "fused_point_updates_per_s": pu_fused / t_fused,
             "fused_speedup": float(t_plain.sum()) / t_fused * (pu_fused / pu),
             "fused_runs_per_s": n / t_fused * (pu_fused / pu),
+            "autotuned_schedule": SCHEDULES[sched], "autotuned_point_updates_per_s": pu_auto / t_auto,
+            "autotuned_speedup": float(t_plain.sum()) / t_auto * (pu_auto / pu),
             "plain_run_seconds_p50": float(np.percentile(t_plain, 50)),
             "plain_run_seconds_p99": float(np.percentile(t_plain, 99)),
             "plain_rate_p50": float(np.percentile(rate_plain, 50)),
@@ -639,8 +651,8 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
     scale = work / full
     reqs = [(k, c, t * scale) for k, c, t in raw]
 
-    def closed(max_active, graphs=True, reqs=reqs):
-        s = Server(budget, max_active=max_active, graphs=graphs)
+    def closed(max_active, graphs=True, reqs=reqs, fused=False):
+        s = Server(budget, max_active=max_active, graphs=graphs, fused=fused)
         for k, (_, cfg, t_end) in enumerate(reqs):
             s.submit(k, params_from_dict(cfg), t_end, 0.05 if cfg.get("mattertype") == "scalar" else 0.0)
         t = time.perf_counter()
@@ -652,6 +664,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
     t_plain, plain = closed(1)
     t_bat, bat = closed(64)
     t_direct, _ = closed(64, graphs=False)
+    t_fus, fus = closed(64, fused=True)
     pu = sum(r.point_updates for r in plain.values())
     step_time = sum(plain[k].t_done - plain[k].t_ready for k in range(n))
     # the ceiling: the fastest request of the mix stepped alone (a large grid
@@ -666,6 +679,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
     t_sp, sp = closed(1, reqs=small)
     t_sb, _ = closed(64, reqs=small)
     t_sd, _ = closed(64, graphs=False, reqs=small)
+    t_sf, sf = closed(64, reqs=small, fused=True)
     pu_s = sum(r.point_updates for r in sp.values())
     rate = load * n / t_bat
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=n))
@@ -704,7 +718,8 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
     svc = np.array([plain[k].t_done - plain[k].t_admit for k in range(n)])
     setup = np.array([plain[k].t_ready - plain[k].t_admit for k in range(n)])
     same = all(np.array_equal(plain[k].norms(), res[k].norms()) and plain[k].steps == res[k].steps
-               for k in range(n))
+               and np.array_equal(plain[k].norms(), fus[k].norms()) for k in range(n))
+    same = same and all(np.array_equal(sp[k].norms(), sf[k].norms()) for k in range(32))
     ok = all(r.status == 0 for r in list(res.values()) + list(plain.values()) + list(bat.values()))
     kinds = [kd for kd, _, _ in reqs]
     return {"workload": "%d requests (%d punctures, %d Brill waves, %d scalar shells), 64^2-1024^2 x 2-6 levels "
@@ -714,6 +729,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
             "t_end_scale": scale, "budget_bytes": budget, "peak_reserved_bytes": peak, "most_running": peak_run,
             "plain_runs_per_s": n / t_plain, "batched_runs_per_s": n / t_bat, "batched_vs_plain": t_plain / t_bat,
             "batched_direct_launch_runs_per_s": n / t_direct,
+            "fused_ticks_runs_per_s": n / t_fus, "fused_ticks_vs_plain": t_plain / t_fus,
             "plain_point_updates_per_s": pu / t_plain, "batched_point_updates_per_s": pu / t_bat,
             "ceiling_point_updates_per_s": ceiling,
             "ceiling_note": "the fastest request of the plain run, stepped alone",
@@ -721,6 +737,7 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
             "small_grids": {"workload": "32 Schwarzschild punctures, 3 levels of 64^2, t_end 2 (40 coarse steps)",
                             "plain_runs_per_s": 32 / t_sp, "batched_runs_per_s": 32 / t_sb,
                             "batched_vs_plain": t_sp / t_sb, "batched_direct_launch_runs_per_s": 32 / t_sd,
+                            "fused_ticks_runs_per_s": 32 / t_sf, "fused_ticks_vs_plain": t_sp / t_sf,
                             "batched_point_updates_per_s": pu_s / t_sb},
             "served": {"arrival_rate_per_s": rate, "runs_per_s": (n + chain) / t_served,
                        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99))},

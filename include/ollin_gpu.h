@@ -337,6 +337,13 @@ int ollin_server_poll(ollin_server* s, ollin_result* out, int max, int* n_out);
 /* Whether evolutions admitted from now on step as captured graphs
  * (ollin_gpu_step_graphs; on by default). */
 int ollin_server_set_graphs(ollin_server* s, int enable);
+/* The loop's schedule: 0 (default) every running evolution keeps its own next
+ * coarse step queued on its stream and moves on as soon as that step ends;
+ * 1 each tick is one fused coarse step of every running evolution
+ * (ollin_gpu_coarse_step_fused: each kernel issued once for all of them),
+ * with new requests joining at the next tick.  Results are the same bit for
+ * bit.  Changed only while no step is queued (OLLIN_ESTATE otherwise). */
+int ollin_server_set_fused(ollin_server* s, int enable);
 /* Device bytes reserved now and at most so far by the server's evolutions. */
 int ollin_server_usage(const ollin_server* s, size_t* used, size_t* peak);
 /* Message for the last failure of an ollin_server_* call on the calling thread. */
@@ -462,10 +469,33 @@ int ollin_gpu_set_clocks(ollin_handle* h, int level, const double in[4]);
  * arguments are those of ollin_gpu_coarse_step, so the results are the same
  * bit for bit; a step is some 150 launches for the whole batch instead of per
  * evolution.  Evolutions with syncboxes copies in their steps are stepped on
- * their own streams.  Returns after every evolution's step has finished.
+ * their own streams.  Returns after every evolution's step has finished,
+ * with the first failure; status (may be NULL) receives each evolution's own
+ * code (OLLIN_ENAN for the one that produced a non-finite value), so that a
+ * caller can retire a failed evolution and keep the others.
  * No counterpart in the reference (it runs one evolution per process).
  */
-int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out);
+int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out, int* status);
+
+/* Whether ollin_gpu_coarse_step_fused records each group's launch sequence as
+ * a CUDA graph the first time it meets it and replays it on later steps of
+ * the same batch (1, the default), or issues the launches directly (0).  The
+ * kernels, arguments and order are the same either way.  No counterpart in
+ * the reference. */
+int ollin_gpu_fused_graphs(int on);
+
+/*
+ * One coarse step of n independent evolutions under the schedule an
+ * autotuner picks for this batch (the same handles in the same order): the
+ * fused launches replayed as graphs (0), the fused launches issued directly
+ * (1), or every evolution on its own stream (2, ollin_gpu_coarse_step_many).
+ * The first calls for a batch try each schedule on live steps, two steps each
+ * (results are the same bit for bit under every schedule, so nothing is
+ * wasted), timing the second by wall clock per point-update; later calls use
+ * the fastest.  *schedule_out (may be NULL) reports the schedule used.  No
+ * counterpart in the reference.
+ */
+int ollin_gpu_coarse_step_auto(ollin_handle* const* hs, int n, double* t_out, int* schedule_out);
 
 /* Message for the last failure on the calling thread ("" if none). */
 const char* ollin_gpu_last_error(void);

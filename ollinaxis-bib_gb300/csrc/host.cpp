@@ -14,6 +14,7 @@
 // state at the start of the current (p) and previous (pp) step, so it is read
 // straight from those slots.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -2572,15 +2573,35 @@ struct FusedWorkspace {
     size_t cap = 0;
     cudaStream_t upload = nullptr;
     cudaEvent_t ready = nullptr;
+    // each group's sequence of fused launches recorded once as a CUDA graph,
+    // keyed by everything the launches bake in (kernels, shapes, table
+    // offsets, the table buffer): a repeated step replays it after uploading
+    // that step's tables
+    bool graphs = true;
+    std::unordered_map<std::string, cudaGraphExec_t> execs;
 };
 FusedWorkspace g_fused;
+
+void drop_fused_graphs() {
+    for (auto& kv : g_fused.execs) cudaGraphExecDestroy(kv.second);
+    g_fused.execs.clear();
+}
 
 size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 }  // namespace
 
-int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
+int ollin_gpu_fused_graphs(int on) {
+    std::lock_guard<std::mutex> lock(g_fused.mu);
+    g_fused.graphs = on != 0;
+    if (!g_fused.graphs) drop_fused_graphs();
+    return OLLIN_OK;
+}
+
+int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out, int* status) {
     if (!hs || n < 0) return fail(OLLIN_EINVAL, "bad handle array");
+    if (status)
+        for (int k = 0; k < n; ++k) status[k] = OLLIN_OK;
     for (int k = 0; k < n; ++k) {
         if (!hs[k]) return fail(OLLIN_EINVAL, "null handle");
         if (!hs[k]->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before the first step");
@@ -2639,6 +2660,7 @@ int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
     }
     std::lock_guard<std::mutex> lock(g_fused.mu);
     if (bytes > g_fused.cap) {
+        drop_fused_graphs();  // they point into the old buffer
         cudaFreeHost(g_fused.host);
         cudaFree(g_fused.dev);
         g_fused.host = nullptr; g_fused.dev = nullptr; g_fused.cap = 0;
@@ -2683,11 +2705,42 @@ int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
         for (auto& [sig, mem] : groups) {
             cudaStream_t st = hs[mem[0]]->stream;
             CUDA_OR_FAIL(cudaStreamWaitEvent(st, g_fused.ready, 0));
-            for (const Fused& f : plan[gi]) {
-                if (f.total == 0) continue;
-                f.fn(g_fused.dev + f.args, (const int*)(g_fused.dev + f.boff), (const int*)(g_fused.dev + f.gx), f.n,
-                     f.total, f.block, st);
+            auto issue = [&](cudaStream_t q) {
+                for (const Fused& f : plan[gi]) {
+                    if (f.total == 0) continue;
+                    f.fn(g_fused.dev + f.args, (const int*)(g_fused.dev + f.boff), (const int*)(g_fused.dev + f.gx),
+                         f.n, f.total, f.block, q);
+                }
+            };
+            cudaGraphExec_t exec = nullptr;
+            if (g_fused.graphs) {
+                std::string key((const char*)&g_fused.dev, sizeof(g_fused.dev));
+                for (const Fused& f : plan[gi]) {
+                    const long long v[8] = {(long long)(uintptr_t)f.fn, (long long)f.args, (long long)f.boff,
+                                            (long long)f.gx, f.n, f.total, (long long)f.block.x, (long long)f.block.y};
+                    key.append((const char*)v, sizeof(v));
+                }
+                auto it = g_fused.execs.find(key);
+                if (it != g_fused.execs.end()) {
+                    exec = it->second;
+                } else {
+                    if (g_fused.execs.size() >= 256) drop_fused_graphs();
+                    cudaGraph_t graph = nullptr;
+                    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                        issue(st);
+                        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+                        if (ec == cudaSuccess && graph &&
+                            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess)
+                            g_fused.execs[key] = exec;
+                        else
+                            exec = nullptr;
+                        if (graph) cudaGraphDestroy(graph);
+                    }
+                    cudaGetLastError();  // a failed capture falls back to direct launches
+                }
             }
+            if (exec) CUDA_OR_FAIL(cudaGraphLaunch(exec, st));
+            else issue(st);
             CUDA_OR_FAIL(cudaGetLastError());
             ++gi;
         }
@@ -2705,6 +2758,7 @@ int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
         unsigned int flag = 0;
         const bool ok = cudaStreamSynchronize(h->stream) == cudaSuccess &&
                         cudaMemcpy(&flag, h->d_flag, sizeof(flag), cudaMemcpyDeviceToHost) == cudaSuccess;
+        if (status) status[k] = !ok ? OLLIN_ECUDA : flag ? OLLIN_ENAN : OLLIN_OK;
         if (first == OLLIN_OK && !ok) { first = OLLIN_ECUDA; first_msg = "stream synchronisation failed"; }
         if (first == OLLIN_OK && flag) {
             first = OLLIN_ENAN;
@@ -2713,6 +2767,80 @@ int ollin_gpu_coarse_step_fused(ollin_handle* const* hs, int n, double* t_out) {
         if (t_out) t_out[k] = h->t[0];
     }
     if (first != OLLIN_OK) return fail(first, first_msg);
+    return OLLIN_OK;
+}
+
+namespace {
+
+// The schedule autotuner of ollin_gpu_coarse_step_auto: per batch (the set of
+// handles), the wall time per point-update of each schedule, tried on live
+// steps (every schedule gives the same results bit for bit, so tuning wastes
+// no work), then the fastest one.
+enum Schedule { kFusedGraphs = 0, kFusedDirect = 1, kStreams = 2, kSchedules = 3 };
+struct TuneEntry {
+    double sec_per_pu[kSchedules] = {0, 0, 0};
+    int tried[kSchedules] = {0, 0, 0};
+    int best = -1;
+};
+std::mutex g_tune_mu;
+std::map<std::vector<const ollin_handle*>, TuneEntry> g_tune;
+constexpr int kTrials = 2;  // steps per schedule before choosing
+
+}  // namespace
+
+int ollin_gpu_coarse_step_auto(ollin_handle* const* hs, int n, double* t_out, int* schedule_out) {
+    if (!hs || n <= 0) return fail(OLLIN_EINVAL, "bad handle array");
+    std::vector<const ollin_handle*> key(hs, hs + n);
+    int sched;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        if (g_tune.size() > 1024) g_tune.clear();
+        TuneEntry& e = g_tune[key];
+        sched = e.best;
+        if (sched < 0) {
+            sched = 0;
+            while (sched < kSchedules && e.tried[sched] >= kTrials) ++sched;
+        }
+    }
+    double pu0 = 0;
+    for (int k = 0; k < n; ++k) pu0 += hs[k]->point_updates;
+    const auto t0 = std::chrono::steady_clock::now();
+    int rc;
+    if (sched == kStreams) {
+        rc = ollin_gpu_coarse_step_many(hs, n, t_out);
+    } else {
+        bool prev;
+        {
+            std::lock_guard<std::mutex> lock(g_fused.mu);
+            prev = g_fused.graphs;
+            g_fused.graphs = sched == kFusedGraphs;
+        }
+        rc = ollin_gpu_coarse_step_fused(hs, n, t_out, nullptr);
+        std::lock_guard<std::mutex> lock(g_fused.mu);
+        g_fused.graphs = prev;
+    }
+    if (rc) return rc;
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    double pu = -pu0;
+    for (int k = 0; k < n; ++k) pu += hs[k]->point_updates;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        TuneEntry& e = g_tune[key];
+        if (e.best < 0 && pu > 0) {
+            // the first step of a schedule also pays its set-up (graph
+            // recording, table growth): only the later trials count
+            if (e.tried[sched] > 0) e.sec_per_pu[sched] += dt / pu;
+            e.tried[sched]++;
+            bool done = true;
+            for (int c = 0; c < kSchedules; ++c) done = done && e.tried[c] >= kTrials;
+            if (done) {
+                e.best = 0;
+                for (int c = 1; c < kSchedules; ++c)
+                    if (e.sec_per_pu[c] < e.sec_per_pu[e.best]) e.best = c;
+            }
+        }
+    }
+    if (schedule_out) *schedule_out = sched;
     return OLLIN_OK;
 }
 

@@ -148,6 +148,7 @@ struct ollin_server {
     std::chrono::steady_clock::time_point t0;
     Workers* workers = nullptr;  // issue threads besides the caller's
     int graphs = 1;              // coarse steps as captured graphs (ollin_gpu_step_graphs)
+    int fused = 0;               // 1: each tick is one fused coarse step of every running evolution
 
     double now() const {
         return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -283,8 +284,61 @@ int ollin_server_submit(ollin_server* s, long long id, const ollin_params* p, in
     return OLLIN_OK;
 }
 
+namespace {
+
+// A tick of the fused schedule: one coarse step of every running evolution,
+// each kernel of the step issued once for all of them
+// (ollin_gpu_coarse_step_fused), then each evolution's end-of-step work and
+// the admissions.  Requests admitted now join the next tick's step.
+int fused_tick(ollin_server* s) {
+    const size_t nrun = s->running.size();
+    if (nrun > 0) {
+        std::vector<ollin_handle*> hs(nrun);
+        for (size_t k = 0; k < nrun; ++k) hs[k] = s->running[k].h;
+        std::vector<double> t(nrun, 0.0);
+        std::vector<int> st(nrun, OLLIN_OK);
+        const int rc_all = ollin_gpu_coarse_step_fused(hs.data(), (int)nrun, t.data(), st.data());
+        std::vector<int> rc(nrun, OLLIN_OK);
+        std::vector<char> coll(nrun, 0), fin(nrun, 0);
+        s->workers->run((int)nrun, [&](int q) {
+            const size_t k = (size_t)q;
+            Running& e = s->running[k];
+            // a failure outside any one evolution's flag ends them all
+            int r = st[k] ? st[k] : (rc_all && rc_all != OLLIN_ENAN ? rc_all : OLLIN_OK);
+            if (!r) { e.t = t[k]; e.steps += 1; }
+            if (!r && maximal_after(e.r, e.steps)) r = ollin_gpu_maximal_slicing(e.h, nullptr);
+            if (!r && e.r.collapse > 0.0) {
+                r = min_lapse(e.h, &e.min_alpha);
+                coll[k] = !r && e.min_alpha < e.r.collapse;
+            }
+            rc[k] = r;
+            fin[k] = r || coll[k] || e.steps >= e.r.nsteps;
+        });
+        for (size_t q = nrun; q-- > 0;)
+            if (fin[q]) s->retire(q, rc[q], coll[q] != 0);
+    }
+    s->admit();
+    return OLLIN_OK;
+}
+
+}  // namespace
+
+int ollin_server_set_fused(ollin_server* s, int enable) {
+    if (!s) return sfail(OLLIN_EINVAL, "null server");
+    for (const Running& e : s->running)
+        if (e.queued) return sfail(OLLIN_ESTATE, "the schedule changes only when no step is queued");
+    s->fused = enable != 0;
+    return OLLIN_OK;
+}
+
 int ollin_server_tick(ollin_server* s, int* n_active, int* n_waiting) {
     if (!s) return sfail(OLLIN_EINVAL, "null server");
+    if (s->fused) {
+        const int rc = fused_tick(s);
+        if (n_active) *n_active = (int)s->running.size();
+        if (n_waiting) *n_waiting = (int)s->waiting.size();
+        return rc;
+    }
     for (int spin = 0;; ++spin) {
         // (1) every evolution whose step finished: the step's end, the solve
         //     that follows it, the checks, then its next step

@@ -75,7 +75,10 @@ def load(build_if_missing=True):
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
-    L.ollin_gpu_coarse_step_fused.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    L.ollin_gpu_coarse_step_fused.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    L.ollin_gpu_fused_graphs.argtypes = [ctypes.c_int]
+    L.ollin_gpu_coarse_step_auto.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                             ctypes.POINTER(ctypes.c_int)]
     L.ollin_gpu_min_lapse.argtypes = [vp, dp]
     L.ollin_gpu_step_begin.argtypes = [vp]
     L.ollin_gpu_step_end.argtypes = [vp, dp]
@@ -90,6 +93,7 @@ def load(build_if_missing=True):
     L.ollin_server_usage.argtypes = [vp, sp, sp]
     L.ollin_server_last_error.restype = ctypes.c_char_p
     L.ollin_server_set_graphs.argtypes = [vp, ctypes.c_int]
+    L.ollin_server_set_fused.argtypes = [vp, ctypes.c_int]
     L.ollin_gpu_step_graphs.argtypes = [vp, ctypes.c_int, ctypes.c_void_p]
     L.ollin_gpu_step_chaining.argtypes = [vp, ctypes.c_int]
     L.ollin_gpu_download_slot.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
@@ -299,10 +303,33 @@ def step_fused(evolutions):
     L = evolutions[0].L
     hs = (ctypes.c_void_p * len(evolutions))(*[e.h.value for e in evolutions])
     t = np.zeros(len(evolutions))
-    rc = L.ollin_gpu_coarse_step_fused(hs, len(evolutions), t.ctypes.data)
+    rc = L.ollin_gpu_coarse_step_fused(hs, len(evolutions), t.ctypes.data, None)
     if rc != 0:
         raise OllinError(rc, L.ollin_gpu_last_error().decode())
     return list(t)
+
+
+SCHEDULES = {0: "fused, graphs", 1: "fused, direct launches", 2: "one stream per evolution"}
+
+
+def step_auto(evolutions):
+    """One coarse step of every evolution under the schedule the autotuner
+    chose for this batch (ollin_gpu_coarse_step_auto); returns (t(0,0) of
+    each, the schedule used)."""
+    L = evolutions[0].L
+    hs = (ctypes.c_void_p * len(evolutions))(*[e.h.value for e in evolutions])
+    t = np.zeros(len(evolutions))
+    sched = ctypes.c_int()
+    rc = L.ollin_gpu_coarse_step_auto(hs, len(evolutions), t.ctypes.data, ctypes.byref(sched))
+    if rc != 0:
+        raise OllinError(rc, L.ollin_gpu_last_error().decode())
+    return list(t), sched.value
+
+
+def fused_graphs(on):
+    """Replay the fused steps' launch sequences as CUDA graphs (default) or
+    issue them directly (ollin_gpu_fused_graphs)."""
+    load().ollin_gpu_fused_graphs(1 if on else 0)
 
 
 def footprint(params):
@@ -336,12 +363,13 @@ class Server:
     """The request loop of the C ABI (ollin_server_*): continuous batching of
     evolutions on the current device, admitted against a byte budget."""
 
-    def __init__(self, budget_bytes, max_active=64, graphs=True):
+    def __init__(self, budget_bytes, max_active=64, graphs=True, fused=False):
         self.L = load()
         h = ctypes.c_void_p()
         self._check(self.L.ollin_server_create(int(budget_bytes), int(max_active), ctypes.byref(h)))
         self.h = h
         self._check(self.L.ollin_server_set_graphs(self.h, 1 if graphs else 0))
+        self._check(self.L.ollin_server_set_fused(self.h, 1 if fused else 0))
 
     def _check(self, rc):
         if rc != 0:

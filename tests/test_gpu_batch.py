@@ -66,12 +66,15 @@ FUSED_CFGS = CFGS + [
 ]
 
 
-def test_fused_steps_equal_single_steps():
+@pytest.mark.parametrize("graphs", [True, False], ids=["graphs", "direct"])
+def test_fused_steps_equal_single_steps(graphs):
     """ollin_gpu_coarse_step_fused: every kernel of the step once for all the
-    evolutions of a group; the fields of every evolution equal, bit for bit,
-    those of stepping it alone."""
-    from ollin.gpu import step_fused
+    evolutions of a group, replayed as a recorded graph from the second step
+    of a group on, or issued directly; the fields of every evolution equal,
+    bit for bit, those of stepping it alone."""
+    from ollin.gpu import fused_graphs, step_fused
     from parity_util import scalar_pulse
+    fused_graphs(graphs)
     alone, fused = [], []
     for cfg in FUSED_CFGS:
         for lst in (alone, fused):
@@ -90,7 +93,7 @@ def test_fused_steps_equal_single_steps():
             if cfg.get("maximalevery"):
                 e.maximal_slicing()
             lst.append(e)
-    for step in range(3):
+    for step in range(4):
         t_alone = [e.step() for e in alone]
         t_fused = step_fused(fused)
         assert t_alone == t_fused
@@ -104,6 +107,7 @@ def test_fused_steps_equal_single_steps():
                 assert np.array_equal(a.download(lev, nm), b.download(lev, nm)), (cfg, lev, nm)
     for e in alone + fused:
         e.close()
+    fused_graphs(True)
 
 
 def test_fused_step_reports_nan():
@@ -115,3 +119,25 @@ def test_fused_step_reports_nan():
     with pytest.raises(OllinError) as ex:
         step_fused(es)
     assert ex.value.code == 3
+
+
+def test_autotuned_steps_equal_single_steps():
+    """ollin_gpu_coarse_step_auto: two live steps under each schedule (fused
+    with graphs, fused direct, one stream per evolution), then the fastest;
+    every step gives the fields of stepping each evolution alone."""
+    from ollin.gpu import step_auto
+    cfgs = FUSED_CFGS[:4]
+    alone = [make(c) for c in cfgs]
+    auto = [make(c) for c in cfgs]
+    used = []
+    for _ in range(8):
+        t_alone = [e.step() for e in alone]
+        t_auto, sched = step_auto(auto)
+        used.append(sched)
+        assert t_alone == t_auto
+    assert used[:6] == [0, 0, 1, 1, 2, 2]
+    assert used[6] == used[7] and used[6] in (0, 1, 2)
+    for cfg, a, b in zip(cfgs, alone, auto):
+        for lev in a.levels():
+            for nm in field_list(cfg):
+                assert np.array_equal(a.download(lev, nm), b.download(lev, nm)), (lev, nm)

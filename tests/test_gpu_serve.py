@@ -32,7 +32,10 @@ def submit_all(s, reqs, ids=None):
         s.submit(k if ids is None else ids[k], params(cfg), t_end, col, me)
 
 
-def test_each_result_is_the_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("fused", [False, True], ids=["streams", "fused_ticks"])
+def test_each_result_is_the_same_alone_and_in_the_mix(fused):
+    """Alone versus in the mix, with each evolution on its own stream or with
+    every tick one fused step of all running evolutions."""
     from ollin.gpu import Server
     alone = {}
     for k, req in enumerate(MIX):
@@ -42,7 +45,7 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         assert r.status == 0, (k, r.status)
         alone[k] = r
         s.close()
-    s = Server(1 << 36, max_active=len(MIX))
+    s = Server(1 << 36, max_active=len(MIX), fused=fused)
     submit_all(s, MIX)
     mixed = {r.id: r for r in s.drain()}
     assert sorted(mixed) == list(range(len(MIX)))
@@ -111,16 +114,18 @@ def test_collapse_threshold_stops_early():
     assert out[1].steps == int(np.ceil(0.8 / (0.25 * 0.4) - 1e-9))
 
 
-def test_a_failing_request_ends_alone():
+@pytest.mark.parametrize("fused", [False, True], ids=["streams", "fused_ticks"])
+def test_a_failing_request_ends_alone(fused):
     """An unstable Courant factor (dtfac = 3) makes the evolution overflow
     within a few steps: its request ends with OLLIN_ENAN, and the request
-    running beside it is unaffected."""
+    running beside it (in the same fused steps, with fused ticks) is
+    unaffected."""
     from ollin.gpu import Server
     good = (dict(C1, nrtotal=32, nztotal=32, nl0=1), 0, 0.5, 0.0)
     s = Server(1 << 36, max_active=1)
     submit_all(s, [good])
     (alone,) = s.drain()
-    s = Server(1 << 36, max_active=4)
+    s = Server(1 << 36, max_active=4, fused=fused)
     submit_all(s, [(dict(C1, nrtotal=24, nztotal=24, nl0=0, dtfac=3.0), 0, 5.0, 0.0), good])
     out = {r.id: r for r in s.drain()}
     assert out[0].status == 3 and 0 < out[0].steps < 10
