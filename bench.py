@@ -443,6 +443,29 @@ def elliptic_precision():
     return out
 
 
+def ceiling_rate(cfg, size=1024, levels=3, steps=2):
+    """Point-updates/s of one large evolution of ``cfg``'s physics alone
+    (size^2 x levels, one untimed coarse step, then ``steps`` timed): a grid
+    that large fills the device, so its rate is the ceiling any batch of that
+    physics can reach."""
+    from ollin.gpu import Evolution
+    from ollin.params import params_from_dict
+    c = dict(cfg, nrtotal=size, nztotal=size, nl0=levels - 1, dr0=cfg["dr0"] * cfg["nrtotal"] / size,
+             dz0=cfg["dz0"] * cfg["nztotal"] / size)
+    e = Evolution(params_from_dict(c))
+    e.initial_data()
+    e.initialize()
+    e.step()
+    p0 = e.point_updates()
+    t = time.perf_counter()
+    for _ in range(steps):
+        e.step()
+    dt = time.perf_counter() - t
+    rate = (e.point_updates() - p0) / dt
+    e.close()
+    return rate
+
+
 def c4_configs(n, seed):
     """The batching configuration's seeded mix: massless scalar-field shells
     phi = a exp(-(r - 5)^2) (r0 = 5, s = 1), a log-uniform in [0.01, 0.1],
@@ -530,9 +553,9 @@ def batch_throughput(n=256, steps=1, seed=7):
     t_plain = np.array(t_plain)
     pu = float(sum(pu_plain))
     rate_plain = np.array(pu_plain) / t_plain
-    # the FP64 ceiling of this physics (no shift, scalar field): the rate of
-    # the mix's largest evolutions stepped alone, which fill the device
-    ceiling = float(np.max(rate_plain))
+    # the ceiling of this physics (scalar field, no shift): one large shell
+    # evolution alone (1024^2 x 3 levels) fills the device
+    ceiling = ceiling_rate(cfgs[0])
     bound = float(t_plain.sum()) / (pu / ceiling)
     return {"workload": "%d massless scalar shells (a log-uniform in [0.01, 0.1], seeded), 64^2-512^2 per level x 2-5 "
                         "levels, elliptic data by the mixed solver; t_end cut to %d coarse step(s) per run"
@@ -550,7 +573,7 @@ def batch_throughput(n=256, steps=1, seed=7):
             "plain_rate_p50": float(np.percentile(rate_plain, 50)),
             "setup_seconds_per_run": t_setup / n,
             "ceiling_point_updates_per_s": ceiling,
-            "ceiling_note": "the fastest plain run of the mix (a large evolution alone fills the device)",
+            "ceiling_note": "one scalar shell of 1024^2 x 3 levels stepped alone",
             "speedup_bound_from_plain_occupancy": bound,
             "identical_results": bool(same)}
 
@@ -667,10 +690,12 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
     t_fus, fus = closed(64, fused=True)
     pu = sum(r.point_updates for r in plain.values())
     step_time = sum(plain[k].t_done - plain[k].t_ready for k in range(n))
-    # the ceiling: the fastest request of the mix stepped alone (a large grid
-    # fills the device); batching cannot beat it on average
-    ceiling = max(plain[k].point_updates / max(plain[k].t_done - plain[k].t_ready, 1e-9) for k in range(n))
-    bound = step_time / (pu / ceiling)
+    # the ceiling of each request type: one large evolution of its physics
+    # alone (1024^2 x 3 levels); batched time >= sum over requests of their
+    # point-updates at their type's ceiling
+    ceil = {kd: ceiling_rate(next(c for k2, c, _ in reqs if k2 == kd)) for kd in sorted(set(k for k, _, _ in reqs))}
+    t_min = sum(plain[k].point_updates / ceil[reqs[k][0]] for k in range(n))
+    bound = step_time / t_min
     # the small end of the mix alone: 32 punctures of 3 levels of 64^2 (the
     # plain-method configuration's grids), where one evolution fills a few
     # SMs and the plain path is bound by kernel latency
@@ -731,8 +756,8 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
             "batched_direct_launch_runs_per_s": n / t_direct,
             "fused_ticks_runs_per_s": n / t_fus, "fused_ticks_vs_plain": t_plain / t_fus,
             "plain_point_updates_per_s": pu / t_plain, "batched_point_updates_per_s": pu / t_bat,
-            "ceiling_point_updates_per_s": ceiling,
-            "ceiling_note": "the fastest request of the plain run, stepped alone",
+            "ceiling_point_updates_per_s": {["puncture", "brill", "shell"][k]: v for k, v in ceil.items()},
+            "ceiling_note": "one evolution of each request type's physics, 1024^2 x 3 levels, stepped alone",
             "speedup_bound_from_plain_occupancy": bound,
             "small_grids": {"workload": "32 Schwarzschild punctures, 3 levels of 64^2, t_end 2 (40 coarse steps)",
                             "plain_runs_per_s": 32 / t_sp, "batched_runs_per_s": 32 / t_sb,
@@ -744,6 +769,63 @@ def serving(n=24, chain=4, seed=11, budget=150e9, load=0.8, work=1.5e9):
             "plain_service": {"p50_s": float(np.percentile(svc, 50)), "p99_s": float(np.percentile(svc, 99)),
                               "setup_share": float(setup.sum() / svc.sum())},
             "bisection_bracket": [lo, hi], "all_ok": bool(ok), "identical_results": bool(same)}
+
+
+OP_NAMES = ["DFMA", "DADD", "DMUL", "DDIV", "sqrt", "cbrt", "exp", "log", "FFMA (FP32)"]
+
+
+def probe(args):
+    """Stand-alone measurements behind the committed profile summaries:
+    ``fp64`` prints the operation-rate table (ollin_gpu_op_rate);
+    ``norms`` runs ollin_gpu_norms on the lapse of one 1024x1024
+    Schwarzschild level five times (the launches an ncu capture of
+    norms_partial_kernel selects from); ``rhs-shapes`` rebuilds rhs.cu for
+    several launch shapes and register budgets (threads per block, blocks per
+    SM of __launch_bounds__), links each with the other objects and times the
+    6-level step with each library."""
+    if args.probe == "rhs-shapes":
+        from ollin import build as B
+        B.build()
+        objs = [os.path.join(B.BUILD, os.path.splitext(x)[0] + ".o") for x in B.SOURCES if x != "rhs.cu"]
+        out = {}
+        for thr, mb in [(128, 3), (128, 2), (64, 4), (64, 5), (256, 1)]:
+            tag = "%d_%d" % (thr, mb)
+            obj = os.path.join(B.BUILD, "rhs_%s.o" % tag)
+            lib = os.path.join(B.BUILD, "libollin_gpu_rhs_%s.so" % tag)
+            subprocess.run([B.nvcc()] + B.ARCH + B.COMMON + ["-DOLLIN_RHS_THREADS=%d" % thr,
+                            "-DOLLIN_RHS_MINBLOCKS=%d" % mb, "-c", os.path.join(B.CSRC, "rhs.cu"), "-o", obj],
+                           check=True)
+            subprocess.run([B.nvcc()] + B.ARCH + ["-shared", "-o", lib] + objs + [obj, "-lcudart"], check=True)
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--steps", "6", "--warmup", "3",
+                                "--no-elliptic", "--no-batch", "--no-serve", "--no-cpu-baseline"],
+                               env=dict(os.environ, OLLIN_GPU_LIB=lib), capture_output=True, text=True)
+            if r.returncode != 0:
+                out[tag] = {"error": r.stderr[-400:]}
+                continue
+            d = json.loads(r.stdout.strip().splitlines()[-1])
+            out[tag] = {"threads": thr, "min_blocks": mb, "ms_per_step": d["ms_per_step"],
+                        "rhs_avg_launch_ms": d["roofline"]["rhs_avg_launch_ms"], "clocks": d["clocks"]}
+        print(json.dumps({"probe": "rhs-shapes", "shapes": out}))
+        return
+    import torch
+    from ollin.gpu import Evolution, load
+    from ollin.params import params_from_dict
+    L = load()
+    L.ollin_gpu_op_rate.argtypes = [ctypes.c_int]
+    L.ollin_gpu_op_rate.restype = ctypes.c_double
+    if args.probe == "fp64":
+        rates = {nm: L.ollin_gpu_op_rate(k) for k, nm in enumerate(OP_NAMES)}
+        dfma = rates["DFMA"]
+        print(json.dumps({"probe": "fp64", "ops_per_s": rates,
+                          "cost_vs_dfma": {nm: dfma / v if v > 0 else None for nm, v in rates.items()}}))
+    else:
+        e = Evolution(params_from_dict(dict(WORKLOAD, nl0=0, nrtotal=1024, nztotal=1024, shift="none")))
+        e.initial_data()
+        e.initialize()
+        out = [e.norms(0, "alpha") for _ in range(5)]
+        torch.cuda.synchronize()
+        e.close()
+        print(json.dumps({"probe": "norms", "alpha_norms": [float(x) for x in out[-1]]}))
 
 
 def main():
@@ -759,7 +841,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the request-loop measurement")
     ap.add_argument("--levels", type=int, default=6, help="box-in-box levels (profiling a smaller case)")
     ap.add_argument("--size", type=int, default=512, help="points per level per direction")
-    ap.add_argument("--probe", choices=["fp64", "norms"], default=None,
+    ap.add_argument("--probe", choices=["fp64", "norms", "rhs-shapes"], default=None,
                     help="print a stand-alone measurement (operation rates, or the norms launches) and exit")
     args = ap.parse_args()
     WORKLOAD.update(nl0=args.levels - 1, nrtotal=args.size, nztotal=args.size)
