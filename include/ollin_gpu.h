@@ -58,6 +58,8 @@ extern "C" {
 #define OLLIN_SHIFT_ZERO        1   /* shift = "zero"         */
 #define OLLIN_SHIFT_STATIC      2   /* shift = "static"       */
 #define OLLIN_SHIFT_GAMMADRIVER2 3  /* shift = "Gammadriver2" */
+#define OLLIN_SHIFT_GAMMADRIVER1 4  /* shift = "Gammadriver1": d_t beta = csi Delta - eta beta */
+#define OLLIN_SHIFT_GAMMADRIVER0 5  /* shift = "Gammadriver0": d_t beta = csi d_t Delta */
 
 #define OLLIN_BOUND_RADIATIVE   0   /* boundtype = "radiative" */
 #define OLLIN_BOUND_NONE        1   /* boundtype = "none"      */

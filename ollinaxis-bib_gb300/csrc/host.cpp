@@ -174,8 +174,9 @@ int check_params(const ollin_params& P) {
     if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
     if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
-    if (P.shift != OLLIN_SHIFT_NONE && P.shift != OLLIN_SHIFT_GAMMADRIVER2)
-        return fail(OLLIN_EINVAL, "shift must be none or Gammadriver2");
+    if (P.shift != OLLIN_SHIFT_NONE && P.shift != OLLIN_SHIFT_GAMMADRIVER2 && P.shift != OLLIN_SHIFT_GAMMADRIVER1 &&
+        P.shift != OLLIN_SHIFT_GAMMADRIVER0)
+        return fail(OLLIN_EINVAL, "shift must be none, Gammadriver0, Gammadriver1 or Gammadriver2");
     if (P.slicing < 0 || P.slicing > OLLIN_SLICING_MAXIMAL) return fail(OLLIN_EINVAL, "unknown slicing");
     if (P.ilapse < OLLIN_ILAPSE_ONE || P.ilapse > OLLIN_ILAPSE_MAXIMAL) return fail(OLLIN_EINVAL, "unknown ilapse");
     if (P.integrator != OLLIN_INTEGRATOR_RK4 && P.integrator != OLLIN_INTEGRATOR_ICN) return fail(OLLIN_EINVAL, "unknown integrator");
@@ -333,7 +334,9 @@ PhysParams make_phys(const ollin_params& P) {
     PhysParams q{};
     q.slicing = P.slicing;
     q.gauge_f = P.gauge_f;
-    q.shift = P.shift == OLLIN_SHIFT_GAMMADRIVER2 ? 1 : 0;
+    q.shift = (P.shift == OLLIN_SHIFT_GAMMADRIVER2 || P.shift == OLLIN_SHIFT_GAMMADRIVER1 ||
+               P.shift == OLLIN_SHIFT_GAMMADRIVER0) ? 1 : 0;
+    q.driver = P.shift == OLLIN_SHIFT_GAMMADRIVER1 ? 1 : P.shift == OLLIN_SHIFT_GAMMADRIVER0 ? 0 : 2;
     q.shiftadvect = P.shiftadvect;
     q.driveradv = P.driveradv;
     q.drivercsi = P.drivercsi;
@@ -2145,7 +2148,8 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
     auto* h = new ollin_handle();
     h->P = *p;
     h->g = 3;
-    h->shift = p->shift == OLLIN_SHIFT_GAMMADRIVER2;
+    h->shift = p->shift == OLLIN_SHIFT_GAMMADRIVER2 || p->shift == OLLIN_SHIFT_GAMMADRIVER1 ||
+               p->shift == OLLIN_SHIFT_GAMMADRIVER0;
     h->scalar = p->mattertype == OLLIN_MATTER_SCALAR;
     h->phys = make_phys(*p);
     parity_table(h);
@@ -2352,7 +2356,7 @@ int ollin_gpu_initialize(ollin_handle* h) {
         int rc = do_aux(h, h->L[l], h->L[l].cur, h->t[l] == 0.0);
         if (rc) return rc;
     }
-    if (h->shift) {  // evolve.f90:174-195
+    if (h->P.shift == OLLIN_SHIFT_GAMMADRIVER2) {  // evolve.f90:174-195
         for (int l = 0; l < h->nlev; ++l) {
             DLevel& L = h->L[l];
             launch_gammadriver_init(L.G, base_ptr(L, L.slot[L.cur][F_DTBETAR]), base_ptr(L, L.slot[L.cur][F_DTBETAZ]),

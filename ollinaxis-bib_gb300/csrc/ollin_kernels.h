@@ -10,7 +10,8 @@ namespace ollin {
 struct PhysParams {
     int slicing;          // OLLIN_SLICING_*
     double gauge_f;
-    int shift;            // 1 = Gammadriver2 active
+    int shift;            // 1 = a Gamma-driver shift is evolved
+    int driver;           // which: 2 Gammadriver2, 1 Gammadriver1, 0 Gammadriver0
     int shiftadvect, driveradv;
     double drivercsi, drivereta;
     double eta;           // Delta damping (momentum-constraint multiple)

@@ -326,11 +326,24 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
         s_Dlz = s_Dlz + third * (rgC * Dr_DIV_beta + gB * Dz_DIV_beta) + Dlz * tdb;
         if (bona_masso)
             s_alpha = s_alpha + ADVp(STALE && !SYNC ? A.alpha_aux + o : X[F_ALPHA] + ox, dao.r, dao.z);
-        s_br = dbr;
-        s_bz = dbz;
-        if (P.driveradv) {
+        // sources_shift.f90: Gammadriver2 d_t beta = dtbeta (:229-260),
+        // Gammadriver1 d_t beta = csi Delta - eta beta (:108-186),
+        // Gammadriver0 d_t beta = csi d_t Delta (below, after the Delta source
+        // is complete)
+        if (P.driver == 2) {
+            s_br = dbr;
+            s_bz = dbz;
+        } else if (P.driver == 1) {
+            s_br = P.drivercsi * Dlr;
+            s_bz = P.drivercsi * Dlz;
+        }
+        if (P.driveradv && P.driver != 0) {
             s_br = s_br + ADV(F_BETAR, dbR.r, dbR.z);
             s_bz = s_bz + ADV(F_BETAZ, dbZ.r, dbZ.z);
+        }
+        if (P.driver == 1) {
+            s_br = s_br - P.drivereta * br;
+            s_bz = s_bz - P.drivereta * bz;
         }
         (void)s_dbr; (void)s_dbz;
         if constexpr (SCALAR) {
@@ -407,7 +420,16 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             diss(F_SXIZ, s_sxz);
         }
     }
-    if constexpr (SHIFT) {
+    if constexpr (SHIFT) if (P.driver != 2) {
+        // dtbeta is not evolved by the first-order and parabolic drivers
+        s_dbr = 0.0;
+        s_dbz = 0.0;
+        if (P.driver == 0) {
+            s_br = P.drivercsi * s_Dlr;
+            s_bz = P.drivercsi * s_Dlz;
+        }
+    }
+    if constexpr (SHIFT) if (P.driver == 2) {
         s_dbr = P.drivercsi * s_Dlr;
         s_dbz = P.drivercsi * s_Dlz;
         if (P.driveradv) {
@@ -431,6 +453,16 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     // (radiative_geometry.f90:70-76)
     const bool maximal = P.slicing == 4;
     if (maximal) s_trK = 0.0;
+
+    // Gammadriver0's boundary in radiative_geometry.f90:203-211 zeroes the
+    // shift sources on the column i = 0 and the row j = 0 of level 0: inside
+    // the grid only where the row j = 0 is not an equator ghost row
+    if constexpr (SHIFT) {
+        if (P.driver == 0 && A.level0 && P.boundtype == 0 && P.drivercsi != 0.0 && (i == 0 || j == 0)) {
+            s_br = 0.0;
+            s_bz = 0.0;
+        }
+    }
 
     // ---- outgoing-wave boundary on the outer edges (radbound.f90)
     const bool edge_r = (i == nr), edge_z = (j == nz) || (!G.eqsym && j == 1 - g);
@@ -459,10 +491,15 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             }
             radb(F_KTC, vl, s_KTC);
             if constexpr (SHIFT) {
-                if (P.drivercsi != 0.0) {
+                if (P.drivercsi != 0.0) {  // radiative_geometry.f90:195-262
                     const double vs = sqrt(4.0 * third * P.drivercsi);
-                    radb(F_DTBETAR, vs, s_dbr);
-                    radb(F_DTBETAZ, vs, s_dbz);
+                    if (P.driver == 2) {
+                        radb(F_DTBETAR, vs, s_dbr);
+                        radb(F_DTBETAZ, vs, s_dbz);
+                    } else if (P.driver == 1) {
+                        radb(F_DLR, vs, s_Dlr);
+                        radb(F_DLZ, vs, s_Dlz);
+                    }
                 }
             }
         }

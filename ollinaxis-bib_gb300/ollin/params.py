@@ -47,7 +47,7 @@ class Params(ctypes.Structure):
 
 INTEGRATOR = {"rk4": 0, "icn": 1}
 SLICING = {"1+log": 0, "harmonic": 1, "shockavoid": 2, "static": 3, "maximal": 4}
-SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3}
+SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3, "Gammadriver1": 4, "Gammadriver0": 5}
 BOUND = {"radiative": 0, "none": 1}
 MATTER = {"vacuum": 0, "scalar": 1}
 POTENTIAL = {"none": 0, "phi2": 1, "phi4": 2}

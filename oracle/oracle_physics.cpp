@@ -1140,6 +1140,29 @@ void sources_shift(Sim& S, Level& L) {
         ALL sbeta_z(i, j) = 0.0;
         return;
     }
+    if (P.shift == OLLIN_SHIFT_GAMMADRIVER0) {  // parabolic driver (:62-85)
+        R(sDelta_r); R(sDelta_z);
+        ALL sbeta_r(i, j) = P.drivercsi * sDelta_r(i, j);
+        ALL sbeta_z(i, j) = P.drivercsi * sDelta_z(i, j);
+        ALL sdtbeta_r(i, j) = 0.0;
+        ALL sdtbeta_z(i, j) = 0.0;
+        return;
+    }
+    if (P.shift == OLLIN_SHIFT_GAMMADRIVER1) {  // first-order hyperbolic driver (:88-186)
+        R(Delta_r); R(Delta_z);
+        ALL sbeta_r(i, j) = P.drivercsi * Delta_r(i, j);
+        ALL sbeta_z(i, j) = P.drivercsi * Delta_z(i, j);
+        if (P.driveradv) {
+            R(DAr_beta_r); R(DAz_beta_r); R(DAr_beta_z); R(DAz_beta_z);
+            ALL sbeta_r(i, j) = sbeta_r(i, j) + beta_r(i, j) * DAr_beta_r(i, j) + beta_z(i, j) * DAz_beta_r(i, j);
+            ALL sbeta_z(i, j) = sbeta_z(i, j) + beta_r(i, j) * DAr_beta_z(i, j) + beta_z(i, j) * DAz_beta_z(i, j);
+        }
+        ALL sbeta_r(i, j) = sbeta_r(i, j) - P.drivereta * beta_r(i, j);
+        ALL sbeta_z(i, j) = sbeta_z(i, j) - P.drivereta * beta_z(i, j);
+        ALL sdtbeta_r(i, j) = 0.0;
+        ALL sdtbeta_z(i, j) = 0.0;
+        return;
+    }
     // Gammadriver2 (:229-306)
     ALL sbeta_r(i, j) = dtbeta_r(i, j);
     ALL sbeta_z(i, j) = dtbeta_z(i, j);
@@ -1261,6 +1284,19 @@ void radiative_geometry(Sim& S, Level& L) {
     if (!P.nolambda) {
         R(Alambda); R(sAlambda); R(Dr_Alambda); R(Dz_Alambda);
         radbound(L, Alambda, sAlambda, Dr_Alambda, Dz_Alambda, vl, var0);
+    }
+    // radiative_geometry.f90:195-262: the Gamma drivers' boundary
+    if (P.shift == OLLIN_SHIFT_GAMMADRIVER0 && P.drivercsi != 0.0) {
+        // zeroes the shift sources on the column i = 0 and the row j = 0
+        R(sbeta_r); R(sbeta_z);
+        for (int j = 1 - g; j <= Nz; ++j) { sbeta_r(0, j) = 0.0; sbeta_z(0, j) = 0.0; }
+        for (int i = 1 - g; i <= Nr; ++i) { sbeta_r(i, 0) = 0.0; sbeta_z(i, 0) = 0.0; }
+    }
+    if (P.shift == OLLIN_SHIFT_GAMMADRIVER1 && P.drivercsi != 0.0) {  // on Delta
+        R(Delta_r); R(sDelta_r); R(Dr_Delta_r); R(Dz_Delta_r);
+        R(Delta_z); R(sDelta_z); R(Dr_Delta_z); R(Dz_Delta_z);
+        radbound(L, Delta_r, sDelta_r, Dr_Delta_r, Dz_Delta_r, vs, var0);
+        radbound(L, Delta_z, sDelta_z, Dr_Delta_z, Dz_Delta_z, vs, var0);
     }
     if (P.shift == OLLIN_SHIFT_GAMMADRIVER2 && P.drivercsi != 0.0) {
         R(dtbeta_r); R(sdtbeta_r); R(Dr_dtbeta_r); R(Dz_dtbeta_r);

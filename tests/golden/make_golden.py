@@ -37,6 +37,16 @@ CASES = {
     # same with the Gamma-driver shift, 3 levels
     "c2_small": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver2",
                      drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # the first-order hyperbolic and the parabolic Gamma drivers
+    # (sources_shift.f90:62-186, radiative_geometry.f90:195-235); the
+    # parabolic one without equatorial symmetry, where the row j = 0 whose
+    # shift sources the reference zeroes is an ordinary row
+    "gd1_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver1",
+                      drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # (a small csi: the parabolic driver is an explicit diffusion of the
+    # shift, stable for csi dt/dr^2 below about 0.7)
+    "gd0_noeqsym": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.25, dz0=0.25, eqsym=False,
+                        shift="Gammadriver0", drivercsi=0.1, _steps=[0, 1, 3]),
     # ICN with harmonic slicing and the isotropic lapse, one level
     "icn_harmonic": dict(BASE, nrtotal=16, nztotal=20, nl0=0, dr0=0.25, dz0=0.25, integrator="icn",
                          icniter=3, slicing="harmonic", gauge_f=1.0, ilapse="isotropic", _steps=[0, 1, 3]),

@@ -171,6 +171,19 @@ def test_gammadriver_shift_three_levels():
     run(cfg, 12, check_every=4)
 
 
+@pytest.mark.parametrize("cfg", [
+    dict(C1, nrtotal=32, nztotal=32, shift="Gammadriver1", drivercsi=0.75, drivereta=2.0),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, dr0=0.25, dz0=0.25, eqsym=0, shift="Gammadriver0", drivercsi=0.1),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="Gammadriver1", drivercsi=0.75, drivereta=1.0, driveradv=1),
+], ids=["gammadriver1_three_levels", "gammadriver0_no_eqsym", "gammadriver1_driveradv"])
+def test_first_order_and_parabolic_gamma_drivers(cfg):
+    """sources_shift.f90:62-186 (d_t beta = csi Delta - eta beta, or
+    csi d_t Delta) with the matching boundaries of radiative_geometry.f90:
+    195-235 (radiative Delta sources; the parabolic driver's zeroed row
+    j = 0, an ordinary row without equatorial symmetry)."""
+    run(cfg, 8, check_every=4)
+
+
 def test_icn_harmonic_isotropic():
     cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
                gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)

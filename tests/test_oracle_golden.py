@@ -12,7 +12,7 @@ from parity_util import params, scalar_pulse
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["c1_small", "c2_small", "icn_harmonic", "scalar_shift", "noeqsym_shift", "box_two", "box_ring_shift",
-         "box_overlap"]
+         "box_overlap", "gd1_shift", "gd0_noeqsym"]
 
 # The oracle restates the reference statement by statement; the remaining
 # differences come from libm (exp/log/pow) last-bit differences amplified by

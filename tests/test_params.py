@@ -36,7 +36,7 @@ def test_par_file_values():
 
 def test_unknown_values_are_refused():
     with pytest.raises(ValueError):
-        params_from_par("shift = Gammadriver1\n")
+        params_from_par("shift = Gammadrivershock2\n")
     with pytest.raises(ValueError):
         params_from_par("nosuchparameter = 3\n")
 
@@ -50,3 +50,9 @@ def test_refinement_box_parameters():
     assert list(p.nrbox) == [12, 1, 1] and list(p.nzbox) == [14, 1, 1]
     assert list(p.rbox) == [0.0, 8.0, 0.0] and list(p.zbox) == [6.0, 0.0, 0.0]
     assert p.slicing == SLICING["maximal"]
+
+
+def test_gamma_driver_names():
+    """shift = Gammadriver0 / 1 / 2 (param.f90 names, sources_shift.f90)."""
+    for name, code in (("Gammadriver0", 5), ("Gammadriver1", 4), ("Gammadriver2", 3)):
+        assert params_from_par("shift = %s\n" % name).shift == code
