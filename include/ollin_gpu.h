@@ -41,6 +41,7 @@ extern "C" {
 #define OLLIN_ENAN          3   /* a non-finite value was detected in the state */
 #define OLLIN_ENOMEM        4   /* device allocation failed */
 #define OLLIN_ESTATE        5   /* call out of order (e.g. step before initialize) */
+#define OLLIN_ECONV         6   /* an iterative solve ("mixed", "fp64mg") stopped above its tolerance */
 
 /* ---- enumerated parameter values (param.f90 character parameters) ---- */
 #define OLLIN_INTEGRATOR_RK4    0   /* integrator = "rk4" */
@@ -60,6 +61,10 @@ extern "C" {
 #define OLLIN_SHIFT_GAMMADRIVER2 3  /* shift = "Gammadriver2" */
 #define OLLIN_SHIFT_GAMMADRIVER1 4  /* shift = "Gammadriver1": d_t beta = csi Delta - eta beta */
 #define OLLIN_SHIFT_GAMMADRIVER0 5  /* shift = "Gammadriver0": d_t beta = csi d_t Delta */
+#define OLLIN_SHIFT_GAMMADRIVERSHOCK1 6  /* shift = "Gammadrivershock1": d_t beta = csi fdriver Delta - eta beta,
+                                          * d_t fdriver = -2/3 fdriver DIV beta */
+#define OLLIN_SHIFT_GAMMADRIVERSHOCK2 7  /* shift = "Gammadrivershock2": d_t dtbeta = csi d_t (fdriver Delta)
+                                          * - eta dtbeta */
 
 #define OLLIN_BOUND_RADIATIVE   0   /* boundtype = "radiative" */
 #define OLLIN_BOUND_NONE        1   /* boundtype = "none"      */
@@ -108,14 +113,14 @@ typedef struct ollin_params {
     /* grid: param.f90:95-141 */
     int    nrtotal, nztotal;   /* Nrtotal, Nztotal: points per level (without ghosts) */
     int    nl0;                /* Nl0: refinement levels above the base grid */
-    int    ghost;              /* 0 = from order (3 for order four) */
+    int    ghost;              /* 0 = from order (2 for order two, 3 for order four); no other value */
     int    eqsym;              /* equatorial symmetry */
     double dr0, dz0;           /* base-grid spacing */
     double dtfac;              /* dt0 = dtfac*min(dr0,dz0) (setupboxes.f90:119) */
     /* time integration: param.f90:410-427 */
     int    integrator;         /* OLLIN_INTEGRATOR_* */
     int    icniter;
-    int    order;              /* 4 ("four"); 2 is rejected */
+    int    order;              /* 2 ("two", the reference's default) or 4 ("four") */
     /* formulation: param.f90:407-438 */
     int    slicing;            /* OLLIN_SLICING_* */
     double gauge_f;
@@ -159,6 +164,9 @@ typedef struct ollin_params {
     int    nl[3];              /* Nl1, Nl2, Nl3 */
     int    nrbox[3], nzbox[3]; /* Nrbox1..3, Nzbox1..3 */
     double rbox[3], zbox[3];   /* rbox1..3, zbox1..3 (before the alignment of setupboxes.f90:186-206) */
+    /* shift options (appended; param.f90:325-352) */
+    int    driverD0;           /* subtract the t = 0 Delta in the driver equations */
+    double shiftafter;         /* shift sources zero while t(box 0, level 0) < shiftafter */
 } ollin_params;
 
 /* Evolved and auxiliary fields addressable by upload/download.  The names are
@@ -171,6 +179,7 @@ enum ollin_field {
     OLLIN_F_LAMBDA, OLLIN_F_ALAMBDA,
     OLLIN_F_BETA_R, OLLIN_F_BETA_Z, OLLIN_F_DTBETA_R, OLLIN_F_DTBETA_Z,
     OLLIN_F_SCALAR_PHI, OLLIN_F_SCALAR_XI_R, OLLIN_F_SCALAR_XI_Z, OLLIN_F_SCALAR_PI,
+    OLLIN_F_FDRIVER,                      /* evolved by the shock-avoiding drivers (else 1) */
     OLLIN_F_NEVOLVED,                     /* number of evolved-field slots */
     /* derived (read-only) fields, computed on request */
     OLLIN_F_HAM = 64, OLLIN_F_MOM_R, OLLIN_F_MOM_Z,
@@ -186,6 +195,7 @@ typedef struct ollin_level_desc {
     double time;                    /* t(box,level) */
     int    steps;                   /* s(box,level) */
     int    box;                     /* refinement box (appended) */
+    double rbox, zbox;              /* the box centre after setupboxes.f90:186-206 (appended) */
 } ollin_level_desc;
 
 typedef struct ollin_handle ollin_handle;
@@ -207,10 +217,25 @@ void ollin_gpu_destroy(ollin_handle* h);
 int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out);
 int ollin_gpu_num_levels(const ollin_handle* h);
 
+/* The grid's coordinates r(i) for i = 1-ghost..Nr into r[0..Nr+ghost-1] and
+ * z(j) into z[0..Nz+ghost-1], the values of evolve.f90:42-70 that the
+ * kernels use (the reference's r(i,j) is r(i) on every row). */
+int ollin_gpu_coords(const ollin_handle* h, int level, double* r, double* z);
+
 /* Host <-> device copies of one grid function of one level.
  * Replaces direct access to grid(0,level)%<field> (generated mytypes.f90). */
 int ollin_gpu_upload(ollin_handle* h, int level, int field, const double* a, int ld_r);
 int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r);
+
+/* The value of ``field`` at n arbitrary points of grid ``level``: rz holds
+ * (r0, z0) pairs, out receives n values (host arrays).  Replaces
+ * ``interp(box,level,r0,z0,flag)`` (src/base/interp.f90:2-270: a node is
+ * copied, bicubic Lagrange inside, bilinear within one cell of the grid's
+ * edge, or bilinear everywhere for interporder = "bilinear"), as the
+ * diagonal output of save1Ddata.f90:624-750 and a horizon finder call it.
+ * A point whose stencil would leave the grid gets NaN and the call returns
+ * OLLIN_EINVAL. */
+int ollin_gpu_interp(ollin_handle* h, int level, int field, const double* rz, int n, double* out);
 
 /* Host-side initial data for the supported ``idata`` values, uploaded to
  * every level.  Replaces: call initial (src/base/evolve.f90:124,
@@ -387,6 +412,15 @@ int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
  * of that solve.  No counterpart call in the reference, which prints these
  * numbers. */
 int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres);
+
+/* The convergence history of the last "mixed" or "fp64mg" solve (initial
+ * data or maximal slicing) on ``level``: the larger of the RMS residuals of
+ * the interior equations and of the Robin rows (level 0), before each
+ * correction and after the last one, up to ``max``
+ * values into ``rms``; ``*n`` receives the full count (0 before any such
+ * solve).  A non-finite residual ends that solve with OLLIN_ENAN.  No
+ * counterpart call in the reference. */
+int ollin_gpu_ell_history(const ollin_handle* h, int level, double* rms, int max, int* n);
 
 /* Total point-updates performed by this handle so far (interior points of
  * each level times the steps taken on it). */

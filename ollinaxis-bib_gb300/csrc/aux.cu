@@ -67,14 +67,17 @@ __device__ __forceinline__ void aux_deriv_body(const AuxArgs& a, unsigned bx, un
     if (i > G.nr || j > G.nz) return;
     const long ld = G.ld;
     const size_t o = (size_t)i + (size_t)j * (size_t)ld;
-    const int kr = pclass(i, G.nr, G.g), kz = pclass(j, G.nz, G.g);
-    const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
+    const int ord = G.order;
+    const int kr = pclass_o(ord, i, G.nr, G.g), kz = pclass_o(ord, j, G.nz, G.g);
+    const double cr1 = c1_o(ord, G.idr), cz1 = c1_o(ord, G.idz);
     const double r = G.rcol[i];
-    const bool rg = i < 1;  // a ghost column of a grid off the axis
-    const double Dr_gA = rg ? 0.0 : d1(a.aux[X_GA] + o, 1, kr, cr1);
-    const double Dz_gB = d1(a.aux[X_GB] + o, ld, kz, cz1);
-    const double Dr_gC = rg ? 0.0 : d1(a.aux[X_GC] + o, 1, kr, cr1);
-    const double Dz_gC = d1(a.aux[X_GC] + o, ld, kz, cz1);
+    // a ghost column of a grid off the axis that diff1r leaves unset (all of
+    // them in order four, the outermost in order two)
+    const bool rg = i < d1r_first(ord, G.g);
+    const double Dr_gA = rg ? 0.0 : d1_o(ord, a.aux[X_GA] + o, 1, kr, cr1);
+    const double Dz_gB = d1_o(ord, a.aux[X_GB] + o, ld, kz, cz1);
+    const double Dr_gC = rg ? 0.0 : d1_o(ord, a.aux[X_GC] + o, 1, kr, cr1);
+    const double Dz_gC = d1_o(ord, a.aux[X_GC] + o, ld, kz, cz1);
     const double glam = a.aux[X_GLAM][o], gC = a.aux[X_GC][o];
     const double ddr = -Dr_gA - r * Dz_gC - r * glam;
     const double ddz = -Dr_gC * r - Dz_gB - 2.0 * gC;
@@ -87,6 +90,10 @@ __device__ __forceinline__ void aux_deriv_body(const AuxArgs& a, unsigned bx, un
     if (a.t0) {
         a.st[F_DLR][o] = ddr;
         a.st[F_DLZ][o] = ddz;
+        if (a.d0r) {
+            a.d0r[o] = ddr;
+            a.d0z[o] = ddz;
+        }
     }
 }
 

@@ -39,20 +39,21 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_c
         const size_t o = (size_t)i + (size_t)j * ld, om = (size_t)mi + (size_t)mj * ld;
         const double* u = A.u_in + om;
         const double* v = A.v_in + om;
-        const int pcr = pclass(mi, nr, g), pcz = pclass(mj, nz, g);
-        const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
-        const double cr2 = G.idr * G.idr * (1.0 / 12.0), cz2 = G.idz * G.idz * (1.0 / 12.0);
+        const int ord = G.order;
+        const int pcr = pclass_o(ord, mi, nr, g), pcz = pclass_o(ord, mj, nz, g);
+        const double cr1 = c1_o(ord, G.idr), cz1 = c1_o(ord, G.idz);
+        const double cr2 = c2_o(ord, G.idr), cz2 = c2_o(ord, G.idz);
         double s;
         if constexpr (!PHYS) {
             // flat Laplacian in (r, z) with the axis term (wave_elliptic.f90:593-597)
-            s = (d2(u, 1, pcr, cr2) + d2(u, ld, pcz, cz2)) + d1(u, 1, pcr, cr1) * G.ircol[mi];
+            s = (d2_o(ord, u, 1, pcr, cr2) + d2_o(ord, u, ld, pcz, cz2)) + d1_o(ord, u, 1, pcr, cr1) * G.ircol[mi];
         } else {
             // physical Laplacian of the conformal metric (wave_elliptic.f90:
             // 781-812); the hdet terms vanish (hdet = 1)
             const WavePhys& q = A.ph;
-            const double ur = d1(u, 1, pcr, cr1), uz = d1(u, ld, pcz, cz1);
-            const double urr = d2(u, 1, pcr, cr2), uzz = d2(u, ld, pcz, cz2);
-            const double urz = d2rz(u, ld, mi, mj, nr, nz, g, G.idr * G.idz);
+            const double ur = d1_o(ord, u, 1, pcr, cr1), uz = d1_o(ord, u, ld, pcz, cz1);
+            const double urr = d2_o(ord, u, 1, pcr, cr2), uzz = d2_o(ord, u, ld, pcz, cz2);
+            const double urz = d2rz_o(ord, u, ld, mi, mj, nr, nz, g, G.idr * G.idz);
             const double gA = q.gA[om], gB = q.gB[om], gC = q.gC[om];
             const double r = G.rcol[mi], rgC = r * gC;
             s = gA * urr + gB * uzz + ((2.0 * r) * gC) * urz;
@@ -67,14 +68,22 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_c
         u5 = u5 * uc;
         s = s + ld_(A.S1 + om) * uc + ld_(A.S5 + om) * u5 - ld_(A.S0 + om);
         s = s - A.eta * ld_(v);
-        // Kreiss-Oliger dissipation on v (dissipation.f90:196-211)
-        const bool diss_r = (mi >= 4 - g && mi <= nr - 3), diss_z = (mj >= 4 - g && mj <= nz - 3);
-        const double kd = A.kdiss * (1.0 / 20.0);
-        if (diss_r && diss_z) {
-            s = ko6rz_apply(v, ld, kd, s);
+        // Kreiss-Oliger dissipation on v (dissipation.f90:196-211; order two
+        // :121-135)
+        if (ord == 2) {
+            const bool diss_r = (mi >= 3 - g && mi <= nr - 2), diss_z = (mj >= 3 - g && mj <= nz - 2);
+            const double kd = A.kdiss * (1.0 / 6.0);
+            if (diss_r) s = s - kd * ko4(v, 1);
+            if (diss_z) s = s - kd * ko4(v, ld);
         } else {
-            if (diss_r) s = s - kd * ko6(v, 1);
-            if (diss_z) s = s - kd * ko6(v, ld);
+            const bool diss_r = (mi >= 4 - g && mi <= nr - 3), diss_z = (mj >= 4 - g && mj <= nz - 3);
+            const double kd = A.kdiss * (1.0 / 20.0);
+            if (diss_r && diss_z) {
+                s = ko6rz_apply(v, ld, kd, s);
+            } else {
+                if (diss_r) s = s - kd * ko6(v, 1);
+                if (diss_z) s = s - kd * ko6(v, ld);
+            }
         }
         // radiative boundary with unit speed and zero asymptotic value
         // (radbound(1.d0, 0.d0), radbound.f90:46-70), also on the lower z
@@ -82,7 +91,7 @@ __global__ void __launch_bounds__(kWaveThreads) wave_stage_kernel(const __grid_c
         if (mi == nr || mj == nz || (!G.eqsym && mj == 1 - g)) {
             const double r = G.rcol[mi], z = G.zrow[mj];
             const double rr = sqrt(r * r + z * z);
-            s = -(r * d1(v, 1, pcr, cr1) + z * d1(v, ld, pcz, cz1) + (ld_(v) - 0.0)) / rr;
+            s = -(r * d1_o(ord, v, 1, pcr, cr1) + z * d1_o(ord, v, ld, pcz, cz1) + (ld_(v) - 0.0)) / rr;
         }
         double su = ld_(A.v_in + o);  // sell_u = ell_v
         double sv = s;
@@ -150,8 +159,9 @@ __global__ void __launch_bounds__(128) pulse_xi_kernel(const __grid_constant__ P
     const long ld = G.ld;
     const size_t o = (size_t)i + (size_t)j * ld;
     const double* f = a.sphi + o;
-    a.xir[o] = i < 1 ? 0.0 : d1(f, 1, pclass(i, G.nr, G.g), G.idr * (1.0 / 12.0));
-    a.xiz[o] = d1(f, ld, pclass(j, G.nz, G.g), G.idz * (1.0 / 12.0));
+    const int ord = G.order;
+    a.xir[o] = i < d1r_first(ord, G.g) ? 0.0 : d1_o(ord, f, 1, pclass_o(ord, i, G.nr, G.g), c1_o(ord, G.idr));
+    a.xiz[o] = d1_o(ord, f, ld, pclass_o(ord, j, G.nz, G.g), c1_o(ord, G.idz));
 }
 
 // idata_scalarpulse.f90:152-170 and potential.f90 at every point
@@ -390,7 +400,8 @@ __global__ void __launch_bounds__(kMaxThreads) max_coeff_kernel(const __grid_con
         // a ghost column of a grid off the axis keeps r derivatives of zero
         // (diff1r leaves them unset there); ghost rows of a grid that does
         // not own the equator take the one-sided z stencils
-        const bool gr = G.axis && i < 1, gz = G.equator && j < 1, r0 = !G.axis && i < 1;
+        const int ord = G.order;
+        const bool gr = G.axis && i < 1, gz = G.equator && j < 1, r0 = !G.axis && i < d1r_first(ord, g);
         const int mi = gr ? 1 - i : i, mj = gz ? 1 - j : j;
         const size_t o = (size_t)i + (size_t)j * ld, om = (size_t)mi + (size_t)mj * ld;
         // the arrays the derivatives are taken from: the live ones, or after
@@ -405,8 +416,9 @@ __global__ void __launch_bounds__(kMaxThreads) max_coeff_kernel(const __grid_con
             for (int k = 0; k < 5; ++k) src[k] = m >= 0 ? A.xb[k] : A.xa[k];
             if (m >= 0) { os = (size_t)m; lds = A.xb_ld; xin = true; }
         }
-        const int pcr = xin ? 0 : pclass(mi, nr, g), pcz = xin ? 0 : pclass(mj, nz, g);
-        const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
+        const int pcr = xin ? 0 : pclass_o(ord, mi, nr, g), pcz = xin ? 0 : pclass_o(ord, mj, nz, g);
+        const double cr1 = c1_o(ord, G.idr), cz1 = c1_o(ord, G.idz);
+        auto d1 = [ord](const double* f, long st, int k, double c) { return d1_o(ord, f, st, k, c); };
         // parities: g_A, g_B, phi, chi even in r and z; g_C even in r, odd in z
         const double er = gr ? -1.0 : 1.0;  // r derivative of an r-even function
         const double ez = gz ? -1.0 : 1.0;  // z derivative of a z-even function
@@ -605,51 +617,128 @@ __device__ __forceinline__ void block_partial(double v, double* out) {
     if (t == 0) out[blockIdx.y * gridDim.x + blockIdx.x] = red[0];
 }
 
-// FP64 residual r = -R(u) at every unknown (zero on Dirichlet rows), its FP32
-// copy, d = 0, and per-block sums over the interior equations of r^2 (into
-// partial[b]) and of (e u)^2, the scale of the equation (partial[nblocks+b]).
-__global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_constant__ MixArgs A) {
+// A sum of products c*u kept as an unevaluated pair (s, e): each product's
+// rounding error from an FMA and each addition's from TwoSum (Knuth; Ogita,
+// Rump and Oishi's Dot2), so the rounded total is good to about one unit of
+// its own last place however much the terms cancel.  With EXACT false it is
+// the plain FP64 sum.
+template <bool EXACT>
+struct RowSum {
+    double s = 0.0, e = 0.0;
+    __device__ __forceinline__ void prod(double c, double u) {
+        if constexpr (EXACT) {
+            const double p = __dmul_rn(c, u);
+            const double ep = __fma_rn(c, u, -p);
+            add_exact(p);
+            e = __dadd_rn(e, ep);
+        } else {
+            s = s + c * u;
+        }
+    }
+    __device__ __forceinline__ void add(double x) {
+        if constexpr (EXACT) add_exact(x);
+        else s = s + x;
+    }
+    __device__ __forceinline__ void add_exact(double x) {
+        const double t = __dadd_rn(s, x);
+        const double bb = __dsub_rn(t, s);
+        const double err = __dadd_rn(__dsub_rn(s, __dsub_rn(t, bb)), __dsub_rn(x, bb));
+        s = t;
+        e = __dadd_rn(e, err);
+    }
+    __device__ __forceinline__ double value() const { return EXACT ? __dadd_rn(s, e) : s; }
+};
+
+// R(u) of the equation at unknown (i, j): the interior nine- or five-point
+// row, or (robin) the Robin row.  The residual (EXACT) sums the products of
+// the FP64 coefficients and unknowns without rounding loss, so the
+// refinement converges to the FP64 solution of the system itself rather
+// than to the rounding floor of its rows (about |e| ulp(u)); the operator
+// applied to a correction (!EXACT) drops the data terms f and uinf and sums
+// plainly.  Returns false on a Dirichlet row.
+template <bool EXACT, typename UF>
+__device__ __forceinline__ bool mix_row(const MixArgs& A, const UF& U, int i, int j, size_t o, double& R,
+                                        bool& interior) {
     const LevelGeom& G = A.G;
     const int nr = G.nr, nz = G.nz;
+    interior = i <= nr - 1 && j <= nz - 1;
+    RowSum<EXACT> acc;
+    if (interior) {
+        if (!A.pa) {
+            acc.prod(A.ca[i], U(i + 1, j));
+            acc.prod(A.cb[i], U(i - 1, j));
+            acc.prod(A.cc, U(i, j + 1));
+            acc.prod(A.cc, U(i, j - 1));
+        } else {
+            acc.prod(A.pa[o], U(i + 1, j));
+            acc.prod(A.pb[o], U(i - 1, j));
+            acc.prod(A.pc[o], U(i, j + 1));
+            acc.prod(A.pd[o], U(i, j - 1));
+            acc.prod(A.pg[o], U(i + 1, j + 1));
+            acc.prod(A.ph[o], U(i - 1, j - 1));
+            acc.prod(A.pi[o], U(i + 1, j - 1));
+            acc.prod(A.pj[o], U(i - 1, j + 1));
+        }
+        acc.prod(A.e64[o], U(i, j));
+        if (EXACT) acc.add(-A.f64[o]);
+        R = acc.value();
+        return true;
+    }
+    if (!A.robin) return false;
+    // (1 + 1.5 (cr + cz)) u - uinf - cr/2 (4 u_1 - u_2) - cz/2 (4 u_1 - u_2)
+    // along each outward direction; a centred difference along the edge
+    const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
+    const double hr = 0.5 * cr, hz = 0.5 * cz;
+    if (i == nr && j == nz) {
+        acc.prod(1.0 + 1.5 * (cr + cz), U(i, j));
+        acc.prod(-4.0 * hr, U(i - 1, j));
+        acc.prod(hr, U(i - 2, j));
+        acc.prod(-4.0 * hz, U(i, j - 1));
+        acc.prod(hz, U(i, j - 2));
+    } else if (i == nr) {
+        acc.prod(1.0 + 1.5 * cr, U(i, j));
+        acc.prod(-4.0 * hr, U(i - 1, j));
+        acc.prod(hr, U(i - 2, j));
+        acc.prod(hz, U(i, j + 1));
+        acc.prod(-hz, U(i, j - 1));
+    } else {
+        acc.prod(1.0 + 1.5 * cz, U(i, j));
+        acc.prod(-4.0 * hz, U(i, j - 1));
+        acc.prod(hz, U(i, j - 2));
+        acc.prod(hr, U(i + 1, j));
+        acc.prod(-hr, U(i - 1, j));
+    }
+    if (EXACT) acc.add(-A.uinf);
+    R = acc.value();
+    return true;
+}
+
+// FP64 residual r = -R(u) at every unknown (zero on Dirichlet rows): into r64
+// when set, and for the FP32 correction solve its FP32 copy with d = 0 (else
+// d64 = 0); per-block sums over the interior equations of r^2 (into
+// partial[b]) and of (e u)^2, the scale of the equation (partial[nblocks+b]),
+// and over the Robin rows of r^2 (partial[2 nblocks+b]).
+__global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_constant__ MixArgs A) {
+    const LevelGeom& G = A.G;
     const long ld = G.ld;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    double sq = 0.0, sc = 0.0;
-    if (i <= nr && j <= nz) {
+    double sq = 0.0, sc = 0.0, sb = 0.0;
+    if (i <= G.nr && j <= G.nz) {
         auto U = [&](int p, int q) { return A.u[(size_t)mir(p) + (size_t)mir(q) * ld]; };
         const size_t o = (size_t)i + (size_t)j * ld;
-        double r = 0.0;
-        if (i <= nr - 1 && j <= nz - 1) {
-            double R;
-            if (!A.pa) {
-                R = A.ca[i] * U(i + 1, j) + A.cb[i] * U(i - 1, j) + A.cc * (U(i, j + 1) + U(i, j - 1))
-                    + A.e64[o] * U(i, j) - A.f64[o];
-            } else {
-                R = A.pa[o] * U(i + 1, j) + A.pb[o] * U(i - 1, j) + A.pc[o] * U(i, j + 1) + A.pd[o] * U(i, j - 1)
-                    + A.pg[o] * U(i + 1, j + 1) + A.ph[o] * U(i - 1, j - 1) + A.pi[o] * U(i + 1, j - 1)
-                    + A.pj[o] * U(i - 1, j + 1) + A.e64[o] * U(i, j) - A.f64[o];
-            }
-            r = -R;
+        double R = 0.0, r = 0.0;
+        bool interior;
+        if (mix_row<true>(A, U, i, j, o, R, interior)) r = -R;
+        if (interior) {
             sq = r * r;
             const double eu = A.e64[o] * U(i, j);
             sc = eu * eu;
-        } else if (A.robin) {
-            const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
-            double R;
-            if (i == nr && j == nz) {
-                R = (1.0 + 1.5 * (cr + cz)) * U(i, j) - A.uinf - 0.5 * cr * (4.0 * U(i - 1, j) - U(i - 2, j))
-                    - 0.5 * cz * (4.0 * U(i, j - 1) - U(i, j - 2));
-            } else if (i == nr) {
-                R = (1.0 + 1.5 * cr) * U(i, j) - A.uinf - 0.5 * cr * (4.0 * U(i - 1, j) - U(i - 2, j))
-                    + 0.5 * cz * (U(i, j + 1) - U(i, j - 1));
-            } else {
-                R = (1.0 + 1.5 * cz) * U(i, j) - A.uinf - 0.5 * cz * (4.0 * U(i, j - 1) - U(i, j - 2))
-                    + 0.5 * cr * (U(i + 1, j) - U(i - 1, j));
-            }
-            r = -R;
+        } else {
+            sb = r * r;
         }
+        if (A.r64) A.r64[o] = r;
         if (A.d64) {
-            A.r64[o] = r;
             A.d64[o] = 0.0;
         } else {
             A.r32[o] = (float)r;
@@ -658,17 +747,75 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
     }
     block_partial(sq, A.partial);
     block_partial(sc, A.partial + gridDim.x * gridDim.y);
+    block_partial(sb, A.partial + 2 * gridDim.x * gridDim.y);
 }
 
-// u += d at the unknowns (FP64); the ghosts are filled once the solve ends
-__global__ void __launch_bounds__(kMixThreads) mix_update_kernel(const __grid_constant__ MixArgs A) {
+// ---- Krylov acceleration of the multigrid corrections (Orthomin) ---------
+// The multigrid correction z of a refinement becomes a search direction: q =
+// A z is made orthogonal to the last few stored A-images, z follows with the
+// same coefficients, and u moves by the alpha that minimises |r - alpha q|.
+// The residual norm then never grows, even where the multigrid cycle alone
+// diverges (a positive zeroth-order coefficient, the Helmholtz sign, on the
+// coarse grids).
+
+// z64 = the correction (widened from FP32 when the solve ran in FP32);
+// q = A z64 (homogeneous rows, zero on Dirichlet rows)
+__global__ void __launch_bounds__(kMixThreads) mix_apply_kernel(const __grid_constant__ MixArgs A, double* z64,
+                                                                 double* q) {
     const LevelGeom& G = A.G;
+    const long ld = G.ld;
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    const int lim_r = A.robin ? G.nr : G.nr - 1, lim_z = A.robin ? G.nz : G.nz - 1;
-    if (i > lim_r || j > lim_z) return;  // Dirichlet rows keep their data
+    if (i > G.nr || j > G.nz) return;
+    auto Z = [&](int p, int qq) {
+        const size_t oo = (size_t)mir(p) + (size_t)mir(qq) * ld;
+        return A.d64 ? A.d64[oo] : (double)A.d[oo];
+    };
+    const size_t o = (size_t)i + (size_t)j * ld;
+    double R = 0.0;
+    bool interior;
+    const bool row = mix_row<false>(A, Z, i, j, o, R, interior);
+    z64[o] = row ? Z(i, j) : 0.0;
+    q[o] = row ? R : 0.0;
+}
+
+// per-block sums of x * y[k] over the unknowns, k < n (partial[k*nblocks+b])
+__global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, const double* x, OrthoVecs Y, int n,
+                                                                double* partial) {
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const bool in = i <= G.nr && j <= G.nz;
+    const size_t o = in ? (size_t)i + (size_t)j * G.ld : 0;
+    const double xv = in ? x[o] : 0.0;
+    const int nb = gridDim.x * gridDim.y;
+    for (int k = 0; k < n; ++k) block_partial(in ? xv * Y.v[k][o] : 0.0, partial + (size_t)k * nb);
+}
+
+// z -= sum_k beta_k Z_k, q -= sum_k beta_k Q_k
+__global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, double* z, double* q, OrthoVecs Zs,
+                                                                OrthoVecs Qs, OrthoCoef beta, int n) {
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    if (i > G.nr || j > G.nz) return;
     const size_t o = (size_t)i + (size_t)j * G.ld;
-    A.u[o] = A.u[o] + (A.d64 ? A.d64[o] : (double)A.d[o]);
+    double zv = z[o], qv = q[o];
+    for (int k = 0; k < n; ++k) {
+        zv = zv - beta.c[k] * Zs.v[k][o];
+        qv = qv - beta.c[k] * Qs.v[k][o];
+    }
+    z[o] = zv;
+    q[o] = qv;
+}
+
+// u += alpha z at the unknowns that are not Dirichlet rows
+__global__ void __launch_bounds__(kMixThreads) mix_step_kernel(LevelGeom G, int robin, double* u, const double* z,
+                                                                double alpha) {
+    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int lim_r = robin ? G.nr : G.nr - 1, lim_z = robin ? G.nz : G.nz - 1;
+    if (i > lim_r || j > lim_z) return;
+    const size_t o = (size_t)i + (size_t)j * G.ld;
+    u[o] = u[o] + alpha * z[o];
 }
 
 }  // namespace
@@ -684,10 +831,29 @@ void launch_mix_resid(const MixArgs& a, cudaStream_t s) {
     mix_resid_kernel<<<grd, blk, 0, s>>>(a);
 }
 
-void launch_mix_update(const MixArgs& a, cudaStream_t s) {
-    dim3 blk(32, 4);
-    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (a.G.nz + blk.y - 1) / blk.y);
-    mix_update_kernel<<<grd, blk, 0, s>>>(a);
+void launch_mix_apply(const MixArgs& a, double* z64, double* q, cudaStream_t s) {
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
+    mix_apply_kernel<<<grd, blk, 0, s>>>(a, z64, q);
+}
+
+void launch_mix_dots(const LevelGeom& G, const double* x, const OrthoVecs& y, int n, double* partial, cudaStream_t s) {
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    mix_dots_kernel<<<grd, blk, 0, s>>>(G, x, y, n, partial);
+}
+
+void launch_mix_orth(const LevelGeom& G, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
+                     const OrthoCoef& beta, int n, cudaStream_t s) {
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    mix_orth_kernel<<<grd, blk, 0, s>>>(G, z, q, Zs, Qs, beta, n);
+}
+
+void launch_mix_step(const LevelGeom& G, int robin, double* u, const double* z, double alpha, cudaStream_t s) {
+    dim3 blk(kMixBX, kMixBY);
+    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    mix_step_kernel<<<grd, blk, 0, s>>>(G, robin, u, z, alpha);
 }
 
 void launch_sor_e(const LevelGeom& G, double* e, const double* eaux, const double* S5, const double* u,

@@ -85,6 +85,9 @@ struct DLevel {
     // solve has replaced the lapse and no ``auxiliary`` has run since
     double* alpha_aux = nullptr;
     bool alpha_stale = false;
+    // driverD0: Delta_r | Delta_z of the last t = 0 ``auxiliary`` call
+    // (auxiliary_geometry.f90:1107-1113)
+    double* delta0 = nullptr;
     // syncboxes: this grid's state before the copies of its level (kept for
     // the partner's next first stage and its own), the map of the points
     // another box copies onto it (offset in the partner's state, or -1), the
@@ -145,6 +148,9 @@ struct ollin_handle {
     // iterations of the last elliptic solve (coarse phase, all-level phase)
     int ell_steps[2] = {0, 0};
     double ell_gres = 0.0;
+    // RMS residual after each FP64 refinement of the last mixed / fp64mg
+    // solve, per level (entry 0: before the first correction)
+    std::vector<std::vector<double>> ell_hist;
 };
 
 namespace {
@@ -163,19 +169,21 @@ void parity_table(ollin_handle* h) {
 double* base_ptr(const DLevel& L, double* p) { return p ? p + (L.g - 1) + (size_t)(L.g - 1) * L.ld : nullptr; }
 
 int check_params(const ollin_params& P) {
-    if (P.order != 4) return fail(OLLIN_EINVAL, "order must be \"four\" (4)");
+    if (P.order != 4 && P.order != 2) return fail(OLLIN_EINVAL, "order must be \"two\" (2) or \"four\" (4)");
     if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
     if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
     if (!P.eqsym && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
         P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
         return fail(OLLIN_EINVAL,
                     "elliptic initial data without equatorial symmetry needs ELL_solver = wave or sor on the device");
-    if (P.ghost != 0 && P.ghost != 3) return fail(OLLIN_EINVAL, "ghost must be 3 for order four");
+    // main.f90:286-318 takes a larger par-file ghost as given; here the
+    // number is the order's own
+    if (P.ghost != 0 && P.ghost != (P.order == 2 ? 2 : 3))
+        return fail(OLLIN_EINVAL, "ghost must be 2 for order two and 3 for order four");
     if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
     if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
-    if (P.shift != OLLIN_SHIFT_NONE && P.shift != OLLIN_SHIFT_GAMMADRIVER2 && P.shift != OLLIN_SHIFT_GAMMADRIVER1 &&
-        P.shift != OLLIN_SHIFT_GAMMADRIVER0)
+    if (P.shift < OLLIN_SHIFT_NONE || P.shift > OLLIN_SHIFT_GAMMADRIVERSHOCK2)
         return fail(OLLIN_EINVAL, "shift must be none, Gammadriver0, Gammadriver1 or Gammadriver2");
     if (P.slicing < 0 || P.slicing > OLLIN_SLICING_MAXIMAL) return fail(OLLIN_EINVAL, "unknown slicing");
     if (P.ilapse < OLLIN_ILAPSE_ONE || P.ilapse > OLLIN_ILAPSE_MAXIMAL) return fail(OLLIN_EINVAL, "unknown ilapse");
@@ -311,6 +319,7 @@ int alloc_level(ollin_handle* h, DLevel& L, int gid) {
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
     LevelGeom& G = L.G;
     G.nr = L.nr; G.nz = L.nz; G.g = g; G.ld = L.ld;
+    G.order = P.order;
     G.eqsym = P.eqsym ? 1 : 0;
     G.axis = rb == 0.0 ? 1 : 0;                        // main.f90:393-403
     G.equator = (P.eqsym && zb == 0.0) ? 1 : 0;        // main.f90:412-424
@@ -334,9 +343,15 @@ PhysParams make_phys(const ollin_params& P) {
     PhysParams q{};
     q.slicing = P.slicing;
     q.gauge_f = P.gauge_f;
-    q.shift = (P.shift == OLLIN_SHIFT_GAMMADRIVER2 || P.shift == OLLIN_SHIFT_GAMMADRIVER1 ||
-               P.shift == OLLIN_SHIFT_GAMMADRIVER0) ? 1 : 0;
-    q.driver = P.shift == OLLIN_SHIFT_GAMMADRIVER1 ? 1 : P.shift == OLLIN_SHIFT_GAMMADRIVER0 ? 0 : 2;
+    q.shift = P.shift != OLLIN_SHIFT_NONE ? 1 : 0;
+    // sources_shift.f90: 2 the second-order drivers, 1 the first-order ones,
+    // 0 the parabolic one, 3 zero or static (no sources, no boundary)
+    q.driver = (P.shift == OLLIN_SHIFT_GAMMADRIVER1 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK1) ? 1
+               : P.shift == OLLIN_SHIFT_GAMMADRIVER0                                             ? 0
+               : (P.shift == OLLIN_SHIFT_ZERO || P.shift == OLLIN_SHIFT_STATIC)                  ? 3
+                                                                                                  : 2;
+    q.shock = (P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK1 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK2) ? 1 : 0;
+    q.driverD0 = P.driverD0 ? 1 : 0;
     q.shiftadvect = P.shiftadvect;
     q.driveradv = P.driveradv;
     q.drivercsi = P.drivercsi;
@@ -397,6 +412,15 @@ int do_aux(ollin_handle* h, DLevel& L, int slot, bool t0, bool project = true) {
     a.t0 = t0 ? 1 : 0;
     a.scalar = h->scalar ? 1 : 0;
     a.project = project ? 1 : 0;
+    if (t0 && h->shift && h->P.driverD0) {
+        if (!L.delta0) {
+            if (cudaMalloc(&L.delta0, 2 * L.n * sizeof(double)) != cudaSuccess)
+                return fail(OLLIN_ENOMEM, "device allocation failed for the t = 0 Delta");
+            CUDA_OR_FAIL(cudaMemsetAsync(L.delta0, 0, 2 * L.n * sizeof(double), h->stream));
+        }
+        a.d0r = base_ptr(L, L.delta0);
+        a.d0z = base_ptr(L, L.delta0 + L.n);
+    }
     launch_aux_point(a, h->stream);
     int rc = after_launch(h);
     if (rc) return rc;
@@ -430,6 +454,10 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
     a.t0 = L.last_aux_t0 ? 1 : 0;
     a.evolve_phi = t0 ? 1 : 0;
     a.level0 = L.level == 0;
+    // sources_shift.f90:43 reads the time of box 0's level 0 when the stage runs
+    a.shift_static = (h->phys.driver == 3 || h->t[0] < h->P.shiftafter) ? 1 : 0;
+    a.d0r = L.delta0 ? base_ptr(L, L.delta0) : nullptr;
+    a.d0z = L.delta0 ? base_ptr(L, L.delta0 + L.n) : nullptr;
     a.rk4 = h->P.integrator == OLLIN_INTEGRATOR_RK4;
     a.nanflag = h->d_flag;
     a.alpha_aux = L.alpha_stale ? base_ptr(L, L.alpha_aux) : nullptr;
@@ -449,10 +477,11 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
 // the lapse quantities of the last ``auxiliary`` call from alpha_aux, the
 // derivatives from the state kept from before ``syncboxes``, or both
 void launch_stage_rhs(const StageArgs& a, cudaStream_t s) {
-    if (a.alpha_aux && a.smap) launch_rhs_stale_sync(a, s);
-    else if (a.alpha_aux) launch_rhs_stale(a, s);
-    else if (a.smap) launch_rhs_sync(a, s);
-    else launch_rhs(a, s);
+    const bool o2 = a.G.order == 2;
+    if (a.alpha_aux && a.smap) (o2 ? launch_rhs_o2_stale_sync : launch_rhs_stale_sync)(a, s);
+    else if (a.alpha_aux) (o2 ? launch_rhs_o2_stale : launch_rhs_stale)(a, s);
+    else if (a.smap) (o2 ? launch_rhs_o2_sync : launch_rhs_sync)(a, s);
+    else (o2 ? launch_rhs_o2 : launch_rhs)(a, s);
 }
 
 // Geometry part of the transfer arguments of grid ``gid`` and its parent
@@ -904,6 +933,7 @@ int internal_field(int field, bool* is_aux) {
         case OLLIN_F_SCALAR_XI_R: return F_SXIR;
         case OLLIN_F_SCALAR_XI_Z: return F_SXIZ;
         case OLLIN_F_SCALAR_PI: return F_SPI;
+        case OLLIN_F_FDRIVER: return F_FDRIVER;
         case OLLIN_F_KTH: *is_aux = true; return X_KTH;
         case OLLIN_F_LAMBDA: *is_aux = true; return X_LAM;
         case OLLIN_F_ALAMBDA: *is_aux = true; return X_ALAM;
@@ -1623,12 +1653,12 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     if (rc) return rc;
     const bool s5 = !S.physical && P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
     const int nparts = mix_blocks(L.G);
-    if (S.nparts < 2 * nparts) {
+    if (S.nparts < 3 * nparts) {
         cudaFree(S.partial);
         S.partial = nullptr;
-        if (cudaMalloc(&S.partial, 2 * nparts * sizeof(double)) != cudaSuccess)
+        if (cudaMalloc(&S.partial, 3 * nparts * sizeof(double)) != cudaSuccess)
             return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
-        S.nparts = 2 * nparts;
+        S.nparts = 3 * nparts;
     }
     // maximal slicing: the nine-point stencil of the physical Laplacian
     double* phys = nullptr;
@@ -1679,9 +1709,53 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     ms.e = a.e64;
     ms.ld = L.ld;
     ms.dr = L.dr; ms.dz = L.dz;
-    std::vector<double> hp(2 * nparts);
+    // Orthomin storage: a ring of kOrthoSlots directions z and their images
+    // q = A z, the FP64 residual for the FP32 solve, per-block dot products
+    constexpr int kOrthoSlots = 7;  // the new direction + up to 6 kept
+    static_assert(kOrthoSlots - 1 <= kOrthoMax, "Orthomin ring larger than the kernels take");
+    const size_t nvec = 2 * (size_t)kOrthoSlots + (fp64 ? 0 : 1);
+    double* ortho = nullptr;
+    double* dpart = nullptr;
+    struct FreeOrtho { double* a; double* b; ~FreeOrtho() { cudaFree(a); cudaFree(b); } } free_ortho{nullptr, nullptr};
+    if (cudaMalloc(&ortho, nvec * L.n * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&dpart, (size_t)(kOrthoMax + 2) * nparts * sizeof(double)) != cudaSuccess) {
+        cudaFree(ortho);
+        return fail(OLLIN_ENOMEM, "device allocation failed for the mixed-precision solver");
+    }
+    free_ortho.a = ortho;
+    free_ortho.b = dpart;
+    CUDA_OR_FAIL(cudaMemsetAsync(ortho, 0, nvec * L.n * sizeof(double), h->stream));
+    double* Zs[kOrthoSlots];
+    double* Qs[kOrthoSlots];
+    for (int k = 0; k < kOrthoSlots; ++k) {
+        Zs[k] = base_ptr(L, ortho + (size_t)k * L.n);
+        Qs[k] = base_ptr(L, ortho + (size_t)(kOrthoSlots + k) * L.n);
+    }
+    if (!fp64) a.r64 = base_ptr(L, ortho + (size_t)(2 * kOrthoSlots) * L.n);
+    double qq[kOrthoSlots] = {0};
+    int head = 0, stored = 0;
+    std::vector<double> hd((size_t)(kOrthoMax + 2) * nparts);
+    // sums over the blocks of the first n dot products, in block order
+    auto dots = [&](const double* x, const OrthoVecs& y, int n, double* out) -> int {
+        launch_mix_dots(L.G, x, y, n, dpart, h->stream);
+        int rc2 = after_launch(h);
+        if (rc2) return rc2;
+        CUDA_OR_FAIL(cudaMemcpyAsync(hd.data(), dpart, (size_t)n * nparts * sizeof(double), cudaMemcpyDeviceToHost,
+                                     h->stream));
+        CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+        for (int k = 0; k < n; ++k) {
+            double acc = 0.0;
+            for (int b = 0; b < nparts; ++b) acc += hd[(size_t)k * nparts + b];
+            out[k] = acc;
+        }
+        return OLLIN_OK;
+    };
+    std::vector<double> hp(3 * nparts);
     int outer = 0, cycles = 0, ncyc = 2, flat = 0;
     double rms = 0.0, last = 0.0;
+    if ((int)h->ell_hist.size() != h->nlev) h->ell_hist.assign(h->nlev, {});
+    std::vector<double>& hist = h->ell_hist[level];
+    hist.clear();
     for (;;) {
         if (s5) {
             launch_sor_e(L.G, base_ptr(L, e), base_ptr(L, eaux), base_ptr(L, w.S5), base_ptr(L, w.u[w.cur]), nullptr,
@@ -1692,17 +1766,40 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         launch_mix_resid(a, h->stream);
         rc = after_launch(h);
         if (rc) return rc;
-        CUDA_OR_FAIL(cudaMemcpyAsync(hp.data(), S.partial, 2 * nparts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_OR_FAIL(cudaMemcpyAsync(hp.data(), S.partial, 3 * nparts * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
         CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
-        double sum = 0.0, scale = 0.0;
-        for (int k = 0; k < nparts; ++k) { sum += hp[k]; scale += hp[nparts + k]; }
-        rms = std::sqrt(sum / (double)((L.nr - 1) * (L.nz - 1)));
-        (void)scale;  // RMS of e*u: the floor is ~1e-16 of it
-        if (!(rms >= P.ell_epsilon) || outer >= 60) break;  // converged, NaN, or too many refinements
+        double sum = 0.0, scale = 0.0, sumb = 0.0;
+        for (int k = 0; k < nparts; ++k) { sum += hp[k]; scale += hp[nparts + k]; sumb += hp[2 * nparts + k]; }
+        const double nint = (double)((L.nr - 1) * (L.nz - 1));
+        const double rms_in = std::sqrt(sum / nint);
+        // the Robin rows (level 0): a smooth offset of the whole solution moves
+        // them by its size while the interior rows hardly see it, so they are
+        // held to the tolerance on their own
+        const double nrob = robin ? (double)(L.nr + L.nz - 1) : 0.0;
+        const double rms_b = robin ? std::sqrt(sumb / nrob) : 0.0;
+        rms = std::max(rms_in, rms_b);
+        // the FP64 floor of a row: the residual of the solution rounded to
+        // FP64, about a unit roundoff of the diagonal term (e*u inside, the
+        // Robin row's 1 + 1.5 (r/dr + z/dz) on the edges)
+        const double floor64 = 1.1e-16 * std::sqrt(scale / nint);
+        const double floor_b = 1.1e-16 * (1.0 + 1.5 * (L.rh[L.nr - 1 + g] / L.dr + L.zh[L.nz - 1 + g] / L.dz));
+        const bool near_floor = rms_in < 100.0 * floor64 && rms_b < 100.0 * floor_b;
+        hist.push_back(rms);
+        if (!std::isfinite(rms))
+            return fail(OLLIN_ENAN, "non-finite residual in the multigrid solve of level " + std::to_string(level)
+                                        + " (refinement " + std::to_string(outer) + ")");
+        if (rms < P.ell_epsilon) break;  // converged
+        if (outer >= 60) {
+            if (near_floor) break;
+            return fail(OLLIN_ECONV, "the multigrid solve of level " + std::to_string(level) + " did not converge: RMS "
+                                         + "residual " + std::to_string(rms) + " after 60 refinements");
+        }
         if (outer > 0) {
-            // at the FP64 floor the residual stops falling
-            flat = (rms > 0.5 * last) ? flat + 1 : 0;
-            if (flat >= 2) break;
+            // at the FP64 floor the residual stops falling; a few more
+            // refinements still take out the smooth error that the floor's
+            // rounding residual hides (the residual sums are exact)
+            flat = (rms > 0.5 * last && near_floor) ? flat + 1 : 0;
+            if (flat >= 3) break;
             // a refinement that gained less than a decade gets more cycles next time
             if (rms > 0.1 * last) ncyc = std::min(ncyc * 2, 16);
         }
@@ -1718,9 +1815,46 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         h->launches += 2 + (long long)ncyc * mg_launches_per_cycle(mg, a.robin);
         CUDA_OR_FAIL(cudaGetLastError());
         cycles += ncyc;
-        launch_mix_update(a, h->stream);
+        // the correction as a search direction: q = A z, orthogonal to the
+        // kept images (none when S5 u^4 changed the operator), then the step
+        // that minimises the residual along q
+        if (s5) stored = 0;
+        launch_mix_apply(a, Zs[head], Qs[head], h->stream);
         rc = after_launch(h);
         if (rc) return rc;
+        const int nprev = std::min(stored, kOrthoSlots - 1);
+        if (nprev > 0) {
+            OrthoVecs zy{}, qy{};
+            OrthoCoef beta{};
+            for (int k = 0; k < nprev; ++k) {
+                const int sl = (head - 1 - k + kOrthoSlots) % kOrthoSlots;
+                zy.v[k] = Zs[sl];
+                qy.v[k] = Qs[sl];
+            }
+            double dq[kOrthoMax];
+            rc = dots(Qs[head], qy, nprev, dq);
+            if (rc) return rc;
+            for (int k = 0; k < nprev; ++k) {
+                const int sl = (head - 1 - k + kOrthoSlots) % kOrthoSlots;
+                beta.c[k] = qq[sl] > 0.0 ? dq[k] / qq[sl] : 0.0;
+            }
+            launch_mix_orth(L.G, Zs[head], Qs[head], zy, qy, beta, nprev, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
+        }
+        OrthoVecs rq{};
+        rq.v[0] = a.r64;
+        rq.v[1] = Qs[head];
+        double d2[2];
+        rc = dots(Qs[head], rq, 2, d2);
+        if (rc) return rc;
+        if (!(d2[1] > 0.0) || !std::isfinite(d2[0])) break;  // no direction left (the residual is zero)
+        launch_mix_step(L.G, a.robin, a.u, Zs[head], d2[0] / d2[1], h->stream);
+        rc = after_launch(h);
+        if (rc) return rc;
+        qq[head] = d2[1];
+        head = (head + 1) % kOrthoSlots;
+        ++stored;
     }
     // parity fill of the solution (the ghosts mirror the first points)
     SymArgs sy{};
@@ -1983,6 +2117,8 @@ int initial_data(ollin_handle* h) {
         if (P.idata == OLLIN_IDATA_SCALARPULSE) {
             F[F_SPHI] = scal[l][0]; F[F_SXIR] = scal[l][1]; F[F_SXIZ] = scal[l][2]; F[F_SPI] = scal[l][3];
         }
+        // initial.f90:71-82: zero shift, fdriver = 1
+        F[F_FDRIVER].assign(n, 1.0);
         for (int f : h->fields) {
             CUDA_OR_FAIL(cudaMemcpyAsync(L.slot[L.cur][f], F[f].data(), n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         }
@@ -2133,6 +2269,7 @@ void ollin_params_default(ollin_params* p) {
     for (int b = 0; b < 3; ++b) {
         p->nl[b] = 0; p->nrbox[b] = 1; p->nzbox[b] = 1; p->rbox[b] = 0.0; p->zbox[b] = 0.0;
     }
+    p->driverD0 = 0; p->shiftafter = 0.0;  // param.f90:347-350
 }
 
 const char* ollin_gpu_last_error(void) { return g_err.c_str(); }
@@ -2147,15 +2284,17 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
         return fail(OLLIN_ECUDA, "no CUDA device is available");
     auto* h = new ollin_handle();
     h->P = *p;
-    h->g = 3;
-    h->shift = p->shift == OLLIN_SHIFT_GAMMADRIVER2 || p->shift == OLLIN_SHIFT_GAMMADRIVER1 ||
-               p->shift == OLLIN_SHIFT_GAMMADRIVER0;
+    h->g = p->order == 2 ? 2 : 3;  // main.f90:286-297
+    h->shift = p->shift != OLLIN_SHIFT_NONE;
     h->scalar = p->mattertype == OLLIN_MATTER_SCALAR;
     h->phys = make_phys(*p);
     parity_table(h);
     for (int f : {F_ALPHA, F_CHI, F_PHI, F_A, F_B, F_H, F_C, F_TRK, F_KTA, F_KTB, F_KTC, F_DLR, F_DLZ}) h->fields.push_back(f);
     if (h->shift)
         for (int f : {F_BETAR, F_BETAZ, F_DTBETAR, F_DTBETAZ}) h->fields.push_back(f);
+    // fdriver has a source only with the shock-avoiding drivers (it stays 1
+    // under the others)
+    if (h->phys.shock) h->fields.push_back(F_FDRIVER);
     if (h->scalar)
         for (int f : {F_SPHI, F_SXIR, F_SXIZ, F_SPI}) h->fields.push_back(f);
     rc = setup_boxes(h);
@@ -2204,6 +2343,7 @@ void ollin_gpu_destroy(ollin_handle* h) {
         if (L.ptab) cudaFree(L.ptab);
         if (L.rtab) cudaFree(L.rtab);
         if (L.alpha_aux) cudaFree(L.alpha_aux);
+        if (L.delta0) cudaFree(L.delta0);
         if (L.snap) cudaFree(L.snap);
         if (L.smap) cudaFree(L.smap);
     }
@@ -2230,6 +2370,16 @@ int ollin_gpu_level_desc(const ollin_handle* h, int level, ollin_level_desc* out
     out->zmin = h->zminl[level]; out->zmax = h->zmaxl[level];
     out->time = h->t[level];
     out->steps = (int)h->s[level];
+    out->rbox = h->rbox[L.box];
+    out->zbox = h->zbox[L.box];
+    return OLLIN_OK;
+}
+
+int ollin_gpu_coords(const ollin_handle* h, int level, double* r, double* z) {
+    if (!h || !r || !z || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad level or pointer");
+    const DLevel& L = h->L[level];
+    for (int k = 0; k < L.nr + L.g; ++k) r[k] = L.rh[k];
+    for (int k = 0; k < L.nz + L.g; ++k) z[k] = L.zh[k];
     return OLLIN_OK;
 }
 
@@ -2247,13 +2397,14 @@ int ollin_gpu_upload(ollin_handle* h, int level, int field, const double* a, int
     return OLLIN_OK;
 }
 
-int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r) {
-    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+// The device array that holds ``field`` of grid ``level`` as the reference
+// holds it now (derived fields computed first; phi from chi after a t > 0
+// ``auxiliary``), element (1-ghost, 1-ghost) first.
+static int field_source(ollin_handle* h, int level, int field, const double** out) {
     DLevel& L = h->L[level];
     bool is_aux;
     const int f = internal_field(field, &is_aux);
     if (f < 0) return fail(OLLIN_EINVAL, "unknown field");
-    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
     const double* src = nullptr;
     if (is_aux) {
         if (f == X_HAM || f == X_MOMR || f == X_MOMZ || f == X_RSCAL || f == X_KT2 || f == X_LAPLA) {
@@ -2273,9 +2424,51 @@ int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_
             src = L.aux[X_RSCAL];
         }
     }
+    *out = src;
+    return OLLIN_OK;
+}
+
+int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r) {
+    if (!h || !a || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    DLevel& L = h->L[level];
+    if (ld_r < L.nr + L.g) return fail(OLLIN_EINVAL, "ld_r smaller than Nr+ghost");
+    const double* src = nullptr;
+    int rc = field_source(h, level, field, &src);
+    if (rc) return rc;
     CUDA_OR_FAIL(cudaMemcpy2DAsync(a, (size_t)ld_r * sizeof(double), src, (size_t)L.ld * sizeof(double),
                                    (size_t)(L.nr + L.g) * sizeof(double), (size_t)(L.nz + L.g), cudaMemcpyDeviceToHost, h->stream));
     CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    return OLLIN_OK;
+}
+
+int ollin_gpu_interp(ollin_handle* h, int level, int field, const double* rz, int n, double* out) {
+    if (!h || level < 0 || level >= h->nlev || n < 0 || (n > 0 && (!rz || !out)))
+        return fail(OLLIN_EINVAL, "bad handle, level or pointer");
+    if (n == 0) return OLLIN_OK;
+    DLevel& L = h->L[level];
+    const double* src = nullptr;
+    int rc = field_source(h, level, field, &src);
+    if (rc) return rc;
+    double* d = nullptr;
+    if (cudaMalloc(&d, (3 * (size_t)n + 1) * sizeof(double)) != cudaSuccess)
+        return fail(OLLIN_ENOMEM, "device allocation failed for the interpolation points");
+    struct FreeD { double* p; ~FreeD() { cudaFree(p); } } free_d{d};
+    unsigned int* bad = reinterpret_cast<unsigned int*>(d + 3 * (size_t)n);
+    CUDA_OR_FAIL(cudaMemcpyAsync(d, rz, 2 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_OR_FAIL(cudaMemsetAsync(bad, 0, sizeof(unsigned int), h->stream));
+    // interp.f90 reads the interpolated array with its ghosts: the base of
+    // the level layout, element (1-ghost, 1-ghost) at offset 0
+    launch_interp_points(L.G, h->rminl[level], h->rmaxl[level], h->zminl[level], h->zmaxl[level],
+                         h->P.interp_bicubic, base_ptr(L, const_cast<double*>(src)), d, n, d + 2 * (size_t)n, bad,
+                         h->stream);
+    rc = after_launch(h);
+    if (rc) return rc;
+    unsigned int nbad = 0;
+    CUDA_OR_FAIL(cudaMemcpyAsync(out, d + 2 * (size_t)n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaMemcpyAsync(&nbad, bad, sizeof(nbad), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_OR_FAIL(cudaStreamSynchronize(h->stream));
+    if (nbad) return fail(OLLIN_EINVAL, std::to_string(nbad) + " point(s) outside the grid's interpolation range "
+                                        "(interp.f90:146-157); their values are NaN");
     return OLLIN_OK;
 }
 
@@ -2356,7 +2549,9 @@ int ollin_gpu_initialize(ollin_handle* h) {
         int rc = do_aux(h, h->L[l], h->L[l].cur, h->t[l] == 0.0);
         if (rc) return rc;
     }
-    if (h->P.shift == OLLIN_SHIFT_GAMMADRIVER2) {  // evolve.f90:174-195
+    // evolve.f90:174-195: dtbeta = csi Delta for the second-order drivers,
+    // unless driverD0
+    if ((h->P.shift == OLLIN_SHIFT_GAMMADRIVER2 || h->P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK2) && !h->P.driverD0) {
         for (int l = 0; l < h->nlev; ++l) {
             DLevel& L = h->L[l];
             launch_gammadriver_init(L.G, base_ptr(L, L.slot[L.cur][F_DTBETAR]), base_ptr(L, L.slot[L.cur][F_DTBETAZ]),
@@ -2505,7 +2700,7 @@ int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transie
     if (rc) return rc;
     ollin_handle tmp;  // the grid list only: no device work
     tmp.P = *p;
-    tmp.g = 3;
+    tmp.g = p->order == 2 ? 2 : 3;
     rc = setup_boxes(&tmp);
     if (rc) return rc;
     // a maximal-slicing solve may run whenever the caller asks (maximalevery
@@ -2524,8 +2719,9 @@ int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transie
         if (maximal) res += n * sizeof(double) + page;  // the lapse of the last auxiliary call
         // the elliptic solver's arrays while a solve runs: 13 arrays of the
         // wave solver's state and sources, 5 of coefficients, and for SOR and
-        // the mixed solver their stencil, residual and FP32 hierarchy (below 22)
-        if (elliptic) tr += 40 * n * sizeof(double) + 4 * page;
+        // the mixed solver their nine-point stencil, residual and correction
+        // (3), multigrid hierarchy (below 6) and the 15 Orthomin vectors
+        if (elliptic) tr += 56 * n * sizeof(double) + 4 * page;
     }
     *resident = res;
     *transient = tr;
@@ -2851,26 +3047,10 @@ int ollin_gpu_coarse_step_auto(ollin_handle* const* hs, int n, double* t_out, in
 int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]) {
     if (!h || !out || level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad handle, level or pointer");
     DLevel& L = h->L[level];
-    bool is_aux;
-    const int f = internal_field(field, &is_aux);
-    if (f < 0) return fail(OLLIN_EINVAL, "unknown field");
-    const double* src;
-    if (is_aux) {
-        if (f == X_HAM || f == X_MOMR || f == X_MOMZ || f == X_RSCAL || f == X_KT2 || f == X_LAPLA) {
-            int rc = analysis(h, level);
-            if (rc) return rc;
-        }
-        src = base_ptr(L, L.aux[f]);
-    } else {
-        if (!field_active(h, f)) return fail(OLLIN_EINVAL, "field is not evolved with these parameters");
-        src = base_ptr(L, L.slot[L.cur][f]);
-        if (f == F_PHI && !L.last_aux_t0) {
-            launch_phi_from_chi(L.G, base_ptr(L, L.slot[L.cur][F_CHI]), base_ptr(L, L.aux[X_RSCAL]), h->stream);
-            int rc = after_launch(h);
-            if (rc) return rc;
-            src = base_ptr(L, L.aux[X_RSCAL]);
-        }
-    }
+    const double* raw = nullptr;
+    int rc0 = field_source(h, level, field, &raw);
+    if (rc0) return rc0;
+    const double* src = base_ptr(L, const_cast<double*>(raw));
     // the origin value only for box 0 (save0Ddata.f90:370-374)
     launch_norms(L.G, src, L.box == 0 ? h->P.interp_bicubic : -1, h->rminl[level], h->zminl[level], h->rmaxl[level],
                  h->zmaxl[level], h->d_norm, norm_partials(h), h->stream);
@@ -2949,6 +3129,17 @@ int ollin_gpu_ell_stats(const ollin_handle* h, int steps[2], double* gres) {
     steps[0] = h->ell_steps[0];
     steps[1] = h->ell_steps[1];
     if (gres) *gres = h->ell_gres;
+    return OLLIN_OK;
+}
+
+int ollin_gpu_ell_history(const ollin_handle* h, int level, double* rms, int max, int* n) {
+    if (!h || !n || (max > 0 && !rms)) return fail(OLLIN_EINVAL, "null argument");
+    if (level < 0 || level >= h->nlev) return fail(OLLIN_EINVAL, "bad level");
+    *n = 0;
+    if ((int)h->ell_hist.size() != h->nlev) return OLLIN_OK;
+    const std::vector<double>& v = h->ell_hist[level];
+    *n = (int)v.size();
+    for (int k = 0; k < std::min(max, *n); ++k) rms[k] = v[k];
     return OLLIN_OK;
 }
 

@@ -130,6 +130,7 @@ enum Field : int {
     F_TRK, F_KTA, F_KTB, F_KTC, F_DLR, F_DLZ,
     F_BETAR, F_BETAZ, F_DTBETAR, F_DTBETAZ,
     F_SPHI, F_SXIR, F_SXIZ, F_SPI,
+    F_FDRIVER,                     // the shock-avoiding drivers' fdriver
     NFIELDS
 };
 
@@ -149,6 +150,7 @@ enum AuxField : int {
 // Geometry of one level as seen by a kernel.
 struct LevelGeom {
     int nr, nz, g, ld;   // Nr, Nz, ghost, leading dimension
+    int order;           // finite-difference order (param order): 2 or 4
     int jlo;             // first z-row with a source: 1 (the grid owns the equator) or 1-g
     int eqsym;           // equatorial symmetry of the run (param eqsym)
     int axis, equator;   // the grid's ghosts are the axis / equator parity images
@@ -272,6 +274,91 @@ __device__ __forceinline__ double dadv(const double* f, long s, int i, int n, in
     if (i == 2 - g) return right();
     return -q * (25.0 * ld_(f) - 48.0 * ld_(f + s) + 36.0 * ld_(f + 2 * s) - 16.0 * ld_(f + 3 * s) + 3.0 * ld_(f + 4 * s)) * (1.0 / 3.0);
 }
+
+// ---------------------------------------------------------------------------
+// order two (derivatives.f90 :50-58, :158-172, :285-301, :402-418, :533-599;
+// derivadvect.f90 :50-100, :249-299; dissipation.f90 :121-135).  Position
+// classes: 0 centred (i = 2-ghost..n-1), 2 last point, -2 first point.
+// ``c`` is 1/(2h) for first and 1/h^2 for second derivatives.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int pclass2(int i, int n, int g) { return i == n ? 2 : (i >= 2 - g ? 0 : -2); }
+
+__device__ __forceinline__ double d1_2(const double* f, long s, int k, double c) {
+    if (k == 0) return c * (ld_(f + s) - ld_(f - s));
+    if (k == 2) return c * (3.0 * ld_(f) - 4.0 * ld_(f - s) + ld_(f - 2 * s));
+    return -c * (3.0 * ld_(f) - 4.0 * ld_(f + s) + ld_(f + 2 * s));
+}
+
+__device__ __forceinline__ double d2_2(const double* f, long s, int k, double c) {
+    if (k == 0) return c * (ld_(f + s) - 2.0 * ld_(f) + ld_(f - s));
+    if (k == 2) return c * (2.0 * ld_(f) - 5.0 * ld_(f - s) + 4.0 * ld_(f - 2 * s) - ld_(f - 3 * s));
+    return c * (2.0 * ld_(f) - 5.0 * ld_(f + s) + 4.0 * ld_(f + 2 * s) - ld_(f + 3 * s));
+}
+
+// centred inside, one-sided on the outermost rows and columns, the corners
+// from both one-sided stencils (the r- and z-edge loops do not overlap)
+__device__ __forceinline__ double d2rz_2(const double* f, long ld, int i, int j, int nr, int nz, int g, double idrz) {
+#define F_(a, b) ld_(f + (a) + (long)(b) * ld)
+    const bool ri = (i >= 2 - g && i <= nr - 1), zi = (j >= 2 - g && j <= nz - 1);
+    const double q = 0.25 * idrz;
+    if (ri && zi) return q * (F_(1, 1) + F_(-1, -1) - F_(1, -1) - F_(-1, 1));
+    if (zi) {  // i = 1-g or nr
+        if (i == nr) return q * ((3.0 * F_(0, 1) - 4.0 * F_(-1, 1) + F_(-2, 1)) - (3.0 * F_(0, -1) - 4.0 * F_(-1, -1) + F_(-2, -1)));
+        return -q * ((3.0 * F_(0, 1) - 4.0 * F_(1, 1) + F_(2, 1)) - (3.0 * F_(0, -1) - 4.0 * F_(1, -1) + F_(2, -1)));
+    }
+    if (ri) {  // j = 1-g or nz
+        if (j == nz) return q * ((3.0 * F_(1, 0) - 4.0 * F_(1, -1) + F_(1, -2)) - (3.0 * F_(-1, 0) - 4.0 * F_(-1, -1) + F_(-1, -2)));
+        return -q * ((3.0 * F_(1, 0) - 4.0 * F_(1, 1) + F_(1, 2)) - (3.0 * F_(-1, 0) - 4.0 * F_(-1, 1) + F_(-1, 2)));
+    }
+    if (i == nr && j == nz)
+        return q * (9.0 * F_(0, 0) + 16.0 * F_(-1, -1) + F_(-2, -2) - 12.0 * (F_(0, -1) + F_(-1, 0))
+                    + 3.0 * (F_(0, -2) + F_(-2, 0)) - 4.0 * (F_(-1, -2) + F_(-2, -1)));
+    if (i == nr)
+        return -q * (9.0 * F_(0, 0) + 16.0 * F_(-1, 1) + F_(-2, 2) - 12.0 * (F_(0, 1) + F_(-1, 0))
+                     + 3.0 * (F_(0, 2) + F_(-2, 0)) - 4.0 * (F_(-1, 2) + F_(-2, 1)));
+    if (j == nz)
+        return -q * (9.0 * F_(0, 0) + 16.0 * F_(1, -1) + F_(2, -2) - 12.0 * (F_(1, 0) + F_(0, -1))
+                     + 3.0 * (F_(2, 0) + F_(0, -2)) - 4.0 * (F_(2, -1) + F_(1, -2)));
+    return q * (9.0 * F_(0, 0) + 16.0 * F_(1, 1) + F_(2, 2) - 12.0 * (F_(0, 1) + F_(1, 0))
+                + 3.0 * (F_(0, 2) + F_(2, 0)) - 4.0 * (F_(1, 2) + F_(2, 1)));
+#undef F_
+}
+
+// second-order lopsided advective derivative; the r and z routines treat
+// every point alike
+__device__ __forceinline__ double dadv_2(const double* f, long s, int i, int n, int g, bool neg, double ih) {
+    const double h = 0.5 * ih;
+    auto left = [&]() { return +h * (3.0 * ld_(f) - 4.0 * ld_(f - s) + ld_(f - 2 * s)); };
+    auto right = [&]() { return -h * (3.0 * ld_(f) - 4.0 * ld_(f + s) + ld_(f + 2 * s)); };
+    auto cent = [&]() { return h * (ld_(f + s) - ld_(f - s)); };
+    if (i >= 3 - g && i <= n - 2) return neg ? left() : right();
+    if (i == 2 - g) return neg ? cent() : right();
+    if (i == 1 - g) return right();
+    if (i == n - 1) return neg ? left() : cent();
+    return left();  // i == n
+}
+
+// the fourth difference of order-two dissipation (without -eps/dt/6)
+__device__ __forceinline__ double ko4(const double* f, long s) {
+    return 6.0 * ld_(f) - 4.0 * (ld_(f + s) + ld_(f - s)) + (ld_(f + 2 * s) + ld_(f - 2 * s));
+}
+
+// ---- order dispatch for the kernels that take the order at run time ------
+__device__ __forceinline__ int pclass_o(int ord, int i, int n, int g) { return ord == 2 ? pclass2(i, n, g) : pclass(i, n, g); }
+__device__ __forceinline__ double c1_o(int ord, double ih) { return ord == 2 ? 0.5 * ih : ih * (1.0 / 12.0); }
+__device__ __forceinline__ double c2_o(int ord, double ih) { return ord == 2 ? ih * ih : ih * ih * (1.0 / 12.0); }
+__device__ __forceinline__ double d1_o(int ord, const double* f, long s, int k, double c) {
+    return ord == 2 ? d1_2(f, s, k, c) : d1(f, s, k, c);
+}
+__device__ __forceinline__ double d2_o(int ord, const double* f, long s, int k, double c) {
+    return ord == 2 ? d2_2(f, s, k, c) : d2(f, s, k, c);
+}
+__device__ __forceinline__ double d2rz_o(int ord, const double* f, long ld, int i, int j, int nr, int nz, int g, double idrz) {
+    return ord == 2 ? d2rz_2(f, ld, i, j, nr, nz, g, idrz) : d2rz(f, ld, i, j, nr, nz, g, idrz);
+}
+// the first point whose r derivative diff1r sets: i = 1 in order four,
+// i = 2-ghost in order two (lower points of a grid off the axis stay unset)
+__device__ __forceinline__ int d1r_first(int ord, int g) { return ord == 2 ? 2 - g : 1; }
 
 // Kreiss-Oliger sixth difference along one direction, the bracket of
 // src/base/dissipation.f90:196-211 (without the -eps/dt/20 factor).

@@ -10,8 +10,11 @@ namespace ollin {
 struct PhysParams {
     int slicing;          // OLLIN_SLICING_*
     double gauge_f;
-    int shift;            // 1 = a Gamma-driver shift is evolved
-    int driver;           // which: 2 Gammadriver2, 1 Gammadriver1, 0 Gammadriver0
+    int shift;            // 1 = the shift is evolved
+    int driver;           // which: 2 Gammadriver2 / shock2, 1 Gammadriver1 / shock1, 0 Gammadriver0,
+                          // 3 zero or static (zero sources, no boundary)
+    int shock;            // the shock-avoiding variant: fdriver evolved
+    int driverD0;         // subtract the t = 0 Delta
     int shiftadvect, driveradv;
     double drivercsi, drivereta;
     double eta;           // Delta damping (momentum-constraint multiple)
@@ -33,6 +36,10 @@ struct StageArgs {
     double* acc[NFIELDS];        // RK4 accumulator (var_a)
     const double* aux[NAUX];     // auxiliary quantities of the stage input
     double* auxw[NAUX];          // writable aux (analysis outputs)
+    int shift_static;            // zero shift sources this stage: shift zero / static, or
+                                 // t(box 0, level 0) < shiftafter (sources_shift.f90:43)
+    const double* d0r;           // Delta at t = 0 (driverD0)
+    const double* d0z;
     int t0;                      // the level's last ``auxiliary`` ran with time == 0
                                  // (phi-based derivatives, auxiliary_geometry.f90:178-202)
     int evolve_phi;              // level time == 0: phi is evolved (it is recomputed from chi otherwise)
@@ -76,6 +83,9 @@ struct AuxArgs {
     // every ``auxiliary`` call of the reference); 0 takes the state as it is
     // (a resumed state that the last ``auxiliary`` call already projected)
     int project;
+    // driverD0: at t = 0 Delta0 = Delta (auxiliary_geometry.f90:1107-1113)
+    double* d0r;
+    double* d0z;
 };
 
 // Parity ghost fill of the evolved fields (generated symmetries_r/_z).
@@ -315,7 +325,17 @@ struct MixArgs {
 
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
 int mix_blocks(const LevelGeom& G);
-void launch_mix_update(const MixArgs& a, cudaStream_t s);
+
+// Orthomin acceleration of the multigrid corrections: up to kOrthoMax stored
+// directions (level-layout FP64 vectors) and their coefficients, by value
+constexpr int kOrthoMax = 8;
+struct OrthoVecs { const double* v[kOrthoMax + 2]; };
+struct OrthoCoef { double c[kOrthoMax]; };
+void launch_mix_apply(const MixArgs& a, double* z64, double* q, cudaStream_t s);
+void launch_mix_dots(const LevelGeom& G, const double* x, const OrthoVecs& y, int n, double* partial, cudaStream_t s);
+void launch_mix_orth(const LevelGeom& G, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
+                     const OrthoCoef& beta, int n, cudaStream_t s);
+void launch_mix_step(const LevelGeom& G, int robin, double* u, const double* z, double alpha, cudaStream_t s);
 
 // The FP64 five-point stencil of a level as the multigrid reads it (level
 // layout, element (i,j) at [i + j*ld]): per-point east/west/north/south
@@ -360,6 +380,11 @@ void launch_ghost_kt2(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale(const StageArgs& a, cudaStream_t s);
 void launch_rhs_sync(const StageArgs& a, cudaStream_t s);
 void launch_rhs_stale_sync(const StageArgs& a, cudaStream_t s);
+// the same four stage kinds with the order-two stencils (rhs_o2*.cu)
+void launch_rhs_o2(const StageArgs& a, cudaStream_t s);
+void launch_rhs_o2_stale(const StageArgs& a, cudaStream_t s);
+void launch_rhs_o2_sync(const StageArgs& a, cudaStream_t s);
+void launch_rhs_o2_stale_sync(const StageArgs& a, cudaStream_t s);
 int sync_table_size(const LevelGeom& P);
 void launch_sync_table(const SyncTableArgs& a, XferPt* tab, cudaStream_t s);
 // maximal slicing (elliptic.cu)
@@ -380,6 +405,10 @@ int norm_blocks(const LevelGeom& G);
 void launch_norms(const LevelGeom& G, const double* f, int origin_bicubic, double rminl, double zminl,
                   double rmaxl, double zmaxl, double* dev_out, double* partials, cudaStream_t s);
 void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s);
+// interp.f90 at n points rz = (r0, z0) pairs of one grid (device arrays);
+// NaN and a count in *bad where the stencil would leave the grid
+void launch_interp_points(const LevelGeom& G, double rminl, double rmaxl, double zminl, double zmaxl, int bicubic,
+                          const double* f, const double* rz, int n, double* out, unsigned int* bad, cudaStream_t s);
 void launch_gammadriver_init(const LevelGeom& G, double* dtbr, double* dtbz, const double* dlr,
                              const double* dlz, double csi, cudaStream_t s);
 // DFMA instructions per second of this GPU (all SMs, independent chains).

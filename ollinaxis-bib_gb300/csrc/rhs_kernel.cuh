@@ -3,7 +3,8 @@
 // One thread owns one grid point (i,j) of one level and does, in registers,
 // everything the reference spreads over ~300 whole-array statements per stage:
 //   * all first, second, mixed and lopsided (advective) derivatives of the
-//     evolved fields (src/base/derivatives.f90, derivadvect.f90, order four);
+//     evolved fields (src/base/derivatives.f90, derivadvect.f90; order four,
+//     or order two with the template parameter ORD = 2);
 //   * the conformal-factor, lapse and curvature algebra of
 //     src/geometry/auxiliary_geometry.f90:49-1502 with calc_conformalRicci1-4
 //     and calc_DIVKTA (non-angmom, BSSN branches);
@@ -43,7 +44,34 @@ struct Deriv5 { double r, z, rr, zz, rz; };
 // (bx, by) is the block's position in its own launch's grid: blockIdx for an
 // ordinary launch, or the block of this evolution in a fused multi-instance
 // launch (multi_kernel)
-template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+// the stencils of the run's finite-difference order
+template <int ORD>
+__device__ __forceinline__ int pcl(int i, int n, int g) {
+    if constexpr (ORD == 2) return pclass2(i, n, g);
+    else return pclass(i, n, g);
+}
+template <int ORD>
+__device__ __forceinline__ double D1(const double* f, long s, int k, double c) {
+    if constexpr (ORD == 2) return d1_2(f, s, k, c);
+    else return d1(f, s, k, c);
+}
+template <int ORD>
+__device__ __forceinline__ double D2(const double* f, long s, int k, double c) {
+    if constexpr (ORD == 2) return d2_2(f, s, k, c);
+    else return d2(f, s, k, c);
+}
+template <int ORD>
+__device__ __forceinline__ double D2RZ(const double* f, long ld, int i, int j, int nr, int nz, int g, double idrz) {
+    if constexpr (ORD == 2) return d2rz_2(f, ld, i, j, nr, nz, g, idrz);
+    else return d2rz(f, ld, i, j, nr, nz, g, idrz);
+}
+template <int ORD>
+__device__ __forceinline__ double DADV(const double* f, long s, int i, int n, int g, bool neg, double ih, bool zdir) {
+    if constexpr (ORD == 2) return dadv_2(f, s, i, n, g, neg, ih);
+    else return dadv(f, s, i, n, g, neg, ih, zdir);
+}
+
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false, int ORD = 4>
 __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsigned by) {
     const LevelGeom& G = A.G;
     const int i = 1 + (int)(bx * blockDim.x + threadIdx.x);
@@ -54,8 +82,10 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     const size_t o = (size_t)i + (size_t)j * (size_t)ld;
     const PhysParams& P = A.P;
 
-    const double cr1 = G.idr * (1.0 / 12.0), cz1 = G.idz * (1.0 / 12.0);
-    const double cr2 = G.idr * G.idr * (1.0 / 12.0), cz2 = G.idz * G.idz * (1.0 / 12.0);
+    // stencil scales: 1/(12h), 1/(12h^2) in order four; 1/(2h), 1/h^2 in order two
+    const double cr1 = ORD == 2 ? 0.5 * G.idr : G.idr * (1.0 / 12.0), cz1 = ORD == 2 ? 0.5 * G.idz : G.idz * (1.0 / 12.0);
+    const double cr2 = ORD == 2 ? G.idr * G.idr : G.idr * G.idr * (1.0 / 12.0);
+    const double cz2 = ORD == 2 ? G.idz * G.idz : G.idz * G.idz * (1.0 / 12.0);
     const double idrz = G.idr * G.idz;
     // The state the derivatives and the point values of this stage are taken
     // from: the stage input, except in the first stage after ``syncboxes``
@@ -72,23 +102,23 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
         if (m >= 0) { X = A.xb; ox = (size_t)m; ldx = A.xb_ld; xin = true; }
         else X = A.xa;
     }
-    const int pcr = xin ? 0 : pclass(i, nr, g), pcz = xin ? 0 : pclass(j, nz, g);
+    const int pcr = xin ? 0 : pcl<ORD>(i, nr, g), pcz = xin ? 0 : pcl<ORD>(j, nz, g);
     // edge position of the mixed derivative: an interior point when copied
     const int ir_ = xin ? 4 : i, jr_ = xin ? 4 : j, nr_ = xin ? (1 << 20) : nr, nz_ = xin ? (1 << 20) : nz;
 
     auto val = [&](int f) { return ld_(X[f] + ox); };
     auto D5p = [&](const double* p) {
         Deriv5 d;
-        d.r = d1(p, 1, pcr, cr1);
-        d.z = d1(p, ldx, pcz, cz1);
-        d.rr = d2(p, 1, pcr, cr2);
-        d.zz = d2(p, ldx, pcz, cz2);
-        d.rz = d2rz(p, ldx, ir_, jr_, nr_, nz_, g, idrz);
+        d.r = D1<ORD>(p, 1, pcr, cr1);
+        d.z = D1<ORD>(p, ldx, pcz, cz1);
+        d.rr = D2<ORD>(p, 1, pcr, cr2);
+        d.zz = D2<ORD>(p, ldx, pcz, cz2);
+        d.rz = D2RZ<ORD>(p, ldx, ir_, jr_, nr_, nz_, g, idrz);
         return d;
     };
     auto D5 = [&](int f) { return D5p(X[f] + ox); };
-    auto Dr = [&](int f) { return d1(X[f] + ox, 1, pcr, cr1); };
-    auto Dz = [&](int f) { return d1(X[f] + ox, ldx, pcz, cz1); };
+    auto Dr = [&](int f) { return D1<ORD>(X[f] + ox, 1, pcr, cr1); };
+    auto Dz = [&](int f) { return D1<ORD>(X[f] + ox, ldx, pcz, cz1); };
     auto aux = [&](int x) { return ld_(A.aux[x] + o); };
 
     const double r = G.rcol[i], ir = G.ircol[i];
@@ -116,13 +146,13 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     Deriv5 da, dao;
     double alpha_o = alpha;
     if constexpr (STALE && SYNC) {
-        const int kr = pclass(i, nr, g), kz = pclass(j, nz, g);
+        const int kr = pcl<ORD>(i, nr, g), kz = pcl<ORD>(j, nz, g);
         const double* p = A.in[F_ALPHA] + o;
-        da.r = d1(p, 1, kr, cr1);
-        da.z = d1(p, ld, kz, cz1);
-        da.rr = d2(p, 1, kr, cr2);
-        da.zz = d2(p, ld, kz, cz2);
-        da.rz = d2rz(p, ld, i, j, nr, nz, g, idrz);
+        da.r = D1<ORD>(p, 1, kr, cr1);
+        da.z = D1<ORD>(p, ld, kz, cz1);
+        da.rr = D2<ORD>(p, 1, kr, cr2);
+        da.zz = D2<ORD>(p, ld, kz, cz2);
+        da.rz = D2RZ<ORD>(p, ld, i, j, nr, nz, g, idrz);
         dao = D5(F_ALPHA);
         alpha_o = ld_(A.alpha_aux + o);
     } else if constexpr (STALE) {
@@ -255,23 +285,30 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     else if (P.slicing == 2) s_alpha = -(sq(alpha_o) + (P.gauge_f - 1.0)) * trK;  // shock avoiding
 
     double s_br = 0, s_bz = 0, s_dbr = 0, s_dbz = 0;
+    // the shock-avoiding drivers' fdriver: its value, its source, and the
+    // source before the advection terms (sources_shift.f90:144, :271)
+    double fdv = 1.0, s_fd = 0.0, s_fd0 = 0.0;
     if constexpr (SHIFT) {
         const double br = val(F_BETAR), bz = val(F_BETAZ), dbr = val(F_DTBETAR), dbz = val(F_DTBETAZ);
         const Deriv5 dbR = D5(F_BETAR), dbZ = D5(F_BETAZ);
         const bool negr = br <= 0.0, negz = bz <= 0.0;
         // Advection term beta^r D_r f + beta^z D_z f with lopsided derivatives
-        // (derivadvect.f90).  Inside i = 4-ghost..Nr-3 the two upwind
-        // stencils are one 5-point sum taken with the stride pointing against
-        // the shift, and beta times its scale is -|beta|/(12 h) for either
-        // sign, so each field costs one stencil and one FMA per direction.
-        const bool lint_r = xin || (i >= 4 - g && i <= nr - 3), lint_z = xin || (j >= 4 - g && j <= nz - 3);
+        // (derivadvect.f90).  Inside i = 4-ghost..Nr-3 (order two:
+        // 3-ghost..Nr-2) the two upwind stencils are one sum taken with the
+        // stride pointing against the shift, and beta times its scale is
+        // -|beta|/(12 h) (order two: -|beta|/(2 h)) for either sign, so each
+        // field costs one stencil and one FMA per direction.
+        constexpr int lo = ORD == 2 ? 3 : 4, hi = ORD == 2 ? 2 : 3;
+        const bool lint_r = xin || (i >= lo - g && i <= nr - hi), lint_z = xin || (j >= lo - g && j <= nz - hi);
         const long lsr = negr ? -1 : 1, lsz = negz ? -ldx : ldx;
-        const double kr = -fabs(br) * (G.idr * (1.0 / 12.0)), kz = -fabs(bz) * (G.idz * (1.0 / 12.0));
+        const double kr = -fabs(br) * (ORD == 2 ? 0.5 * G.idr : G.idr * (1.0 / 12.0));
+        const double kz = -fabs(bz) * (ORD == 2 ? 0.5 * G.idz : G.idz * (1.0 / 12.0));
         auto lop = [&](const double* p, long st) {
-            return 3.0 * ld_(p - st) + 10.0 * ld_(p) - 18.0 * ld_(p + st) + 6.0 * ld_(p + 2 * st) - ld_(p + 3 * st);
+            if constexpr (ORD == 2) return 3.0 * ld_(p) - 4.0 * ld_(p + st) + ld_(p + 2 * st);
+            else return 3.0 * ld_(p - st) + 10.0 * ld_(p) - 18.0 * ld_(p + st) + 6.0 * ld_(p + 2 * st) - ld_(p + 3 * st);
         };
-        auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * dadv(p, 1, i, nr, g, negr, G.idr, false); };
-        auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * dadv(p, ldx, j, nz, g, negz, G.idz, true); };
+        auto ladv_r = [&](const double* p) { return lint_r ? kr * lop(p, lsr) : br * DADV<ORD>(p, 1, i, nr, g, negr, G.idr, false); };
+        auto ladv_z = [&](const double* p) { return lint_z ? kz * lop(p, lsz) : bz * DADV<ORD>(p, ldx, j, nz, g, negz, G.idz, true); };
         // shiftadvect is a template parameter: with it on, the centred
         // derivatives need not stay live for this block
         auto ADVp = [&](const double* p, double dr_, double dz_) {
@@ -289,9 +326,14 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             const double* pb = X[F_BETAR] + ox;
             const double* ic = G.ircol + i;
             auto q = [&](int m) { return ld_(pb + m) * ic[m]; };
-            if (pcr == 0) DD_beta_rr = cr1 * (8.0 * (q(1) - q(-1)) - (q(2) - q(-2)));
-            else if (pcr == 1) DD_beta_rr = cr1 * (3.0 * q(1) + 10.0 * q(0) - 18.0 * q(-1) + 6.0 * q(-2) - q(-3));
-            else DD_beta_rr = cr1 * (25.0 * q(0) - 48.0 * q(-1) + 36.0 * q(-2) - 16.0 * q(-3) + 3.0 * q(-4));
+            if constexpr (ORD == 2) {
+                if (pcr == 0) DD_beta_rr = cr1 * (q(1) - q(-1));
+                else DD_beta_rr = cr1 * (3.0 * q(0) - 4.0 * q(-1) + q(-2));
+            } else {
+                if (pcr == 0) DD_beta_rr = cr1 * (8.0 * (q(1) - q(-1)) - (q(2) - q(-2)));
+                else if (pcr == 1) DD_beta_rr = cr1 * (3.0 * q(1) + 10.0 * q(0) - 18.0 * q(-1) + 6.0 * q(-2) - q(-3));
+                else DD_beta_rr = cr1 * (25.0 * q(0) - 48.0 * q(-1) + 36.0 * q(-2) - 16.0 * q(-3) + 3.0 * q(-4));
+            }
         }
         const double DIV_beta = dbR.r + dbZ.z + br * ir;
         const double Dr_DIV_beta = dbR.rr + dbZ.rz + DD_beta_rr;
@@ -329,21 +371,44 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
         // sources_shift.f90: Gammadriver2 d_t beta = dtbeta (:229-260),
         // Gammadriver1 d_t beta = csi Delta - eta beta (:108-186),
         // Gammadriver0 d_t beta = csi d_t Delta (below, after the Delta source
-        // is complete)
-        if (P.driver == 2) {
-            s_br = dbr;
-            s_bz = dbz;
-        } else if (P.driver == 1) {
-            s_br = P.drivercsi * Dlr;
-            s_bz = P.drivercsi * Dlz;
-        }
-        if (P.driveradv && P.driver != 0) {
-            s_br = s_br + ADV(F_BETAR, dbR.r, dbR.z);
-            s_bz = s_bz + ADV(F_BETAZ, dbZ.r, dbZ.z);
-        }
-        if (P.driver == 1) {
-            s_br = s_br - P.drivereta * br;
-            s_bz = s_bz - P.drivereta * bz;
+        // is complete); the shock-avoiding variants put fdriver on Delta and
+        // evolve it; zero sources for the static shift and before shiftafter
+        // (:43-52)
+        if (A.shift_static) {
+            s_br = 0.0;
+            s_bz = 0.0;
+        } else {
+            if (P.shock) {
+                fdv = val(F_FDRIVER);
+                s_fd0 = -two * third * fdv * DIV_beta;
+                s_fd = s_fd0;
+                if (P.driveradv) {
+                    // lopsided derivatives in the first-order driver, centred ones
+                    // in the second-order one (:150, :277)
+                    if (P.driver == 1) s_fd = s_fd + ADV(F_FDRIVER, Dr(F_FDRIVER), Dz(F_FDRIVER));
+                    else s_fd = s_fd + br * Dr(F_FDRIVER) + bz * Dz(F_FDRIVER);
+                }
+            }
+            const double cf = P.shock ? P.drivercsi * fdv : P.drivercsi;
+            if (P.driver == 2) {
+                s_br = dbr;
+                s_bz = dbz;
+            } else if (P.driver == 1) {
+                s_br = cf * Dlr;
+                s_bz = cf * Dlz;
+            }
+            if (P.driveradv && (P.driver == 1 || P.driver == 2)) {
+                s_br = s_br + ADV(F_BETAR, dbR.r, dbR.z);
+                s_bz = s_bz + ADV(F_BETAZ, dbZ.r, dbZ.z);
+            }
+            if (P.driver == 1) {
+                if (P.driverD0) {
+                    s_br = s_br - cf * ld_(A.d0r + o);
+                    s_bz = s_bz - cf * ld_(A.d0z + o);
+                }
+                s_br = s_br - P.drivereta * br;
+                s_bz = s_bz - P.drivereta * bz;
+            }
         }
         (void)s_dbr; (void)s_dbz;
         if constexpr (SCALAR) {
@@ -387,13 +452,21 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
         return;
     }
 
-    // ---- Kreiss-Oliger dissipation (dissipation.f90:196-211)
-    const bool diss_r = (i >= 4 - g && i <= nr - 3);
-    const bool diss_z = (j >= 4 - g && j <= nz - 3);
+    // ---- Kreiss-Oliger dissipation (dissipation.f90:196-211; order two: the
+    //      fourth difference of :121-135 on i = 3-ghost..Nr-2)
+    constexpr int dlo = ORD == 2 ? 3 : 4, dhi = ORD == 2 ? 2 : 3;
+    constexpr double dscale = ORD == 2 ? 1.0 / 6.0 : 1.0 / 20.0;
+    const bool diss_r = (i >= dlo - g && i <= nr - dhi);
+    const bool diss_z = (j >= dlo - g && j <= nz - dhi);
     if (P.geodiss != 0.0) {
-        const double kd = P.geodiss / G.dt * (1.0 / 20.0);
+        const double kd = P.geodiss / G.dt * dscale;
         auto diss = [&](int f, double& s) {
             const double* p = A.in[f] + o;
+            if constexpr (ORD == 2) {
+                if (diss_r) s = s - kd * ko4(p, 1);
+                if (diss_z) s = s - kd * ko4(p, ld);
+                return;
+            }
             if (diss_r && diss_z) { s = ko6rz_apply(p, ld, kd, s); return; }
             if (diss_r) s = s - kd * ko6(p, 1);
             if (diss_z) s = s - kd * ko6(p, ld);
@@ -407,9 +480,14 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     }
     if constexpr (SCALAR) {
         if (P.scalardiss != 0.0) {
-            const double kd = P.scalardiss / G.dt * (1.0 / 20.0);
+            const double kd = P.scalardiss / G.dt * dscale;
             auto diss = [&](int f, double& s) {
                 const double* p = A.in[f] + o;
+                if constexpr (ORD == 2) {
+                    if (diss_r) s = s - kd * ko4(p, 1);
+                    if (diss_z) s = s - kd * ko4(p, ld);
+                    return;
+                }
                 if (diss_r && diss_z) { s = ko6rz_apply(p, ld, kd, s); return; }
                 if (diss_r) s = s - kd * ko6(p, 1);
                 if (diss_z) s = s - kd * ko6(p, ld);
@@ -420,29 +498,40 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             diss(F_SXIZ, s_sxz);
         }
     }
-    if constexpr (SHIFT) if (P.driver != 2) {
-        // dtbeta is not evolved by the first-order and parabolic drivers
+    if constexpr (SHIFT) if (A.shift_static || P.driver != 2) {
+        // dtbeta is not evolved by the first-order and parabolic drivers, and
+        // keeps a zero source while the shift is static
         s_dbr = 0.0;
         s_dbz = 0.0;
-        if (P.driver == 0) {
+        if (P.driver == 0 && !A.shift_static) {
             s_br = P.drivercsi * s_Dlr;
             s_bz = P.drivercsi * s_Dlz;
         }
     }
-    if constexpr (SHIFT) if (P.driver == 2) {
-        s_dbr = P.drivercsi * s_Dlr;
-        s_dbz = P.drivercsi * s_Dlz;
+    if constexpr (SHIFT) if (!A.shift_static && P.driver == 2) {
+        if (P.shock) {
+            // d_t dtbeta = csi d_t (fdriver Delta) (:273-274)
+            s_dbr = P.drivercsi * (fdv * s_Dlr + s_fd0 * Dlr);
+            s_dbz = P.drivercsi * (fdv * s_Dlz + s_fd0 * Dlz);
+        } else {
+            s_dbr = P.drivercsi * s_Dlr;
+            s_dbz = P.drivercsi * s_Dlz;
+        }
         if (P.driveradv) {
             const double br = val(F_BETAR), bz = val(F_BETAZ);
             const bool negr = br <= 0.0, negz = bz <= 0.0;
             auto DAr = [&](int f) {
-                return ADVECT ? dadv(X[f] + ox, 1, xin ? 4 : i, xin ? (1 << 20) : nr, g, negr, G.idr, false) : Dr(f);
+                return ADVECT ? DADV<ORD>(X[f] + ox, 1, xin ? 4 : i, xin ? (1 << 20) : nr, g, negr, G.idr, false) : Dr(f);
             };
             auto DAz = [&](int f) {
-                return ADVECT ? dadv(X[f] + ox, ldx, xin ? 4 : j, xin ? (1 << 20) : nz, g, negz, G.idz, true) : Dz(f);
+                return ADVECT ? DADV<ORD>(X[f] + ox, ldx, xin ? 4 : j, xin ? (1 << 20) : nz, g, negz, G.idz, true) : Dz(f);
             };
             s_dbr = s_dbr + br * (DAr(F_DTBETAR) - DAr(F_DLR)) + bz * (DAz(F_DTBETAR) - DAz(F_DLR));
             s_dbz = s_dbz + br * (DAr(F_DTBETAZ) - DAr(F_DLZ)) + bz * (DAz(F_DTBETAZ) - DAz(F_DLZ));
+        }
+        if (P.shock && P.driverD0) {
+            s_dbr = s_dbr - P.drivercsi * s_fd * ld_(A.d0r + o);
+            s_dbz = s_dbz - P.drivercsi * s_fd * ld_(A.d0z + o);
         }
         s_dbr = s_dbr - P.drivereta * val(F_DTBETAR);
         s_dbz = s_dbz - P.drivereta * val(F_DTBETAZ);
@@ -525,24 +614,53 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     upd(F_A, s_A); upd(F_B, s_B); upd(F_H, s_H); upd(F_C, s_C);
     upd(F_TRK, s_trK); upd(F_KTA, s_KTA); upd(F_KTB, s_KTB); upd(F_KTC, s_KTC);
     upd(F_DLR, s_Dlr); upd(F_DLZ, s_Dlz);
-    if constexpr (SHIFT) { upd(F_BETAR, s_br); upd(F_BETAZ, s_bz); upd(F_DTBETAR, s_dbr); upd(F_DTBETAZ, s_dbz); }
+    if constexpr (SHIFT) {
+        upd(F_BETAR, s_br); upd(F_BETAZ, s_bz); upd(F_DTBETAR, s_dbr); upd(F_DTBETAZ, s_dbz);
+        if (P.shock) upd(F_FDRIVER, s_fd);
+    }
     if constexpr (SCALAR) { upd(F_SPHI, s_sphi); upd(F_SXIR, s_sxr); upd(F_SXIZ, s_sxz); upd(F_SPI, s_spi); }
     if (bad && A.nanflag) atomicOr(A.nanflag, 1u);
     (void)zero; (void)phi_c;
 }
 
-template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false, int ORD = 4>
 __global__ void __launch_bounds__(OLLIN_RHS_THREADS, OLLIN_RHS_MINBLOCKS) rhs_kernel(const __grid_constant__ StageArgs A) {
     chain_enter();
-    rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC>(A, blockIdx.x, blockIdx.y);
+    rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC, ORD>(A, blockIdx.x, blockIdx.y);
 }
 
 // the fused multi-instance twin of one instantiation
-template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false>
+template <bool SHIFT, bool SCALAR, bool ADVECT, bool STALE, bool SYNC = false, int ORD = 4>
 void register_rhs_multi() {
-    register_multi((const void*)rhs_kernel<SHIFT, SCALAR, ADVECT, STALE, SYNC>,
-                   multi_launch<StageArgs, rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC>, OLLIN_RHS_THREADS,
+    register_multi((const void*)rhs_kernel<SHIFT, SCALAR, ADVECT, STALE, SYNC, ORD>,
+                   multi_launch<StageArgs, rhs_body<SHIFT, SCALAR, ADVECT, STALE, SYNC, ORD>, OLLIN_RHS_THREADS,
                                 OLLIN_RHS_MINBLOCKS>);
+}
+
+// the launch of one stage: the six (shift, scalar, advection) variants of a
+// (stale, sync, order) family
+template <bool STALE, bool SYNC, int ORD>
+void launch_rhs_family(const StageArgs& a, cudaStream_t s) {
+    dim3 blk(32, OLLIN_RHS_THREADS / 32);
+    const int nj = a.G.nz - a.G.jlo + 1;
+    dim3 grd((a.G.nr + blk.x - 1) / blk.x, (nj + blk.y - 1) / blk.y);
+    const bool sh = a.P.shift != 0, sc = a.P.scalar != 0, ad = a.P.shiftadvect != 0;
+    if (!sh && !sc) launch_chained(rhs_kernel<false, false, false, STALE, SYNC, ORD>, grd, blk, s, a);
+    else if (!sh && sc) launch_chained(rhs_kernel<false, true, false, STALE, SYNC, ORD>, grd, blk, s, a);
+    else if (!sc && ad) launch_chained(rhs_kernel<true, false, true, STALE, SYNC, ORD>, grd, blk, s, a);
+    else if (!sc) launch_chained(rhs_kernel<true, false, false, STALE, SYNC, ORD>, grd, blk, s, a);
+    else if (ad) launch_chained(rhs_kernel<true, true, true, STALE, SYNC, ORD>, grd, blk, s, a);
+    else launch_chained(rhs_kernel<true, true, false, STALE, SYNC, ORD>, grd, blk, s, a);
+}
+
+template <bool STALE, bool SYNC, int ORD>
+void register_rhs_family() {
+    register_rhs_multi<false, false, false, STALE, SYNC, ORD>();
+    register_rhs_multi<false, true, false, STALE, SYNC, ORD>();
+    register_rhs_multi<true, false, true, STALE, SYNC, ORD>();
+    register_rhs_multi<true, false, false, STALE, SYNC, ORD>();
+    register_rhs_multi<true, true, true, STALE, SYNC, ORD>();
+    register_rhs_multi<true, true, false, STALE, SYNC, ORD>();
 }
 
 }  // namespace

@@ -594,6 +594,23 @@ dim3 full_grid(const LevelGeom& G, dim3 blk) {
     return dim3((G.nr + G.g + blk.x - 1) / blk.x, (G.nz + G.g + blk.y - 1) / blk.y);
 }
 
+// interp.f90 at n arbitrary points (rz[2k], rz[2k+1]) of one grid: out[k],
+// or NaN where the stencil would leave the grid (counted in *bad)
+__global__ void __launch_bounds__(128) interp_points_kernel(LevelGeom G, double rminl, double rmaxl, double zminl,
+                                                            double zmaxl, int bicubic, const double* f,
+                                                            const double* rz, int n, double* out,
+                                                            unsigned int* bad) {
+    const int k = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (k >= n) return;
+    InterpPt p;
+    if (interp_weights(G, rminl, rmaxl, zminl, zmaxl, rz[2 * k], rz[2 * k + 1], bicubic, p)) {
+        out[k] = interp_apply(G, f, p);
+    } else {
+        out[k] = __longlong_as_double(0x7ff8000000000000LL);
+        atomicAdd(bad, 1u);
+    }
+}
+
 const MultiRegistration reg_symmetry((const void*)symmetry_kernel, multi_launch<SymArgs, symmetry_body, 256, 1>);
 const MultiRegistration reg_prolong((const void*)prolong_tab_kernel,
                                     multi_launch<ProlongArgs, prolong_tab_body, 256, 1>);
@@ -666,6 +683,12 @@ void launch_norms(const LevelGeom& G, const double* f, int bicubic, double rminl
     const int nb = norm_blocks(G);
     norms_partial_kernel<<<nb, kNormThreads, 0, s>>>(G, f, partials);
     norms_final_kernel<<<1, kNormThreads, 0, s>>>(G, f, bicubic, rminl, zminl, rmaxl, zmaxl, partials, nb, dev_out);
+}
+
+void launch_interp_points(const LevelGeom& G, double rminl, double rmaxl, double zminl, double zmaxl, int bicubic,
+                          const double* f, const double* rz, int n, double* out, unsigned int* bad, cudaStream_t s) {
+    if (n <= 0) return;
+    interp_points_kernel<<<(n + 127) / 128, 128, 0, s>>>(G, rminl, rmaxl, zminl, zmaxl, bicubic, f, rz, n, out, bad);
 }
 
 void launch_ham_edges(const LevelGeom& G, double* ham, cudaStream_t s) {

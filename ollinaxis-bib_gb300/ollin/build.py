@@ -13,7 +13,8 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(CSRC, "_build")
 LIB = os.environ.get("OLLIN_GPU_LIB") or os.path.join(BUILD, "libollin_gpu.so")
-SOURCES = ["rhs.cu", "rhs_stale.cu", "rhs_sync.cu", "rhs_stale_sync.cu", "aux.cu", "transfer.cu", "elliptic.cu", "multigrid.cu", "noalloc.cu", "host.cpp", "serve.cpp"]
+SOURCES = ["rhs.cu", "rhs_stale.cu", "rhs_sync.cu", "rhs_stale_sync.cu", "rhs_o2.cu", "rhs_o2_stale.cu",
+           "rhs_o2_sync.cu", "rhs_o2_stale_sync.cu", "aux.cu", "transfer.cu", "elliptic.cu", "multigrid.cu", "noalloc.cu", "host.cpp", "serve.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off,-O2"]
 

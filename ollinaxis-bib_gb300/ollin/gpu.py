@@ -16,7 +16,7 @@ from .params import FIELD_ID, DERIVED_ID, Params
 
 _lib = None
 
-ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENAN", 4: "ENOMEM", 5: "ESTATE"}
+ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENAN", 4: "ENOMEM", 5: "ESTATE", 6: "ECONV"}
 
 
 class OllinError(RuntimeError):
@@ -30,7 +30,7 @@ class LevelDesc(ctypes.Structure):
                 ("dr", ctypes.c_double), ("dz", ctypes.c_double), ("dt", ctypes.c_double),
                 ("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("zmin", ctypes.c_double),
                 ("zmax", ctypes.c_double), ("time", ctypes.c_double), ("steps", ctypes.c_int),
-                ("box", ctypes.c_int)]
+                ("box", ctypes.c_int), ("rbox", ctypes.c_double), ("zbox", ctypes.c_double)]
 
 
 def library_path():
@@ -73,6 +73,9 @@ def load(build_if_missing=True):
     L.ollin_gpu_fp64_rate.restype = ctypes.c_double
     L.ollin_gpu_kernel_stats.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_longlong), dp]
     L.ollin_gpu_ell_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), dp]
+    L.ollin_gpu_ell_history.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.ollin_gpu_interp.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp]
+    L.ollin_gpu_coords.argtypes = [vp, ctypes.c_int, vp, vp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_fused.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
@@ -174,6 +177,14 @@ class Evolution:
         d = self.desc(gid)
         return d.box, d.level
 
+    def coords(self, level):
+        """(r(1-g..Nr), z(1-g..Nz)) of a grid, as the kernels use them."""
+        d = self.desc(level)
+        r = np.zeros(d.nr + d.ghost)
+        z = np.zeros(d.nz + d.ghost)
+        self._check(self.L.ollin_gpu_coords(self.h, level, r.ctypes.data, z.ctypes.data))
+        return r, z
+
     def download(self, level, name):
         """(Nr+g, Nz+g) array indexed [i+g-1, j+g-1] for Fortran (i, j)."""
         d = self.desc(level)
@@ -273,6 +284,24 @@ class Evolution:
         gres = ctypes.c_double()
         self._check(self.L.ollin_gpu_ell_stats(self.h, steps, ctypes.byref(gres)))
         return steps[0], steps[1], gres.value
+
+    def interp(self, level, name, r, z):
+        """``name`` at the points (r, z) of grid ``level`` (interp.f90)."""
+        r = np.asarray(r, dtype=np.float64).ravel()
+        z = np.asarray(z, dtype=np.float64).ravel()
+        rz = np.ascontiguousarray(np.stack([r, z], axis=1))
+        out = np.zeros(len(r))
+        self._check(self.L.ollin_gpu_interp(self.h, level, field_id(name), rz.ctypes.data, len(r), out.ctypes.data))
+        return out
+
+    def ell_history(self, level):
+        """RMS residuals of the last mixed / fp64mg solve on ``level``, one per
+        FP64 refinement (the first before any correction)."""
+        n = ctypes.c_int()
+        self._check(self.L.ollin_gpu_ell_history(self.h, level, None, 0, ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1))
+        self._check(self.L.ollin_gpu_ell_history(self.h, level, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out[:n.value]
 
     def kernel_stats(self):
         """(total rhs-kernel ms, rhs launches, grid points x stages) since timing was enabled."""

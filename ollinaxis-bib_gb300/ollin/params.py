@@ -42,12 +42,14 @@ class Params(ctypes.Structure):
         ("nb", ctypes.c_int), ("nl", ctypes.c_int * 3),
         ("nrbox", ctypes.c_int * 3), ("nzbox", ctypes.c_int * 3),
         ("rbox", ctypes.c_double * 3), ("zbox", ctypes.c_double * 3),
+        ("driverD0", ctypes.c_int), ("shiftafter", ctypes.c_double),
     ]
 
 
 INTEGRATOR = {"rk4": 0, "icn": 1}
 SLICING = {"1+log": 0, "harmonic": 1, "shockavoid": 2, "static": 3, "maximal": 4}
-SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3, "Gammadriver1": 4, "Gammadriver0": 5}
+SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3, "Gammadriver1": 4, "Gammadriver0": 5,
+         "Gammadrivershock1": 6, "Gammadrivershock2": 7}
 BOUND = {"radiative": 0, "none": 1}
 MATTER = {"vacuum": 0, "scalar": 1}
 POTENTIAL = {"none": 0, "phi2": 1, "phi4": 2}
@@ -60,7 +62,7 @@ ILAPSE = {"one": 0, "isotropic": 1, "psiminus2": 2, "psiminus4": 3, "maximal": 4
 # field ids of enum ollin_field
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
           "Delta_r", "Delta_z", "lambda", "Alambda", "beta_r", "beta_z", "dtbeta_r",
-          "dtbeta_z", "scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi"]
+          "dtbeta_z", "scalar_phi", "scalar_xi_r", "scalar_xi_z", "scalar_pi", "fdriver"]
 FIELD_ID = {n: k for k, n in enumerate(FIELDS)}
 DERIVED_ID = {"ham": 64, "mom_r": 65, "mom_z": 66, "RSCAL": 67, "KT2": 68, "Lapla_alpha": 69}
 
@@ -101,6 +103,7 @@ def default_params():
     p.nb = 0
     for k in range(3):
         p.nl[k], p.nrbox[k], p.nzbox[k], p.rbox[k], p.zbox[k] = 0, 1, 1, 0.0, 0.0
+    p.driverD0, p.shiftafter = 0, 0.0
     return p
 
 

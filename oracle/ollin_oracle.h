@@ -24,6 +24,7 @@ int ollin_oracle_constraints(ollin_oracle* o, int level);
 int ollin_oracle_maximal_slicing(ollin_oracle* o, const double* va_max);
 int ollin_oracle_grid(const ollin_oracle* o, int gid, int* box, int* level);
 int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[5]);
+int ollin_oracle_interp(ollin_oracle* o, int level, const char* name, const double* rz, int n, double* out);
 double ollin_oracle_point_updates(const ollin_oracle* o);
 /* OpenMP threads of the oracle's loops from now on (>= 1), and the current
  * number; the CPU baselines time one and all host cores in one process */

@@ -10,7 +10,7 @@
 //   radiative_geometry.f90, constraints.f90,
 //   src/matter/auxiliary_matter.f90, potential.f90, stressenergy.f90,
 //   scalar.f90 (real scalar field).
-// Branches implemented: formulation bssn, angmom false, order four,
+// Branches implemented: formulation bssn, angmom false, order two and four,
 // chimethod, chipower 2, lagrangian flavour with factorhdet.  Each whole-array
 // Fortran statement is one loop over (1-ghost:Nr, 1-ghost:Nz).
 #include "oracle_sim.h"
@@ -25,13 +25,25 @@ namespace oracle {
 static inline int isign1(int s) { return s >= 0 ? 1 : -1; }
 
 // ---------------------------------------------------------------------------
-// derivatives.f90 (order four branch)
+// derivatives.f90 (order two and order four branches)
 // ---------------------------------------------------------------------------
 
-// diff1r: derivatives.f90:15-117
+// diff1r: derivatives.f90:15-117 (order two :50-58: i = 1-ghost is left unset)
 void diff1r(Level& L, const Arr& f, Arr& d, int symr) {
     GRID_DIMS;
     const double idr = 1.0 / L.dr;
+    const double hidr = 0.5 * idr;
+    if (L.order == 2) {
+#pragma omp parallel for schedule(static)
+        for (int j = 1 - g; j <= Nz; ++j) {
+            for (int i = 2 - g; i <= Nr - 1; ++i) d(i, j) = hidr * (f(i + 1, j) - f(i - 1, j));
+            const int i = Nr;
+            d(i, j) = hidr * (3.0 * f(Nr, j) - 4.0 * f(Nr - 1, j) + f(Nr - 2, j));
+            if (L.ownaxis)
+                for (int ii = 1; ii <= g; ++ii) d(1 - ii, j) = -isign1(symr) * d(ii, j);
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 1 - g; j <= Nz; ++j) {
         for (int i = 1; i <= Nr - 2; ++i)
@@ -45,10 +57,26 @@ void diff1r(Level& L, const Arr& f, Arr& d, int symr) {
     }
 }
 
-// diff1z: derivatives.f90:123-241
+// diff1z: derivatives.f90:123-241 (order two :158-172)
 void diff1z(Level& L, const Arr& f, Arr& d, int symz) {
     GRID_DIMS;
     const double idz = 1.0 / L.dz;
+    const double hidz = 0.5 * idz;
+    if (L.order == 2) {
+#pragma omp parallel for schedule(static)
+        for (int j = 2 - g; j <= Nz - 1; ++j)
+            for (int i = 1 - g; i <= Nr; ++i) d(i, j) = hidz * (f(i, j + 1) - f(i, j - 1));
+#pragma omp parallel for schedule(static)
+        for (int i = 1 - g; i <= Nr; ++i) {
+            int j = 1 - g;
+            d(i, j) = -hidz * (3.0 * f(i, j) - 4.0 * f(i, j + 1) + f(i, j + 2));
+            j = Nz;
+            d(i, j) = +hidz * (3.0 * f(i, j) - 4.0 * f(i, j - 1) + f(i, j - 2));
+            if (L.eqsym && L.ownequator)
+                for (int jj = 1; jj <= g; ++jj) d(i, 1 - jj) = -isign1(symz) * d(i, jj);
+        }
+        return;
+    }
     // the interior rows with r innermost (contiguous), then the edge rows and
     // the equator fill: every point gets the statement the reference gives it
 #pragma omp parallel for schedule(static)
@@ -70,11 +98,24 @@ void diff1z(Level& L, const Arr& f, Arr& d, int symz) {
     }
 }
 
-// diff2r: derivatives.f90:250-359
+// diff2r: derivatives.f90:250-359 (order two :285-301)
 void diff2r(Level& L, const Arr& f, Arr& d, int symr) {
     GRID_DIMS;
     const double idr = 1.0 / L.dr;
     const double idr2 = idr * idr;
+    if (L.order == 2) {
+#pragma omp parallel for schedule(static)
+        for (int j = 1 - g; j <= Nz; ++j) {
+            for (int i = 2 - g; i <= Nr - 1; ++i) d(i, j) = idr2 * (f(i + 1, j) - 2.0 * f(i, j) + f(i - 1, j));
+            int i = 1 - g;
+            d(i, j) = idr2 * (2.0 * f(i, j) - 5.0 * f(i + 1, j) + 4.0 * f(i + 2, j) - f(i + 3, j));
+            i = Nr;
+            d(i, j) = idr2 * (2.0 * f(i, j) - 5.0 * f(i - 1, j) + 4.0 * f(i - 2, j) - f(i - 3, j));
+            if (L.ownaxis)
+                for (int ii = 1; ii <= g; ++ii) d(1 - ii, j) = isign1(symr) * d(ii, j);
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 1 - g; j <= Nz; ++j) {
         for (int i = 3 - g; i <= Nr - 2; ++i)
@@ -88,11 +129,26 @@ void diff2r(Level& L, const Arr& f, Arr& d, int symr) {
     }
 }
 
-// diff2z: derivatives.f90:367-488
+// diff2z: derivatives.f90:367-488 (order two :402-418)
 void diff2z(Level& L, const Arr& f, Arr& d, int symz) {
     GRID_DIMS;
     const double idz = 1.0 / L.dz;
     const double idz2 = idz * idz;
+    if (L.order == 2) {
+#pragma omp parallel for schedule(static)
+        for (int j = 2 - g; j <= Nz - 1; ++j)
+            for (int i = 1 - g; i <= Nr; ++i) d(i, j) = idz2 * (f(i, j + 1) - 2.0 * f(i, j) + f(i, j - 1));
+#pragma omp parallel for schedule(static)
+        for (int i = 1 - g; i <= Nr; ++i) {
+            int j = 1 - g;
+            d(i, j) = idz2 * (2.0 * f(i, j) - 5.0 * f(i, j + 1) + 4.0 * f(i, j + 2) - f(i, j + 3));
+            j = Nz;
+            d(i, j) = idz2 * (2.0 * f(i, j) - 5.0 * f(i, j - 1) + 4.0 * f(i, j - 2) - f(i, j - 3));
+            if (L.eqsym && L.ownequator)
+                for (int jj = 1; jj <= g; ++jj) d(i, 1 - jj) = isign1(symz) * d(i, jj);
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 3 - g; j <= Nz - 2; ++j)
         for (int i = 1 - g; i <= Nr; ++i)
@@ -118,6 +174,30 @@ void diff2rz(Level& L, const Arr& f, Arr& d, int symr, int symz) {
     GRID_DIMS;
     const double idr = 1.0 / L.dr, idz = 1.0 / L.dz;
     const double idrz = idr * idz;
+    if (L.order == 2) {
+        // derivatives.f90:533-599: centred inside, one-sided on the outermost
+        // rows and columns, the corners from both one-sided stencils
+#pragma omp parallel for schedule(static)
+        for (int i = 2 - g; i <= Nr - 1; ++i)
+            for (int j = 2 - g; j <= Nz - 1; ++j)
+                d(i, j) = 0.25 * idrz * (f(i + 1, j + 1) + f(i - 1, j - 1) - f(i + 1, j - 1) - f(i - 1, j + 1));
+        for (int j = 2 - g; j <= Nz - 1; ++j) {
+            int i = 1 - g;
+            d(i, j) = -0.25 * idrz * ((3.0 * f(i, j + 1) - 4.0 * f(i + 1, j + 1) + f(i + 2, j + 1))
+                                      - (3.0 * f(i, j - 1) - 4.0 * f(i + 1, j - 1) + f(i + 2, j - 1)));
+            i = Nr;
+            d(i, j) = +0.25 * idrz * ((3.0 * f(i, j + 1) - 4.0 * f(i - 1, j + 1) + f(i - 2, j + 1))
+                                      - (3.0 * f(i, j - 1) - 4.0 * f(i - 1, j - 1) + f(i - 2, j - 1)));
+        }
+        for (int i = 2 - g; i <= Nr - 1; ++i) {
+            int j = 1 - g;
+            d(i, j) = -0.25 * idrz * ((3.0 * f(i + 1, j) - 4.0 * f(i + 1, j + 1) + f(i + 1, j + 2))
+                                      - (3.0 * f(i - 1, j) - 4.0 * f(i - 1, j + 1) + f(i - 1, j + 2)));
+            j = Nz;
+            d(i, j) = +0.25 * idrz * ((3.0 * f(i + 1, j) - 4.0 * f(i + 1, j - 1) + f(i + 1, j - 2))
+                                      - (3.0 * f(i - 1, j) - 4.0 * f(i - 1, j - 1) + f(i - 1, j - 2)));
+        }
+    } else {
 #pragma omp parallel for schedule(static)
     for (int j = 3 - g; j <= Nz - 2; ++j)
         for (int i = 3 - g; i <= Nr - 2; ++i)
@@ -168,6 +248,27 @@ void diff2rz(Level& L, const Arr& f, Arr& d, int symr, int symz) {
                                   - 12.0 * (f(i, j - 1) + f(i - 1, j)) + 3.0 * (f(i, j - 2) + f(i - 2, j))
                                   - 4.0 * (f(i - 1, j - 2) + f(i - 2, j - 1)));
     }
+    }  // order four
+    if (L.order == 2) {
+        // the same four corner statements close the order-two branch
+        // (derivatives.f90:571-597)
+        int i = 1 - g, j = 1 - g;
+        d(i, j) = +0.25 * idrz * (9.0 * f(i, j) + 16.0 * f(i + 1, j + 1) + f(i + 2, j + 2)
+                                  - 12.0 * (f(i, j + 1) + f(i + 1, j)) + 3.0 * (f(i, j + 2) + f(i + 2, j))
+                                  - 4.0 * (f(i + 1, j + 2) + f(i + 2, j + 1)));
+        i = 1 - g; j = Nz;
+        d(i, j) = -0.25 * idrz * (9.0 * f(i, j) + 16.0 * f(i + 1, j - 1) + f(i + 2, j - 2)
+                                  - 12.0 * (f(i + 1, j) + f(i, j - 1)) + 3.0 * (f(i + 2, j) + f(i, j - 2))
+                                  - 4.0 * (f(i + 2, j - 1) + f(i + 1, j - 2)));
+        i = Nr; j = 1 - g;
+        d(i, j) = -0.25 * idrz * (9.0 * f(i, j) + 16.0 * f(i - 1, j + 1) + f(i - 2, j + 2)
+                                  - 12.0 * (f(i, j + 1) + f(i - 1, j)) + 3.0 * (f(i, j + 2) + f(i - 2, j))
+                                  - 4.0 * (f(i - 1, j + 2) + f(i - 2, j + 1)));
+        i = Nr; j = Nz;
+        d(i, j) = +0.25 * idrz * (9.0 * f(i, j) + 16.0 * f(i - 1, j - 1) + f(i - 2, j - 2)
+                                  - 12.0 * (f(i, j - 1) + f(i - 1, j)) + 3.0 * (f(i, j - 2) + f(i - 2, j))
+                                  - 4.0 * (f(i - 1, j - 2) + f(i - 2, j - 1)));
+    }
     // symmetries: z first, then r (derivatives.f90:702-714)
     if (L.eqsym && L.ownequator)
         for (int jj = 1; jj <= g; ++jj)
@@ -178,13 +279,37 @@ void diff2rz(Level& L, const Arr& f, Arr& d, int symr, int symz) {
 }
 
 // ---------------------------------------------------------------------------
-// derivadvect.f90 (order four): lopsided derivatives, side chosen by the
+// derivadvect.f90 (order two and four): lopsided derivatives, side chosen by the
 // sign of the shift component at the point
 // ---------------------------------------------------------------------------
 void diffadvr(Level& L, const Arr& f, Arr& d, int symr) {
     GRID_DIMS;
     const Arr& beta_r = L.a("beta_r");
     const double idr = 1.0 / L.dr;
+    if (L.order == 2) {
+        // derivadvect.f90:50-100: second-order one-sided
+        const double hidr = 0.5 * idr;
+#pragma omp parallel for schedule(static)
+        for (int j = 1 - g; j <= Nz; ++j) {
+            for (int i = 3 - g; i <= Nr - 2; ++i) {
+                if (beta_r(i, j) <= 0.0) d(i, j) = +hidr * (3.0 * f(i, j) - 4.0 * f(i - 1, j) + f(i - 2, j));
+                else d(i, j) = -hidr * (3.0 * f(i, j) - 4.0 * f(i + 1, j) + f(i + 2, j));
+            }
+            int i = 2 - g;
+            if (beta_r(i, j) <= 0.0) d(i, j) = hidr * (f(i + 1, j) - f(i - 1, j));
+            else d(i, j) = -hidr * (3.0 * f(i, j) - 4.0 * f(i + 1, j) + f(i + 2, j));
+            i = 1 - g;
+            d(i, j) = -hidr * (3.0 * f(i, j) - 4.0 * f(i + 1, j) + f(i + 2, j));
+            i = Nr - 1;
+            if (beta_r(i, j) <= 0.0) d(i, j) = hidr * (3.0 * f(i, j) - 4.0 * f(i - 1, j) + f(i - 2, j));
+            else d(i, j) = hidr * (f(i + 1, j) - f(i - 1, j));
+            i = Nr;
+            d(i, j) = hidr * (3.0 * f(i, j) - 4.0 * f(i - 1, j) + f(i - 2, j));
+            if (L.ownaxis)
+                for (int ii = 1; ii <= g; ++ii) d(1 - ii, j) = -symr * d(ii, j);
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 1 - g; j <= Nz; ++j) {
         for (int i = 4 - g; i <= Nr - 3; ++i) {
@@ -220,6 +345,32 @@ void diffadvz(Level& L, const Arr& f, Arr& d, int symz) {
     GRID_DIMS;
     const Arr& beta_z = L.a("beta_z");
     const double idz = 1.0 / L.dz;
+    if (L.order == 2) {
+        // derivadvect.f90:249-299
+        const double hidz = 0.5 * idz;
+#pragma omp parallel for schedule(static)
+        for (int j = 3 - g; j <= Nz - 2; ++j)
+            for (int i = 1 - g; i <= Nr; ++i) {
+                if (beta_z(i, j) <= 0.0) d(i, j) = +hidz * (3.0 * f(i, j) - 4.0 * f(i, j - 1) + f(i, j - 2));
+                else d(i, j) = -hidz * (3.0 * f(i, j) - 4.0 * f(i, j + 1) + f(i, j + 2));
+            }
+#pragma omp parallel for schedule(static)
+        for (int i = 1 - g; i <= Nr; ++i) {
+            int j = 2 - g;
+            if (beta_z(i, j) <= 0.0) d(i, j) = hidz * (f(i, j + 1) - f(i, j - 1));
+            else d(i, j) = -hidz * (3.0 * f(i, j) - 4.0 * f(i, j + 1) + f(i, j + 2));
+            j = 1 - g;
+            d(i, j) = -hidz * (3.0 * f(i, j) - 4.0 * f(i, j + 1) + f(i, j + 2));
+            j = Nz - 1;
+            if (beta_z(i, j) <= 0.0) d(i, j) = hidz * (3.0 * f(i, j) - 4.0 * f(i, j - 1) + f(i, j - 2));
+            else d(i, j) = hidz * (f(i, j + 1) - f(i, j - 1));
+            j = Nz;
+            d(i, j) = hidz * (3.0 * f(i, j) - 4.0 * f(i, j - 1) + f(i, j - 2));
+            if (L.eqsym && L.ownequator)
+                for (int jj = 1; jj <= g; ++jj) d(i, 1 - jj) = -symz * d(i, jj);
+        }
+        return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 4 - g; j <= Nz - 3; ++j)
         for (int i = 1 - g; i <= Nr; ++i) {
@@ -254,11 +405,26 @@ void diffadvz(Level& L, const Arr& f, Arr& d, int symz) {
 }
 
 // ---------------------------------------------------------------------------
-// dissipation.f90 (order four): KO D^6 in r then z, then symmetry fill
+// dissipation.f90: KO D^6 (order four) or D^4 (order two) in r then z, then
+// symmetry fill
 // ---------------------------------------------------------------------------
 void dissipation(Level& L, const Arr& ev, Arr& src, int symr, int symz, double diss) {
     GRID_DIMS;
     const double idt = 1.0 / L.dt;
+    if (L.order == 2) {
+        // dissipation.f90:121-135: D^4 in r, then in z (the mixed operator is
+        // commented out in the reference)
+#pragma omp parallel for schedule(static)
+        for (int j = 1 - g; j <= Nz; ++j)
+            for (int i = 3 - g; i <= Nr - 2; ++i)
+                src(i, j) = src(i, j) - diss * idt * (6.0 * ev(i, j) - 4.0 * (ev(i + 1, j) + ev(i - 1, j))
+                                                      + (ev(i + 2, j) + ev(i - 2, j))) / 6.0;
+#pragma omp parallel for schedule(static)
+        for (int j = 3 - g; j <= Nz - 2; ++j)
+            for (int i = 1 - g; i <= Nr; ++i)
+                src(i, j) = src(i, j) - diss * idt * (6.0 * ev(i, j) - 4.0 * (ev(i, j + 1) + ev(i, j - 1))
+                                                      + (ev(i, j + 2) + ev(i, j - 2))) / 6.0;
+    } else {
 #pragma omp parallel for schedule(static)
     for (int j = 1 - g; j <= Nz; ++j)
         for (int i = 4 - g; i <= Nr - 3; ++i)
@@ -269,6 +435,7 @@ void dissipation(Level& L, const Arr& ev, Arr& src, int symr, int symz, double d
         for (int i = 1 - g; i <= Nr; ++i)
             src(i, j) = src(i, j) - diss * idt * (20.0 * ev(i, j) - 15.0 * (ev(i, j + 1) + ev(i, j - 1))
                                                   + 6.0 * (ev(i, j + 2) + ev(i, j - 2)) - (ev(i, j + 3) + ev(i, j - 3))) / 20.0;
+    }
     if (L.eqsym && L.ownequator)
         for (int jj = 1; jj <= g; ++jj)
             for (int i = 1 - g; i <= Nr; ++i) src(i, 1 - jj) = symz * src(i, jj);
@@ -1134,8 +1301,11 @@ void sources_lapse(Sim& S, Level& L) {
 void sources_shift(Sim& S, Level& L) {
     GRID_DIMS;
     const ollin_params& P = S.P;
+    const double two = 2.0, third = 1.0 / 3.0;
     R(sbeta_r); R(sbeta_z); R(sdtbeta_r); R(sdtbeta_z); R(beta_r); R(beta_z); R(dtbeta_r); R(dtbeta_z);
-    if (P.shift == OLLIN_SHIFT_ZERO || P.shift == OLLIN_SHIFT_STATIC) {  // shiftafter = 0
+    // static shift (:40-52), also before shiftafter (the time of box 0's
+    // level 0); sdtbeta keeps what it holds
+    if (P.shift == OLLIN_SHIFT_ZERO || P.shift == OLLIN_SHIFT_STATIC || S.t[0] < P.shiftafter) {
         ALL sbeta_r(i, j) = 0.0;
         ALL sbeta_z(i, j) = 0.0;
         return;
@@ -1148,14 +1318,38 @@ void sources_shift(Sim& S, Level& L) {
         ALL sdtbeta_z(i, j) = 0.0;
         return;
     }
-    if (P.shift == OLLIN_SHIFT_GAMMADRIVER1) {  // first-order hyperbolic driver (:88-186)
+    auto shift_advection = [&]() {
+        R(DAr_beta_r); R(DAz_beta_r); R(DAr_beta_z); R(DAz_beta_z);
+        ALL sbeta_r(i, j) = sbeta_r(i, j) + beta_r(i, j) * DAr_beta_r(i, j) + beta_z(i, j) * DAz_beta_r(i, j);
+        ALL sbeta_z(i, j) = sbeta_z(i, j) + beta_r(i, j) * DAr_beta_z(i, j) + beta_z(i, j) * DAz_beta_z(i, j);
+    };
+    const bool shock = P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK1 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK2;
+    if (P.shift == OLLIN_SHIFT_GAMMADRIVER1 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK1) {  // (:113-186)
         R(Delta_r); R(Delta_z);
-        ALL sbeta_r(i, j) = P.drivercsi * Delta_r(i, j);
-        ALL sbeta_z(i, j) = P.drivercsi * Delta_z(i, j);
-        if (P.driveradv) {
-            R(DAr_beta_r); R(DAz_beta_r); R(DAr_beta_z); R(DAz_beta_z);
-            ALL sbeta_r(i, j) = sbeta_r(i, j) + beta_r(i, j) * DAr_beta_r(i, j) + beta_z(i, j) * DAz_beta_r(i, j);
-            ALL sbeta_z(i, j) = sbeta_z(i, j) + beta_r(i, j) * DAr_beta_z(i, j) + beta_z(i, j) * DAz_beta_z(i, j);
+        if (!shock) {
+            ALL sbeta_r(i, j) = P.drivercsi * Delta_r(i, j);
+            ALL sbeta_z(i, j) = P.drivercsi * Delta_z(i, j);
+            if (P.driveradv) shift_advection();
+            if (P.driverD0) {
+                R(Delta0_r); R(Delta0_z);
+                ALL sbeta_r(i, j) = sbeta_r(i, j) - P.drivercsi * Delta0_r(i, j);
+                ALL sbeta_z(i, j) = sbeta_z(i, j) - P.drivercsi * Delta0_z(i, j);
+            }
+        } else {
+            R(sfdriver); R(fdriver); R(DIV_beta);
+            ALL sfdriver(i, j) = -two * third * fdriver(i, j) * DIV_beta(i, j);
+            ALL sbeta_r(i, j) = P.drivercsi * fdriver(i, j) * Delta_r(i, j);
+            ALL sbeta_z(i, j) = P.drivercsi * fdriver(i, j) * Delta_z(i, j);
+            if (P.driveradv) {
+                R(DAr_fdriver); R(DAz_fdriver);
+                ALL sfdriver(i, j) = sfdriver(i, j) + beta_r(i, j) * DAr_fdriver(i, j) + beta_z(i, j) * DAz_fdriver(i, j);
+                shift_advection();
+            }
+            if (P.driverD0) {
+                R(Delta0_r); R(Delta0_z);
+                ALL sbeta_r(i, j) = sbeta_r(i, j) - P.drivercsi * fdriver(i, j) * Delta0_r(i, j);
+                ALL sbeta_z(i, j) = sbeta_z(i, j) - P.drivercsi * fdriver(i, j) * Delta0_z(i, j);
+            }
         }
         ALL sbeta_r(i, j) = sbeta_r(i, j) - P.drivereta * beta_r(i, j);
         ALL sbeta_z(i, j) = sbeta_z(i, j) - P.drivereta * beta_z(i, j);
@@ -1163,24 +1357,38 @@ void sources_shift(Sim& S, Level& L) {
         ALL sdtbeta_z(i, j) = 0.0;
         return;
     }
-    // Gammadriver2 (:229-306)
+    // Gammadriver2 and Gammadrivershock2 (:229-306)
     ALL sbeta_r(i, j) = dtbeta_r(i, j);
     ALL sbeta_z(i, j) = dtbeta_z(i, j);
-    if (P.driveradv) {
-        R(DAr_beta_r); R(DAz_beta_r); R(DAr_beta_z); R(DAz_beta_z);
-        ALL sbeta_r(i, j) = sbeta_r(i, j) + beta_r(i, j) * DAr_beta_r(i, j) + beta_z(i, j) * DAz_beta_r(i, j);
-        ALL sbeta_z(i, j) = sbeta_z(i, j) + beta_r(i, j) * DAr_beta_z(i, j) + beta_z(i, j) * DAz_beta_z(i, j);
-    }
+    if (P.driveradv) shift_advection();
     R(sDelta_r); R(sDelta_z);
-    ALL sdtbeta_r(i, j) = P.drivercsi * sDelta_r(i, j);
-    ALL sdtbeta_z(i, j) = P.drivercsi * sDelta_z(i, j);
-    if (P.driveradv) {
+    auto dtbeta_advection = [&]() {
         R(DAr_dtbeta_r); R(DAz_dtbeta_r); R(DAr_Delta_r); R(DAz_Delta_r);
         R(DAr_dtbeta_z); R(DAz_dtbeta_z); R(DAr_Delta_z); R(DAz_Delta_z);
         ALL sdtbeta_r(i, j) = sdtbeta_r(i, j) + beta_r(i, j) * (DAr_dtbeta_r(i, j) - DAr_Delta_r(i, j))
             + beta_z(i, j) * (DAz_dtbeta_r(i, j) - DAz_Delta_r(i, j));
         ALL sdtbeta_z(i, j) = sdtbeta_z(i, j) + beta_r(i, j) * (DAr_dtbeta_z(i, j) - DAr_Delta_z(i, j))
             + beta_z(i, j) * (DAz_dtbeta_z(i, j) - DAz_Delta_z(i, j));
+    };
+    if (!shock) {
+        ALL sdtbeta_r(i, j) = P.drivercsi * sDelta_r(i, j);
+        ALL sdtbeta_z(i, j) = P.drivercsi * sDelta_z(i, j);
+        if (P.driveradv) dtbeta_advection();
+    } else {
+        R(sfdriver); R(fdriver); R(DIV_beta); R(Delta_r); R(Delta_z);
+        ALL sfdriver(i, j) = -two * third * fdriver(i, j) * DIV_beta(i, j);
+        ALL sdtbeta_r(i, j) = P.drivercsi * (fdriver(i, j) * sDelta_r(i, j) + sfdriver(i, j) * Delta_r(i, j));
+        ALL sdtbeta_z(i, j) = P.drivercsi * (fdriver(i, j) * sDelta_z(i, j) + sfdriver(i, j) * Delta_z(i, j));
+        if (P.driveradv) {
+            R(Dr_fdriver); R(Dz_fdriver);
+            ALL sfdriver(i, j) = sfdriver(i, j) + beta_r(i, j) * Dr_fdriver(i, j) + beta_z(i, j) * Dz_fdriver(i, j);
+            dtbeta_advection();
+        }
+        if (P.driverD0) {
+            R(Delta0_r); R(Delta0_z);
+            ALL sdtbeta_r(i, j) = sdtbeta_r(i, j) - P.drivercsi * sfdriver(i, j) * Delta0_r(i, j);
+            ALL sdtbeta_z(i, j) = sdtbeta_z(i, j) - P.drivercsi * sfdriver(i, j) * Delta0_z(i, j);
+        }
     }
     ALL sdtbeta_r(i, j) = sdtbeta_r(i, j) - P.drivereta * dtbeta_r(i, j);
     ALL sdtbeta_z(i, j) = sdtbeta_z(i, j) - P.drivereta * dtbeta_z(i, j);
@@ -1292,13 +1500,13 @@ void radiative_geometry(Sim& S, Level& L) {
         for (int j = 1 - g; j <= Nz; ++j) { sbeta_r(0, j) = 0.0; sbeta_z(0, j) = 0.0; }
         for (int i = 1 - g; i <= Nr; ++i) { sbeta_r(i, 0) = 0.0; sbeta_z(i, 0) = 0.0; }
     }
-    if (P.shift == OLLIN_SHIFT_GAMMADRIVER1 && P.drivercsi != 0.0) {  // on Delta
+    if ((P.shift == OLLIN_SHIFT_GAMMADRIVER1 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK1) && P.drivercsi != 0.0) {
         R(Delta_r); R(sDelta_r); R(Dr_Delta_r); R(Dz_Delta_r);
         R(Delta_z); R(sDelta_z); R(Dr_Delta_z); R(Dz_Delta_z);
         radbound(L, Delta_r, sDelta_r, Dr_Delta_r, Dz_Delta_r, vs, var0);
         radbound(L, Delta_z, sDelta_z, Dr_Delta_z, Dz_Delta_z, vs, var0);
     }
-    if (P.shift == OLLIN_SHIFT_GAMMADRIVER2 && P.drivercsi != 0.0) {
+    if ((P.shift == OLLIN_SHIFT_GAMMADRIVER2 || P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK2) && P.drivercsi != 0.0) {
         R(dtbeta_r); R(sdtbeta_r); R(Dr_dtbeta_r); R(Dz_dtbeta_r);
         R(dtbeta_z); R(sdtbeta_z); R(Dr_dtbeta_z); R(Dz_dtbeta_z);
         radbound(L, dtbeta_r, sdtbeta_r, Dr_dtbeta_r, Dz_dtbeta_r, vs, var0);

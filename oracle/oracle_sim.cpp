@@ -28,11 +28,14 @@ namespace oracle {
 // ---------------------------------------------------------------------------
 static void setup(Sim& S) {
     const ollin_params& P = S.P;
-    if (P.order != 4) throw std::runtime_error("oracle: only order four is restated");
+    if (P.order != 4 && P.order != 2) throw std::runtime_error("oracle: order must be two or four");
     if (P.chipower != 2 || !P.chimethod) throw std::runtime_error("oracle: chimethod with chipower 2 only");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) throw std::runtime_error("oracle: lagrangian+factorhdet+evolveH only");
     if (P.evolveKTH) throw std::runtime_error("oracle: evolveKTH unsupported");
-    S.g = P.ghost ? P.ghost : 3;
+    // main.f90:286-318: 2 ghost zones for order two, 3 for order four, or
+    // the par file's number when it is not smaller
+    const int gmin = P.order == 2 ? 2 : 3;
+    S.g = std::max(P.ghost, gmin);
     const int g = S.g;
     // setupboxes.f90:25-80: boxes and their levels
     if (P.nb < 0 || P.nb > 3) throw std::runtime_error("The number of refinement boxes must be between 0 and 3");
@@ -101,7 +104,7 @@ static void setup(Sim& S) {
         const int b = grids[k].first, l = grids[k].second;
         Level& lv = S.L[k];
         lv.gid = k;
-        lv.level = l; lv.box = b; lv.g = g; lv.Nr = Nrbox[b]; lv.Nz = Nzbox[b];
+        lv.level = l; lv.box = b; lv.g = g; lv.order = P.order; lv.Nr = Nrbox[b]; lv.Nz = Nzbox[b];
         // finebound/restrict partner: level 1 of any box talks to the base grid
         lv.parent = -1;
         if (l > 0) {
@@ -690,7 +693,9 @@ static void initialize(Sim& S) {
         currentgrid(S, L);
         auxiliary(S, L);
     }
-    if (S.P.shift == OLLIN_SHIFT_GAMMADRIVER2) {
+    // evolve.f90:174-195: dtbeta = csi Delta for the second-order drivers,
+    // unless driverD0
+    if ((S.P.shift == OLLIN_SHIFT_GAMMADRIVER2 || S.P.shift == OLLIN_SHIFT_GAMMADRIVERSHOCK2) && !S.P.driverD0) {
         for (Level& L : S.L) {
             Arr& b = L.a("dtbeta_r"); Arr& bz = L.a("dtbeta_z"); Arr& dr_ = L.a("Delta_r"); Arr& dz_ = L.a("Delta_z");
             for (size_t q = 0; q < b.v.size(); ++q) { b.v[q] = S.P.drivercsi * dr_.v[q]; bz.v[q] = S.P.drivercsi * dz_.v[q]; }
@@ -833,6 +838,20 @@ int ollin_oracle_norms(ollin_oracle* o, int level, const char* name, double out[
         auto it = L.arrs.find(name);
         if (it == L.arrs.end()) { g_oracle_err = std::string("unknown array ") + name; return 1; }
         norms(o->S, level, it->second, out);
+        return 0;
+    } catch (const std::exception& e) {
+        g_oracle_err = e.what();
+        return 1;
+    }
+}
+
+// interp.f90 at n points rz = (r0, z0) pairs of grid ``level``
+int ollin_oracle_interp(ollin_oracle* o, int level, const char* name, const double* rz, int n, double* out) {
+    try {
+        Level& L = o->S.L[level];
+        auto it = L.arrs.find(name);
+        if (it == L.arrs.end()) { g_oracle_err = std::string("unknown array ") + name; return 1; }
+        for (int k = 0; k < n; ++k) out[k] = interp(o->S, level, it->second, rz[2 * k], rz[2 * k + 1]);
         return 0;
     } catch (const std::exception& e) {
         g_oracle_err = e.what();

@@ -12,6 +12,7 @@ namespace oracle {
 
 struct Level {
     int level = 0, g = 3, Nr = 0, Nz = 0;
+    int order = 4;             // finite-difference order (param order: 2 or 4)
     int box = 0, parent = -1;  // refinement box; grid of the next coarser level (finebound/restrict)
     int gid = 0;               // index in Sim::L
     double dr = 0, dz = 0, dt = 0, time = 0;

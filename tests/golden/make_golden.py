@@ -151,6 +151,35 @@ CASES = {
                             _elliptic=True),
     "max_noeqsym_sor": dict(BASE, nrtotal=16, nztotal=16, nl0=0, dr0=0.25, dz0=0.25, eqsym=False,
                             maximalevery=1, ell_solver="sor", _steps=[0, 1], _elliptic=True),
+    # the shock-avoiding drivers (sources_shift.f90:141-170, :268-294): fdriver
+    # evolved with -2/3 fdriver DIV beta, the advection terms on; the second
+    # one with driverD0 (the t = 0 Delta subtracted, no dtbeta initialisation)
+    "gds1_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadrivershock1",
+                       drivercsi=0.75, drivereta=2.0, driveradv=True, _steps=[0, 1, 3]),
+    "gds2_d0": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, shift="Gammadrivershock2",
+                    drivercsi=0.75, drivereta=2.0, driveradv=True, driverD0=True, _steps=[0, 1, 3]),
+    # shiftafter: the shift sources are zero until t(0,0) reaches it (dt0 =
+    # 0.05: the first two coarse steps), while the dtbeta boundary still acts
+    "gd2_shiftafter": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, shift="Gammadriver2",
+                           drivercsi=0.75, drivereta=2.0, shiftafter=0.1, _steps=[0, 1, 3, 4]),
+    # order two (the reference's default order, two ghost zones): centred
+    # second-order differences, second-order one-sided advection and the
+    # fourth-difference dissipation (derivatives.f90, derivadvect.f90,
+    # dissipation.f90 :121-135), with the hierarchy's strips and margins
+    # from ghost = 2: the puncture on 2 levels, the Gamma driver on 3
+    "o2_c1": dict(BASE, order="two", nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, _steps=[0, 1, 2, 4]),
+    "o2_shift": dict(BASE, order="two", nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver2",
+                     drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # without equatorial symmetry (the one-sided rows at the lower z edge), a
+    # massive scalar field with the shift
+    "o2_noeqsym_scalar": dict(BASE, order="two", nrtotal=16, nztotal=16, nl0=1, dr0=0.25, dz0=0.25,
+                              eqsym=False, idata="minkowski", ilapse="one", mattertype="scalar",
+                              scalarpotential="phi2", scalar_mass=0.5, shift="Gammadriver2", drivercsi=0.75,
+                              drivereta=2.0, scalardiss=0.02, _steps=[0, 1, 3]),
+    # the wave elliptic solver on order-two stencils, then one step
+    "o2_ell_pulse": dict(BASE, order="two", nrtotal=16, nztotal=16, nl0=0, dr0=0.5, dz0=0.5, idata="scalarpulse",
+                         ilapse="one", mattertype="scalar", scalar_a0=0.05, scalardiss=0.02, _steps=[0, 1],
+                         _elliptic=True),
 }
 
 FIELDS = ["alpha", "phi", "chi", "A", "B", "H", "C", "trK", "KTA", "KTB", "KTH", "KTC",
@@ -199,6 +228,8 @@ def run_case(refdir, name, cfg):
     names = list(FIELDS)
     if cfg.get("shift", "none") != "none":
         names += SHIFT_FIELDS
+    if cfg.get("shift", "none").startswith("Gammadrivershock"):
+        names += ["fdriver"]
     if cfg.get("mattertype") == "scalar":
         names += SCALAR_FIELDS
     out = {}
@@ -229,7 +260,10 @@ def run_case(refdir, name, cfg):
                 for nm in DERIVED:
                     out["s%d_L%d_%s" % (done, lev, nm)] = sim.field(lev, nm)
             out["s%d_L%d_time" % (done, lev)] = np.array(sim.time(lev))
-    meta = dict(cfg, steps=steps, fields=names, grids=[list(sim.box_level(k)) for k in sim.levels()])
+    import ftn_subset
+    meta = dict(cfg, steps=steps, fields=names, grids=[list(sim.box_level(k)) for k in sim.levels()],
+                oob_beyond_reads=ftn_subset.OOB_BEYOND[0])
+    ftn_subset.OOB_BEYOND[0] = 0
     out["meta"] = np.array(json.dumps(meta))
     return out
 

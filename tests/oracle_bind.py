@@ -44,6 +44,8 @@ def lib():
         L.ollin_oracle_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
         L.ollin_oracle_grid.argtypes = [vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.ollin_oracle_norms.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p]
+        L.ollin_oracle_interp.argtypes = [vp, ctypes.c_int, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int,
+                                          ctypes.c_void_p]
         L.ollin_oracle_point_updates.argtypes = [vp]
         L.ollin_oracle_point_updates.restype = ctypes.c_double
         L.ollin_oracle_last_error.restype = ctypes.c_char_p
@@ -132,6 +134,16 @@ class Oracle:
     def norms(self, level, name):
         out = np.zeros(5)
         self._check(self.L.ollin_oracle_norms(self.h, level, name.encode(), out.ctypes.data))
+        return out
+
+    def interp(self, level, name, r, z):
+        """``name`` at the points (r, z) of grid ``level`` (interp.f90)."""
+        r = np.asarray(r, dtype=np.float64).ravel()
+        z = np.asarray(z, dtype=np.float64).ravel()
+        rz = np.ascontiguousarray(np.stack([r, z], axis=1))
+        out = np.zeros(len(r))
+        self._check(self.L.ollin_oracle_interp(self.h, level, name.encode(), rz.ctypes.data, len(r),
+                                               out.ctypes.data))
         return out
 
     def point_updates(self):

@@ -16,7 +16,7 @@ OUT_NAMES = ("alpha", "phi", "trK", "ham")
 def load_fixture(name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     meta = json.loads(str(d["meta"]))
-    cfg = {k: v for k, v in meta.items() if k not in ("steps", "fields", "grids")}
+    cfg = {k: v for k, v in meta.items() if k not in ("steps", "fields", "grids", "oob_beyond_reads")}
     cfg["eqsym"] = 1 if cfg.get("eqsym") else 0
     return d, meta, cfg
 
@@ -29,3 +29,44 @@ def fixture_stats(a, g=3):
     origin = float(w @ a[g - 2:g + 2, g - 2:g + 2] @ w)
     return (float(inner.max()), float(inner.min()), float(np.abs(inner).max()),
             float(np.sqrt(np.mean(inner ** 2))), origin)
+
+
+class OracleView:
+    """What the 1-D and 2-D writers read (grids, descriptors, coordinates,
+    arrays, interpolation), from an oracle evolution with box 0 only."""
+
+    class Desc:
+        pass
+
+    def __init__(self, oracle, cfg):
+        self.o = oracle
+        self.cfg = cfg
+
+    def levels(self):
+        return self.o.levels()
+
+    def grid(self, gid):
+        return self.o.grid(gid)
+
+    def coords(self, gid):
+        r, z = self.o.get(gid, "r"), self.o.get(gid, "z")
+        return r[:, 0].copy(), z[0, :].copy()
+
+    def desc(self, gid):
+        nr, nz, g = self.o.dims(gid)
+        box, level = self.o.grid(gid)
+        r, z = self.coords(gid)
+        d = OracleView.Desc()
+        d.nr, d.nz, d.ghost, d.box, d.level = nr, nz, g, box, level
+        d.dr = self.cfg["dr0"] / 2.0 ** level
+        d.dz = self.cfg["dz0"] / 2.0 ** level
+        d.rmin, d.rmax, d.zmin, d.zmax = r[0], r[-1], z[0], z[-1]
+        d.time = self.o.time(gid)
+        d.rbox = d.zbox = 0.0
+        return d
+
+    def download(self, gid, name):
+        return self.o.get(gid, name)
+
+    def interp(self, gid, name, r, z):
+        return self.o.interp(gid, name, r, z)

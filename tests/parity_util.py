@@ -34,6 +34,8 @@ def field_list(cfg):
     names = list(BASE_FIELDS)
     if cfg.get("shift", "none") != "none":
         names += SHIFT_FIELDS
+    if str(cfg.get("shift", "none")).startswith("Gammadrivershock"):
+        names += ["fdriver"]
     if cfg.get("mattertype") == "scalar":
         names += SCALAR_FIELDS
     return names

@@ -70,10 +70,11 @@ def test_unsupported_parameters_are_rejected_before_any_device_work():
     from ollin import gpu
     from ollin.params import params_from_dict
     lib = gpu.load()
-    p = params_from_dict(dict(order="two", eqsym=1))
+    # a par-file ghost larger than the order needs (main.f90:298-318 keeps it)
+    p = params_from_dict(dict(order="four", ghost=4, eqsym=1))
     h = ctypes.c_void_p()
     rc = lib.ollin_gpu_create(ctypes.byref(p), ctypes.byref(h))
-    assert rc == 1 and b"order" in lib.ollin_gpu_last_error()
+    assert rc == 1 and b"ghost" in lib.ollin_gpu_last_error()
 
 
 @pytest.mark.skipif(os.path.exists("/dev/nvidia0"), reason="host has a GPU")

@@ -108,6 +108,14 @@ def test_maximal_every_step_without_equatorial_symmetry(solver):
     run(dict(EVERY, eqsym=0, nl0=0, ell_solver=solver), 2)
 
 
+@pytest.mark.parametrize("solver", ["wave", "sor"])
+def test_maximal_every_step_order_two(solver):
+    """Order two: the wave solver's second-order physical Laplacian and
+    fourth-difference dissipation, and the coefficient derivatives of either
+    solver on second-order stencils."""
+    run(dict(EVERY, order="two", ell_solver=solver), 2)
+
+
 def test_maximal_every_step_with_refinement_boxes():
     """Box 0's level 1 and an overlapping box above it: the wave solver's box
     loops and syncboxes, then the stale lapse of the next stage on each grid."""

@@ -10,12 +10,16 @@
   evolution bit for bit; ollin_gpu_initialize runs the reference's
   post-restart sequence instead (``auxiliary`` re-projects the metric, and
   with the Gamma-driver shift dtbeta = drivercsi Delta, evolve.f90:174-195),
-  which stays within rounding of the uninterrupted evolution."""
+  which stays within rounding of the uninterrupted evolution.
+* 1-D and 2-D records (save1Ddata.f90, save2Ddata.f90) of the GPU state
+  against the same writers fed by the oracle after the same steps, and the
+  point interpolation behind the diagonals (ollin_gpu_interp, interp.f90)."""
 import numpy as np
 import pytest
 
-from ollin.output import Save0D, header, lines
-from output_util import OUT_NAMES, fixture_stats, load_fixture
+from ollin.output import Save0D, header, lines, lines_1d, lines_2d
+from oracle_bind import Oracle
+from output_util import OUT_NAMES, OracleView, fixture_stats, load_fixture
 from parity_util import C1, params
 
 pytestmark = pytest.mark.gpu
@@ -157,3 +161,69 @@ def test_clocks_only_before_initialize():
     with pytest.raises(OllinError):
         e.set_clocks(0, [1.0, 0.5, 0.0, 2.0])
     e.close()
+
+
+def _numbers(rec, width):
+    return [float(rec[k:k + width]) for k in range(0, len(rec), width)]
+
+
+@pytest.mark.parametrize("eqsym", [1, 0], ids=["eqsym", "no_eqsym"])
+def test_1d_2d_records_match_oracle(eqsym):
+    from ollin.gpu import Evolution
+    cfg = dict(C1, nrtotal=24, nztotal=24, nl0=1, eqsym=eqsym)
+    o = Oracle(params(cfg))
+    e = Evolution(params(cfg))
+    for x in (o, e):
+        x.initial_data()
+        x.initialize()
+    for _ in range(2):
+        assert o.step() == e.step()
+    v = OracleView(o, cfg)
+    for lev in o.levels():
+        for nm in ("alpha", "trK"):
+            got, ref = lines_1d(e, lev, nm, eqsym), lines_1d(v, lev, nm, eqsym)
+            assert sorted(got) == sorted(ref)
+            for ext in got:
+                assert got[ext][0] == ref[ext][0] and len(got[ext]) == len(ref[ext]), ext
+                a = np.array([_numbers(x, 20) for x in got[ext][1:-1]])
+                b = np.array([_numbers(x, 20) for x in ref[ext][1:-1]])
+                assert np.array_equal(a[:, 0], b[:, 0]), ext
+                scale = max(np.abs(b[:, 1]).max(), 1e-6)
+                assert np.abs(a[:, 1] - b[:, 1]).max() <= 1e-9 * scale, (lev, nm, ext)
+            g2, r2 = lines_2d(e, lev, nm, True), lines_2d(v, lev, nm, True)
+            assert g2[0] == r2[0] and len(g2) == len(r2)
+            a = np.array([_numbers(x, 23) for x in g2[1:] if x])
+            b = np.array([_numbers(x, 23) for x in r2[1:] if x])
+            assert np.array_equal(a[:, :2], b[:, :2])
+            assert np.abs(a[:, 2] - b[:, 2]).max() <= 1e-9 * max(np.abs(b[:, 2]).max(), 1e-6)
+
+
+def test_interp_points_match_oracle():
+    """ollin_gpu_interp against the oracle's interp.f90 at random points of
+    each level (bicubic inside, bilinear next to the edges), at nodes (a
+    copy), and a point outside the grid refused."""
+    from ollin.gpu import Evolution, OllinError
+    cfg = dict(C1, nrtotal=24, nztotal=24, nl0=1)
+    o = Oracle(params(cfg))
+    e = Evolution(params(cfg))
+    for x in (o, e):
+        x.initial_data()
+        x.initialize()
+    assert o.step() == e.step()
+    rng = np.random.default_rng(5)
+    for lev in o.levels():
+        r, z = e.coords(lev)
+        rr = rng.uniform(r[0], r[-1], 200)
+        zz = rng.uniform(z[0], z[-1], 200)
+        for nm in ("alpha", "KTA"):
+            a, b = e.interp(lev, nm, rr, zz), o.interp(lev, nm, rr, zz)
+            assert np.abs(a - b).max() <= 1e-10 * max(np.abs(b).max(), 1e-6), (lev, nm)
+            # at nodes: the node's value (copied when r0 - r(1-ghost) divides
+            # by dr exactly, else a Lagrange stencil whose weights are 0 and 1)
+            node = e.interp(lev, nm, r[5:8], z[4:7])
+            arr = e.download(lev, nm)
+            want = np.array([arr[5, 4], arr[6, 5], arr[7, 6]])
+            assert np.abs(node - want).max() <= 1e-13 * max(np.abs(want).max(), 1e-6), (lev, nm)
+            assert np.abs(node - o.interp(lev, nm, r[5:8], z[4:7])).max() <= 1e-13 * max(np.abs(want).max(), 1e-6)
+        with pytest.raises(OllinError):
+            e.interp(lev, "alpha", [r[-1] + 10.0], [z[3]])

@@ -184,6 +184,46 @@ def test_first_order_and_parabolic_gamma_drivers(cfg):
     run(cfg, 8, check_every=4)
 
 
+# order two (the reference's default order): two ghost zones, centred
+# second-order differences, second-order lopsided advection and the fourth-
+# difference dissipation; the hierarchy's strips and margins follow ghost = 2
+@pytest.mark.parametrize("cfg", [
+    dict(C1, order="two", nrtotal=32, nztotal=32),
+    dict(C1, order="two", nrtotal=32, nztotal=32, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+    dict(C1, order="two", nrtotal=32, nztotal=32, nl0=1, dr0=0.25, dz0=0.25, eqsym=0, idata="minkowski",
+         ilapse="one", mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5, shift="Gammadriver2",
+         drivercsi=0.75, drivereta=2.0, scalardiss=0.02),
+    dict(C1, order="two", nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
+         gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25),
+], ids=["puncture_three_levels", "gammadriver2_three_levels", "scalar_shift_no_eqsym", "icn_harmonic"])
+def test_order_two(cfg):
+    o, e, w = run(cfg, 8, check_every=4)
+    for lev in o.levels():
+        o.constraints(lev)
+        for nm in ["ham", "mom_r", "mom_z"]:
+            ng, no = e.norms(lev, nm), o.norms(lev, nm)
+            for k in (2, 3):
+                assert abs(ng[k] - no[k]) <= 1e-8 * max(abs(no[k]), 1e-12), (lev, nm, k, ng[k], no[k])
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(C1, nrtotal=32, nztotal=32, shift="Gammadrivershock1", drivercsi=0.75, drivereta=2.0, driveradv=1),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="Gammadrivershock2", drivercsi=0.75, drivereta=2.0, driveradv=1,
+         driverD0=1),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="Gammadrivershock2", drivercsi=0.75, drivereta=2.0, eqsym=0),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="Gammadriver1", drivercsi=0.75, drivereta=1.0, driverD0=1),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, shiftafter=0.3),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, shift="zero"),
+], ids=["shock1_driveradv_three_levels", "shock2_driverD0_driveradv", "shock2_no_eqsym", "gammadriver1_driverD0",
+        "gammadriver2_shiftafter", "zero_shift"])
+def test_shock_avoiding_and_static_shifts(cfg):
+    """sources_shift.f90:40-52 (zero and static shifts, and any driver before
+    shiftafter: zero shift sources, the driver's boundary still acting),
+    :141-170 and :268-294 (the shock-avoiding drivers: fdriver evolved with
+    -2/3 fdriver DIV beta on Delta), driverD0 (the t = 0 Delta subtracted)."""
+    run(cfg, 8, check_every=4)
+
+
 def test_icn_harmonic_isotropic():
     cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
                gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)
@@ -226,7 +266,8 @@ RING = dict(C1, nrtotal=24, nztotal=24, nl0=0, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nr
             zbox1=5.0, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)
 
 
-@pytest.mark.parametrize("cfg", [BOXES, RING], ids=["axis_and_ring_boxes", "ring_off_equator_shift"])
+@pytest.mark.parametrize("cfg", [BOXES, RING, dict(RING, order="two")],
+                         ids=["axis_and_ring_boxes", "ring_off_equator_shift", "ring_order_two"])
 def test_refinement_boxes(cfg):
     """Box loops of onestep.f90 (every box of a level, restriction of each box
     into box 0's level 0 or its own coarser level), the lower-edge strips of
@@ -267,12 +308,16 @@ def test_refinement_boxes(cfg):
 
 
 # box 0's level 1 around the origin and box 1 on the axis above it overlap
-# on level 1 (syncboxes.f90)
+# on level 1 (syncboxes.f90).  In order two (ghost = 2) the box is 15 points
+# high, so that its nodes coincide with box 0's (Nzbox - ghost + 1 even),
+# and sits higher, so that no point a copy reads was written by the other
+# copy of the level (a chain the device refuses)
 OVERLAP = dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
 
 
-@pytest.mark.parametrize("cfg", [OVERLAP, dict(OVERLAP, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)],
-                         ids=["overlap", "overlap_shift"])
+@pytest.mark.parametrize("cfg", [OVERLAP, dict(OVERLAP, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=5.0)],
+                         ids=["overlap", "overlap_shift", "overlap_order_two"])
 def test_overlapping_boxes(cfg):
     """syncboxes copies the evolved and auxiliary arrays of the partner box
     on each box's strips; the next first stage reads the auxiliary

@@ -12,7 +12,8 @@ from parity_util import params, scalar_pulse
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["c1_small", "c2_small", "icn_harmonic", "scalar_shift", "noeqsym_shift", "box_two", "box_ring_shift",
-         "box_overlap", "gd1_shift", "gd0_noeqsym"]
+         "box_overlap", "gd1_shift", "gd0_noeqsym", "o2_c1", "o2_shift", "o2_noeqsym_scalar", "gds1_shift",
+         "gds2_d0", "gd2_shiftafter"]
 
 # The oracle restates the reference statement by statement; the remaining
 # differences come from libm (exp/log/pow) last-bit differences amplified by
@@ -27,7 +28,7 @@ def load(name):
 
 
 def cfg_of(meta):
-    skip = {"steps", "fields", "grids"}
+    skip = {"steps", "fields", "grids", "oob_beyond_reads"}
     cfg = {k: v for k, v in meta.items() if k not in skip}
     cfg["eqsym"] = 1 if cfg.get("eqsym") else 0
     return cfg
@@ -91,7 +92,7 @@ def test_oracle_matches_reference_fortran(name):
 
 
 ELL_CASES = ["ell_pulse_1lev", "ell_pulse_2lev", "ell_brill_2lev", "ell_sor_2lev", "ell_pulse_noeqsym",
-             "ell_pulse_boxes", "ell_sor_boxes", "ell_sor_noeqsym"]
+             "ell_pulse_boxes", "ell_sor_boxes", "ell_sor_noeqsym", "o2_ell_pulse"]
 
 
 def ell_cfg(meta):

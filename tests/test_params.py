@@ -36,7 +36,7 @@ def test_par_file_values():
 
 def test_unknown_values_are_refused():
     with pytest.raises(ValueError):
-        params_from_par("shift = Gammadrivershock2\n")
+        params_from_par("shift = Gammadriver3\n")
     with pytest.raises(ValueError):
         params_from_par("nosuchparameter = 3\n")
 
@@ -53,6 +53,10 @@ def test_refinement_box_parameters():
 
 
 def test_gamma_driver_names():
-    """shift = Gammadriver0 / 1 / 2 (param.f90 names, sources_shift.f90)."""
-    for name, code in (("Gammadriver0", 5), ("Gammadriver1", 4), ("Gammadriver2", 3)):
+    """shift = Gammadriver0 / 1 / 2, the shock-avoiding drivers, zero and
+    static (param.f90:344 names, sources_shift.f90); driverD0, shiftafter."""
+    for name, code in (("Gammadriver0", 5), ("Gammadriver1", 4), ("Gammadriver2", 3), ("Gammadrivershock1", 6),
+                       ("Gammadrivershock2", 7), ("zero", 1), ("static", 2)):
         assert params_from_par("shift = %s\n" % name).shift == code
+    p = params_from_par("shift = Gammadrivershock2\ndriverD0 = .true.\nshiftafter = 1.5\n")
+    assert p.driverD0 == 1 and p.shiftafter == 1.5
