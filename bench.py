@@ -290,18 +290,22 @@ def run_gpu(args):
             e.L.ollin_gpu_download(e.h, lev, field_id(nm), ctypes.c_void_p(host[(lev, nm)].data_ptr()),
                                    d.nr + d.ghost)
     bytes_per_dir = sum(t.numel() * 8 for t in host.values())
+    # the whole state in one ollin_gpu_upload_many / download_many call per
+    # direction and step: every array of the reference's layout, one
+    # synchronisation each way
+    nq = len(host)
+    q_lev = (ctypes.c_int * nq)(*[lev for (lev, _) in host])
+    q_fld = (ctypes.c_int * nq)(*[field_id(nm) for (_, nm) in host])
+    q_ptr = (ctypes.c_void_p * nq)(*[t.data_ptr() for t in host.values()])
+    q_ld = (ctypes.c_int * nq)(*[t.shape[1] for t in host.values()])
     e2e_steps = max(2, args.steps // 2)
     barrier(pg)
     t0 = time.perf_counter()
     pu1 = e.point_updates()
     for _ in range(e2e_steps):
-        for (lev, nm), t in host.items():
-            rc = e.L.ollin_gpu_upload(e.h, lev, field_id(nm), ctypes.c_void_p(t.data_ptr()), t.shape[1])
-            assert rc == 0
+        assert e.L.ollin_gpu_upload_many(e.h, nq, q_lev, q_fld, q_ptr, q_ld) == 0
         e.step()
-        for (lev, nm), t in host.items():
-            rc = e.L.ollin_gpu_download(e.h, lev, field_id(nm), ctypes.c_void_p(t.data_ptr()), t.shape[1])
-            assert rc == 0
+        assert e.L.ollin_gpu_download_many(e.h, nq, q_lev, q_fld, q_ptr, q_ld) == 0
     torch.cuda.synchronize()
     dt_e2e = max_over_ranks(pg, time.perf_counter() - t0)
     e2e_value = sum_over_ranks(pg, e.point_updates() - pu1) / dt_e2e

@@ -86,9 +86,10 @@ extern "C" {
 #define OLLIN_ELL_WAVE          1   /* ELL_solver = "wave" (WaveElliptic, the default) */
 #define OLLIN_ELL_SOR           2   /* ELL_solver = "sor"  */
 #define OLLIN_ELL_MIXED         3   /* "mixed": no counterpart in the reference -- the system that "sor"
-                                       converges to, solved by FP64 iterative refinement with FP32 multigrid
-                                       corrections, to an RMS residual of ELL_epsilon or the FP64
-                                       rounding floor of the residual, whichever is larger */
+                                       converges to, solved by FP64 iterative refinement (exactly summed
+                                       residuals) whose FP32 multigrid corrections are Orthomin search
+                                       directions, to an RMS residual of ELL_epsilon (interior and Robin
+                                       rows each) plus two refinements, or the FP64 floor */
 #define OLLIN_ELL_FP64MG        4   /* "fp64mg": no counterpart in the reference -- the same solve as "mixed"
                                        with FP64 multigrid corrections: the all-FP64 solve of the system
                                        that the mixed-precision solve's error is measured against */
@@ -226,6 +227,17 @@ int ollin_gpu_coords(const ollin_handle* h, int level, double* r, double* z);
  * Replaces direct access to grid(0,level)%<field> (generated mytypes.f90). */
 int ollin_gpu_upload(ollin_handle* h, int level, int field, const double* a, int ld_r);
 int ollin_gpu_download(ollin_handle* h, int level, int field, double* a, int ld_r);
+
+/* n uploads / downloads in one call: copy k moves ``fields[k]`` of grid
+ * ``levels[k]`` from / to the host array a[k] (leading dimension ld_r[k]),
+ * as ollin_gpu_upload / ollin_gpu_download do, with one synchronisation for
+ * all of them.  Evolved fields only; every copy is checked before any is
+ * queued.  A host that moves a whole state per step (a Fortran driver that
+ * keeps its arrays) uses these. */
+int ollin_gpu_upload_many(ollin_handle* h, int n, const int* levels, const int* fields, const double* const* a,
+                          const int* ld_r);
+int ollin_gpu_download_many(ollin_handle* h, int n, const int* levels, const int* fields, double* const* a,
+                            const int* ld_r);
 
 /* The value of ``field`` at n arbitrary points of grid ``level``: rz holds
  * (r0, z0) pairs, out receives n values (host arrays).  Replaces
@@ -399,8 +411,8 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
  * Laplacian, falpha and advective derivatives of the lapse before the solve.
  * ELL_solver = "mixed" solves the same discrete system as "sor" with FP64
  * residuals and FP32 multigrid corrections, "fp64mg" with FP64 ones (no
- * counterpart in the reference); both need eqsym and Nb = 0.  "wave" and
- * "sor" work without equatorial symmetry too. */
+ * counterpart in the reference); both need eqsym and work with refinement
+ * boxes.  "wave" and "sor" work without equatorial symmetry too. */
 int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
 
 /* Iterations of the elliptic solve run by ollin_gpu_initial_data for
@@ -546,11 +558,12 @@ const char* ollin_gpu_last_error(void);
  * synchronise the device, tools that may only read.
  *
  * d_field points at element (1-ghost, 1-ghost) of a column-major
- * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost must be 3
- * and the grid equatorially symmetric (box-0 coordinates r = (i-1/2) dr,
- * z = (j-1/2) dz); eqsym = 0 is refused with OLLIN_EINVAL.  ``stream`` is a
- * cudaStream_t or NULL; the call returns after the result has reached ``out``
- * (host memory).  out[4] is the bicubic origin value, which is
+ * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost is 3
+ * (order four) or 2 (order two) and the grid equatorially symmetric (box-0
+ * coordinates r = (i-1/2) dr, z = (j-1/2) dz); eqsym = 0 is refused with
+ * OLLIN_EINVAL.  ``stream`` is a cudaStream_t or NULL; the call returns after
+ * the result has reached ``out`` (host memory), so a capturing stream is
+ * refused with OLLIN_EINVAL.  out[4] is the bicubic origin value, which is
  * save0Dvariable's for interporder = "bicubic" (the default) only.
  *
  * Limit: nz - ghost <= 8192 interior rows (larger grids get OLLIN_EINVAL).

@@ -605,6 +605,19 @@ constexpr int kMixBX = 32, kMixBY = 4, kMixThreads = kMixBX * kMixBY;
 
 __device__ __forceinline__ int mir(int k) { return k < 1 ? 1 - k : k; }
 
+// The unknowns of a level's system: i from 1 on a grid that owns the axis
+// (mirrored ghosts), from 2-ghost on a refinement box off it, where the
+// outermost ghost column is the Dirichlet row from the parent, as SOR sweeps
+// them (sor_elliptic.f90:648); likewise in z.  The upper rows nr, nz are
+// Robin rows on the coarse problem and Dirichlet rows otherwise.
+__device__ __forceinline__ int mix_ilo(const LevelGeom& G) { return G.axis ? 1 : 2 - G.g; }
+__device__ __forceinline__ int mix_jlo(const LevelGeom& G) { return G.equator ? 1 : 2 - G.g; }
+// element (p, q) of a level array, mirrored across the axis / equator where
+// the grid owns them
+__device__ __forceinline__ size_t mix_at(const LevelGeom& G, int p, int q) {
+    return (size_t)(G.axis ? mir(p) : p) + (size_t)(G.equator ? mir(q) : q) * (size_t)G.ld;
+}
+
 __device__ __forceinline__ void block_partial(double v, double* out) {
     __shared__ double red[kMixThreads];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -661,7 +674,7 @@ __device__ __forceinline__ bool mix_row(const MixArgs& A, const UF& U, int i, in
                                         bool& interior) {
     const LevelGeom& G = A.G;
     const int nr = G.nr, nz = G.nz;
-    interior = i <= nr - 1 && j <= nz - 1;
+    interior = i <= nr - 1 && j <= nz - 1;  // and i >= mix_ilo, j >= mix_jlo (the callers' range)
     RowSum<EXACT> acc;
     if (interior) {
         if (!A.pa) {
@@ -721,11 +734,12 @@ __device__ __forceinline__ bool mix_row(const MixArgs& A, const UF& U, int i, in
 __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_constant__ MixArgs A) {
     const LevelGeom& G = A.G;
     const long ld = G.ld;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     double sq = 0.0, sc = 0.0, sb = 0.0;
+    (void)ld;
     if (i <= G.nr && j <= G.nz) {
-        auto U = [&](int p, int q) { return A.u[(size_t)mir(p) + (size_t)mir(q) * ld]; };
+        auto U = [&](int p, int q) { return A.u[mix_at(G, p, q)]; };
         const size_t o = (size_t)i + (size_t)j * ld;
         double R = 0.0, r = 0.0;
         bool interior;
@@ -764,11 +778,12 @@ __global__ void __launch_bounds__(kMixThreads) mix_apply_kernel(const __grid_con
                                                                  double* q) {
     const LevelGeom& G = A.G;
     const long ld = G.ld;
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     auto Z = [&](int p, int qq) {
-        const size_t oo = (size_t)mir(p) + (size_t)mir(qq) * ld;
+        // the correction is zero on a Dirichlet row (left zero by the solve)
+        const size_t oo = mix_at(G, p, qq);
         return A.d64 ? A.d64[oo] : (double)A.d[oo];
     };
     const size_t o = (size_t)i + (size_t)j * ld;
@@ -782,8 +797,8 @@ __global__ void __launch_bounds__(kMixThreads) mix_apply_kernel(const __grid_con
 // per-block sums of x * y[k] over the unknowns, k < n (partial[k*nblocks+b])
 __global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, const double* x, OrthoVecs Y, int n,
                                                                 double* partial) {
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const bool in = i <= G.nr && j <= G.nz;
     const size_t o = in ? (size_t)i + (size_t)j * G.ld : 0;
     const double xv = in ? x[o] : 0.0;
@@ -794,8 +809,8 @@ __global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, cons
 // z -= sum_k beta_k Z_k, q -= sum_k beta_k Q_k
 __global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, double* z, double* q, OrthoVecs Zs,
                                                                 OrthoVecs Qs, OrthoCoef beta, int n) {
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const size_t o = (size_t)i + (size_t)j * G.ld;
     double zv = z[o], qv = q[o];
@@ -810,8 +825,8 @@ __global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, doub
 // u += alpha z at the unknowns that are not Dirichlet rows
 __global__ void __launch_bounds__(kMixThreads) mix_step_kernel(LevelGeom G, int robin, double* u, const double* z,
                                                                 double alpha) {
-    const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int lim_r = robin ? G.nr : G.nr - 1, lim_z = robin ? G.nz : G.nz - 1;
     if (i > lim_r || j > lim_z) return;
     const size_t o = (size_t)i + (size_t)j * G.ld;
@@ -820,39 +835,46 @@ __global__ void __launch_bounds__(kMixThreads) mix_step_kernel(LevelGeom G, int 
 
 }  // namespace
 
+// the mixed kernels' blocks over a level's unknowns
+static dim3 mix_grid(const LevelGeom& G) {
+    const int ni = G.nr - (G.axis ? 1 : 2 - G.g) + 1, nj = G.nz - (G.equator ? 1 : 2 - G.g) + 1;
+    return dim3((ni + kMixBX - 1) / kMixBX, (nj + kMixBY - 1) / kMixBY);
+}
+
 int mix_blocks(const LevelGeom& G) {
-    const int nx = (G.nr + kMixBX - 1) / kMixBX, ny = (G.nz + kMixBY - 1) / kMixBY;
+    const int ni = G.nr - (G.axis ? 1 : 2 - G.g) + 1, nj = G.nz - (G.equator ? 1 : 2 - G.g) + 1;
+    const int nx = (ni + kMixBX - 1) / kMixBX, ny = (nj + kMixBY - 1) / kMixBY;
     return nx * ny;
 }
 
 void launch_mix_resid(const MixArgs& a, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
+    dim3 grd = mix_grid(a.G);
     mix_resid_kernel<<<grd, blk, 0, s>>>(a);
 }
 
 void launch_mix_apply(const MixArgs& a, double* z64, double* q, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd((a.G.nr + kMixBX - 1) / kMixBX, (a.G.nz + kMixBY - 1) / kMixBY);
+    dim3 grd = mix_grid(a.G);
     mix_apply_kernel<<<grd, blk, 0, s>>>(a, z64, q);
 }
 
 void launch_mix_dots(const LevelGeom& G, const double* x, const OrthoVecs& y, int n, double* partial, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    dim3 grd = mix_grid(G);
     mix_dots_kernel<<<grd, blk, 0, s>>>(G, x, y, n, partial);
 }
 
 void launch_mix_orth(const LevelGeom& G, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
                      const OrthoCoef& beta, int n, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    dim3 grd = mix_grid(G);
     mix_orth_kernel<<<grd, blk, 0, s>>>(G, z, q, Zs, Qs, beta, n);
 }
 
 void launch_mix_step(const LevelGeom& G, int robin, double* u, const double* z, double alpha, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd((G.nr + kMixBX - 1) / kMixBX, (G.nz + kMixBY - 1) / kMixBY);
+    dim3 grd = mix_grid(G);
     mix_step_kernel<<<grd, blk, 0, s>>>(G, robin, u, z, alpha);
 }
 

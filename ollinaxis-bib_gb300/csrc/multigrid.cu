@@ -12,10 +12,12 @@
 //   aE = krr (1/Hr + 1/(2 r_I))/Hr + vr/(2Hr),  aW = krr (1/Hr - 1/(2 r_I))/Hr - vr/(2Hr)
 //   aN = kzz/Hz^2 + vz/(2Hz),                    aS = kzz/Hz^2 - vz/(2Hz)
 //   e  = -2 (krr/Hr^2 + kzz/Hz^2) + s
-// per cell of a grid of n x m cells, cell centres r_I = (I-1/2) Hr,
-// z_J = (J-1/2) Hz, Hr = 2^k dr, with d(0,J) = d(1,J), d(I,0) = d(I,1) (axis
-// and equator mirrors); Robin rows I = n / J = m on the coarse problem, zero
-// rows on the Dirichlet problems of the finer refinement levels.  The nine-
+// per cell of a grid of n x m cells, cell centres r_I = r0 + (I-1/2) Hr,
+// z_J = (J-1/2) Hz, Hr = 2^k dr; at the lower edges d(0,J) = d(1,J),
+// d(I,0) = d(I,1) (axis and equator mirrors) or, on a refinement box off the
+// axis or the equator, d = 0 there (the Dirichlet row of its problem); Robin
+// rows I = n / J = m on the coarse problem, zero rows on the Dirichlet
+// problems of the finer refinement levels and boxes.  The nine-
 // point couplings of a metric with g^rz /= 0 are left to the FP64 residual of
 // the outer iteration.
 // Cell (I,J) of grid k+1 covers cells 2I-1..2I x 2J-1..2J of grid k: the
@@ -35,6 +37,8 @@ namespace {
 template <typename T>
 struct Grid {
     int n, m, ld;
+    int mr, mz;                          // lower edges mirrored (1) or Dirichlet zero rows (0)
+    T r0;                                // r of the lower face of cell 1
     T hr, hz;                            // spacings
     T* d; T* r;                          // correction, right-hand side
     T* krr; T* kzz; T* vr; T* vz; T* s;  // coefficient fields
@@ -42,8 +46,11 @@ struct Grid {
 
 __device__ __forceinline__ int mirror(int k) { return k < 1 ? 1 - k : k; }
 
+// a Dirichlet lower edge keeps index 0 at zero, so it reads as it is
 template <typename T>
-__device__ __forceinline__ T Dv(const Grid<T>& G, int i, int j) { return G.d[mirror(i) + mirror(j) * G.ld]; }
+__device__ __forceinline__ T Dv(const Grid<T>& G, int i, int j) {
+    return G.d[(G.mr ? mirror(i) : i) + (G.mz ? mirror(j) : j) * G.ld];
+}
 
 template <typename T>
 struct Stencil { T e, w, n, s, c; };
@@ -51,7 +58,7 @@ struct Stencil { T e, w, n, s, c; };
 template <typename T>
 __device__ __forceinline__ Stencil<T> stencil(const Grid<T>& G, int i, int j) {
     const int o = i + j * G.ld;
-    const T ri = ((T)i - T(0.5)) * G.hr;
+    const T ri = G.r0 + ((T)i - T(0.5)) * G.hr;
     const T krr = G.krr[o], kzz = G.kzz[o];
     const T ihr = T(1.0) / G.hr, ihz = T(1.0) / G.hz;
     const T ur = T(0.5) * G.vr[o] * ihr, uz = T(0.5) * G.vz[o] * ihz;
@@ -95,15 +102,16 @@ __device__ __forceinline__ T robin_res(const Grid<T>& G, int i, int j) {
 }
 
 // Gauss-Seidel update of one interior cell (the mirrored neighbours across
-// the axis and the equator fold into the diagonal)
+// the axis and the equator fold into the diagonal; a Dirichlet lower row
+// contributes nothing)
 template <typename T>
 __device__ __forceinline__ void relax(const Grid<T>& G, int i, int j) {
     const Stencil<T> q = stencil(G, i, j);
     const int o = i + j * G.ld;
     T diag = q.c;
     T off = q.e * G.d[o + 1] + q.n * G.d[o + G.ld];
-    if (i > 1) off += q.w * G.d[o - 1]; else diag += q.w;
-    if (j > 1) off += q.s * G.d[o - G.ld]; else diag += q.s;
+    if (i > 1) off += q.w * G.d[o - 1]; else if (G.mr) diag += q.w;
+    if (j > 1) off += q.s * G.d[o - G.ld]; else if (G.mz) diag += q.s;
     G.d[o] = (G.r[o] - off) / diag;
 }
 
@@ -196,6 +204,7 @@ __global__ void __launch_bounds__(128) mg_prolong_kernel(Grid<T> F, Grid<T> C, i
     const int I = (i + 1) / 2, J = (j + 1) / 2;
     const int I2 = (i & 1) ? I - 1 : I + 1, J2 = (j & 1) ? J - 1 : J + 1;
     auto c = [&](int p, int q) {
+        if ((p < 1 && !C.mr) || (q < 1 && !C.mz)) return T(0.0);  // a Dirichlet lower row
         p = p < 1 ? 1 : (p > C.n ? C.n : p);
         q = q < 1 ? 1 : (q > C.m ? C.m : q);
         return C.d[p + q * C.ld];
@@ -220,8 +229,9 @@ __global__ void __launch_bounds__(128) mg_coarsen_kernel(Grid<T> F, Grid<T> C) {
 }
 
 // grid 0 from the level's FP64 five-point stencil (level layout: element
-// (i,j) at [i + j*ld]): krr = (a+b) dr^2/2, vr = (a-b) dr - krr/r,
-// kzz = (c+d) dz^2/2, vz = (c-d) dz, s = e + 2 (krr/dr^2 + kzz/dz^2)
+// (i,j) at [i + j*ld]; cell (I,J) is level point (I + ioff, J + joff)):
+// krr = (a+b) dr^2/2, vr = (a-b) dr - krr/r, kzz = (c+d) dz^2/2,
+// vz = (c-d) dz, s = e + 2 (krr/dr^2 + kzz/dz^2)
 template <typename T>
 __global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, MgStencil S) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
@@ -233,10 +243,11 @@ __global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, MgStencil S) {
         G.krr[o] = T(0.0); G.kzz[o] = T(0.0); G.vr[o] = T(0.0); G.vz[o] = T(0.0); G.s[o] = T(0.0);
         return;
     }
-    const size_t q = (size_t)i + (size_t)j * S.ld;
-    const double a = S.pa ? S.pa[q] : S.ca[i], b = S.pb ? S.pb[q] : S.cb[i];
+    const long li = (long)i + S.ioff, lj = (long)j + S.joff;
+    const long q = li + lj * S.ld;
+    const double a = S.pa ? S.pa[q] : S.ca[li], b = S.pb ? S.pb[q] : S.cb[li];
     const double c = S.pc ? S.pc[q] : S.cc, d = S.pd ? S.pd[q] : S.cc;
-    const double dr = S.dr, dz = S.dz, ri = ((double)i - 0.5) * dr;
+    const double dr = S.dr, dz = S.dz, ri = S.r0 + ((double)i - 0.5) * dr;
     const double krr = (a + b) * (dr * dr) * 0.5, kzz = (c + d) * (dz * dz) * 0.5;
     G.krr[o] = (T)krr;
     G.kzz[o] = (T)kzz;
@@ -247,22 +258,22 @@ __global__ void __launch_bounds__(128) mg_load_kernel(Grid<T> G, MgStencil S) {
 
 // the right-hand side of grid 0 (the hierarchy's precision, level layout); d = 0
 template <typename T>
-__global__ void __launch_bounds__(128) mg_rhs_kernel(Grid<T> G, const T* r, long ld) {
+__global__ void __launch_bounds__(128) mg_rhs_kernel(Grid<T> G, const T* r, long ld, int ioff, int joff) {
     const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.n + 1 || j > G.m + 1) return;
     const int o = i + j * G.ld;
     G.d[o] = T(0.0);
     const bool in = i >= 1 && i <= G.n && j >= 1 && j <= G.m;
-    G.r[o] = in ? r[(size_t)i + (size_t)j * ld] : T(0.0);
+    G.r[o] = in ? r[(long)(i + ioff) + (long)(j + joff) * ld] : T(0.0);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) mg_store_kernel(Grid<T> G, T* d, long ld) {
+__global__ void __launch_bounds__(128) mg_store_kernel(Grid<T> G, T* d, long ld, int ioff, int joff) {
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.n || j > G.m) return;
-    d[(size_t)i + (size_t)j * ld] = G.d[i + j * G.ld];
+    d[(long)(i + ioff) + (long)(j + joff) * ld] = G.d[i + j * G.ld];
 }
 
 template <typename T>
@@ -273,6 +284,7 @@ template <typename T>
 struct MgGrids {
     std::vector<Grid<T>> g;
     T* pool = nullptr;
+    int ioff = 0, joff = 0;  // level point of cell (0, 0)
 
     bool create(int n, int m, double dr, double dz) {
         size_t total = 0;
@@ -300,6 +312,13 @@ struct MgGrids {
 
     void load(const MgStencil& S, cudaStream_t s) {
         dim3 blk(32, 4);
+        ioff = S.ioff;
+        joff = S.joff;
+        for (Grid<T>& G : g) {
+            G.mr = S.mr;
+            G.mz = S.mz;
+            G.r0 = (T)S.r0;
+        }
         const Grid<T>& G0 = g[0];
         mg_load_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, S);
         for (size_t k = 1; k < g.size(); ++k) mg_coarsen_kernel<T><<<cells(g[k], blk), blk, 0, s>>>(g[k - 1], g[k]);
@@ -308,7 +327,7 @@ struct MgGrids {
     void rhs(const T* r, long ld, cudaStream_t s) {
         dim3 blk(32, 4);
         const Grid<T>& G0 = g[0];
-        mg_rhs_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, r, ld);
+        mg_rhs_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, r, ld, ioff, joff);
     }
 
     void smooth(const Grid<T>& G, int robin, int sweeps, cudaStream_t s) {
@@ -341,7 +360,7 @@ struct MgGrids {
     void solve(int robin, int ncycles, T* d, long ld, cudaStream_t s) {
         for (int c = 0; c < ncycles; ++c) vcycle(0, robin, s);
         dim3 blk(32, 4);
-        mg_store_kernel<T><<<cells(g[0], blk), blk, 0, s>>>(g[0], d, ld);
+        mg_store_kernel<T><<<cells(g[0], blk), blk, 0, s>>>(g[0], d, ld, ioff, joff);
     }
 };
 

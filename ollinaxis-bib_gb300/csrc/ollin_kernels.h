@@ -347,6 +347,12 @@ struct MgStencil {
     const double* e;
     long ld;
     double dr, dz;
+    // the level point of multigrid cell (0, 0), r of the lower face of cell
+    // 1, and whether the lower edges are the axis / equator mirrors (else
+    // Dirichlet rows of a refinement box off them)
+    int ioff, joff;
+    double r0;
+    int mr, mz;
 };
 // Geometric multigrid for the correction equation (multigrid.cu), FP32 or
 // FP64 (fp64 = 1); r and d are arrays of that precision

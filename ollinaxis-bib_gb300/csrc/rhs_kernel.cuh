@@ -285,9 +285,10 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     else if (P.slicing == 2) s_alpha = -(sq(alpha_o) + (P.gauge_f - 1.0)) * trK;  // shock avoiding
 
     double s_br = 0, s_bz = 0, s_dbr = 0, s_dbz = 0;
-    // the shock-avoiding drivers' fdriver: its value, its source, and the
-    // source before the advection terms (sources_shift.f90:144, :271)
-    double fdv = 1.0, s_fd = 0.0, s_fd0 = 0.0;
+    // the shock-avoiding drivers' fdriver source (sources_shift.f90:144,
+    // :271), formed after the dissipation so that nothing of it stays live
+    // through the kernel's widest region
+    double s_fd = 0.0;
     if constexpr (SHIFT) {
         const double br = val(F_BETAR), bz = val(F_BETAZ), dbr = val(F_DTBETAR), dbz = val(F_DTBETAZ);
         const Deriv5 dbR = D5(F_BETAR), dbZ = D5(F_BETAZ);
@@ -378,18 +379,7 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             s_br = 0.0;
             s_bz = 0.0;
         } else {
-            if (P.shock) {
-                fdv = val(F_FDRIVER);
-                s_fd0 = -two * third * fdv * DIV_beta;
-                s_fd = s_fd0;
-                if (P.driveradv) {
-                    // lopsided derivatives in the first-order driver, centred ones
-                    // in the second-order one (:150, :277)
-                    if (P.driver == 1) s_fd = s_fd + ADV(F_FDRIVER, Dr(F_FDRIVER), Dz(F_FDRIVER));
-                    else s_fd = s_fd + br * Dr(F_FDRIVER) + bz * Dz(F_FDRIVER);
-                }
-            }
-            const double cf = P.shock ? P.drivercsi * fdv : P.drivercsi;
+            const double cf = P.shock ? P.drivercsi * val(F_FDRIVER) : P.drivercsi;
             if (P.driver == 2) {
                 s_br = dbr;
                 s_bz = dbz;
@@ -508,9 +498,28 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
             s_bz = P.drivercsi * s_Dlz;
         }
     }
+    // d_t fdriver = -2/3 fdriver DIV beta (+ beta . D fdriver): lopsided
+    // derivatives in the first-order driver, centred ones in the second-order
+    // one (:144-151, :271-278); DIV beta again from the shift's stencils
+    double s_fd0 = 0.0;
+    if constexpr (SHIFT) if (P.shock && !A.shift_static) {
+        const double fdv = val(F_FDRIVER), br = val(F_BETAR), bz = val(F_BETAZ);
+        s_fd0 = -two * third * fdv * (Dr(F_BETAR) + Dz(F_BETAZ) + br * ir);
+        s_fd = s_fd0;
+        if (P.driveradv) {
+            if (P.driver == 1 && ADVECT) {
+                const double* pf = X[F_FDRIVER] + ox;
+                s_fd = s_fd + (br * DADV<ORD>(pf, 1, xin ? 4 : i, xin ? (1 << 20) : nr, g, br <= 0.0, G.idr, false)
+                               + bz * DADV<ORD>(pf, ldx, xin ? 4 : j, xin ? (1 << 20) : nz, g, bz <= 0.0, G.idz, true));
+            } else {
+                s_fd = s_fd + br * Dr(F_FDRIVER) + bz * Dz(F_FDRIVER);
+            }
+        }
+    }
     if constexpr (SHIFT) if (!A.shift_static && P.driver == 2) {
         if (P.shock) {
             // d_t dtbeta = csi d_t (fdriver Delta) (:273-274)
+            const double fdv = val(F_FDRIVER);
             s_dbr = P.drivercsi * (fdv * s_Dlr + s_fd0 * Dlr);
             s_dbz = P.drivercsi * (fdv * s_Dlz + s_fd0 * Dlz);
         } else {

@@ -76,6 +76,8 @@ def load(build_if_missing=True):
     L.ollin_gpu_ell_history.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
     L.ollin_gpu_interp.argtypes = [vp, ctypes.c_int, ctypes.c_int, vp, ctypes.c_int, vp]
     L.ollin_gpu_coords.argtypes = [vp, ctypes.c_int, vp, vp]
+    L.ollin_gpu_upload_many.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
+    L.ollin_gpu_download_many.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp]
     L.ollin_gpu_maximal_slicing.argtypes = [vp, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_many.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
     L.ollin_gpu_coarse_step_fused.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]

@@ -148,10 +148,16 @@ MIXED_2LEV = dict(SOR_2LEV, ell_solver="mixed", ell_epsilon=1e-12)
 MIXED_BRILL = dict(SOR_BRILL, ell_solver="mixed", ell_epsilon=1e-12)
 FP64MG_2LEV = dict(MIXED_2LEV, ell_solver="fp64mg")
 FP64MG_BRILL = dict(MIXED_BRILL, ell_solver="fp64mg")
+# refinement boxes: a box on the axis above box 0's level 1, and a ring off
+# the axis and the equator (Dirichlet rows on all its edges, its ghost
+# columns and rows unknowns as SOR sweeps them)
+MIXED_BOXES = dict(SOR_BOXES, ell_solver="mixed", ell_epsilon=1e-12)
+MIXED_RING = dict(SOR_RING, ell_solver="mixed", ell_epsilon=1e-12)
 
 
-@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL],
-                         ids=["mixed_pulse_2lev", "mixed_brill_3lev", "fp64mg_pulse_2lev", "fp64mg_brill_3lev"])
+@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL, MIXED_BOXES, MIXED_RING],
+                         ids=["mixed_pulse_2lev", "mixed_brill_3lev", "fp64mg_pulse_2lev", "fp64mg_brill_3lev",
+                              "mixed_boxes", "mixed_ring"])
 def test_mixed_precision_solve_matches_fp64_sor(cfg):
     """ELL_solver = "mixed" (FP64 iterative refinement, FP32 multigrid
     corrections) and "fp64mg" (the same with FP64 multigrid corrections)

@@ -8,7 +8,8 @@ the library image.
 Checked through the C ABI against the existing entry point ollin_gpu_norms
 on the same field, on two calls in a row, within the parity tolerance of the
 other GPU tests; then on a caller's stream, at the largest accepted grid
-(8192 interior rows, against NumPy), and on a field holding a NaN.  This file
+(8192 interior rows, against NumPy), on a field holding a NaN, on an
+order-two grid (two ghost zones), and on a capturing stream (refused).  This file
 is collected last so that a stop-at-first-failure run has run every other
 test before it."""
 import ctypes
@@ -34,10 +35,10 @@ def _lib():
     return lib
 
 
-def _call(lib, dev, nr, nz, dr, dz, stream=None, ld=None):
+def _call(lib, dev, nr, nz, dr, dz, stream=None, ld=None, ghost=3):
     out = np.zeros(5)
-    rc = lib.ollin_gpu_norms_noalloc(ctypes.c_void_p(dev.data_ptr()), nr, nz, 3, nr + 3 if ld is None else ld,
-                                     dr, dz, 1, stream, out.ctypes.data)
+    rc = lib.ollin_gpu_norms_noalloc(ctypes.c_void_p(dev.data_ptr()), nr, nz, ghost,
+                                     nr + ghost if ld is None else ld, dr, dz, 1, stream, out.ctypes.data)
     return rc, out
 
 
@@ -106,3 +107,32 @@ def test_noalloc_norms_at_the_row_limit_and_nan():
     rc, out = _call(lib, dev, nr, nz, 0.1, 0.1)
     assert rc == 0, lib.ollin_gpu_noalloc_last_error()
     np.testing.assert_allclose(out, _numpy_stats(f, 0.1, 0.1), rtol=1e-12, atol=1e-14)
+
+
+def test_noalloc_norms_order_two_and_capture_refused():
+    """Two ghost zones (order two) against ollin_gpu_norms; a capturing
+    stream is refused before any work is queued (the call ends by
+    synchronising its stream)."""
+    torch = pytest.importorskip("torch")
+    from ollin.gpu import Evolution
+    lib = _lib()
+    e = Evolution(params(dict(C1, nl0=1, order="two")))
+    e.initial_data()
+    e.initialize()
+    e.step()
+    d = e.desc(1)
+    assert d.ghost == 2
+    host = e.download(1, "alpha")
+    dev = torch.from_numpy(np.ascontiguousarray(host.T)).cuda()
+    torch.cuda.synchronize()
+    rc, out = _call(lib, dev, d.nr, d.nz, d.dr, d.dz, ghost=2)
+    assert rc == 0, lib.ollin_gpu_noalloc_last_error()
+    np.testing.assert_allclose(out, e.norms(1, "alpha"), rtol=1e-10, atol=1e-14)
+    s = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        rc, _ = _call(lib, dev, d.nr, d.nz, d.dr, d.dz, stream=ctypes.c_void_p(s.cuda_stream), ghost=2)
+        spare = dev * 1.0  # keeps the captured graph non-empty
+    assert rc == EINVAL and b"capturing" in lib.ollin_gpu_noalloc_last_error()
+    del spare
+    e.close()
