@@ -411,8 +411,8 @@ int ollin_gpu_norms(ollin_handle* h, int level, int field, double out[5]);
  * Laplacian, falpha and advective derivatives of the lapse before the solve.
  * ELL_solver = "mixed" solves the same discrete system as "sor" with FP64
  * residuals and FP32 multigrid corrections, "fp64mg" with FP64 ones (no
- * counterpart in the reference); both need eqsym and work with refinement
- * boxes.  "wave" and "sor" work without equatorial symmetry too. */
+ * counterpart in the reference); every solver works with refinement boxes
+ * and without equatorial symmetry. */
 int ollin_gpu_maximal_slicing(ollin_handle* h, const double* va_max);
 
 /* Iterations of the elliptic solve run by ollin_gpu_initial_data for

@@ -610,8 +610,12 @@ __device__ __forceinline__ int mir(int k) { return k < 1 ? 1 - k : k; }
 // outermost ghost column is the Dirichlet row from the parent, as SOR sweeps
 // them (sor_elliptic.f90:648); likewise in z.  The upper rows nr, nz are
 // Robin rows on the coarse problem and Dirichlet rows otherwise.
+// Without equatorial symmetry the coarse problem's lowest row j = 1-ghost is a
+// Robin row (sor_elliptic.f90:724-756), an unknown too.
 __device__ __forceinline__ int mix_ilo(const LevelGeom& G) { return G.axis ? 1 : 2 - G.g; }
-__device__ __forceinline__ int mix_jlo(const LevelGeom& G) { return G.equator ? 1 : 2 - G.g; }
+__device__ __forceinline__ int mix_jlo(const LevelGeom& G, int robin) {
+    return G.equator ? 1 : (robin ? 1 - G.g : 2 - G.g);
+}
 // element (p, q) of a level array, mirrored across the axis / equator where
 // the grid owns them
 __device__ __forceinline__ size_t mix_at(const LevelGeom& G, int p, int q) {
@@ -674,7 +678,8 @@ __device__ __forceinline__ bool mix_row(const MixArgs& A, const UF& U, int i, in
                                         bool& interior) {
     const LevelGeom& G = A.G;
     const int nr = G.nr, nz = G.nz;
-    interior = i <= nr - 1 && j <= nz - 1;  // and i >= mix_ilo, j >= mix_jlo (the callers' range)
+    const bool low = A.robin && !G.equator && j == 1 - G.g;  // the lower Robin row
+    interior = i <= nr - 1 && j <= nz - 1 && !low;  // and i >= mix_ilo, j >= mix_jlo (the callers' range)
     RowSum<EXACT> acc;
     if (interior) {
         if (!A.pa) {
@@ -699,10 +704,23 @@ __device__ __forceinline__ bool mix_row(const MixArgs& A, const UF& U, int i, in
     }
     if (!A.robin) return false;
     // (1 + 1.5 (cr + cz)) u - uinf - cr/2 (4 u_1 - u_2) - cz/2 (4 u_1 - u_2)
-    // along each outward direction; a centred difference along the edge
+    // along each outward direction; a centred difference along the edge; on
+    // the lower z edge the outward direction is -z (cz < 0 there)
     const double cr = G.rcol[i] / G.dr, cz = G.zrow[j] / G.dz;
     const double hr = 0.5 * cr, hz = 0.5 * cz;
-    if (i == nr && j == nz) {
+    if (low && i == nr) {
+        acc.prod(1.0 + 1.5 * (cr - cz), U(i, j));
+        acc.prod(-4.0 * hr, U(i - 1, j));
+        acc.prod(hr, U(i - 2, j));
+        acc.prod(4.0 * hz, U(i, j + 1));
+        acc.prod(-hz, U(i, j + 2));
+    } else if (low) {
+        acc.prod(1.0 - 1.5 * cz, U(i, j));
+        acc.prod(4.0 * hz, U(i, j + 1));
+        acc.prod(-hz, U(i, j + 2));
+        acc.prod(hr, U(i + 1, j));
+        acc.prod(-hr, U(i - 1, j));
+    } else if (i == nr && j == nz) {
         acc.prod(1.0 + 1.5 * (cr + cz), U(i, j));
         acc.prod(-4.0 * hr, U(i - 1, j));
         acc.prod(hr, U(i - 2, j));
@@ -735,7 +753,7 @@ __global__ void __launch_bounds__(kMixThreads) mix_resid_kernel(const __grid_con
     const LevelGeom& G = A.G;
     const long ld = G.ld;
     const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = mix_jlo(G, A.robin) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     double sq = 0.0, sc = 0.0, sb = 0.0;
     (void)ld;
     if (i <= G.nr && j <= G.nz) {
@@ -779,7 +797,7 @@ __global__ void __launch_bounds__(kMixThreads) mix_apply_kernel(const __grid_con
     const LevelGeom& G = A.G;
     const long ld = G.ld;
     const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = mix_jlo(G, A.robin) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     auto Z = [&](int p, int qq) {
         // the correction is zero on a Dirichlet row (left zero by the solve)
@@ -795,10 +813,10 @@ __global__ void __launch_bounds__(kMixThreads) mix_apply_kernel(const __grid_con
 }
 
 // per-block sums of x * y[k] over the unknowns, k < n (partial[k*nblocks+b])
-__global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, const double* x, OrthoVecs Y, int n,
-                                                                double* partial) {
+__global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, int robin, const double* x, OrthoVecs Y,
+                                                                int n, double* partial) {
     const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = mix_jlo(G, robin) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const bool in = i <= G.nr && j <= G.nz;
     const size_t o = in ? (size_t)i + (size_t)j * G.ld : 0;
     const double xv = in ? x[o] : 0.0;
@@ -807,10 +825,10 @@ __global__ void __launch_bounds__(kMixThreads) mix_dots_kernel(LevelGeom G, cons
 }
 
 // z -= sum_k beta_k Z_k, q -= sum_k beta_k Q_k
-__global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, double* z, double* q, OrthoVecs Zs,
-                                                                OrthoVecs Qs, OrthoCoef beta, int n) {
+__global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, int robin, double* z, double* q,
+                                                                OrthoVecs Zs, OrthoVecs Qs, OrthoCoef beta, int n) {
     const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = mix_jlo(G, robin) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.nr || j > G.nz) return;
     const size_t o = (size_t)i + (size_t)j * G.ld;
     double zv = z[o], qv = q[o];
@@ -826,7 +844,7 @@ __global__ void __launch_bounds__(kMixThreads) mix_orth_kernel(LevelGeom G, doub
 __global__ void __launch_bounds__(kMixThreads) mix_step_kernel(LevelGeom G, int robin, double* u, const double* z,
                                                                 double alpha) {
     const int i = mix_ilo(G) + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = mix_jlo(G) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = mix_jlo(G, robin) + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     const int lim_r = robin ? G.nr : G.nr - 1, lim_z = robin ? G.nz : G.nz - 1;
     if (i > lim_r || j > lim_z) return;
     const size_t o = (size_t)i + (size_t)j * G.ld;
@@ -836,45 +854,48 @@ __global__ void __launch_bounds__(kMixThreads) mix_step_kernel(LevelGeom G, int 
 }  // namespace
 
 // the mixed kernels' blocks over a level's unknowns
-static dim3 mix_grid(const LevelGeom& G) {
-    const int ni = G.nr - (G.axis ? 1 : 2 - G.g) + 1, nj = G.nz - (G.equator ? 1 : 2 - G.g) + 1;
+static dim3 mix_grid(const LevelGeom& G, int robin) {
+    const int ni = G.nr - (G.axis ? 1 : 2 - G.g) + 1;
+    const int nj = G.nz - (G.equator ? 1 : (robin ? 1 - G.g : 2 - G.g)) + 1;
     return dim3((ni + kMixBX - 1) / kMixBX, (nj + kMixBY - 1) / kMixBY);
 }
 
-int mix_blocks(const LevelGeom& G) {
-    const int ni = G.nr - (G.axis ? 1 : 2 - G.g) + 1, nj = G.nz - (G.equator ? 1 : 2 - G.g) + 1;
-    const int nx = (ni + kMixBX - 1) / kMixBX, ny = (nj + kMixBY - 1) / kMixBY;
+int mix_blocks(const LevelGeom& G, int robin) {
+    const dim3 b = mix_grid(G, robin);
+    const int nx = (int)b.x, ny = (int)b.y;
     return nx * ny;
 }
 
 void launch_mix_resid(const MixArgs& a, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd = mix_grid(a.G);
+    dim3 grd = mix_grid(a.G, a.robin);
     mix_resid_kernel<<<grd, blk, 0, s>>>(a);
 }
 
 void launch_mix_apply(const MixArgs& a, double* z64, double* q, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd = mix_grid(a.G);
+    dim3 grd = mix_grid(a.G, a.robin);
     mix_apply_kernel<<<grd, blk, 0, s>>>(a, z64, q);
 }
 
-void launch_mix_dots(const LevelGeom& G, const double* x, const OrthoVecs& y, int n, double* partial, cudaStream_t s) {
+void launch_mix_dots(const LevelGeom& G, int robin, const double* x, const OrthoVecs& y, int n, double* partial,
+                     cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd = mix_grid(G);
-    mix_dots_kernel<<<grd, blk, 0, s>>>(G, x, y, n, partial);
+    dim3 grd = mix_grid(G, robin);
+    mix_dots_kernel<<<grd, blk, 0, s>>>(G, robin, x, y, n, partial);
 }
 
-void launch_mix_orth(const LevelGeom& G, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
+void launch_mix_orth(const LevelGeom& G, int robin, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
                      const OrthoCoef& beta, int n, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd = mix_grid(G);
-    mix_orth_kernel<<<grd, blk, 0, s>>>(G, z, q, Zs, Qs, beta, n);
+    dim3 grd = mix_grid(G, robin);
+    mix_orth_kernel<<<grd, blk, 0, s>>>(G, robin, z, q, Zs, Qs, beta, n);
 }
+
 
 void launch_mix_step(const LevelGeom& G, int robin, double* u, const double* z, double alpha, cudaStream_t s) {
     dim3 blk(kMixBX, kMixBY);
-    dim3 grd = mix_grid(G);
+    dim3 grd = mix_grid(G, robin);
     mix_step_kernel<<<grd, blk, 0, s>>>(G, robin, u, z, alpha);
 }
 

@@ -172,10 +172,6 @@ int check_params(const ollin_params& P) {
     if (P.order != 4 && P.order != 2) return fail(OLLIN_EINVAL, "order must be \"two\" (2) or \"four\" (4)");
     if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
     if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
-    if (!P.eqsym && (P.idata == OLLIN_IDATA_SCALARPULSE || P.idata == OLLIN_IDATA_BRILLWAVE) &&
-        P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
-        return fail(OLLIN_EINVAL,
-                    "elliptic initial data without equatorial symmetry needs ELL_solver = wave or sor on the device");
     // main.f90:286-318 takes a larger par-file ghost as given; here the
     // number is the order's own
     if (P.ghost != 0 && P.ghost != (P.order == 2 ? 2 : 3))
@@ -1652,7 +1648,7 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     int rc = after_launch(h);
     if (rc) return rc;
     const bool s5 = !S.physical && P.idata == OLLIN_IDATA_SCALARPULSE && P.scalarpotential != OLLIN_POTENTIAL_NONE;
-    const int nparts = mix_blocks(L.G);
+    const int nparts = mix_blocks(L.G, robin ? 1 : 0);
     if (S.nparts < 3 * nparts) {
         cudaFree(S.partial);
         S.partial = nullptr;
@@ -1711,7 +1707,11 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     ms.dr = L.dr; ms.dz = L.dz;
     ms.ioff = ilo - 1; ms.joff = jlo - 1;
     ms.r0 = L.G.axis ? 0.0 : L.rh[ilo - 1 + g] - 0.5 * L.dr;
+    ms.z0 = L.G.equator ? 0.0 : L.zh[jlo - 1 + g] - 0.5 * L.dz;
     ms.mr = L.G.axis; ms.mz = L.G.equator;
+    // without equatorial symmetry the coarse problem's lowest row j = 1-ghost
+    // is a Robin row: the multigrid holds it as its row 0
+    ms.rz = robin && !L.G.equator ? 1 : 0;
     // Orthomin storage: a ring of kOrthoSlots directions z and their images
     // q = A z, the FP64 residual for the FP32 solve, per-block dot products
     constexpr int kOrthoSlots = 7;  // the new direction + up to 6 kept
@@ -1740,7 +1740,7 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
     std::vector<double> hd((size_t)(kOrthoMax + 2) * nparts);
     // sums over the blocks of the first n dot products, in block order
     auto dots = [&](const double* x, const OrthoVecs& y, int n, double* out) -> int {
-        launch_mix_dots(L.G, x, y, n, dpart, h->stream);
+        launch_mix_dots(L.G, a.robin, x, y, n, dpart, h->stream);
         int rc2 = after_launch(h);
         if (rc2) return rc2;
         CUDA_OR_FAIL(cudaMemcpyAsync(hd.data(), dpart, (size_t)n * nparts * sizeof(double), cudaMemcpyDeviceToHost,
@@ -1778,7 +1778,8 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
         // the Robin rows (level 0): a smooth offset of the whole solution moves
         // them by its size while the interior rows hardly see it, so they are
         // held to the tolerance on their own
-        const double nrob = robin ? (double)(L.nr + L.nz - 1) : 0.0;
+        const double nrob = !robin ? 0.0 : L.G.equator ? (double)(L.nr + L.nz - 1)
+                                                        : (double)(L.nz + g + 2 * (L.nr - 1));
         const double rms_b = robin ? std::sqrt(sumb / nrob) : 0.0;
         rms = std::max(rms_in, rms_b);
         // the FP64 floor of a row: the residual of the solution rounded to
@@ -1846,7 +1847,7 @@ int mix_level(ollin_handle* h, WaveSolve& S, int level, bool robin, int* outer_o
                 const int sl = (head - 1 - k + kOrthoSlots) % kOrthoSlots;
                 beta.c[k] = qq[sl] > 0.0 ? dq[k] / qq[sl] : 0.0;
             }
-            launch_mix_orth(L.G, Zs[head], Qs[head], zy, qy, beta, nprev, h->stream);
+            launch_mix_orth(L.G, a.robin, Zs[head], Qs[head], zy, qy, beta, nprev, h->stream);
             rc = after_launch(h);
             if (rc) return rc;
         }
@@ -2146,8 +2147,6 @@ int initial_data(ollin_handle* h) {
 int maximal_slicing(ollin_handle* h, const double* va_max) {
     const ollin_params& P = h->P;
     if (!h->initialized) return fail(OLLIN_ESTATE, "ollin_gpu_initialize must run before a maximal-slicing solve");
-    if (!P.eqsym && P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR)
-        return fail(OLLIN_EINVAL, "maximal slicing without equatorial symmetry needs ELL_solver = wave or sor on the device");
     if (P.ell_solver != OLLIN_ELL_WAVE && P.ell_solver != OLLIN_ELL_SOR && P.ell_solver != OLLIN_ELL_MIXED &&
         P.ell_solver != OLLIN_ELL_FP64MG)
         return fail(OLLIN_EINVAL, "maximal slicing needs ELL_solver = wave, sor, mixed or fp64mg");

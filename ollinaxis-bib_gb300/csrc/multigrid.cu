@@ -16,8 +16,9 @@
 // z_J = (J-1/2) Hz, Hr = 2^k dr; at the lower edges d(0,J) = d(1,J),
 // d(I,0) = d(I,1) (axis and equator mirrors) or, on a refinement box off the
 // axis or the equator, d = 0 there (the Dirichlet row of its problem); Robin
-// rows I = n / J = m on the coarse problem, zero rows on the Dirichlet
-// problems of the finer refinement levels and boxes.  The nine-
+// rows I = n / J = m on the coarse problem (and J = 0 on a coarse problem
+// without equatorial symmetry, whose lowest level row is a Robin row), zero
+// rows on the Dirichlet problems of the finer refinement levels and boxes.  The nine-
 // point couplings of a metric with g^rz /= 0 are left to the FP64 residual of
 // the outer iteration.
 // Cell (I,J) of grid k+1 covers cells 2I-1..2I x 2J-1..2J of grid k: the
@@ -38,7 +39,8 @@ template <typename T>
 struct Grid {
     int n, m, ld;
     int mr, mz;                          // lower edges mirrored (1) or Dirichlet zero rows (0)
-    T r0;                                // r of the lower face of cell 1
+    int rz;                              // row J = 0 is a Robin row (no equatorial symmetry)
+    T r0, z0;                            // r, z of the lower faces of cell (1, 1)
     T hr, hz;                            // spacings
     T* d; T* r;                          // correction, right-hand side
     T* krr; T* kzz; T* vr; T* vz; T* s;  // coefficient fields
@@ -46,7 +48,8 @@ struct Grid {
 
 __device__ __forceinline__ int mirror(int k) { return k < 1 ? 1 - k : k; }
 
-// a Dirichlet lower edge keeps index 0 at zero, so it reads as it is
+// a Dirichlet lower edge keeps index 0 at zero and a lower Robin row holds
+// its unknowns there, so both read as they are
 template <typename T>
 __device__ __forceinline__ T Dv(const Grid<T>& G, int i, int j) {
     return G.d[(G.mr ? mirror(i) : i) + (G.mz ? mirror(j) : j) * G.ld];
@@ -80,21 +83,32 @@ __device__ __forceinline__ T interior_res(const Grid<T>& G, int i, int j) {
                      + q.c * G.d[o]);
 }
 
-// residual of a Robin row (coarse problem); cr = r_n/Hr = n - 1/2, cz = J - 1/2
+// residual of a Robin row (coarse problem); cr = r_n/Hr = n - 1/2, cz = J - 1/2.
+// The lower Robin row J = 0 faces -z (cz < 0 there):
+//   (1 - 1.5 cz) d + cz/2 (4 d(I,1) - d(I,2)) + cr_I/2 (d(I+1,0) - d(I-1,0)) = r
 template <typename T>
 __device__ __forceinline__ T robin_res(const Grid<T>& G, int i, int j) {
     const int n = G.n, m = G.m;
-    const T cr = (T)n - T(0.5), czn = (T)m - T(0.5);
+    // r/Hr and z/Hz at the cell centres of the Robin rows
+    const T cr = G.r0 / G.hr + (T)n - T(0.5), czn = G.z0 / G.hz + (T)m - T(0.5);
+    const T cz0 = G.z0 / G.hz - T(0.5);
     T lhs;
-    if (i == n && j == m) {
+    if (j == 0 && i == n) {
+        lhs = (T(1.0) + T(1.5) * (cr - cz0)) * Dv(G, i, 0) - T(0.5) * cr * (T(4.0) * Dv(G, i - 1, 0) - Dv(G, i - 2, 0))
+              + T(0.5) * cz0 * (T(4.0) * Dv(G, i, 1) - Dv(G, i, 2));
+    } else if (j == 0) {
+        const T crr = G.r0 / G.hr + (T)i - T(0.5);
+        lhs = (T(1.0) - T(1.5) * cz0) * Dv(G, i, 0) + T(0.5) * cz0 * (T(4.0) * Dv(G, i, 1) - Dv(G, i, 2))
+              + T(0.5) * crr * (Dv(G, i + 1, 0) - Dv(G, i - 1, 0));
+    } else if (i == n && j == m) {
         lhs = (T(1.0) + T(1.5) * (cr + czn)) * Dv(G, i, j) - T(0.5) * cr * (T(4.0) * Dv(G, i - 1, j) - Dv(G, i - 2, j))
               - T(0.5) * czn * (T(4.0) * Dv(G, i, j - 1) - Dv(G, i, j - 2));
     } else if (i == n) {
-        const T cz = (T)j - T(0.5);
+        const T cz = G.z0 / G.hz + (T)j - T(0.5);
         lhs = (T(1.0) + T(1.5) * cr) * Dv(G, i, j) - T(0.5) * cr * (T(4.0) * Dv(G, i - 1, j) - Dv(G, i - 2, j))
               + T(0.5) * cz * (Dv(G, i, j + 1) - Dv(G, i, j - 1));
     } else {
-        const T crr = (T)i - T(0.5);
+        const T crr = G.r0 / G.hr + (T)i - T(0.5);
         lhs = (T(1.0) + T(1.5) * czn) * Dv(G, i, j) - T(0.5) * czn * (T(4.0) * Dv(G, i, j - 1) - Dv(G, i, j - 2))
               + T(0.5) * crr * (Dv(G, i + 1, j) - Dv(G, i - 1, j));
     }
@@ -111,7 +125,7 @@ __device__ __forceinline__ void relax(const Grid<T>& G, int i, int j) {
     T diag = q.c;
     T off = q.e * G.d[o + 1] + q.n * G.d[o + G.ld];
     if (i > 1) off += q.w * G.d[o - 1]; else if (G.mr) diag += q.w;
-    if (j > 1) off += q.s * G.d[o - G.ld]; else if (G.mz) diag += q.s;
+    if (j > 1 || G.rz) off += q.s * G.d[o - G.ld]; else if (G.mz) diag += q.s;
     G.d[o] = (G.r[o] - off) / diag;
 }
 
@@ -131,24 +145,32 @@ __global__ void __launch_bounds__(128) mg_smooth_kernel(Grid<T> G, int parity) {
 template <typename T>
 __device__ void robin_sweep(const Grid<T>& G) {
     const int n = G.n, m = G.m;
-    const T cr = (T)n - T(0.5), czn = (T)m - T(0.5);
-    auto D = [&](int i, int j) -> T& { return G.d[mirror(i) + mirror(j) * G.ld]; };
+    const T cr = G.r0 / G.hr + (T)n - T(0.5), czn = G.z0 / G.hz + (T)m - T(0.5);
+    const T cz0 = G.z0 / G.hz - T(0.5);
+    auto D = [&](int i, int j) -> T& { return G.d[(G.mr ? mirror(i) : i) + (G.mz ? mirror(j) : j) * G.ld]; };
     for (int colour = 0; colour < 2; ++colour) {
         for (int j = 1 + colour + 2 * (int)threadIdx.x; j <= m - 1; j += 2 * blockDim.x) {
-            const T cz = (T)j - T(0.5);
+            const T cz = G.z0 / G.hz + (T)j - T(0.5);
             D(n, j) = (G.r[n + j * G.ld] + T(0.5) * cr * (T(4.0) * D(n - 1, j) - D(n - 2, j)) - T(0.5) * cz * (D(n, j + 1) - D(n, j - 1)))
                       / (T(1.0) + T(1.5) * cr);
         }
         for (int i = 1 + colour + 2 * (int)threadIdx.x; i <= n - 1; i += 2 * blockDim.x) {
-            const T crr = (T)i - T(0.5);
+            const T crr = G.r0 / G.hr + (T)i - T(0.5);
             D(i, m) = (G.r[i + m * G.ld] + T(0.5) * czn * (T(4.0) * D(i, m - 1) - D(i, m - 2)) - T(0.5) * crr * (D(i + 1, m) - D(i - 1, m)))
                       / (T(1.0) + T(1.5) * czn);
+            if (G.rz)
+                D(i, 0) = (G.r[i] - T(0.5) * cz0 * (T(4.0) * D(i, 1) - D(i, 2)) - T(0.5) * crr * (D(i + 1, 0) - D(i - 1, 0)))
+                          / (T(1.0) - T(1.5) * cz0);
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         D(n, m) = (G.r[n + m * G.ld] + T(0.5) * cr * (T(4.0) * D(n - 1, m) - D(n - 2, m)) + T(0.5) * czn * (T(4.0) * D(n, m - 1) - D(n, m - 2)))
                   / (T(1.0) + T(1.5) * (cr + czn));
+        if (G.rz)
+            D(n, 0) = (G.r[n] + T(0.5) * cr * (T(4.0) * D(n - 1, 0) - D(n - 2, 0)) - T(0.5) * cz0 * (T(4.0) * D(n, 1) - D(n, 2)))
+                      / (T(1.0) + T(1.5) * (cr - cz0));
+    }
     __syncthreads();
 }
 
@@ -174,16 +196,19 @@ __global__ void __launch_bounds__(1024) mg_coarse_kernel(Grid<T> G, int robin, i
 }
 
 // residual of grid F restricted to the right-hand side of grid C; d_C = 0
+// (a lower Robin row J = 0 from the fine grid's row 0)
 template <typename T>
 __global__ void __launch_bounds__(128) mg_restrict_kernel(Grid<T> F, Grid<T> C, int robin) {
     const int I = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int J = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int J = 1 - C.rz + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (I > C.n || J > C.m) return;
     const int o = I + J * C.ld;
     C.d[o] = T(0.0);
     const bool bI = I == C.n, bJ = J == C.m;
     T v = T(0.0);
-    if (!bI && !bJ) {
+    if (J == 0) {
+        v = bI ? robin_res(F, F.n, 0) : T(0.5) * (robin_res(F, 2 * I - 1, 0) + robin_res(F, 2 * I, 0));
+    } else if (!bI && !bJ) {
         v = T(0.25) * (interior_res(F, 2 * I - 1, 2 * J - 1) + interior_res(F, 2 * I, 2 * J - 1)
                        + interior_res(F, 2 * I - 1, 2 * J) + interior_res(F, 2 * I, 2 * J));
     } else if (robin) {
@@ -194,19 +219,21 @@ __global__ void __launch_bounds__(128) mg_restrict_kernel(Grid<T> F, Grid<T> C, 
     C.r[o] = v;
 }
 
-// d_F += bilinear interpolation of d_C (zero rows of a Dirichlet problem stay)
+// d_F += bilinear interpolation of d_C (zero rows of a Dirichlet problem
+// stay; a lower Robin row, centred half a fine cell below cell 1, takes 3/4
+// of the coarse row 0 and 1/4 of the coarse row 1)
 template <typename T>
 __global__ void __launch_bounds__(128) mg_prolong_kernel(Grid<T> F, Grid<T> C, int robin) {
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = 1 - F.rz + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > F.n || j > F.m) return;
     if (!robin && (i == F.n || j == F.m)) return;
     const int I = (i + 1) / 2, J = (j + 1) / 2;
     const int I2 = (i & 1) ? I - 1 : I + 1, J2 = (j & 1) ? J - 1 : J + 1;
     auto c = [&](int p, int q) {
-        if ((p < 1 && !C.mr) || (q < 1 && !C.mz)) return T(0.0);  // a Dirichlet lower row
+        if ((p < 1 && !C.mr) || (q < 1 && !C.mz && !C.rz)) return T(0.0);  // a Dirichlet lower row
         p = p < 1 ? 1 : (p > C.n ? C.n : p);
-        q = q < 1 ? 1 : (q > C.m ? C.m : q);
+        q = q < 1 ? (C.rz ? 0 : 1) : (q > C.m ? C.m : q);
         return C.d[p + q * C.ld];
     };
     const T v = T(0.5625) * c(I, J) + T(0.1875) * (c(I2, J) + c(I, J2)) + T(0.0625) * c(I2, J2);
@@ -264,20 +291,21 @@ __global__ void __launch_bounds__(128) mg_rhs_kernel(Grid<T> G, const T* r, long
     if (i > G.n + 1 || j > G.m + 1) return;
     const int o = i + j * G.ld;
     G.d[o] = T(0.0);
-    const bool in = i >= 1 && i <= G.n && j >= 1 && j <= G.m;
+    const bool in = i >= 1 && i <= G.n && j >= 1 - G.rz && j <= G.m;
     G.r[o] = in ? r[(long)(i + ioff) + (long)(j + joff) * ld] : T(0.0);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(128) mg_store_kernel(Grid<T> G, T* d, long ld, int ioff, int joff) {
     const int i = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int j = 1 + (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int j = 1 - G.rz + (int)(blockIdx.y * blockDim.y + threadIdx.y);
     if (i > G.n || j > G.m) return;
     d[(long)(i + ioff) + (long)(j + joff) * ld] = G.d[i + j * G.ld];
 }
 
+// the cells 1..n x 1..m, from row 0 when it is a Robin row
 template <typename T>
-dim3 cells(const Grid<T>& G, dim3 blk) { return dim3((G.n + blk.x - 1) / blk.x, (G.m + blk.y - 1) / blk.y); }
+dim3 cells(const Grid<T>& G, dim3 blk) { return dim3((G.n + blk.x - 1) / blk.x, (G.m + G.rz + blk.y - 1) / blk.y); }
 
 // ---- host side of the hierarchy ---------------------------------------------
 template <typename T>
@@ -317,7 +345,9 @@ struct MgGrids {
         for (Grid<T>& G : g) {
             G.mr = S.mr;
             G.mz = S.mz;
+            G.rz = S.rz;
             G.r0 = (T)S.r0;
+            G.z0 = (T)S.z0;
         }
         const Grid<T>& G0 = g[0];
         mg_load_kernel<T><<<dim3((G0.n + 2 + 31) / 32, (G0.m + 2 + 3) / 4), blk, 0, s>>>(G0, S);

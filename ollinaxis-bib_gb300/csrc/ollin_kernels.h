@@ -324,7 +324,7 @@ struct MixArgs {
 };
 
 void launch_mix_resid(const MixArgs& a, cudaStream_t s);
-int mix_blocks(const LevelGeom& G);
+int mix_blocks(const LevelGeom& G, int robin);
 
 // Orthomin acceleration of the multigrid corrections: up to kOrthoMax stored
 // directions (level-layout FP64 vectors) and their coefficients, by value
@@ -332,8 +332,9 @@ constexpr int kOrthoMax = 8;
 struct OrthoVecs { const double* v[kOrthoMax + 2]; };
 struct OrthoCoef { double c[kOrthoMax]; };
 void launch_mix_apply(const MixArgs& a, double* z64, double* q, cudaStream_t s);
-void launch_mix_dots(const LevelGeom& G, const double* x, const OrthoVecs& y, int n, double* partial, cudaStream_t s);
-void launch_mix_orth(const LevelGeom& G, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
+void launch_mix_dots(const LevelGeom& G, int robin, const double* x, const OrthoVecs& y, int n, double* partial,
+                     cudaStream_t s);
+void launch_mix_orth(const LevelGeom& G, int robin, double* z, double* q, const OrthoVecs& Zs, const OrthoVecs& Qs,
                      const OrthoCoef& beta, int n, cudaStream_t s);
 void launch_mix_step(const LevelGeom& G, int robin, double* u, const double* z, double alpha, cudaStream_t s);
 
@@ -347,12 +348,13 @@ struct MgStencil {
     const double* e;
     long ld;
     double dr, dz;
-    // the level point of multigrid cell (0, 0), r of the lower face of cell
-    // 1, and whether the lower edges are the axis / equator mirrors (else
-    // Dirichlet rows of a refinement box off them)
+    // the level point of multigrid cell (0, 0), r and z of the lower faces of
+    // cell (1, 1), and whether the lower edges are the axis / equator mirrors
+    // (else Dirichlet rows of a refinement box off them); rz: row 0 is the
+    // lower Robin row of a coarse problem without equatorial symmetry
     int ioff, joff;
-    double r0;
-    int mr, mz;
+    double r0, z0;
+    int mr, mz, rz;
 };
 // Geometric multigrid for the correction equation (multigrid.cu), FP32 or
 // FP64 (fp64 = 1); r and d are arrays of that precision

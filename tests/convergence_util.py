@@ -11,9 +11,9 @@ RESOLUTIONS = ((20, 0.4), (40, 0.2), (80, 0.1))
 T_END = 0.8
 
 
-def config(n, h, matter):
+def config(n, h, matter, order="four"):
     cfg = dict(nrtotal=n, nztotal=n, nl0=0, dr0=h, dz0=h, eqsym=1, idata="minkowski", ilapse="one",
-               slicing="1+log", gauge_f=2.0, shift="none", integrator="rk4", order="four", geodiss=0.02,
+               slicing="1+log", gauge_f=2.0, shift="none", integrator="rk4", order=order, geodiss=0.02,
                dtfac=0.25, boundtype="radiative")
     if matter:
         cfg.update(mattertype="scalar", scalardiss=0.02)

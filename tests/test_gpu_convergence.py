@@ -15,11 +15,11 @@ pytestmark = pytest.mark.gpu
 FIELDS = ["alpha", "trK", "phi", "A"]
 
 
-def gpu_origin_values(matter, fields):
+def gpu_origin_values(matter, fields, order="four"):
     from ollin.gpu import Evolution
     out = []
     for n, h in RESOLUTIONS:
-        e = Evolution(params(config(n, h, matter)))
+        e = Evolution(params(config(n, h, matter, order)))
         e.initial_data()
         prepare(e, matter, lambda nm: _coord(e, nm), lambda nm, v: e.upload(0, nm, v))
         e.initialize()
@@ -48,3 +48,16 @@ def test_gpu_reproduces_reference_convergence(matter):
         assert abs(cg - co) <= 1e-4 * abs(co), "%s: gpu factor %.6f oracle %.6f" % (f, cg, co)
         if f in ("trK", "scalar_phi") or (f == "phi" and not matter):
             assert 13.0 < cg < 20.0, "%s: convergence factor %.2f" % (f, cg)
+
+
+def test_gpu_reproduces_order_two_convergence():
+    """order = two: the device's factors equal the oracle's (second order in
+    trK and KTA; the lapse and phi are pre-asymptotic at these resolutions)."""
+    fields = ["alpha", "trK", "phi", "KTA"]
+    og = gpu_origin_values(False, fields, order="two")
+    oo = oracle_origin_values(False, fields, order="two")
+    for k, f in enumerate(fields):
+        cg, co = factors([v[k] for v in og]), factors([v[k] for v in oo])
+        assert abs(cg - co) <= 1e-4 * abs(co), "%s: gpu factor %.6f oracle %.6f" % (f, cg, co)
+        if f in ("trK", "KTA"):
+            assert 3.5 < cg < 6.0, "%s: convergence factor %.2f" % (f, cg)

@@ -153,11 +153,16 @@ FP64MG_BRILL = dict(MIXED_BRILL, ell_solver="fp64mg")
 # columns and rows unknowns as SOR sweeps them)
 MIXED_BOXES = dict(SOR_BOXES, ell_solver="mixed", ell_epsilon=1e-12)
 MIXED_RING = dict(SOR_RING, ell_solver="mixed", ell_epsilon=1e-12)
+# without equatorial symmetry: the lower z edge of the coarse problem is a
+# Robin row (and its corner), the finer levels' lower edge a Dirichlet row
+MIXED_NOEQSYM = dict(SOR_NOEQSYM, ell_solver="mixed", ell_epsilon=1e-12)
+MIXED_BRILL_NOEQSYM = dict(SOR_BRILL_NOEQSYM, ell_solver="mixed", ell_epsilon=1e-12)
 
 
-@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL, MIXED_BOXES, MIXED_RING],
+@pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL, MIXED_BOXES, MIXED_RING,
+                                 MIXED_NOEQSYM, MIXED_BRILL_NOEQSYM],
                          ids=["mixed_pulse_2lev", "mixed_brill_3lev", "fp64mg_pulse_2lev", "fp64mg_brill_3lev",
-                              "mixed_boxes", "mixed_ring"])
+                              "mixed_boxes", "mixed_ring", "mixed_no_eqsym", "mixed_brill_no_eqsym"])
 def test_mixed_precision_solve_matches_fp64_sor(cfg):
     """ELL_solver = "mixed" (FP64 iterative refinement, FP32 multigrid
     corrections) and "fp64mg" (the same with FP64 multigrid corrections)

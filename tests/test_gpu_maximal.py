@@ -172,8 +172,9 @@ def test_maximal_slicing_sor_with_refinement_boxes():
 
 
 @pytest.mark.parametrize("cfg", [EVERY, dict(SOR_SHIFT, slicing="1+log", maximalevery=1),
-                                 dict(EVERY, nl0=1, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0)],
-                         ids=["schwarzschild_two_levels", "shift_c_nonzero", "refinement_box"])
+                                 dict(EVERY, nl0=1, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=2.0),
+                                 dict(EVERY, eqsym=0)],
+                         ids=["schwarzschild_two_levels", "shift_c_nonzero", "refinement_box", "no_eqsym"])
 def test_maximal_lapse_mixed_precision_matches_fp64_sor(cfg):
     """ELL_solver = "mixed" for the physical Laplacian: FP64 residual of the
     nine-point SOR system, FP32 multigrid corrections of the flat operator
