@@ -792,14 +792,24 @@ def probe(args):
         B.build()
         objs = [os.path.join(B.BUILD, os.path.splitext(x)[0] + ".o") for x in B.SOURCES if x != "rhs.cu"]
         out = {}
-        for thr, mb in [(128, 3), (128, 2), (64, 4), (64, 5), (256, 1)]:
-            tag = "%d_%d" % (thr, mb)
-            obj = os.path.join(B.BUILD, "rhs_%s.o" % tag)
-            lib = os.path.join(B.BUILD, "libollin_gpu_rhs_%s.so" % tag)
+        shapes = [(128, 3), (64, 6), (64, 5), (96, 4), (128, 2), (32, 12)]
+
+        def make(shape):  # one library per launch shape, compiled side by side
+            thr, mb = shape
+            obj = os.path.join(B.BUILD, "rhs_%d_%d.o" % shape)
+            lib = os.path.join(B.BUILD, "libollin_gpu_rhs_%d_%d.so" % shape)
             subprocess.run([B.nvcc()] + B.ARCH + B.COMMON + ["-DOLLIN_RHS_THREADS=%d" % thr,
                             "-DOLLIN_RHS_MINBLOCKS=%d" % mb, "-c", os.path.join(B.CSRC, "rhs.cu"), "-o", obj],
                            check=True)
             subprocess.run([B.nvcc()] + B.ARCH + ["-shared", "-o", lib] + objs + [obj, "-lcudart"], check=True)
+            return lib
+
+        import concurrent.futures
+        with concurrent.futures.ThreadPoolExecutor(max_workers=len(shapes)) as ex:
+            libs = dict(zip(shapes, ex.map(make, shapes)))
+        for thr, mb in shapes:
+            tag = "%d_%d" % (thr, mb)
+            lib = libs[(thr, mb)]
             r = subprocess.run([sys.executable, os.path.abspath(__file__), "--steps", "6", "--warmup", "3",
                                 "--no-elliptic", "--no-batch", "--no-serve", "--no-cpu-baseline"],
                                env=dict(os.environ, OLLIN_GPU_LIB=lib), capture_output=True, text=True)
