@@ -413,8 +413,9 @@ __global__ void __launch_bounds__(kMaxThreads) max_coeff_kernel(const __grid_con
         bool xin = false;
         if (A.smap) {
             const int m = A.smap[om];
-            for (int k = 0; k < 5; ++k) src[k] = m >= 0 ? A.xb[k] : A.xa[k];
-            if (m >= 0) { os = (size_t)m; lds = A.xb_ld; xin = true; }
+            const int pk = m >= 0 ? m >> kPartnerShift : 0;
+            for (int k = 0; k < 5; ++k) src[k] = m >= 0 ? A.xb[pk][k] : A.xa[k];
+            if (m >= 0) { os = (size_t)(m & kPartnerOffset); lds = A.xb_ld[pk]; xin = true; }
         }
         const int pcr = xin ? 0 : pclass_o(ord, mi, nr, g), pcz = xin ? 0 : pclass_o(ord, mj, nz, g);
         const double cr1 = c1_o(ord, G.idr), cz1 = c1_o(ord, G.idz);

@@ -95,7 +95,8 @@ struct DLevel {
     // ``auxiliary``
     double* snap = nullptr;
     int* smap = nullptr;
-    int spartner = -1;
+    std::vector<int> spartners;  // the grids copied from (index k of a copied point's smap entry)
+    std::vector<int> hsmap;      // host copy of smap
     bool sync_pending = false;
 };
 
@@ -105,6 +106,7 @@ struct SyncPair {
     int p = -1, q = -1;
     XferPt* tab = nullptr;
     int ntab = 0;
+    std::vector<size_t> written;  // level offsets of grid p that this copy writes
 };
 
 }  // namespace
@@ -455,13 +457,13 @@ StageArgs stage_args(ollin_handle* h, DLevel& L, int in_slot, int out_slot, bool
     a.nanflag = h->d_flag;
     a.alpha_aux = L.alpha_stale ? base_ptr(L, L.alpha_aux) : nullptr;
     if (L.sync_pending) {
-        const DLevel& Q = h->L[L.spartner];
         a.smap = L.smap + (L.g - 1) + (size_t)(L.g - 1) * L.ld;
-        for (int f = 0; f < NFIELDS; ++f) {
-            a.xa[f] = base_ptr(L, L.snap + (size_t)f * L.n);
-            a.xb[f] = base_ptr(Q, Q.snap + (size_t)f * Q.n);
+        for (int f = 0; f < NFIELDS; ++f) a.xa[f] = base_ptr(L, L.snap + (size_t)f * L.n);
+        for (size_t k = 0; k < L.spartners.size(); ++k) {
+            const DLevel& Q = h->L[L.spartners[k]];
+            for (int f = 0; f < NFIELDS; ++f) a.xb[k][f] = base_ptr(Q, Q.snap + (size_t)f * Q.n);
+            a.xb_ld[k] = Q.ld;
         }
-        a.xb_ld = Q.ld;
     }
     return a;
 }
@@ -793,22 +795,35 @@ int build_sync_tables(ollin_handle* h) {
                     }
                 }
                 if (used == 0) { cudaFree(tab); continue; }
-                if (P.spartner >= 0 && P.spartner != q) {
-                    cudaFree(tab);
-                    return fail(OLLIN_EINVAL, "a grid that overlaps two other boxes on one level is not supported");
+                // partner k of this grid; a point copied by two partners keeps
+                // the later copy, as the copies of the level run in this order
+                int k = (int)(std::find(P.spartners.begin(), P.spartners.end(), q) - P.spartners.begin());
+                if (k == (int)P.spartners.size()) {
+                    if (k == kMaxPartners) {
+                        cudaFree(tab);
+                        return fail(OLLIN_EINVAL, "syncboxes: a grid overlaps more than three other grids on one level");
+                    }
+                    P.spartners.push_back(q);
                 }
-                P.spartner = q;
-                std::vector<int> map(P.n, -1);
-                for (const XferPt& x : host)
-                    if (x.o_out != kNoPoint) map[(size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld] = x.depth;
+                if (P.hsmap.empty()) P.hsmap.assign(P.n, -1);
+                for (const XferPt& x : host) {
+                    if (x.o_out == kNoPoint) continue;
+                    if (x.depth > kPartnerOffset) {
+                        cudaFree(tab);
+                        return fail(OLLIN_EINVAL, "syncboxes: a partner grid too large for the copy map");
+                    }
+                    P.hsmap[(size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld] = x.depth | (k << kPartnerShift);
+                }
                 if (!P.smap && cudaMalloc(&P.smap, P.n * sizeof(int)) != cudaSuccess) {
                     cudaFree(tab);
                     return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes map");
                 }
-                CUDA_OR_FAIL(cudaMemcpy(P.smap, map.data(), P.n * sizeof(int), cudaMemcpyHostToDevice));
+                CUDA_OR_FAIL(cudaMemcpy(P.smap, P.hsmap.data(), P.n * sizeof(int), cudaMemcpyHostToDevice));
                 SyncPair sp;
                 sp.p = p; sp.q = q; sp.tab = tab; sp.ntab = n;
-                h->sync.push_back(sp);
+                for (const XferPt& x : host)
+                    if (x.o_out != kNoPoint) sp.written.push_back((size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld);
+                h->sync.push_back(std::move(sp));
             }
         }
     // a later copy of the level may not read a point an earlier one wrote
@@ -818,17 +833,17 @@ int build_sync_tables(ollin_handle* h) {
             const SyncPair& r = h->sync[e];
             if (r.q != w.p) continue;
             std::vector<XferPt> hr(r.ntab);
-            std::vector<int> map(h->L[w.p].n);
             CUDA_OR_FAIL(cudaMemcpy(hr.data(), r.tab, (size_t)r.ntab * sizeof(XferPt), cudaMemcpyDeviceToHost));
-            CUDA_OR_FAIL(cudaMemcpy(map.data(), h->L[w.p].smap, map.size() * sizeof(int), cudaMemcpyDeviceToHost));
             const DLevel& W = h->L[w.p];
+            std::vector<char> map(W.n, 0);
+            for (size_t o : w.written) map[o] = 1;
             const size_t shift = (size_t)(W.g - 1) + (size_t)(W.g - 1) * W.ld;
             // the copy reads the node it coincides with (the other weights
             // of a near-node stencil are rounding)
             for (const XferPt& x : hr) {
                 if (x.o_out == kNoPoint) continue;
                 const size_t o = (size_t)x.depth + shift;
-                if (o < W.n && map[o] >= 0)
+                if (o < W.n && map[o])
                     return fail(OLLIN_EINVAL, "syncboxes: a copy reads a point another copy of the level wrote");
             }
         }
@@ -2180,14 +2195,14 @@ int maximal_slicing(ollin_handle* h, const double* va_max) {
         a.rhos = h->scalar ? base_ptr(L, L.aux[X_RHOS]) : nullptr;
         a.t0 = L.last_aux_t0 ? 1 : 0;
         if (L.sync_pending) {
-            const DLevel& Q = h->L[L.spartner];
             a.smap = L.smap + (L.g - 1) + (size_t)(L.g - 1) * L.ld;
             const int slots[5] = {NFIELDS, NFIELDS + 1, NFIELDS + 2, F_CHI, F_PHI};
-            for (int k = 0; k < 5; ++k) {
-                a.xa[k] = base_ptr(L, L.snap + (size_t)slots[k] * L.n);
-                a.xb[k] = base_ptr(Q, Q.snap + (size_t)slots[k] * Q.n);
+            for (int k = 0; k < 5; ++k) a.xa[k] = base_ptr(L, L.snap + (size_t)slots[k] * L.n);
+            for (size_t p = 0; p < L.spartners.size(); ++p) {
+                const DLevel& Q = h->L[L.spartners[p]];
+                for (int k = 0; k < 5; ++k) a.xb[p][k] = base_ptr(Q, Q.snap + (size_t)slots[k] * Q.n);
+                a.xb_ld[p] = Q.ld;
             }
-            a.xb_ld = Q.ld;
         }
         a.S1 = base_ptr(L, w.S1);
         a.P1 = base_ptr(L, q[0]); a.P2 = base_ptr(L, q[1]);

@@ -27,6 +27,12 @@ struct PhysParams {
 };
 
 // One RK/ICN stage of one level.
+// ``syncboxes`` partners of one grid on a level (boxes 0..3 share a level),
+// and the packing of a copied point's partner and offset into one int
+constexpr int kMaxPartners = 3;
+constexpr int kPartnerShift = 28;
+constexpr int kPartnerOffset = (1 << kPartnerShift) - 1;
+
 struct StageArgs {
     LevelGeom G;
     PhysParams P;
@@ -54,14 +60,16 @@ struct StageArgs {
     // derivatives of the lapse come from it, the lapse itself and the
     // gradient that maximalslicing.f90:156-170 recomputes from the new one.
     const double* alpha_aux;
-    // The first stage after ``syncboxes`` copied another box's data onto this
-    // grid (launch_rhs_sync, _stale_sync): smap[o] >= 0 marks a copied point and its
-    // offset in the partner's state xb (leading dimension xb_ld); the other
-    // points read this grid's state before the copy, xa.
+    // The first stage after ``syncboxes`` copied other boxes' data onto this
+    // grid (launch_rhs_sync, _stale_sync): smap[o] >= 0 marks a copied point,
+    // its partner k = smap[o] >> kPartnerShift and its offset
+    // smap[o] & kPartnerOffset in that partner's state xb[k] (leading
+    // dimension xb_ld[k]); the other points read this grid's state before
+    // the copy, xa.
     const int* smap;
     const double* xa[NFIELDS];
-    const double* xb[NFIELDS];
-    long xb_ld;
+    const double* xb[kMaxPartners][NFIELDS];
+    long xb_ld[kMaxPartners];
 };
 
 // Table of a ``syncboxes`` copy onto grid P from grid Q of the same level.
@@ -192,12 +200,12 @@ struct MaxCoeffArgs {
     double* Drphi; double* Dzphi; double* psi4;
     double* vmax;                                          // [2*block]: per-block max sqrt|g^rr/psi4|, sqrt|g^zz/psi4|
     // after ``syncboxes`` (as StageArgs::smap): the derivatives come from the
-    // grid's state before the copy (xa) or the partner's (xb) at the copied
+    // grid's state before the copy (xa) or the partner's (xb[k]) at the copied
     // points; order g_A, g_B, g_C, chi, phi
     const int* smap;
     const double* xa[5];
-    const double* xb[5];
-    long xb_ld;
+    const double* xb[kMaxPartners][5];
+    long xb_ld[kMaxPartners];
 };
 
 // The physical-Laplacian coefficients of one wave stage.

@@ -99,7 +99,10 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     bool xin = false;  // a copied point: stencils of the partner's interior
     if constexpr (SYNC) {
         const int m = A.smap[o];
-        if (m >= 0) { X = A.xb; ox = (size_t)m; ldx = A.xb_ld; xin = true; }
+        if (m >= 0) {
+            const int k = m >> kPartnerShift;
+            X = A.xb[k]; ox = (size_t)(m & kPartnerOffset); ldx = A.xb_ld[k]; xin = true;
+        }
         else X = A.xa;
     }
     const int pcr = xin ? 0 : pcl<ORD>(i, nr, g), pcz = xin ? 0 : pcl<ORD>(j, nz, g);

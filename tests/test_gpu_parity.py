@@ -313,11 +313,17 @@ def test_refinement_boxes(cfg):
 # and sits higher, so that no point a copy reads was written by the other
 # copy of the level (a chain the device refuses)
 OVERLAP = dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
+# three grids on level 1 in a column on the axis: box 1 takes copies from
+# box 0's level 1 below it (80 points) and from box 2 above it (18 points),
+# two partners for one grid; no copy reads a point another copy wrote
+THREE_BOXES = dict(C1, nrtotal=32, nztotal=32, nl0=1, dr0=0.5, dz0=0.5, Nb=2, Nl1=1, Nl2=1, Nrbox1=16, Nzbox1=16,
+                   zbox1=6.0, Nrbox2=24, Nzbox2=24, zbox2=9.0)
 
 
 @pytest.mark.parametrize("cfg", [OVERLAP, dict(OVERLAP, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
-                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=5.0)],
-                         ids=["overlap", "overlap_shift", "overlap_order_two"])
+                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=5.0), THREE_BOXES,
+                                 dict(THREE_BOXES, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)],
+                         ids=["overlap", "overlap_shift", "overlap_order_two", "two_partners", "two_partners_shift"])
 def test_overlapping_boxes(cfg):
     """syncboxes copies the evolved and auxiliary arrays of the partner box
     on each box's strips; the next first stage reads the auxiliary
