@@ -106,7 +106,8 @@ struct SyncPair {
     int p = -1, q = -1;
     XferPt* tab = nullptr;
     int ntab = 0;
-    std::vector<size_t> written;  // level offsets of grid p that this copy writes
+    // (offset in p from its element (0, 0), offset of the coinciding node in q) of each copied point
+    std::vector<std::pair<int, int>> copies;
 };
 
 }  // namespace
@@ -756,9 +757,15 @@ int onestep(ollin_handle* h, int level) {
 
 // ``syncboxes`` tables of every ordered pair of boxes on a level that
 // overlap (onestep.f90:446-466).  The device reproduces the copy and, for
-// the next first stage, the auxiliary quantities it carries: that needs each
-// copied point to coincide with a node of the partner, one partner per grid,
-// and no copied point to be read by a later copy of the same level.
+// the next first stage, the auxiliary quantities it carries; that needs each
+// copied point to coincide with a node of the partner.
+//
+// The copies of a level run in this order, so a copy that reads a node an
+// earlier copy wrote (a chain) takes the value that copy brought, and with
+// it, in the reference, that copy's auxiliary arrays.  The copy map of each
+// grid therefore records the origin of every copied point: the grid and node
+// whose state before the level's copies the value and its auxiliary
+// quantities come from (possibly the grid itself).
 int build_sync_tables(ollin_handle* h) {
     for (int level = 1; level <= h->nlmax; ++level)
         for (int p = 0; p < h->nlev; ++p) {
@@ -795,58 +802,55 @@ int build_sync_tables(ollin_handle* h) {
                     }
                 }
                 if (used == 0) { cudaFree(tab); continue; }
-                // partner k of this grid; a point copied by two partners keeps
-                // the later copy, as the copies of the level run in this order
-                int k = (int)(std::find(P.spartners.begin(), P.spartners.end(), q) - P.spartners.begin());
-                if (k == (int)P.spartners.size()) {
-                    if (k == kMaxPartners) {
-                        cudaFree(tab);
-                        return fail(OLLIN_EINVAL, "syncboxes: a grid overlaps more than three other grids on one level");
-                    }
-                    P.spartners.push_back(q);
-                }
-                if (P.hsmap.empty()) P.hsmap.assign(P.n, -1);
-                for (const XferPt& x : host) {
-                    if (x.o_out == kNoPoint) continue;
-                    if (x.depth > kPartnerOffset) {
-                        cudaFree(tab);
-                        return fail(OLLIN_EINVAL, "syncboxes: a partner grid too large for the copy map");
-                    }
-                    P.hsmap[(size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld] = x.depth | (k << kPartnerShift);
-                }
-                if (!P.smap && cudaMalloc(&P.smap, P.n * sizeof(int)) != cudaSuccess) {
-                    cudaFree(tab);
-                    return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes map");
-                }
-                CUDA_OR_FAIL(cudaMemcpy(P.smap, P.hsmap.data(), P.n * sizeof(int), cudaMemcpyHostToDevice));
                 SyncPair sp;
                 sp.p = p; sp.q = q; sp.tab = tab; sp.ntab = n;
                 for (const XferPt& x : host)
-                    if (x.o_out != kNoPoint) sp.written.push_back((size_t)x.o_out + (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld);
+                    if (x.o_out != kNoPoint) sp.copies.emplace_back(x.o_out, x.depth);
                 h->sync.push_back(std::move(sp));
             }
         }
-    // a later copy of the level may not read a point an earlier one wrote
-    for (size_t k = 0; k < h->sync.size(); ++k)
-        for (size_t e = k + 1; e < h->sync.size(); ++e) {
-            const SyncPair& w = h->sync[k];
-            const SyncPair& r = h->sync[e];
-            if (r.q != w.p) continue;
-            std::vector<XferPt> hr(r.ntab);
-            CUDA_OR_FAIL(cudaMemcpy(hr.data(), r.tab, (size_t)r.ntab * sizeof(XferPt), cudaMemcpyDeviceToHost));
-            const DLevel& W = h->L[w.p];
-            std::vector<char> map(W.n, 0);
-            for (size_t o : w.written) map[o] = 1;
-            const size_t shift = (size_t)(W.g - 1) + (size_t)(W.g - 1) * W.ld;
-            // the copy reads the node it coincides with (the other weights
-            // of a near-node stencil are rounding)
-            for (const XferPt& x : hr) {
-                if (x.o_out == kNoPoint) continue;
-                const size_t o = (size_t)x.depth + shift;
-                if (o < W.n && map[o])
-                    return fail(OLLIN_EINVAL, "syncboxes: a copy reads a point another copy of the level wrote");
-            }
+    // origin of every copied point, in the order the copies run: origin[g][o]
+    // = (source grid, offset from its element (0, 0)) of array element o of
+    // grid g, or (-1, -1)
+    std::vector<std::vector<std::pair<int, long>>> origin(h->nlev);
+    for (const SyncPair& sp : h->sync) {
+        const DLevel& P = h->L[sp.p];
+        const DLevel& Q = h->L[sp.q];
+        const size_t shp = (size_t)(P.g - 1) + (size_t)(P.g - 1) * P.ld;
+        const size_t shq = (size_t)(Q.g - 1) + (size_t)(Q.g - 1) * Q.ld;
+        if (origin[sp.p].empty()) origin[sp.p].assign(P.n, {-1, -1L});
+        // the reads of this copy see the writes of the copies before it only
+        std::vector<std::pair<size_t, std::pair<int, long>>> upd;
+        for (const auto& c : sp.copies) {
+            std::pair<int, long> src{sp.q, c.second};
+            const size_t oq = (size_t)c.second + shq;
+            if (!origin[sp.q].empty() && oq < Q.n && origin[sp.q][oq].first >= 0) src = origin[sp.q][oq];
+            upd.emplace_back((size_t)c.first + shp, src);
         }
+        for (const auto& u : upd) origin[sp.p][u.first] = u.second;
+    }
+    for (int p = 0; p < h->nlev; ++p) {
+        if (origin[p].empty()) continue;
+        DLevel& P = h->L[p];
+        P.spartners.clear();
+        P.hsmap.assign(P.n, -1);
+        for (size_t o = 0; o < P.n; ++o) {
+            const std::pair<int, long>& src = origin[p][o];
+            if (src.first < 0) continue;
+            int k = (int)(std::find(P.spartners.begin(), P.spartners.end(), src.first) - P.spartners.begin());
+            if (k == (int)P.spartners.size()) {
+                if (k == kMaxPartners)
+                    return fail(OLLIN_EINVAL, "syncboxes: the copies onto a grid come from more than four grids");
+                P.spartners.push_back(src.first);
+            }
+            if (src.second > kPartnerOffset)
+                return fail(OLLIN_EINVAL, "syncboxes: a partner grid too large for the copy map");
+            P.hsmap[o] = (int)src.second | (k << kPartnerShift);
+        }
+        if (!P.smap && cudaMalloc(&P.smap, P.n * sizeof(int)) != cudaSuccess)
+            return fail(OLLIN_ENOMEM, "device allocation failed for the syncboxes map");
+        CUDA_OR_FAIL(cudaMemcpy(P.smap, P.hsmap.data(), P.n * sizeof(int), cudaMemcpyHostToDevice));
+    }
     for (const SyncPair& sp : h->sync)
         for (int g2 : {sp.p, sp.q}) {
             DLevel& G = h->L[g2];

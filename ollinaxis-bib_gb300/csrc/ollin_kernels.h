@@ -26,13 +26,14 @@ struct PhysParams {
     int boundtype;        // OLLIN_BOUND_*
 };
 
-// One RK/ICN stage of one level.
-// ``syncboxes`` partners of one grid on a level (boxes 0..3 share a level),
-// and the packing of a copied point's partner and offset into one int
-constexpr int kMaxPartners = 3;
+// ``syncboxes`` sources of one grid on a level (boxes 0..3 share a level; a
+// chain of copies can lead back to the grid itself), and the packing of a
+// copied point's source and offset into one int
+constexpr int kMaxPartners = 4;
 constexpr int kPartnerShift = 28;
 constexpr int kPartnerOffset = (1 << kPartnerShift) - 1;
 
+// One RK/ICN stage of one level.
 struct StageArgs {
     LevelGeom G;
     PhysParams P;

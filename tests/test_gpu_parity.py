@@ -309,21 +309,29 @@ def test_refinement_boxes(cfg):
 
 # box 0's level 1 around the origin and box 1 on the axis above it overlap
 # on level 1 (syncboxes.f90).  In order two (ghost = 2) the box is 15 points
-# high, so that its nodes coincide with box 0's (Nzbox - ghost + 1 even),
-# and sits higher, so that no point a copy reads was written by the other
-# copy of the level (a chain the device refuses)
+# high, so that its nodes coincide with box 0's (Nzbox - ghost + 1 even).
+# At zbox1 = 4 the copy onto box 1 reads one node of box 0 that the copy
+# onto box 0 wrote just before (a chain): its auxiliary quantities are box
+# 1's own from before the copies
 OVERLAP = dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16, zbox1=4.0)
 # three grids on level 1 in a column on the axis: box 1 takes copies from
 # box 0's level 1 below it (80 points) and from box 2 above it (18 points),
 # two partners for one grid; no copy reads a point another copy wrote
 THREE_BOXES = dict(C1, nrtotal=32, nztotal=32, nl0=1, dr0=0.5, dz0=0.5, Nb=2, Nl1=1, Nl2=1, Nrbox1=16, Nzbox1=16,
                    zbox1=6.0, Nrbox2=24, Nzbox2=24, zbox2=9.0)
+# the same column with a larger box 1 (24 points, zbox1 = 6, zbox2 = 10):
+# copies 0 <- 1 (63 points), 1 <- 0 (188, one of them a node the first copy
+# wrote), 1 <- 2 and 2 <- 1 (18 each)
+THREE_BOXES_CHAIN = dict(THREE_BOXES, Nrbox1=24, Nzbox1=24, zbox2=10.0)
 
 
 @pytest.mark.parametrize("cfg", [OVERLAP, dict(OVERLAP, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
-                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=5.0), THREE_BOXES,
-                                 dict(THREE_BOXES, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0)],
-                         ids=["overlap", "overlap_shift", "overlap_order_two", "two_partners", "two_partners_shift"])
+                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=5.0),
+                                 dict(OVERLAP, order="two", Nzbox1=15, zbox1=4.0), THREE_BOXES,
+                                 dict(THREE_BOXES, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+                                 THREE_BOXES_CHAIN],
+                         ids=["overlap", "overlap_shift", "overlap_order_two", "overlap_chain_order_two",
+                              "two_partners", "two_partners_shift", "three_boxes_chain"])
 def test_overlapping_boxes(cfg):
     """syncboxes copies the evolved and auxiliary arrays of the partner box
     on each box's strips; the next first stage reads the auxiliary
