@@ -119,6 +119,11 @@ CASES = {
     # box 0's level 1 around the origin and box 1 on the axis above it
     "box_overlap": dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=16,
                         Nzbox1=16, zbox1=4.0, _steps=[0, 1, 2]),
+    # three grids on level 1 in a column on the axis: box 1 takes copies from
+    # box 0's level 1 and from box 2 (two partners), and one copy reads a node
+    # that the copy before it wrote (a chain)
+    "box_three_chain": dict(BASE, nrtotal=32, nztotal=32, nl0=1, dr0=0.5, dz0=0.5, Nb=2, Nl1=1, Nl2=1,
+                            Nrbox1=24, Nzbox1=24, zbox1=6.0, Nrbox2=24, Nzbox2=24, zbox2=10.0, _steps=[0, 1, 2]),
     # maximal slicing (maximalslicing.f90, physical Laplacian).  Time-symmetric
     # vacuum data have K_ij = 0 and a maximal lapse of exactly 1, and so does
     # a static massless scalar field (rho + S = 0), so the cases solve where
