@@ -114,7 +114,8 @@ typedef struct ollin_params {
     /* grid: param.f90:95-141 */
     int    nrtotal, nztotal;   /* Nrtotal, Nztotal: points per level (without ghosts) */
     int    nl0;                /* Nl0: refinement levels above the base grid */
-    int    ghost;              /* 0 = from order (2 for order two, 3 for order four); no other value */
+    int    ghost;              /* ghost zones: 0 or fewer than the order needs gives 2 (order two) or
+                                  3 (order four), a larger value up to 8 is kept (main.f90:286-318) */
     int    eqsym;              /* equatorial symmetry */
     double dr0, dz0;           /* base-grid spacing */
     double dtfac;              /* dt0 = dtfac*min(dr0,dz0) (setupboxes.f90:119) */
@@ -558,8 +559,8 @@ const char* ollin_gpu_last_error(void);
  * synchronise the device, tools that may only read.
  *
  * d_field points at element (1-ghost, 1-ghost) of a column-major
- * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost is 3
- * (order four) or 2 (order two) and the grid equatorially symmetric (box-0
+ * (1-ghost:nr, 1-ghost:nz) array with leading dimension ld_r; ghost is the
+ * grid's number of ghost zones (2 to 8) and the grid equatorially symmetric (box-0
  * coordinates r = (i-1/2) dr, z = (j-1/2) dz); eqsym = 0 is refused with
  * OLLIN_EINVAL.  ``stream`` is a cudaStream_t or NULL; the call returns after
  * the result has reached ``out`` (host memory), so a capturing stream is

@@ -169,16 +169,19 @@ void parity_table(ollin_handle* h) {
     set(F_SXIR, -1, +1); set(F_SXIZ, +1, -1);
 }
 
+// ghost zones of every grid (main.f90:286-318)
+int ghost_zones(const ollin_params& P) { return std::max(P.ghost, P.order == 2 ? 2 : 3); }
+
 double* base_ptr(const DLevel& L, double* p) { return p ? p + (L.g - 1) + (size_t)(L.g - 1) * L.ld : nullptr; }
 
 int check_params(const ollin_params& P) {
     if (P.order != 4 && P.order != 2) return fail(OLLIN_EINVAL, "order must be \"two\" (2) or \"four\" (4)");
     if (P.nrtotal < 8 || P.nztotal < 8) return fail(OLLIN_EINVAL, "Nrtotal and Nztotal must be at least 8");
     if (P.nl0 < 0 || P.nl0 >= kMaxLevels) return fail(OLLIN_EINVAL, "Nl0 out of range");
-    // main.f90:286-318 takes a larger par-file ghost as given; here the
-    // number is the order's own
-    if (P.ghost != 0 && P.ghost != (P.order == 2 ? 2 : 3))
-        return fail(OLLIN_EINVAL, "ghost must be 2 for order two and 3 for order four");
+    // main.f90:286-318: 0 or fewer than the order needs gives the order's own
+    // number (ghost_zones), a larger one is kept
+    if (P.ghost < 0 || P.ghost > kMaxGhost)
+        return fail(OLLIN_EINVAL, "ghost must be between 0 and " + std::to_string(kMaxGhost));
     if (!P.chimethod || P.chipower != 2) return fail(OLLIN_EINVAL, "chimethod with chipower = 2 is required");
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
     if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
@@ -2308,7 +2311,7 @@ int ollin_gpu_create(const ollin_params* p, ollin_handle** out) {
         return fail(OLLIN_ECUDA, "no CUDA device is available");
     auto* h = new ollin_handle();
     h->P = *p;
-    h->g = p->order == 2 ? 2 : 3;  // main.f90:286-297
+    h->g = ghost_zones(*p);
     h->shift = p->shift != OLLIN_SHIFT_NONE;
     h->scalar = p->mattertype == OLLIN_MATTER_SCALAR;
     h->phys = make_phys(*p);
@@ -2774,7 +2777,7 @@ int ollin_gpu_footprint(const ollin_params* p, size_t* resident, size_t* transie
     if (rc) return rc;
     ollin_handle tmp;  // the grid list only: no device work
     tmp.P = *p;
-    tmp.g = p->order == 2 ? 2 : 3;
+    tmp.g = ghost_zones(*p);
     rc = setup_boxes(&tmp);
     if (rc) return rc;
     // a maximal-slicing solve may run whenever the caller asks (maximalevery

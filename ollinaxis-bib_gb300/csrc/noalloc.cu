@@ -184,9 +184,9 @@ const char* ollin_gpu_noalloc_last_error(void) { return g_noalloc_err; }
 int ollin_gpu_norms_noalloc(const double* d_field, int nr, int nz, int ghost, int ld_r, double dr, double dz,
                             int eqsym, void* stream, double out[5]) {
     if (!d_field || !out) return noalloc_fail(OLLIN_EINVAL, "null field or output pointer");
-    if ((ghost != 2 && ghost != 3) || nr <= ghost + 1 || nz <= ghost + 1 || ld_r < nr + ghost || !(dr > 0.0) ||
+    if (ghost < 2 || ghost > 8 || nr <= ghost + 1 || nz <= ghost + 1 || ld_r < nr + ghost || !(dr > 0.0) ||
         !(dz > 0.0))
-        return noalloc_fail(OLLIN_EINVAL, "bad grid description (ghost 2 or 3, ld_r >= nr+ghost)");
+        return noalloc_fail(OLLIN_EINVAL, "bad grid description (ghost 2 to 8, ld_r >= nr+ghost)");
     if (!eqsym) return noalloc_fail(OLLIN_EINVAL, "only equatorially symmetric grids are supported");
     if (nz - ghost > kMaxRows)
         return noalloc_fail(OLLIN_EINVAL, "nz - ghost exceeds the 8192 interior rows the fixed scratch holds");

@@ -30,6 +30,8 @@ struct PhysParams {
 // chain of copies can lead back to the grid itself), and the packing of a
 // copied point's source and offset into one int
 constexpr int kMaxPartners = 4;
+// largest par-file ghost accepted (main.f90 sets no bound)
+constexpr int kMaxGhost = 8;
 constexpr int kPartnerShift = 28;
 constexpr int kPartnerOffset = (1 << kPartnerShift) - 1;
 

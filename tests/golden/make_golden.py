@@ -37,6 +37,12 @@ CASES = {
     # same with the Gamma-driver shift, 3 levels
     "c2_small": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver2",
                      drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # a par-file ghost larger than the order needs (main.f90:298-318 keeps
+    # it): four ghost zones in order four, three in order two
+    "ghost4_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, ghost=4, shift="Gammadriver2",
+                         drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 2]),
+    "ghost3_o2_box": dict(BASE, order="two", ghost=3, nrtotal=20, nztotal=20, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1,
+                          Nrbox1=12, Nzbox1=12, rbox1=2.0, zbox1=2.0, _steps=[0, 1, 2]),
     # the first-order hyperbolic and the parabolic Gamma drivers
     # (sources_shift.f90:62-186, radiative_geometry.f90:195-235); the
     # parabolic one without equatorial symmetry, where the row j = 0 whose

@@ -70,8 +70,8 @@ def test_unsupported_parameters_are_rejected_before_any_device_work():
     from ollin import gpu
     from ollin.params import params_from_dict
     lib = gpu.load()
-    # a par-file ghost larger than the order needs (main.f90:298-318 keeps it)
-    p = params_from_dict(dict(order="four", ghost=4, eqsym=1))
+    # a negative number of ghost zones
+    p = params_from_dict(dict(order="four", ghost=-1, eqsym=1))
     h = ctypes.c_void_p()
     rc = lib.ollin_gpu_create(ctypes.byref(p), ctypes.byref(h))
     assert rc == 1 and b"ghost" in lib.ollin_gpu_last_error()

@@ -224,6 +224,19 @@ def test_shock_avoiding_and_static_shifts(cfg):
     run(cfg, 8, check_every=4)
 
 
+@pytest.mark.parametrize("cfg", [
+    dict(C1, nrtotal=32, nztotal=32, nl0=2, ghost=4, shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+    dict(C1, order="two", ghost=3, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, Nl1=1, Nrbox1=12,
+         Nzbox1=12, rbox1=2.0, zbox1=2.0),
+    dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, ghost=5, Nb=1, Nl1=1, Nrbox1=16, Nzbox1=16,
+         zbox1=4.0)], ids=["ghost4_shift", "ghost3_order_two_ring", "ghost5_overlap"])
+def test_larger_ghost(cfg):
+    """A par-file ghost larger than the order needs (main.f90:286-318 keeps
+    it) moves the dissipation and advection interiors, the finebound strip
+    depth, the restriction margin and the syncboxes strips."""
+    run(cfg, 6, check_every=3)
+
+
 def test_icn_harmonic_isotropic():
     cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
                gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)

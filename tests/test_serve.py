@@ -30,7 +30,7 @@ def test_footprint_grows_with_the_hierarchy():
 def test_footprint_rejects_what_create_rejects():
     from ollin.gpu import OllinError, footprint
     with pytest.raises(OllinError) as e:
-        footprint(params(dict(C1, ghost=4)))
+        footprint(params(dict(C1, ghost=-1)))
     assert e.value.code == 1
     with pytest.raises(OllinError):
         footprint(params(dict(C1, Nb=1, Nl1=1, Nrbox1=200, Nzbox1=16, rbox1=1.0)))
