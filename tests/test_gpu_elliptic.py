@@ -69,9 +69,10 @@ PULSE_RING = dict(BASE, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, Nb=1, N
 
 @pytest.mark.parametrize("cfg", [PULSE_1LEV, PULSE_2LEV, BRILL_3LEV, BRILL_RK4, PULSE_NOEQSYM, PULSE_BOXES,
                                  PULSE_RING, dict(PULSE_2LEV, order="two"),
-                                 dict(PULSE_RING, order="two", Nrbox1=13, Nzbox1=13)],
+                                 dict(PULSE_RING, order="two", Nrbox1=13, Nzbox1=13), dict(PULSE_RING, ghost=4)],
                          ids=["pulse_1lev", "pulse_2lev", "brill_3lev", "brill_rk4_damped", "pulse_no_eqsym",
-                              "pulse_boxes", "pulse_ring", "pulse_2lev_order_two", "pulse_ring_order_two"])
+                              "pulse_boxes", "pulse_ring", "pulse_2lev_order_two", "pulse_ring_order_two",
+                              "pulse_ring_ghost4"])
 def test_elliptic_data_matches_oracle(cfg):
     o, e, (o0, o1, ophases, ogres), (g0, g1, ggres) = solve_pair(cfg)
     assert (g0, g1) == (o0, o1), "iterations gpu %s oracle %s" % ((g0, g1), (o0, o1))
@@ -127,9 +128,10 @@ SOR_BRILL_NOEQSYM = dict(SOR_BRILL, eqsym=0, nztotal=48)
 
 
 @pytest.mark.parametrize("cfg", [SOR_2LEV, SOR_POTENTIAL, SOR_BRILL, SOR_BOXES, SOR_RING, SOR_NOEQSYM,
-                                 SOR_BRILL_NOEQSYM],
+                                 SOR_BRILL_NOEQSYM, dict(SOR_RING, ghost=4), dict(SOR_NOEQSYM, ghost=4)],
                          ids=["sor_pulse_2lev", "sor_pulse_potential", "sor_brill_3lev", "sor_boxes",
-                              "sor_ring_two_levels", "sor_pulse_no_eqsym", "sor_brill_no_eqsym"])
+                              "sor_ring_two_levels", "sor_pulse_no_eqsym", "sor_brill_no_eqsym",
+                              "sor_ring_ghost4", "sor_no_eqsym_ghost4"])
 def test_sor_data_matches_oracle(cfg):
     """SOR (sor_elliptic.f90): the red-black sweeps and the sequential Robin
     boundary reproduce the reference's arithmetic; the residual norm that
@@ -160,9 +162,11 @@ MIXED_BRILL_NOEQSYM = dict(SOR_BRILL_NOEQSYM, ell_solver="mixed", ell_epsilon=1e
 
 
 @pytest.mark.parametrize("cfg", [MIXED_2LEV, MIXED_BRILL, FP64MG_2LEV, FP64MG_BRILL, MIXED_BOXES, MIXED_RING,
-                                 MIXED_NOEQSYM, MIXED_BRILL_NOEQSYM],
+                                 MIXED_NOEQSYM, MIXED_BRILL_NOEQSYM, dict(MIXED_RING, ghost=4),
+                                 dict(MIXED_NOEQSYM, ghost=4)],
                          ids=["mixed_pulse_2lev", "mixed_brill_3lev", "fp64mg_pulse_2lev", "fp64mg_brill_3lev",
-                              "mixed_boxes", "mixed_ring", "mixed_no_eqsym", "mixed_brill_no_eqsym"])
+                              "mixed_boxes", "mixed_ring", "mixed_no_eqsym", "mixed_brill_no_eqsym",
+                              "mixed_ring_ghost4", "mixed_no_eqsym_ghost4"])
 def test_mixed_precision_solve_matches_fp64_sor(cfg):
     """ELL_solver = "mixed" (FP64 iterative refinement, FP32 multigrid
     corrections) and "fp64mg" (the same with FP64 multigrid corrections)
