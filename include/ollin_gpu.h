@@ -68,6 +68,8 @@ extern "C" {
 
 #define OLLIN_BOUND_RADIATIVE   0   /* boundtype = "radiative" */
 #define OLLIN_BOUND_NONE        1   /* boundtype = "none"      */
+#define OLLIN_BOUND_STATIC      2   /* boundtype = "static": zero sources on the outer edges */
+#define OLLIN_BOUND_FLAT        3   /* boundtype = "flat": the sources of the row inside */
 
 #define OLLIN_MATTER_VACUUM     0   /* mattertype = "vacuum" */
 #define OLLIN_MATTER_SCALAR     1   /* mattertype = "scalar" */

@@ -153,10 +153,78 @@ __global__ void __launch_bounds__(128) ghost_kt2_kernel(const __grid_constant__ 
     A.auxw[X_RHOS][o] = rho + trS;
 }
 
+// boundtype = "flat" on level 0 (generated simpleboundary.f90): the outer
+// edge points take the sources of the column Nr-1 (i = Nr, the r edge first),
+// of the row Nz-1 (j = Nz) and, without equatorial symmetry, of the row
+// 2-ghost (j = 1-ghost); the edge corners thereby the sources of the points
+// diagonally inside.  The right-hand side stored those sources (A.flat) and
+// left these arrays alone on the edges; here they take the stage's
+// accumulate and update (generated accumulate.f90 / update.f90).
+__device__ __forceinline__ bool not_finite(double x) {
+    return ((__double_as_longlong(x) >> 52) & 0x7ff) == 0x7ff;
+}
+
+__device__ __forceinline__ void flat_edges_body(const StageArgs& A, unsigned bx, unsigned) {
+    const LevelGeom& G = A.G;
+    const int g = G.g, nr = G.nr, nz = G.nz;
+    const int nR = nz - G.jlo + 1;                  // r edge: j = jlo..nz
+    const int nZ = nr - 1, nL = G.eqsym ? 0 : nr - 1;  // z edges: i = 1..nr-1
+    const int t = (int)(bx * blockDim.x + threadIdx.x);
+    if (t >= nR + nZ + nL) return;
+    int i, j, src;  // the point and the offset of its source in a flat strip
+    if (t < nR) {
+        i = nr;
+        j = G.jlo + t;
+        const int js = (j == nz) ? nz - 1 : ((!G.eqsym && j == 1 - g) ? 2 - g : j);
+        src = js - G.jlo;
+    } else if (t < nR + nZ) {
+        i = 1 + (t - nR);
+        j = nz;
+        src = nR + i - 1;
+    } else {
+        i = 1 + (t - nR - nZ);
+        j = 1 - g;
+        src = nR + nr + i - 1;
+    }
+    const size_t o = (size_t)i + (size_t)j * (size_t)G.ld;
+    const PhysParams& P = A.P;
+    unsigned bad = 0;
+    constexpr int fields[kNBound] = {F_TRK, F_KTA, F_KTB, F_KTC, F_DLR, F_DLZ, F_DTBETAR, F_DTBETAZ, F_FDRIVER, F_SPI};
+#pragma unroll
+    for (int b = 0; b < kNBound; ++b) {
+        const int f = fields[b];
+        if (b >= 6 && b <= 8 && !P.shift) continue;
+        if (b == 8 && !P.shock) continue;
+        if (b == 9 && !P.scalar) continue;
+        const double s = A.flat[(size_t)b * (size_t)A.flat_len + (size_t)src];
+        double seff = s;
+        if (A.rk4) {
+            double* ac = A.acc[f] + o;
+            if (A.iter < A.niter) *ac = (A.iter == 1) ? A.weight * s : *ac + A.weight * s;
+            else seff = *ac + A.weight * s;
+        }
+        const double v = A.pst[f][o] + A.dtw * seff;
+        A.out[f][o] = v;
+        bad |= not_finite(v);
+    }
+    if (bad && A.nanflag) atomicOr(A.nanflag, 1u);
+}
+
+__global__ void __launch_bounds__(128) flat_edges_kernel(const __grid_constant__ StageArgs A) {
+    chain_enter();
+    flat_edges_body(A, blockIdx.x, blockIdx.y);
+}
+
 const MultiRegistration reg_aux_point((const void*)aux_point_kernel, multi_launch<AuxArgs, aux_point_body, 256, 1>);
 const MultiRegistration reg_aux_deriv((const void*)aux_deriv_kernel, multi_launch<AuxArgs, aux_deriv_body, 256, 1>);
+const MultiRegistration reg_flat_edges((const void*)flat_edges_kernel, multi_launch<StageArgs, flat_edges_body, 128, 1>);
 
 }  // namespace
+
+void launch_flat_edges(const StageArgs& a, cudaStream_t s) {
+    const int n = (a.G.nz - a.G.jlo + 1) + (a.G.nr - 1) + (a.G.eqsym ? 0 : a.G.nr - 1);
+    launch_chained(flat_edges_kernel, dim3((n + 127) / 128), dim3(128), s, a);
+}
 
 void launch_ghost_kt2(const StageArgs& a, cudaStream_t s) {
     if (a.G.axis) return;

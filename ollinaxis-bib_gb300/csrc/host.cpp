@@ -88,6 +88,7 @@ struct DLevel {
     // driverD0: Delta_r | Delta_z of the last t = 0 ``auxiliary`` call
     // (auxiliary_geometry.f90:1107-1113)
     double* delta0 = nullptr;
+    double* flat = nullptr;  // boundtype = "flat", level 0: the edge sources (StageArgs::flat)
     // syncboxes: this grid's state before the copies of its level (kept for
     // the partner's next first stage and its own), the map of the points
     // another box copies onto it (offset in the partner's state, or -1), the
@@ -192,7 +193,7 @@ int check_params(const ollin_params& P) {
     if (P.integrator != OLLIN_INTEGRATOR_RK4 && P.integrator != OLLIN_INTEGRATOR_ICN) return fail(OLLIN_EINVAL, "unknown integrator");
     if (P.integrator == OLLIN_INTEGRATOR_ICN && P.icniter < 1) return fail(OLLIN_EINVAL, "icniter must be positive");
     if (P.mattertype != OLLIN_MATTER_VACUUM && P.mattertype != OLLIN_MATTER_SCALAR) return fail(OLLIN_EINVAL, "unknown mattertype");
-    if (P.boundtype != OLLIN_BOUND_RADIATIVE && P.boundtype != OLLIN_BOUND_NONE) return fail(OLLIN_EINVAL, "unknown boundtype");
+    if (P.boundtype < OLLIN_BOUND_RADIATIVE || P.boundtype > OLLIN_BOUND_FLAT) return fail(OLLIN_EINVAL, "unknown boundtype");
     if (!(P.dr0 > 0 && P.dz0 > 0 && P.dtfac > 0)) return fail(OLLIN_EINVAL, "dr0, dz0 and dtfac must be positive");
     if (P.idata < OLLIN_IDATA_MINKOWSKI || P.idata > OLLIN_IDATA_SCALARPULSE) return fail(OLLIN_EINVAL, "unknown idata");
     if (P.idata == OLLIN_IDATA_SCALARPULSE && P.mattertype != OLLIN_MATTER_SCALAR)
@@ -666,6 +667,10 @@ int step_grid(ollin_handle* h, int level) {
     const int niter = rk4 ? 4 : h->P.icniter;
     const double dt = L.dt;
     int in_slot = L.p;
+    const bool flat = L.level == 0 && h->P.boundtype == OLLIN_BOUND_FLAT;
+    const int flat_len = (L.nz - L.G.jlo + 1) + 2 * L.nr;
+    if (flat && !L.flat && cudaMalloc(&L.flat, (size_t)kNBound * flat_len * sizeof(double)) != cudaSuccess)
+        return fail(OLLIN_ENOMEM, "device allocation failed for the flat boundary");
     for (int iter = 1; iter <= niter; ++iter) {
         double dtw, weight = 0;
         if (rk4) {
@@ -682,6 +687,10 @@ int step_grid(ollin_handle* h, int level) {
         StageArgs a = stage_args(h, L, in_slot, out_slot, t0);
         a.iter = iter;
         a.niter = niter;
+        if (flat) {
+            a.flat = L.flat;
+            a.flat_len = flat_len;
+        }
         a.dtw = dtw;
         a.weight = weight;
         if (h->ktime) {
@@ -702,6 +711,11 @@ int step_grid(ollin_handle* h, int level) {
             h->ev_used += 2;
             h->rhs_point_stages += (double)L.nr * (double)(L.nz - L.G.jlo + 1);
             h->rhs_launches++;
+        }
+        if (flat) {
+            launch_flat_edges(a, h->stream);
+            rc = after_launch(h);
+            if (rc) return rc;
         }
         if (L.level > 0) {
             rc = prolong(h, level, out_slot, dtw);
@@ -2371,6 +2385,7 @@ void ollin_gpu_destroy(ollin_handle* h) {
         if (L.rtab) cudaFree(L.rtab);
         if (L.alpha_aux) cudaFree(L.alpha_aux);
         if (L.delta0) cudaFree(L.delta0);
+        if (L.flat) cudaFree(L.flat);
         if (L.snap) cudaFree(L.snap);
         if (L.smap) cudaFree(L.smap);
     }

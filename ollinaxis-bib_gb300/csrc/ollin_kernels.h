@@ -73,7 +73,19 @@ struct StageArgs {
     const double* xa[NFIELDS];
     const double* xb[kMaxPartners][NFIELDS];
     long xb_ld[kMaxPartners];
+    // boundtype = "flat" on level 0: the sources that the outer-edge points
+    // take, of the kNBound arrays in their order; per array flat_len values:
+    // column Nr-1 (j = jlo..Nz), then row Nz-1 and (no equatorial symmetry)
+    // row 2-ghost (i = 1..Nr)
+    double* flat;
+    int flat_len;
 };
+// The evolved arrays that simpleboundary.f90 sets (EVOLVE without NOBOUND in
+// src/base/arrays.config), in the order of StageArgs::flat: trK, KTA, KTB,
+// KTC, Delta_r, Delta_z, dtbeta_r, dtbeta_z, fdriver, scalar_pi
+constexpr int kNBound = 10;
+// the outer-edge updates of boundtype = "flat" after the stage's right-hand side
+void launch_flat_edges(const StageArgs& a, cudaStream_t s);
 
 // Table of a ``syncboxes`` copy onto grid P from grid Q of the same level.
 struct SyncTableArgs {

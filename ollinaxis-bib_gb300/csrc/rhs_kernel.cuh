@@ -607,6 +607,35 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
         if constexpr (SCALAR) radb(F_SPI, 1.0, s_spi);
     }
 
+    // boundtype = "static" / "flat" on level 0 (generated simpleboundary.f90,
+    // after the matter sources): the sources of the arrays without NOBOUND on
+    // the outer edges are zero, or those of the column Nr-1 / row Nz-1 / row
+    // 2-ghost inside.  For "flat" the points inside store theirs (A.flat), the
+    // edge points leave those arrays alone, and flat_edges_kernel updates
+    // them once every source of the stage is known.
+    const bool simple = A.level0 && P.boundtype >= 2;
+    const bool skip_bound = simple && P.boundtype == 3 && (edge_r || edge_z);
+    if (simple && P.boundtype == 2 && (edge_r || edge_z)) {
+        s_trK = 0.0; s_KTA = 0.0; s_KTB = 0.0; s_KTC = 0.0; s_Dlr = 0.0; s_Dlz = 0.0;
+        if constexpr (SHIFT) { s_dbr = 0.0; s_dbz = 0.0; s_fd = 0.0; }
+        if constexpr (SCALAR) s_spi = 0.0;
+    }
+    if (simple && P.boundtype == 3 && A.flat) {
+        const bool in_r = i == nr - 1, in_z = j == nz - 1, in_l = !G.eqsym && j == 2 - g;
+        if (in_r || in_z || in_l) {
+            const int nR = nz - G.jlo + 1;
+            auto put = [&](int b, double s) {
+                double* base = A.flat + (size_t)b * (size_t)A.flat_len;
+                if (in_r) base[j - G.jlo] = s;
+                if (in_z) base[nR + i - 1] = s;
+                if (in_l) base[nR + nr + i - 1] = s;
+            };
+            put(0, s_trK); put(1, s_KTA); put(2, s_KTB); put(3, s_KTC); put(4, s_Dlr); put(5, s_Dlz);
+            if constexpr (SHIFT) { put(6, s_dbr); put(7, s_dbz); put(8, s_fd); }
+            if constexpr (SCALAR) put(9, s_spi);
+        }
+    }
+
     // ---- accumulate + update (generated accumulate.f90 / update.f90)
     unsigned bad = 0;
     auto upd = [&](int f, double s) {
@@ -624,13 +653,21 @@ __device__ __forceinline__ void rhs_body(const StageArgs& A, unsigned bx, unsign
     upd(F_CHI, s_chi);
     if (A.evolve_phi) upd(F_PHI, s_phi);
     upd(F_A, s_A); upd(F_B, s_B); upd(F_H, s_H); upd(F_C, s_C);
-    upd(F_TRK, s_trK); upd(F_KTA, s_KTA); upd(F_KTB, s_KTB); upd(F_KTC, s_KTC);
-    upd(F_DLR, s_Dlr); upd(F_DLZ, s_Dlz);
-    if constexpr (SHIFT) {
-        upd(F_BETAR, s_br); upd(F_BETAZ, s_bz); upd(F_DTBETAR, s_dbr); upd(F_DTBETAZ, s_dbz);
-        if (P.shock) upd(F_FDRIVER, s_fd);
+    if (!skip_bound) {
+        upd(F_TRK, s_trK); upd(F_KTA, s_KTA); upd(F_KTB, s_KTB); upd(F_KTC, s_KTC);
+        upd(F_DLR, s_Dlr); upd(F_DLZ, s_Dlz);
     }
-    if constexpr (SCALAR) { upd(F_SPHI, s_sphi); upd(F_SXIR, s_sxr); upd(F_SXIZ, s_sxz); upd(F_SPI, s_spi); }
+    if constexpr (SHIFT) {
+        upd(F_BETAR, s_br); upd(F_BETAZ, s_bz);
+        if (!skip_bound) {
+            upd(F_DTBETAR, s_dbr); upd(F_DTBETAZ, s_dbz);
+            if (P.shock) upd(F_FDRIVER, s_fd);
+        }
+    }
+    if constexpr (SCALAR) {
+        upd(F_SPHI, s_sphi); upd(F_SXIR, s_sxr); upd(F_SXIZ, s_sxz);
+        if (!skip_bound) upd(F_SPI, s_spi);
+    }
     if (bad && A.nanflag) atomicOr(A.nanflag, 1u);
     (void)zero; (void)phi_c;
 }

@@ -50,7 +50,7 @@ INTEGRATOR = {"rk4": 0, "icn": 1}
 SLICING = {"1+log": 0, "harmonic": 1, "shockavoid": 2, "static": 3, "maximal": 4}
 SHIFT = {"none": 0, "zero": 1, "static": 2, "Gammadriver2": 3, "Gammadriver1": 4, "Gammadriver0": 5,
          "Gammadrivershock1": 6, "Gammadrivershock2": 7}
-BOUND = {"radiative": 0, "none": 1}
+BOUND = {"radiative": 0, "none": 1, "static": 2, "flat": 3}
 MATTER = {"vacuum": 0, "scalar": 1}
 POTENTIAL = {"none": 0, "phi2": 1, "phi4": 2}
 IDATA = {"minkowski": 0, "schwarzschild": 1, "BrillLindquist": 2, "BrillWave": 3, "scalarpulse": 4}

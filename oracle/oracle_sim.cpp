@@ -213,6 +213,28 @@ void accumulate(Sim& S, Level& L, int k, int niter, double w) {
     }
 }
 
+// generated simpleboundary.f90 (prl/arrays.pl:880-905): on level 0, the
+// sources of every EVOLVE array not declared NOBOUND (src/base/arrays.config)
+// on the outer edges i = Nr, j = Nz and, without equatorial symmetry, the
+// lower edge j = 1-ghost: zero ("static"), or the source of the row or column
+// inside ("flat"), the r edge first
+void simpleboundary(Sim& S, Level& L) {
+    static const char* nobound[] = {"alpha", "beta_r", "beta_z", "phi", "dtphi", "chi", "A", "B", "H", "C", "lambda",
+                                    "scalar_phi", "scalar_xi_r", "scalar_xi_z"};
+    const bool flat = S.P.boundtype == OLLIN_BOUND_FLAT;
+    const int g = L.g, Nr = L.Nr, Nz = L.Nz;
+    for (const EvolvedVar& e : S.evolved) {
+        bool skip = false;
+        for (const char* n : nobound) skip = skip || e.name == n;
+        if (skip) continue;
+        Arr& s = L.a("s" + e.name);
+        for (int j = 1 - g; j <= Nz; ++j) s(Nr, j) = flat ? s(Nr - 1, j) : 0.0;
+        for (int i = 1 - g; i <= Nr; ++i) s(i, Nz) = flat ? s(i, Nz - 1) : 0.0;
+        if (!S.P.eqsym)
+            for (int i = 1 - g; i <= Nr; ++i) s(i, 1 - g) = flat ? s(i, 2 - g) : 0.0;
+    }
+}
+
 void update(Sim& S, Level& L, double dtw) {
     for (const EvolvedVar& e : S.evolved) {
         Arr& v = L.a(e.name); Arr& vp = L.a(e.name + "_p"); Arr& s = L.a("s" + e.name);
@@ -559,6 +581,8 @@ static void step_grid(Sim& S, Level& L) {
         if (P.shift != OLLIN_SHIFT_NONE) sources_shift(S, L);
         if (matter) sources_scalar(S, L);
         if (L.level == 0 && P.boundtype == OLLIN_BOUND_RADIATIVE) radiative_geometry(S, L);
+        if (L.level == 0 && (P.boundtype == OLLIN_BOUND_STATIC || P.boundtype == OLLIN_BOUND_FLAT))
+            simpleboundary(S, L);
         if (rk4) accumulate(S, L, iter, niter, weight);
         update(S, L, dtw);
         if (L.level > 0) finebound(S, gid, dtw);

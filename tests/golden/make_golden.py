@@ -37,6 +37,13 @@ CASES = {
     # same with the Gamma-driver shift, 3 levels
     "c2_small": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, shift="Gammadriver2",
                      drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 3]),
+    # boundtype = "static" and "flat" (the generated simpleboundary.f90) on
+    # level 0, the latter without equatorial symmetry (its lower edge too)
+    "bound_static": dict(BASE, nrtotal=16, nztotal=16, nl0=1, dr0=0.2, dz0=0.2, boundtype="static",
+                         shift="Gammadriver2", drivercsi=0.75, drivereta=2.0, _steps=[0, 1, 2]),
+    "bound_flat_noeqsym": dict(BASE, nrtotal=16, nztotal=24, nl0=1, dr0=0.2, dz0=0.2, eqsym=False,
+                               boundtype="flat", shift="Gammadriver2", drivercsi=0.75, drivereta=2.0,
+                               _steps=[0, 1, 2]),
     # a par-file ghost larger than the order needs (main.f90:298-318 keeps
     # it): four ghost zones in order four, three in order two
     "ghost4_shift": dict(BASE, nrtotal=16, nztotal=16, nl0=2, dr0=0.2, dz0=0.2, ghost=4, shift="Gammadriver2",

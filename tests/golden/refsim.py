@@ -44,7 +44,7 @@ SOURCES = [
     "src/geometry/maximalslicing.f90", "src/base/syncboxes.f90",
 ]
 GENERATED = ["saveold.f90", "accumulate.f90", "update.f90", "symmetries_r.f90",
-             "symmetries_z.f90"]
+             "symmetries_z.f90", "simpleboundary.f90"]
 
 
 def _param_value(typ, val):
@@ -168,7 +168,7 @@ class RefSim:
         prog.define("sync", lambda *a: None)
         for nm in ("idata_kerr", "idata_complexpulse",
                    "idata_bosonstarcf", "idata_rotboson", "checkpointrestart",
-                   "sources_complex", "constraintbound", "simpleboundary"):
+                   "sources_complex", "constraintbound"):
             prog.define(nm, self._unsupported(nm))
         prog.define("grabarray", lambda *a: None)
 

@@ -237,6 +237,22 @@ def test_larger_ghost(cfg):
     run(cfg, 6, check_every=3)
 
 
+@pytest.mark.parametrize("cfg", [
+    dict(C1, nrtotal=32, nztotal=32, boundtype="static", shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+    dict(C1, nrtotal=32, nztotal=48, nl0=1, eqsym=0, boundtype="flat", shift="Gammadriver2", drivercsi=0.75,
+         drivereta=2.0),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, dr0=0.25, dz0=0.25, boundtype="flat", idata="minkowski", ilapse="one",
+         mattertype="scalar", scalarpotential="phi2", scalar_mass=0.5, scalardiss=0.02),
+    dict(C1, nrtotal=32, nztotal=32, nl0=1, order="two", boundtype="flat", integrator="icn", icniter=3)],
+    ids=["static_shift", "flat_shift_no_eqsym", "flat_scalar", "flat_order_two_icn"])
+def test_static_and_flat_boundaries(cfg):
+    """boundtype = "static" / "flat" (the generated simpleboundary.f90): on
+    level 0 the sources of the arrays without NOBOUND on the outer edges are
+    zero, or those of the column / row inside (the edge corners take the
+    point diagonally inside)."""
+    run(cfg, 8, check_every=4)
+
+
 def test_icn_harmonic_isotropic():
     cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
                gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)

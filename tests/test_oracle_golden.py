@@ -13,7 +13,8 @@ from parity_util import params, scalar_pulse
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["c1_small", "c2_small", "icn_harmonic", "scalar_shift", "noeqsym_shift", "box_two", "box_ring_shift",
          "box_overlap", "gd1_shift", "gd0_noeqsym", "o2_c1", "o2_shift", "o2_noeqsym_scalar", "gds1_shift",
-         "gds2_d0", "gd2_shiftafter", "box_three_chain", "ghost4_shift", "ghost3_o2_box"]
+         "gds2_d0", "gd2_shiftafter", "box_three_chain", "ghost4_shift", "ghost3_o2_box",
+         "bound_static", "bound_flat_noeqsym"]
 
 # The oracle restates the reference statement by statement; the remaining
 # differences come from libm (exp/log/pow) last-bit differences amplified by
