@@ -27,6 +27,23 @@ def test_footprint_grows_with_the_hierarchy():
     assert big > 1 << 30
 
 
+def test_footprint_takes_the_reference_ghost_and_boundary_choices():
+    """main.f90:286-318 keeps a par-file ghost larger than the order needs
+    (fewer is raised to the order's own), and boundtype takes none, static
+    and flat beside radiative; more than 8 ghost zones is refused."""
+    from ollin.gpu import OllinError, footprint
+    from ollin.params import BOUND, params_from_par
+    base, _ = footprint(params(C1))
+    assert footprint(params(dict(C1, ghost=1)))[0] == base
+    assert footprint(params(dict(C1, ghost=4)))[0] > base
+    for b in ("none", "static", "flat"):
+        footprint(params(dict(C1, boundtype=b)))
+    p = params_from_par("boundtype = flat\nghost = 5\n")
+    assert p.boundtype == BOUND["flat"] and p.ghost == 5
+    with pytest.raises(OllinError):
+        footprint(params(dict(C1, ghost=9)))
+
+
 def test_footprint_rejects_what_create_rejects():
     from ollin.gpu import OllinError, footprint
     with pytest.raises(OllinError) as e:
