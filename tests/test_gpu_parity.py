@@ -253,6 +253,16 @@ def test_static_and_flat_boundaries(cfg):
     run(cfg, 8, check_every=4)
 
 
+@pytest.mark.parametrize("cfg", [
+    dict(C1, nrtotal=32, nztotal=32, interporder="bilinear", shift="Gammadriver2", drivercsi=0.75, drivereta=2.0),
+    dict(C1, nrtotal=24, nztotal=24, nl0=1, dr0=0.5, dz0=0.5, interporder="bilinear", Nb=1, Nl1=1, Nrbox1=12,
+         Nzbox1=12, rbox1=5.0, zbox1=5.0)], ids=["bilinear_three_levels", "bilinear_ring"])
+def test_bilinear_interpolation(cfg):
+    """interporder = "bilinear" (interp.f90:221-235): the coarse-to-fine
+    strips and the restriction interpolate bilinearly everywhere."""
+    run(cfg, 8, check_every=4)
+
+
 def test_icn_harmonic_isotropic():
     cfg = dict(C1, nrtotal=24, nztotal=32, nl0=1, integrator="icn", icniter=3, slicing="harmonic",
                gauge_f=1.0, ilapse="isotropic", dr0=0.25, dz0=0.25)
