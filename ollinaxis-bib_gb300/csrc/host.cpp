@@ -187,7 +187,7 @@ int check_params(const ollin_params& P) {
     if (!P.lagrangian || !P.factorhdet || !P.evolveH) return fail(OLLIN_EINVAL, "lagrangian flavour with factorhdet and evolveH is required");
     if (P.evolveKTH || !P.nolambda) return fail(OLLIN_EINVAL, "evolveKTH must be off and nolambda on");
     if (P.shift < OLLIN_SHIFT_NONE || P.shift > OLLIN_SHIFT_GAMMADRIVERSHOCK2)
-        return fail(OLLIN_EINVAL, "shift must be none, Gammadriver0, Gammadriver1 or Gammadriver2");
+        return fail(OLLIN_EINVAL, "shift must be none, zero, static, Gammadriver0, Gammadriver1, Gammadriver2, Gammadrivershock1 or Gammadrivershock2");
     if (P.slicing < 0 || P.slicing > OLLIN_SLICING_MAXIMAL) return fail(OLLIN_EINVAL, "unknown slicing");
     if (P.ilapse < OLLIN_ILAPSE_ONE || P.ilapse > OLLIN_ILAPSE_MAXIMAL) return fail(OLLIN_EINVAL, "unknown ilapse");
     if (P.integrator != OLLIN_INTEGRATOR_RK4 && P.integrator != OLLIN_INTEGRATOR_ICN) return fail(OLLIN_EINVAL, "unknown integrator");
