@@ -136,3 +136,26 @@ def test_noalloc_norms_order_two_and_capture_refused():
     assert rc == EINVAL and b"capturing" in lib.ollin_gpu_noalloc_last_error()
     del spare
     e.close()
+
+
+def test_noalloc_norms_with_four_ghost_zones():
+    """A par-file ghost of 4 (order four): the interior i = 1..Nr-ghost,
+    j = 1..Nz-ghost of save0Dvariable and the origin value, against
+    ollin_gpu_norms on the same grid."""
+    torch = pytest.importorskip("torch")
+    from ollin.gpu import Evolution
+    lib = _lib()
+    e = Evolution(params(dict(C1, nl0=1, ghost=4)))
+    e.initial_data()
+    e.initialize()
+    e.step()
+    d = e.desc(1)
+    assert d.ghost == 4
+    for name in ("alpha", "trK"):
+        host = e.download(1, name)
+        dev = torch.from_numpy(np.ascontiguousarray(host.T)).cuda()
+        torch.cuda.synchronize()
+        rc, out = _call(lib, dev, d.nr, d.nz, d.dr, d.dz, ghost=4)
+        assert rc == 0, lib.ollin_gpu_noalloc_last_error()
+        np.testing.assert_allclose(out, e.norms(1, name), rtol=1e-10, atol=1e-14)
+    e.close()
